@@ -1,0 +1,370 @@
+"""Throughput benchmark of the GB300 wavefront path tracer (Msamples/s).
+
+Workload (default): the Cornell box of cornell_box_world (raytracing/scenes.rs:226-294)
+with a GGX box and a glass sphere, 600x600, 16x16 stratified samples (256 spp), max depth
+50, the ceiling light sampled through a SamplingTargetList mixture — one step is one full
+frame.  `--config final` runs the reference's final scene (400x225, 32 spp) instead.
+
+Arms:
+  default          : this library (f32 wavefront) through the C ABI.
+  --impl reference : the reference's CPU path.  The Rust crate cannot be built here, so
+                     this times the C++ restatement of it (oracle/, "port") with every
+                     host thread, on a bounded band of rows of the same frame.
+
+One JSON line is printed by rank 0.  Multi-GPU runs (torchrun) render one independent
+frame per GPU (replicas; there is no exchange step), so `scaling` is "weak".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Msamples/s"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="cornell", choices=["cornell", "final"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(name):
+    from gartus_gb300 import scenes
+    if name == "cornell":
+        scene, lights = scenes.cornell_scene()
+        cam = scenes.cornell_camera(600, 16, 50)
+        cfg = {"workload": "cornell_box_ggx_glass", "width": 600, "height": 600, "spp": 256, "max_depth": 50,
+               "sampling": "stratified 16x16", "lights": "SamplingTargetList mixture (weight 0.5)",
+               "primitives": len(scene), "precision": "f32"}
+        return scene, lights, cam, cfg
+    scene = scenes.final_scene_ray_scene()
+    cam = scenes.final_scene_camera(400, 32)
+    cfg = {"workload": "final_scene_spheres", "width": 400, "height": 225, "spp": 32, "max_depth": 10,
+           "sampling": "random", "lights": "none (sky gradient)", "primitives": len(scene), "precision": "f32"}
+    return scene, None, cam, cfg
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = Path(tempfile.mkstemp(suffix=".csv")[1])
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = [r.split(",") for r in self.path.read_text().strip().splitlines() if r.count(",") >= 8]
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel: str, workload_name: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if present."""
+    p = ROOT / "profiles" / f"{kernel}_{workload_name}.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+# ----------------------------------------------------------------------------------
+def cpu_baseline(scene, lights, cam, seconds: float):
+    """The oracle (C++ restatement of the reference's rayon renderer) on a band of rows
+    of the same frame, with every host thread; returns (Msamples/s, threads, sample)."""
+    import oracle
+    o = oracle.OracleScene.from_ray_scene(scene)
+    la = lights.to_array() if lights is not None else None
+    w, h, spp = cam.image_size()
+    threads = os.cpu_count() or 1
+    rows = 1
+    t0 = time.perf_counter()
+    o.render(cam.desc(), la, None, precision=1, threads=threads, window=(0, h // 2, w, rows))
+    dt = max(time.perf_counter() - t0, 1e-3)
+    rows = max(1, min(h, int(rows * seconds / dt)))
+    y0 = max(0, h // 2 - rows // 2)
+    t0 = time.perf_counter()
+    _, acc = o.render(cam.desc(), la, None, precision=1, threads=threads, window=(0, y0, w, rows))
+    dt = time.perf_counter() - t0
+    samples = float(acc.sum())
+    return samples / dt / 1e6, threads, f"rows {y0}..{y0 + rows} of {h} ({w * rows} pixels x {spp} spp), f64", dt
+
+
+def run_reference_arm(args):
+    world, rank, _ = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        if rank != 0:
+            dist.barrier()
+            return
+    scene, lights, cam, cfg = workload(args.config)
+    per_step = max(args.cpu_seconds / 3.0, 2.0)
+    for _ in range(args.warmup):
+        cpu_baseline(scene, lights, cam, 0.5)
+    vals, dts = [], []
+    sample = ""
+    threads = 1
+    for _ in range(args.steps):
+        v, threads, sample, dt = cpu_baseline(scene, lights, cam, per_step)
+        vals.append(v)
+        dts.append(dt)
+    value = statistics.median(vals)
+    cfg = dict(cfg, precision="f64", implementation="C++ restatement of the reference (oracle/)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(dts), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded procedural scene)",
+        "config": cfg,
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_ours(args):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from gartus_gb300 import abi
+    from gartus_gb300 import build as gbuild
+    from gartus_gb300._lib import check, lib
+    from gartus_gb300.raytracing import Context, PathTracer
+
+    gbuild.build()
+    world, rank, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = local if world > 1 else 0
+    torch.cuda.set_device(device)
+    ctx = Context(device)
+    scene, lights, cam, cfg = workload(args.config)
+    pt = PathTracer(cam, context=ctx)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
+
+    def render():
+        if lights is not None:
+            return pt.render_with_lights_hdr_image(scene, lights)
+        return pt.render_hdr_image(scene)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(device)
+
+    for _ in range(max(args.warmup, 3)):
+        render()
+    kernels_per_iter = 4 if (cam.desc().direct_lighting_mode == abi.GT_DIRECT_NEXT_EVENT_ESTIMATION) else 3
+    dev_ms, samples, rays, launches = 0.0, 0, 0, 0
+    barrier()
+    wall0 = time.perf_counter()
+    with ClockSampler(device) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()  # L2 flush between timed iterations (outside the device-timed region)
+            torch.cuda.synchronize(device)
+            img = render()
+            st = pt.last_stats
+            dev_ms += st["gpu_ms"]
+            samples += st["samples"]
+            rays += st["rays"] + st["shadow_rays"]
+            launches += 2 + st["iterations"] * kernels_per_iter
+    barrier()
+    wall_s = time.perf_counter() - wall0
+    clock = clocks.summary()
+    assert np.isfinite(img.pixels).all()
+
+    # Max over ranks of the device time; the aggregate counts every rank's samples.
+    t = torch.tensor([dev_ms, float(samples)], dtype=torch.float64, device=f"cuda:{device}")
+    if dist is not None:
+        tmax = t.clone()
+        dist.all_reduce(tmax[0:1], op=dist.ReduceOp.MAX)
+        dist.all_reduce(tmax[1:2], op=dist.ReduceOp.SUM)
+        t = tmax
+    dev_ms_max, total_samples = float(t[0]), float(t[1])
+    value = total_samples / (dev_ms_max / 1e3) / 1e6
+
+    # End to end through the C ABI with host buffers: scene + lights upload (host BVH
+    # build included), render, image read-back — each step.
+    e2e_vals = []
+    h2d = d2h = 0
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        prims = np.ascontiguousarray(scene.primitives_array())
+        mats = np.ascontiguousarray(scene.materials_array())
+        d = abi.gt_scene_desc()
+        d.struct_size = C.sizeof(abi.gt_scene_desc)
+        d.num_primitives, d.num_materials, d.bvh_leaf_size = len(prims), len(mats), scene.leaf_size
+        d.primitives = prims.ctypes.data_as(C.POINTER(abi.gt_primitive))
+        d.materials = mats.ctypes.data_as(C.POINTER(abi.gt_material))
+        sh, lh = C.c_void_p(), C.c_void_p()
+        check(lib().gt_scene_create(ctx.handle, C.byref(d), C.byref(sh)))
+        la = lights.to_array() if lights is not None else None
+        if la is not None:
+            check(lib().gt_lights_create(ctx.handle, la.ctypes.data_as(C.c_void_p), len(la), C.byref(lh)))
+        w, h, _ = cam.image_size()
+        rgb = np.empty((h, w, 3), dtype=np.float32)
+        acc = np.empty((h, w), dtype=np.uint32)
+        f = abi.gt_frame()
+        f.struct_size = C.sizeof(abi.gt_frame)
+        f.width, f.height, f.device_buffers = w, h, 0
+        f.rgb, f.accepted = rgb.ctypes.data, acc.ctypes.data
+        o = abi.gt_render_opts()
+        o.struct_size = C.sizeof(abi.gt_render_opts)
+        stt = abi.gt_render_stats()
+        o.stats = C.pointer(stt)
+        check(lib().gt_render(sh, lh if la is not None else None, None, C.byref(cam.desc()), C.byref(o), C.byref(f)))
+        lib().gt_scene_destroy(sh)
+        if la is not None:
+            lib().gt_lights_destroy(lh)
+        dt = time.perf_counter() - t0
+        e2e_vals.append(stt.samples / dt / 1e6)
+        nodes = max(len(prims) - 1, 1)
+        h2d = len(prims) * 64 + len(prims) * 8 + nodes * 64 + len(mats) * 64 + (len(la) * 128 if la is not None else 0)
+        d2h = rgb.nbytes + acc.nbytes
+    e2e = statistics.median(e2e_vals) * world
+
+    # Roofline of the dominant kernel from one profiled frame (events around every launch).
+    prof = PathTracer(cam, context=ctx, profile=True)
+    (prof.render_with_lights_hdr_image(scene, lights) if lights is not None else prof.render_hdr_image(scene))
+    ps = prof.last_stats
+    kms = ps["kernel_ms"]
+    dom = max(("trace", "shade", "generate", "shadow"), key=lambda k: kms[k])
+    ids, _, bstats = PathTracer(cam.with_samples_per_pixel(1), context=ctx).trace_primary(scene, 1)
+    per_ray_nodes = bstats["node_bounds_tests"] / max(bstats["rays"], 1)
+    per_ray_prims = bstats["primitive_candidates"] / max(bstats["rays"], 1)
+    kinds = scene.primitives_array()["geometry"]["kind"]
+    s_by_kind = {0: 16, 1: 28, 2: 36, 3: 48}
+    s_prim = float(np.mean([s_by_kind[int(k)] for k in kinds])) if len(kinds) else 0.0
+    b_ray = 32.0 * per_ray_nodes + s_prim * per_ray_prims + 64.0
+    b_state = 2 * (32 + 12 + 8 + 4 + 4) + 8
+    bytes_per_unit = {"trace": b_ray, "shade": float(b_state), "generate": float(b_state), "shadow": b_ray}
+    units = {"trace": ps["rays"], "shade": ps["rays"], "generate": ps["samples_started"], "shadow": ps["shadow_rays"]}
+    launches_dom = max(ps["kernel_launches"][dom], 1)
+    avg_ms = kms[dom] / launches_dom
+    algo_bytes = units[dom] * bytes_per_unit[dom] / launches_dom
+    peak, peak_kind = measured_peaks()
+    achieved = algo_bytes / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else 0.0
+    traffic = traffic_from_profiles(f"k_{dom}", cfg["workload"])
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, threads, sample, _ = cpu_baseline(scene, lights, cam, args.cpu_seconds)
+        cpu = {"value": v, "unit": METRIC, "cores": threads, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": dict(cfg, l2="flushed between timed steps (512 MiB write)",
+                           parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+            "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "clocks": clock,
+            "roofline": {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": algo_bytes,
+                         "avg_launch_ms": avg_ms, "bytes_per_unit": bytes_per_unit[dom],
+                         "units_per_launch": units[dom] / launches_dom},
+            "cpu_baseline": cpu,
+            "detail": {"wall_s_timed": wall_s, "rays_per_s": rays / (dev_ms / 1e3), "kernel_ms_profiled": kms,
+                       "kernel_launches_profiled": ps["kernel_launches"], "iterations_per_frame": ps["iterations"],
+                       "bvh_per_ray": {"node_tests": per_ray_nodes, "prim_candidates": per_ray_prims}},
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

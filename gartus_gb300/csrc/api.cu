@@ -1,0 +1,511 @@
+// api.cu — the extern "C" boundary of include/gartus_gpu.h: argument validation (the
+// reference's assert! panics become GT_ERR_INVALID_ARG), handle lifetimes, camera set-up
+// in f64 on the host, and dispatch to the f32 or f64 wavefront.
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <new>
+
+#include "internal.h"
+
+namespace gt {
+
+namespace {
+thread_local std::string g_last_error;
+constexpr double kEps = 2.220446049250313e-16;
+
+struct D3 {
+    double x, y, z;
+};
+D3 d3(const double* p) { return D3{p[0], p[1], p[2]}; }
+D3 sub(D3 a, D3 b) { return D3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+D3 add(D3 a, D3 b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+D3 mul(D3 a, double s) { return D3{a.x * s, a.y * s, a.z * s}; }
+D3 divs(D3 a, double s) { return D3{a.x / s, a.y / s, a.z / s}; }
+double dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+D3 cross(D3 a, D3 b) { return D3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+D3 normalized(D3 a) { // vector.rs:147-155
+    double l = std::sqrt(dot(a, a));
+    return l < kEps ? D3{0, 0, 0} : divs(a, l);
+}
+void put(double* dst, D3 v) {
+    dst[0] = v.x;
+    dst[1] = v.y;
+    dst[2] = v.z;
+}
+bool finite3(const double* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+
+uint32_t image_height(const gt_camera_desc& d) { // `(w / aspect) as u32`, then max(1)
+    double h = double(d.image_width) / d.aspect_ratio;
+    uint32_t v = !(h > 0.0) ? 0u : (h >= 4294967295.0 ? UINT32_MAX : uint32_t(h));
+    return v < 1 ? 1 : v;
+}
+
+// RayCamera::validate_view (camera.rs:1161-1201) plus the builder clamps.
+gt_status validate_camera(const gt_camera_desc& d) {
+    if (d.struct_size < sizeof(gt_camera_desc)) return fail(GT_ERR_INVALID_ARG, "camera struct_size too small");
+    if (d.image_width == 0) return fail(GT_ERR_INVALID_ARG, "image width must be positive");
+    if (!std::isfinite(d.aspect_ratio) || !(d.aspect_ratio > 0.0))
+        return fail(GT_ERR_INVALID_ARG, "aspect ratio must be positive and finite");
+    if (!std::isfinite(d.vertical_fov) || !(0.0 < d.vertical_fov && d.vertical_fov < 180.0))
+        return fail(GT_ERR_INVALID_ARG, "vertical field of view must be finite and in 0..180 degrees");
+    D3 w = sub(d3(d.lookfrom), d3(d.lookat));
+    if (!(dot(w, w) > kEps)) return fail(GT_ERR_INVALID_ARG, "lookfrom and lookat must be distinct");
+    D3 vup = d3(d.view_up);
+    if (!(dot(vup, vup) > kEps)) return fail(GT_ERR_INVALID_ARG, "view-up vector must be nonzero");
+    D3 fwd = normalized(sub(d3(d.lookat), d3(d.lookfrom)));
+    D3 right = normalized(cross(fwd, vup));
+    if (dot(fwd, fwd) <= kEps || dot(right, right) <= kEps)
+        return fail(GT_ERR_INVALID_ARG, "view-up vector must not be parallel to the viewing direction");
+    if (!std::isfinite(d.defocus_angle) || !(d.defocus_angle >= 0.0 && d.defocus_angle < 180.0))
+        return fail(GT_ERR_INVALID_ARG, "defocus angle must be finite and in 0..180 degrees");
+    if (!std::isfinite(d.focus_distance) || !(d.focus_distance > 0.0))
+        return fail(GT_ERR_INVALID_ARG, "focus distance must be positive and finite");
+    if (!std::isfinite(d.shutter_start) || !std::isfinite(d.shutter_end) || !(d.shutter_start <= d.shutter_end))
+        return fail(GT_ERR_INVALID_ARG, "shutter interval must be finite and ordered");
+    if (d.background_kind > GT_BG_VERTICAL_GRADIENT)
+        return fail(GT_ERR_UNSUPPORTED, "only constant and vertical-gradient backgrounds cross the ABI");
+    for (int i = 0; i < 9; ++i)
+        if (!std::isfinite(d.background[i])) return fail(GT_ERR_INVALID_ARG, "background color components must be finite");
+    if (d.pixel_sample_mode > GT_SAMPLE_STRATIFIED_GRID) return fail(GT_ERR_INVALID_ARG, "unknown pixel sample mode");
+    if (d.direct_lighting_mode > GT_DIRECT_NEXT_EVENT_ESTIMATION)
+        return fail(GT_ERR_INVALID_ARG, "unknown direct lighting mode");
+    if (!std::isfinite(d.light_pdf_weight)) return fail(GT_ERR_INVALID_ARG, "light PDF weight must be finite");
+    if (d.adaptive && (!std::isfinite(d.adaptive_error_threshold) || !(d.adaptive_error_threshold > 0.0)))
+        return fail(GT_ERR_INVALID_ARG, "adaptive sampling error threshold must be positive and finite");
+    uint64_t pixels = uint64_t(d.image_width) * image_height(d);
+    if (pixels > (1ull << 30)) return fail(GT_ERR_INVALID_ARG, "image is too large");
+    return GT_OK;
+}
+
+// RayCamera::initialized (camera.rs:1068-1130), in f64.
+CamHost init_camera(const gt_camera_desc& d, bool env) {
+    CamHost c;
+    std::memset(&c, 0, sizeof(c));
+    c.desc = d;
+    c.desc.samples_per_pixel = d.samples_per_pixel < 1 ? 1 : d.samples_per_pixel;
+    c.width = d.image_width;
+    c.height = image_height(d);
+    const double pi = 3.141592653589793;
+    double theta = d.vertical_fov * pi / 180.0;
+    double h = std::tan(theta * 0.5);
+    double vh = 2.0 * h * d.focus_distance;
+    double vw = vh * (double(d.image_width) / double(c.height));
+    D3 center = d3(d.lookfrom);
+    D3 fwd = normalized(sub(d3(d.lookat), center)); // CameraBasis::looking_at, geometry.rs:23-37
+    D3 right = normalized(cross(fwd, d3(d.view_up)));
+    D3 up = cross(right, fwd);
+    D3 w = D3{-fwd.x, -fwd.y, -fwd.z};
+    D3 vu = mul(right, vw);
+    D3 vv = mul(D3{-up.x, -up.y, -up.z}, vh);
+    D3 pdu = divs(vu, double(d.image_width));
+    D3 pdv = divs(vv, double(c.height));
+    D3 ul = sub(sub(sub(center, mul(w, d.focus_distance)), divs(vu, 2.0)), divs(vv, 2.0));
+    D3 p00 = add(ul, mul(add(pdu, pdv), 0.5));
+    double dr = d.focus_distance * std::tan((d.defocus_angle * 0.5) * pi / 180.0);
+    put(c.center, center);
+    put(c.pixel00, p00);
+    put(c.du, pdu);
+    put(c.dv, pdv);
+    put(c.ddu, mul(right, dr));
+    put(c.ddv, mul(up, dr));
+    // Samples the loops run (effective_samples_per_pixel, camera.rs:1547-1556) and the
+    // stratified grid (camera.rs:1706-1708, 3028-3034); a zero grid width is clamped to 1
+    // as RayCamera::with_stratified_grid_width does.
+    if (d.pixel_sample_mode == GT_SAMPLE_RANDOM) {
+        c.grid = 1;
+        c.spp = c.desc.samples_per_pixel;
+    } else if (d.pixel_sample_mode == GT_SAMPLE_STRATIFIED) {
+        double r = std::sqrt(double(c.desc.samples_per_pixel));
+        uint32_t g = !(r > 0.0) ? 0u : uint32_t(r);
+        c.grid = g < 1 ? 1 : g;
+        c.spp = c.grid * c.grid;
+    } else {
+        c.grid = d.grid_width < 1 ? 1 : d.grid_width;
+        c.spp = c.grid * c.grid;
+    }
+    // The environment entry points switch to next-event estimation
+    // (environment_importance_camera, camera.rs:4171-4173).
+    c.nee = d.direct_lighting_mode == GT_DIRECT_NEXT_EVENT_ESTIMATION || env;
+    c.light_pdf_weight = c.nee ? 0.0 : std::fmin(std::fmax(d.light_pdf_weight, 0.0), 1.0);
+    return c;
+}
+
+gt_status validate_geometry(const gt_geometry& g) {
+    if (g.kind > GT_GEOM_QUAD) return fail(GT_ERR_INVALID_ARG, "unknown geometry kind");
+    for (int i = 0; i < 9; ++i)
+        if (!std::isfinite(g.p[i])) return fail(GT_ERR_INVALID_ARG, "geometry parameters must be finite");
+    return GT_OK;
+}
+
+} // namespace
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+gt_status fail(gt_status status, const std::string& msg) {
+    g_last_error = msg;
+    return status;
+}
+gt_status cuda_fail(cudaError_t e, const char* what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? GT_ERR_OOM : GT_ERR_CUDA;
+}
+
+} // namespace gt
+
+using namespace gt;
+
+#define GT_GUARD_BEGIN try {
+#define GT_GUARD_END                                                  \
+    }                                                                 \
+    catch (const std::bad_alloc&) {                                   \
+        return fail(GT_ERR_OOM, "host allocation failed");            \
+    }                                                                 \
+    catch (const std::exception& ex) {                                \
+        return fail(GT_ERR_INTERNAL, ex.what());                      \
+    }
+
+extern "C" {
+
+uint32_t gt_abi_version(void) { return GT_ABI_VERSION; }
+
+const char* gt_last_error(void) { return g_last_error.c_str(); }
+
+gt_status gt_camera_default(uint32_t image_width, double aspect_ratio, gt_camera_desc* c) {
+    if (!c) return fail(GT_ERR_INVALID_ARG, "null camera");
+    if (image_width == 0) return fail(GT_ERR_INVALID_ARG, "image width must be positive");
+    if (!std::isfinite(aspect_ratio) || !(aspect_ratio > 0.0))
+        return fail(GT_ERR_INVALID_ARG, "aspect ratio must be positive and finite");
+    std::memset(c, 0, sizeof(*c));
+    c->struct_size = sizeof(gt_camera_desc);
+    c->image_width = image_width;
+    c->aspect_ratio = aspect_ratio;
+    c->samples_per_pixel = 1;
+    c->pixel_sample_mode = GT_SAMPLE_RANDOM;
+    c->grid_width = 1;
+    c->direct_lighting_mode = GT_DIRECT_CURRENT_PATH_CONTINUATION;
+    c->light_pdf_weight = 0.5;
+    c->max_depth = 10;
+    c->russian_roulette_min_depth = 5;
+    c->rng_seed = 1;
+    c->vertical_fov = 90.0;
+    c->lookat[2] = -1.0;
+    c->view_up[1] = 1.0;
+    c->focus_distance = 1.0;
+    c->shutter_end = 1.0;
+    c->background_kind = GT_BG_CONSTANT;
+    c->background[0] = 0.70;
+    c->background[1] = 0.80;
+    c->background[2] = 1.00;
+    return GT_OK;
+}
+
+gt_status gt_camera_image_size(const gt_camera_desc* c, uint32_t* w, uint32_t* h, uint32_t* spp) {
+    if (!c) return fail(GT_ERR_INVALID_ARG, "null camera");
+    gt_status rc = validate_camera(*c);
+    if (rc != GT_OK) return rc;
+    CamHost ch = init_camera(*c, false);
+    if (w) *w = ch.width;
+    if (h) *h = ch.height;
+    if (spp) *spp = ch.spp;
+    return GT_OK;
+}
+
+gt_status gt_context_create(int device, gt_context** out) {
+    GT_GUARD_BEGIN
+    if (!out) return fail(GT_ERR_INVALID_ARG, "null output handle");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return fail(GT_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    if (device < 0 || device >= count) return fail(GT_ERR_INVALID_ARG, "device index out of range");
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    auto* ctx = new gt_context();
+    ctx->device = device;
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&ctx->pinned), 64);
+    if (e != cudaSuccess) {
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return cuda_fail(e, "context creation");
+    }
+    *out = ctx;
+    return GT_OK;
+    GT_GUARD_END
+}
+
+void gt_context_destroy(gt_context* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->ws);
+    cudaFreeHost(ctx->pinned);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+gt_status gt_scene_create(gt_context* ctx, const gt_scene_desc* d, gt_scene** out) {
+    GT_GUARD_BEGIN
+    if (!ctx || !d || !out) return fail(GT_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    if (d->struct_size < sizeof(gt_scene_desc)) return fail(GT_ERR_INVALID_ARG, "scene struct_size too small");
+    if ((d->num_primitives && !d->primitives) || (d->num_materials && !d->materials))
+        return fail(GT_ERR_INVALID_ARG, "null primitive or material array");
+    if (d->num_primitives > (1u << 28)) return fail(GT_ERR_INVALID_ARG, "too many primitives");
+    for (uint32_t i = 0; i < d->num_materials; ++i) {
+        const gt_material& m = d->materials[i];
+        if (m.kind > GT_MAT_DIELECTRIC) return fail(GT_ERR_INVALID_ARG, "unknown material kind");
+        if (m.texture_kind > GT_TEX_CHECKER) return fail(GT_ERR_INVALID_ARG, "unknown texture kind");
+        if (!finite3(m.color) || !std::isfinite(m.param)) return fail(GT_ERR_INVALID_ARG, "material values must be finite");
+        if (m.kind == GT_MAT_DIELECTRIC && !(m.param > 0.0))
+            return fail(GT_ERR_INVALID_ARG, "refractive index must be positive and finite");
+    }
+    for (uint32_t i = 0; i < d->num_primitives; ++i) {
+        gt_status rc = validate_geometry(d->primitives[i].geometry);
+        if (rc != GT_OK) return rc;
+        if (d->primitives[i].material >= d->num_materials)
+            return fail(GT_ERR_INVALID_ARG, "ray scene material id out of bounds"); // scene.rs:1158-1161
+    }
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    auto* s = new gt_scene();
+    s->ctx = ctx;
+    s->prims.assign(d->primitives, d->primitives + d->num_primitives);
+    s->mats.assign(d->materials, d->materials + d->num_materials);
+    build_reference_bvh(s->prims.data(), d->num_primitives, d->bvh_leaf_size ? d->bvh_leaf_size : 4u, s->bvh);
+    if (s->bvh.max_depth + 1 > 62) {
+        delete s;
+        return fail(GT_ERR_UNSUPPORTED, "BVH deeper than the device traversal stack");
+    }
+    *out = s;
+    return GT_OK;
+    GT_GUARD_END
+}
+
+void gt_scene_destroy(gt_scene* s) {
+    if (!s) return;
+    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    free_gpu_f32(s);
+    free_gpu_f64(s);
+    delete s;
+}
+
+gt_status gt_scene_bvh_node_count(const gt_scene* s, uint32_t* count) {
+    if (!s || !count) return fail(GT_ERR_INVALID_ARG, "null argument");
+    *count = uint32_t(s->bvh.nodes.size());
+    return GT_OK;
+}
+
+gt_status gt_scene_emissive_targets(const gt_scene* s, gt_light_target* targets, uint32_t capacity, uint32_t* count) {
+    if (!s || !count) return fail(GT_ERR_INVALID_ARG, "null argument");
+    uint32_t n = 0;
+    for (const gt_primitive& p : s->prims) {
+        if (s->mats[p.material].kind != GT_MAT_DIFFUSE_LIGHT) continue; // RayMaterial::is_emissive
+        if (targets && n < capacity) {
+            targets[n].geometry = p.geometry;
+            targets[n].weight = 1.0;
+        }
+        ++n;
+    }
+    *count = n;
+    return GT_OK;
+}
+
+gt_status gt_lights_create(gt_context* ctx, const gt_light_target* t, uint32_t count, gt_lights** out) {
+    GT_GUARD_BEGIN
+    if (!ctx || !out || (count && !t)) return fail(GT_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    double total = 0.0;
+    for (uint32_t i = 0; i < count; ++i) { // add_target_weighted, scene.rs:460-476
+        gt_status rc = validate_geometry(t[i].geometry);
+        if (rc != GT_OK) return rc;
+        if (!std::isfinite(t[i].weight) || !(t[i].weight > 0.0))
+            return fail(GT_ERR_INVALID_ARG, "sampling target weight must be finite and positive");
+        total = total + t[i].weight;
+        if (!std::isfinite(total)) return fail(GT_ERR_INVALID_ARG, "sampling target total weight must remain finite");
+    }
+    auto* l = new gt_lights();
+    l->ctx = ctx;
+    l->targets.assign(t, t + count);
+    l->total = total;
+    *out = l;
+    return GT_OK;
+    GT_GUARD_END
+}
+
+void gt_lights_destroy(gt_lights* l) {
+    if (!l) return;
+    std::lock_guard<std::mutex> lock(l->ctx->mu);
+    cudaSetDevice(l->ctx->device);
+    cudaStreamSynchronize(l->ctx->stream);
+    free_lights_f32(l);
+    free_lights_f64(l);
+    delete l;
+}
+
+gt_status gt_environment_create(gt_context* ctx, const gt_environment_desc* d, gt_environment** out) {
+    GT_GUARD_BEGIN
+    if (!ctx || !d || !out) return fail(GT_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    if (d->struct_size < sizeof(gt_environment_desc)) return fail(GT_ERR_INVALID_ARG, "environment struct_size too small");
+    if (d->format > GT_ENV_RGB32F) return fail(GT_ERR_INVALID_ARG, "unknown environment format");
+    if (d->width == 0 || d->height == 0 || !d->texels) return fail(GT_ERR_INVALID_ARG, "empty environment image");
+    if (uint64_t(d->width) * d->height > (1ull << 27)) return fail(GT_ERR_INVALID_ARG, "environment image too large");
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    auto* e = new gt_environment();
+    e->ctx = ctx;
+    e->format = d->format;
+    e->width = d->width;
+    e->height = d->height;
+    const size_t n = size_t(d->width) * d->height;
+    if (d->format == GT_ENV_SRGB8) {
+        const uint8_t* p = static_cast<const uint8_t*>(d->texels);
+        e->px8.assign(p, p + n * 3);
+    } else {
+        const float* p = static_cast<const float*>(d->texels);
+        e->px32.assign(p, p + n * 3);
+        for (float v : e->px32)
+            if (!std::isfinite(v)) {
+                delete e;
+                return fail(GT_ERR_INVALID_ARG, "environment texels must be finite");
+            }
+    }
+    // EnvironmentLight::rebuild_distribution (environment.rs:155-185): weight =
+    // max(luminance(texel), 0) * sin(theta at the row centre), running-sum CDF.
+    const double pi = 3.141592653589793;
+    e->weights.reserve(n);
+    e->cdf.reserve(n);
+    for (uint32_t y = 0; y < d->height; ++y) {
+        double theta = pi * ((double(y) + 0.5) / double(d->height));
+        double s = std::fmax(std::sin(theta), 0.0);
+        for (uint32_t x = 0; x < d->width; ++x) {
+            size_t i = (size_t(y) * d->width + x) * 3;
+            double c[3];
+            for (int k = 0; k < 3; ++k) {
+                if (d->format == GT_ENV_SRGB8) {
+                    double v = double(e->px8[i + k]) / 255.0;
+                    c[k] = v * v;
+                } else {
+                    c[k] = double(e->px32[i + k]);
+                }
+            }
+            double lum = 0.2126 * c[0] + 0.7152 * c[1] + 0.0722 * c[2];
+            double w = std::fmax(lum, 0.0) * s;
+            e->total += w;
+            e->weights.push_back(w);
+            e->cdf.push_back(e->total);
+        }
+    }
+    cudaSetDevice(ctx->device);
+    cudaError_t ce;
+    if (d->format == GT_ENV_SRGB8) {
+        ce = cudaMalloc(&e->d_px8, n * 3);
+        if (ce == cudaSuccess) ce = cudaMemcpy(e->d_px8, e->px8.data(), n * 3, cudaMemcpyHostToDevice);
+    } else {
+        ce = cudaMalloc(&e->d_px32, n * 3 * sizeof(float));
+        if (ce == cudaSuccess) ce = cudaMemcpy(e->d_px32, e->px32.data(), n * 3 * sizeof(float), cudaMemcpyHostToDevice);
+    }
+    if (ce != cudaSuccess) {
+        cudaFree(e->d_px8);
+        cudaFree(e->d_px32);
+        delete e;
+        return cuda_fail(ce, "environment upload");
+    }
+    *out = e;
+    return GT_OK;
+    GT_GUARD_END
+}
+
+void gt_environment_destroy(gt_environment* e) {
+    if (!e) return;
+    std::lock_guard<std::mutex> lock(e->ctx->mu);
+    cudaSetDevice(e->ctx->device);
+    cudaStreamSynchronize(e->ctx->stream);
+    free_env_f32(e);
+    free_env_f64(e);
+    cudaFree(e->d_px8);
+    cudaFree(e->d_px32);
+    delete e;
+}
+
+gt_status gt_render(gt_scene* s, const gt_lights* l, const gt_environment* e, const gt_camera_desc* c,
+                    const gt_render_opts* o, gt_frame* f) {
+    GT_GUARD_BEGIN
+    if (!s || !c || !f) return fail(GT_ERR_INVALID_ARG, "null argument");
+    if (f->struct_size < sizeof(gt_frame)) return fail(GT_ERR_INVALID_ARG, "frame struct_size too small");
+    gt_render_opts opts;
+    std::memset(&opts, 0, sizeof(opts));
+    if (o) {
+        if (o->struct_size < sizeof(gt_render_opts)) return fail(GT_ERR_INVALID_ARG, "options struct_size too small");
+        opts = *o;
+    }
+    if (opts.precision > GT_PRECISION_F64) return fail(GT_ERR_INVALID_ARG, "unknown precision");
+    if ((l && l->ctx != s->ctx) || (e && e->ctx != s->ctx))
+        return fail(GT_ERR_INVALID_ARG, "lights, environment and scene must share a context");
+    gt_status rc = validate_camera(*c);
+    if (rc != GT_OK) return rc;
+    CamHost cam = init_camera(*c, e != nullptr);
+    if (f->width != cam.width || f->height != cam.height)
+        return fail(GT_ERR_INVALID_ARG, "frame size does not match the camera's image size");
+    if (!f->rgb) return fail(GT_ERR_INVALID_ARG, "frame has no rgb buffer");
+    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    cudaError_t ce = cudaSetDevice(s->ctx->device);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
+    auto* env = const_cast<gt_environment*>(e);
+    if (opts.precision == GT_PRECISION_F64) return render_f64(s, l, env, cam, opts, f);
+    return render_f32(s, l, env, cam, opts, f);
+    GT_GUARD_END
+}
+
+gt_status gt_trace_rays(gt_scene* s, const double* rays, uint32_t count, double tmin, double tmax, int32_t* ids,
+                        double* t, gt_bvh_stats* stats) {
+    GT_GUARD_BEGIN
+    if (!s || (count && (!rays || !ids))) return fail(GT_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    cudaError_t ce = cudaSetDevice(s->ctx->device);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
+    if (s->prims.empty()) { // no BVH: RayScene counts a linear scan of zero primitives
+        for (uint32_t i = 0; i < count; ++i) {
+            ids[i] = -1;
+            if (t) t[i] = 0.0;
+        }
+        if (stats) {
+            std::memset(stats, 0, sizeof(*stats));
+            stats->rays = count;
+        }
+        return GT_OK;
+    }
+    return trace_rays_f64(s, rays, count, tmin, tmax, ids, t, stats);
+    GT_GUARD_END
+}
+
+gt_status gt_trace_primary(gt_scene* s, const gt_camera_desc* c, uint32_t stride, int32_t* ids, double* t,
+                           gt_bvh_stats* stats) {
+    GT_GUARD_BEGIN
+    if (!s || !c || !ids) return fail(GT_ERR_INVALID_ARG, "null argument");
+    gt_status rc = validate_camera(*c);
+    if (rc != GT_OK) return rc;
+    if (stride == 0) stride = 1;
+    CamHost cam = init_camera(*c, false);
+    std::vector<double> rays;
+    for (uint32_t y = 0; y < cam.height; y += stride)
+        for (uint32_t x = 0; x < cam.width; x += stride) {
+            // RayCamera::ray_for_pixel (camera.rs:1641-1653), in f64.
+            double pc[3];
+            for (int k = 0; k < 3; ++k) pc[k] = (cam.pixel00[k] + cam.du[k] * double(x)) + cam.dv[k] * double(y);
+            rays.push_back(cam.center[0]);
+            rays.push_back(cam.center[1]);
+            rays.push_back(cam.center[2]);
+            for (int k = 0; k < 3; ++k) rays.push_back(pc[k] - cam.center[k]);
+            rays.push_back(c->shutter_start);
+        }
+    return gt_trace_rays(s, rays.data(), uint32_t(rays.size() / 7), 0.001, INFINITY, ids, t, stats);
+    GT_GUARD_END
+}
+
+} // extern "C"

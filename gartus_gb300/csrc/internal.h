@@ -1,0 +1,111 @@
+// internal.h — host-side objects behind the opaque handles of gartus_gpu.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gartus_gpu.h"
+#include "bvh_build.h"
+#include "layout.h"
+
+namespace gt {
+
+template <class R> struct GpuScene {
+    bool ready = false;
+    PrimRec<R>* prims = nullptr;
+    uint2* meta = nullptr;
+    Node<R>* nodes = nullptr;
+    MatDev<R>* mats = nullptr;
+    SceneDev<R> view{};
+};
+
+template <class R> struct GpuLights {
+    bool ready = false;
+    LightDev<R>* t = nullptr;
+    LightsDev<R> view{};
+};
+
+template <class R> struct GpuEnv {
+    bool ready = false;
+    R* weights = nullptr;
+    R* cdf = nullptr;
+    EnvDev<R> view{};
+};
+
+// Camera after RayCamera::initialized (camera.rs:1068-1130), in f64.
+struct CamHost {
+    double center[3], pixel00[3], du[3], dv[3], ddu[3], ddv[3];
+    uint32_t width, height;
+    uint32_t spp;  // samples per pixel the loops run (effective count)
+    uint32_t grid; // stratified grid width (1 in random mode)
+    gt_camera_desc desc;
+    bool nee;
+    double light_pdf_weight;
+};
+
+void set_error(const std::string& msg);
+gt_status fail(gt_status status, const std::string& msg);
+gt_status cuda_fail(cudaError_t e, const char* what);
+
+} // namespace gt
+
+struct gt_context {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    void* ws = nullptr; // render workspace (path state, queues, staging)
+    size_t ws_bytes = 0;
+    uint32_t* pinned = nullptr; // host-pinned copy of the loop counters
+};
+
+struct gt_scene {
+    gt_context* ctx = nullptr;
+    std::vector<gt_primitive> prims;
+    std::vector<gt_material> mats;
+    gt::BuiltBvh bvh;
+    gt::GpuScene<float> f32;
+    gt::GpuScene<double> f64;
+};
+
+struct gt_lights {
+    gt_context* ctx = nullptr;
+    std::vector<gt_light_target> targets;
+    double total = 0.0;
+    gt::GpuLights<float> f32;
+    gt::GpuLights<double> f64;
+};
+
+struct gt_environment {
+    gt_context* ctx = nullptr;
+    uint32_t format = 0, width = 0, height = 0;
+    uint8_t* d_px8 = nullptr;
+    float* d_px32 = nullptr;
+    std::vector<uint8_t> px8;
+    std::vector<float> px32;
+    std::vector<double> weights, cdf;
+    double total = 0.0;
+    gt::GpuEnv<float> f32;
+    gt::GpuEnv<double> f64;
+};
+
+namespace gt {
+
+// Per-precision entry points (render_f32.cu / render_f64.cu).
+gt_status render_f32(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost& cam,
+                     const gt_render_opts& opts, gt_frame* frame);
+gt_status render_f64(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost& cam,
+                     const gt_render_opts& opts, gt_frame* frame);
+gt_status trace_rays_f64(gt_scene* s, const double* rays, uint32_t count, double tmin, double tmax,
+                         int32_t* ids, double* t, gt_bvh_stats* stats);
+void free_gpu_f32(gt_scene* s);
+void free_gpu_f64(gt_scene* s);
+void free_lights_f32(gt_lights* l);
+void free_lights_f64(gt_lights* l);
+void free_env_f32(gt_environment* e);
+void free_env_f64(gt_environment* e);
+
+} // namespace gt

@@ -1,0 +1,24 @@
+// render_f32.cu — the f32 throughput instantiation of the wavefront integrator.
+#include "render_host.cuh"
+
+namespace gt {
+
+gt_status render_f32(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost& cam,
+                     const gt_render_opts& opts, gt_frame* frame) {
+    return render_impl<float>(s, l, e, cam, opts, frame);
+}
+
+void free_gpu_f32(gt_scene* s) { free_gpu<float>(s); }
+
+void free_lights_f32(gt_lights* l) {
+    cudaFree(l->f32.t);
+    l->f32 = GpuLights<float>();
+}
+
+void free_env_f32(gt_environment* e) {
+    cudaFree(e->f32.weights);
+    cudaFree(e->f32.cdf);
+    e->f32 = GpuEnv<float>();
+}
+
+} // namespace gt

@@ -1,0 +1,722 @@
+// render_host.cuh — per-precision host orchestration: scene/light/environment upload,
+// the wavefront loop (captured as a CUDA graph of two iterations and replayed until every
+// pixel slot has finished), resolve, AOVs, and the statistics trace.  Included by exactly
+// one translation unit per precision.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "internal.h"
+#include "wavefront.cuh"
+
+namespace gt {
+
+#define GT_CUDA(call)                                                   \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);             \
+    } while (0)
+
+template <class R> inline void put3(R* dst, const double* src) {
+    dst[0] = R(src[0]);
+    dst[1] = R(src[1]);
+    dst[2] = R(src[2]);
+}
+
+// f32 child boxes are rounded outward so the f32 slab test never culls a primitive the
+// f64 box contains; f64 boxes are the reference's exactly.
+template <class R> inline R round_down(double v);
+template <class R> inline R round_up(double v);
+template <> inline double round_down<double>(double v) { return v; }
+template <> inline double round_up<double>(double v) { return v; }
+template <> inline float round_down<float>(double v) {
+    float f = float(v);
+    return double(f) > v ? std::nextafter(f, -INFINITY) : f;
+}
+template <> inline float round_up<float>(double v) {
+    float f = float(v);
+    return double(f) < v ? std::nextafter(f, INFINITY) : f;
+}
+
+template <class R> inline void put_box(R* dst, const Aabb& b) {
+    for (int i = 0; i < 3; ++i) {
+        dst[i] = round_down<R>(b.lo[i]);
+        dst[3 + i] = round_up<R>(b.hi[i]);
+    }
+}
+
+template <class R> GpuScene<R>& gpu_of(gt_scene* s);
+template <> inline GpuScene<float>& gpu_of<float>(gt_scene* s) { return s->f32; }
+template <> inline GpuScene<double>& gpu_of<double>(gt_scene* s) { return s->f64; }
+template <class R> GpuLights<R>& lights_of(gt_lights* l);
+template <> inline GpuLights<float>& lights_of<float>(gt_lights* l) { return l->f32; }
+template <> inline GpuLights<double>& lights_of<double>(gt_lights* l) { return l->f64; }
+template <class R> GpuEnv<R>& env_of(gt_environment* e);
+template <> inline GpuEnv<float>& env_of<float>(gt_environment* e) { return e->f32; }
+template <> inline GpuEnv<double>& env_of<double>(gt_environment* e) { return e->f64; }
+
+template <class R> void free_gpu(gt_scene* s) {
+    GpuScene<R>& g = gpu_of<R>(s);
+    cudaFree(g.prims);
+    cudaFree(g.meta);
+    cudaFree(g.nodes);
+    cudaFree(g.mats);
+    g = GpuScene<R>();
+}
+
+// Flattens the primitives into leaf order with derived quantities computed in f64
+// (QuadGeometry::new, geometry.rs:271-301; TriangleGeometry::geometric_normal 171-179).
+template <class R> gt_status upload_scene(gt_scene* s) {
+    GpuScene<R>& g = gpu_of<R>(s);
+    if (g.ready) return GT_OK;
+    const BuiltBvh& bvh = s->bvh;
+    const size_t n = s->prims.size();
+    std::vector<PrimRec<R>> recs(n);
+    std::vector<uint2> meta(n);
+    for (size_t j = 0; j < n; ++j) {
+        const uint32_t pi = bvh.order[j];
+        const gt_primitive& p = s->prims[pi];
+        const double* q = p.geometry.p;
+        R* v = recs[j].v;
+        std::fill(v, v + 16, R(0));
+        uint32_t kind = p.geometry.kind;
+        switch (p.geometry.kind) {
+        case GT_GEOM_SPHERE:
+            put3(v, q);
+            v[3] = R(std::fmax(q[3], 0.0));
+            break;
+        case GT_GEOM_MOVING_SPHERE: {
+            put3(v, q);
+            v[3] = R(std::fmax(q[6], 0.0));
+            double dl[3] = {q[3] - q[0], q[4] - q[1], q[5] - q[2]};
+            put3(v + 4, dl);
+            break;
+        }
+        case GT_GEOM_TRIANGLE: {
+            double e1[3] = {q[3] - q[0], q[4] - q[1], q[5] - q[2]};
+            double e2[3] = {q[6] - q[0], q[7] - q[1], q[8] - q[2]};
+            double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+            double len = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+            double nrm[3] = {0, 0, 0};
+            if (!(len < 2.220446049250313e-16))
+                for (int k = 0; k < 3; ++k) nrm[k] = c[k] / len;
+            put3(v, q);
+            put3(v + 4, e1);
+            put3(v + 8, e2);
+            put3(v + 12, nrm);
+            if (nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2] <= 2.220446049250313e-16) kind = K_NEVER;
+            break;
+        }
+        case GT_GEOM_QUAD: {
+            const double* u = q + 3;
+            const double* w = q + 6;
+            double c[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+            double l2 = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+            double len = std::sqrt(l2);
+            double nrm[3] = {0, 0, 0};
+            if (!(len < 2.220446049250313e-16))
+                for (int k = 0; k < 3; ++k) nrm[k] = c[k] / len;
+            double pd = nrm[0] * q[0] + nrm[1] * q[1] + nrm[2] * q[2];
+            double ww[3] = {0, 0, 0};
+            if (!(l2 <= 2.220446049250313e-16))
+                for (int k = 0; k < 3; ++k) ww[k] = c[k] / l2;
+            put3(v, q);
+            v[3] = R(pd);
+            put3(v + 4, u);
+            v[7] = R(nrm[0]);
+            put3(v + 8, w);
+            v[11] = R(nrm[1]);
+            put3(v + 12, ww);
+            v[15] = R(nrm[2]);
+            if (l2 <= 2.220446049250313e-16) kind = K_NEVER; // area_squared() <= EPS
+            if (nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2] <= 2.220446049250313e-16) kind = K_NEVER;
+            break;
+        }
+        default:
+            return fail(GT_ERR_INVALID_ARG, "unknown geometry kind");
+        }
+        meta[j] = make_uint2(kind | (p.material << 3), pi);
+    }
+    // Internal nodes, renumbered densely in pre-order; leaf children become links.
+    std::vector<int32_t> internal_id(bvh.nodes.size(), -1);
+    int32_t ni = 0;
+    for (size_t i = 0; i < bvh.nodes.size(); ++i)
+        if (!bvh.nodes[i].leaf) internal_id[i] = ni++;
+    std::vector<Node<R>> nodes(static_cast<size_t>(ni));
+    auto link_of = [&](uint32_t child, int32_t& link, int32_t& count) {
+        const BuildNode& c = bvh.nodes[child];
+        if (c.leaf) {
+            link = ~int32_t(c.first);
+            count = int32_t(c.count);
+        } else {
+            link = internal_id[child];
+            count = 0;
+        }
+    };
+    for (size_t i = 0; i < bvh.nodes.size(); ++i) {
+        const BuildNode& b = bvh.nodes[i];
+        if (b.leaf) continue;
+        Node<R>& nd = nodes[size_t(internal_id[i])];
+        put_box<R>(nd.box, bvh.nodes[b.left].box);
+        put_box<R>(nd.box + 6, bvh.nodes[b.right].box);
+        link_of(b.left, nd.link[0], nd.link[1]);
+        link_of(b.right, nd.link[2], nd.link[3]);
+    }
+    std::vector<MatDev<R>> mats(s->mats.size());
+    for (size_t i = 0; i < s->mats.size(); ++i) {
+        const gt_material& m = s->mats[i];
+        MatDev<R>& d = mats[i];
+        std::memset(&d, 0, sizeof(d));
+        d.kind = int32_t(m.kind);
+        d.tex = int32_t(m.texture_kind);
+        put3(d.color, m.color);
+        d.param = R(m.param);
+        if (m.kind == GT_MAT_GGX || m.kind == GT_MAT_METAL) // material.rs:1386, 1972
+            d.param = R(std::fmin(std::fmax(m.param, 0.0), 1.0));
+        if (m.texture_kind == GT_TEX_CHECKER) { // CheckerTexture::new, raytracing/texture.rs:71-82
+            double sc = m.tex[0];
+            d.inv_scale = R((std::isfinite(sc) && std::fabs(sc) > 2.220446049250313e-16) ? 1.0 / std::fabs(sc) : 1.0);
+            put3(d.even, m.tex + 1);
+            put3(d.odd, m.tex + 4);
+        }
+    }
+    free_gpu<R>(s);
+    GT_CUDA(cudaMalloc(&g.prims, std::max<size_t>(n, 1) * sizeof(PrimRec<R>)));
+    GT_CUDA(cudaMalloc(&g.meta, std::max<size_t>(n, 1) * sizeof(uint2)));
+    GT_CUDA(cudaMalloc(&g.nodes, std::max<size_t>(nodes.size(), 1) * sizeof(Node<R>)));
+    GT_CUDA(cudaMalloc(&g.mats, std::max<size_t>(mats.size(), 1) * sizeof(MatDev<R>)));
+    cudaStream_t st = s->ctx->stream;
+    if (n) {
+        GT_CUDA(cudaMemcpyAsync(g.prims, recs.data(), n * sizeof(PrimRec<R>), cudaMemcpyHostToDevice, st));
+        GT_CUDA(cudaMemcpyAsync(g.meta, meta.data(), n * sizeof(uint2), cudaMemcpyHostToDevice, st));
+    }
+    if (!nodes.empty())
+        GT_CUDA(cudaMemcpyAsync(g.nodes, nodes.data(), nodes.size() * sizeof(Node<R>), cudaMemcpyHostToDevice, st));
+    if (!mats.empty())
+        GT_CUDA(cudaMemcpyAsync(g.mats, mats.data(), mats.size() * sizeof(MatDev<R>), cudaMemcpyHostToDevice, st));
+    GT_CUDA(cudaStreamSynchronize(st));
+    SceneDev<R>& v = g.view;
+    v.prims = g.prims;
+    v.meta = g.meta;
+    v.nodes = g.nodes;
+    v.mats = g.mats;
+    v.num_prims = uint32_t(n);
+    v.num_nodes = uint32_t(nodes.size());
+    if (!bvh.nodes.empty()) {
+        put_box<R>(v.root_box, bvh.nodes[0].box);
+        link_of(0, v.root_link, v.root_count);
+    } else { // an empty scene: a root box that no ray can enter
+        for (int k = 0; k < 3; ++k) {
+            v.root_box[k] = R(1);
+            v.root_box[3 + k] = R(-1);
+        }
+        v.root_link = ~0;
+        v.root_count = 0;
+    }
+    g.ready = true;
+    return GT_OK;
+}
+
+template <class R> gt_status upload_lights(gt_lights* l) {
+    GpuLights<R>& g = lights_of<R>(l);
+    if (g.ready) return GT_OK;
+    std::vector<LightDev<R>> t(l->targets.size());
+    for (size_t i = 0; i < t.size(); ++i) {
+        const gt_geometry& geo = l->targets[i].geometry;
+        const double* q = geo.p;
+        LightDev<R>& d = t[i];
+        std::memset(&d, 0, sizeof(d));
+        d.kind = int32_t(geo.kind);
+        d.weight = R(l->targets[i].weight);
+        switch (geo.kind) {
+        case GT_GEOM_SPHERE:
+            put3(d.a, q);
+            d.radius = R(std::fmax(q[3], 0.0));
+            break;
+        case GT_GEOM_MOVING_SPHERE: {
+            put3(d.a, q);
+            double dl[3] = {q[3] - q[0], q[4] - q[1], q[5] - q[2]};
+            put3(d.b, dl);
+            d.radius = R(std::fmax(q[6], 0.0));
+            break;
+        }
+        case GT_GEOM_QUAD: {
+            const double* u = q + 3;
+            const double* w = q + 6;
+            double c[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+            double l2 = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+            double len = std::sqrt(l2);
+            double nrm[3] = {0, 0, 0}, ww[3] = {0, 0, 0};
+            if (!(len < 2.220446049250313e-16))
+                for (int k = 0; k < 3; ++k) nrm[k] = c[k] / len;
+            if (!(l2 <= 2.220446049250313e-16))
+                for (int k = 0; k < 3; ++k) ww[k] = c[k] / l2;
+            put3(d.a, q);
+            put3(d.b, u);
+            put3(d.c, w);
+            put3(d.n, nrm);
+            put3(d.w, ww);
+            d.plane_d = R(nrm[0] * q[0] + nrm[1] * q[1] + nrm[2] * q[2]);
+            d.area_sq = R(l2);
+            d.area = R(std::sqrt(l2));
+            break;
+        }
+        case GT_GEOM_TRIANGLE: {
+            double e1[3] = {q[3] - q[0], q[4] - q[1], q[5] - q[2]};
+            double e2[3] = {q[6] - q[0], q[7] - q[1], q[8] - q[2]};
+            double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+            double l2 = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+            double len = std::sqrt(l2);
+            double nrm[3] = {0, 0, 0};
+            if (!(len < 2.220446049250313e-16))
+                for (int k = 0; k < 3; ++k) nrm[k] = c[k] / len;
+            put3(d.a, q);
+            put3(d.b, q + 3);
+            put3(d.c, q + 6);
+            put3(d.n, nrm);
+            d.area = R(0.5 * std::sqrt(l2));
+            break;
+        }
+        default:
+            return fail(GT_ERR_INVALID_ARG, "unknown light geometry kind");
+        }
+    }
+    cudaFree(g.t);
+    g.t = nullptr;
+    GT_CUDA(cudaMalloc(&g.t, std::max<size_t>(t.size(), 1) * sizeof(LightDev<R>)));
+    if (!t.empty())
+        GT_CUDA(cudaMemcpyAsync(g.t, t.data(), t.size() * sizeof(LightDev<R>), cudaMemcpyHostToDevice, l->ctx->stream));
+    GT_CUDA(cudaStreamSynchronize(l->ctx->stream));
+    g.view.t = g.t;
+    g.view.count = uint32_t(t.size());
+    g.view.total = R(l->total);
+    g.ready = true;
+    return GT_OK;
+}
+
+template <class R> gt_status upload_env(gt_environment* e) {
+    GpuEnv<R>& g = env_of<R>(e);
+    if (g.ready) return GT_OK;
+    const size_t n = e->weights.size();
+    std::vector<R> w(n), c(n);
+    for (size_t i = 0; i < n; ++i) {
+        w[i] = R(e->weights[i]);
+        c[i] = R(e->cdf[i]);
+    }
+    cudaFree(g.weights);
+    cudaFree(g.cdf);
+    g.weights = g.cdf = nullptr;
+    GT_CUDA(cudaMalloc(&g.weights, std::max<size_t>(n, 1) * sizeof(R)));
+    GT_CUDA(cudaMalloc(&g.cdf, std::max<size_t>(n, 1) * sizeof(R)));
+    if (n) {
+        GT_CUDA(cudaMemcpyAsync(g.weights, w.data(), n * sizeof(R), cudaMemcpyHostToDevice, e->ctx->stream));
+        GT_CUDA(cudaMemcpyAsync(g.cdf, c.data(), n * sizeof(R), cudaMemcpyHostToDevice, e->ctx->stream));
+    }
+    GT_CUDA(cudaStreamSynchronize(e->ctx->stream));
+    g.view.format = int32_t(e->format);
+    g.view.width = e->width;
+    g.view.height = e->height;
+    g.view.px8 = e->d_px8;
+    g.view.px32 = e->d_px32;
+    g.view.weights = g.weights;
+    g.view.cdf = g.cdf;
+    g.view.total = R(e->total);
+    g.ready = true;
+    return GT_OK;
+}
+
+template <class R> CamDev<R> cam_dev(const CamHost& h, bool use_lights, bool use_env) {
+    CamDev<R> c;
+    std::memset(&c, 0, sizeof(c));
+    put3(c.center, h.center);
+    put3(c.pixel00, h.pixel00);
+    put3(c.du, h.du);
+    put3(c.dv, h.dv);
+    put3(c.ddu, h.ddu);
+    put3(c.ddv, h.ddv);
+    const gt_camera_desc& d = h.desc;
+    c.shutter0 = R(d.shutter_start);
+    c.shutter1 = R(d.shutter_end);
+    c.light_pdf_weight = R(h.light_pdf_weight);
+    c.adaptive_threshold = R(d.adaptive_error_threshold);
+    for (int i = 0; i < 9; ++i) c.bg[i] = R(d.background[i]);
+    c.seed = d.rng_seed;
+    c.width = h.width;
+    c.height = h.height;
+    c.spp = h.spp;
+    c.mode = d.pixel_sample_mode;
+    c.grid = h.grid;
+    c.adaptive = (d.adaptive && d.pixel_sample_mode == GT_SAMPLE_RANDOM) ? 1u : 0u;
+    c.adaptive_min = std::max<uint32_t>(d.adaptive_min_samples, 1u);
+    c.adaptive_max = std::max<uint32_t>(d.adaptive_max_samples, c.adaptive_min);
+    c.max_depth = d.max_depth;
+    c.rr_min_depth = d.russian_roulette_min_depth;
+    c.defocus = d.defocus_angle <= 0.0 ? 0u : 1u;
+    c.bg_kind = d.background_kind;
+    c.nee = h.nee ? 1u : 0u;
+    c.use_lights = use_lights ? 1u : 0u;
+    c.use_env = use_env ? 1u : 0u;
+    return c;
+}
+
+// Bump allocator over the context workspace.
+struct Bump {
+    char* base;
+    size_t off = 0;
+    template <class T> T* take(size_t count) {
+        off = (off + 255) & ~size_t(255);
+        T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
+        off += count * sizeof(T);
+        return p;
+    }
+};
+
+template <class R> size_t layout_state(Bump& b, PathState<R>& ps, uint32_t n, bool nee) {
+    ps.n = n;
+    ps.ray_o = b.take<R4<R>>(n);
+    ps.ray_d = b.take<R4<R>>(n);
+    ps.att = b.take<R4<R>>(n);
+    ps.col = b.take<R4<R>>(n);
+    ps.st = b.take<uint4>(n);
+    ps.hit_t = b.take<R>(n);
+    ps.hit_prim = b.take<int32_t>(n);
+    ps.acc = b.take<R4<R>>(n);
+    ps.comp = b.take<R4<R>>(n);
+    ps.accepted = b.take<uint32_t>(n);
+    const size_t ns = nee ? size_t(n) * 2 : 2;
+    ps.sh_o = b.take<R4<R>>(ns);
+    ps.sh_d = b.take<R4<R>>(ns);
+    ps.sh_a = b.take<R4<R>>(ns);
+    ps.sh_s = b.take<R4<R>>(ns);
+    ps.q_trace[0] = b.take<uint32_t>(n);
+    ps.q_trace[1] = b.take<uint32_t>(n);
+    ps.q_mat = b.take<uint32_t>(size_t(n) * NUM_KEYS);
+    ps.q_shadow = b.take<uint32_t>(nee ? n : 1);
+    ps.counters = b.take<uint32_t>(C_COUNT);
+    ps.totals = b.take<unsigned long long>(4);
+    return b.off;
+}
+
+inline gt_status ensure_workspace(gt_context* ctx, size_t bytes) {
+    if (ctx->ws_bytes >= bytes) return GT_OK;
+    if (ctx->ws) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->ws);
+        ctx->ws = nullptr;
+        ctx->ws_bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&ctx->ws, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GT_ERR_OOM, "cannot allocate the render workspace");
+    }
+    ctx->ws_bytes = bytes;
+    return GT_OK;
+}
+
+// CUDA events for whole-render timing and, in profile mode, per-kernel timing.
+struct EventPool {
+    cudaEvent_t begin = nullptr, end = nullptr;
+    struct Rec {
+        int kernel;
+        cudaEvent_t a, z;
+    };
+    std::vector<cudaEvent_t> free_events;
+    std::vector<Rec> pending;
+    gt_status init() {
+        if (cudaEventCreate(&begin) != cudaSuccess || cudaEventCreate(&end) != cudaSuccess)
+            return fail(GT_ERR_CUDA, "cudaEventCreate");
+        return GT_OK;
+    }
+    cudaError_t get(cudaEvent_t& e) {
+        if (!free_events.empty()) {
+            e = free_events.back();
+            free_events.pop_back();
+            return cudaSuccess;
+        }
+        return cudaEventCreate(&e);
+    }
+    cudaError_t pair(cudaEvent_t& a, cudaEvent_t& z) {
+        cudaError_t r = get(a);
+        return r == cudaSuccess ? get(z) : r;
+    }
+    void note(int kernel, cudaEvent_t a, cudaEvent_t z) { pending.push_back(Rec{kernel, a, z}); }
+    // Call after a stream synchronize: folds finished pairs into the totals.
+    void harvest(double* ms, uint64_t* launches) {
+        for (const Rec& r : pending) {
+            float t = 0.f;
+            if (cudaEventElapsedTime(&t, r.a, r.z) == cudaSuccess) ms[r.kernel] += t;
+            launches[r.kernel] += 1;
+            free_events.push_back(r.a);
+            free_events.push_back(r.z);
+        }
+        pending.clear();
+    }
+    ~EventPool() {
+        for (const Rec& r : pending) {
+            free_events.push_back(r.a);
+            free_events.push_back(r.z);
+        }
+        for (cudaEvent_t e : free_events) cudaEventDestroy(e);
+        if (begin) cudaEventDestroy(begin);
+        if (end) cudaEventDestroy(end);
+    }
+};
+
+template <class R>
+gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost& cam,
+                      const gt_render_opts& opts, gt_frame* frame) {
+    gt_context* ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    gt_status rc;
+    if ((rc = upload_scene<R>(s)) != GT_OK) return rc;
+    const bool use_lights = l != nullptr;
+    const bool use_env = e != nullptr;
+    Params<R> P;
+    std::memset(&P, 0, sizeof(P));
+    P.sc = gpu_of<R>(s).view;
+    if (use_lights) {
+        if ((rc = upload_lights<R>(const_cast<gt_lights*>(l))) != GT_OK) return rc;
+        P.lights = lights_of<R>(const_cast<gt_lights*>(l)).view;
+    }
+    if (use_env) {
+        if ((rc = upload_env<R>(e)) != GT_OK) return rc;
+        P.env = env_of<R>(e).view;
+    }
+    P.cam = cam_dev<R>(cam, use_lights, use_env);
+    const uint32_t n = cam.width * cam.height;
+    const bool nee = P.cam.nee && (use_lights || use_env);
+
+    // Workspace: path state, queues, and device staging for host outputs.
+    const bool host_out = frame->device_buffers == 0;
+    Bump sizing{nullptr};
+    layout_state<R>(sizing, P.ps, n, nee);
+    sizing.take<float>(size_t(n) * 3 * 3);
+    sizing.take<double>(size_t(n) * 3);
+    sizing.take<uint32_t>(n);
+    if ((rc = ensure_workspace(ctx, sizing.off + 4096)) != GT_OK) return rc;
+    Bump b{static_cast<char*>(ctx->ws)};
+    layout_state<R>(b, P.ps, n, nee);
+    float* d_rgb = b.take<float>(size_t(n) * 3);
+    float* d_alb = b.take<float>(size_t(n) * 3);
+    float* d_nrm = b.take<float>(size_t(n) * 3);
+    double* d_rgb64 = b.take<double>(size_t(n) * 3);
+    uint32_t* d_acc = b.take<uint32_t>(n);
+    float* o_rgb = host_out ? d_rgb : frame->rgb;
+    float* o_alb = host_out ? (frame->albedo ? d_alb : nullptr) : frame->albedo;
+    float* o_nrm = host_out ? (frame->normal ? d_nrm : nullptr) : frame->normal;
+    double* o_rgb64 = host_out ? (frame->rgb64 ? d_rgb64 : nullptr) : frame->rgb64;
+    uint32_t* o_acc = host_out ? (frame->accepted ? d_acc : nullptr) : frame->accepted;
+
+    const int sms = ctx->num_sms > 0 ? ctx->num_sms : 1;
+    const uint32_t threads = 256;
+    const uint32_t slot_blocks = std::max<uint32_t>(1u, std::min<uint32_t>((n + threads - 1) / threads, uint32_t(sms) * 8));
+    const uint32_t work_blocks = std::max<uint32_t>(1u, std::min<uint32_t>((n + threads - 1) / threads, uint32_t(sms) * 6));
+
+    // Device time of the whole render, and in profile mode of every kernel launch.
+    EventPool ev;
+    if ((rc = ev.init()) != GT_OK) return rc;
+    const bool profile = opts.profile != 0;
+    double kms[GT_KERNEL_COUNT] = {0};
+    uint64_t klaunch[GT_KERNEL_COUNT] = {0};
+    GT_CUDA(cudaEventRecord(ev.begin, st));
+    {
+        cudaEvent_t a = nullptr, z = nullptr;
+        if (profile) GT_CUDA(ev.pair(a, z));
+        if (profile) GT_CUDA(cudaEventRecord(a, st));
+        k_init<R><<<slot_blocks, threads, 0, st>>>(P);
+        GT_CUDA(cudaGetLastError());
+        if (profile) {
+            GT_CUDA(cudaEventRecord(z, st));
+            ev.note(GT_KERNEL_OTHER, a, z);
+        }
+    }
+
+    // One iteration = generate, trace, shade (+ shadow); two iterations (ping-pong trace
+    // queues) are captured once as a graph and replayed.
+    auto launch_iteration = [&](uint32_t cur, bool timed) -> cudaError_t {
+        for (int k = 0; k < 4; ++k) {
+            if (k == 3 && !nee) break;
+            cudaEvent_t a = nullptr, z = nullptr;
+            if (timed) {
+                cudaError_t e = ev.pair(a, z);
+                if (e != cudaSuccess) return e;
+                cudaEventRecord(a, st);
+            }
+            if (k == 0) k_generate<R><<<slot_blocks, threads, 0, st>>>(P, cur);
+            else if (k == 1) k_trace<R><<<work_blocks, threads, 0, st>>>(P, cur);
+            else if (k == 2) k_shade<R><<<work_blocks, threads, 0, st>>>(P, cur);
+            else k_shadow<R><<<work_blocks, threads, 0, st>>>(P);
+            if (timed) {
+                cudaEventRecord(z, st);
+                ev.note(k == 0 ? GT_KERNEL_GENERATE : k == 1 ? GT_KERNEL_TRACE : k == 2 ? GT_KERNEL_SHADE : GT_KERNEL_SHADOW,
+                        a, z);
+            }
+        }
+        return cudaGetLastError();
+    };
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t ce = cudaSuccess;
+    if (!profile) {
+        cudaGraph_t graph = nullptr;
+        GT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        cudaError_t le = launch_iteration(0, false);
+        if (le == cudaSuccess) le = launch_iteration(1, false);
+        ce = cudaStreamEndCapture(st, &graph);
+        if (le != cudaSuccess) return cuda_fail(le, "kernel launch during capture");
+        if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+        ce = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) return cuda_fail(ce, "cudaGraphInstantiate");
+    }
+
+    const uint32_t limit = P.cam.adaptive ? P.cam.adaptive_max : P.cam.spp;
+    const uint64_t max_iters = uint64_t(limit) * uint64_t(std::max<uint32_t>(P.cam.max_depth, 1u)) + 8;
+    uint64_t iters = 0;
+    uint32_t batch = 2;
+    rc = GT_OK;
+    for (;;) {
+        for (uint32_t k = 0; k < batch && ce == cudaSuccess; ++k) {
+            if (profile) {
+                ce = launch_iteration(0, true);
+                if (ce == cudaSuccess) ce = launch_iteration(1, true);
+            } else {
+                ce = cudaGraphLaunch(exec, st);
+            }
+        }
+        if (ce != cudaSuccess) {
+            rc = cuda_fail(ce, "wavefront launch");
+            break;
+        }
+        iters += 2ull * batch;
+        ce = cudaMemcpyAsync(ctx->pinned, P.ps.counters + C_DONE, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+        if (ce != cudaSuccess) {
+            rc = cuda_fail(ce, "render loop");
+            break;
+        }
+        if (profile) ev.harvest(kms, klaunch);
+        const uint32_t done = ctx->pinned[0], err = ctx->pinned[1];
+        if (err) {
+            rc = fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
+            break;
+        }
+        if (done >= n) break;
+        if (opts.progress && opts.progress(opts.progress_user, uint64_t(done) * limit, uint64_t(n) * limit)) {
+            rc = fail(GT_ERR_CANCELLED, "render cancelled by the progress callback");
+            break;
+        }
+        if (iters > max_iters) {
+            rc = fail(GT_ERR_INTERNAL, "wavefront did not terminate within its iteration bound");
+            break;
+        }
+        batch = std::min<uint32_t>(batch * 2, profile ? 8u : 64u);
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (rc != GT_OK) {
+        cudaStreamSynchronize(st);
+        return rc;
+    }
+
+    {
+        cudaEvent_t a = nullptr, z = nullptr;
+        if (profile) GT_CUDA(ev.pair(a, z));
+        if (profile) GT_CUDA(cudaEventRecord(a, st));
+        k_resolve<R><<<slot_blocks, threads, 0, st>>>(P, o_rgb, o_rgb64, o_acc);
+        GT_CUDA(cudaGetLastError());
+        if (opts.aovs && (o_alb || o_nrm)) {
+            k_aov<R><<<slot_blocks, threads, 0, st>>>(P, o_alb, o_nrm);
+            GT_CUDA(cudaGetLastError());
+        }
+        if (profile) {
+            GT_CUDA(cudaEventRecord(z, st));
+            ev.note(GT_KERNEL_OTHER, a, z);
+        }
+    }
+    GT_CUDA(cudaEventRecord(ev.end, st));
+    if (host_out) {
+        GT_CUDA(cudaMemcpyAsync(frame->rgb, o_rgb, size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (frame->rgb64)
+            GT_CUDA(cudaMemcpyAsync(frame->rgb64, o_rgb64, size_t(n) * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (frame->accepted)
+            GT_CUDA(cudaMemcpyAsync(frame->accepted, o_acc, size_t(n) * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        if (opts.aovs && frame->albedo)
+            GT_CUDA(cudaMemcpyAsync(frame->albedo, o_alb, size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (opts.aovs && frame->normal)
+            GT_CUDA(cudaMemcpyAsync(frame->normal, o_nrm, size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+    }
+    unsigned long long tot[4];
+    GT_CUDA(cudaMemcpyAsync(ctx->pinned + 2, P.ps.totals, sizeof(tot), cudaMemcpyDeviceToHost, st));
+    GT_CUDA(cudaMemcpyAsync(ctx->pinned, P.ps.counters + C_ERROR, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GT_CUDA(cudaStreamSynchronize(st));
+    if (ctx->pinned[0]) return fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
+    std::memcpy(tot, ctx->pinned + 2, sizeof(tot));
+    if (opts.stats) {
+        gt_render_stats& o = *opts.stats;
+        std::memset(&o, 0, sizeof(o));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev.begin, ev.end);
+        o.gpu_ms = ms;
+        o.iterations = iters;
+        o.rays = tot[0];
+        o.shadow_rays = tot[1];
+        o.samples = tot[2];
+        o.samples_started = tot[3];
+        if (profile) {
+            ev.harvest(kms, klaunch);
+            for (int k = 0; k < GT_KERNEL_COUNT; ++k) {
+                o.kernel_ms[k] = kms[k];
+                o.kernel_launches[k] = klaunch[k];
+            }
+        }
+    }
+    return GT_OK;
+}
+
+template <class R>
+gt_status trace_impl(gt_scene* s, const double* rays, uint32_t count, double tmin, double tmax, int32_t* ids,
+                     double* t, gt_bvh_stats* stats) {
+    gt_context* ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    gt_status rc;
+    if ((rc = upload_scene<R>(s)) != GT_OK) return rc;
+    Bump sizing{nullptr};
+    sizing.take<double>(size_t(count) * 7);
+    sizing.take<int32_t>(count);
+    sizing.take<double>(count);
+    sizing.take<unsigned long long>(8);
+    if ((rc = ensure_workspace(ctx, sizing.off + 4096)) != GT_OK) return rc;
+    Bump b{static_cast<char*>(ctx->ws)};
+    double* d_rays = b.take<double>(size_t(count) * 7);
+    int32_t* d_ids = b.take<int32_t>(count);
+    double* d_t = b.take<double>(count);
+    unsigned long long* d_stats = b.take<unsigned long long>(8);
+    if (count) GT_CUDA(cudaMemcpyAsync(d_rays, rays, size_t(count) * 7 * sizeof(double), cudaMemcpyHostToDevice, st));
+    GT_CUDA(cudaMemsetAsync(d_stats, 0, 8 * sizeof(unsigned long long), st));
+    if (count) {
+        const uint32_t blocks = std::min<uint32_t>((count + 127) / 128, uint32_t(std::max(ctx->num_sms, 1)) * 8);
+        k_trace_rays<R><<<blocks, 128, 0, st>>>(gpu_of<R>(s).view, d_rays, count, tmin, tmax, d_ids, d_t, d_stats,
+                                                reinterpret_cast<uint32_t*>(d_stats + 7));
+        GT_CUDA(cudaGetLastError());
+        GT_CUDA(cudaMemcpyAsync(ids, d_ids, size_t(count) * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        if (t) GT_CUDA(cudaMemcpyAsync(t, d_t, size_t(count) * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    unsigned long long h[8];
+    GT_CUDA(cudaMemcpyAsync(h, d_stats, sizeof(h), cudaMemcpyDeviceToHost, st));
+    GT_CUDA(cudaStreamSynchronize(st));
+    if (h[7] & 0xffffffffull) return fail(GT_ERR_INTERNAL, "traversal stack overflow");
+    if (stats) {
+        stats->rays = count;
+        stats->node_bounds_tests = h[0];
+        stats->node_bounds_hits = h[1];
+        stats->leaf_visits = h[2];
+        stats->primitive_candidates = h[3];
+        stats->leaf_hit_results = h[4];
+        stats->max_stack_depth = h[5];
+    }
+    return GT_OK;
+}
+
+} // namespace gt

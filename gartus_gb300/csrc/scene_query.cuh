@@ -1,0 +1,674 @@
+// scene_query.cuh — device-side scene queries: BVH traversal (with the reference's
+// visiting order and statistics), primitive intersection, hit records, materials,
+// sampling targets, the environment light and camera rays.
+#pragma once
+
+#include "device_math.cuh"
+
+namespace gt {
+
+// Vector loads of 4 scalars (one LDG.128 in f32, two in f64).
+template <class R> GT_DEV R4<R> ld4(const R* p) { return *reinterpret_cast<const R4<R>*>(p); }
+template <class R> GT_DEV R4<R> ldg4(const R* p);
+template <> GT_DEV R4<float> ldg4<float>(const float* p) {
+    float4 v = __ldg(reinterpret_cast<const float4*>(p));
+    return R4<float>{v.x, v.y, v.z, v.w};
+}
+template <> GT_DEV R4<double> ldg4<double>(const double* p) {
+    double2 a = __ldg(reinterpret_cast<const double2*>(p));
+    double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+    return R4<double>{a.x, a.y, b.x, b.y};
+}
+template <class R> GT_DEV V3<R> xyz(R4<R> v) { return V3<R>{v.x, v.y, v.z}; }
+
+// The f32 slab test widens the exit distance by 1 + 2*gamma(3) (gamma(n) = n u / (1 - n u),
+// u = 2^-24) so rounding never culls a box the ray passes through (Ize, "Robust BVH Ray
+// Traversal", JCGT 2013).  The f64 test is the reference's exactly (bvh.rs:119-146).
+template <class R> struct SlabPad;
+template <> struct SlabPad<float> {
+    static GT_DEV float pad(float t) { return t * 1.00000036f; }
+};
+template <> struct SlabPad<double> {
+    static GT_DEV double pad(double t) { return t; }
+};
+
+template <class R> struct RayT {
+    R o[3], inv[3];
+    bool par[3];
+};
+template <class R> GT_DEV RayT<R> make_rayt(V3<R> o, V3<R> d) { // RayTraversal::new, bvh.rs:99-117
+    RayT<R> r;
+    R dd[3] = {d.x, d.y, d.z};
+    r.o[0] = o.x;
+    r.o[1] = o.y;
+    r.o[2] = o.z;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        r.par[i] = Num<R>::fabs(dd[i]) <= R(kEps);
+        r.inv[i] = r.par[i] ? R(0) : R(1) / dd[i];
+    }
+    return r;
+}
+// RayTraversal::hit_bounds (bvh.rs:119-146): box = {min xyz, max xyz}.
+template <class R> GT_DEV bool hit_box(const RayT<R>& r, const R* mn, const R* mx, R tmin, R tmax, R& entry) {
+    R en = tmin, ex = tmax;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (r.par[a]) {
+            if (r.o[a] < mn[a] || r.o[a] > mx[a]) return false;
+            continue;
+        }
+        R t0 = (mn[a] - r.o[a]) * r.inv[a];
+        R t1 = (mx[a] - r.o[a]) * r.inv[a];
+        if (r.inv[a] < R(0)) {
+            R tmp = t0;
+            t0 = t1;
+            t1 = tmp;
+        }
+        en = Num<R>::fmax(en, t0);
+        ex = Num<R>::fmin(ex, SlabPad<R>::pad(t1));
+        if (ex <= en) return false;
+    }
+    entry = en;
+    return true;
+}
+
+// --------------------------------------------------------------- intersection
+template <class R> GT_DEV bool sphere_root(V3<R> center, R radius, V3<R> o, V3<R> d, R tmin, R tmax, R& root) {
+    V3<R> oc = center - o; // hit_sphere_in_interval, object.rs:986-1013
+    R a = len2(d);
+    if (a <= R(kEps)) return false;
+    R h = dot(d, oc);
+    R c = len2(oc) - radius * radius;
+    R disc = h * h - a * c;
+    if (disc < R(0)) return false;
+    R sq = Num<R>::sqrt(disc);
+    R first = (h - sq) / a;
+    if (tmin < first && first < tmax) {
+        root = first;
+        return true;
+    }
+    R second = (h + sq) / a;
+    if (tmin < second && second < tmax) {
+        root = second;
+        return true;
+    }
+    return false;
+}
+
+// Möller–Trumbore with the reference's tolerances (geometry.rs:239-265), edges given.
+template <class R> GT_DEV bool tri_hit(V3<R> p0, V3<R> e1, V3<R> e2, V3<R> o, V3<R> d, R tmin, R tmax, R& t) {
+    V3<R> pvec = cross(d, e2);
+    R det = dot(e1, pvec);
+    if (Num<R>::fabs(det) < R(kTriHitEps)) return false;
+    R inv_det = R(1) / det;
+    V3<R> tvec = o - p0;
+    R u = dot(tvec, pvec) * inv_det;
+    if (!(u >= R(0) && u <= R(1))) return false;
+    V3<R> qvec = cross(tvec, e1);
+    R v = dot(d, qvec) * inv_det;
+    if (v < R(0) || u + v > R(1)) return false;
+    t = dot(e2, qvec) * inv_det;
+    return tmin < t && t < tmax;
+}
+
+// QuadGeometry::hit_ray (geometry.rs:394-415); the degenerate-area test is folded into
+// the K_NEVER kind at upload.
+template <class R> GT_DEV bool quad_hit(V3<R> corner, V3<R> u, V3<R> v, V3<R> n, V3<R> w, R plane_d, V3<R> o,
+                                        V3<R> d, R tmin, R tmax, R& t) {
+    R denom = dot(n, d);
+    if (Num<R>::fabs(denom) < R(kQuadHitEps)) return false;
+    t = (plane_d - dot(n, o)) / denom;
+    if (!(tmin < t && t < tmax)) return false;
+    V3<R> planar = (o + d * t) - corner;
+    R a = dot(w, cross(planar, v));
+    R b = dot(w, cross(u, planar));
+    return (a >= R(0) && a <= R(1)) && (b >= R(0) && b <= R(1));
+}
+
+// RayGeometry::intersect for leaf-order primitive `i` (object.rs:338-346).
+template <class R> GT_DEV bool prim_hit(const SceneDev<R>& sc, uint32_t i, V3<R> o, V3<R> d, R time, R tmin, R tmax,
+                                        R& t) {
+    const uint32_t kind = __ldg(&sc.meta[i].x) & 7u;
+    const R* rec = sc.prims[i].v;
+    switch (kind) {
+    case K_SPHERE: {
+        R4<R> s = ldg4(rec);
+        return sphere_root(xyz(s), s.w, o, d, tmin, tmax, t);
+    }
+    case K_MOVING: {
+        R4<R> s = ldg4(rec), dl = ldg4(rec + 4);
+        V3<R> c = xyz(s) + xyz(dl) * time; // center_at, geometry.rs:510-513
+        return sphere_root(c, s.w, o, d, tmin, tmax, t);
+    }
+    case K_TRIANGLE: {
+        R4<R> a = ldg4(rec), b = ldg4(rec + 4), c = ldg4(rec + 8);
+        return tri_hit(xyz(a), xyz(b), xyz(c), o, d, tmin, tmax, t);
+    }
+    case K_QUAD: {
+        R4<R> a = ldg4(rec), b = ldg4(rec + 4), c = ldg4(rec + 8), e = ldg4(rec + 12);
+        return quad_hit(xyz(a), xyz(b), xyz(c), V3<R>{b.w, c.w, e.w}, xyz(e), a.w, o, d, tmin, tmax, t);
+    }
+    default:
+        return false;
+    }
+}
+
+struct TraceStats {
+    unsigned long long node_tests, node_hits, leaf_visits, candidates, leaf_hits;
+    uint32_t max_depth;
+};
+
+constexpr int kStackSize = 64;
+
+// FlatBvh::hit_with_stats (bvh.rs:306-399): root test, LIFO stack of (node, entry t),
+// skip entries at or beyond the closest hit, test both children of an internal node and
+// push the farther first.  ANY = stop at the first hit (occlusion).  Returns the leaf-
+// order primitive index of the closest hit or -1; sets *err on stack overflow.
+template <class R, bool STATS, bool ANY>
+GT_DEV int traverse(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, R tmax, R& t_out, TraceStats* st,
+                    uint32_t* err) {
+    RayT<R> rt = make_rayt(o, d);
+    if (STATS) st->node_tests += 1;
+    R root_entry;
+    if (!hit_box(rt, sc.root_box, sc.root_box + 3, tmin, tmax, root_entry)) return -1;
+    if (STATS) st->node_hits += 1;
+    int32_t s_link[kStackSize];
+    int32_t s_count[kStackSize];
+    R s_t[kStackSize];
+    int sp = 0;
+    s_link[0] = sc.root_link;
+    s_count[0] = sc.root_count;
+    s_t[0] = root_entry;
+    sp = 1;
+    if (STATS) st->max_depth = max(st->max_depth, 1u);
+    R closest = tmax;
+    int best = -1;
+    while (sp > 0) {
+        --sp;
+        const int32_t link = s_link[sp];
+        const int32_t count = s_count[sp];
+        const R et = s_t[sp];
+        if (et >= closest) continue;
+        if (link < 0) {
+            // hit_ray_scene_indices (scene.rs:849-874) with Interval(t_min, closest).
+            const uint32_t first = uint32_t(~link);
+            if (STATS) {
+                st->leaf_visits += 1;
+                st->candidates += uint32_t(count);
+            }
+            bool leaf_hit = false;
+            for (int k = 0; k < count; ++k) {
+                R t;
+                if (prim_hit(sc, first + k, o, d, time, tmin, closest, t)) {
+                    closest = t;
+                    best = int(first + k);
+                    leaf_hit = true;
+                    if (ANY) {
+                        t_out = closest;
+                        return best;
+                    }
+                }
+            }
+            if (STATS && leaf_hit) st->leaf_hits += 1;
+            continue;
+        }
+        const Node<R>& nd = sc.nodes[link];
+        R b[12];
+        if (sizeof(R) == 4) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                R4<R> v = ldg4(nd.box + 4 * q);
+                b[4 * q] = v.x;
+                b[4 * q + 1] = v.y;
+                b[4 * q + 2] = v.z;
+                b[4 * q + 3] = v.w;
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                R4<R> v = ldg4(nd.box + 4 * q);
+                b[4 * q] = v.x;
+                b[4 * q + 1] = v.y;
+                b[4 * q + 2] = v.z;
+                b[4 * q + 3] = v.w;
+            }
+        }
+        const int4 ln = __ldg(reinterpret_cast<const int4*>(nd.link));
+        R le, re;
+        const bool lh = hit_box(rt, b, b + 3, tmin, closest, le);
+        const bool rh = hit_box(rt, b + 6, b + 9, tmin, closest, re);
+        if (STATS) {
+            st->node_tests += 2;
+            st->node_hits += uint32_t(lh) + uint32_t(rh);
+        }
+        if (sp + 2 > kStackSize) {
+            atomicOr(err, E_STACK_OVERFLOW);
+            break;
+        }
+        if (lh && rh) {
+            if (re < le) {
+                s_link[sp] = ln.x, s_count[sp] = ln.y, s_t[sp] = le, ++sp;
+                s_link[sp] = ln.z, s_count[sp] = ln.w, s_t[sp] = re, ++sp;
+            } else {
+                s_link[sp] = ln.z, s_count[sp] = ln.w, s_t[sp] = re, ++sp;
+                s_link[sp] = ln.x, s_count[sp] = ln.y, s_t[sp] = le, ++sp;
+            }
+        } else if (lh) {
+            s_link[sp] = ln.x, s_count[sp] = ln.y, s_t[sp] = le, ++sp;
+        } else if (rh) {
+            s_link[sp] = ln.z, s_count[sp] = ln.w, s_t[sp] = re, ++sp;
+        }
+        if (STATS) st->max_depth = max(st->max_depth, uint32_t(sp));
+    }
+    t_out = closest;
+    return best;
+}
+
+// ------------------------------------------------------------------ hit record
+template <class R> struct HitRec {
+    V3<R> p, n; // n oriented against the ray (SurfaceHit::with_uv, object.rs:127-149)
+    bool front;
+    uint32_t mat;
+};
+template <class R> GT_DEV HitRec<R> make_hit(const SceneDev<R>& sc, uint32_t i, V3<R> o, V3<R> d, R time, R t) {
+    HitRec<R> h;
+    const uint32_t m = __ldg(&sc.meta[i].x);
+    const uint32_t kind = m & 7u;
+    h.mat = m >> 3;
+    h.p = o + d * t; // Ray::at
+    const R* rec = sc.prims[i].v;
+    V3<R> out;
+    if (kind == K_SPHERE || kind == K_MOVING) {
+        R4<R> s = ldg4(rec);
+        V3<R> c = xyz(s);
+        if (kind == K_MOVING) c = c + xyz(ldg4(rec + 4)) * time;
+        V3<R> diff = h.p - c; // outward_normal_at, geometry.rs:476-484
+        out = Num<R>::fabs(s.w) <= R(kEps) ? normalize(diff) : vdiv(diff, s.w);
+    } else if (kind == K_TRIANGLE) {
+        out = xyz(ldg4(rec + 12));
+    } else {
+        out = V3<R>{rec[7], rec[11], rec[15]};
+    }
+    h.front = dot(d, out) < R(0);
+    h.n = h.front ? out : -out;
+    return h;
+}
+
+// ------------------------------------------------------------------ materials
+template <class R> GT_DEV V3<R> mat_color(const MatDev<R>& m, V3<R> p) {
+    if (m.tex == 1) { // CheckerTexture::sample_linear (raytracing/texture.rs:97-108)
+        long long xi = (long long)Num<R>::floor(m.inv_scale * p.x);
+        long long yi = (long long)Num<R>::floor(m.inv_scale * p.y);
+        long long zi = (long long)Num<R>::floor(m.inv_scale * p.z);
+        return ((xi + yi + zi) % 2) == 0 ? load3(m.even) : load3(m.odd);
+    }
+    return load3(m.color);
+}
+
+enum : int { SC_NONE = 0, SC_SPECULAR = 1, SC_PDF = 2 };
+template <class R> struct ScatterRec {
+    int kind;
+    V3<R> dir; // specular direction
+    V3<R> att;
+    MatPdf<R> pdf;
+};
+
+template <class R> GT_DEV ScatterRec<R> mat_scatter(const MatDev<R>& m, V3<R> din, const HitRec<R>& h, Rng& g) {
+    ScatterRec<R> s;
+    s.kind = SC_NONE;
+    switch (m.kind) {
+    case 0: // Lambertian, material.rs:508-521
+        if (!onb_from_w(h.n, s.pdf.basis)) return s;
+        s.kind = SC_PDF;
+        s.pdf.kind = PDF_COSINE;
+        s.att = mat_color(m, h.p);
+        return s;
+    case 2: // Isotropic, material.rs:1124-1137
+        s.kind = SC_PDF;
+        s.pdf.kind = PDF_SPHERE;
+        s.att = mat_color(m, h.p);
+        return s;
+    case 3: { // GgxMicrofacet, material.rs:1583-1597; GgxReflectionPdf::new sampling.rs:146-170
+        V3<R> outgoing = -normalize(din);
+        if (!onb_from_w(h.n, s.pdf.basis)) return s;
+        s.pdf.out = normalize(outgoing);
+        if (len2(s.pdf.out) <= R(kEps) || dot(s.pdf.out, s.pdf.basis.w) <= R(0)) return s;
+        s.pdf.rough = clampr(m.param, R(0), R(1));
+        s.pdf.alpha = ggx_alpha(s.pdf.rough);
+        s.pdf.kind = PDF_GGX;
+        s.kind = SC_PDF;
+        s.att = mat_color(m, h.p);
+        return s;
+    }
+    case 4: { // Metal, material.rs:2087-2106
+        V3<R> refl = reflect(normalize(din), h.n);
+        V3<R> dir = refl + unit_vector_spherical<R>(g) * m.param;
+        if (dot(dir, h.n) <= R(0)) return s;
+        s.kind = SC_SPECULAR;
+        s.dir = dir;
+        s.att = load3(m.color);
+        return s;
+    }
+    case 5: { // Dielectric, material.rs:2321-2351
+        R ratio = h.front ? R(1) / m.param : m.param;
+        V3<R> unit = normalize(din);
+        R ct = Num<R>::fmin(dot(-unit, h.n), R(1));
+        R st = Num<R>::sqrt(R(1) - ct * ct);
+        bool refl = ratio * st > R(1);
+        if (!refl) {
+            R r0 = (R(1) - ratio) / (R(1) + ratio); // Dielectric::reflectance, material.rs:2213-2219
+            r0 = r0 * r0;
+            R rf = r0 + (R(1) - r0) * pow5(R(1) - ct);
+            refl = rf > rnd<R>(g);
+        }
+        s.dir = refl ? reflect(unit, h.n) : refract(unit, h.n, ratio);
+        s.kind = SC_SPECULAR;
+        s.att = V3<R>{1, 1, 1};
+        return s;
+    }
+    default: // DiffuseLight: no scatter
+        return s;
+    }
+}
+
+template <class R> GT_DEV R mat_scattering_pdf(const MatDev<R>& m, V3<R> din, const HitRec<R>& h, V3<R> dout) {
+    switch (m.kind) {
+    case 0: { // material.rs:523-530
+        R c = dot(h.n, normalize(dout));
+        return c <= R(0) ? R(0) : c / R(kPi);
+    }
+    case 2:
+        return R(1) / (R(4) * R(kPi));
+    case 3: { // material.rs:1599-1617 and ggx_reflection_scattering_weight 1717-1758
+        V3<R> outgoing = -normalize(din);
+        V3<R> incoming = normalize(dout);
+        if (dot(incoming, h.n) <= R(0) || dot(outgoing, h.n) <= R(0)) return R(0);
+        V3<R> sc = mat_color(m, h.p); // specular_luminance, material.rs:1760-1762
+        R f0 = clampr(R(0.2126) * sc.x + R(0.7152) * sc.y + R(0.0722) * sc.z, R(0), R(1));
+        V3<R> n = normalize(h.n), o = normalize(outgoing), i = normalize(incoming);
+        R ndi = dot(n, i), ndo = dot(n, o);
+        if (ndi <= R(0) || ndo <= R(0)) return R(0);
+        V3<R> half = normalize(i + o);
+        if (len2(half) <= R(kEps)) return R(0);
+        R ndh = dot(n, half), odh = dot(o, half);
+        if (ndh <= R(0) || odh <= R(0)) return R(0);
+        R D = ggx_D(ndh, m.param);
+        R G = smith_G1(ndi, m.param) * smith_G1(ndo, m.param);
+        f0 = clampr(f0, R(0), R(1));
+        if (f0 <= R(kEps)) return R(0);
+        R F = schlick_f(odh, f0) / f0;
+        return D * G * F / (R(4) * ndo);
+    }
+    default:
+        return R(0);
+    }
+}
+
+template <class R> GT_DEV V3<R> mat_emitted(const MatDev<R>& m, const HitRec<R>& h) {
+    if (m.kind == 1 && h.front) return mat_color(m, h.p); // material.rs:1008-1022
+    return V3<R>{0, 0, 0};
+}
+
+template <class R> GT_DEV V3<R> mat_albedo(const MatDev<R>& m, const HitRec<R>& h) { // denoise_albedo
+    if (m.kind == 4) return load3(m.color);
+    if (m.kind == 5) return V3<R>{1, 1, 1};
+    return mat_color(m, h.p);
+}
+
+// ------------------------------------------------------------- light targets
+template <class R> GT_DEV R area_pdf(V3<R> dir, R t, V3<R> n, R area) { // object.rs:1100-1111
+    if (area <= R(kEps)) return R(0);
+    R d2 = len2(dir * t);
+    R cosine = Num<R>::fabs(dot(normalize(dir), n));
+    if (cosine <= R(kEps)) return R(0);
+    return d2 / (cosine * area);
+}
+
+template <class R> GT_DEV R light_pdf_one(const LightDev<R>& L, V3<R> origin, R time, V3<R> dir) {
+    const R inf = Num<R>::inf();
+    switch (L.kind) {
+    case K_SPHERE:
+    case K_MOVING: { // sphere_pdf_value, object.rs:1044-1070
+        V3<R> c = load3(L.a);
+        if (L.kind == K_MOVING) c = c + load3(L.b) * time;
+        R root;
+        if (!sphere_root(c, L.radius, origin, dir, R(kShadowAcnePdf), inf, root)) return R(0);
+        V3<R> cd = c - origin;
+        R d2 = len2(cd);
+        R r2 = L.radius * L.radius;
+        if (d2 <= r2) return R(1) / (R(4) * R(kPi));
+        R cmax = Num<R>::sqrt(R(1) - r2 / d2);
+        R solid = R(2) * R(kPi) * (R(1) - cmax);
+        return solid <= R(kEps) ? R(0) : R(1) / solid;
+    }
+    case K_QUAD: { // quad_pdf_value, object.rs:1072-1084
+        if (L.area_sq <= R(kEps)) return R(0);
+        R t;
+        if (!quad_hit(load3(L.a), load3(L.b), load3(L.c), load3(L.n), load3(L.w), L.plane_d, origin, dir,
+                      R(kShadowAcnePdf), inf, t))
+            return R(0);
+        return area_pdf(dir, t, load3(L.n), L.area);
+    }
+    case K_TRIANGLE: { // triangle_pdf_value, object.rs:1086-1098
+        V3<R> p0 = load3(L.a);
+        R t;
+        if (!tri_hit(p0, load3(L.b) - p0, load3(L.c) - p0, origin, dir, R(kShadowAcnePdf), inf, t)) return R(0);
+        return area_pdf(dir, t, load3(L.n), L.area);
+    }
+    }
+    return R(0);
+}
+
+template <class R> GT_DEV V3<R> light_dir_one(const LightDev<R>& L, V3<R> origin, R time, Rng& g) {
+    switch (L.kind) {
+    case K_SPHERE:
+    case K_MOVING: { // random_direction_to_sphere, object.rs:1113-1128
+        V3<R> c = load3(L.a);
+        if (L.kind == K_MOVING) c = c + load3(L.b) * time;
+        V3<R> dir = c - origin;
+        R d2 = len2(dir);
+        R r2 = L.radius * L.radius;
+        if (d2 <= r2 || d2 <= R(kEps)) return unit_vector_spherical<R>(g);
+        R r1 = rnd<R>(g); // random_to_sphere, object.rs:1153-1161
+        R rr2 = rnd<R>(g);
+        R z = R(1) + rr2 * (Num<R>::sqrt(R(1) - L.radius * L.radius / d2) - R(1));
+        R phi = R(2) * R(kPi) * r1;
+        R rz = Num<R>::sqrt(R(1) - z * z);
+        R s, cc;
+        Num<R>::sincos(phi, &s, &cc);
+        V3<R> local{cc * rz, s * rz, z};
+        Onb<R> b;
+        if (!onb_from_w(dir, b)) return local;
+        return onb_local(b, local);
+    }
+    case K_QUAD: { // object.rs:1130-1134
+        R r1 = rnd<R>(g);
+        V3<R> p = load3(L.a) + load3(L.b) * r1;
+        R r2 = rnd<R>(g);
+        p = p + load3(L.c) * r2;
+        return p - origin;
+    }
+    case K_TRIANGLE: { // object.rs:1136-1151
+        R a = rnd<R>(g);
+        R b = rnd<R>(g);
+        if (a + b > R(1)) {
+            a = R(1) - a;
+            b = R(1) - b;
+        }
+        V3<R> p0 = load3(L.a);
+        V3<R> p = (p0 + (load3(L.b) - p0) * a) + (load3(L.c) - p0) * b;
+        return p - origin;
+    }
+    }
+    return V3<R>{1, 0, 0};
+}
+
+// WeightedSamplingTargetList::pdf_value / random_direction (scene.rs:479-497).
+template <class R> GT_DEV R lights_pdf(const LightsDev<R>& L, V3<R> origin, R time, V3<R> dir) {
+    if (L.count == 0 || L.total <= R(0)) return R(0);
+    R sum = R(-0.0);
+    for (uint32_t i = 0; i < L.count; ++i) sum = sum + (L.t[i].weight / L.total) * light_pdf_one(L.t[i], origin, time, dir);
+    return sum;
+}
+template <class R> GT_DEV V3<R> lights_dir(const LightsDev<R>& L, V3<R> origin, R time, Rng& g) {
+    if (L.count == 0 || L.total <= R(0)) return V3<R>{1, 0, 0};
+    R pick = rnd_range<R>(g, R(0), L.total);
+    for (uint32_t i = 0; i < L.count; ++i) {
+        pick -= L.t[i].weight;
+        if (pick <= R(0)) return light_dir_one(L.t[i], origin, time, g);
+    }
+    return light_dir_one(L.t[L.count - 1], origin, time, g);
+}
+
+// --------------------------------------------------------------- environment
+template <class R> GT_DEV R env_pdf(const EnvDev<R>& E, V3<R> dir) { // environment.rs:133-153
+    if (E.total <= R(kEps) || E.width == 0) return R(1) / R(4.0 * kPi);
+    V3<R> d = normalize(dir);
+    R theta = Num<R>::acos(clampr(d.y, R(-1), R(1)));
+    R phi = rem_euclid(Num<R>::atan2(d.z, d.x), R(kTau));
+    R fx = Num<R>::floor((phi / R(kTau)) * R(E.width));
+    R fy = Num<R>::floor((theta / R(kPi)) * R(E.height));
+    uint32_t x = fx > R(0) ? (uint32_t)fx : 0u;
+    uint32_t y = fy > R(0) ? (uint32_t)fy : 0u;
+    x = min(x, E.width - 1);
+    y = min(y, E.height - 1);
+    R prob = E.weights[size_t(y) * E.width + x] / E.total;
+    R t0 = R(kPi) * (R(y) / R(E.height));
+    R t1 = R(kPi) * (R(y + 1) / R(E.height));
+    R s0, c0, s1, c1;
+    Num<R>::sincos(t0, &s0, &c0);
+    Num<R>::sincos(t1, &s1, &c1);
+    R sa = (R(kTau) / R(E.width)) * Num<R>::fmax(c0 - c1, R(0));
+    return sa <= R(kEps) ? R(0) : prob / sa;
+}
+
+template <class R> GT_DEV void env_sample(const EnvDev<R>& E, Rng& g, V3<R>& dir, R& pdf) { // environment.rs:107-131
+    if (E.total <= R(kEps) || E.width == 0) {
+        dir = unit_vector_spherical<R>(g);
+        pdf = R(1) / R(4.0 * kPi);
+        return;
+    }
+    R target = rnd<R>(g) * E.total;
+    // partition_point(cdf < target): first index whose running sum is >= target.
+    uint32_t lo = 0, hi = E.width * E.height;
+    while (lo < hi) {
+        uint32_t mid = lo + (hi - lo) / 2;
+        if (E.cdf[mid] < target) lo = mid + 1;
+        else hi = mid;
+    }
+    uint32_t idx = min(lo, E.width * E.height - 1);
+    uint32_t x = idx % E.width, y = idx / E.width;
+    R u = (R(x) + rnd<R>(g)) / R(E.width);
+    R t0 = R(kPi) * (R(y) / R(E.height));
+    R t1 = R(kPi) * (R(y + 1) / R(E.height));
+    R s0, c0, s1, c1;
+    Num<R>::sincos(t0, &s0, &c0);
+    Num<R>::sincos(t1, &s1, &c1);
+    R ct = c0 + rnd<R>(g) * (c1 - c0);
+    R st = Num<R>::sqrt(Num<R>::fmax(R(1) - ct * ct, R(0)));
+    R phi = R(kTau) * u;
+    R sp, cp;
+    Num<R>::sincos(phi, &sp, &cp);
+    dir = V3<R>{st * cp, ct, st * sp};
+    pdf = env_pdf(E, dir);
+}
+
+template <class R> GT_DEV uint8_t lerp_u8(uint8_t a, uint8_t b, R t) { // Rgb::lerp, colors.rs:525-537
+    t = clampr(t, R(0), R(1));
+    R v = Num<R>::round(R(a) + R(int(b) - int(a)) * t);
+    if (!(v > R(0))) return 0;
+    if (v >= R(255)) return 255;
+    return (uint8_t)v;
+}
+
+// EnvironmentLight::radiance (environment.rs:98-105) through the bilinear texture
+// sampler (graphics/texture.rs:657-711): Repeat in u, Clamp in v.
+template <class R> GT_DEV V3<R> env_radiance(const EnvDev<R>& E, V3<R> dir) {
+    V3<R> d = normalize(dir);
+    R phi = rem_euclid(Num<R>::atan2(d.z, d.x), R(kTau));
+    R theta = Num<R>::acos(clampr(d.y, R(-1), R(1)));
+    R s = phi / R(kTau), t = R(1) - theta / R(kPi);
+    if (E.width == 0 || !Num<R>::finite(s) || !Num<R>::finite(t)) return V3<R>{0, 0, 0};
+    R xc = rem_euclid(s, R(1)) * R(E.width);
+    R fx = Num<R>::floor(xc);
+    uint32_t x0 = min(fx > R(0) ? (uint32_t)fx : 0u, E.width - 1);
+    uint32_t x1 = x0 + 1 == E.width ? 0 : x0 + 1;
+    R yc = clampr(R(1) - t, R(0), R(1)) * R(E.height - 1);
+    R fy = Num<R>::floor(yc);
+    uint32_t y0 = fy > R(0) ? (uint32_t)fy : 0u;
+    uint32_t y1 = min(y0 + 1, E.height - 1);
+    R tx = xc - R(x0), ty = yc - R(y0);
+    size_t i00 = (size_t(y0) * E.width + x0) * 3, i10 = (size_t(y0) * E.width + x1) * 3;
+    size_t i01 = (size_t(y1) * E.width + x0) * 3, i11 = (size_t(y1) * E.width + x1) * 3;
+    R out[3];
+    if (E.format == 0) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            uint8_t top = lerp_u8<R>(E.px8[i00 + c], E.px8[i10 + c], tx);
+            uint8_t bot = lerp_u8<R>(E.px8[i01 + c], E.px8[i11 + c], tx);
+            R v = R(lerp_u8<R>(top, bot, ty)) / R(255);
+            out[c] = v * v; // gamma-2 decode, colors.rs:78-84
+        }
+    } else {
+        R ctx = clampr(tx, R(0), R(1)), cty = clampr(ty, R(0), R(1));
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            R p00 = R(E.px32[i00 + c]), p10 = R(E.px32[i10 + c]);
+            R p01 = R(E.px32[i01 + c]), p11 = R(E.px32[i11 + c]);
+            R top = p00 + (p10 - p00) * ctx;
+            R bot = p01 + (p11 - p01) * ctx;
+            out[c] = top + (bot - top) * cty;
+        }
+    }
+    return V3<R>{out[0], out[1], out[2]};
+}
+
+// ----------------------------------------------------------------- background
+template <class R> GT_DEV V3<R> background(const CamDev<R>& c, V3<R> dir) { // camera.rs:301-322
+    if (c.bg_kind == 0) return load3(c.bg);
+    V3<R> nadir = load3(c.bg), hor = load3(c.bg + 3), zen = load3(c.bg + 6);
+    R t = R(0.5) * (normalize(dir).y + R(1));
+    if (t < R(0.5)) {
+        R b = R(2) * t;
+        return nadir * (R(1) - b) + hor * b;
+    }
+    R b = R(2) * (t - R(0.5));
+    return hor * (R(1) - b) + zen * b;
+}
+
+// -------------------------------------------------------------------- camera
+// ray_for_pixel_sample / ray_for_pixel_stratified_sample (camera.rs:1658-1704); returns
+// origin and direction, draws the time.
+template <class R> GT_DEV void camera_ray(const CamDev<R>& c, uint32_t x, uint32_t y, uint32_t sample, Rng& g,
+                                          V3<R>& o, V3<R>& d, R& time) {
+    R ox, oy;
+    if (c.mode == 0) {
+        ox = rnd<R>(g) - R(0.5);
+        oy = rnd<R>(g) - R(0.5);
+    } else {
+        uint32_t sx = sample % c.grid, sy = sample / c.grid;
+        R rec = R(1) / R(c.grid);
+        ox = ((R(sx) + rnd<R>(g)) * rec) - R(0.5);
+        oy = ((R(sy) + rnd<R>(g)) * rec) - R(0.5);
+    }
+    V3<R> ps = (load3(c.pixel00) + load3(c.du) * (R(x) + ox)) + load3(c.dv) * (R(y) + oy);
+    V3<R> org = load3(c.center);
+    if (c.defocus) { // defocus_disk_sample + random_in_unit_disk (camera.rs:1710-1713, random.rs:141-152)
+        // Rejection sampling; each try is accepted with probability pi/4, so the cap of
+        // 4096 tries (reached with probability ~1e-2700) only bounds the loop.
+        V3<R> p{0, 0, 0};
+        for (int tries = 0; tries < 4096; ++tries) {
+            R a = rnd_range<R>(g, R(-1), R(1));
+            R b = rnd_range<R>(g, R(-1), R(1));
+            p = V3<R>{a, b, R(0)};
+            if (len2(p) < R(1)) break;
+        }
+        org = (org + load3(c.ddu) * p.x) + load3(c.ddv) * p.y;
+    }
+    time = rnd_range<R>(g, c.shutter0, c.shutter1);
+    o = org;
+    d = ps - org;
+}
+
+} // namespace gt

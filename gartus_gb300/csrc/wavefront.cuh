@@ -1,0 +1,477 @@
+// wavefront.cuh — the wavefront integrator.  One path slot per pixel carries that pixel's
+// sequential SplitMix64 stream from sample to sample (camera.rs:2669, 2685-2717).  Each
+// iteration runs four kernels over compacted queues:
+//   generate : finish the slot's previous sample (accumulate), start the next camera ray
+//   trace    : closest hit for every queued ray, then bin the slot by material kind
+//   shade    : one bounce of RayCamera::ray_color (camera.rs:1730-1862) per slot, with
+//              warps reading one material's queue at a time
+//   shadow   : the deferred next-event shadow queries of this bounce
+// Queues are filled with warp-aggregated atomics (ballot / match_any + popc).
+#pragma once
+
+#include "scene_query.cuh"
+
+namespace gt {
+
+template <class R> struct Params {
+    SceneDev<R> sc;
+    LightsDev<R> lights;
+    EnvDev<R> env;
+    CamDev<R> cam;
+    PathState<R> ps;
+};
+
+GT_DEV uint32_t lane_id() { return threadIdx.x & 31u; }
+GT_DEV uint32_t lanemask_lt() { return (1u << lane_id()) - 1u; }
+
+// All 32 lanes call; lanes with `want` append `value` to `queue`.
+GT_DEV void warp_push(bool want, uint32_t value, uint32_t* queue, uint32_t* counter) {
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    if (m == 0) return;
+    const uint32_t leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane_id() == leader) base = atomicAdd(counter, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (want) queue[base + __popc(m & lanemask_lt())] = value;
+}
+
+// All 32 lanes call; lanes with `want` append `value` to queue `key` (capacity `cap`).
+GT_DEV void warp_push_keyed(bool want, uint32_t key, uint32_t value, uint32_t* queues, uint32_t cap,
+                            uint32_t* counters) {
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    if (!want) return;
+    const unsigned peers = __match_any_sync(m, key);
+    const uint32_t leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (lane_id() == leader) base = atomicAdd(&counters[key], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    queues[size_t(key) * cap + base + __popc(peers & lanemask_lt())] = value;
+}
+
+template <class R> GT_DEV void kahan_add(R4<R>& sum, R4<R>& c, V3<R> s);
+// f32: Kahan-compensated running sum.
+template <> GT_DEV void kahan_add<float>(R4<float>& sum, R4<float>& c, V3<float> s) {
+    float in[3] = {s.x, s.y, s.z};
+    float* sp[3] = {&sum.x, &sum.y, &sum.z};
+    float* cp[3] = {&c.x, &c.y, &c.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float y = in[k] - *cp[k];
+        float t = *sp[k] + y;
+        *cp[k] = (t - *sp[k]) - y;
+        *sp[k] = t;
+    }
+}
+// f64: the reference's plain `pixel_color += sample` (camera.rs:2984-2991).
+template <> GT_DEV void kahan_add<double>(R4<double>& sum, R4<double>& c, V3<double> s) {
+    (void)c;
+    sum.x = sum.x + s.x;
+    sum.y = sum.y + s.y;
+    sum.z = sum.z + s.z;
+}
+
+template <class R> GT_DEV R adaptive_error(V3<R> m2, uint32_t n) { // camera.rs:2962-2972
+    if (n <= 1) return Num<R>::inf();
+    V3<R> var = cdiv(m2, R(n - 1));
+    return Num<R>::sqrt(Num<R>::fmax(maxc(cdiv(var, R(n))), R(0)));
+}
+
+template <class R> __global__ void k_init(Params<R> P) {
+    const uint32_t n = P.ps.n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t x = i % P.cam.width, y = i / P.cam.width;
+        const uint64_t s = pixel_seed(P.cam.seed, x, y);
+        P.ps.st[i] = make_uint4(uint32_t(s), uint32_t(s >> 32), F_NEWSAMPLE, 0u);
+        P.ps.acc[i] = R4<R>{0, 0, 0, 0};
+        P.ps.comp[i] = R4<R>{0, 0, 0, 0};
+        P.ps.accepted[i] = 0;
+    }
+    if (blockIdx.x == 0 && threadIdx.x < C_COUNT) P.ps.counters[threadIdx.x] = 0;
+    if (blockIdx.x == 0 && threadIdx.x < 4) P.ps.totals[threadIdx.x] = 0;
+}
+
+// Folds a finished sample into the pixel; returns true when adaptive sampling stops.
+template <class R> GT_DEV bool finish_sample(const Params<R>& P, uint32_t slot, V3<R> s) {
+    if (!finite3(s)) return false; // non-finite samples are dropped (camera.rs:2984-2999, 2951-2953)
+    R4<R> a = P.ps.acc[slot], c = P.ps.comp[slot];
+    uint32_t acc_n = P.ps.accepted[slot] + 1;
+    bool stop = false;
+    if (P.cam.adaptive) { // Welford update, camera.rs:2955-2960
+        V3<R> mean = xyz(a), m2 = xyz(c);
+        V3<R> delta = s - mean;
+        mean = mean + cdiv(delta, R(acc_n));
+        V3<R> delta2 = s - mean;
+        m2 = m2 + cmul(delta, delta2);
+        a = R4<R>{mean.x, mean.y, mean.z, R(0)};
+        c = R4<R>{m2.x, m2.y, m2.z, R(0)};
+        stop = acc_n >= P.cam.adaptive_min && adaptive_error(m2, acc_n) < P.cam.adaptive_threshold;
+    } else {
+        kahan_add(a, c, s);
+    }
+    P.ps.acc[slot] = a;
+    P.ps.comp[slot] = c;
+    P.ps.accepted[slot] = acc_n;
+    return stop;
+}
+
+template <class R> __global__ void __launch_bounds__(256) k_generate(Params<R> P, uint32_t cur) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        P.ps.counters[C_TRACE0 + (cur ^ 1u)] = 0;
+        for (uint32_t k = 0; k < NUM_KEYS; ++k) P.ps.counters[C_MAT + k] = 0;
+        P.ps.counters[C_SHADOW] = 0;
+    }
+    const uint32_t n = P.ps.n;
+    const uint32_t limit = P.cam.adaptive ? P.cam.adaptive_max : P.cam.spp;
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = warp0; base < n; base += stride) {
+        const uint32_t slot = base + lane_id();
+        bool push = false;
+        if (slot < n) {
+            uint4 st = P.ps.st[slot];
+            if (st.z & F_NEWSAMPLE) {
+                Rng g{uint64_t(st.x) | (uint64_t(st.y) << 32)};
+                uint32_t started = st.w;
+                bool stop = false;
+                if (started > 0) stop = finish_sample(P, slot, xyz(P.ps.col[slot]));
+                const uint32_t x = slot % P.cam.width, y = slot / P.cam.width;
+                uint32_t flags = F_DONE;
+                while (!stop && started < limit) {
+                    V3<R> o, d;
+                    R time;
+                    camera_ray(P.cam, x, y, started, g, o, d, time);
+                    ++started;
+                    if (P.cam.max_depth == 0) { // the bounce loop never runs: a black sample
+                        stop = finish_sample(P, slot, V3<R>{0, 0, 0});
+                        continue;
+                    }
+                    P.ps.ray_o[slot] = R4<R>{o.x, o.y, o.z, time};
+                    P.ps.ray_d[slot] = R4<R>{d.x, d.y, d.z, R(1)};
+                    P.ps.att[slot] = R4<R>{1, 1, 1, 0};
+                    P.ps.col[slot] = R4<R>{0, 0, 0, 0};
+                    flags = F_TRACE | F_ALLOW_EMIT;
+                    push = true;
+                    break;
+                }
+                if (!push) atomicAdd(&P.ps.counters[C_DONE], 1u);
+                P.ps.st[slot] = make_uint4(uint32_t(g.s), uint32_t(g.s >> 32), flags, started);
+            }
+        }
+        warp_push(push, slot, P.ps.q_trace[cur], &P.ps.counters[C_TRACE0 + cur]);
+    }
+}
+
+template <class R> __global__ void __launch_bounds__(256) k_trace(Params<R> P, uint32_t cur) {
+    const uint32_t count = *reinterpret_cast<volatile uint32_t*>(&P.ps.counters[C_TRACE0 + cur]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) P.ps.totals[0] += count;
+    const uint32_t* q = P.ps.q_trace[cur];
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const R inf = Num<R>::inf();
+    for (uint32_t base = warp0; base < count; base += stride) {
+        const uint32_t i = base + lane_id();
+        const bool valid = i < count;
+        uint32_t slot = 0, key = 0;
+        if (valid) {
+            slot = q[i];
+            R4<R> o = P.ps.ray_o[slot], d = P.ps.ray_d[slot];
+            R t = R(0);
+            int prim = traverse<R, false, false>(P.sc, xyz(o), xyz(d), o.w, R(kShadowAcne), inf, t, nullptr,
+                                                 &P.ps.counters[C_ERROR]);
+            P.ps.hit_t[slot] = t;
+            P.ps.hit_prim[slot] = prim;
+            key = prim < 0 ? KEY_MISS : uint32_t(P.sc.mats[__ldg(&P.sc.meta[prim].x) >> 3].kind);
+        }
+        warp_push_keyed(valid, key, slot, P.ps.q_mat, P.ps.n, &P.ps.counters[C_MAT]);
+    }
+}
+
+template <class R> GT_DEV bool rr_survives(const CamDev<R>& cam, uint32_t bounce, V3<R>& att, Rng& g) {
+    if (cam.rr_min_depth < 0 || bounce < uint32_t(cam.rr_min_depth)) return true; // camera.rs:2498-2523
+    R m = maxc(att);
+    if (!Num<R>::finite(m) || m <= R(kEps)) return false;
+    R p = clampr(m, R(0.05), R(0.95));
+    if (rnd<R>(g) >= p) return false;
+    att = cdiv(att, p);
+    return true;
+}
+
+// One bounce of ray_color for `slot`.  Returns true if the path continues.
+template <class R> GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uint32_t key, bool& shadow) {
+    uint4 st = P.ps.st[slot];
+    Rng g{uint64_t(st.x) | (uint64_t(st.y) << 32)};
+    uint32_t flags = st.z;
+    const uint32_t bounce = flags & F_BOUNCE_MASK;
+    R4<R> ro = P.ps.ray_o[slot], rd = P.ps.ray_d[slot];
+    V3<R> o = xyz(ro), d = xyz(rd);
+    const R time = ro.w;
+    R miss_w = rd.w;
+    V3<R> att = xyz(P.ps.att[slot]);
+    V3<R> col = xyz(P.ps.col[slot]);
+    bool cont = false;
+    shadow = false;
+    uint32_t sh_bits = 0;
+
+    if (key == KEY_MISS) {
+        V3<R> bg = P.cam.use_env ? env_radiance(P.env, d) : background(P.cam, d);
+        V3<R> miss = bg * miss_w;
+        col = col + cmul(att, miss);
+    } else {
+        const uint32_t prim = uint32_t(P.ps.hit_prim[slot]);
+        const HitRec<R> h = make_hit(P.sc, prim, o, d, time, P.ps.hit_t[slot]);
+        const MatDev<R> m = P.sc.mats[h.mat];
+        if (flags & F_ALLOW_EMIT) col = col + cmul(att, mat_emitted(m, h));
+        ScatterRec<R> s = mat_scatter(m, d, h, g);
+        if (s.kind == SC_SPECULAR) {
+            att = cmul(att, s.att);
+            o = h.p;
+            d = s.dir;
+            flags |= F_ALLOW_EMIT;
+            miss_w = R(1);
+            cont = rr_survives(P.cam, bounce, att, g);
+        } else if (s.kind == SC_PDF) {
+            if (P.cam.nee) {
+                if (P.cam.use_lights) { // estimate_direct_lighting, camera.rs:2225-2262
+                    V3<R> ldir = lights_dir(P.lights, h.p, time, g);
+                    R lp = lights_pdf(P.lights, h.p, time, ldir);
+                    if (Num<R>::finite(lp) && lp > R(kEps)) {
+                        R sp = mat_scattering_pdf(m, d, h, ldir);
+                        if (Num<R>::finite(sp) && sp > R(0)) {
+                            const size_t k = size_t(slot) * 2;
+                            P.ps.sh_o[k] = R4<R>{h.p.x, h.p.y, h.p.z, time};
+                            P.ps.sh_d[k] = R4<R>{ldir.x, ldir.y, ldir.z, R(1)};
+                            P.ps.sh_a[k] = R4<R>{att.x, att.y, att.z, sp / lp};
+                            P.ps.sh_s[k] = R4<R>{s.att.x, s.att.y, s.att.z, R(0)};
+                            sh_bits |= F_SHADOW0;
+                        }
+                    }
+                }
+                if (P.cam.use_env) { // estimate_environment_lighting, camera.rs:2264-2297
+                    V3<R> edir;
+                    R ep;
+                    env_sample(P.env, g, edir, ep);
+                    if (Num<R>::finite(ep) && ep > R(kEps)) {
+                        R sp = mat_scattering_pdf(m, d, h, edir);
+                        if (Num<R>::finite(sp) && sp > R(0)) {
+                            R mis = power_heuristic(ep, sp);
+                            V3<R> sr = cmul(s.att, env_radiance(P.env, edir));
+                            const size_t k = size_t(slot) * 2 + 1;
+                            P.ps.sh_o[k] = R4<R>{h.p.x, h.p.y, h.p.z, time};
+                            P.ps.sh_d[k] = R4<R>{edir.x, edir.y, edir.z, R(2)};
+                            P.ps.sh_a[k] = R4<R>{att.x, att.y, att.z, mis * sp / ep};
+                            P.ps.sh_s[k] = R4<R>{sr.x, sr.y, sr.z, R(0)};
+                            sh_bits |= F_SHADOW1;
+                        }
+                    }
+                }
+            }
+            // SamplingStrategy::continuation_sample (camera.rs:165-195)
+            V3<R> dir;
+            R pdf;
+            bool suppress = false, weight_env = false;
+            if (!P.cam.nee && P.cam.use_lights) {
+                const R w = P.cam.light_pdf_weight;
+                if (rnd<R>(g) < w) dir = lights_dir(P.lights, h.p, time, g);
+                else dir = matpdf_generate(s.pdf, g);
+                pdf = w * lights_pdf(P.lights, h.p, time, dir) + (R(1) - w) * matpdf_value(s.pdf, dir);
+            } else {
+                dir = matpdf_generate(s.pdf, g);
+                pdf = matpdf_value(s.pdf, dir);
+                suppress = P.cam.nee && P.cam.use_lights;
+                weight_env = P.cam.nee && P.cam.use_env;
+            }
+            if (Num<R>::finite(pdf) && pdf > R(kEps)) {
+                R sp = mat_scattering_pdf(m, d, h, dir);
+                if (Num<R>::finite(sp) && sp > R(0)) {
+                    R next_w = R(1);
+                    if (weight_env) next_w = power_heuristic(pdf, env_pdf(P.env, dir));
+                    att = cmul(att, s.att * (sp / pdf));
+                    o = h.p;
+                    d = dir;
+                    if (suppress) flags &= ~F_ALLOW_EMIT;
+                    else flags |= F_ALLOW_EMIT;
+                    miss_w = next_w;
+                    cont = rr_survives(P.cam, bounce, att, g);
+                }
+            }
+        }
+    }
+    if (cont && bounce + 1 >= P.cam.max_depth) cont = false; // the bounce loop is exhausted
+    flags &= ~(F_BOUNCE_MASK | F_TRACE | F_SHADOW0 | F_SHADOW1);
+    flags |= sh_bits;
+    if (cont) {
+        flags |= F_TRACE | ((bounce + 1) & F_BOUNCE_MASK);
+        P.ps.ray_o[slot] = R4<R>{o.x, o.y, o.z, time};
+        P.ps.ray_d[slot] = R4<R>{d.x, d.y, d.z, miss_w};
+        P.ps.att[slot] = R4<R>{att.x, att.y, att.z, R(0)};
+    } else {
+        flags |= F_NEWSAMPLE;
+    }
+    P.ps.col[slot] = R4<R>{col.x, col.y, col.z, R(0)};
+    P.ps.st[slot] = make_uint4(uint32_t(g.s), uint32_t(g.s >> 32), flags, st.w);
+    shadow = sh_bits != 0;
+    return cont;
+}
+
+template <class R> __global__ void __launch_bounds__(256) k_shade(Params<R> P, uint32_t cur) {
+    uint32_t prefix[NUM_KEYS + 1];
+    prefix[0] = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < NUM_KEYS; ++k)
+        prefix[k + 1] = prefix[k] + *reinterpret_cast<volatile uint32_t*>(&P.ps.counters[C_MAT + k]);
+    const uint32_t total = prefix[NUM_KEYS];
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = warp0; base < total; base += stride) {
+        const uint32_t i = base + lane_id();
+        bool cont = false, shadow = false;
+        uint32_t slot = 0;
+        if (i < total) {
+            uint32_t key = 0;
+#pragma unroll
+            for (uint32_t k = 1; k < NUM_KEYS; ++k)
+                if (i >= prefix[k]) key = k;
+            slot = P.ps.q_mat[size_t(key) * P.ps.n + (i - prefix[key])];
+            cont = shade_slot(P, slot, key, shadow);
+        }
+        warp_push(cont, slot, P.ps.q_trace[cur ^ 1u], &P.ps.counters[C_TRACE0 + (cur ^ 1u)]);
+        warp_push(shadow, slot, P.ps.q_shadow, &P.ps.counters[C_SHADOW]);
+    }
+}
+
+template <class R> __global__ void __launch_bounds__(256) k_shadow(Params<R> P) {
+    const uint32_t count = *reinterpret_cast<volatile uint32_t*>(&P.ps.counters[C_SHADOW]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) P.ps.totals[1] += count;
+    const R inf = Num<R>::inf();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t slot = P.ps.q_shadow[i];
+        uint4 st = P.ps.st[slot];
+        V3<R> col = xyz(P.ps.col[slot]);
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            if (!(st.z & (k == 0 ? F_SHADOW0 : F_SHADOW1))) continue;
+            const size_t j = size_t(slot) * 2 + k;
+            R4<R> so = P.ps.sh_o[j], sd = P.ps.sh_d[j], sa = P.ps.sh_a[j], ss = P.ps.sh_s[j];
+            V3<R> o = xyz(so), d = xyz(sd);
+            R t;
+            if (k == 0) { // closest hit; the emission of whatever is hit (camera.rs:2248-2261)
+                int prim = traverse<R, false, false>(P.sc, o, d, so.w, R(kShadowAcne), inf, t, nullptr,
+                                                     &P.ps.counters[C_ERROR]);
+                if (prim < 0) continue;
+                HitRec<R> h = make_hit(P.sc, uint32_t(prim), o, d, so.w, t);
+                V3<R> e = mat_emitted(P.sc.mats[h.mat], h);
+                if (!finite3(e)) continue;
+                V3<R> direct = cmul(xyz(ss), e) * sa.w;
+                col = col + cmul(xyz(sa), direct);
+            } else { // occlusion only (camera.rs:2284-2293)
+                int prim = traverse<R, false, true>(P.sc, o, d, so.w, R(kShadowAcne), inf, t, nullptr,
+                                                    &P.ps.counters[C_ERROR]);
+                if (prim >= 0) continue;
+                V3<R> direct = xyz(ss) * sa.w;
+                col = col + cmul(xyz(sa), direct);
+            }
+        }
+        P.ps.col[slot] = R4<R>{col.x, col.y, col.z, R(0)};
+        P.ps.st[slot].z = st.z & ~(F_SHADOW0 | F_SHADOW1);
+    }
+}
+
+// Pixel estimate: sum / accepted (camera.rs:2993-2999) or the Welford mean.
+template <class R>
+__global__ void k_resolve(Params<R> P, float* rgb, double* rgb64, uint32_t* accepted) {
+    const uint32_t n = P.ps.n;
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = warp0; base < n; base += stride) {
+        const uint32_t i = base + lane_id();
+        unsigned long long va = 0, vs = 0;
+        if (i < n) {
+            const uint32_t a = P.ps.accepted[i];
+            V3<R> s = xyz(P.ps.acc[i]);
+            V3<R> c;
+            if (P.cam.adaptive) c = s;
+            else c = a == 0 ? V3<R>{0, 0, 0} : cdiv(s, R(a));
+            if (rgb) {
+                rgb[size_t(i) * 3 + 0] = float(c.x);
+                rgb[size_t(i) * 3 + 1] = float(c.y);
+                rgb[size_t(i) * 3 + 2] = float(c.z);
+            }
+            if (rgb64) {
+                rgb64[size_t(i) * 3 + 0] = double(c.x);
+                rgb64[size_t(i) * 3 + 1] = double(c.y);
+                rgb64[size_t(i) * 3 + 2] = double(c.z);
+            }
+            if (accepted) accepted[i] = a;
+            va = a;
+            vs = P.ps.st[i].w;
+        }
+        // Sample totals for throughput reporting (warp-reduced, one atomic per warp).
+        for (int off = 16; off > 0; off >>= 1) {
+            va += __shfl_down_sync(0xffffffffu, va, off);
+            vs += __shfl_down_sync(0xffffffffu, vs, off);
+        }
+        if (lane_id() == 0) {
+            atomicAdd(&P.ps.totals[2], va);
+            atomicAdd(&P.ps.totals[3], vs);
+        }
+    }
+}
+
+// Denoising AOVs (camera.rs:3064-3116): first-hit albedo and 0.5 (n + 1), same per-pixel
+// stream as the beauty pass, divided by the sample count.
+template <class R> __global__ void k_aov(Params<R> P, float* albedo, float* normal) {
+    const uint32_t n = P.cam.width * P.cam.height;
+    const R inf = Num<R>::inf();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t x = i % P.cam.width, y = i / P.cam.width;
+        Rng g{pixel_seed(P.cam.seed, x, y)};
+        V3<R> sa{0, 0, 0}, sn{0, 0, 0};
+        for (uint32_t k = 0; k < P.cam.spp; ++k) {
+            V3<R> o, d;
+            R time, t;
+            camera_ray(P.cam, x, y, k, g, o, d, time);
+            int prim = traverse<R, false, false>(P.sc, o, d, time, R(kShadowAcne), inf, t, nullptr,
+                                                 &P.ps.counters[C_ERROR]);
+            if (prim < 0) continue; // black on a miss
+            HitRec<R> h = make_hit(P.sc, uint32_t(prim), o, d, time, t);
+            sa = sa + mat_albedo(P.sc.mats[h.mat], h);
+            sn = sn + (h.n + V3<R>{1, 1, 1}) * R(0.5);
+        }
+        sa = cdiv(sa, R(P.cam.spp));
+        sn = cdiv(sn, R(P.cam.spp));
+        if (albedo) {
+            albedo[size_t(i) * 3 + 0] = float(sa.x);
+            albedo[size_t(i) * 3 + 1] = float(sa.y);
+            albedo[size_t(i) * 3 + 2] = float(sa.z);
+        }
+        if (normal) {
+            normal[size_t(i) * 3 + 0] = float(sn.x);
+            normal[size_t(i) * 3 + 1] = float(sn.y);
+            normal[size_t(i) * 3 + 2] = float(sn.z);
+        }
+    }
+}
+
+// Closest-hit queries with BvhTraversalStats (bvh.rs:9-52, 306-399); rays are
+// {origin xyz, direction xyz, time} in f64.  stats: [0..5) sums, [5] max stack depth.
+template <class R>
+__global__ void k_trace_rays(SceneDev<R> sc, const double* rays, uint32_t count, double tmin, double tmax,
+                             int32_t* ids, double* tout, unsigned long long* stats, uint32_t* err) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const double* r = rays + size_t(i) * 7;
+        V3<R> o{R(r[0]), R(r[1]), R(r[2])}, d{R(r[3]), R(r[4]), R(r[5])};
+        TraceStats st{0, 0, 0, 0, 0, 0};
+        R t = R(0);
+        int prim = traverse<R, true, false>(sc, o, d, R(r[6]), R(tmin), R(tmax), t, &st, err);
+        ids[i] = prim < 0 ? -1 : int32_t(__ldg(&sc.meta[prim].y));
+        if (tout) tout[i] = prim < 0 ? 0.0 : double(t);
+        atomicAdd(&stats[0], st.node_tests);
+        atomicAdd(&stats[1], st.node_hits);
+        atomicAdd(&stats[2], st.leaf_visits);
+        atomicAdd(&stats[3], st.candidates);
+        atomicAdd(&stats[4], st.leaf_hits);
+        atomicMax(&stats[5], (unsigned long long)st.max_depth);
+    }
+}
+
+} // namespace gt

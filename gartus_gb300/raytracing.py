@@ -1,0 +1,864 @@
+"""Host-side mirror of gartus's path-tracing API over the C ABI (include/gartus_gpu.h).
+
+The names, argument meanings and error behaviour follow the reference crate:
+`RayMaterial` (raytracing/material.rs:2355-2508), `RayScene` (raytracing/scene.rs:1102-1696),
+`SamplingTargetList` / `WeightedSamplingTargetList` (scene.rs:355-497),
+`EnvironmentLight` (raytracing/environment.rs), `RayCamera` builder (graphics/camera.rs:
+1034-1481), `PathTracer` (raytracing/renderer.rs:55-875) and `SurfaceScene::to_ray_scene`
+(scene.rs:1517-1621).  Invalid input that makes the reference panic raises ValueError or a
+GartusError carrying GT_ERR_INVALID_ARG.
+
+Primitives are kept in a numpy structured array with gt_primitive's exact layout, so a
+multi-million-triangle scene crosses the ABI without per-primitive Python objects.
+"""
+from __future__ import annotations
+
+import copy
+import ctypes as C
+import math
+import threading
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import abi
+from ._lib import GartusError, check, lib
+
+GEOMETRY_DTYPE = np.dtype([("kind", "<u4"), ("reserved", "<u4"), ("p", "<f8", (9,))])
+PRIMITIVE_DTYPE = np.dtype([("geometry", GEOMETRY_DTYPE), ("material", "<u4"), ("reserved", "<u4")])
+MATERIAL_DTYPE = np.dtype([
+    ("kind", "<u4"), ("texture_kind", "<u4"), ("color", "<f8", (3,)), ("param", "<f8"), ("tex", "<f8", (7,)),
+])
+LIGHT_DTYPE = np.dtype([("geometry", GEOMETRY_DTYPE), ("weight", "<f8")])
+assert PRIMITIVE_DTYPE.itemsize == C.sizeof(abi.gt_primitive)
+assert MATERIAL_DTYPE.itemsize == C.sizeof(abi.gt_material)
+assert LIGHT_DTYPE.itemsize == C.sizeof(abi.gt_light_target)
+
+INFINITY = math.inf
+SHADOW_ACNE_EPSILON = 0.001  # raytracing.rs:146
+WIDESCREEN_ASPECT_RATIO = 16.0 / 9.0
+
+
+def _vec(v, n=3) -> tuple:
+    t = tuple(float(x) for x in v)
+    if len(t) != n:
+        raise ValueError(f"expected {n} components, got {len(t)}")
+    return t
+
+
+def _finite(*vals) -> bool:
+    return all(math.isfinite(x) for v in vals for x in (v if isinstance(v, tuple) else (v,)))
+
+
+# ------------------------------------------------------------------- geometry
+@dataclass(frozen=True)
+class RayGeometry:
+    """RayGeometry (raytracing/object.rs:252-320)."""
+
+    kind: int
+    p: tuple
+
+    @staticmethod
+    def sphere(center, radius) -> "RayGeometry":
+        return RayGeometry(abi.GT_GEOM_SPHERE, _vec(center) + (float(radius),) + (0.0,) * 5)
+
+    @staticmethod
+    def moving_sphere(center_start, center_end, radius) -> "RayGeometry":
+        return RayGeometry(abi.GT_GEOM_MOVING_SPHERE, _vec(center_start) + _vec(center_end) + (float(radius), 0.0, 0.0))
+
+    @staticmethod
+    def triangle(p0, p1, p2) -> "RayGeometry":
+        return RayGeometry(abi.GT_GEOM_TRIANGLE, _vec(p0) + _vec(p1) + _vec(p2))
+
+    @staticmethod
+    def quad(corner, u, v) -> "RayGeometry":
+        return RayGeometry(abi.GT_GEOM_QUAD, _vec(corner) + _vec(u) + _vec(v))
+
+    def to_abi(self) -> abi.gt_geometry:
+        g = abi.gt_geometry()
+        g.kind = self.kind
+        for i, x in enumerate(self.p):
+            g.p[i] = x
+        return g
+
+
+# ------------------------------------------------------------------ materials
+@dataclass(frozen=True)
+class RayMaterial:
+    """RayMaterial variants on the GPU path (raytracing/material.rs:2355-2363)."""
+
+    kind: int
+    color: tuple = (0.0, 0.0, 0.0)
+    param: float = 0.0
+    texture_kind: int = abi.GT_TEX_SOLID
+    tex: tuple = (0.0,) * 7
+
+    @staticmethod
+    def lambertian(albedo) -> "RayMaterial":
+        albedo = _vec(albedo)
+        if not _finite(albedo):
+            raise ValueError("Lambertian albedo must be finite")
+        return RayMaterial(abi.GT_MAT_LAMBERTIAN, albedo)
+
+    @staticmethod
+    def checker_lambertian(scale, even, odd) -> "RayMaterial":
+        """Lambertian::checker (material.rs:443-446)."""
+        return RayMaterial(abi.GT_MAT_LAMBERTIAN, (0.5, 0.5, 0.5), 0.0, abi.GT_TEX_CHECKER,
+                           (float(scale),) + _vec(even) + _vec(odd))
+
+    @staticmethod
+    def diffuse_light(emit) -> "RayMaterial":
+        emit = _vec(emit)
+        if not _finite(emit):
+            raise ValueError("diffuse light color must be finite")
+        return RayMaterial(abi.GT_MAT_DIFFUSE_LIGHT, emit)
+
+    @staticmethod
+    def isotropic(albedo) -> "RayMaterial":
+        albedo = _vec(albedo)
+        if not _finite(albedo):
+            raise ValueError("isotropic albedo must be finite")
+        return RayMaterial(abi.GT_MAT_ISOTROPIC, albedo)
+
+    @staticmethod
+    def ggx_microfacet(specular_color, roughness) -> "RayMaterial":
+        c = _vec(specular_color)
+        if not _finite(c, float(roughness)):
+            raise ValueError("GGX microfacet material values must be finite")
+        return RayMaterial(abi.GT_MAT_GGX, c, min(max(float(roughness), 0.0), 1.0))
+
+    @staticmethod
+    def metal(albedo, fuzz) -> "RayMaterial":
+        c = _vec(albedo)
+        if not _finite(c, float(fuzz)):
+            raise ValueError("metal material values must be finite")
+        return RayMaterial(abi.GT_MAT_METAL, c, min(max(float(fuzz), 0.0), 1.0))
+
+    @staticmethod
+    def dielectric(refraction_index) -> "RayMaterial":
+        ri = float(refraction_index)
+        if not (math.isfinite(ri) and ri > 0.0):
+            raise ValueError("refractive index must be positive and finite")
+        return RayMaterial(abi.GT_MAT_DIELECTRIC, (1.0, 1.0, 1.0), ri)
+
+    def is_emissive(self) -> bool:  # material.rs:2555-2557
+        return self.kind == abi.GT_MAT_DIFFUSE_LIGHT
+
+    def to_record(self) -> tuple:
+        return (self.kind, self.texture_kind, self.color, self.param, self.tex)
+
+
+GLASS = 1.5  # RefractiveIndex::GLASS, graphics/lighting.rs:287
+
+
+# -------------------------------------------------------------- sampling targets
+class WeightedSamplingTargetList:
+    """WeightedSamplingTargetList (raytracing/scene.rs:423-497)."""
+
+    def __init__(self):
+        self._targets: list[tuple[RayGeometry, float]] = []
+        self._total = 0.0
+        self._handles: dict = {}
+
+    def add_target_weighted(self, geometry: RayGeometry, weight: float) -> None:
+        weight = float(weight)
+        if not (math.isfinite(weight) and weight > 0.0):
+            raise ValueError("sampling target weight must be finite and positive")
+        total = self._total + weight
+        if not math.isfinite(total):
+            raise ValueError("sampling target total weight must remain finite")
+        self._total = total
+        self._targets.append((geometry, weight))
+        self._invalidate()
+
+    def add_sphere_weighted(self, center, radius, weight):
+        self.add_target_weighted(RayGeometry.sphere(center, radius), weight)
+
+    def add_moving_sphere_weighted(self, c0, c1, radius, weight):
+        self.add_target_weighted(RayGeometry.moving_sphere(c0, c1, radius), weight)
+
+    def add_quad_weighted(self, corner, u, v, weight):
+        self.add_target_weighted(RayGeometry.quad(corner, u, v), weight)
+
+    def clear(self):
+        self._targets.clear()
+        self._total = 0.0
+        self._invalidate()
+
+    def __len__(self):
+        return len(self._targets)
+
+    def is_empty(self) -> bool:
+        return not self._targets
+
+    def total_weight(self) -> float:
+        return self._total
+
+    def to_array(self) -> np.ndarray:
+        arr = np.zeros(len(self._targets), dtype=LIGHT_DTYPE)
+        for i, (g, w) in enumerate(self._targets):
+            arr[i]["geometry"]["kind"] = g.kind
+            arr[i]["geometry"]["p"] = g.p
+            arr[i]["weight"] = w
+        return arr
+
+    def _invalidate(self):
+        for h in self._handles.values():
+            h.close()
+        self._handles = {}
+
+    def _handle(self, ctx: "Context"):
+        h = self._handles.get(id(ctx))
+        if h is None:
+            h = _LightsHandle(ctx, self.to_array())
+            self._handles[id(ctx)] = h
+        return h
+
+
+class SamplingTargetList(WeightedSamplingTargetList):
+    """SamplingTargetList (raytracing/scene.rs:355-421): every target has weight 1."""
+
+    def add_sphere(self, center, radius):
+        self.add_target_weighted(RayGeometry.sphere(center, radius), 1.0)
+
+    def add_moving_sphere(self, c0, c1, radius):
+        self.add_target_weighted(RayGeometry.moving_sphere(c0, c1, radius), 1.0)
+
+    def add_quad(self, corner, u, v):
+        self.add_target_weighted(RayGeometry.quad(corner, u, v), 1.0)
+
+    def add_target(self, geometry: RayGeometry):
+        self.add_target_weighted(geometry, 1.0)
+
+
+# --------------------------------------------------------------------- context
+class Context:
+    """A CUDA device context with its own stream (gt_context)."""
+
+    _default = None
+    _default_lock = threading.Lock()
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(lib().gt_context_create(int(device), C.byref(h)))
+        self._h = h
+        self.device = device
+
+    @classmethod
+    def default(cls) -> "Context":
+        with cls._default_lock:
+            if cls._default is None:
+                cls._default = Context(0)
+            return cls._default
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().gt_context_destroy(self._h)
+            self._h = None
+
+
+class _SceneHandle:
+    def __init__(self, ctx: Context, prims: np.ndarray, mats: np.ndarray, leaf_size: int):
+        self.ctx = ctx
+        prims = np.ascontiguousarray(prims)
+        mats = np.ascontiguousarray(mats)
+        d = abi.gt_scene_desc()
+        d.struct_size = C.sizeof(abi.gt_scene_desc)
+        d.num_primitives = len(prims)
+        d.primitives = prims.ctypes.data_as(C.POINTER(abi.gt_primitive))
+        d.num_materials = len(mats)
+        d.materials = mats.ctypes.data_as(C.POINTER(abi.gt_material))
+        d.bvh_leaf_size = leaf_size
+        h = C.c_void_p()
+        check(lib().gt_scene_create(ctx.handle, C.byref(d), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().gt_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _LightsHandle:
+    def __init__(self, ctx: Context, arr: np.ndarray):
+        arr = np.ascontiguousarray(arr)
+        h = C.c_void_p()
+        check(lib().gt_lights_create(ctx.handle, arr.ctypes.data_as(C.c_void_p), len(arr), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().gt_lights_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ----------------------------------------------------------------------- scene
+class RayScene:
+    """RayScene (raytracing/scene.rs:1102-1696): material and primitive tables plus a
+    lazily built BVH (the device copy is built on first use and reused)."""
+
+    def __init__(self):
+        self._materials: list[RayMaterial] = []
+        self._chunks: list[np.ndarray] = []
+        self._prims: Optional[np.ndarray] = np.zeros(0, dtype=PRIMITIVE_DTYPE)
+        self._leaf_size = 4
+        self._handles: dict = {}
+
+    # -- tables
+    def add_material(self, material: RayMaterial) -> int:
+        self._materials.append(material)
+        self._invalidate()
+        return len(self._materials) - 1
+
+    def _check_material(self, material: int) -> None:
+        if not (0 <= int(material) < len(self._materials)):
+            raise ValueError("ray scene material id out of bounds")  # scene.rs:1158-1161
+
+    def add_primitive(self, geometry: RayGeometry, material: int) -> None:
+        self._check_material(material)
+        rec = np.zeros(1, dtype=PRIMITIVE_DTYPE)
+        rec["geometry"]["kind"] = geometry.kind
+        rec["geometry"]["p"] = geometry.p
+        rec["material"] = int(material)
+        self._chunks.append(rec)
+        self._invalidate()
+
+    def add_primitives_array(self, prims: np.ndarray) -> None:
+        """Bulk add_primitives (scene.rs:1174-1191) from a PRIMITIVE_DTYPE array."""
+        prims = np.asarray(prims, dtype=PRIMITIVE_DTYPE)
+        if len(prims) and (prims["material"].max() >= len(self._materials)):
+            raise ValueError("ray scene material id out of bounds")
+        self._chunks.append(prims.copy())
+        self._invalidate()
+
+    def add_triangles_array(self, material: int, vertices: np.ndarray) -> None:
+        """add_triangles (scene.rs:1313-1324) from an (N, 3, 3) float64 array."""
+        self._check_material(material)
+        v = np.asarray(vertices, dtype=np.float64).reshape(-1, 9)
+        rec = np.zeros(len(v), dtype=PRIMITIVE_DTYPE)
+        rec["geometry"]["kind"] = abi.GT_GEOM_TRIANGLE
+        rec["geometry"]["p"] = v
+        rec["material"] = int(material)
+        self._chunks.append(rec)
+        self._invalidate()
+
+    def add_sphere(self, center, radius, material):
+        self.add_primitive(RayGeometry.sphere(center, radius), material)
+
+    def add_moving_sphere(self, center_start, center_end, radius, material):
+        self.add_primitive(RayGeometry.moving_sphere(center_start, center_end, radius), material)
+
+    def add_quad(self, corner, u, v, material):
+        self.add_primitive(RayGeometry.quad(corner, u, v), material)
+
+    def add_triangle(self, p0, p1, p2, material):
+        self.add_primitive(RayGeometry.triangle(p0, p1, p2), material)
+
+    def add_sphere_with_material(self, center, radius, material: RayMaterial) -> int:
+        mid = self.add_material(material)
+        self.add_sphere(center, radius, mid)
+        return mid
+
+    def add_moving_sphere_with_material(self, c0, c1, radius, material: RayMaterial) -> int:
+        mid = self.add_material(material)
+        self.add_moving_sphere(c0, c1, radius, mid)
+        return mid
+
+    def add_quad_with_material(self, corner, u, v, material: RayMaterial) -> int:
+        mid = self.add_material(material)
+        self.add_quad(corner, u, v, mid)
+        return mid
+
+    # -- BVH options
+    def build_bvh(self) -> None:
+        self.build_bvh_with_options(4)
+
+    def build_bvh_with_options(self, leaf_size: int = 4) -> None:
+        """BvhBuildOptions::with_leaf_size clamps 0 to 1 (bvh.rs:73-77)."""
+        self._leaf_size = max(int(leaf_size), 1)
+        self._invalidate()
+
+    def with_bvh(self) -> "RayScene":
+        self.build_bvh()
+        return self
+
+    # -- views
+    def materials(self) -> list[RayMaterial]:
+        return list(self._materials)
+
+    def primitives_array(self) -> np.ndarray:
+        if self._chunks:
+            parts = [self._prims] + self._chunks if len(self._prims) else self._chunks
+            self._prims = np.concatenate(parts) if len(parts) > 1 else parts[0]
+            self._chunks = []
+        return self._prims
+
+    def materials_array(self) -> np.ndarray:
+        arr = np.zeros(len(self._materials), dtype=MATERIAL_DTYPE)
+        for i, m in enumerate(self._materials):
+            arr[i] = m.to_record()
+        return arr
+
+    @property
+    def leaf_size(self) -> int:
+        return self._leaf_size
+
+    def __len__(self) -> int:
+        return len(self.primitives_array())
+
+    def is_empty(self) -> bool:
+        return len(self) == 0
+
+    def material_count(self) -> int:
+        return len(self._materials)
+
+    def emissive_targets(self) -> SamplingTargetList:
+        """RayScene::emissive_targets (scene.rs:1401-1423)."""
+        targets = SamplingTargetList()
+        prims = self.primitives_array()
+        for rec in prims:
+            if self._materials[int(rec["material"])].is_emissive():
+                targets.add_target(RayGeometry(int(rec["geometry"]["kind"]), tuple(float(x) for x in rec["geometry"]["p"])))
+        return targets
+
+    # -- device handle
+    def _invalidate(self):
+        for h in self._handles.values():
+            h.close()
+        self._handles = {}
+
+    def _handle(self, ctx: Context) -> _SceneHandle:
+        h = self._handles.get(id(ctx))
+        if h is None:
+            h = _SceneHandle(ctx, self.primitives_array(), self.materials_array(), self._leaf_size)
+            self._handles[id(ctx)] = h
+        return h
+
+    def bvh_node_count(self, ctx: Optional[Context] = None) -> int:
+        n = C.c_uint32()
+        check(lib().gt_scene_bvh_node_count(self._handle(ctx or Context.default()).h, C.byref(n)))
+        return n.value
+
+    def hit_rays(self, rays: np.ndarray, t_min: float = SHADOW_ACNE_EPSILON, t_max: float = INFINITY,
+                 ctx: Optional[Context] = None):
+        """Closest hits of (N, 7) rays {origin, direction, time} in f64 with the summed
+        BvhTraversalStats (scene.rs:1474-1492).  Returns (prim_ids, t, stats)."""
+        rays = np.ascontiguousarray(rays, dtype=np.float64).reshape(-1, 7)
+        ids = np.empty(len(rays), dtype=np.int32)
+        t = np.empty(len(rays), dtype=np.float64)
+        st = abi.gt_bvh_stats()
+        check(lib().gt_trace_rays(self._handle(ctx or Context.default()).h, rays.ctypes.data_as(C.c_void_p),
+                                  len(rays), float(t_min), float(t_max), ids.ctypes.data_as(C.c_void_p),
+                                  t.ctypes.data_as(C.c_void_p), C.byref(st)))
+        return ids, t, st.as_dict()
+
+    def bvh_traversal_stats_for_rays(self, rays: np.ndarray, t_min: float = SHADOW_ACNE_EPSILON,
+                                     t_max: float = INFINITY) -> dict:
+        return self.hit_rays(rays, t_min, t_max)[2]
+
+
+# ---------------------------------------------------------------- environment
+class EnvironmentLight:
+    """EnvironmentLight (raytracing/environment.rs:22-202).  `texels` is (H, W, 3): uint8
+    for the reference's 8-bit gamma-2 canvas, float32 for the linear HDR extension.
+    Row 0 is the zenith."""
+
+    def __init__(self, texels: np.ndarray):
+        texels = np.asarray(texels)
+        if texels.ndim != 3 or texels.shape[2] != 3 or texels.shape[0] == 0 or texels.shape[1] == 0:
+            raise ValueError("environment texels must be a non-empty (H, W, 3) array")
+        if texels.dtype == np.uint8:
+            self.format = abi.GT_ENV_SRGB8
+        else:
+            texels = texels.astype(np.float32)
+            if not np.isfinite(texels).all():
+                raise ValueError("environment texels must be finite")
+            self.format = abi.GT_ENV_RGB32F
+        self.texels = np.ascontiguousarray(texels)
+        self._handles: dict = {}
+
+    @property
+    def width(self) -> int:
+        return self.texels.shape[1]
+
+    @property
+    def height(self) -> int:
+        return self.texels.shape[0]
+
+    def desc(self) -> abi.gt_environment_desc:
+        d = abi.gt_environment_desc()
+        d.struct_size = C.sizeof(abi.gt_environment_desc)
+        d.format = self.format
+        d.width = self.width
+        d.height = self.height
+        d.texels = self.texels.ctypes.data_as(C.c_void_p)
+        return d
+
+    def _handle(self, ctx: Context):
+        h = self._handles.get(id(ctx))
+        if h is None:
+            h = _EnvHandle(ctx, self)
+            self._handles[id(ctx)] = h
+        return h
+
+
+class _EnvHandle:
+    def __init__(self, ctx: Context, env: EnvironmentLight):
+        d = env.desc()
+        h = C.c_void_p()
+        check(lib().gt_environment_create(ctx.handle, C.byref(d), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().gt_environment_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# --------------------------------------------------------------------- camera
+PixelSampleMode = {"random": abi.GT_SAMPLE_RANDOM, "stratified": abi.GT_SAMPLE_STRATIFIED,
+                   "grid": abi.GT_SAMPLE_STRATIFIED_GRID}
+
+
+class RayCamera:
+    """RayCamera builder (graphics/camera.rs:1034-1481).  Each with_* returns a new camera."""
+
+    def __init__(self, image_width: int, aspect_ratio: float):
+        d = abi.gt_camera_desc()
+        check(lib().gt_camera_default(int(image_width), float(aspect_ratio), C.byref(d)))
+        self._d = d
+
+    @classmethod
+    def from_desc(cls, d: abi.gt_camera_desc) -> "RayCamera":
+        cam = cls.__new__(cls)
+        cam._d = copy.copy(d)
+        return cam
+
+    def desc(self) -> abi.gt_camera_desc:
+        return self._d
+
+    def _with(self, **kw) -> "RayCamera":
+        d = abi.gt_camera_desc()
+        C.pointer(d)[0] = self._d
+        for k, v in kw.items():
+            if isinstance(v, tuple):
+                arr = getattr(d, k)
+                for i, x in enumerate(v):
+                    arr[i] = x
+            else:
+                setattr(d, k, v)
+        return RayCamera.from_desc(d)
+
+    def with_samples_per_pixel(self, spp: int):
+        return self._with(samples_per_pixel=max(int(spp), 1))
+
+    def with_pixel_sample_mode(self, mode: int):
+        return self._with(pixel_sample_mode=int(mode))
+
+    def with_stratified_sampling(self):
+        return self._with(pixel_sample_mode=abi.GT_SAMPLE_STRATIFIED)
+
+    def with_stratified_grid_width(self, grid_width: int):
+        g = max(int(grid_width), 1)
+        return self._with(samples_per_pixel=g * g, pixel_sample_mode=abi.GT_SAMPLE_STRATIFIED_GRID, grid_width=g)
+
+    def with_adaptive_sampling(self, min_samples: int, max_samples: int, error_threshold: float):
+        thr = float(error_threshold)
+        if not (math.isfinite(thr) and thr > 0.0):
+            raise ValueError("adaptive sampling error threshold must be positive and finite")
+        mn = max(int(min_samples), 1)
+        mx = max(int(max_samples), mn)
+        return self._with(adaptive=1, adaptive_min_samples=mn, adaptive_max_samples=mx,
+                          adaptive_error_threshold=thr, samples_per_pixel=mx)
+
+    def without_adaptive_sampling(self):
+        return self._with(adaptive=0)
+
+    def with_direct_lighting_mode(self, mode: int):
+        w = 0.5 if mode == abi.GT_DIRECT_CURRENT_PATH_CONTINUATION else 0.0
+        return self._with(direct_lighting_mode=int(mode), light_pdf_weight=w)
+
+    def with_light_pdf_weight(self, weight: float):
+        weight = float(weight)
+        if not math.isfinite(weight):
+            raise ValueError("light PDF weight must be finite")
+        return self._with(direct_lighting_mode=abi.GT_DIRECT_CURRENT_PATH_CONTINUATION,
+                          light_pdf_weight=min(max(weight, 0.0), 1.0))
+
+    def with_max_depth(self, depth: int):
+        return self._with(max_depth=int(depth))
+
+    def with_russian_roulette_min_depth(self, depth: int):
+        return self._with(russian_roulette_min_depth=int(depth))
+
+    def without_russian_roulette(self):
+        return self._with(russian_roulette_min_depth=-1)
+
+    def with_rng_seed(self, seed: int):
+        return self._with(rng_seed=int(seed) & 0xFFFFFFFFFFFFFFFF)
+
+    def with_vertical_fov(self, fov: float):
+        return self._with(vertical_fov=float(fov))
+
+    def with_look_at(self, lookfrom, lookat):
+        return self._with(lookfrom=_vec(lookfrom), lookat=_vec(lookat))
+
+    def with_view_up(self, vup):
+        return self._with(view_up=_vec(vup))
+
+    def with_defocus_angle(self, angle: float):
+        return self._with(defocus_angle=float(angle))
+
+    def with_focus_distance(self, dist: float):
+        return self._with(focus_distance=float(dist))
+
+    def with_shutter_interval(self, start: float, end: float):
+        if not (math.isfinite(start) and math.isfinite(end) and start <= end):
+            raise ValueError("shutter interval must be finite and ordered")
+        return self._with(shutter_start=float(start), shutter_end=float(end))
+
+    def with_background(self, color):
+        return self._with(background_kind=abi.GT_BG_CONSTANT, background=_vec(color) + (0.0,) * 6)
+
+    def with_vertical_gradient_background(self, nadir, horizon, zenith):
+        return self._with(background_kind=abi.GT_BG_VERTICAL_GRADIENT,
+                          background=_vec(nadir) + _vec(horizon) + _vec(zenith))
+
+    def image_size(self) -> tuple[int, int, int]:
+        w, h, s = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        check(lib().gt_camera_image_size(C.byref(self._d), C.byref(w), C.byref(h), C.byref(s)))
+        return w.value, h.value, s.value
+
+    @property
+    def image_width(self) -> int:
+        return self._d.image_width
+
+    @property
+    def image_height(self) -> int:
+        return self.image_size()[1]
+
+    def effective_samples_per_pixel(self) -> int:
+        return self.image_size()[2]
+
+
+# --------------------------------------------------------------------- images
+@dataclass
+class HdrImage:
+    """HdrImage (graphics/display.rs:282-440): row-major linear RGB, row 0 at the top."""
+
+    width: int
+    height: int
+    pixels: np.ndarray  # (H, W, 3) float32
+    accepted: Optional[np.ndarray] = None
+    pixels64: Optional[np.ndarray] = None
+
+    def to_canvas(self) -> np.ndarray:
+        """Gamma-2 bytes, (256 * clamp(sqrt(c), 0, 0.999)) as u8 (colors.rs:388-407)."""
+        c = np.nan_to_num(self.pixels.astype(np.float64), nan=0.0)
+        g = np.sqrt(np.clip(c, 0.0, None))
+        return (256.0 * np.clip(g, 0.0, 0.999)).astype(np.uint8)
+
+    def save_pfm(self, path) -> None:
+        """Little-endian PFM, bottom row first (display.rs:359-388)."""
+        with open(path, "wb") as f:
+            f.write(f"PF\n{self.width} {self.height}\n-1.0\n".encode())
+            f.write(np.ascontiguousarray(self.pixels[::-1].astype("<f4")).tobytes())
+
+
+@dataclass
+class DenoisingAovs:
+    """DenoisingAovs (graphics/camera.rs:491-526), linear planes."""
+
+    beauty_linear: np.ndarray
+    albedo_linear: np.ndarray
+    normal_linear: np.ndarray
+
+
+# ------------------------------------------------------------------- renderer
+@dataclass(frozen=True)
+class RenderOptions:
+    """RenderOptions (renderer.rs:20-45).  Tiles do not exist on the wavefront path;
+    the tile size is accepted and ignored because the image does not depend on it."""
+
+    tile_size: Optional[int] = None
+
+
+class PathTracer:
+    """PathTracer (raytracing/renderer.rs:55-875) on the GB300 wavefront integrator.
+
+    precision: "f32" (throughput) or "f64" (the reference's arithmetic, op for op)."""
+
+    def __init__(self, camera: RayCamera, options: RenderOptions = RenderOptions(), precision: str = "f32",
+                 context: Optional[Context] = None, profile: bool = False):
+        if precision not in ("f32", "f64"):
+            raise ValueError("precision must be 'f32' or 'f64'")
+        self.camera = camera
+        self.options = options
+        self.precision = precision
+        self.profile = profile
+        self._ctx = context
+        self.last_stats: Optional[dict] = None
+
+    @property
+    def context(self) -> Context:
+        return self._ctx or Context.default()
+
+    def with_options(self, options: RenderOptions) -> "PathTracer":
+        return PathTracer(self.camera, options, self.precision, self._ctx, self.profile)
+
+    def _render(self, world: RayScene, lights: Optional[WeightedSamplingTargetList],
+                environment: Optional[EnvironmentLight], aovs: bool = False, want64: bool = False):
+        ctx = self.context
+        w, h, _ = self.camera.image_size()
+        rgb = np.empty((h, w, 3), dtype=np.float32)
+        acc = np.empty((h, w), dtype=np.uint32)
+        rgb64 = np.empty((h, w, 3), dtype=np.float64) if want64 else None
+        alb = np.empty((h, w, 3), dtype=np.float32) if aovs else None
+        nrm = np.empty((h, w, 3), dtype=np.float32) if aovs else None
+        f = abi.gt_frame()
+        f.struct_size = C.sizeof(abi.gt_frame)
+        f.width, f.height, f.device_buffers = w, h, 0
+        f.rgb = rgb.ctypes.data
+        f.accepted = acc.ctypes.data
+        f.rgb64 = rgb64.ctypes.data if want64 else None
+        f.albedo = alb.ctypes.data if aovs else None
+        f.normal = nrm.ctypes.data if aovs else None
+        o = abi.gt_render_opts()
+        o.struct_size = C.sizeof(abi.gt_render_opts)
+        o.precision = abi.GT_PRECISION_F64 if self.precision == "f64" else abi.GT_PRECISION_F32
+        o.aovs = 1 if aovs else 0
+        o.profile = 1 if self.profile else 0
+        stats = abi.gt_render_stats()
+        o.stats = C.pointer(stats)
+        sh = world._handle(ctx)
+        lh = lights._handle(ctx).h if lights is not None else None
+        eh = environment._handle(ctx).h if environment is not None else None
+        check(lib().gt_render(sh.h, lh, eh, C.byref(self.camera.desc()), C.byref(o), C.byref(f)))
+        self.last_stats = stats.as_dict()
+        img = HdrImage(w, h, rgb, acc, rgb64)
+        if aovs:
+            return img, alb, nrm
+        return img
+
+    # render / render_hdr_image (renderer.rs:101-117)
+    def render_hdr_image(self, world: RayScene, want64: bool = False) -> HdrImage:
+        return self._render(world, None, None, want64=want64)
+
+    def render(self, world: RayScene) -> np.ndarray:
+        return self.render_hdr_image(world).to_canvas()
+
+    # render_ray_scene_hdr_image (renderer.rs:193-200)
+    def render_ray_scene_hdr_image(self, scene: RayScene, want64: bool = False) -> HdrImage:
+        lights = scene.emissive_targets()
+        if lights.is_empty():
+            return self.render_hdr_image(scene, want64)
+        return self.render_with_lights_hdr_image(scene, lights, want64)
+
+    def render_ray_scene(self, scene: RayScene) -> np.ndarray:
+        return self.render_ray_scene_hdr_image(scene).to_canvas()
+
+    # render_with_lights_hdr_image (renderer.rs:391-406)
+    def render_with_lights_hdr_image(self, world: RayScene, lights: WeightedSamplingTargetList,
+                                     want64: bool = False) -> HdrImage:
+        return self._render(world, lights, None, want64=want64)
+
+    def render_with_lights(self, world, lights) -> np.ndarray:
+        return self.render_with_lights_hdr_image(world, lights).to_canvas()
+
+    # render_with_light_connections (renderer.rs:771-786): forces NEE
+    def render_with_light_connections_hdr_image(self, world, lights, want64: bool = False) -> HdrImage:
+        cam = self.camera.with_direct_lighting_mode(abi.GT_DIRECT_NEXT_EVENT_ESTIMATION)
+        return PathTracer(cam, self.options, self.precision, self._ctx, self.profile)._render(world, lights, None,
+                                                                                           want64=want64)
+
+    # render_with_environment_hdr_image (renderer.rs:431-449)
+    def render_with_environment_hdr_image(self, world: RayScene, environment: EnvironmentLight,
+                                          want64: bool = False) -> HdrImage:
+        return self._render(world, None, environment, want64=want64)
+
+    def render_with_environment(self, world, environment) -> np.ndarray:
+        return self.render_with_environment_hdr_image(world, environment).to_canvas()
+
+    # render_with_lights_and_environment_hdr_image (renderer.rs:588-609)
+    def render_with_lights_and_environment_hdr_image(self, world, lights, environment,
+                                                     want64: bool = False) -> HdrImage:
+        return self._render(world, lights, environment, want64=want64)
+
+    # render_denoising_aovs (renderer.rs:121-129) and render_ray_scene_denoising_aovs (217-224)
+    def render_denoising_aovs(self, world: RayScene) -> DenoisingAovs:
+        img, alb, nrm = self._render(world, None, None, aovs=True)
+        return DenoisingAovs(img.pixels, alb, nrm)
+
+    def render_ray_scene_denoising_aovs(self, scene: RayScene) -> DenoisingAovs:
+        lights = scene.emissive_targets()
+        img, alb, nrm = self._render(scene, None if lights.is_empty() else lights, None, aovs=True)
+        return DenoisingAovs(img.pixels, alb, nrm)
+
+    # render_scene_hdr_image (renderer.rs:321-324)
+    def render_scene_hdr_image(self, scene: "SurfaceScene") -> HdrImage:
+        return self.render_hdr_image(scene.to_ray_scene())
+
+    def trace_primary(self, scene: RayScene, stride: int = 1):
+        """Primary probe rays (ray_for_pixel) through the f64 reference-layout BVH:
+        (prim_ids, t, BvhTraversalStats) (benches/render_performance.rs:42-93)."""
+        w, h, _ = self.camera.image_size()
+        stride = max(int(stride), 1)
+        n = ((w + stride - 1) // stride) * ((h + stride - 1) // stride)
+        ids = np.empty(n, dtype=np.int32)
+        t = np.empty(n, dtype=np.float64)
+        st = abi.gt_bvh_stats()
+        check(lib().gt_trace_primary(scene._handle(self.context).h, C.byref(self.camera.desc()), stride,
+                                     ids.ctypes.data_as(C.c_void_p), t.ctypes.data_as(C.c_void_p), C.byref(st)))
+        return ids, t, st.as_dict()
+
+
+# ------------------------------------------------------------ surface scenes
+@dataclass
+class SurfaceMesh:
+    """SurfaceMesh (graphics/scene.rs:17-60): triangles plus a base colour."""
+
+    triangles: np.ndarray  # (N, 3, 3)
+    base_color: tuple = (0.5, 0.5, 0.5)
+
+
+@dataclass
+class SurfaceScene:
+    """SurfaceScene (graphics/scene.rs) restricted to what to_ray_scene consumes."""
+
+    meshes: list = field(default_factory=list)
+
+    def add_mesh(self, triangles: np.ndarray, base_color=(0.5, 0.5, 0.5)) -> None:
+        self.meshes.append(SurfaceMesh(np.asarray(triangles, dtype=np.float64).reshape(-1, 3, 3), _vec(base_color)))
+
+    def to_ray_scene(self, leaf_size: int = 4) -> RayScene:
+        """SurfaceScene::to_ray_scene (scene.rs:1517-1547, 1606-1608): one Lambertian per
+        mesh from its base colour, triangles in mesh order, BVH built."""
+        scene = RayScene()
+        for mesh in self.meshes:
+            mid = scene.add_material(RayMaterial.lambertian(mesh.base_color))
+            scene.add_triangles_array(mid, mesh.triangles)
+        scene.build_bvh_with_options(leaf_size)
+        return scene

@@ -1,0 +1,339 @@
+/*
+ * gartus_gpu.h — C ABI of the GB300 (sm_103a) path tracer that drops in for the
+ * gartus `PathTracer` render path over a compiled `RayScene`.
+ *
+ * Every entry point here replaces one piece of the reference's Rust surface; the
+ * reference interface is cited beside each declaration (paths are relative to the
+ * gartus crate root).  The boundary is plain C: POD structs, raw pointers and sizes,
+ * status codes instead of panics.  Nothing here exposes CUDA or torch types.
+ *
+ * Ownership: the library copies every input array it is given.  Handles are opaque
+ * and are released by their matching *_destroy call.  Output buffers belong to the
+ * caller.
+ *
+ * Errors: every fallible call returns a gt_status.  The reference panics through
+ * `assert!` on invalid input (e.g. graphics/camera.rs:1161-1201,
+ * raytracing/scene.rs:1158-1161); here those cases return GT_ERR_INVALID_ARG and the
+ * message is available from gt_last_error() on the calling thread.
+ *
+ * Threading: a gt_context owns one CUDA stream.  Calls on one context (and on the
+ * scenes, light lists and environments created from it) are serialised by an
+ * internal mutex, so a scene may be shared between threads the way the reference's
+ * `RayScene: Send + Sync` is (raytracing/object.rs:594).
+ */
+#ifndef GARTUS_GPU_H
+#define GARTUS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GT_ABI_VERSION 1u
+
+typedef enum gt_status {
+    GT_OK = 0,
+    GT_ERR_INVALID_ARG = 1,
+    GT_ERR_OOM = 2,
+    GT_ERR_CUDA = 3,
+    GT_ERR_TIMEOUT = 4,
+    GT_ERR_CANCELLED = 5,
+    GT_ERR_UNSUPPORTED = 6,
+    GT_ERR_NO_DEVICE = 7,
+    GT_ERR_INTERNAL = 8
+} gt_status;
+
+/* ---------------------------------------------------------------- geometry */
+
+/* RayGeometry (raytracing/object.rs:252-258). */
+typedef enum gt_geometry_kind {
+    GT_GEOM_SPHERE = 0,        /* p[0..3] centre, p[3] radius (geometry.rs:419-431)        */
+    GT_GEOM_MOVING_SPHERE = 1, /* p[0..3] centre at t=0, p[3..6] centre at t=1, p[6] radius */
+    GT_GEOM_TRIANGLE = 2,      /* p[0..3] p0, p[3..6] p1, p[6..9] p2 (geometry.rs:129-133)  */
+    GT_GEOM_QUAD = 3           /* p[0..3] corner, p[3..6] u, p[6..9] v (geometry.rs:271-301) */
+} gt_geometry_kind;
+
+typedef struct gt_geometry {
+    uint32_t kind; /* gt_geometry_kind */
+    uint32_t reserved;
+    double p[9];
+} gt_geometry;
+
+/* RayPrimitive { geometry, material } (raytracing/scene.rs:876-880). */
+typedef struct gt_primitive {
+    gt_geometry geometry;
+    uint32_t material; /* index into gt_scene_desc.materials */
+    uint32_t reserved;
+} gt_primitive;
+
+/* ---------------------------------------------------------------- materials */
+
+/* RayMaterial variants on the path (raytracing/material.rs:2355-2363). */
+typedef enum gt_material_kind {
+    GT_MAT_LAMBERTIAN = 0,    /* color = albedo                         (material.rs:508-537)   */
+    GT_MAT_DIFFUSE_LIGHT = 1, /* color = emission                       (material.rs:1008-1028) */
+    GT_MAT_ISOTROPIC = 2,     /* color = albedo                         (material.rs:1124-1147) */
+    GT_MAT_GGX = 3,           /* color = specular colour, param = roughness (material.rs:1583-1622) */
+    GT_MAT_METAL = 4,         /* color = albedo, param = fuzz           (material.rs:2087-2112) */
+    GT_MAT_DIELECTRIC = 5     /* param = refraction index               (material.rs:2264-2351) */
+} gt_material_kind;
+
+/* Colour source of a material (raytracing/texture.rs SolidColor / CheckerTexture). */
+typedef enum gt_texture_kind {
+    GT_TEX_SOLID = 0,  /* the material's color                                          */
+    GT_TEX_CHECKER = 1 /* tex[0] = scale, tex[1..4] = even colour, tex[4..7] = odd colour */
+} gt_texture_kind;
+
+typedef struct gt_material {
+    uint32_t kind;         /* gt_material_kind */
+    uint32_t texture_kind; /* gt_texture_kind  */
+    double color[3];
+    double param;
+    double tex[7];
+} gt_material;
+
+/* ------------------------------------------------------------------- scene */
+
+/* A compiled RayScene (raytracing/scene.rs:1102-1106) with its BVH build options
+ * (BvhBuildOptions, raytracing/bvh.rs:55-89). */
+typedef struct gt_scene_desc {
+    uint32_t struct_size; /* sizeof(gt_scene_desc) */
+    uint32_t num_primitives;
+    const gt_primitive* primitives;
+    uint32_t num_materials;
+    uint32_t bvh_leaf_size; /* 0 selects the reference default of 4 */
+    const gt_material* materials;
+} gt_scene_desc;
+
+/* One weighted sampling target (WeightedSamplingTargetList, raytracing/scene.rs:423-497).
+ * SamplingTargetList::add_* uses weight 1.0 (scene.rs:381-391). */
+typedef struct gt_light_target {
+    gt_geometry geometry;
+    double weight;
+} gt_light_target;
+
+/* EnvironmentLight texels (raytracing/environment.rs:22-31).  GT_ENV_SRGB8 is the
+ * reference's 8-bit gamma-2 canvas; GT_ENV_RGB32F is the linear f32 extension whose
+ * radiance is not limited to 1.0.  Texel (x, y) is at y*width + x, row 0 = zenith. */
+typedef enum gt_environment_format {
+    GT_ENV_SRGB8 = 0,
+    GT_ENV_RGB32F = 1
+} gt_environment_format;
+
+typedef struct gt_environment_desc {
+    uint32_t struct_size;
+    uint32_t format; /* gt_environment_format */
+    uint32_t width;
+    uint32_t height;
+    const void* texels; /* width*height*3 bytes (SRGB8) or floats (RGB32F) */
+} gt_environment_desc;
+
+/* ------------------------------------------------------------------ camera */
+
+/* PixelSampleMode (graphics/camera.rs:43-56). */
+typedef enum gt_pixel_sample_mode {
+    GT_SAMPLE_RANDOM = 0,
+    GT_SAMPLE_STRATIFIED = 1,
+    GT_SAMPLE_STRATIFIED_GRID = 2
+} gt_pixel_sample_mode;
+
+/* DirectLightingMode (graphics/camera.rs:58-64). */
+typedef enum gt_direct_lighting_mode {
+    GT_DIRECT_CURRENT_PATH_CONTINUATION = 0,
+    GT_DIRECT_NEXT_EVENT_ESTIMATION = 1
+} gt_direct_lighting_mode;
+
+/* RayBackground (graphics/camera.rs:203-215); the Function variant cannot cross the ABI. */
+typedef enum gt_background_kind {
+    GT_BG_CONSTANT = 0,         /* background[0..3] */
+    GT_BG_VERTICAL_GRADIENT = 1 /* background[0..3] nadir, [3..6] horizon, [6..9] zenith */
+} gt_background_kind;
+
+/* RayCameraParams (graphics/camera.rs:646-669) plus the builder state of RayCamera
+ * (camera.rs:613-643).  gt_camera_default() fills the values of RayCamera::new
+ * (camera.rs:1034-1065). */
+typedef struct gt_camera_desc {
+    uint32_t struct_size;
+    uint32_t image_width;
+    double aspect_ratio;
+    uint32_t samples_per_pixel;
+    uint32_t pixel_sample_mode; /* gt_pixel_sample_mode */
+    uint32_t grid_width;        /* used by GT_SAMPLE_STRATIFIED_GRID */
+    uint32_t adaptive;          /* 1 = AdaptiveSampling enabled (camera.rs:367-396) */
+    uint32_t adaptive_min_samples;
+    uint32_t adaptive_max_samples;
+    double adaptive_error_threshold;
+    uint32_t direct_lighting_mode; /* gt_direct_lighting_mode */
+    uint32_t max_depth;
+    double light_pdf_weight;
+    int32_t russian_roulette_min_depth; /* negative = None (without_russian_roulette) */
+    uint32_t reserved0;
+    uint64_t rng_seed;
+    double vertical_fov;
+    double lookfrom[3];
+    double lookat[3];
+    double view_up[3];
+    double defocus_angle;
+    double focus_distance;
+    double shutter_start;
+    double shutter_end;
+    uint32_t background_kind; /* gt_background_kind */
+    uint32_t reserved1;
+    double background[9];
+} gt_camera_desc;
+
+/* ------------------------------------------------------------------ render */
+
+typedef enum gt_precision {
+    GT_PRECISION_F32 = 0, /* throughput path: f32 arithmetic, Kahan-compensated accumulation */
+    GT_PRECISION_F64 = 1  /* reference-exact path: the reference's f64 arithmetic, op for op  */
+} gt_precision;
+
+/* Progress callback between wavefront batches; a nonzero return cancels the render
+ * (the reference cancels remaining tiles when its progress callback returns Err,
+ * graphics/camera.rs:3195-3243). */
+typedef int (*gt_progress_fn)(void* user, uint64_t samples_done, uint64_t samples_total);
+
+/* Per-render measurements (no reference counterpart: the reference's bench only prints
+ * wall-clock milliseconds, benches/render_performance.rs:52-61). */
+typedef enum gt_kernel_id {
+    GT_KERNEL_GENERATE = 0, /* finish samples, start camera rays          */
+    GT_KERNEL_TRACE = 1,    /* closest-hit traversal + material binning    */
+    GT_KERNEL_SHADE = 2,    /* one bounce of the integrator per path       */
+    GT_KERNEL_SHADOW = 3,   /* deferred next-event shadow queries          */
+    GT_KERNEL_OTHER = 4,    /* init, resolve, AOVs                         */
+    GT_KERNEL_COUNT = 5
+} gt_kernel_id;
+
+typedef struct gt_render_stats {
+    double gpu_ms;          /* device time of the whole render (CUDA events on the library's stream) */
+    uint64_t iterations;    /* wavefront iterations launched                                          */
+    uint64_t rays;          /* closest-hit queries (camera + bounce rays)                             */
+    uint64_t shadow_rays;   /* next-event shadow queries                                              */
+    uint64_t samples;       /* accepted camera samples summed over pixels                             */
+    uint64_t samples_started;
+    double kernel_ms[GT_KERNEL_COUNT];     /* filled when gt_render_opts.profile = 1 */
+    uint64_t kernel_launches[GT_KERNEL_COUNT];
+} gt_render_stats;
+
+typedef struct gt_render_opts {
+    uint32_t struct_size;
+    uint32_t precision;   /* gt_precision */
+    uint32_t aovs;        /* 1 = also produce albedo and normal AOVs (camera.rs:3064-3116) */
+    uint32_t profile;     /* 1 = launch kernels one by one with CUDA events around each (slower) */
+    gt_progress_fn progress;
+    void* progress_user;
+    gt_render_stats* stats; /* optional output */
+} gt_render_opts;
+
+/* Caller-owned output images, row-major, 3 channels, y = 0 is the top row
+ * (HdrImage, graphics/display.rs:282-295).  Any pointer may be NULL except rgb. */
+typedef struct gt_frame {
+    uint32_t struct_size;
+    uint32_t width;
+    uint32_t height;
+    uint32_t device_buffers; /* 0: host pointers, 1: pointers into device memory */
+    float* rgb;
+    float* albedo;
+    float* normal;
+    double* rgb64;      /* host or device, f64 copy of rgb (useful with GT_PRECISION_F64) */
+    uint32_t* accepted; /* accepted (finite) samples per pixel */
+} gt_frame;
+
+/* BvhTraversalStats (raytracing/bvh.rs:9-17). */
+typedef struct gt_bvh_stats {
+    uint64_t rays;
+    uint64_t node_bounds_tests;
+    uint64_t node_bounds_hits;
+    uint64_t leaf_visits;
+    uint64_t primitive_candidates;
+    uint64_t leaf_hit_results;
+    uint64_t max_stack_depth;
+} gt_bvh_stats;
+
+/* Opaque handles. */
+typedef struct gt_context gt_context;
+typedef struct gt_scene gt_scene;
+typedef struct gt_lights gt_lights;
+typedef struct gt_environment gt_environment;
+
+/* ------------------------------------------------------------ entry points */
+
+/* ABI version of the loaded library (GT_ABI_VERSION). */
+uint32_t gt_abi_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* gt_last_error(void);
+
+/* Fills *camera with RayCamera::new(image_width, aspect_ratio) defaults
+ * (graphics/camera.rs:1034-1065). */
+gt_status gt_camera_default(uint32_t image_width, double aspect_ratio, gt_camera_desc* camera);
+
+/* Image height of RayCamera::initialized (graphics/camera.rs:1071) and the
+ * effective samples per pixel (camera.rs:1547-1556). */
+gt_status gt_camera_image_size(const gt_camera_desc* camera, uint32_t* width, uint32_t* height,
+                               uint32_t* samples_per_pixel);
+
+/* Creates a context on CUDA device `device` with its own stream. */
+gt_status gt_context_create(int device, gt_context** out);
+void gt_context_destroy(gt_context* context);
+
+/* Copies a RayScene to the device and builds its BVH on the host with the
+ * reference's binary SAH builder (RayScene::build_bvh_with_options,
+ * raytracing/scene.rs:1562-1565; FlatBvh::build, raytracing/bvh.rs:233-288). */
+gt_status gt_scene_create(gt_context* context, const gt_scene_desc* desc, gt_scene** out);
+void gt_scene_destroy(gt_scene* scene);
+
+/* RayScene::bvh_node_count (raytracing/scene.rs:1432-1437). */
+gt_status gt_scene_bvh_node_count(const gt_scene* scene, uint32_t* count);
+
+/* RayScene::emissive_targets (raytracing/scene.rs:1401-1423): one weight-1 target per
+ * primitive whose material is a DiffuseLight, in primitive order.  Writes at most
+ * `capacity` targets and the total count to *count. */
+gt_status gt_scene_emissive_targets(const gt_scene* scene, gt_light_target* targets,
+                                    uint32_t capacity, uint32_t* count);
+
+/* A SamplingTargetList / WeightedSamplingTargetList (raytracing/scene.rs:355-497). */
+gt_status gt_lights_create(gt_context* context, const gt_light_target* targets, uint32_t count,
+                           gt_lights** out);
+void gt_lights_destroy(gt_lights* lights);
+
+/* EnvironmentLight::new (raytracing/environment.rs:36-51) and its f32 extension. */
+gt_status gt_environment_create(gt_context* context, const gt_environment_desc* desc,
+                                gt_environment** out);
+void gt_environment_destroy(gt_environment* environment);
+
+/* Renders one frame.  Replaces, by which handles are passed:
+ *   lights = NULL, environment = NULL : PathTracer::render_hdr_image (renderer.rs:112-117)
+ *   lights != NULL                    : PathTracer::render_with_lights_hdr_image (renderer.rs:391-406)
+ *   environment != NULL               : PathTracer::render_with_environment_hdr_image (renderer.rs:431-449),
+ *                                       which forces next-event estimation (camera.rs:4171-4173)
+ *   both                              : render_with_lights_and_environment_hdr_image (renderer.rs:588-609)
+ * With opts->aovs = 1 it also fills frame->albedo / frame->normal like
+ * PathTracer::render_denoising_aovs (renderer.rs:121-129). */
+gt_status gt_render(gt_scene* scene, const gt_lights* lights, const gt_environment* environment,
+                    const gt_camera_desc* camera, const gt_render_opts* opts, gt_frame* frame);
+
+/* Closest-hit queries with traversal statistics on the reference-layout BVH in f64:
+ * RayScene::hit (raytracing/scene.rs:1639-1657) and
+ * RayScene::bvh_traversal_stats_for_rays (scene.rs:1478-1492).
+ * rays: count * 7 doubles (origin xyz, direction xyz, time), host memory.
+ * prim_ids[i] = primitive index or -1 on a miss; t may be NULL. */
+gt_status gt_trace_rays(gt_scene* scene, const double* rays, uint32_t count, double t_min,
+                        double t_max, int32_t* prim_ids, double* t, gt_bvh_stats* stats);
+
+/* Primary probe rays RayCamera::ray_for_pixel (graphics/camera.rs:1641-1653) for every
+ * `stride`-th pixel in x and y (the reference bench uses 4,
+ * benches/render_performance.rs:42-50), traced as gt_trace_rays does with
+ * Interval(0.001, inf).  prim_ids receives ceil(w/stride)*ceil(h/stride) entries in
+ * row-major probe order. */
+gt_status gt_trace_primary(gt_scene* scene, const gt_camera_desc* camera, uint32_t stride,
+                           int32_t* prim_ids, double* t, gt_bvh_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GARTUS_GPU_H */

@@ -1,0 +1,175 @@
+"""TEST INFRASTRUCTURE ONLY — ctypes access to the CPU oracle (gartus_oracle.hpp).
+
+The oracle restates the reference's f64 renderer on the CPU.  Only tests/, the smoke
+check in __graft_entry__ and bench.py's CPU-baseline leg may use it, and only as the
+checker or the timed CPU baseline, never as the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+import threading
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "liboracle.so"
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    srcs = [HERE / "gartus_oracle.hpp", HERE / "oracle_capi.cpp", HERE.parent / "include" / "gartus_gpu.h"]
+    if force or not LIB_PATH.exists() or any(s.stat().st_mtime > LIB_PATH.stat().st_mtime for s in srcs):
+        subprocess.run(["make", "-C", str(HERE), "-B" if force else "all"], check=True, capture_output=True)
+    return LIB_PATH
+
+
+def lib() -> C.CDLL:
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = C.CDLL(str(LIB_PATH))
+            vp, u32, i32, f64, u64 = C.c_void_p, C.c_uint32, C.c_int, C.c_double, C.c_uint64
+            sig = {
+                "orc_scene_create": (vp, [vp]),
+                "orc_scene_destroy": (None, [vp]),
+                "orc_scene_node_count": (u32, [vp]),
+                "orc_scene_bvh": (None, [vp, vp, vp, vp]),
+                "orc_trace_rays": (i32, [vp, vp, u32, f64, f64, i32, i32, vp, vp, vp, vp]),
+                "orc_camera": (i32, [vp, vp, vp, vp, vp]),
+                "orc_trace_primary": (i32, [vp, vp, u32, vp, vp, vp]),
+                "orc_render": (i32, [vp, vp, u32, vp, vp, i32, u32, u32, u32, u32, u32, i32, vp, vp, vp, vp]),
+                "orc_pixel_seed": (u64, [u64, u32, u32]),
+                "orc_rng_u64": (None, [u64, u32, vp]),
+                "orc_rng_double": (None, [u64, u32, vp]),
+                "orc_intersect": (i32, [vp, vp, f64, f64, vp]),
+                "orc_geometry_bounds": (None, [vp, vp]),
+                "orc_geometry_pdf": (f64, [vp, vp, f64, vp]),
+                "orc_lights_first_fraction": (f64, [vp, u32, vp, u64, u32]),
+                "orc_env_pdf": (f64, [vp, vp]),
+                "orc_ggx_d": (f64, [f64, f64]),
+                "orc_ggx_g": (f64, [f64, f64, f64]),
+                "orc_schlick": (f64, [f64, f64]),
+                "orc_dielectric_reflectance": (f64, [f64, f64]),
+                "orc_power_heuristic": (f64, [f64, f64]),
+                "orc_adaptive_error": (f64, [vp, u32]),
+                "orc_background": (None, [vp, vp, vp]),
+                "orc_scatter": (i32, [vp, vp, vp, vp, i32, u64, vp, vp, vp]),
+                "orc_scattering_pdf": (f64, [vp, vp, vp, vp, i32, vp]),
+                "orc_cosine_pdf": (f64, [vp, vp]),
+            }
+            for name, (res, args) in sig.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+        return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class OracleScene:
+    """A RayScene loaded into the oracle (f64 and f32 copies, reference BVH built)."""
+
+    def __init__(self, prims: np.ndarray, mats: np.ndarray, leaf_size: int = 4):
+        from gartus_gb300 import abi
+        self._prims = np.ascontiguousarray(prims)
+        self._mats = np.ascontiguousarray(mats)
+        d = abi.gt_scene_desc()
+        d.struct_size = C.sizeof(abi.gt_scene_desc)
+        d.num_primitives = len(self._prims)
+        d.primitives = self._prims.ctypes.data_as(C.POINTER(abi.gt_primitive))
+        d.num_materials = len(self._mats)
+        d.materials = self._mats.ctypes.data_as(C.POINTER(abi.gt_material))
+        d.bvh_leaf_size = leaf_size
+        self.h = lib().orc_scene_create(C.byref(d))
+        if not self.h:
+            raise ValueError("oracle rejected the scene")
+
+    @classmethod
+    def from_ray_scene(cls, scene) -> "OracleScene":
+        return cls(scene.primitives_array(), scene.materials_array(), scene.leaf_size)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_scene_destroy(self.h)
+            self.h = None
+
+    def node_count(self) -> int:
+        return lib().orc_scene_node_count(self.h)
+
+    def bvh(self):
+        n = self.node_count()
+        bounds = np.zeros((n, 6))
+        info = np.zeros((n, 3), dtype=np.uint32)
+        idx = np.zeros(len(self._prims), dtype=np.uint32)
+        lib().orc_scene_bvh(self.h, _ptr(bounds), _ptr(info), _ptr(idx))
+        return bounds, info, idx
+
+    def trace(self, rays: np.ndarray, t_min=0.001, t_max=np.inf, bruteforce=False, precision=1):
+        from gartus_gb300 import abi
+        rays = np.ascontiguousarray(rays, dtype=np.float64).reshape(-1, 7)
+        ids = np.empty(len(rays), dtype=np.int32)
+        t = np.empty(len(rays))
+        info = np.empty((len(rays), 8))
+        st = abi.gt_bvh_stats()
+        lib().orc_trace_rays(self.h, _ptr(rays), len(rays), t_min, t_max, int(bruteforce), precision, _ptr(ids),
+                             _ptr(t), _ptr(info), C.byref(st))
+        return ids, t, info, st.as_dict()
+
+    def trace_primary(self, camera_desc, stride=1):
+        from gartus_gb300 import abi
+        w, h, spp = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        out = np.zeros(18)
+        lib().orc_camera(C.byref(camera_desc), C.byref(w), C.byref(h), C.byref(spp), _ptr(out))
+        n = ((w.value + stride - 1) // stride) * ((h.value + stride - 1) // stride)
+        ids = np.empty(n, dtype=np.int32)
+        t = np.empty(n)
+        st = abi.gt_bvh_stats()
+        lib().orc_trace_primary(self.h, C.byref(camera_desc), stride, _ptr(ids), _ptr(t), C.byref(st))
+        return ids, t, st.as_dict()
+
+    def render(self, camera_desc, lights: np.ndarray | None = None, env=None, precision: int = 1,
+               threads: int = 1, window=(0, 0, 0, 0), aovs: bool = False):
+        """Renders (a window of) the image; returns (rgb, accepted[, albedo, normal])."""
+        w, h, spp = camera_size(camera_desc)
+        x0, y0, ww, hh = window
+        ww = ww or w
+        hh = hh or h
+        rgb = np.zeros((hh, ww, 3))
+        acc = np.zeros((hh, ww), dtype=np.uint32)
+        alb = np.zeros((hh, ww, 3)) if aovs else None
+        nrm = np.zeros((hh, ww, 3)) if aovs else None
+        lp = None
+        nl = 0
+        if lights is not None:
+            lights = np.ascontiguousarray(lights)
+            lp = _ptr(lights)
+            nl = len(lights)
+        envd = C.byref(env.desc()) if env is not None else None
+        rc = lib().orc_render(self.h, lp, nl, envd, C.byref(camera_desc), precision, threads, x0, y0, ww, hh,
+                              int(aovs), _ptr(rgb), _ptr(alb), _ptr(nrm), _ptr(acc))
+        if rc != 0:
+            raise RuntimeError(f"oracle render failed ({rc})")
+        if aovs:
+            return rgb, acc, alb, nrm
+        return rgb, acc
+
+
+def camera_size(camera_desc):
+    w, h, spp = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    out = np.zeros(18)
+    lib().orc_camera(C.byref(camera_desc), C.byref(w), C.byref(h), C.byref(spp), _ptr(out))
+    return w.value, h.value, spp.value
+
+
+def camera_vectors(camera_desc) -> np.ndarray:
+    w, h, spp = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    out = np.zeros(18)
+    lib().orc_camera(C.byref(camera_desc), C.byref(w), C.byref(h), C.byref(spp), _ptr(out))
+    return out.reshape(6, 3)

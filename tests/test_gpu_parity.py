@@ -1,0 +1,270 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle on the same inputs.
+
+Checks (from the spec contract):
+  1. primary-ray closest-hit primitive ids and BvhTraversalStats: bit-exact (f64 kernel);
+  2. per-pixel radiance under identical RNG streams: the f64 wavefront matches the oracle
+     to round-off; the f32 wavefront is within 1e-4 relative except on pixels where an f32
+     rounding flipped a discrete decision (counted, bounded);
+  3. converged images: relMSE of the f32 render against an f64 oracle render.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from gartus_gb300 import abi, scenes
+from gartus_gb300._lib import GartusError, lib
+from gartus_gb300.raytracing import (EnvironmentLight, PathTracer, RayCamera, RayGeometry, RayMaterial,
+                                     RayScene, SamplingTargetList)
+from tests.helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def relmse(x, r):
+    return float(np.mean((x - r) ** 2 / (r * r + 1e-2)))
+
+
+def probe_rays(seed):
+    rr = scenes.SampleRng(seed ^ 0x9E3779B97F4A7C15)  # graphics/raytracing.rs:1344-1358
+    rays = np.zeros((64, 7))
+    for i in range(64):
+        o = (rr.random_range(-4.0, 4.0), rr.random_range(-3.0, 3.0), rr.random_range(0.0, 3.0))
+        t = (rr.random_range(-3.0, 3.0), rr.random_range(-2.0, 2.0), rr.random_range(-8.0, -1.0))
+        rays[i, :3] = o
+        rays[i, 3:6] = (t[0] - o[0], t[1] - o[1], t[2] - o[2])
+    return rays
+
+
+# -------------------------------------------------------------- check 1: hits
+@pytest.mark.parametrize("name", ["final", "cornell", "bench"])
+def test_primary_hits_and_stats_bit_exact(gpu_context, name):
+    if name == "final":
+        scene, cam, stride = scenes.final_scene_ray_scene(), scenes.final_scene_camera(160, 1), 1
+    elif name == "cornell":
+        scene, cam, stride = scenes.cornell_scene()[0], scenes.cornell_camera(96, 1), 1
+    else:  # the reference bench's probe set: every 4th pixel (benches/render_performance.rs:42-50)
+        scene, cam, stride = scenes.render_performance_scene(), scenes.render_performance_camera(), 4
+    pt = PathTracer(cam, context=gpu_context)
+    ids, t, stats = pt.trace_primary(scene, stride)
+    o_ids, o_t, o_stats = oracle.OracleScene.from_ray_scene(scene).trace_primary(cam.desc(), stride)
+    np.testing.assert_array_equal(ids, o_ids)
+    np.testing.assert_array_equal(t, o_t)
+    assert stats == o_stats
+    assert scene.bvh_node_count(gpu_context) == oracle.OracleScene.from_ray_scene(scene).node_count()
+
+
+def test_randomized_scenes_match_oracle_and_bruteforce(gpu_context):
+    # graphics/raytracing.rs:1340-1370 on the GPU: BVH hits equal brute force, stats equal.
+    for seed in range(1, 17):
+        scene = scenes.randomized_ray_scene(seed)
+        rays = probe_rays(seed)
+        ids, t, stats = scene.hit_rays(rays, ctx=gpu_context)
+        o = oracle.OracleScene.from_ray_scene(scene)
+        o_ids, o_t, _, o_stats = o.trace(rays)
+        b_ids, b_t, _, _ = o.trace(rays, bruteforce=True)
+        np.testing.assert_array_equal(ids, o_ids)
+        np.testing.assert_array_equal(t, o_t)
+        np.testing.assert_array_equal(ids >= 0, b_ids >= 0)
+        assert stats == o_stats
+
+
+def test_empty_scene_trace_and_render(gpu_context):
+    scene = RayScene()
+    scene.add_material(RayMaterial.lambertian((0.5, 0.5, 0.5)))
+    ids, _, stats = scene.hit_rays(np.array([[0, 0, 0, 0, 0, -1, 0.0]]), ctx=gpu_context)
+    assert ids[0] == -1 and stats["rays"] == 1 and stats["node_bounds_tests"] == 0
+    cam = RayCamera(3, 1.0).with_background((4.0, 2.0, 0.25)).with_samples_per_pixel(2)
+    img = PathTracer(cam, context=gpu_context).render_hdr_image(scene)
+    assert (img.pixels == np.array([4.0, 2.0, 0.25], dtype=np.float32)).all()
+    assert (img.accepted == 2).all()
+
+
+# ------------------------------------------------------ check 2: same streams
+def _oracle_render(scene, cam, lights=None, env=None, precision=1, aovs=False):
+    o = oracle.OracleScene.from_ray_scene(scene)
+    la = lights.to_array() if lights is not None else None
+    return o.render(cam.desc(), la, env, precision=precision, threads=8, aovs=aovs)
+
+
+def _cases():
+    final = scenes.final_scene_ray_scene()
+    cornell, lights = scenes.cornell_scene()
+    bench = scenes.render_performance_scene()
+    return {
+        "final": (final, scenes.final_scene_camera(64, 4), None),
+        "cornell_mixture": (cornell, scenes.cornell_camera(40, 3, 50), lights),
+        "cornell_nee": (cornell, scenes.cornell_camera(32, 2, 50).with_direct_lighting_mode(
+            abi.GT_DIRECT_NEXT_EVENT_ESTIMATION), lights),
+        "bench": (bench, scenes.render_performance_camera(), None),
+    }
+
+
+@pytest.mark.parametrize("case", ["final", "cornell_mixture", "cornell_nee", "bench"])
+def test_f64_wavefront_matches_oracle(gpu_context, case):
+    scene, cam, lights = _cases()[case]
+    pt = PathTracer(cam, precision="f64", context=gpu_context)
+    img = pt.render_with_lights_hdr_image(scene, lights, want64=True) if lights else pt.render_hdr_image(
+        scene, want64=True)
+    ref, acc = _oracle_render(scene, cam, lights)
+    np.testing.assert_array_equal(img.accepted, acc)
+    err = rel_err(img.pixels64, ref, floor=1e-12).max(axis=2)
+    # Transcendentals (sin/cos/acos/atan2) may differ from glibc in the last ulp; that is
+    # the only source of difference, so nearly every pixel agrees to round-off.
+    assert (err <= 1e-9).mean() >= 0.995, (err > 1e-9).sum()
+    assert (err <= 1e-4).mean() >= 0.999
+
+
+@pytest.mark.parametrize("case", ["final", "cornell_mixture", "cornell_nee", "bench"])
+def test_f32_wavefront_same_streams(gpu_context, case):
+    scene, cam, lights = _cases()[case]
+    pt = PathTracer(cam, precision="f32", context=gpu_context)
+    img = pt.render_with_lights_hdr_image(scene, lights) if lights else pt.render_hdr_image(scene)
+    ref, acc = _oracle_render(scene, cam, lights)
+    err = rel_err(img.pixels, ref, floor=1e-3).max(axis=2)
+    within = (err <= 1e-4).mean()
+    # Divergent pixels: an f32 rounding flipped a Russian-roulette, Schlick, TIR, mixture
+    # or hit decision in one of the pixel's samples.  They are counted and bounded.
+    print(f"{case}: {within:.4%} of pixels within 1e-4 relative; divergent {int((err > 1e-4).sum())}")
+    assert within >= 0.95
+    assert np.isfinite(img.pixels).all()
+
+
+def test_converged_relmse_against_f64_oracle(gpu_context):
+    # Check 3: a converged f32 render against an independently seeded f64 oracle render.
+    scene, lights = scenes.cornell_scene()
+    cam = scenes.cornell_camera(24, 24, 50)
+    img = PathTracer(cam, context=gpu_context).render_with_lights_hdr_image(scene, lights)
+    ref, _ = _oracle_render(scene, cam.with_rng_seed(12345), lights)
+    e = relmse(img.pixels.astype(np.float64), ref)
+    print(f"relMSE f32 GPU vs f64 oracle (576 spp each): {e:.3e}")
+    assert e < 5e-3
+
+
+def test_aovs_match_oracle(gpu_context):
+    # render_denoising_aovs (camera.rs:4187-4244): albedo and normal AOVs.
+    scene = scenes.final_scene_ray_scene()
+    cam = scenes.final_scene_camera(48, 3)
+    aovs = PathTracer(cam, precision="f64", context=gpu_context).render_denoising_aovs(scene)
+    _, _, alb, nrm = _oracle_render(scene, cam, aovs=True)
+    np.testing.assert_allclose(aovs.albedo_linear, alb, rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(aovs.normal_linear, nrm, rtol=1e-6, atol=1e-6)
+
+
+def _env_u8(seed=3, w=16, h=8):
+    rng = np.random.default_rng(seed)
+    return rng.integers(0, 256, size=(h, w, 3), dtype=np.uint8)
+
+
+@pytest.mark.parametrize("fmt", ["srgb8", "rgb32f"])
+def test_environment_light_matches_oracle(gpu_context, fmt):
+    # render_with_environment_hdr_image (renderer.rs:431-449): forced NEE, env MIS.
+    texels = _env_u8()
+    if fmt == "rgb32f":
+        texels = (texels.astype(np.float32) / 255.0) ** 2 * 4.0
+    env = EnvironmentLight(texels)
+    scene = scenes.render_performance_scene()
+    cam = scenes.render_performance_camera().with_samples_per_pixel(3)
+    img = PathTracer(cam, precision="f64", context=gpu_context).render_with_environment_hdr_image(
+        scene, env, want64=True)
+    ref, acc = _oracle_render(scene, cam, env=env)
+    err = rel_err(img.pixels64, ref, floor=1e-12).max(axis=2)
+    assert (err <= 1e-9).mean() >= 0.99
+    assert (err <= 1e-4).mean() >= 0.995
+    img32 = PathTracer(cam, precision="f32", context=gpu_context).render_with_environment_hdr_image(scene, env)
+    err32 = rel_err(img32.pixels, ref, floor=1e-3).max(axis=2)
+    assert (err32 <= 1e-4).mean() >= 0.9
+
+
+def test_adaptive_sampling_matches_oracle(gpu_context):
+    # render_world_pixel_adaptive (camera.rs:2937-2982): Welford stopping rule.
+    scene = scenes.final_scene_ray_scene()
+    cam = scenes.final_scene_camera(40, 1).with_adaptive_sampling(4, 24, 0.05)
+    img = PathTracer(cam, precision="f64", context=gpu_context).render_hdr_image(scene, want64=True)
+    ref, acc = _oracle_render(scene, cam)
+    np.testing.assert_array_equal(img.accepted, acc)
+    err = rel_err(img.pixels64, ref, floor=1e-12).max(axis=2)
+    assert (err <= 1e-9).mean() >= 0.99
+
+
+def test_moving_spheres_and_checker(gpu_context):
+    scene = RayScene()
+    chk = scene.add_material(RayMaterial.checker_lambertian(0.5, (0.9, 0.9, 0.9), (0.2, 0.3, 0.1)))
+    scene.add_sphere((0.0, -100.5, -1.0), 100.0, chk)
+    blur = scene.add_material(RayMaterial.lambertian((0.7, 0.3, 0.3)))
+    scene.add_moving_sphere((0.0, 0.0, -1.0), (0.0, 0.3, -1.0), 0.5, blur)
+    iso = scene.add_material(RayMaterial.isotropic((0.5, 0.6, 0.7)))
+    scene.add_sphere((1.1, 0.0, -1.2), 0.3, iso)
+    scene.build_bvh()
+    cam = RayCamera(48, 1.5).with_samples_per_pixel(4).with_max_depth(8)
+    img = PathTracer(cam, precision="f64", context=gpu_context).render_hdr_image(scene, want64=True)
+    ref, _ = _oracle_render(scene, cam)
+    err = rel_err(img.pixels64, ref, floor=1e-12).max(axis=2)
+    assert (err <= 1e-9).mean() >= 0.99
+
+
+def test_edge_cases(gpu_context):
+    scene = scenes.final_scene_ray_scene()
+    # max_depth 0: the bounce loop never runs, every sample is black (camera.rs:1742).
+    img = PathTracer(scenes.final_scene_camera(8, 2).with_max_depth(0), context=gpu_context).render_hdr_image(scene)
+    assert (img.pixels == 0).all() and (img.accepted == 2).all()
+    # A 1x1 image.
+    img = PathTracer(RayCamera(1, 1.0).with_samples_per_pixel(3), context=gpu_context).render_hdr_image(scene)
+    assert img.pixels.shape == (1, 1, 3) and np.isfinite(img.pixels).all()
+    # Russian roulette off, deep paths.
+    cam = scenes.final_scene_camera(16, 2).without_russian_roulette().with_max_depth(30)
+    img = PathTracer(cam, precision="f64", context=gpu_context).render_hdr_image(scene, want64=True)
+    ref, _ = _oracle_render(scene, cam)
+    assert (rel_err(img.pixels64, ref, floor=1e-12).max(axis=2) <= 1e-9).mean() >= 0.99
+
+
+def test_invalid_arguments_return_status(gpu_context):
+    from gartus_gb300.raytracing import _SceneHandle, PRIMITIVE_DTYPE, MATERIAL_DTYPE
+    prims = np.zeros(1, dtype=PRIMITIVE_DTYPE)
+    prims[0]["geometry"]["kind"] = abi.GT_GEOM_SPHERE
+    prims[0]["geometry"]["p"][3] = 1.0
+    prims[0]["material"] = 3  # out of bounds (scene.rs:1158-1161 panics)
+    mats = np.zeros(1, dtype=MATERIAL_DTYPE)
+    with pytest.raises(GartusError) as e:
+        _SceneHandle(gpu_context, prims, mats, 4)
+    assert e.value.status == abi.GT_ERR_INVALID_ARG
+    # A frame whose size does not match the camera.
+    scene = scenes.final_scene_ray_scene()
+    cam = RayCamera(8, 1.0)
+    f = abi.gt_frame()
+    f.struct_size = C.sizeof(abi.gt_frame)
+    buf = np.zeros((9, 8, 3), dtype=np.float32)
+    f.width, f.height, f.rgb = 8, 9, buf.ctypes.data
+    st = lib().gt_render(scene._handle(gpu_context).h, None, None, C.byref(cam.desc()), None, C.byref(f))
+    assert st == abi.GT_ERR_INVALID_ARG
+    # Non-positive light weight (scene.rs:460-465).
+    lights = SamplingTargetList()
+    with pytest.raises(ValueError):
+        lights.add_target_weighted(RayGeometry.sphere((0, 0, 0), 1), 0.0)
+
+
+def test_progress_callback_can_cancel(gpu_context):
+    scene, lights = scenes.cornell_scene()
+    cam = scenes.cornell_camera(64, 8, 50)
+    calls = []
+
+    @abi.GT_PROGRESS_FN
+    def cb(user, done, total):
+        calls.append((done, total))
+        return 1  # cancel at the first report
+
+    f = abi.gt_frame()
+    f.struct_size = C.sizeof(abi.gt_frame)
+    buf = np.zeros((64, 64, 3), dtype=np.float32)
+    f.width, f.height, f.rgb = 64, 64, buf.ctypes.data
+    o = abi.gt_render_opts()
+    o.struct_size = C.sizeof(abi.gt_render_opts)
+    o.progress = cb
+    st = lib().gt_render(scene._handle(gpu_context).h, lights._handle(gpu_context).h, None, C.byref(cam.desc()),
+                         C.byref(o), C.byref(f))
+    assert st == abi.GT_ERR_CANCELLED and len(calls) == 1
+    # The context stays usable after a cancelled render.
+    img = PathTracer(scenes.cornell_camera(16, 1, 5), context=gpu_context).render_with_lights_hdr_image(scene, lights)
+    assert np.isfinite(img.pixels).all()
