@@ -43,21 +43,30 @@ def parse():
     ap.add_argument("--config", default="cornell", choices=["cornell", "final"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--schedule", default="auto", choices=["auto", "wavefront", "persistent"])
+    ap.add_argument("--width", type=int, default=0, help="smaller image for profiling runs (0 = the workload's)")
+    ap.add_argument("--grid", type=int, default=0, help="stratified grid width for profiling runs (0 = 16)")
+    ap.add_argument("--profile-run", action="store_true",
+                    help="render warmup+steps frames and print nothing else (for ncu captures)")
     return ap.parse_args()
 
 
-def workload(name):
+def workload(name, width=0, grid=0):
     from gartus_gb300 import scenes
     if name == "cornell":
         scene, lights = scenes.cornell_scene()
-        cam = scenes.cornell_camera(600, 16, 50)
-        cfg = {"workload": "cornell_box_ggx_glass", "width": 600, "height": 600, "spp": 256, "max_depth": 50,
-               "sampling": "stratified 16x16", "lights": "SamplingTargetList mixture (weight 0.5)",
+        width, grid = width or 600, grid or 16
+        cam = scenes.cornell_camera(width, grid, 50)
+        cfg = {"workload": "cornell_box_ggx_glass", "width": width, "height": width, "spp": grid * grid,
+               "max_depth": 50,
+               "sampling": f"stratified {grid}x{grid}", "lights": "SamplingTargetList mixture (weight 0.5)",
                "primitives": len(scene), "precision": "f32"}
         return scene, lights, cam, cfg
     scene = scenes.final_scene_ray_scene()
-    cam = scenes.final_scene_camera(400, 32)
-    cfg = {"workload": "final_scene_spheres", "width": 400, "height": 225, "spp": 32, "max_depth": 10,
+    width = width or 400
+    cam = scenes.final_scene_camera(width, 32)
+    cfg = {"workload": "final_scene_spheres", "width": width, "height": cam.image_size()[1], "spp": 32,
+           "max_depth": 10,
            "sampling": "random", "lights": "none (sky gradient)", "primitives": len(scene), "precision": "f32"}
     return scene, None, cam, cfg
 
@@ -171,7 +180,7 @@ def run_reference_arm(args):
         if rank != 0:
             dist.barrier()
             return
-    scene, lights, cam, cfg = workload(args.config)
+    scene, lights, cam, cfg = workload(args.config, args.width, args.grid)
     per_step = max(args.cpu_seconds / 3.0, 2.0)
     for _ in range(args.warmup):
         cpu_baseline(scene, lights, cam, 0.5)
@@ -219,8 +228,8 @@ def run_ours(args):
     device = local if world > 1 else 0
     torch.cuda.set_device(device)
     ctx = Context(device)
-    scene, lights, cam, cfg = workload(args.config)
-    pt = PathTracer(cam, context=ctx)
+    scene, lights, cam, cfg = workload(args.config, args.width, args.grid)
+    pt = PathTracer(cam, context=ctx, schedule=args.schedule)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
 
     def render():
@@ -233,9 +242,15 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize(device)
 
+    if args.profile_run:  # a fixed number of frames for an ncu capture; no timing, no output
+        for _ in range(args.warmup + args.steps):
+            render()
+        torch.cuda.synchronize(device)
+        return
     for _ in range(max(args.warmup, 3)):
         render()
-    kernels_per_iter = 4 if (cam.desc().direct_lighting_mode == abi.GT_DIRECT_NEXT_EVENT_ESTIMATION) else 3
+    nee_mode = cam.desc().direct_lighting_mode == abi.GT_DIRECT_NEXT_EVENT_ESTIMATION
+    kernels_per_iter = 0 if args.schedule != "wavefront" else (4 if nee_mode else 3)
     dev_ms, samples, rays, launches = 0.0, 0, 0, 0
     barrier()
     wall0 = time.perf_counter()
@@ -248,7 +263,7 @@ def run_ours(args):
             dev_ms += st["gpu_ms"]
             samples += st["samples"]
             rays += st["rays"] + st["shadow_rays"]
-            launches += 2 + st["iterations"] * kernels_per_iter
+            launches += (1 if args.schedule != "wavefront" else 2) + st["iterations"] * kernels_per_iter
     barrier()
     wall_s = time.perf_counter() - wall0
     clock = clocks.summary()
@@ -305,11 +320,11 @@ def run_ours(args):
     e2e = statistics.median(e2e_vals) * world
 
     # Roofline of the dominant kernel from one profiled frame (events around every launch).
-    prof = PathTracer(cam, context=ctx, profile=True)
+    prof = PathTracer(cam, context=ctx, profile=True, schedule=args.schedule)
     (prof.render_with_lights_hdr_image(scene, lights) if lights is not None else prof.render_hdr_image(scene))
     ps = prof.last_stats
     kms = ps["kernel_ms"]
-    dom = max(("trace", "shade", "generate", "shadow"), key=lambda k: kms[k])
+    dom = max(("trace", "shade", "generate", "shadow", "persistent"), key=lambda k: kms[k])
     ids, _, bstats = PathTracer(cam.with_samples_per_pixel(1), context=ctx).trace_primary(scene, 1)
     per_ray_nodes = bstats["node_bounds_tests"] / max(bstats["rays"], 1)
     per_ray_prims = bstats["primitive_candidates"] / max(bstats["rays"], 1)
@@ -318,8 +333,10 @@ def run_ours(args):
     s_prim = float(np.mean([s_by_kind[int(k)] for k in kinds])) if len(kinds) else 0.0
     b_ray = 32.0 * per_ray_nodes + s_prim * per_ray_prims + 64.0
     b_state = 2 * (32 + 12 + 8 + 4 + 4) + 8
-    bytes_per_unit = {"trace": b_ray, "shade": float(b_state), "generate": float(b_state), "shadow": b_ray}
-    units = {"trace": ps["rays"], "shade": ps["rays"], "generate": ps["samples_started"], "shadow": ps["shadow_rays"]}
+    bytes_per_unit = {"trace": b_ray, "shade": float(b_state), "generate": float(b_state), "shadow": b_ray,
+                      "persistent": b_ray}
+    units = {"trace": ps["rays"], "shade": ps["rays"], "generate": ps["samples_started"], "shadow": ps["shadow_rays"],
+             "persistent": ps["rays"] + ps["shadow_rays"]}
     launches_dom = max(ps["kernel_launches"][dom], 1)
     avg_ms = kms[dom] / launches_dom
     algo_bytes = units[dom] * bytes_per_unit[dom] / launches_dom
@@ -337,7 +354,7 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": dict(cfg, l2="flushed between timed steps (512 MiB write)",
+            "config": dict(cfg, l2="flushed between timed steps (512 MiB write)", schedule=args.schedule,
                            parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
             "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,

@@ -141,14 +141,20 @@ class gt_camera_desc(C.Structure):
 
 GT_PROGRESS_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.c_uint64)
 
+# gt_schedule
+GT_SCHEDULE_AUTO = 0
+GT_SCHEDULE_WAVEFRONT = 1
+GT_SCHEDULE_PERSISTENT = 2
+
 # gt_kernel_id
 GT_KERNEL_GENERATE = 0
 GT_KERNEL_TRACE = 1
 GT_KERNEL_SHADE = 2
 GT_KERNEL_SHADOW = 3
 GT_KERNEL_OTHER = 4
-GT_KERNEL_COUNT = 5
-KERNEL_NAMES = ["generate", "trace", "shade", "shadow", "other"]
+GT_KERNEL_PERSISTENT = 5
+GT_KERNEL_COUNT = 6
+KERNEL_NAMES = ["generate", "trace", "shade", "shadow", "other", "persistent"]
 
 
 class gt_render_stats(C.Structure):
@@ -181,6 +187,8 @@ class gt_render_opts(C.Structure):
         ("progress", GT_PROGRESS_FN),
         ("progress_user", C.c_void_p),
         ("stats", C.POINTER(gt_render_stats)),
+        ("schedule", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
 
 

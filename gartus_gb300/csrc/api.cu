@@ -2,6 +2,7 @@
 // reference's assert! panics become GT_ERR_INVALID_ARG), handle lifetimes, camera set-up
 // in f64 on the host, and dispatch to the f32 or f64 wavefront.
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <exception>
 #include <new>
@@ -228,6 +229,13 @@ gt_status gt_context_create(int device, gt_context** out) {
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&ctx->pinned), 64);
+    void* mapped = nullptr;
+    if (e == cudaSuccess) e = cudaHostAlloc(&mapped, 64, cudaHostAllocMapped);
+    if (e == cudaSuccess) {
+        std::memset(mapped, 0, 64);
+        ctx->mapped = static_cast<volatile uint32_t*>(mapped);
+        e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->mapped_dev), mapped, 0);
+    }
     if (e != cudaSuccess) {
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
@@ -244,6 +252,7 @@ void gt_context_destroy(gt_context* ctx) {
     cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->ws);
     cudaFreeHost(ctx->pinned);
+    cudaFreeHost(const_cast<uint32_t*>(ctx->mapped));
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -445,6 +454,10 @@ gt_status gt_render(gt_scene* s, const gt_lights* l, const gt_environment* e, co
         opts = *o;
     }
     if (opts.precision > GT_PRECISION_F64) return fail(GT_ERR_INVALID_ARG, "unknown precision");
+    if (opts.struct_size >= offsetof(gt_render_opts, schedule) + sizeof(uint32_t) &&
+        opts.schedule > GT_SCHEDULE_PERSISTENT)
+        return fail(GT_ERR_INVALID_ARG, "unknown schedule");
+    if (opts.struct_size < offsetof(gt_render_opts, schedule) + sizeof(uint32_t)) opts.schedule = GT_SCHEDULE_AUTO;
     if ((l && l->ctx != s->ctx) || (e && e->ctx != s->ctx))
         return fail(GT_ERR_INVALID_ARG, "lights, environment and scene must share a context");
     gt_status rc = validate_camera(*c);

@@ -60,6 +60,9 @@ struct gt_context {
     void* ws = nullptr; // render workspace (path state, queues, staging)
     size_t ws_bytes = 0;
     uint32_t* pinned = nullptr; // host-pinned copy of the loop counters
+    // Host memory mapped into the device: [0] cancel word, [1] pixels handed out.
+    volatile uint32_t* mapped = nullptr;
+    uint32_t* mapped_dev = nullptr;
 };
 
 struct gt_scene {

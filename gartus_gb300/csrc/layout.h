@@ -82,6 +82,7 @@ template <class R> struct EnvDev {
 // Camera and integrator constants for one render (camera.rs:613-643 after initialize()).
 template <class R> struct CamDev {
     R center[3], pixel00[3], du[3], dv[3], ddu[3], ddv[3];
+    R p00_rel[3]; // pixel00 - center, computed in f64 (the f32 camera's cancellation-free form)
     R shutter0, shutter1;
     R light_pdf_weight;
     R adaptive_threshold;

@@ -4,6 +4,8 @@
 // one translation unit per precision.
 #pragma once
 
+#include <time.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -336,6 +338,8 @@ template <class R> CamDev<R> cam_dev(const CamHost& h, bool use_lights, bool use
     put3(c.dv, h.dv);
     put3(c.ddu, h.ddu);
     put3(c.ddv, h.ddv);
+    double rel[3] = {h.pixel00[0] - h.center[0], h.pixel00[1] - h.center[1], h.pixel00[2] - h.center[2]};
+    put3(c.p00_rel, rel);
     const gt_camera_desc& d = h.desc;
     c.shutter0 = R(d.shutter_start);
     c.shutter1 = R(d.shutter_end);
@@ -465,6 +469,109 @@ struct EventPool {
     }
 };
 
+// Persistent schedule: one launch sized to fill every SM; with a progress callback the
+// host polls the mapped pixel counter while the kernel runs and can raise the cancel word.
+template <class R>
+gt_status run_persistent(gt_context* ctx, Params<R>& P, uint32_t* d_next, float* o_rgb, double* o_rgb64,
+                         uint32_t* o_acc, const gt_render_opts& opts, EventPool& ev, double* kms, uint64_t* klaunch) {
+    cudaStream_t st = ctx->stream;
+    const uint32_t n = P.ps.n;
+    GT_CUDA(cudaMemsetAsync(P.ps.counters, 0, C_COUNT * sizeof(uint32_t), st));
+    GT_CUDA(cudaMemsetAsync(P.ps.totals, 0, 4 * sizeof(unsigned long long), st));
+    GT_CUDA(cudaMemsetAsync(d_next, 0, sizeof(uint32_t), st));
+    // Cost-ordered pixel queues (the C_MAT counters hold the class sizes).
+    const uint32_t sms0 = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1);
+    const uint32_t cblocks = std::max<uint32_t>(1u, std::min<uint32_t>((n + 255) / 256, sms0 * 8));
+    k_classify<R><<<cblocks, 256, 0, st>>>(P, P.ps.q_mat, P.ps.counters + C_MAT);
+    GT_CUDA(cudaGetLastError());
+    ctx->mapped[0] = 0;
+    ctx->mapped[1] = 0;
+    int per_sm = 0;
+    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<R>, 128, 0));
+    const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1);
+    const uint32_t blocks = std::max<uint32_t>(1u, std::min<uint32_t>(sms * uint32_t(std::max(per_sm, 1)), (n + 127) / 128));
+    const bool profile = opts.profile != 0;
+    cudaEvent_t a = nullptr, z = nullptr;
+    GT_CUDA(ev.pair(a, z));
+    GT_CUDA(cudaEventRecord(a, st));
+    k_persistent<R><<<blocks, 128, 0, st>>>(P, d_next, P.ps.q_mat, P.ps.counters + C_MAT, ctx->mapped_dev,
+                                            ctx->mapped_dev + 1, o_rgb, o_rgb64, o_acc);
+    GT_CUDA(cudaGetLastError());
+    GT_CUDA(cudaEventRecord(z, st));
+    bool cancelled = false;
+    if (opts.progress) {
+        const uint32_t limit = P.cam.adaptive ? P.cam.adaptive_max : P.cam.spp;
+        for (;;) {
+            cudaError_t q = cudaEventQuery(z);
+            if (q == cudaSuccess) break;
+            if (q != cudaErrorNotReady) return cuda_fail(q, "persistent render");
+            struct timespec ts{0, 2000000};
+            nanosleep(&ts, nullptr);
+            const uint32_t handed = std::min<uint32_t>(uint32_t(ctx->mapped[1]), n);
+            if (!cancelled && opts.progress(opts.progress_user, uint64_t(handed) * limit, uint64_t(n) * limit)) {
+                ctx->mapped[0] = 1; // raise the cancel word: threads stop taking pixels
+                cancelled = true;
+            }
+        }
+    }
+    GT_CUDA(cudaEventSynchronize(z));
+    if (profile) {
+        ev.note(GT_KERNEL_PERSISTENT, a, z);
+        ev.harvest(kms, klaunch);
+    } else {
+        ev.free_events.push_back(a);
+        ev.free_events.push_back(z);
+    }
+    if (cancelled) return fail(GT_ERR_CANCELLED, "render cancelled by the progress callback");
+    return GT_OK;
+}
+
+// Copies results to host buffers, checks the device error word and fills the stats.
+template <class R>
+gt_status finish_render(gt_context* ctx, const Params<R>& P, gt_frame* frame, const gt_render_opts& opts,
+                        bool host_out, uint32_t n, float* o_rgb, double* o_rgb64, uint32_t* o_acc, float* o_alb,
+                        float* o_nrm, EventPool& ev, double* kms, uint64_t* klaunch, uint64_t iters) {
+    cudaStream_t st = ctx->stream;
+    GT_CUDA(cudaEventRecord(ev.end, st));
+    if (host_out) {
+        GT_CUDA(cudaMemcpyAsync(frame->rgb, o_rgb, size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (frame->rgb64)
+            GT_CUDA(cudaMemcpyAsync(frame->rgb64, o_rgb64, size_t(n) * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (frame->accepted)
+            GT_CUDA(cudaMemcpyAsync(frame->accepted, o_acc, size_t(n) * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        if (opts.aovs && frame->albedo)
+            GT_CUDA(cudaMemcpyAsync(frame->albedo, o_alb, size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (opts.aovs && frame->normal)
+            GT_CUDA(cudaMemcpyAsync(frame->normal, o_nrm, size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+    }
+    unsigned long long tot[4];
+    GT_CUDA(cudaMemcpyAsync(ctx->pinned + 2, P.ps.totals, sizeof(tot), cudaMemcpyDeviceToHost, st));
+    GT_CUDA(cudaMemcpyAsync(ctx->pinned, P.ps.counters + C_ERROR, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GT_CUDA(cudaStreamSynchronize(st));
+    if (ctx->pinned[0]) return fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
+    std::memcpy(tot, ctx->pinned + 2, sizeof(tot));
+    if (opts.stats) {
+        gt_render_stats& o = *opts.stats;
+        std::memset(&o, 0, sizeof(o));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev.begin, ev.end);
+        o.gpu_ms = ms;
+        o.iterations = iters;
+        o.rays = tot[0];
+        o.shadow_rays = tot[1];
+        o.samples = tot[2];
+        o.samples_started = tot[3];
+        if (opts.profile) {
+            ev.harvest(kms, klaunch);
+            for (int k = 0; k < GT_KERNEL_COUNT; ++k) {
+                o.kernel_ms[k] = kms[k];
+                o.kernel_launches[k] = klaunch[k];
+            }
+        }
+    }
+    return GT_OK;
+}
+
 template <class R>
 gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost& cam,
                       const gt_render_opts& opts, gt_frame* frame) {
@@ -489,16 +596,29 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     const uint32_t n = cam.width * cam.height;
     const bool nee = P.cam.nee && (use_lights || use_env);
 
-    // Workspace: path state, queues, and device staging for host outputs.
+    // Workspace: path state and queues (wavefront only), counters, and device staging
+    // for host outputs.
+    const bool persistent = opts.schedule != GT_SCHEDULE_WAVEFRONT;
     const bool host_out = frame->device_buffers == 0;
+    auto lay = [&](Bump& bb) {
+        if (persistent) {
+            P.ps.n = n;
+            P.ps.counters = bb.take<uint32_t>(C_COUNT);
+            P.ps.totals = bb.take<unsigned long long>(4);
+            P.ps.q_mat = bb.take<uint32_t>(size_t(n) * NUM_COST_CLASSES); // cost-ordered pixel queues
+        } else {
+            layout_state<R>(bb, P.ps, n, nee);
+        }
+        return bb.take<uint32_t>(1); // persistent pixel counter
+    };
     Bump sizing{nullptr};
-    layout_state<R>(sizing, P.ps, n, nee);
+    lay(sizing);
     sizing.take<float>(size_t(n) * 3 * 3);
     sizing.take<double>(size_t(n) * 3);
     sizing.take<uint32_t>(n);
     if ((rc = ensure_workspace(ctx, sizing.off + 4096)) != GT_OK) return rc;
     Bump b{static_cast<char*>(ctx->ws)};
-    layout_state<R>(b, P.ps, n, nee);
+    uint32_t* d_next = lay(b);
     float* d_rgb = b.take<float>(size_t(n) * 3);
     float* d_alb = b.take<float>(size_t(n) * 3);
     float* d_nrm = b.take<float>(size_t(n) * 3);
@@ -522,6 +642,23 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     double kms[GT_KERNEL_COUNT] = {0};
     uint64_t klaunch[GT_KERNEL_COUNT] = {0};
     GT_CUDA(cudaEventRecord(ev.begin, st));
+    if (persistent) {
+        rc = run_persistent<R>(ctx, P, d_next, o_rgb, o_rgb64, o_acc, opts, ev, kms, klaunch);
+        if (rc != GT_OK) return rc;
+        if (opts.aovs && (o_alb || o_nrm)) {
+            cudaEvent_t a = nullptr, z = nullptr;
+            if (profile) GT_CUDA(ev.pair(a, z));
+            if (profile) GT_CUDA(cudaEventRecord(a, st));
+            k_aov<R><<<slot_blocks, threads, 0, st>>>(P, o_alb, o_nrm);
+            GT_CUDA(cudaGetLastError());
+            if (profile) {
+                GT_CUDA(cudaEventRecord(z, st));
+                ev.note(GT_KERNEL_OTHER, a, z);
+            }
+        }
+        return finish_render<R>(ctx, P, frame, opts, host_out, n, o_rgb, o_rgb64, o_acc, o_alb, o_nrm, ev, kms,
+                                klaunch, 1);
+    }
     {
         cudaEvent_t a = nullptr, z = nullptr;
         if (profile) GT_CUDA(ev.pair(a, z));
@@ -635,44 +772,8 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             ev.note(GT_KERNEL_OTHER, a, z);
         }
     }
-    GT_CUDA(cudaEventRecord(ev.end, st));
-    if (host_out) {
-        GT_CUDA(cudaMemcpyAsync(frame->rgb, o_rgb, size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
-        if (frame->rgb64)
-            GT_CUDA(cudaMemcpyAsync(frame->rgb64, o_rgb64, size_t(n) * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
-        if (frame->accepted)
-            GT_CUDA(cudaMemcpyAsync(frame->accepted, o_acc, size_t(n) * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        if (opts.aovs && frame->albedo)
-            GT_CUDA(cudaMemcpyAsync(frame->albedo, o_alb, size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
-        if (opts.aovs && frame->normal)
-            GT_CUDA(cudaMemcpyAsync(frame->normal, o_nrm, size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
-    }
-    unsigned long long tot[4];
-    GT_CUDA(cudaMemcpyAsync(ctx->pinned + 2, P.ps.totals, sizeof(tot), cudaMemcpyDeviceToHost, st));
-    GT_CUDA(cudaMemcpyAsync(ctx->pinned, P.ps.counters + C_ERROR, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    GT_CUDA(cudaStreamSynchronize(st));
-    if (ctx->pinned[0]) return fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
-    std::memcpy(tot, ctx->pinned + 2, sizeof(tot));
-    if (opts.stats) {
-        gt_render_stats& o = *opts.stats;
-        std::memset(&o, 0, sizeof(o));
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ev.begin, ev.end);
-        o.gpu_ms = ms;
-        o.iterations = iters;
-        o.rays = tot[0];
-        o.shadow_rays = tot[1];
-        o.samples = tot[2];
-        o.samples_started = tot[3];
-        if (profile) {
-            ev.harvest(kms, klaunch);
-            for (int k = 0; k < GT_KERNEL_COUNT; ++k) {
-                o.kernel_ms[k] = kms[k];
-                o.kernel_launches[k] = klaunch[k];
-            }
-        }
-    }
-    return GT_OK;
+    return finish_render<R>(ctx, P, frame, opts, host_out, n, o_rgb, o_rgb64, o_acc, o_alb, o_nrm, ev, kms, klaunch,
+                            iters);
 }
 
 template <class R>

@@ -167,7 +167,7 @@ constexpr int kStackSize = 64;
 // order primitive index of the closest hit or -1; sets *err on stack overflow.
 template <class R, bool STATS, bool ANY>
 GT_DEV int traverse(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, R tmax, R& t_out, TraceStats* st,
-                    uint32_t* err) {
+                    uint32_t* err, bool any_hit = ANY) {
     RayT<R> rt = make_rayt(o, d);
     if (STATS) st->node_tests += 1;
     R root_entry;
@@ -204,7 +204,7 @@ GT_DEV int traverse(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, R t
                     closest = t;
                     best = int(first + k);
                     leaf_hit = true;
-                    if (ANY) {
+                    if (any_hit) {
                         t_out = closest;
                         return best;
                     }
@@ -638,8 +638,12 @@ template <class R> GT_DEV V3<R> background(const CamDev<R>& c, V3<R> dir) { // c
 }
 
 // -------------------------------------------------------------------- camera
-// ray_for_pixel_sample / ray_for_pixel_stratified_sample (camera.rs:1658-1704); returns
-// origin and direction, draws the time.
+// ray_for_pixel_sample / ray_for_pixel_stratified_sample (camera.rs:1658-1704): jitter,
+// optional defocus-disk origin, shutter time.  In f64 the direction is the reference's
+// pixel_sample - origin.  In f32 that difference of two points far from the world origin
+// cancels (a camera 800 units out with its viewport 1 unit ahead loses ~1e-4 relative),
+// so the f32 path builds the same vector from center-relative terms whose base,
+// pixel00 - center, was computed in f64.
 template <class R> GT_DEV void camera_ray(const CamDev<R>& c, uint32_t x, uint32_t y, uint32_t sample, Rng& g,
                                           V3<R>& o, V3<R>& d, R& time) {
     R ox, oy;
@@ -652,23 +656,32 @@ template <class R> GT_DEV void camera_ray(const CamDev<R>& c, uint32_t x, uint32
         ox = ((R(sx) + rnd<R>(g)) * rec) - R(0.5);
         oy = ((R(sy) + rnd<R>(g)) * rec) - R(0.5);
     }
-    V3<R> ps = (load3(c.pixel00) + load3(c.du) * (R(x) + ox)) + load3(c.dv) * (R(y) + oy);
-    V3<R> org = load3(c.center);
-    if (c.defocus) { // defocus_disk_sample + random_in_unit_disk (camera.rs:1710-1713, random.rs:141-152)
-        // Rejection sampling; each try is accepted with probability pi/4, so the cap of
-        // 4096 tries (reached with probability ~1e-2700) only bounds the loop.
-        V3<R> p{0, 0, 0};
+    const R fx = R(x) + ox, fy = R(y) + oy;
+    // Rejection sampling of the unit disk (random.rs:141-152); each try is accepted with
+    // probability pi/4, so the cap of 4096 tries (reached with probability ~1e-2700)
+    // only bounds the loop.
+    V3<R> p{0, 0, 0};
+    if (c.defocus) {
         for (int tries = 0; tries < 4096; ++tries) {
             R a = rnd_range<R>(g, R(-1), R(1));
             R b = rnd_range<R>(g, R(-1), R(1));
             p = V3<R>{a, b, R(0)};
             if (len2(p) < R(1)) break;
         }
-        org = (org + load3(c.ddu) * p.x) + load3(c.ddv) * p.y;
     }
     time = rnd_range<R>(g, c.shutter0, c.shutter1);
-    o = org;
-    d = ps - org;
+    if (sizeof(R) == sizeof(double)) {
+        V3<R> ps = (load3(c.pixel00) + load3(c.du) * fx) + load3(c.dv) * fy;
+        V3<R> org = load3(c.center);
+        if (c.defocus) org = (org + load3(c.ddu) * p.x) + load3(c.ddv) * p.y; // camera.rs:1710-1713
+        o = org;
+        d = ps - org;
+    } else {
+        V3<R> off{0, 0, 0};
+        if (c.defocus) off = load3(c.ddu) * p.x + load3(c.ddv) * p.y;
+        o = load3(c.center) + off;
+        d = ((load3(c.p00_rel) + load3(c.du) * fx) + load3(c.dv) * fy) - off;
+    }
 }
 
 } // namespace gt

@@ -196,118 +196,177 @@ template <class R> GT_DEV bool rr_survives(const CamDev<R>& cam, uint32_t bounce
     return true;
 }
 
-// One bounce of ray_color for `slot`.  Returns true if the path continues.
+// The in-flight state of one path (one sample of RayCamera::ray_color).
+template <class R> struct Path {
+    V3<R> o, d;
+    R time;
+    R miss_w; // miss_radiance_weight
+    V3<R> att, col;
+    uint32_t bounce;
+    bool allow_emit;
+};
+
+// Next-event shadow queries produced by a bounce: k = 0 area light (closest hit, the hit's
+// emission counts), k = 1 environment (occlusion only).  The contribution added to the
+// sample is att * ((s * e) * ratio) with e the emission found (area) or 1 (environment).
+template <class R> struct Shadow {
+    bool valid[2];
+    V3<R> o;
+    R time;
+    V3<R> dir[2];
+    V3<R> att;
+    V3<R> s[2];
+    R ratio[2];
+};
+
+// One iteration of the bounce loop of ray_color (camera.rs:1742-1859): miss radiance,
+// emission, scatter, next-event sampling (camera.rs:2225-2297), continuation sample
+// (camera.rs:165-195) and Russian roulette (camera.rs:2498-2523).  `prim` < 0 is a miss.
+// Returns true if the path continues to another bounce.
+template <class R>
+GT_DEV bool integrate_bounce(const Params<R>& P, Path<R>& p, int prim, R t, Rng& g, Shadow<R>& sh) {
+    sh.valid[0] = sh.valid[1] = false;
+    bool cont = false;
+    if (prim < 0) {
+        V3<R> bg = P.cam.use_env ? env_radiance(P.env, p.d) : background(P.cam, p.d);
+        V3<R> miss = bg * p.miss_w;
+        p.col = p.col + cmul(p.att, miss);
+        return false;
+    }
+    const HitRec<R> h = make_hit(P.sc, uint32_t(prim), p.o, p.d, p.time, t);
+    const MatDev<R> m = P.sc.mats[h.mat];
+    if (p.allow_emit) p.col = p.col + cmul(p.att, mat_emitted(m, h));
+    ScatterRec<R> s = mat_scatter(m, p.d, h, g);
+    if (s.kind == SC_SPECULAR) {
+        p.att = cmul(p.att, s.att);
+        p.o = h.p;
+        p.d = s.dir;
+        p.allow_emit = true;
+        p.miss_w = R(1);
+        cont = rr_survives(P.cam, p.bounce, p.att, g);
+    } else if (s.kind == SC_PDF) {
+        if (P.cam.nee) {
+            sh.o = h.p;
+            sh.time = p.time;
+            sh.att = p.att;
+            if (P.cam.use_lights) { // estimate_direct_lighting, camera.rs:2225-2262
+                V3<R> ldir = lights_dir(P.lights, h.p, p.time, g);
+                R lp = lights_pdf(P.lights, h.p, p.time, ldir);
+                if (Num<R>::finite(lp) && lp > R(kEps)) {
+                    R sp = mat_scattering_pdf(m, p.d, h, ldir);
+                    if (Num<R>::finite(sp) && sp > R(0)) {
+                        sh.valid[0] = true;
+                        sh.dir[0] = ldir;
+                        sh.s[0] = s.att;
+                        sh.ratio[0] = sp / lp;
+                    }
+                }
+            }
+            if (P.cam.use_env) { // estimate_environment_lighting, camera.rs:2264-2297
+                V3<R> edir;
+                R ep;
+                env_sample(P.env, g, edir, ep);
+                if (Num<R>::finite(ep) && ep > R(kEps)) {
+                    R sp = mat_scattering_pdf(m, p.d, h, edir);
+                    if (Num<R>::finite(sp) && sp > R(0)) {
+                        R mis = power_heuristic(ep, sp);
+                        sh.valid[1] = true;
+                        sh.dir[1] = edir;
+                        sh.s[1] = cmul(s.att, env_radiance(P.env, edir));
+                        sh.ratio[1] = mis * sp / ep;
+                    }
+                }
+            }
+        }
+        V3<R> dir;
+        R pdf;
+        bool suppress = false, weight_env = false;
+        if (!P.cam.nee && P.cam.use_lights) {
+            const R w = P.cam.light_pdf_weight;
+            if (rnd<R>(g) < w) dir = lights_dir(P.lights, h.p, p.time, g);
+            else dir = matpdf_generate(s.pdf, g);
+            pdf = w * lights_pdf(P.lights, h.p, p.time, dir) + (R(1) - w) * matpdf_value(s.pdf, dir);
+        } else {
+            dir = matpdf_generate(s.pdf, g);
+            pdf = matpdf_value(s.pdf, dir);
+            suppress = P.cam.nee && P.cam.use_lights;
+            weight_env = P.cam.nee && P.cam.use_env;
+        }
+        if (Num<R>::finite(pdf) && pdf > R(kEps)) {
+            R sp = mat_scattering_pdf(m, p.d, h, dir);
+            if (Num<R>::finite(sp) && sp > R(0)) {
+                R next_w = R(1);
+                if (weight_env) next_w = power_heuristic(pdf, env_pdf(P.env, dir));
+                p.att = cmul(p.att, s.att * (sp / pdf));
+                p.o = h.p;
+                p.d = dir;
+                p.allow_emit = !suppress;
+                p.miss_w = next_w;
+                cont = rr_survives(P.cam, p.bounce, p.att, g);
+            }
+        }
+    }
+    if (cont && p.bounce + 1 >= P.cam.max_depth) cont = false; // the bounce loop is exhausted
+    if (cont) p.bounce += 1;
+    return cont;
+}
+
+// Resolves shadow query k (after traversal) into the sample's radiance.
+template <class R> GT_DEV void apply_shadow(const Params<R>& P, V3<R>& col, const Shadow<R>& sh, int k, int prim, R t) {
+    if (k == 0) { // closest hit; the emission of whatever is hit (camera.rs:2248-2261)
+        if (prim < 0) return;
+        HitRec<R> h = make_hit(P.sc, uint32_t(prim), sh.o, sh.dir[0], sh.time, t);
+        V3<R> e = mat_emitted(P.sc.mats[h.mat], h);
+        if (!finite3(e)) return;
+        V3<R> direct = cmul(sh.s[0], e) * sh.ratio[0];
+        col = col + cmul(sh.att, direct);
+    } else { // occlusion only (camera.rs:2284-2293)
+        if (prim >= 0) return;
+        V3<R> direct = sh.s[1] * sh.ratio[1];
+        col = col + cmul(sh.att, direct);
+    }
+}
+
+// Wavefront shade step for `slot`: one bounce, pending shadow queries stored for k_shadow.
 template <class R> GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uint32_t key, bool& shadow) {
     uint4 st = P.ps.st[slot];
     Rng g{uint64_t(st.x) | (uint64_t(st.y) << 32)};
     uint32_t flags = st.z;
-    const uint32_t bounce = flags & F_BOUNCE_MASK;
     R4<R> ro = P.ps.ray_o[slot], rd = P.ps.ray_d[slot];
-    V3<R> o = xyz(ro), d = xyz(rd);
-    const R time = ro.w;
-    R miss_w = rd.w;
-    V3<R> att = xyz(P.ps.att[slot]);
-    V3<R> col = xyz(P.ps.col[slot]);
-    bool cont = false;
-    shadow = false;
+    Path<R> p;
+    p.o = xyz(ro);
+    p.d = xyz(rd);
+    p.time = ro.w;
+    p.miss_w = rd.w;
+    p.att = xyz(P.ps.att[slot]);
+    p.col = xyz(P.ps.col[slot]);
+    p.bounce = flags & F_BOUNCE_MASK;
+    p.allow_emit = (flags & F_ALLOW_EMIT) != 0;
+    Shadow<R> sh;
+    const int prim = key == KEY_MISS ? -1 : P.ps.hit_prim[slot];
+    const bool cont = integrate_bounce(P, p, prim, key == KEY_MISS ? R(0) : P.ps.hit_t[slot], g, sh);
     uint32_t sh_bits = 0;
-
-    if (key == KEY_MISS) {
-        V3<R> bg = P.cam.use_env ? env_radiance(P.env, d) : background(P.cam, d);
-        V3<R> miss = bg * miss_w;
-        col = col + cmul(att, miss);
-    } else {
-        const uint32_t prim = uint32_t(P.ps.hit_prim[slot]);
-        const HitRec<R> h = make_hit(P.sc, prim, o, d, time, P.ps.hit_t[slot]);
-        const MatDev<R> m = P.sc.mats[h.mat];
-        if (flags & F_ALLOW_EMIT) col = col + cmul(att, mat_emitted(m, h));
-        ScatterRec<R> s = mat_scatter(m, d, h, g);
-        if (s.kind == SC_SPECULAR) {
-            att = cmul(att, s.att);
-            o = h.p;
-            d = s.dir;
-            flags |= F_ALLOW_EMIT;
-            miss_w = R(1);
-            cont = rr_survives(P.cam, bounce, att, g);
-        } else if (s.kind == SC_PDF) {
-            if (P.cam.nee) {
-                if (P.cam.use_lights) { // estimate_direct_lighting, camera.rs:2225-2262
-                    V3<R> ldir = lights_dir(P.lights, h.p, time, g);
-                    R lp = lights_pdf(P.lights, h.p, time, ldir);
-                    if (Num<R>::finite(lp) && lp > R(kEps)) {
-                        R sp = mat_scattering_pdf(m, d, h, ldir);
-                        if (Num<R>::finite(sp) && sp > R(0)) {
-                            const size_t k = size_t(slot) * 2;
-                            P.ps.sh_o[k] = R4<R>{h.p.x, h.p.y, h.p.z, time};
-                            P.ps.sh_d[k] = R4<R>{ldir.x, ldir.y, ldir.z, R(1)};
-                            P.ps.sh_a[k] = R4<R>{att.x, att.y, att.z, sp / lp};
-                            P.ps.sh_s[k] = R4<R>{s.att.x, s.att.y, s.att.z, R(0)};
-                            sh_bits |= F_SHADOW0;
-                        }
-                    }
-                }
-                if (P.cam.use_env) { // estimate_environment_lighting, camera.rs:2264-2297
-                    V3<R> edir;
-                    R ep;
-                    env_sample(P.env, g, edir, ep);
-                    if (Num<R>::finite(ep) && ep > R(kEps)) {
-                        R sp = mat_scattering_pdf(m, d, h, edir);
-                        if (Num<R>::finite(sp) && sp > R(0)) {
-                            R mis = power_heuristic(ep, sp);
-                            V3<R> sr = cmul(s.att, env_radiance(P.env, edir));
-                            const size_t k = size_t(slot) * 2 + 1;
-                            P.ps.sh_o[k] = R4<R>{h.p.x, h.p.y, h.p.z, time};
-                            P.ps.sh_d[k] = R4<R>{edir.x, edir.y, edir.z, R(2)};
-                            P.ps.sh_a[k] = R4<R>{att.x, att.y, att.z, mis * sp / ep};
-                            P.ps.sh_s[k] = R4<R>{sr.x, sr.y, sr.z, R(0)};
-                            sh_bits |= F_SHADOW1;
-                        }
-                    }
-                }
-            }
-            // SamplingStrategy::continuation_sample (camera.rs:165-195)
-            V3<R> dir;
-            R pdf;
-            bool suppress = false, weight_env = false;
-            if (!P.cam.nee && P.cam.use_lights) {
-                const R w = P.cam.light_pdf_weight;
-                if (rnd<R>(g) < w) dir = lights_dir(P.lights, h.p, time, g);
-                else dir = matpdf_generate(s.pdf, g);
-                pdf = w * lights_pdf(P.lights, h.p, time, dir) + (R(1) - w) * matpdf_value(s.pdf, dir);
-            } else {
-                dir = matpdf_generate(s.pdf, g);
-                pdf = matpdf_value(s.pdf, dir);
-                suppress = P.cam.nee && P.cam.use_lights;
-                weight_env = P.cam.nee && P.cam.use_env;
-            }
-            if (Num<R>::finite(pdf) && pdf > R(kEps)) {
-                R sp = mat_scattering_pdf(m, d, h, dir);
-                if (Num<R>::finite(sp) && sp > R(0)) {
-                    R next_w = R(1);
-                    if (weight_env) next_w = power_heuristic(pdf, env_pdf(P.env, dir));
-                    att = cmul(att, s.att * (sp / pdf));
-                    o = h.p;
-                    d = dir;
-                    if (suppress) flags &= ~F_ALLOW_EMIT;
-                    else flags |= F_ALLOW_EMIT;
-                    miss_w = next_w;
-                    cont = rr_survives(P.cam, bounce, att, g);
-                }
-            }
-        }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        if (!sh.valid[k]) continue;
+        const size_t j = size_t(slot) * 2 + k;
+        P.ps.sh_o[j] = R4<R>{sh.o.x, sh.o.y, sh.o.z, sh.time};
+        P.ps.sh_d[j] = R4<R>{sh.dir[k].x, sh.dir[k].y, sh.dir[k].z, R(k + 1)};
+        P.ps.sh_a[j] = R4<R>{sh.att.x, sh.att.y, sh.att.z, sh.ratio[k]};
+        P.ps.sh_s[j] = R4<R>{sh.s[k].x, sh.s[k].y, sh.s[k].z, R(0)};
+        sh_bits |= k == 0 ? F_SHADOW0 : F_SHADOW1;
     }
-    if (cont && bounce + 1 >= P.cam.max_depth) cont = false; // the bounce loop is exhausted
-    flags &= ~(F_BOUNCE_MASK | F_TRACE | F_SHADOW0 | F_SHADOW1);
-    flags |= sh_bits;
+    flags &= ~(F_BOUNCE_MASK | F_TRACE | F_SHADOW0 | F_SHADOW1 | F_ALLOW_EMIT);
+    flags |= sh_bits | (p.allow_emit ? F_ALLOW_EMIT : 0u);
     if (cont) {
-        flags |= F_TRACE | ((bounce + 1) & F_BOUNCE_MASK);
-        P.ps.ray_o[slot] = R4<R>{o.x, o.y, o.z, time};
-        P.ps.ray_d[slot] = R4<R>{d.x, d.y, d.z, miss_w};
-        P.ps.att[slot] = R4<R>{att.x, att.y, att.z, R(0)};
+        flags |= F_TRACE | (p.bounce & F_BOUNCE_MASK);
+        P.ps.ray_o[slot] = R4<R>{p.o.x, p.o.y, p.o.z, p.time};
+        P.ps.ray_d[slot] = R4<R>{p.d.x, p.d.y, p.d.z, p.miss_w};
+        P.ps.att[slot] = R4<R>{p.att.x, p.att.y, p.att.z, R(0)};
     } else {
         flags |= F_NEWSAMPLE;
     }
-    P.ps.col[slot] = R4<R>{col.x, col.y, col.z, R(0)};
+    P.ps.col[slot] = R4<R>{p.col.x, p.col.y, p.col.z, R(0)};
     P.ps.st[slot] = make_uint4(uint32_t(g.s), uint32_t(g.s >> 32), flags, st.w);
     shadow = sh_bits != 0;
     return cont;
@@ -352,24 +411,19 @@ template <class R> __global__ void __launch_bounds__(256) k_shadow(Params<R> P) 
             if (!(st.z & (k == 0 ? F_SHADOW0 : F_SHADOW1))) continue;
             const size_t j = size_t(slot) * 2 + k;
             R4<R> so = P.ps.sh_o[j], sd = P.ps.sh_d[j], sa = P.ps.sh_a[j], ss = P.ps.sh_s[j];
-            V3<R> o = xyz(so), d = xyz(sd);
-            R t;
-            if (k == 0) { // closest hit; the emission of whatever is hit (camera.rs:2248-2261)
-                int prim = traverse<R, false, false>(P.sc, o, d, so.w, R(kShadowAcne), inf, t, nullptr,
-                                                     &P.ps.counters[C_ERROR]);
-                if (prim < 0) continue;
-                HitRec<R> h = make_hit(P.sc, uint32_t(prim), o, d, so.w, t);
-                V3<R> e = mat_emitted(P.sc.mats[h.mat], h);
-                if (!finite3(e)) continue;
-                V3<R> direct = cmul(xyz(ss), e) * sa.w;
-                col = col + cmul(xyz(sa), direct);
-            } else { // occlusion only (camera.rs:2284-2293)
-                int prim = traverse<R, false, true>(P.sc, o, d, so.w, R(kShadowAcne), inf, t, nullptr,
-                                                    &P.ps.counters[C_ERROR]);
-                if (prim >= 0) continue;
-                V3<R> direct = xyz(ss) * sa.w;
-                col = col + cmul(xyz(sa), direct);
-            }
+            Shadow<R> sh;
+            sh.o = xyz(so);
+            sh.time = so.w;
+            sh.att = xyz(sa);
+            sh.dir[k] = xyz(sd);
+            sh.s[k] = xyz(ss);
+            sh.ratio[k] = sa.w;
+            R t = R(0);
+            int prim = k == 0 ? traverse<R, false, false>(P.sc, sh.o, sh.dir[k], sh.time, R(kShadowAcne), inf, t,
+                                                          nullptr, &P.ps.counters[C_ERROR])
+                              : traverse<R, false, true>(P.sc, sh.o, sh.dir[k], sh.time, R(kShadowAcne), inf, t,
+                                                         nullptr, &P.ps.counters[C_ERROR]);
+            apply_shadow(P, col, sh, k, prim, t);
         }
         P.ps.col[slot] = R4<R>{col.x, col.y, col.z, R(0)};
         P.ps.st[slot].z = st.z & ~(F_SHADOW0 | F_SHADOW1);
@@ -414,6 +468,208 @@ __global__ void k_resolve(Params<R> P, float* rgb, double* rgb64, uint32_t* acce
             atomicAdd(&P.ps.totals[2], va);
             atomicAdd(&P.ps.totals[3], vs);
         }
+    }
+}
+
+// Pixel estimate from the running sums (camera.rs:2993-2999) or the Welford mean.
+template <class R> GT_DEV V3<R> pixel_estimate(const CamDev<R>& cam, R4<R> a, uint32_t acc_n) {
+    if (cam.adaptive) return xyz(a);
+    return acc_n == 0 ? V3<R>{0, 0, 0} : cdiv(xyz(a), R(acc_n));
+}
+
+// Register form of finish_sample: folds one sample into the pixel's sums.
+template <class R> GT_DEV bool fold_sample(const CamDev<R>& cam, R4<R>& a, R4<R>& c, uint32_t& acc_n, V3<R> s) {
+    if (!finite3(s)) return false;
+    acc_n += 1;
+    if (cam.adaptive) {
+        V3<R> mean = xyz(a), m2 = xyz(c);
+        V3<R> delta = s - mean;
+        mean = mean + cdiv(delta, R(acc_n));
+        V3<R> delta2 = s - mean;
+        m2 = m2 + cmul(delta, delta2);
+        a = R4<R>{mean.x, mean.y, mean.z, R(0)};
+        c = R4<R>{m2.x, m2.y, m2.z, R(0)};
+        return acc_n >= cam.adaptive_min && adaptive_error(m2, acc_n) < cam.adaptive_threshold;
+    }
+    kahan_add(a, c, s);
+    return false;
+}
+
+// Cost classes for the persistent schedule's pixel order.  A pixel's samples form one
+// sequential chain, so the frame can finish no sooner than its longest chain; pixels whose
+// centre ray sees glass (long specular paths, Russian roulette surviving at 0.95) start
+// first, then metal, glossy, diffuse, and emitters or misses last.
+enum : uint32_t { NUM_COST_CLASSES = 5 };
+GT_DEV uint32_t cost_class(int prim_kind_or_miss) {
+    switch (prim_kind_or_miss) {
+    case 5: return 0; // Dielectric
+    case 4: return 1; // Metal
+    case 3: return 2; // GGX
+    case 0:           // Lambertian
+    case 2: return 3; // Isotropic
+    default: return 4; // DiffuseLight or a miss
+    }
+}
+
+template <class R> __global__ void __launch_bounds__(256) k_classify(Params<R> P, uint32_t* queues, uint32_t* counts) {
+    const uint32_t n = P.cam.width * P.cam.height;
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const R inf = Num<R>::inf();
+    for (uint32_t base = warp0; base < n; base += stride) {
+        const uint32_t pix = base + lane_id();
+        uint32_t key = 0;
+        if (pix < n) {
+            const R x = R(pix % P.cam.width), y = R(pix / P.cam.width);
+            V3<R> d = (load3(P.cam.p00_rel) + load3(P.cam.du) * x) + load3(P.cam.dv) * y;
+            R t;
+            const int prim = traverse<R, false, false>(P.sc, load3(P.cam.center), d, P.cam.shutter0, R(kShadowAcne), inf,
+                                                       t, nullptr, &P.ps.counters[C_ERROR]);
+            key = cost_class(prim < 0 ? -1 : P.sc.mats[__ldg(&P.sc.meta[prim].x) >> 3].kind);
+        }
+        warp_push_keyed(pix < n, key, pix, queues, n, counts);
+    }
+}
+
+// Persistent schedule: the whole frame in one launch.  Each thread takes pixels in cost
+// order from a device counter and runs that pixel's samples in order in registers (the
+// pixel's stream is sequential, camera.rs:2669).  Every loop iteration traces exactly one
+// ray through one traversal call site — the live path's next ray or one of its pending
+// next-event shadow rays — so lanes on different samples, pixels or ray kinds stay on the
+// same instructions.  `cancel` is polled at each pixel fetch; `progress` receives the
+// number of pixels handed out.
+template <class R>
+__global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next, const uint32_t* queues,
+                                                    const uint32_t* class_counts, const volatile uint32_t* cancel,
+                                                    volatile uint32_t* progress, float* rgb, double* rgb64,
+                                                    uint32_t* accepted) {
+    const uint32_t n = P.cam.width * P.cam.height;
+    const uint32_t limit = P.cam.adaptive ? P.cam.adaptive_max : P.cam.spp;
+    const R inf = Num<R>::inf();
+    uint32_t prefix[NUM_COST_CLASSES + 1];
+    prefix[0] = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < NUM_COST_CLASSES; ++k) prefix[k + 1] = prefix[k] + class_counts[k];
+    auto fetch = [&]() -> uint32_t {
+        if (cancel && *cancel) return n;
+        const uint32_t i = atomicAdd(next, 1u);
+        if (i >= n) return n;
+        if (progress && (i & 1023u) == 0) *progress = i;
+        uint32_t k = 0;
+#pragma unroll
+        for (uint32_t c = 1; c < NUM_COST_CLASSES; ++c)
+            if (i >= prefix[c]) k = c;
+        return queues[size_t(k) * n + (i - prefix[k])];
+    };
+    unsigned long long n_rays = 0, n_shadow = 0, n_acc = 0, n_started = 0;
+    uint32_t pix = fetch();
+    Rng g{0};
+    R4<R> a{0, 0, 0, 0}, c{0, 0, 0, 0};
+    uint32_t acc_n = 0, started = 0;
+    if (pix < n) g.s = pixel_seed(P.cam.seed, pix % P.cam.width, pix / P.cam.width);
+    Path<R> p;
+    Shadow<R> sh;
+    uint32_t pending = 0; // bit k: shadow query k still to trace
+    bool cont = false;
+    bool need_sample = true;
+    bool alive = pix < n;
+    // The loop is warp-uniform and reconverges at each phase boundary (__syncwarp), so
+    // the warp executes setup, one traversal and one integration step together instead
+    // of drifting apart into sub-warps at different instructions.
+    while (__any_sync(0xffffffffu, alive)) {
+        if (alive && need_sample) {
+            bool stop = false;
+            if (started > 0) stop = fold_sample(P.cam, a, c, acc_n, p.col);
+            bool got = false;
+            for (;;) {
+                const uint32_t x = pix % P.cam.width, y = pix / P.cam.width;
+                while (!stop && started < limit) {
+                    camera_ray(P.cam, x, y, started, g, p.o, p.d, p.time);
+                    ++started;
+                    if (P.cam.max_depth == 0) { // the bounce loop never runs: a black sample
+                        stop = fold_sample(P.cam, a, c, acc_n, V3<R>{0, 0, 0});
+                        continue;
+                    }
+                    p.att = V3<R>{1, 1, 1};
+                    p.col = V3<R>{0, 0, 0};
+                    p.miss_w = R(1);
+                    p.bounce = 0;
+                    p.allow_emit = true;
+                    got = true;
+                    break;
+                }
+                if (got) break;
+                // The pixel is finished: write it and take the next one.
+                const V3<R> v = pixel_estimate(P.cam, a, acc_n);
+                if (rgb) {
+                    rgb[size_t(pix) * 3 + 0] = float(v.x);
+                    rgb[size_t(pix) * 3 + 1] = float(v.y);
+                    rgb[size_t(pix) * 3 + 2] = float(v.z);
+                }
+                if (rgb64) {
+                    rgb64[size_t(pix) * 3 + 0] = double(v.x);
+                    rgb64[size_t(pix) * 3 + 1] = double(v.y);
+                    rgb64[size_t(pix) * 3 + 2] = double(v.z);
+                }
+                if (accepted) accepted[pix] = acc_n;
+                n_acc += acc_n;
+                n_started += started;
+                pix = fetch();
+                if (pix >= n) {
+                    alive = false;
+                    break;
+                }
+                g.s = pixel_seed(P.cam.seed, pix % P.cam.width, pix / P.cam.width);
+                a = R4<R>{0, 0, 0, 0};
+                c = R4<R>{0, 0, 0, 0};
+                acc_n = 0;
+                started = 0;
+                stop = false;
+            }
+            need_sample = false;
+        }
+        __syncwarp();
+        // One traversal per iteration: a pending shadow query first (area, then
+        // environment, in the reference's order), otherwise the path's next ray.
+        const int which = (pending & 1u) ? 0 : ((pending & 2u) ? 1 : -1);
+        R t = R(0);
+        int prim = -1;
+        if (alive) {
+            const V3<R> ro = which >= 0 ? sh.o : p.o;
+            const V3<R> rd = which >= 0 ? sh.dir[which] : p.d;
+            const R rt = which >= 0 ? sh.time : p.time;
+            prim = traverse<R, false, false>(P.sc, ro, rd, rt, R(kShadowAcne), inf, t, nullptr,
+                                             &P.ps.counters[C_ERROR], which == 1);
+        }
+        __syncwarp();
+        if (alive) {
+            if (which >= 0) {
+                apply_shadow(P, p.col, sh, which, prim, t);
+                pending &= ~(1u << which);
+                ++n_shadow;
+            } else {
+                ++n_rays;
+                cont = integrate_bounce(P, p, prim, t, g, sh);
+                pending = (sh.valid[0] ? 1u : 0u) | (sh.valid[1] ? 2u : 0u);
+            }
+            if (pending == 0 && !cont) need_sample = true;
+        }
+        __syncwarp();
+    }
+    // Throughput totals: warp-reduce, one atomic per warp (every lane of the launch's
+    // full warps arrives here).
+    __syncwarp();
+    for (int off = 16; off > 0; off >>= 1) {
+        n_rays += __shfl_down_sync(0xffffffffu, n_rays, off);
+        n_shadow += __shfl_down_sync(0xffffffffu, n_shadow, off);
+        n_acc += __shfl_down_sync(0xffffffffu, n_acc, off);
+        n_started += __shfl_down_sync(0xffffffffu, n_started, off);
+    }
+    if (lane_id() == 0) {
+        atomicAdd(&P.ps.totals[0], n_rays);
+        atomicAdd(&P.ps.totals[1], n_shadow);
+        atomicAdd(&P.ps.totals[2], n_acc);
+        atomicAdd(&P.ps.totals[3], n_started);
     }
 }
 

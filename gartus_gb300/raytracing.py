@@ -711,14 +711,20 @@ class PathTracer:
 
     precision: "f32" (throughput) or "f64" (the reference's arithmetic, op for op)."""
 
+    SCHEDULES = {"auto": abi.GT_SCHEDULE_AUTO, "wavefront": abi.GT_SCHEDULE_WAVEFRONT,
+                 "persistent": abi.GT_SCHEDULE_PERSISTENT}
+
     def __init__(self, camera: RayCamera, options: RenderOptions = RenderOptions(), precision: str = "f32",
-                 context: Optional[Context] = None, profile: bool = False):
+                 context: Optional[Context] = None, profile: bool = False, schedule: str = "auto"):
         if precision not in ("f32", "f64"):
             raise ValueError("precision must be 'f32' or 'f64'")
+        if schedule not in self.SCHEDULES:
+            raise ValueError(f"schedule must be one of {sorted(self.SCHEDULES)}")
         self.camera = camera
         self.options = options
         self.precision = precision
         self.profile = profile
+        self.schedule = schedule
         self._ctx = context
         self.last_stats: Optional[dict] = None
 
@@ -727,7 +733,7 @@ class PathTracer:
         return self._ctx or Context.default()
 
     def with_options(self, options: RenderOptions) -> "PathTracer":
-        return PathTracer(self.camera, options, self.precision, self._ctx, self.profile)
+        return PathTracer(self.camera, options, self.precision, self._ctx, self.profile, self.schedule)
 
     def _render(self, world: RayScene, lights: Optional[WeightedSamplingTargetList],
                 environment: Optional[EnvironmentLight], aovs: bool = False, want64: bool = False):
@@ -751,6 +757,7 @@ class PathTracer:
         o.precision = abi.GT_PRECISION_F64 if self.precision == "f64" else abi.GT_PRECISION_F32
         o.aovs = 1 if aovs else 0
         o.profile = 1 if self.profile else 0
+        o.schedule = self.SCHEDULES[self.schedule]
         stats = abi.gt_render_stats()
         o.stats = C.pointer(stats)
         sh = world._handle(ctx)
@@ -791,8 +798,8 @@ class PathTracer:
     # render_with_light_connections (renderer.rs:771-786): forces NEE
     def render_with_light_connections_hdr_image(self, world, lights, want64: bool = False) -> HdrImage:
         cam = self.camera.with_direct_lighting_mode(abi.GT_DIRECT_NEXT_EVENT_ESTIMATION)
-        return PathTracer(cam, self.options, self.precision, self._ctx, self.profile)._render(world, lights, None,
-                                                                                           want64=want64)
+        return PathTracer(cam, self.options, self.precision, self._ctx, self.profile, self.schedule)._render(
+            world, lights, None, want64=want64)
 
     # render_with_environment_hdr_image (renderer.rs:431-449)
     def render_with_environment_hdr_image(self, world: RayScene, environment: EnvironmentLight,

@@ -204,7 +204,8 @@ typedef enum gt_kernel_id {
     GT_KERNEL_SHADE = 2,    /* one bounce of the integrator per path       */
     GT_KERNEL_SHADOW = 3,   /* deferred next-event shadow queries          */
     GT_KERNEL_OTHER = 4,    /* init, resolve, AOVs                         */
-    GT_KERNEL_COUNT = 5
+    GT_KERNEL_PERSISTENT = 5, /* the persistent schedule's single kernel   */
+    GT_KERNEL_COUNT = 6
 } gt_kernel_id;
 
 typedef struct gt_render_stats {
@@ -218,6 +219,13 @@ typedef struct gt_render_stats {
     uint64_t kernel_launches[GT_KERNEL_COUNT];
 } gt_render_stats;
 
+/* How the frame is scheduled on the GPU.  Both give identical images. */
+typedef enum gt_schedule {
+    GT_SCHEDULE_AUTO = 0,       /* the persistent kernel                                        */
+    GT_SCHEDULE_WAVEFRONT = 1,  /* per-bounce kernels over material-binned queues, graph-replayed */
+    GT_SCHEDULE_PERSISTENT = 2  /* one launch; threads pull pixels and run their paths in registers */
+} gt_schedule;
+
 typedef struct gt_render_opts {
     uint32_t struct_size;
     uint32_t precision;   /* gt_precision */
@@ -226,6 +234,8 @@ typedef struct gt_render_opts {
     gt_progress_fn progress;
     void* progress_user;
     gt_render_stats* stats; /* optional output */
+    uint32_t schedule;      /* gt_schedule */
+    uint32_t reserved;
 } gt_render_opts;
 
 /* Caller-owned output images, row-major, 3 channels, y = 0 is the top row

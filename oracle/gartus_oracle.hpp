@@ -1242,6 +1242,7 @@ template <class R> struct Camera {
     gt_camera_desc desc;
     uint32_t width = 0, height = 0;
     V3<R> center, pixel00, du, dv, ddu, ddv;
+    V3<R> p00_rel; // pixel00 - center in f64, reduced to R (used by the f32 evaluation)
 
     // RayCamera::initialized (camera.rs:1068-1130); computed in f64 then reduced to R.
     void init(const gt_camera_desc& d) {
@@ -1268,6 +1269,7 @@ template <class R> struct Camera {
         auto cv = [](V3<double> a) { return V3<R>(R(a.x), R(a.y), R(a.z)); };
         center = cv(c);
         pixel00 = cv(p00);
+        p00_rel = cv(p00 - c);
         du = cv(pdu);
         dv = cv(pdv);
         ddu = cv(u * dr);
@@ -1289,28 +1291,34 @@ template <class R> struct Camera {
         V3<R> pc = (pixel00 + du * R(x)) + dv * R(y);
         return Ray<R>{center, pc - center, R(desc.shutter_start)};
     }
-    Ray<R> finish_ray(V3<R> ps, SampleRng& rng) const { // camera.rs:1658-1670 tail
-        V3<R> origin = center;
-        if (!(desc.defocus_angle <= 0.0)) {
-            V3<R> p = rng.random_in_unit_disk<R>();
-            origin = (center + ddu * p.x) + ddv * p.y;
-        }
+    // camera.rs:1658-1670 tail.  In f64 the direction is pixel_sample - origin as the
+    // reference computes it.  In f32 that difference of two points far from the origin
+    // cancels (a camera 800 units out with a viewport 1 unit ahead loses ~1e-4), so the
+    // f32 evaluation forms the same vector from center-relative terms instead.
+    Ray<R> finish_ray(R sx, R sy, SampleRng& rng) const {
+        const bool defocus = !(desc.defocus_angle <= 0.0);
+        V3<R> p;
+        if (defocus) p = rng.random_in_unit_disk<R>();
         R time = rng.random_range<R>(R(desc.shutter_start), R(desc.shutter_end));
-        return Ray<R>{origin, ps - origin, time};
+        if (sizeof(R) == sizeof(double)) {
+            V3<R> ps = (pixel00 + du * sx) + dv * sy;
+            V3<R> origin = defocus ? (center + ddu * p.x) + ddv * p.y : center;
+            return Ray<R>{origin, ps - origin, time};
+        }
+        V3<R> off = defocus ? ddu * p.x + ddv * p.y : V3<R>();
+        return Ray<R>{center + off, ((p00_rel + du * sx) + dv * sy) - off, time};
     }
     Ray<R> ray_for_pixel_sample(uint32_t x, uint32_t y, SampleRng& rng) const {
         R ox = rng.random_double<R>() - R(0.5);
         R oy = rng.random_double<R>() - R(0.5);
-        V3<R> ps = (pixel00 + du * (R(x) + ox)) + dv * (R(y) + oy);
-        return finish_ray(ps, rng);
+        return finish_ray(R(x) + ox, R(y) + oy, rng);
     }
     Ray<R> ray_for_pixel_stratified(uint32_t x, uint32_t y, uint32_t sx, uint32_t sy, uint32_t g,
                                     SampleRng& rng) const { // camera.rs:1672-1704
         R rec = R(1) / R(g);
         R ox = ((R(sx) + rng.random_double<R>()) * rec) - R(0.5);
         R oy = ((R(sy) + rng.random_double<R>()) * rec) - R(0.5);
-        V3<R> ps = (pixel00 + du * (R(x) + ox)) + dv * (R(y) + oy);
-        return finish_ray(ps, rng);
+        return finish_ray(R(x) + ox, R(y) + oy, rng);
     }
 };
 
