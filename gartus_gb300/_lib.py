@@ -48,6 +48,8 @@ def _declare(L: C.CDLL) -> None:
                                C.c_void_p, P(abi.gt_bvh_stats)]),
         "gt_trace_primary": (st, [C.c_void_p, P(abi.gt_camera_desc), C.c_uint32, C.c_void_p, C.c_void_p,
                                   P(abi.gt_bvh_stats)]),
+        "gt_render_noalloc": (st, [C.c_void_p, C.c_void_p, C.c_void_p, P(abi.gt_camera_desc), C.c_void_p,
+                                   C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -82,5 +84,5 @@ EXPORTED_SYMBOLS = [
     "gt_abi_version", "gt_last_error", "gt_camera_default", "gt_camera_image_size", "gt_context_create",
     "gt_context_destroy", "gt_scene_create", "gt_scene_destroy", "gt_scene_bvh_node_count",
     "gt_scene_emissive_targets", "gt_lights_create", "gt_lights_destroy", "gt_environment_create",
-    "gt_environment_destroy", "gt_render", "gt_trace_rays", "gt_trace_primary",
+    "gt_environment_destroy", "gt_render", "gt_trace_rays", "gt_trace_primary", "gt_render_noalloc",
 ]

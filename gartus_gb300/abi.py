@@ -141,6 +141,8 @@ class gt_camera_desc(C.Structure):
 
 GT_PROGRESS_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.c_uint64)
 
+GT_NOALLOC_MAX_PIXELS = 1048576
+
 # gt_schedule
 GT_SCHEDULE_AUTO = 0
 GT_SCHEDULE_WAVEFRONT = 1

@@ -30,6 +30,7 @@ UNITS = [
     ("api.cu", []),
     ("render_f32.cu", ["-fmad=true"]),
     ("render_f64.cu", ["-fmad=false"]),
+    ("noalloc.cu", ["-fmad=true"]),
 ]
 CXX_UNITS = ["bvh_build.cpp"]
 

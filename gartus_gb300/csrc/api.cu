@@ -142,6 +142,7 @@ gt_status validate_geometry(const gt_geometry& g) {
 } // namespace
 
 void set_error(const std::string& msg) { g_last_error = msg; }
+CamHost camera_setup(const gt_camera_desc& d, bool env) { return init_camera(d, env); }
 gt_status fail(gt_status status, const std::string& msg) {
     g_last_error = msg;
     return status;

@@ -47,6 +47,8 @@ struct CamHost {
 };
 
 void set_error(const std::string& msg);
+// RayCamera::initialized in f64 for an already validated camera (api.cu).
+CamHost camera_setup(const gt_camera_desc& d, bool env);
 gt_status fail(gt_status status, const std::string& msg);
 gt_status cuda_fail(cudaError_t e, const char* what);
 

@@ -342,6 +342,33 @@ gt_status gt_trace_rays(gt_scene* scene, const double* rays, uint32_t count, dou
 gt_status gt_trace_primary(gt_scene* scene, const gt_camera_desc* camera, uint32_t stride,
                            int32_t* prim_ids, double* t, gt_bvh_stats* stats);
 
+/* Largest image gt_render_noalloc accepts (1024 x 1024 pixels). */
+#define GT_NOALLOC_MAX_PIXELS 1048576u
+
+/* Renders one f32 frame without allocating any memory.  It has no counterpart in the
+ * reference; it exists for callers that cannot allocate device memory while they render:
+ * a real-time loop that must not pay cudaMalloc's latency and synchronisation, a host
+ * runtime whose own allocator owns all device memory, or code running where allocation
+ * is not allowed.
+ *
+ * Same image as gt_render with GT_PRECISION_F32 and GT_SCHEDULE_PERSISTENT.  Its scratch
+ * is one fixed array in the library's device code (about 20 MiB, enough for
+ * GT_NOALLOC_MAX_PIXELS pixels); every GPU that loads the library holds that array until
+ * the process exits.  Images larger than GT_NOALLOC_MAX_PIXELS return GT_ERR_INVALID_ARG.
+ *
+ * - rgb (width*height*3 floats, required) and accepted (width*height, optional) are
+ *   DEVICE pointers on the context's device; the call returns when they are complete.
+ * - The scene, lights and environment must already be resident on the device in f32:
+ *   render them once with gt_render during set-up, otherwise GT_ERR_INVALID_ARG.
+ * - The first call on a device looks up the array's device address (and may load the
+ *   library's device code); make that first call during set-up, before any stream
+ *   capture.
+ * - All calls share the one array: calls whose work overlaps on the GPU (from different
+ *   contexts on the same device) race and must be serialised by the caller.
+ * - No progress callback, no cancellation, no statistics. */
+gt_status gt_render_noalloc(gt_scene* scene, const gt_lights* lights, const gt_environment* environment,
+                            const gt_camera_desc* camera, float* rgb, uint32_t* accepted);
+
 #ifdef __cplusplus
 }
 #endif
