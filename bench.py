@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--schedule", default="auto", choices=["auto", "wavefront", "persistent"])
+    ap.add_argument("--tail-slots", type=int, default=0,
+                    help="auto schedule: unfinished pixels at which the persistent kernel takes over (0 = library)")
     ap.add_argument("--width", type=int, default=0, help="smaller image for profiling runs (0 = the workload's)")
     ap.add_argument("--grid", type=int, default=0, help="stratified grid width for profiling runs (0 = 16)")
     ap.add_argument("--profile-run", action="store_true",
@@ -229,7 +231,7 @@ def run_ours(args):
     torch.cuda.set_device(device)
     ctx = Context(device)
     scene, lights, cam, cfg = workload(args.config, args.width, args.grid)
-    pt = PathTracer(cam, context=ctx, schedule=args.schedule)
+    pt = PathTracer(cam, context=ctx, schedule=args.schedule, tail_slots=args.tail_slots)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
 
     def render():
@@ -249,8 +251,6 @@ def run_ours(args):
         return
     for _ in range(max(args.warmup, 3)):
         render()
-    nee_mode = cam.desc().direct_lighting_mode == abi.GT_DIRECT_NEXT_EVENT_ESTIMATION
-    kernels_per_iter = 0 if args.schedule != "wavefront" else (4 if nee_mode else 3)
     dev_ms, samples, rays, launches = 0.0, 0, 0, 0
     barrier()
     wall0 = time.perf_counter()
@@ -263,7 +263,7 @@ def run_ours(args):
             dev_ms += st["gpu_ms"]
             samples += st["samples"]
             rays += st["rays"] + st["shadow_rays"]
-            launches += (1 if args.schedule != "wavefront" else 2) + st["iterations"] * kernels_per_iter
+            launches += sum(st["kernel_launches"].values())
     barrier()
     wall_s = time.perf_counter() - wall0
     clock = clocks.summary()
@@ -320,7 +320,7 @@ def run_ours(args):
     e2e = statistics.median(e2e_vals) * world
 
     # Roofline of the dominant kernel from one profiled frame (events around every launch).
-    prof = PathTracer(cam, context=ctx, profile=True, schedule=args.schedule)
+    prof = PathTracer(cam, context=ctx, profile=True, schedule=args.schedule, tail_slots=args.tail_slots)
     (prof.render_with_lights_hdr_image(scene, lights) if lights is not None else prof.render_hdr_image(scene))
     ps = prof.last_stats
     kms = ps["kernel_ms"]

@@ -190,7 +190,7 @@ class gt_render_opts(C.Structure):
         ("progress_user", C.c_void_p),
         ("stats", C.POINTER(gt_render_stats)),
         ("schedule", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("tail_slots", C.c_uint32),
     ]
 
 

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "internal.h"
@@ -447,12 +448,11 @@ struct EventPool {
         return r == cudaSuccess ? get(z) : r;
     }
     void note(int kernel, cudaEvent_t a, cudaEvent_t z) { pending.push_back(Rec{kernel, a, z}); }
-    // Call after a stream synchronize: folds finished pairs into the totals.
-    void harvest(double* ms, uint64_t* launches) {
+    // Call after a stream synchronize: folds finished pairs into the per-kernel times.
+    void harvest(double* ms) {
         for (const Rec& r : pending) {
             float t = 0.f;
             if (cudaEventElapsedTime(&t, r.a, r.z) == cudaSuccess) ms[r.kernel] += t;
-            launches[r.kernel] += 1;
             free_events.push_back(r.a);
             free_events.push_back(r.z);
         }
@@ -484,19 +484,21 @@ gt_status run_persistent(gt_context* ctx, Params<R>& P, uint32_t* d_next, float*
     const uint32_t cblocks = std::max<uint32_t>(1u, std::min<uint32_t>((n + 255) / 256, sms0 * 8));
     k_classify<R><<<cblocks, 256, 0, st>>>(P, P.ps.q_mat, P.ps.counters + C_MAT);
     GT_CUDA(cudaGetLastError());
+    klaunch[GT_KERNEL_OTHER] += 1;
     ctx->mapped[0] = 0;
     ctx->mapped[1] = 0;
     int per_sm = 0;
-    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<R>, 128, 0));
+    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<R, false>, 128, 0));
     const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1);
     const uint32_t blocks = std::max<uint32_t>(1u, std::min<uint32_t>(sms * uint32_t(std::max(per_sm, 1)), (n + 127) / 128));
     const bool profile = opts.profile != 0;
     cudaEvent_t a = nullptr, z = nullptr;
     GT_CUDA(ev.pair(a, z));
     GT_CUDA(cudaEventRecord(a, st));
-    k_persistent<R><<<blocks, 128, 0, st>>>(P, d_next, P.ps.q_mat, P.ps.counters + C_MAT, ctx->mapped_dev,
+    k_persistent<R, false><<<blocks, 128, 0, st>>>(P, d_next, P.ps.q_mat, P.ps.counters + C_MAT, ctx->mapped_dev,
                                             ctx->mapped_dev + 1, o_rgb, o_rgb64, o_acc);
     GT_CUDA(cudaGetLastError());
+    klaunch[GT_KERNEL_PERSISTENT] += 1;
     GT_CUDA(cudaEventRecord(z, st));
     bool cancelled = false;
     if (opts.progress) {
@@ -517,7 +519,7 @@ gt_status run_persistent(gt_context* ctx, Params<R>& P, uint32_t* d_next, float*
     GT_CUDA(cudaEventSynchronize(z));
     if (profile) {
         ev.note(GT_KERNEL_PERSISTENT, a, z);
-        ev.harvest(kms, klaunch);
+        ev.harvest(kms);
     } else {
         ev.free_events.push_back(a);
         ev.free_events.push_back(z);
@@ -561,12 +563,10 @@ gt_status finish_render(gt_context* ctx, const Params<R>& P, gt_frame* frame, co
         o.shadow_rays = tot[1];
         o.samples = tot[2];
         o.samples_started = tot[3];
-        if (opts.profile) {
-            ev.harvest(kms, klaunch);
-            for (int k = 0; k < GT_KERNEL_COUNT; ++k) {
-                o.kernel_ms[k] = kms[k];
-                o.kernel_launches[k] = klaunch[k];
-            }
+        if (opts.profile) ev.harvest(kms);
+        for (int k = 0; k < GT_KERNEL_COUNT; ++k) {
+            o.kernel_ms[k] = opts.profile ? kms[k] : 0.0;
+            o.kernel_launches[k] = klaunch[k];
         }
     }
     return GT_OK;
@@ -598,7 +598,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
 
     // Workspace: path state and queues (wavefront only), counters, and device staging
     // for host outputs.
-    const bool persistent = opts.schedule != GT_SCHEDULE_WAVEFRONT;
+    const bool persistent = opts.schedule == GT_SCHEDULE_PERSISTENT;
     const bool host_out = frame->device_buffers == 0;
     auto lay = [&](Bump& bb) {
         if (persistent) {
@@ -651,6 +651,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             if (profile) GT_CUDA(cudaEventRecord(a, st));
             k_aov<R><<<slot_blocks, threads, 0, st>>>(P, o_alb, o_nrm);
             GT_CUDA(cudaGetLastError());
+            klaunch[GT_KERNEL_OTHER] += 1;
             if (profile) {
                 GT_CUDA(cudaEventRecord(z, st));
                 ev.note(GT_KERNEL_OTHER, a, z);
@@ -665,6 +666,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         if (profile) GT_CUDA(cudaEventRecord(a, st));
         k_init<R><<<slot_blocks, threads, 0, st>>>(P);
         GT_CUDA(cudaGetLastError());
+        klaunch[GT_KERNEL_OTHER] += 1;
         if (profile) {
             GT_CUDA(cudaEventRecord(z, st));
             ev.note(GT_KERNEL_OTHER, a, z);
@@ -673,9 +675,9 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
 
     // One iteration = generate, trace, shade (+ shadow); two iterations (ping-pong trace
     // queues) are captured once as a graph and replayed.
+    const int kernels_per_iteration = nee ? 4 : 3;
     auto launch_iteration = [&](uint32_t cur, bool timed) -> cudaError_t {
-        for (int k = 0; k < 4; ++k) {
-            if (k == 3 && !nee) break;
+        for (int k = 0; k < kernels_per_iteration; ++k) {
             cudaEvent_t a = nullptr, z = nullptr;
             if (timed) {
                 cudaError_t e = ev.pair(a, z);
@@ -714,6 +716,15 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     uint64_t iters = 0;
     uint32_t batch = 2;
     rc = GT_OK;
+    // The last pixels of a frame are the longest sample chains; once no more than one
+    // persistent launch's worth of slots is left, per-bounce launches would run nearly
+    // empty, so the remaining slots finish in k_persistent's RESUME mode.
+    int tail_per_sm = 0;
+    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tail_per_sm, k_persistent<R, true>, 128, 0));
+    uint32_t tail_slots = 0;
+    if (opts.schedule == GT_SCHEDULE_AUTO)
+        tail_slots = opts.tail_slots ? opts.tail_slots : uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1)) * 128u;
+    bool run_tail = false;
     for (;;) {
         for (uint32_t k = 0; k < batch && ce == cudaSuccess; ++k) {
             if (profile) {
@@ -722,6 +733,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             } else {
                 ce = cudaGraphLaunch(exec, st);
             }
+            for (int kk = 0; kk < kernels_per_iteration; ++kk) klaunch[GT_KERNEL_GENERATE + kk] += 2;
         }
         if (ce != cudaSuccess) {
             rc = cuda_fail(ce, "wavefront launch");
@@ -734,13 +746,17 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             rc = cuda_fail(ce, "render loop");
             break;
         }
-        if (profile) ev.harvest(kms, klaunch);
+        if (profile) ev.harvest(kms);
         const uint32_t done = ctx->pinned[0], err = ctx->pinned[1];
         if (err) {
             rc = fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
             break;
         }
         if (done >= n) break;
+        if (n - done <= tail_slots) { // few pixels left: finish them in one persistent launch
+            run_tail = true;
+            break;
+        }
         if (opts.progress && opts.progress(opts.progress_user, uint64_t(done) * limit, uint64_t(n) * limit)) {
             rc = fail(GT_ERR_CANCELLED, "render cancelled by the progress callback");
             break;
@@ -756,6 +772,26 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         cudaStreamSynchronize(st);
         return rc;
     }
+    if (run_tail) {
+        cudaEvent_t a = nullptr, z = nullptr;
+        if (profile) GT_CUDA(ev.pair(a, z));
+        if (profile) GT_CUDA(cudaEventRecord(a, st));
+        uint32_t* list = P.ps.q_trace[0];
+        uint32_t* count = P.ps.counters + C_TRACE0;
+        GT_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t), st));
+        GT_CUDA(cudaMemsetAsync(d_next, 0, sizeof(uint32_t), st));
+        k_collect<R><<<slot_blocks, threads, 0, st>>>(P, list, count);
+        const uint32_t tblocks = uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1));
+        k_persistent<R, true><<<tblocks, 128, 0, st>>>(P, d_next, list, count, nullptr, nullptr, nullptr, nullptr,
+                                                       nullptr);
+        GT_CUDA(cudaGetLastError());
+        klaunch[GT_KERNEL_OTHER] += 1;
+        klaunch[GT_KERNEL_PERSISTENT] += 1;
+        if (profile) {
+            GT_CUDA(cudaEventRecord(z, st));
+            ev.note(GT_KERNEL_PERSISTENT, a, z);
+        }
+    }
 
     {
         cudaEvent_t a = nullptr, z = nullptr;
@@ -763,9 +799,11 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         if (profile) GT_CUDA(cudaEventRecord(a, st));
         k_resolve<R><<<slot_blocks, threads, 0, st>>>(P, o_rgb, o_rgb64, o_acc);
         GT_CUDA(cudaGetLastError());
+        klaunch[GT_KERNEL_OTHER] += 1;
         if (opts.aovs && (o_alb || o_nrm)) {
             k_aov<R><<<slot_blocks, threads, 0, st>>>(P, o_alb, o_nrm);
             GT_CUDA(cudaGetLastError());
+            klaunch[GT_KERNEL_OTHER] += 1;
         }
         if (profile) {
             GT_CUDA(cudaEventRecord(z, st));

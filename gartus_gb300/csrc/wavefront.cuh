@@ -538,23 +538,29 @@ template <class R> __global__ void __launch_bounds__(256) k_classify(Params<R> P
 // next-event shadow rays — so lanes on different samples, pixels or ray kinds stay on the
 // same instructions.  `cancel` is polled at each pixel fetch; `progress` receives the
 // number of pixels handed out.
-template <class R>
+//
+// RESUME = true finishes a wavefront render instead: `queues` is a list of the slots that
+// are still running (class_counts[0] entries), each thread picks up a slot's saved state
+// (its path mid-flight, or a finished sample waiting to be folded in) and, when the
+// slot's pixel is done, stores the pixel sums back for k_resolve.
+template <class R, bool RESUME>
 __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next, const uint32_t* queues,
                                                     const uint32_t* class_counts, const volatile uint32_t* cancel,
                                                     volatile uint32_t* progress, float* rgb, double* rgb64,
                                                     uint32_t* accepted) {
-    const uint32_t n = P.cam.width * P.cam.height;
+    const uint32_t n = RESUME ? class_counts[0] : P.cam.width * P.cam.height;
     const uint32_t limit = P.cam.adaptive ? P.cam.adaptive_max : P.cam.spp;
     const R inf = Num<R>::inf();
     uint32_t prefix[NUM_COST_CLASSES + 1];
     prefix[0] = 0;
 #pragma unroll
-    for (uint32_t k = 0; k < NUM_COST_CLASSES; ++k) prefix[k + 1] = prefix[k] + class_counts[k];
+    for (uint32_t k = 0; k < NUM_COST_CLASSES; ++k) prefix[k + 1] = prefix[k] + (RESUME ? 0u : class_counts[k]);
     auto fetch = [&]() -> uint32_t {
         if (cancel && *cancel) return n;
         const uint32_t i = atomicAdd(next, 1u);
         if (i >= n) return n;
         if (progress && (i & 1023u) == 0) *progress = i;
+        if (RESUME) return i;
         uint32_t k = 0;
 #pragma unroll
         for (uint32_t c = 1; c < NUM_COST_CLASSES; ++c)
@@ -562,17 +568,44 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
         return queues[size_t(k) * n + (i - prefix[k])];
     };
     unsigned long long n_rays = 0, n_shadow = 0, n_acc = 0, n_started = 0;
-    uint32_t pix = fetch();
+    uint32_t item = fetch();
+    uint32_t pix = RESUME ? (item < n ? queues[item] : 0u) : item;
     Rng g{0};
     R4<R> a{0, 0, 0, 0}, c{0, 0, 0, 0};
     uint32_t acc_n = 0, started = 0;
-    if (pix < n) g.s = pixel_seed(P.cam.seed, pix % P.cam.width, pix / P.cam.width);
     Path<R> p;
     Shadow<R> sh;
     uint32_t pending = 0; // bit k: shadow query k still to trace
     bool cont = false;
     bool need_sample = true;
-    bool alive = pix < n;
+    // Loads a wavefront slot's saved state (RESUME).
+    auto resume = [&](uint32_t slot) {
+        const uint4 st = P.ps.st[slot];
+        g.s = uint64_t(st.x) | (uint64_t(st.y) << 32);
+        started = st.w;
+        a = P.ps.acc[slot];
+        c = P.ps.comp[slot];
+        acc_n = P.ps.accepted[slot];
+        p.col = xyz(P.ps.col[slot]);
+        need_sample = (st.z & F_TRACE) == 0;
+        if (!need_sample) {
+            const R4<R> ro = P.ps.ray_o[slot], rd = P.ps.ray_d[slot];
+            p.o = xyz(ro);
+            p.time = ro.w;
+            p.d = xyz(rd);
+            p.miss_w = rd.w;
+            p.att = xyz(P.ps.att[slot]);
+            p.bounce = st.z & F_BOUNCE_MASK;
+            p.allow_emit = (st.z & F_ALLOW_EMIT) != 0;
+        }
+        pending = 0;
+        cont = !need_sample;
+    };
+    if (item < n) {
+        if (RESUME) resume(pix);
+        else g.s = pixel_seed(P.cam.seed, pix % P.cam.width, pix / P.cam.width);
+    }
+    bool alive = item < n;
     // The loop is warp-uniform and reconverges at each phase boundary (__syncwarp), so
     // the warp executes setup, one traversal and one integration step together instead
     // of drifting apart into sub-warps at different instructions.
@@ -599,26 +632,45 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
                     break;
                 }
                 if (got) break;
-                // The pixel is finished: write it and take the next one.
-                const V3<R> v = pixel_estimate(P.cam, a, acc_n);
-                if (rgb) {
-                    rgb[size_t(pix) * 3 + 0] = float(v.x);
-                    rgb[size_t(pix) * 3 + 1] = float(v.y);
-                    rgb[size_t(pix) * 3 + 2] = float(v.z);
+                // The pixel is finished: write it (or hand its sums back to the
+                // wavefront's resolve) and take the next one.
+                if (RESUME) {
+                    P.ps.acc[pix] = a;
+                    P.ps.comp[pix] = c;
+                    P.ps.accepted[pix] = acc_n;
+                    P.ps.st[pix] = make_uint4(uint32_t(g.s), uint32_t(g.s >> 32), F_DONE, started);
+                } else {
+                    const V3<R> v = pixel_estimate(P.cam, a, acc_n);
+                    if (rgb) {
+                        rgb[size_t(pix) * 3 + 0] = float(v.x);
+                        rgb[size_t(pix) * 3 + 1] = float(v.y);
+                        rgb[size_t(pix) * 3 + 2] = float(v.z);
+                    }
+                    if (rgb64) {
+                        rgb64[size_t(pix) * 3 + 0] = double(v.x);
+                        rgb64[size_t(pix) * 3 + 1] = double(v.y);
+                        rgb64[size_t(pix) * 3 + 2] = double(v.z);
+                    }
+                    if (accepted) accepted[pix] = acc_n;
+                    n_acc += acc_n;
+                    n_started += started;
                 }
-                if (rgb64) {
-                    rgb64[size_t(pix) * 3 + 0] = double(v.x);
-                    rgb64[size_t(pix) * 3 + 1] = double(v.y);
-                    rgb64[size_t(pix) * 3 + 2] = double(v.z);
-                }
-                if (accepted) accepted[pix] = acc_n;
-                n_acc += acc_n;
-                n_started += started;
-                pix = fetch();
-                if (pix >= n) {
+                item = fetch();
+                if (item >= n) {
                     alive = false;
                     break;
                 }
+                if (RESUME) {
+                    pix = queues[item];
+                    resume(pix);
+                    if (!need_sample) break; // a path in flight: trace it
+                    stop = false;
+                    got = false;
+                    // a finished sample: fold it in before starting the next one
+                    if (started > 0) stop = fold_sample(P.cam, a, c, acc_n, p.col);
+                    continue;
+                }
+                pix = item;
                 g.s = pixel_seed(P.cam.seed, pix % P.cam.width, pix / P.cam.width);
                 a = R4<R>{0, 0, 0, 0};
                 c = R4<R>{0, 0, 0, 0};
@@ -670,6 +722,18 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
         atomicAdd(&P.ps.totals[1], n_shadow);
         atomicAdd(&P.ps.totals[2], n_acc);
         atomicAdd(&P.ps.totals[3], n_started);
+    }
+}
+
+// Lists the wavefront slots that have not finished their pixel (for the RESUME pass).
+template <class R> __global__ void __launch_bounds__(256) k_collect(Params<R> P, uint32_t* list, uint32_t* count) {
+    const uint32_t n = P.ps.n;
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = warp0; base < n; base += stride) {
+        const uint32_t slot = base + lane_id();
+        const bool live = slot < n && (P.ps.st[slot].z & F_DONE) == 0;
+        warp_push(live, slot, list, count);
     }
 }
 

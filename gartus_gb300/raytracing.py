@@ -709,13 +709,16 @@ class RenderOptions:
 class PathTracer:
     """PathTracer (raytracing/renderer.rs:55-875) on the GB300 wavefront integrator.
 
-    precision: "f32" (throughput) or "f64" (the reference's arithmetic, op for op)."""
+    precision: "f32" (throughput) or "f64" (the reference's arithmetic, op for op).
+    schedule: "auto" (wavefront, then the persistent kernel for the last tail_slots
+    pixels; 0 = the library's choice), "wavefront" or "persistent"; the image is the same."""
 
     SCHEDULES = {"auto": abi.GT_SCHEDULE_AUTO, "wavefront": abi.GT_SCHEDULE_WAVEFRONT,
                  "persistent": abi.GT_SCHEDULE_PERSISTENT}
 
     def __init__(self, camera: RayCamera, options: RenderOptions = RenderOptions(), precision: str = "f32",
-                 context: Optional[Context] = None, profile: bool = False, schedule: str = "auto"):
+                 context: Optional[Context] = None, profile: bool = False, schedule: str = "auto",
+                 tail_slots: int = 0):
         if precision not in ("f32", "f64"):
             raise ValueError("precision must be 'f32' or 'f64'")
         if schedule not in self.SCHEDULES:
@@ -725,6 +728,7 @@ class PathTracer:
         self.precision = precision
         self.profile = profile
         self.schedule = schedule
+        self.tail_slots = int(tail_slots)
         self._ctx = context
         self.last_stats: Optional[dict] = None
 
@@ -733,7 +737,8 @@ class PathTracer:
         return self._ctx or Context.default()
 
     def with_options(self, options: RenderOptions) -> "PathTracer":
-        return PathTracer(self.camera, options, self.precision, self._ctx, self.profile, self.schedule)
+        return PathTracer(self.camera, options, self.precision, self._ctx, self.profile, self.schedule,
+                          self.tail_slots)
 
     def _render(self, world: RayScene, lights: Optional[WeightedSamplingTargetList],
                 environment: Optional[EnvironmentLight], aovs: bool = False, want64: bool = False):
@@ -758,6 +763,7 @@ class PathTracer:
         o.aovs = 1 if aovs else 0
         o.profile = 1 if self.profile else 0
         o.schedule = self.SCHEDULES[self.schedule]
+        o.tail_slots = self.tail_slots
         stats = abi.gt_render_stats()
         o.stats = C.pointer(stats)
         sh = world._handle(ctx)
@@ -798,7 +804,8 @@ class PathTracer:
     # render_with_light_connections (renderer.rs:771-786): forces NEE
     def render_with_light_connections_hdr_image(self, world, lights, want64: bool = False) -> HdrImage:
         cam = self.camera.with_direct_lighting_mode(abi.GT_DIRECT_NEXT_EVENT_ESTIMATION)
-        return PathTracer(cam, self.options, self.precision, self._ctx, self.profile, self.schedule)._render(
+        return PathTracer(cam, self.options, self.precision, self._ctx, self.profile, self.schedule,
+                          self.tail_slots)._render(
             world, lights, None, want64=want64)
 
     # render_with_environment_hdr_image (renderer.rs:431-449)

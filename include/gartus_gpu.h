@@ -216,12 +216,13 @@ typedef struct gt_render_stats {
     uint64_t samples;       /* accepted camera samples summed over pixels                             */
     uint64_t samples_started;
     double kernel_ms[GT_KERNEL_COUNT];     /* filled when gt_render_opts.profile = 1 */
-    uint64_t kernel_launches[GT_KERNEL_COUNT];
+    uint64_t kernel_launches[GT_KERNEL_COUNT]; /* always filled: this library's kernel launches */
 } gt_render_stats;
 
-/* How the frame is scheduled on the GPU.  Both give identical images. */
+/* How the frame is scheduled on the GPU.  All give identical images. */
 typedef enum gt_schedule {
-    GT_SCHEDULE_AUTO = 0,       /* the persistent kernel                                        */
+    GT_SCHEDULE_AUTO = 0,       /* wavefront until few pixels are left, then the persistent kernel
+                                   finishes them (gt_render_opts.tail_slots)                      */
     GT_SCHEDULE_WAVEFRONT = 1,  /* per-bounce kernels over material-binned queues, graph-replayed */
     GT_SCHEDULE_PERSISTENT = 2  /* one launch; threads pull pixels and run their paths in registers */
 } gt_schedule;
@@ -235,7 +236,9 @@ typedef struct gt_render_opts {
     void* progress_user;
     gt_render_stats* stats; /* optional output */
     uint32_t schedule;      /* gt_schedule */
-    uint32_t reserved;
+    uint32_t tail_slots;    /* GT_SCHEDULE_AUTO: hand over to the persistent kernel once at most
+                               this many pixels are unfinished; 0 = as many as one persistent
+                               launch keeps resident */
 } gt_render_opts;
 
 /* Caller-owned output images, row-major, 3 channels, y = 0 is the top row

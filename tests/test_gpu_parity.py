@@ -22,6 +22,10 @@ from tests.helpers import rel_err
 
 pytestmark = pytest.mark.gpu
 
+# "wavefront": per-bounce kernels to the end; "auto": the wavefront hands its last slots
+# to the persistent kernel (the default); "persistent": one persistent launch.
+SCHEDULES = ["wavefront", "auto", "persistent"]
+
 
 def relmse(x, r):
     return float(np.mean((x - r) ** 2 / (r * r + 1e-2)))
@@ -102,7 +106,7 @@ def _cases():
     }
 
 
-@pytest.mark.parametrize("schedule", ["wavefront", "persistent"])
+@pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("case", ["final", "cornell_mixture", "cornell_nee", "bench"])
 def test_f64_path_matches_oracle(gpu_context, case, schedule):
     scene, cam, lights = _cases()[case]
@@ -119,11 +123,12 @@ def test_f64_path_matches_oracle(gpu_context, case, schedule):
     assert err.max() <= 1e-9
 
 
+
 def _divergent(x, r, tol=1e-4):
     return int((rel_err(x, r, floor=1e-3).max(axis=2) > tol).sum())
 
 
-@pytest.mark.parametrize("schedule", ["wavefront", "persistent"])
+@pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("case", ["final", "cornell_mixture", "cornell_nee", "bench"])
 def test_f32_path_same_streams(gpu_context, case, schedule):
     # Same RNG streams in f32.  f32 rounding alone moves some pixels by more than 1e-4
@@ -340,18 +345,23 @@ def test_persistent_progress_and_cancel(gpu_context):
     assert np.isfinite(img.pixels).all()
 
 
-def test_schedules_agree(gpu_context):
-    # Both schedules evaluate the same per-pixel arithmetic in the same order: bit-identical
-    # in f64 (no fused multiply-add anywhere); in f32 the compiler may fuse differently in
-    # the two kernels, so the images agree to f32 rounding on almost every pixel.
+@pytest.mark.parametrize("schedule,tail", [("wavefront", 0), ("auto", 100), ("auto", 1000000)])
+def test_schedules_agree(gpu_context, schedule, tail):
+    # Every schedule evaluates the same per-pixel arithmetic in the same order: bit-identical
+    # in f64 (no fused multiply-add anywhere), whether the wavefront runs to the end, hands
+    # its last 100 slots to the persistent kernel, or hands over at once; in f32 the
+    # compiler may fuse differently in the kernels, so images agree to f32 rounding.
     scene, lights = scenes.cornell_scene()
     cam = scenes.cornell_camera(48, 4, 50)
-    a = PathTracer(cam, precision="f64", context=gpu_context, schedule="wavefront")
+    a = PathTracer(cam, precision="f64", context=gpu_context, schedule=schedule, tail_slots=tail)
     b = PathTracer(cam, precision="f64", context=gpu_context, schedule="persistent")
     ia = a.render_with_lights_hdr_image(scene, lights, want64=True)
     ib = b.render_with_lights_hdr_image(scene, lights, want64=True)
     np.testing.assert_array_equal(ia.pixels64, ib.pixels64)
     np.testing.assert_array_equal(ia.accepted, ib.accepted)
-    fa = PathTracer(cam, context=gpu_context, schedule="wavefront").render_with_lights_hdr_image(scene, lights)
+    assert a.last_stats["samples"] == b.last_stats["samples"]
+    assert a.last_stats["rays"] == b.last_stats["rays"]
+    fa = PathTracer(cam, context=gpu_context, schedule=schedule,
+                    tail_slots=tail).render_with_lights_hdr_image(scene, lights)
     fb = PathTracer(cam, context=gpu_context, schedule="persistent").render_with_lights_hdr_image(scene, lights)
     assert _divergent(fa.pixels, fb.pixels.astype(np.float64)) <= 0.05 * fa.pixels.shape[0] * fa.pixels.shape[1]
