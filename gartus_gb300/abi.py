@@ -7,7 +7,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-GT_ABI_VERSION = 1
+GT_ABI_VERSION = 2
 
 # gt_status
 GT_OK = 0
@@ -169,6 +169,8 @@ class gt_render_stats(C.Structure):
         ("samples_started", C.c_uint64),
         ("kernel_ms", C.c_double * GT_KERNEL_COUNT),
         ("kernel_launches", C.c_uint64 * GT_KERNEL_COUNT),
+        ("migrated_pixels", C.c_uint64),
+        ("tail_pixels", C.c_uint64),
     ]
 
     def as_dict(self) -> dict:
@@ -177,6 +179,7 @@ class gt_render_stats(C.Structure):
             "shadow_rays": self.shadow_rays, "samples": self.samples, "samples_started": self.samples_started,
             "kernel_ms": {KERNEL_NAMES[i]: self.kernel_ms[i] for i in range(GT_KERNEL_COUNT)},
             "kernel_launches": {KERNEL_NAMES[i]: int(self.kernel_launches[i]) for i in range(GT_KERNEL_COUNT)},
+            "migrated_pixels": int(self.migrated_pixels), "tail_pixels": int(self.tail_pixels),
         }
 
 

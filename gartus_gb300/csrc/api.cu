@@ -229,6 +229,7 @@ gt_status gt_context_create(int device, gt_context** out) {
     ctx->device = device;
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&ctx->pinned), 64);
     void* mapped = nullptr;
     if (e == cudaSuccess) e = cudaHostAlloc(&mapped, 64, cudaHostAllocMapped);
@@ -239,6 +240,9 @@ gt_status gt_context_create(int device, gt_context** out) {
     }
     if (e != cudaSuccess) {
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
+        if (ctx->side) cudaStreamDestroy(ctx->side);
+        if (ctx->pinned) cudaFreeHost(ctx->pinned);
+        if (ctx->mapped) cudaFreeHost(const_cast<uint32_t*>(ctx->mapped));
         delete ctx;
         return cuda_fail(e, "context creation");
     }
@@ -251,10 +255,12 @@ void gt_context_destroy(gt_context* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    cudaStreamSynchronize(ctx->side);
     cudaFree(ctx->ws);
     cudaFreeHost(ctx->pinned);
     cudaFreeHost(const_cast<uint32_t*>(ctx->mapped));
     cudaStreamDestroy(ctx->stream);
+    cudaStreamDestroy(ctx->side);
     delete ctx;
 }
 

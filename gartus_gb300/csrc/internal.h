@@ -58,6 +58,7 @@ struct gt_context {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr; // concurrent persistent kernel for migrated wavefront slots
     std::mutex mu;
     void* ws = nullptr; // render workspace (path state, queues, staging)
     size_t ws_bytes = 0;

@@ -147,8 +147,11 @@ template <class R> struct PathState {
     uint32_t* q_trace[2];
     uint32_t* q_mat; // 8 queues of capacity n (key = material kind, 7 = miss)
     uint32_t* q_shadow;
-    uint32_t* counters; // [0,1] trace, [2..10) mat keys, [10] shadow, [11] done, [12] error
-    unsigned long long* totals; // [0] rays, [1] shadow rays, [2] accepted samples, [3] started samples
+    uint32_t* q_migrate; // slots handed to the concurrent persistent kernel
+    uint32_t* counters; // [0,1] trace, [2..10) mat keys, [10] shadow, [11] done, [12] error,
+                        // [13] migrated slots, [14] their pull counter, [15] tail slots
+    unsigned long long* totals; // [0] rays, [1] shadow rays, [2] accepted samples, [3] started samples,
+                                // [4] samples started by unfinished slots, [5] unfinished slots
     uint32_t n;
 };
 
@@ -159,6 +162,9 @@ enum : uint32_t {
     C_SHADOW = 10,
     C_DONE = 11,
     C_ERROR = 12,
+    C_MIGRATED = 13,
+    C_MIGRATE_NEXT = 14,
+    C_TAIL = 15, // slots finished by the tail launch
     C_COUNT = 16
 };
 
@@ -172,7 +178,8 @@ enum : uint32_t {
     F_TRACE = 1u << 18,
     F_DONE = 1u << 19,
     F_SHADOW0 = 1u << 20, // pending area-light shadow query
-    F_SHADOW1 = 1u << 21  // pending environment shadow query
+    F_SHADOW1 = 1u << 21, // pending environment shadow query
+    F_MIGRATED = 1u << 22 // finished by the concurrent persistent kernel, not the wavefront
 };
 
 // Error bits in counters[C_ERROR].

@@ -399,8 +399,9 @@ template <class R> size_t layout_state(Bump& b, PathState<R>& ps, uint32_t n, bo
     ps.q_trace[1] = b.take<uint32_t>(n);
     ps.q_mat = b.take<uint32_t>(size_t(n) * NUM_KEYS);
     ps.q_shadow = b.take<uint32_t>(nee ? n : 1);
+    ps.q_migrate = b.take<uint32_t>(n);
     ps.counters = b.take<uint32_t>(C_COUNT);
-    ps.totals = b.take<unsigned long long>(4);
+    ps.totals = b.take<unsigned long long>(8);
     return b.off;
 }
 
@@ -408,6 +409,7 @@ inline gt_status ensure_workspace(gt_context* ctx, size_t bytes) {
     if (ctx->ws_bytes >= bytes) return GT_OK;
     if (ctx->ws) {
         cudaStreamSynchronize(ctx->stream);
+        cudaStreamSynchronize(ctx->side);
         cudaFree(ctx->ws);
         ctx->ws = nullptr;
         ctx->ws_bytes = 0;
@@ -548,9 +550,10 @@ gt_status finish_render(gt_context* ctx, const Params<R>& P, gt_frame* frame, co
     }
     unsigned long long tot[4];
     GT_CUDA(cudaMemcpyAsync(ctx->pinned + 2, P.ps.totals, sizeof(tot), cudaMemcpyDeviceToHost, st));
-    GT_CUDA(cudaMemcpyAsync(ctx->pinned, P.ps.counters + C_ERROR, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    // counters[C_ERROR .. C_TAIL] after the totals (pinned words 2..9)
+    GT_CUDA(cudaMemcpyAsync(ctx->pinned + 10, P.ps.counters + C_ERROR, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     GT_CUDA(cudaStreamSynchronize(st));
-    if (ctx->pinned[0]) return fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
+    if (ctx->pinned[10]) return fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
     std::memcpy(tot, ctx->pinned + 2, sizeof(tot));
     if (opts.stats) {
         gt_render_stats& o = *opts.stats;
@@ -563,6 +566,8 @@ gt_status finish_render(gt_context* ctx, const Params<R>& P, gt_frame* frame, co
         o.shadow_rays = tot[1];
         o.samples = tot[2];
         o.samples_started = tot[3];
+        o.migrated_pixels = ctx->pinned[10 + (C_MIGRATED - C_ERROR)];
+        o.tail_pixels = ctx->pinned[10 + (C_TAIL - C_ERROR)];
         if (opts.profile) ev.harvest(kms);
         for (int k = 0; k < GT_KERNEL_COUNT; ++k) {
             o.kernel_ms[k] = opts.profile ? kms[k] : 0.0;
@@ -725,6 +730,37 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     if (opts.schedule == GT_SCHEDULE_AUTO)
         tail_slots = opts.tail_slots ? opts.tail_slots : uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1)) * 128u;
     bool run_tail = false;
+    // Slow-slot migration: once, after kMigrateAfter iterations, the slots progressing at
+    // less than 1/kMigrateRatio of the mean sample rate move to k_persistent (resume mode)
+    // on the context's side stream, concurrently with the rest of the wavefront.
+    constexpr uint64_t kMigrateAfter = 60;
+    constexpr float kMigrateRatio = 2.0f;
+    const bool may_migrate = opts.schedule == GT_SCHEDULE_AUTO;
+    bool migrated = false;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    ctx->mapped[0] = 0; // the side kernel's cancel word
+    auto migrate = [&]() -> gt_status {
+        GT_CUDA(cudaMemsetAsync(P.ps.totals + 4, 0, 2 * sizeof(unsigned long long), st));
+        GT_CUDA(cudaMemsetAsync(P.ps.counters + C_MIGRATED, 0, 2 * sizeof(uint32_t), st));
+        GT_CUDA(cudaMemsetAsync(P.ps.counters + C_TRACE1, 0, sizeof(uint32_t), st));
+        k_progress_sum<R><<<slot_blocks, threads, 0, st>>>(P);
+        k_migrate<R><<<slot_blocks, threads, 0, st>>>(P, kMigrateRatio);
+        k_drop_migrated<R><<<work_blocks, threads, 0, st>>>(P);
+        k_restore_queue<R><<<work_blocks, threads, 0, st>>>(P);
+        GT_CUDA(cudaGetLastError());
+        klaunch[GT_KERNEL_OTHER] += 4;
+        GT_CUDA(ev.pair(fork, join));
+        GT_CUDA(cudaEventRecord(fork, st));
+        GT_CUDA(cudaStreamWaitEvent(ctx->side, fork, 0));
+        const uint32_t side_blocks = uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1));
+        k_persistent<R, true><<<side_blocks, 128, 0, ctx->side>>>(P, P.ps.counters + C_MIGRATE_NEXT, P.ps.q_migrate,
+                                                                  P.ps.counters + C_MIGRATED, ctx->mapped_dev,
+                                                                  nullptr, nullptr, nullptr, nullptr);
+        GT_CUDA(cudaGetLastError());
+        klaunch[GT_KERNEL_PERSISTENT] += 1;
+        GT_CUDA(cudaEventRecord(join, ctx->side));
+        return GT_OK;
+    };
     for (;;) {
         for (uint32_t k = 0; k < batch && ce == cudaSuccess; ++k) {
             if (profile) {
@@ -757,6 +793,10 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             run_tail = true;
             break;
         }
+        if (may_migrate && !migrated && iters >= kMigrateAfter) {
+            migrated = true;
+            if ((rc = migrate()) != GT_OK) break;
+        }
         if (opts.progress && opts.progress(opts.progress_user, uint64_t(done) * limit, uint64_t(n) * limit)) {
             rc = fail(GT_ERR_CANCELLED, "render cancelled by the progress callback");
             break;
@@ -769,7 +809,9 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     }
     if (exec) cudaGraphExecDestroy(exec);
     if (rc != GT_OK) {
+        ctx->mapped[0] = 1; // the side kernel stops taking slots
         cudaStreamSynchronize(st);
+        cudaStreamSynchronize(ctx->side);
         return rc;
     }
     if (run_tail) {
@@ -777,7 +819,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         if (profile) GT_CUDA(ev.pair(a, z));
         if (profile) GT_CUDA(cudaEventRecord(a, st));
         uint32_t* list = P.ps.q_trace[0];
-        uint32_t* count = P.ps.counters + C_TRACE0;
+        uint32_t* count = P.ps.counters + C_TAIL;
         GT_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t), st));
         GT_CUDA(cudaMemsetAsync(d_next, 0, sizeof(uint32_t), st));
         k_collect<R><<<slot_blocks, threads, 0, st>>>(P, list, count);
@@ -791,6 +833,10 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             GT_CUDA(cudaEventRecord(z, st));
             ev.note(GT_KERNEL_PERSISTENT, a, z);
         }
+    }
+    if (migrated) { // join the side stream before the resolve reads every slot
+        GT_CUDA(cudaStreamWaitEvent(st, join, 0));
+        ev.note(GT_KERNEL_PERSISTENT, fork, join);
     }
 
     {

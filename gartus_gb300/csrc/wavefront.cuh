@@ -87,7 +87,7 @@ template <class R> __global__ void k_init(Params<R> P) {
         P.ps.accepted[i] = 0;
     }
     if (blockIdx.x == 0 && threadIdx.x < C_COUNT) P.ps.counters[threadIdx.x] = 0;
-    if (blockIdx.x == 0 && threadIdx.x < 4) P.ps.totals[threadIdx.x] = 0;
+    if (blockIdx.x == 0 && threadIdx.x < 8) P.ps.totals[threadIdx.x] = 0;
 }
 
 // Folds a finished sample into the pixel; returns true when adaptive sampling stops.
@@ -163,7 +163,7 @@ template <class R> __global__ void __launch_bounds__(256) k_generate(Params<R> P
 
 template <class R> __global__ void __launch_bounds__(256) k_trace(Params<R> P, uint32_t cur) {
     const uint32_t count = *reinterpret_cast<volatile uint32_t*>(&P.ps.counters[C_TRACE0 + cur]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) P.ps.totals[0] += count;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&P.ps.totals[0], (unsigned long long)count);
     const uint32_t* q = P.ps.q_trace[cur];
     const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -400,7 +400,7 @@ template <class R> __global__ void __launch_bounds__(256) k_shade(Params<R> P, u
 
 template <class R> __global__ void __launch_bounds__(256) k_shadow(Params<R> P) {
     const uint32_t count = *reinterpret_cast<volatile uint32_t*>(&P.ps.counters[C_SHADOW]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) P.ps.totals[1] += count;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&P.ps.totals[1], (unsigned long long)count);
     const R inf = Num<R>::inf();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t slot = P.ps.q_shadow[i];
@@ -732,9 +732,87 @@ template <class R> __global__ void __launch_bounds__(256) k_collect(Params<R> P,
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = warp0; base < n; base += stride) {
         const uint32_t slot = base + lane_id();
-        const bool live = slot < n && (P.ps.st[slot].z & F_DONE) == 0;
+        const bool live = slot < n && (P.ps.st[slot].z & (F_DONE | F_MIGRATED)) == 0;
         warp_push(live, slot, list, count);
     }
+}
+
+// Slow-slot migration.  A wavefront slot advances one bounce per iteration, so a frame
+// lasts as long as its longest per-pixel sample chain (pixels behind glass run several
+// times the median number of bounces).  Early in the frame the slots whose sample rate
+// is far below the mean move to a persistent kernel on a second stream, which runs them
+// concurrently with the wavefront at one bounce per loop instead of one per iteration.
+//
+// Pass 1: samples started by unfinished slots, and their number, into totals[4], [5].
+template <class R> __global__ void __launch_bounds__(256) k_progress_sum(Params<R> P) {
+    const uint32_t n = P.ps.n;
+    unsigned long long s = 0, c = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint4 st = P.ps.st[i];
+        if ((st.z & (F_DONE | F_MIGRATED)) == 0) {
+            s += st.w;
+            c += 1;
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, off);
+        c += __shfl_down_sync(0xffffffffu, c, off);
+    }
+    if (lane_id() == 0 && c) {
+        atomicAdd(&P.ps.totals[4], s);
+        atomicAdd(&P.ps.totals[5], c);
+    }
+}
+
+// Pass 2: marks every unfinished slot with started * ratio < mean started as migrated,
+// lists it in q_migrate and counts it as done for the wavefront's termination test.
+// A migrated slot keeps its path state; clearing F_NEWSAMPLE keeps k_generate away.
+template <class R> __global__ void __launch_bounds__(256) k_migrate(Params<R> P, float ratio) {
+    const uint32_t n = P.ps.n;
+    const double sum = double(P.ps.totals[4]), live = double(P.ps.totals[5]);
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = warp0; base < n; base += stride) {
+        const uint32_t slot = base + lane_id();
+        bool mig = false;
+        if (slot < n && live > 0.0) {
+            uint4 st = P.ps.st[slot];
+            mig = (st.z & (F_DONE | F_MIGRATED)) == 0 && double(st.w) * double(ratio) * live < sum;
+            if (mig) {
+                st.z = (st.z & ~F_NEWSAMPLE) | F_MIGRATED;
+                P.ps.st[slot] = st;
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, mig);
+        if (m && lane_id() == 0) atomicAdd(&P.ps.counters[C_DONE], uint32_t(__popc(m)));
+        warp_push(mig, slot, P.ps.q_migrate, &P.ps.counters[C_MIGRATED]);
+    }
+}
+
+// Pass 3: the trace queue the next iteration starts from, q_trace[0], without migrated
+// slots: survivors go to q_trace[1] (its counter zeroed before) ...
+template <class R> __global__ void __launch_bounds__(256) k_drop_migrated(Params<R> P) {
+    const uint32_t count = P.ps.counters[C_TRACE0];
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = warp0; base < count; base += stride) {
+        const uint32_t i = base + lane_id();
+        uint32_t slot = 0;
+        bool keep = false;
+        if (i < count) {
+            slot = P.ps.q_trace[0][i];
+            keep = (P.ps.st[slot].z & F_MIGRATED) == 0;
+        }
+        warp_push(keep, slot, P.ps.q_trace[1], &P.ps.counters[C_TRACE1]);
+    }
+}
+
+// ... and are copied back.
+template <class R> __global__ void __launch_bounds__(256) k_restore_queue(Params<R> P) {
+    const uint32_t count = P.ps.counters[C_TRACE1];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+        P.ps.q_trace[0][i] = P.ps.q_trace[1][i];
+    if (blockIdx.x == 0 && threadIdx.x == 0) P.ps.counters[C_TRACE0] = count;
 }
 
 // Denoising AOVs (camera.rs:3064-3116): first-hit albedo and 0.5 (n + 1), same per-pixel

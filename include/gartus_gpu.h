@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define GT_ABI_VERSION 1u
+#define GT_ABI_VERSION 2u
 
 typedef enum gt_status {
     GT_OK = 0,
@@ -217,6 +217,8 @@ typedef struct gt_render_stats {
     uint64_t samples_started;
     double kernel_ms[GT_KERNEL_COUNT];     /* filled when gt_render_opts.profile = 1 */
     uint64_t kernel_launches[GT_KERNEL_COUNT]; /* always filled: this library's kernel launches */
+    uint64_t migrated_pixels; /* GT_SCHEDULE_AUTO: slow pixels moved early to the concurrent persistent kernel */
+    uint64_t tail_pixels;     /* GT_SCHEDULE_AUTO: pixels the persistent kernel finished after the wavefront */
 } gt_render_stats;
 
 /* How the frame is scheduled on the GPU.  All give identical images. */

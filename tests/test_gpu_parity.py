@@ -345,14 +345,17 @@ def test_persistent_progress_and_cancel(gpu_context):
     assert np.isfinite(img.pixels).all()
 
 
-@pytest.mark.parametrize("schedule,tail", [("wavefront", 0), ("auto", 100), ("auto", 1000000)])
-def test_schedules_agree(gpu_context, schedule, tail):
+@pytest.mark.parametrize("schedule,tail,grid", [("wavefront", 0, 4), ("auto", 100, 4), ("auto", 1000000, 4),
+                                               ("auto", 1, 8)])
+def test_schedules_agree(gpu_context, schedule, tail, grid):
     # Every schedule evaluates the same per-pixel arithmetic in the same order: bit-identical
     # in f64 (no fused multiply-add anywhere), whether the wavefront runs to the end, hands
-    # its last 100 slots to the persistent kernel, or hands over at once; in f32 the
-    # compiler may fuse differently in the kernels, so images agree to f32 rounding.
+    # its last 100 slots to the persistent kernel, hands over at once, or (64 samples per
+    # pixel, tail of one slot) first moves its slowest pixels to the concurrent persistent
+    # kernel; in f32 the compiler may fuse differently in the kernels, so images agree to
+    # f32 rounding.
     scene, lights = scenes.cornell_scene()
-    cam = scenes.cornell_camera(48, 4, 50)
+    cam = scenes.cornell_camera(48, grid, 50)
     a = PathTracer(cam, precision="f64", context=gpu_context, schedule=schedule, tail_slots=tail)
     b = PathTracer(cam, precision="f64", context=gpu_context, schedule="persistent")
     ia = a.render_with_lights_hdr_image(scene, lights, want64=True)
@@ -361,6 +364,10 @@ def test_schedules_agree(gpu_context, schedule, tail):
     np.testing.assert_array_equal(ia.accepted, ib.accepted)
     assert a.last_stats["samples"] == b.last_stats["samples"]
     assert a.last_stats["rays"] == b.last_stats["rays"]
+    if grid == 8:
+        assert a.last_stats["migrated_pixels"] > 0
+    if schedule == "wavefront":
+        assert a.last_stats["migrated_pixels"] == 0 and a.last_stats["tail_pixels"] == 0
     fa = PathTracer(cam, context=gpu_context, schedule=schedule,
                     tail_slots=tail).render_with_lights_hdr_image(scene, lights)
     fb = PathTracer(cam, context=gpu_context, schedule="persistent").render_with_lights_hdr_image(scene, lights)
