@@ -336,7 +336,7 @@ def run_ours(args):
     bytes_per_unit = {"trace": b_ray, "shade": float(b_state), "generate": float(b_state), "shadow": b_ray,
                       "persistent": b_ray}
     units = {"trace": ps["rays"], "shade": ps["rays"], "generate": ps["samples_started"], "shadow": ps["shadow_rays"],
-             "persistent": ps["rays"] + ps["shadow_rays"]}
+             "persistent": ps["persistent_rays"]}
     launches_dom = max(ps["kernel_launches"][dom], 1)
     avg_ms = kms[dom] / launches_dom
     algo_bytes = units[dom] * bytes_per_unit[dom] / launches_dom

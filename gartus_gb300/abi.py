@@ -171,6 +171,7 @@ class gt_render_stats(C.Structure):
         ("kernel_launches", C.c_uint64 * GT_KERNEL_COUNT),
         ("migrated_pixels", C.c_uint64),
         ("tail_pixels", C.c_uint64),
+        ("persistent_rays", C.c_uint64),
     ]
 
     def as_dict(self) -> dict:
@@ -180,6 +181,7 @@ class gt_render_stats(C.Structure):
             "kernel_ms": {KERNEL_NAMES[i]: self.kernel_ms[i] for i in range(GT_KERNEL_COUNT)},
             "kernel_launches": {KERNEL_NAMES[i]: int(self.kernel_launches[i]) for i in range(GT_KERNEL_COUNT)},
             "migrated_pixels": int(self.migrated_pixels), "tail_pixels": int(self.tail_pixels),
+            "persistent_rays": int(self.persistent_rays),
         }
 
 

@@ -151,7 +151,8 @@ template <class R> struct PathState {
     uint32_t* counters; // [0,1] trace, [2..10) mat keys, [10] shadow, [11] done, [12] error,
                         // [13] migrated slots, [14] their pull counter, [15] tail slots
     unsigned long long* totals; // [0] rays, [1] shadow rays, [2] accepted samples, [3] started samples,
-                                // [4] samples started by unfinished slots, [5] unfinished slots
+                                // [4] samples started by unfinished slots, [5] unfinished slots,
+                                // [6] queries traced by k_persistent
     uint32_t n;
 };
 

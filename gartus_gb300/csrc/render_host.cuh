@@ -479,7 +479,7 @@ gt_status run_persistent(gt_context* ctx, Params<R>& P, uint32_t* d_next, float*
     cudaStream_t st = ctx->stream;
     const uint32_t n = P.ps.n;
     GT_CUDA(cudaMemsetAsync(P.ps.counters, 0, C_COUNT * sizeof(uint32_t), st));
-    GT_CUDA(cudaMemsetAsync(P.ps.totals, 0, 4 * sizeof(unsigned long long), st));
+    GT_CUDA(cudaMemsetAsync(P.ps.totals, 0, 8 * sizeof(unsigned long long), st));
     GT_CUDA(cudaMemsetAsync(d_next, 0, sizeof(uint32_t), st));
     // Cost-ordered pixel queues (the C_MAT counters hold the class sizes).
     const uint32_t sms0 = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1);
@@ -548,13 +548,16 @@ gt_status finish_render(gt_context* ctx, const Params<R>& P, gt_frame* frame, co
         if (opts.aovs && frame->normal)
             GT_CUDA(cudaMemcpyAsync(frame->normal, o_nrm, size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
     }
-    unsigned long long tot[4];
+    // totals[0..3] and [6] into pinned words 2..9 and 14..15
+    unsigned long long tot[4], prays = 0;
     GT_CUDA(cudaMemcpyAsync(ctx->pinned + 2, P.ps.totals, sizeof(tot), cudaMemcpyDeviceToHost, st));
-    // counters[C_ERROR .. C_TAIL] after the totals (pinned words 2..9)
+    GT_CUDA(cudaMemcpyAsync(ctx->pinned + 14, P.ps.totals + 6, sizeof(prays), cudaMemcpyDeviceToHost, st));
+    // counters[C_ERROR .. C_TAIL] into pinned words 10..13
     GT_CUDA(cudaMemcpyAsync(ctx->pinned + 10, P.ps.counters + C_ERROR, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     GT_CUDA(cudaStreamSynchronize(st));
     if (ctx->pinned[10]) return fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
     std::memcpy(tot, ctx->pinned + 2, sizeof(tot));
+    std::memcpy(&prays, ctx->pinned + 14, sizeof(prays));
     if (opts.stats) {
         gt_render_stats& o = *opts.stats;
         std::memset(&o, 0, sizeof(o));
@@ -568,6 +571,7 @@ gt_status finish_render(gt_context* ctx, const Params<R>& P, gt_frame* frame, co
         o.samples_started = tot[3];
         o.migrated_pixels = ctx->pinned[10 + (C_MIGRATED - C_ERROR)];
         o.tail_pixels = ctx->pinned[10 + (C_TAIL - C_ERROR)];
+        o.persistent_rays = prays;
         if (opts.profile) ev.harvest(kms);
         for (int k = 0; k < GT_KERNEL_COUNT; ++k) {
             o.kernel_ms[k] = opts.profile ? kms[k] : 0.0;
@@ -609,7 +613,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         if (persistent) {
             P.ps.n = n;
             P.ps.counters = bb.take<uint32_t>(C_COUNT);
-            P.ps.totals = bb.take<unsigned long long>(4);
+            P.ps.totals = bb.take<unsigned long long>(8);
             P.ps.q_mat = bb.take<uint32_t>(size_t(n) * NUM_COST_CLASSES); // cost-ordered pixel queues
         } else {
             layout_state<R>(bb, P.ps, n, nee);

@@ -722,6 +722,7 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
         atomicAdd(&P.ps.totals[1], n_shadow);
         atomicAdd(&P.ps.totals[2], n_acc);
         atomicAdd(&P.ps.totals[3], n_started);
+        atomicAdd(&P.ps.totals[6], n_rays + n_shadow);
     }
 }
 

@@ -219,6 +219,7 @@ typedef struct gt_render_stats {
     uint64_t kernel_launches[GT_KERNEL_COUNT]; /* always filled: this library's kernel launches */
     uint64_t migrated_pixels; /* GT_SCHEDULE_AUTO: slow pixels moved early to the concurrent persistent kernel */
     uint64_t tail_pixels;     /* GT_SCHEDULE_AUTO: pixels the persistent kernel finished after the wavefront */
+    uint64_t persistent_rays; /* closest-hit + shadow queries traced inside k_persistent launches           */
 } gt_render_stats;
 
 /* How the frame is scheduled on the GPU.  All give identical images. */
