@@ -40,7 +40,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="cornell", choices=["cornell", "final"])
+    ap.add_argument("--config", default="cornell", choices=["cornell", "final", "mesh"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--schedule", default="auto", choices=["auto", "wavefront", "persistent"])
@@ -63,14 +63,24 @@ def workload(name, width=0, grid=0):
                "max_depth": 50,
                "sampling": f"stratified {grid}x{grid}", "lights": "SamplingTargetList mixture (weight 0.5)",
                "primitives": len(scene), "precision": "f32"}
-        return scene, lights, cam, cfg
+        return scene, lights, None, cam, cfg
+    if name == "mesh":
+        scene, env = scenes.mesh_heavy_scene()
+        width = width or 1920
+        grid = grid or 8
+        cam = scenes.mesh_heavy_camera(width, width * 1080 // 1920, grid, 8)
+        w, h, spp = cam.image_size()
+        cfg = {"workload": "mesh_heavy_perlin_tori_sun", "width": w, "height": h, "spp": spp, "max_depth": 8,
+               "sampling": f"stratified {grid}x{grid}", "lights": "HDR environment 2048x1024 f32 with sun (NEE)",
+               "primitives": len(scene), "precision": "f32"}
+        return scene, None, env, cam, cfg
     scene = scenes.final_scene_ray_scene()
     width = width or 400
     cam = scenes.final_scene_camera(width, 32)
     cfg = {"workload": "final_scene_spheres", "width": width, "height": cam.image_size()[1], "spp": 32,
            "max_depth": 10,
            "sampling": "random", "lights": "none (sky gradient)", "primitives": len(scene), "precision": "f32"}
-    return scene, None, cam, cfg
+    return scene, None, None, cam, cfg
 
 
 def dist_env():
@@ -153,7 +163,7 @@ def traffic_from_profiles(kernel: str, workload_name: str):
 
 
 # ----------------------------------------------------------------------------------
-def cpu_baseline(scene, lights, cam, seconds: float):
+def cpu_baseline(scene, lights, env, cam, seconds: float):
     """The oracle (C++ restatement of the reference's rayon renderer) on a band of rows
     of the same frame, with every host thread; returns (Msamples/s, threads, sample)."""
     import oracle
@@ -163,12 +173,12 @@ def cpu_baseline(scene, lights, cam, seconds: float):
     threads = os.cpu_count() or 1
     rows = 1
     t0 = time.perf_counter()
-    o.render(cam.desc(), la, None, precision=1, threads=threads, window=(0, h // 2, w, rows))
+    o.render(cam.desc(), la, env, precision=1, threads=threads, window=(0, h // 2, w, rows))
     dt = max(time.perf_counter() - t0, 1e-3)
     rows = max(1, min(h, int(rows * seconds / dt)))
     y0 = max(0, h // 2 - rows // 2)
     t0 = time.perf_counter()
-    _, acc = o.render(cam.desc(), la, None, precision=1, threads=threads, window=(0, y0, w, rows))
+    _, acc = o.render(cam.desc(), la, env, precision=1, threads=threads, window=(0, y0, w, rows))
     dt = time.perf_counter() - t0
     samples = float(acc.sum())
     return samples / dt / 1e6, threads, f"rows {y0}..{y0 + rows} of {h} ({w * rows} pixels x {spp} spp), f64", dt
@@ -182,15 +192,15 @@ def run_reference_arm(args):
         if rank != 0:
             dist.barrier()
             return
-    scene, lights, cam, cfg = workload(args.config, args.width, args.grid)
+    scene, lights, env, cam, cfg = workload(args.config, args.width, args.grid)
     per_step = max(args.cpu_seconds / 3.0, 2.0)
     for _ in range(args.warmup):
-        cpu_baseline(scene, lights, cam, 0.5)
+        cpu_baseline(scene, lights, env, cam, 0.5)
     vals, dts = [], []
     sample = ""
     threads = 1
     for _ in range(args.steps):
-        v, threads, sample, dt = cpu_baseline(scene, lights, cam, per_step)
+        v, threads, sample, dt = cpu_baseline(scene, lights, env, cam, per_step)
         vals.append(v)
         dts.append(dt)
     value = statistics.median(vals)
@@ -230,11 +240,13 @@ def run_ours(args):
     device = local if world > 1 else 0
     torch.cuda.set_device(device)
     ctx = Context(device)
-    scene, lights, cam, cfg = workload(args.config, args.width, args.grid)
+    scene, lights, env, cam, cfg = workload(args.config, args.width, args.grid)
     pt = PathTracer(cam, context=ctx, schedule=args.schedule, tail_slots=args.tail_slots)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
 
     def render():
+        if env is not None:
+            return pt.render_with_environment_hdr_image(scene, env)
         if lights is not None:
             return pt.render_with_lights_hdr_image(scene, lights)
         return pt.render_hdr_image(scene)
@@ -297,6 +309,9 @@ def run_ours(args):
         la = lights.to_array() if lights is not None else None
         if la is not None:
             check(lib().gt_lights_create(ctx.handle, la.ctypes.data_as(C.c_void_p), len(la), C.byref(lh)))
+        eh = C.c_void_p()
+        if env is not None:
+            check(lib().gt_environment_create(ctx.handle, C.byref(env.desc()), C.byref(eh)))
         w, h, _ = cam.image_size()
         rgb = np.empty((h, w, 3), dtype=np.float32)
         acc = np.empty((h, w), dtype=np.uint32)
@@ -308,20 +323,29 @@ def run_ours(args):
         o.struct_size = C.sizeof(abi.gt_render_opts)
         stt = abi.gt_render_stats()
         o.stats = C.pointer(stt)
-        check(lib().gt_render(sh, lh if la is not None else None, None, C.byref(cam.desc()), C.byref(o), C.byref(f)))
+        check(lib().gt_render(sh, lh if la is not None else None, eh if env is not None else None,
+                              C.byref(cam.desc()), C.byref(o), C.byref(f)))
         lib().gt_scene_destroy(sh)
         if la is not None:
             lib().gt_lights_destroy(lh)
+        if env is not None:
+            lib().gt_environment_destroy(eh)
         dt = time.perf_counter() - t0
         e2e_vals.append(stt.samples / dt / 1e6)
         nodes = max(len(prims) - 1, 1)
         h2d = len(prims) * 64 + len(prims) * 8 + nodes * 64 + len(mats) * 64 + (len(la) * 128 if la is not None else 0)
+        h2d += env.texels.nbytes if env is not None else 0
         d2h = rgb.nbytes + acc.nbytes
     e2e = statistics.median(e2e_vals) * world
 
     # Roofline of the dominant kernel from one profiled frame (events around every launch).
     prof = PathTracer(cam, context=ctx, profile=True, schedule=args.schedule, tail_slots=args.tail_slots)
-    (prof.render_with_lights_hdr_image(scene, lights) if lights is not None else prof.render_hdr_image(scene))
+    if env is not None:
+        prof.render_with_environment_hdr_image(scene, env)
+    elif lights is not None:
+        prof.render_with_lights_hdr_image(scene, lights)
+    else:
+        prof.render_hdr_image(scene)
     ps = prof.last_stats
     kms = ps["kernel_ms"]
     dom = max(("trace", "shade", "generate", "shadow", "persistent"), key=lambda k: kms[k])
@@ -346,7 +370,7 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, threads, sample, _ = cpu_baseline(scene, lights, cam, args.cpu_seconds)
+        v, threads, sample, _ = cpu_baseline(scene, lights, env, cam, args.cpu_seconds)
         cpu = {"value": v, "unit": METRIC, "cores": threads, "kind": "port", "sample": sample}
 
     if rank == 0:

@@ -41,6 +41,11 @@ GT_MAT_DIELECTRIC = 5
 # gt_texture_kind
 GT_TEX_SOLID = 0
 GT_TEX_CHECKER = 1
+GT_TEX_NOISE = 2
+# gt_noise_variant
+GT_NOISE_PLAIN = 0
+GT_NOISE_TURBULENCE = 1
+GT_NOISE_MARBLE = 2
 
 # gt_environment_format
 GT_ENV_SRGB8 = 0

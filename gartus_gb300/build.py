@@ -32,7 +32,7 @@ UNITS = [
     ("render_f64.cu", ["-fmad=false"]),
     ("noalloc.cu", ["-fmad=true"]),
 ]
-CXX_UNITS = ["bvh_build.cpp"]
+CXX_UNITS = ["bvh_build.cpp", "scene_tables.cpp"]
 
 
 def _nvcc() -> str:

@@ -275,7 +275,15 @@ gt_status gt_scene_create(gt_context* ctx, const gt_scene_desc* d, gt_scene** ou
     for (uint32_t i = 0; i < d->num_materials; ++i) {
         const gt_material& m = d->materials[i];
         if (m.kind > GT_MAT_DIELECTRIC) return fail(GT_ERR_INVALID_ARG, "unknown material kind");
-        if (m.texture_kind > GT_TEX_CHECKER) return fail(GT_ERR_INVALID_ARG, "unknown texture kind");
+        if (m.texture_kind > GT_TEX_NOISE) return fail(GT_ERR_INVALID_ARG, "unknown texture kind");
+        if (m.texture_kind == GT_TEX_NOISE) {
+            const double v = m.tex[1], depth = m.tex[2], lo = m.tex[3], hi = m.tex[4];
+            if (!std::isfinite(m.tex[0]) || !(v == 0.0 || v == 1.0 || v == 2.0) || !(depth >= 0.0 && depth <= 64.0) ||
+                depth != std::floor(depth) || !(lo >= 0.0 && lo < 4294967296.0) || lo != std::floor(lo) ||
+                !(hi >= 0.0 && hi < 4294967296.0) || hi != std::floor(hi))
+                return fail(GT_ERR_INVALID_ARG, "noise texture needs a finite scale, variant 0-2, integer depth "
+                                                "0-64 and a seed split into two 32-bit halves");
+        }
         if (!finite3(m.color) || !std::isfinite(m.param)) return fail(GT_ERR_INVALID_ARG, "material values must be finite");
         if (m.kind == GT_MAT_DIELECTRIC && !(m.param > 0.0))
             return fail(GT_ERR_INVALID_ARG, "refractive index must be positive and finite");

@@ -33,6 +33,8 @@ template <> struct Num<float> {
     static GT_DEV float fmin(float a, float b) { return fminf(a, b); }
     static GT_DEV float fmax(float a, float b) { return fmaxf(a, b); }
     static GT_DEV float floor(float x) { return floorf(x); }
+    static GT_DEV float sin(float x) { return sinf(x); }
+    static GT_DEV int32_t to_i32(float x) { return __float2int_rz(x); } // saturating, NaN -> 0 (Rust `as`)
     static GT_DEV float fmod(float a, float b) { return fmodf(a, b); }
     static GT_DEV float round(float x) { return roundf(x); }
     static GT_DEV bool finite(float x) { return isfinite(x); }
@@ -47,6 +49,8 @@ template <> struct Num<double> {
     static GT_DEV double fmin(double a, double b) { return ::fmin(a, b); }
     static GT_DEV double fmax(double a, double b) { return ::fmax(a, b); }
     static GT_DEV double floor(double x) { return ::floor(x); }
+    static GT_DEV double sin(double x) { return ::sin(x); }
+    static GT_DEV int32_t to_i32(double x) { return __double2int_rz(x); } // saturating, NaN -> 0 (Rust `as`)
     static GT_DEV double fmod(double a, double b) { return ::fmod(a, b); }
     static GT_DEV double round(double x) { return ::round(x); }
     static GT_DEV bool finite(double x) { return isfinite(x); }

@@ -19,6 +19,7 @@ template <class R> struct GpuScene {
     uint2* meta = nullptr;
     Node<R>* nodes = nullptr;
     MatDev<R>* mats = nullptr;
+    PerlinDev<R>* perlin = nullptr; // one table set per noise-textured material
     SceneDev<R> view{};
 };
 

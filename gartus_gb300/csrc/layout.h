@@ -40,14 +40,24 @@ template <class R> struct alignas(16) Node {
 };
 
 // Materials (raytracing/material.rs) with a solid or checker colour source.
+// Perlin tables of one NoiseTexture (gmath/perlin.rs:8-31): 256 unit gradients (made in
+// f64 on the host, stored as R) and the three 256-entry permutations.
+template <class R> struct PerlinDev {
+    R gx[256], gy[256], gz[256];
+    uint16_t perm[3][256];
+};
+
 template <class R> struct MatDev {
     int32_t kind;
     int32_t tex;
     R color[3];
     R param;
-    R inv_scale;
+    R inv_scale; // checker: 1 / |scale|; noise: scale
     R even[3];
     R odd[3];
+    int32_t noise_variant;
+    int32_t noise_depth;
+    const PerlinDev<R>* noise; // this material's tables (GT_TEX_NOISE)
 };
 
 // Weighted sampling target (raytracing/scene.rs:423-497) with the geometry's derived

@@ -12,6 +12,7 @@
 #include <cstring>
 
 #include "internal.h"
+#include "scene_tables.h"
 #include "wavefront.cuh"
 
 namespace gt {
@@ -66,6 +67,7 @@ template <class R> void free_gpu(gt_scene* s) {
     cudaFree(g.meta);
     cudaFree(g.nodes);
     cudaFree(g.mats);
+    cudaFree(g.perlin);
     g = GpuScene<R>();
 }
 
@@ -168,6 +170,8 @@ template <class R> gt_status upload_scene(gt_scene* s) {
         link_of(b.right, nd.link[2], nd.link[3]);
     }
     std::vector<MatDev<R>> mats(s->mats.size());
+    std::vector<PerlinDev<R>> perlin;
+    std::vector<size_t> perlin_of; // material index of each table set
     for (size_t i = 0; i < s->mats.size(); ++i) {
         const gt_material& m = s->mats[i];
         MatDev<R>& d = mats[i];
@@ -184,8 +188,28 @@ template <class R> gt_status upload_scene(gt_scene* s) {
             put3(d.even, m.tex + 1);
             put3(d.odd, m.tex + 4);
         }
+        if (m.texture_kind == GT_TEX_NOISE) { // NoiseTexture (graphics/raytracing/texture.rs:293-322)
+            d.inv_scale = R(m.tex[0]);
+            d.noise_variant = int32_t(m.tex[1]);
+            d.noise_depth = int32_t(m.tex[2]);
+            PerlinTables t;
+            make_perlin_tables(uint64_t(m.tex[3]) | (uint64_t(m.tex[4]) << 32), t);
+            PerlinDev<R> pd;
+            for (int k = 0; k < 256; ++k) {
+                pd.gx[k] = R(t.grad[k][0]);
+                pd.gy[k] = R(t.grad[k][1]);
+                pd.gz[k] = R(t.grad[k][2]);
+            }
+            std::memcpy(pd.perm, t.perm, sizeof(pd.perm));
+            perlin.push_back(pd);
+            perlin_of.push_back(i);
+        }
     }
     free_gpu<R>(s);
+    if (!perlin.empty()) {
+        GT_CUDA(cudaMalloc(&g.perlin, perlin.size() * sizeof(PerlinDev<R>)));
+        for (size_t k = 0; k < perlin.size(); ++k) mats[perlin_of[k]].noise = g.perlin + k;
+    }
     GT_CUDA(cudaMalloc(&g.prims, std::max<size_t>(n, 1) * sizeof(PrimRec<R>)));
     GT_CUDA(cudaMalloc(&g.meta, std::max<size_t>(n, 1) * sizeof(uint2)));
     GT_CUDA(cudaMalloc(&g.nodes, std::max<size_t>(nodes.size(), 1) * sizeof(Node<R>)));
@@ -199,6 +223,9 @@ template <class R> gt_status upload_scene(gt_scene* s) {
         GT_CUDA(cudaMemcpyAsync(g.nodes, nodes.data(), nodes.size() * sizeof(Node<R>), cudaMemcpyHostToDevice, st));
     if (!mats.empty())
         GT_CUDA(cudaMemcpyAsync(g.mats, mats.data(), mats.size() * sizeof(MatDev<R>), cudaMemcpyHostToDevice, st));
+    if (!perlin.empty())
+        GT_CUDA(cudaMemcpyAsync(g.perlin, perlin.data(), perlin.size() * sizeof(PerlinDev<R>), cudaMemcpyHostToDevice,
+                                st));
     GT_CUDA(cudaStreamSynchronize(st));
     SceneDev<R>& v = g.view;
     v.prims = g.prims;

@@ -296,7 +296,59 @@ template <class R> GT_DEV HitRec<R> make_hit(const SceneDev<R>& sc, uint32_t i, 
 }
 
 // ------------------------------------------------------------------ materials
+// Perlin::noise (gmath/perlin.rs:36-58) and perlin_interp (106-124): the eight corner
+// gradients picked through the three permutations, weighted by smoothstep blends, summed
+// x-major in the reference's order.
+template <class R> GT_DEV R perlin_noise(const PerlinDev<R>* t, V3<R> p) {
+    const R fx = Num<R>::floor(p.x), fy = Num<R>::floor(p.y), fz = Num<R>::floor(p.z);
+    const R u = p.x - fx, v = p.y - fy, w = p.z - fz;
+    const uint32_t bx = uint32_t(Num<R>::to_i32(fx)), by = uint32_t(Num<R>::to_i32(fy)),
+                   bz = uint32_t(Num<R>::to_i32(fz));
+    const R uu = u * u * (R(3) - R(2) * u);
+    const R vv = v * v * (R(3) - R(2) * v);
+    const R ww = w * w * (R(3) - R(2) * w);
+    R accum = R(0);
+#pragma unroll
+    for (uint32_t ox = 0; ox < 2; ++ox)
+#pragma unroll
+        for (uint32_t oy = 0; oy < 2; ++oy)
+#pragma unroll
+            for (uint32_t oz = 0; oz < 2; ++oz) {
+                const uint32_t gi = uint32_t(t->perm[0][(bx + ox) & 255u]) ^ uint32_t(t->perm[1][(by + oy) & 255u]) ^
+                                    uint32_t(t->perm[2][(bz + oz) & 255u]);
+                const R wx = u - R(ox), wy = v - R(oy), wz = w - R(oz);
+                const R dot = t->gx[gi] * wx + t->gy[gi] * wy + t->gz[gi] * wz;
+                const R bxw = ox ? uu : R(1) - uu, byw = oy ? vv : R(1) - vv, bzw = oz ? ww : R(1) - ww;
+                accum = accum + bxw * byw * bzw * dot;
+            }
+    return accum;
+}
+
+// Perlin::turbulence (perlin.rs:61-74).
+template <class R> GT_DEV R perlin_turbulence(const PerlinDev<R>* t, V3<R> p, int32_t depth) {
+    R accum = R(0), weight = R(1);
+    for (int32_t k = 0; k < depth; ++k) {
+        accum = accum + weight * perlin_noise(t, p);
+        weight = weight * R(0.5);
+        p = V3<R>{p.x * R(2), p.y * R(2), p.z * R(2)};
+    }
+    return Num<R>::fabs(accum);
+}
+
+// NoiseTexture::sample_linear (graphics/raytracing/texture.rs:337-352).
+template <class R> GT_DEV R noise_intensity(const MatDev<R>& m, V3<R> p) {
+    const V3<R> q{p.x * m.inv_scale, p.y * m.inv_scale, p.z * m.inv_scale};
+    if (m.noise_variant == GT_NOISE_TURBULENCE) return perlin_turbulence(m.noise, q, m.noise_depth);
+    if (m.noise_variant == GT_NOISE_MARBLE)
+        return R(0.5) * (R(1) + Num<R>::sin(q.z + R(10) * perlin_turbulence(m.noise, q, m.noise_depth)));
+    return R(0.5) * (R(1) + perlin_noise(m.noise, q));
+}
+
 template <class R> GT_DEV V3<R> mat_color(const MatDev<R>& m, V3<R> p) {
+    if (m.tex == GT_TEX_NOISE) {
+        const R i = noise_intensity(m, p);
+        return V3<R>{i, i, i};
+    }
     if (m.tex == 1) { // CheckerTexture::sample_linear (raytracing/texture.rs:97-108)
         long long xi = (long long)Num<R>::floor(m.inv_scale * p.x);
         long long yi = (long long)Num<R>::floor(m.inv_scale * p.y);

@@ -161,7 +161,7 @@ template <class R> __global__ void __launch_bounds__(256) k_generate(Params<R> P
     }
 }
 
-template <class R> __global__ void __launch_bounds__(256) k_trace(Params<R> P, uint32_t cur) {
+template <class R> __global__ void __launch_bounds__(256, 6) k_trace(Params<R> P, uint32_t cur) {
     const uint32_t count = *reinterpret_cast<volatile uint32_t*>(&P.ps.counters[C_TRACE0 + cur]);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&P.ps.totals[0], (unsigned long long)count);
     const uint32_t* q = P.ps.q_trace[cur];

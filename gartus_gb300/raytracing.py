@@ -108,6 +108,32 @@ class RayMaterial:
                            (float(scale),) + _vec(even) + _vec(odd))
 
     @staticmethod
+    def _noise_tex(scale, variant: int, depth: int, seed: int) -> tuple:
+        seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+        depth = int(depth)
+        if not math.isfinite(float(scale)) or not 0 <= depth <= 64:
+            raise ValueError("noise texture needs a finite scale and a depth in 0..=64")
+        return (float(scale), float(variant), float(depth), float(seed & 0xFFFFFFFF), float(seed >> 32), 0.0, 0.0)
+
+    @staticmethod
+    def noise_lambertian(scale, seed=1) -> "RayMaterial":
+        """Lambertian::noise (material.rs:436-440): NoiseTexture::new(scale, seed)."""
+        return RayMaterial(abi.GT_MAT_LAMBERTIAN, (0.5, 0.5, 0.5), 0.0, abi.GT_TEX_NOISE,
+                           RayMaterial._noise_tex(scale, abi.GT_NOISE_PLAIN, 0, seed))
+
+    @staticmethod
+    def turbulence_lambertian(scale, depth=7, seed=1) -> "RayMaterial":
+        """Lambertian::from_texture(NoiseTexture::turbulence(scale, depth, seed))."""
+        return RayMaterial(abi.GT_MAT_LAMBERTIAN, (0.5, 0.5, 0.5), 0.0, abi.GT_TEX_NOISE,
+                           RayMaterial._noise_tex(scale, abi.GT_NOISE_TURBULENCE, depth, seed))
+
+    @staticmethod
+    def marble_lambertian(scale, seed=1) -> "RayMaterial":
+        """Lambertian::marble (material.rs:442-446): NoiseTexture::marble(scale, 7, seed)."""
+        return RayMaterial(abi.GT_MAT_LAMBERTIAN, (0.5, 0.5, 0.5), 0.0, abi.GT_TEX_NOISE,
+                           RayMaterial._noise_tex(scale, abi.GT_NOISE_MARBLE, 7, seed))
+
+    @staticmethod
     def diffuse_light(emit) -> "RayMaterial":
         emit = _vec(emit)
         if not _finite(emit):

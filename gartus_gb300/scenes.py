@@ -258,3 +258,150 @@ CONFIGS = {
     "final_scene": "400x225, 32 spp, depth 10, 486-sphere final scene (reference scenes.rs:563-624)",
     "cornell": "600x600, 16x16 stratified (256 spp), depth 50, GGX box + glass sphere, light-target mixture",
 }
+
+
+# ------------------------------------------------------- mesh-heavy scene (cfg 2)
+def perlin_tables(seed: int) -> tuple[np.ndarray, np.ndarray]:
+    """Perlin::new(seed) (gmath/perlin.rs:19-31, 83-101): 256 unit gradients, then the
+    x, y, z permutations (identity shuffled from the last index down)."""
+    rng = SampleRng(seed)
+    grad = np.array([rng.random_unit_vector() for _ in range(256)], dtype=np.float64)
+    perm = np.zeros((3, 256), dtype=np.int64)
+    for axis in range(3):
+        p = list(range(256))
+        for i in range(255, 0, -1):
+            t = int(rng.random_double() * (float(i) + 1.0))
+            p[i], p[t] = p[t], p[i]
+        perm[axis] = p
+    return grad, perm
+
+
+def perlin_noise(grad: np.ndarray, perm: np.ndarray, pts: np.ndarray) -> np.ndarray:
+    """Perlin::noise (perlin.rs:36-58) with perlin_interp (106-124) over an (N, 3) array of
+    points: the same f64 operations, in the same order, elementwise."""
+    pts = np.asarray(pts, dtype=np.float64)
+    fl = np.floor(pts)
+    f = pts - fl
+    base = fl.astype(np.int64)
+    s = f * f * (3.0 - 2.0 * f)
+    acc = np.zeros(len(pts))
+    for ox in (0, 1):
+        for oy in (0, 1):
+            for oz in (0, 1):
+                gi = (perm[0][(base[:, 0] + ox) & 255] ^ perm[1][(base[:, 1] + oy) & 255]
+                      ^ perm[2][(base[:, 2] + oz) & 255])
+                g = grad[gi]
+                dot = g[:, 0] * (f[:, 0] - ox) + g[:, 1] * (f[:, 1] - oy) + g[:, 2] * (f[:, 2] - oz)
+                bw = ((s[:, 0] if ox else 1.0 - s[:, 0]) * (s[:, 1] if oy else 1.0 - s[:, 1])
+                      * (s[:, 2] if oz else 1.0 - s[:, 2]))
+                acc = acc + bw * dot
+    return acc
+
+
+def height_map_triangles(heights: np.ndarray, x_size: float, z_size: float, height_scale: float,
+                         y_offset: float = 0.0) -> np.ndarray:
+    """PolygonMatrix::from_height_map (gmath/polygon_matrix.rs:510-541) as an (N, 3, 3)
+    vertex array: per cell (row-major, z outer) the triangles (p00, p01, p11), (p00, p11, p10)."""
+    rows, cols = heights.shape
+    xs = (np.arange(cols, dtype=np.float64) / float(cols - 1) - 0.5) * x_size
+    zs = (np.arange(rows, dtype=np.float64) / float(rows - 1) - 0.5) * z_size
+    ys = heights * height_scale + y_offset
+    X = np.broadcast_to(xs[None, :], (rows, cols))
+    Z = np.broadcast_to(zs[:, None], (rows, cols))
+    P = np.stack([X, ys, Z], axis=-1)
+    p00, p10, p01, p11 = P[:-1, :-1], P[:-1, 1:], P[1:, :-1], P[1:, 1:]
+    t0 = np.stack([p00, p01, p11], axis=2)
+    t1 = np.stack([p00, p11, p10], axis=2)
+    return np.stack([t0, t1], axis=2).reshape(-1, 3, 3)
+
+
+def torus_triangles(center, radius_small: float, radius_big: float, rings: int, tube: int) -> np.ndarray:
+    """PolygonMatrix::add_torus (gmath/polygon_matrix.rs:795-864) with separate ring and
+    tube counts (the reference takes one `steps` for both): ring i, tube j gives the
+    outward triangles (p0, p3, p2), (p0, p2, p1)."""
+    cx, cy, cz = center
+    theta = np.array([j * (1.0 / tube) * math.pi * 2.0 for j in range(tube)])
+    sin_t, cos_t = np.sin(theta), np.cos(theta)
+    ringpts = []
+    for i in range(rings):
+        phi = i * (1.0 / rings) * math.pi * 2.0
+        sp, cp = math.sin(phi), math.cos(phi)
+        x = cp * (radius_small * cos_t + radius_big) + cx
+        y = radius_small * sin_t + cy
+        z = -sp * (radius_small * cos_t + radius_big) + cz
+        ringpts.append(np.stack([x, y, z], axis=-1))
+    tris = []
+    for i in range(rings):
+        cur, nxt = ringpts[i], ringpts[(i + 1) % rings]
+        j1 = (np.arange(tube) + 1) % tube
+        p0, p1, p2, p3 = cur, cur[j1], nxt[j1], nxt
+        tris.append(np.stack([np.stack([p0, p3, p2], axis=1), np.stack([p0, p2, p1], axis=1)], axis=1))
+    return np.concatenate(tris).reshape(-1, 3, 3)
+
+
+def sky_with_sun(width: int = 2048, height: int = 1024, sun_elevation_deg: float = 35.0,
+                 sun_azimuth_deg: float = 60.0, sun_radius_deg: float = 0.5,
+                 sun_radiance: float = 5.0e4) -> np.ndarray:
+    """A linear f32 lat-long sky (row 0 = zenith, the EnvironmentLight layout of
+    environment.rs:174-202): a smooth horizon-to-zenith gradient, a dim ground and a
+    disc of the given angular radius and radiance around the sun direction."""
+    theta = (np.arange(height) + 0.5) / height * math.pi
+    phi = (np.arange(width) + 0.5) / width * 2.0 * math.pi
+    T, Ph = np.meshgrid(theta, phi, indexing="ij")
+    d = np.stack([np.sin(T) * np.cos(Ph), np.cos(T), np.sin(T) * np.sin(Ph)], axis=-1)
+    up = np.clip(d[..., 1], 0.0, 1.0)[..., None]
+    horizon, zenith, ground = np.array([0.85, 0.9, 1.0]), np.array([0.25, 0.45, 0.95]), np.array([0.18, 0.16, 0.14])
+    sky = horizon + (zenith - horizon) * np.sqrt(up)
+    img = np.where(d[..., 1:2] >= 0.0, sky, ground)
+    el, az = math.radians(sun_elevation_deg), math.radians(sun_azimuth_deg)
+    sun = np.array([math.cos(el) * math.cos(az), math.sin(el), math.cos(el) * math.sin(az)])
+    in_disc = (d @ sun) >= math.cos(math.radians(sun_radius_deg))
+    img[in_disc] = sun_radiance * np.array([1.0, 0.96, 0.9])
+    return img.astype(np.float32)
+
+
+def mesh_heavy_scene(size: int = 1024, tori: int = 64, rings: int = 32, tube: int = 64, seed: int = 1000,
+                     env_width: int = 2048, env_height: int = 1024):
+    """The mesh-heavy workload: a size x size Perlin fBm height field over a 100 x 100
+    extent (2 (size-1)^2 triangles: 2,093,058 at 1024), `tori` tori of rings x tube x 2
+    triangles at seeded positions, GGX microfacet materials (roughness U[0.05, 0.6],
+    grey albedo U[0.2, 0.9]) and an HDR sky with a 0.5 degree, 5e4-radiance sun.
+    Returns (scene, environment)."""
+    rng = SampleRng(seed)
+    extent = 100.0
+    grad, perm = perlin_tables(seed)
+    u = np.arange(size, dtype=np.float64) / float(size - 1) * 6.0
+    U, V = np.meshgrid(u, u, indexing="xy")  # rows = z, columns = x
+    base = np.stack([U.ravel(), np.full(U.size, 0.5), V.ravel()], axis=-1)
+    h = np.zeros(U.size)
+    for octave in range(4):  # fBm: sum_o 0.5^o noise(2^o p)
+        h = h + 0.5 ** octave * perlin_noise(grad, perm, base * 2.0 ** octave)
+    heights = h.reshape(size, size)
+
+    def ggx() -> RayMaterial:
+        a = rng.random_range(0.2, 0.9)
+        r = rng.random_range(0.05, 0.6)
+        return RayMaterial.ggx_microfacet((a, a, a), r)
+
+    scene = RayScene()
+    terrain = scene.add_material(ggx())
+    scene.add_triangles_array(terrain, height_map_triangles(heights, extent, extent, 0.15 * extent))
+    for _ in range(tori):
+        c = (rng.random_range(-35.0, 35.0), rng.random_range(14.0, 24.0), rng.random_range(-35.0, 35.0))
+        big = rng.random_range(1.5, 3.5)
+        small = rng.random_range(0.3, 0.8)
+        m = scene.add_material(ggx())
+        scene.add_triangles_array(m, torus_triangles(c, small, big, rings, tube))
+    scene.build_bvh()
+    from .raytracing import EnvironmentLight
+    return scene, EnvironmentLight(sky_with_sun(env_width, env_height))
+
+
+def mesh_heavy_camera(width: int = 1920, height: int = 1080, grid: int = 8, max_depth: int = 8) -> RayCamera:
+    """1920x1080, 8x8 stratified (64 spp), depth 8, looking over the height field at the tori."""
+    return (RayCamera(width, width / height)
+            .with_stratified_grid_width(grid)
+            .with_max_depth(max_depth)
+            .with_vertical_fov(40.0)
+            .with_look_at((0.0, 38.0, 75.0), (0.0, 8.0, 0.0))
+            .with_view_up((0.0, 1.0, 0.0)))

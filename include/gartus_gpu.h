@@ -80,11 +80,21 @@ typedef enum gt_material_kind {
     GT_MAT_DIELECTRIC = 5     /* param = refraction index               (material.rs:2264-2351) */
 } gt_material_kind;
 
-/* Colour source of a material (raytracing/texture.rs SolidColor / CheckerTexture). */
+/* Colour source of a material (graphics/raytracing/texture.rs SolidColor, CheckerTexture,
+ * NoiseTexture). */
 typedef enum gt_texture_kind {
-    GT_TEX_SOLID = 0,  /* the material's color                                          */
-    GT_TEX_CHECKER = 1 /* tex[0] = scale, tex[1..4] = even colour, tex[4..7] = odd colour */
+    GT_TEX_SOLID = 0,   /* the material's color                                           */
+    GT_TEX_CHECKER = 1, /* tex[0] = scale, tex[1..4] = even colour, tex[4..7] = odd colour  */
+    GT_TEX_NOISE = 2    /* Perlin: tex[0] = scale, tex[1] = variant (gt_noise_variant),
+                           tex[2] = octave depth, tex[3] / tex[4] = seed bits 0-31 / 32-63  */
 } gt_texture_kind;
+
+/* NoiseTexture kinds (graphics/raytracing/texture.rs:287-291). */
+typedef enum gt_noise_variant {
+    GT_NOISE_PLAIN = 0,      /* 0.5 (1 + noise(scale p))                         */
+    GT_NOISE_TURBULENCE = 1, /* turbulence(scale p, depth)                      */
+    GT_NOISE_MARBLE = 2      /* 0.5 (1 + sin(q.z + 10 turbulence(q, depth))), q = scale p */
+} gt_noise_variant;
 
 typedef struct gt_material {
     uint32_t kind;         /* gt_material_kind */

@@ -45,6 +45,8 @@ def lib() -> C.CDLL:
                 "orc_pixel_seed": (u64, [u64, u32, u32]),
                 "orc_rng_u64": (None, [u64, u32, vp]),
                 "orc_rng_double": (None, [u64, u32, vp]),
+                "orc_perlin": (None, [u64, C.c_int, C.c_int, u32, vp, vp]),
+                "orc_perlin_tables": (None, [u64, vp, vp]),
                 "orc_intersect": (i32, [vp, vp, f64, f64, vp]),
                 "orc_geometry_bounds": (None, [vp, vp]),
                 "orc_geometry_pdf": (f64, [vp, vp, f64, vp]),

@@ -19,10 +19,12 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <memory>
 #include <numeric>
 #include <optional>
 #include <stdexcept>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "../include/gartus_gpu.h"
@@ -61,6 +63,12 @@ inline uint32_t as_u32(double x) {
     if (!(x > 0.0)) return 0;
     if (x >= 4294967295.0) return UINT32_MAX;
     return static_cast<uint32_t>(x);
+}
+inline int32_t as_i32(double x) { // Rust `as i32`: saturating, NaN -> 0
+    if (std::isnan(x)) return 0;
+    if (x >= 2147483647.0) return INT32_MAX;
+    if (x <= -2147483648.0) return INT32_MIN;
+    return static_cast<int32_t>(x);
 }
 inline int64_t as_i64(double x) {
     if (std::isnan(x)) return 0;
@@ -626,6 +634,63 @@ template <class R> struct RayTraversal {
     }
 };
 
+// ------------------------------------------------------------------ Perlin noise
+// Perlin (gmath/perlin.rs:8-137).  The tables are made in f64 as in the reference and
+// read as R when evaluated.
+struct Perlin {
+    double grad[256][3];
+    int perm[3][256];
+    explicit Perlin(uint64_t seed = 1) { // Perlin::new, perlin.rs:19-31
+        SampleRng rng(seed);
+        for (auto& g : grad) { // random_unit_vector = the spherical form, random.rs:88-91
+            V3<double> v = rng.random_unit_vector_spherical<double>();
+            g[0] = v.x;
+            g[1] = v.y;
+            g[2] = v.z;
+        }
+        for (auto& p : perm) { // generate_permutation / permute, perlin.rs:83-101
+            for (int i = 0; i < 256; ++i) p[i] = i;
+            for (int i = 255; i > 0; --i) {
+                int target = int(rng.random_double<double>() * (double(i) + 1.0));
+                std::swap(p[i], p[target]);
+            }
+        }
+    }
+    template <class R> R noise(V3<R> p) const { // perlin.rs:36-58, perlin_interp 106-124
+        R fx = p.x - std::floor(p.x), fy = p.y - std::floor(p.y), fz = p.z - std::floor(p.z);
+        int32_t bx = as_i32(double(std::floor(p.x))), by = as_i32(double(std::floor(p.y))),
+                bz = as_i32(double(std::floor(p.z)));
+        R uu = fx * fx * (R(3) - R(2) * fx);
+        R vv = fy * fy * (R(3) - R(2) * fy);
+        R ww = fz * fz * (R(3) - R(2) * fz);
+        R accum = R(0);
+        for (int ox = 0; ox < 2; ++ox)
+            for (int oy = 0; oy < 2; ++oy)
+                for (int oz = 0; oz < 2; ++oz) {
+                    // (base + offset) & 255 on i32 (wrapping add in release builds)
+                    auto idx = [](int32_t b, int o) { return int((uint32_t(b) + uint32_t(o)) & 255u); };
+                    int gi = perm[0][idx(bx, ox)] ^ perm[1][idx(by, oy)] ^ perm[2][idx(bz, oz)];
+                    R gx = R(grad[gi][0]), gy = R(grad[gi][1]), gz = R(grad[gi][2]);
+                    R wx = fx - R(ox), wy = fy - R(oy), wz = fz - R(oz);
+                    R dot = gx * wx + gy * wy + gz * wz;
+                    R bxw = ox ? uu : R(1) - uu; // blend, perlin.rs:130-136
+                    R byw = oy ? vv : R(1) - vv;
+                    R bzw = oz ? ww : R(1) - ww;
+                    accum = accum + bxw * byw * bzw * dot;
+                }
+        return accum;
+    }
+    template <class R> R turbulence(V3<R> p, int depth) const { // perlin.rs:61-74
+        R accum = R(0), weight = R(1);
+        for (int k = 0; k < depth; ++k) {
+            accum = accum + weight * noise(p);
+            weight = weight * R(0.5);
+            p = V3<R>{p.x * R(2), p.y * R(2), p.z * R(2)};
+        }
+        return std::fabs(accum);
+    }
+};
+
 // ------------------------------------------------------------------ materials
 template <class R> struct Material {
     int kind = GT_MAT_LAMBERTIAN;
@@ -634,6 +699,9 @@ template <class R> struct Material {
     R param{0};
     R tex_inv_scale{1};
     V3<R> even, odd;
+    R noise_scale{1};
+    int noise_variant = 0, noise_depth = 0;
+    std::shared_ptr<Perlin> perlin;
     static Material from_desc(const gt_material& m) {
         Material r;
         r.kind = int(m.kind);
@@ -647,11 +715,26 @@ template <class R> struct Material {
             r.even = v3<R>(m.tex + 1);
             r.odd = v3<R>(m.tex + 4);
         }
+        if (m.texture_kind == GT_TEX_NOISE) { // NoiseTexture::{new, turbulence, marble}, texture.rs:293-322
+            r.noise_scale = R(m.tex[0]);
+            r.noise_variant = int(m.tex[1]);
+            r.noise_depth = int(m.tex[2]);
+            r.perlin = std::make_shared<Perlin>(uint64_t(m.tex[3]) | (uint64_t(m.tex[4]) << 32));
+        }
         return r;
     }
     // MaterialColorSource::sample (material.rs:307-314): SolidColor or CheckerTexture
     // (raytracing/texture.rs:97-108: parity of floor(p * inv_scale) summed over axes).
     V3<R> sample(const Hit<R>& h) const {
+        if (texture == GT_TEX_NOISE) { // NoiseTexture::sample_linear, texture.rs:337-352
+            V3<R> q{h.point.x * noise_scale, h.point.y * noise_scale, h.point.z * noise_scale};
+            R i;
+            if (noise_variant == GT_NOISE_TURBULENCE) i = perlin->turbulence(q, noise_depth);
+            else if (noise_variant == GT_NOISE_MARBLE)
+                i = R(0.5) * (R(1) + std::sin(q.z + R(10) * perlin->turbulence(q, noise_depth)));
+            else i = R(0.5) * (R(1) + perlin->noise(q));
+            return V3<R>{i, i, i};
+        }
         if (texture == GT_TEX_CHECKER) {
             int64_t xi = as_i64(double(std::floor(tex_inv_scale * h.point.x)));
             int64_t yi = as_i64(double(std::floor(tex_inv_scale * h.point.y)));

@@ -244,6 +244,30 @@ void orc_rng_u64(uint64_t seed, uint32_t n, uint64_t* out) {
     for (uint32_t i = 0; i < n; ++i) out[i] = r.next_u64();
 }
 
+// Perlin::noise / turbulence at n points (xyz triples); depth < 0 = noise, else turbulence.
+void orc_perlin(uint64_t seed, int precision, int depth, uint32_t n, const double* pts, double* out) {
+    Perlin p(seed);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (precision == 1) {
+            V3<double> q{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+            out[i] = depth < 0 ? p.noise(q) : p.turbulence(q, depth);
+        } else {
+            V3<float> q{float(pts[3 * i]), float(pts[3 * i + 1]), float(pts[3 * i + 2])};
+            out[i] = depth < 0 ? double(p.noise(q)) : double(p.turbulence(q, depth));
+        }
+    }
+}
+
+// The permutation tables and gradients of Perlin::new(seed).
+void orc_perlin_tables(uint64_t seed, double* grad768, int32_t* perm768) {
+    Perlin p(seed);
+    for (int i = 0; i < 256; ++i)
+        for (int k = 0; k < 3; ++k) {
+            grad768[i * 3 + k] = p.grad[i][k];
+            perm768[k * 256 + i] = p.perm[k][i];
+        }
+}
+
 void orc_rng_double(uint64_t seed, uint32_t n, double* out) {
     SampleRng r(seed);
     for (uint32_t i = 0; i < n; ++i) out[i] = r.random_double<double>();

@@ -60,6 +60,24 @@ def test_primary_hits_and_stats_bit_exact(gpu_context, name):
     assert scene.bvh_node_count(gpu_context) == oracle.OracleScene.from_ray_scene(scene).node_count()
 
 
+def test_mesh_heavy_primary_hits_bit_exact(gpu_context):
+    # The full 2,355,202-triangle mesh scene (Perlin height field + 64 tori): ids, hit
+    # distances and traversal statistics of every 16th pixel's primary ray equal the
+    # oracle's on the reference-layout BVH.
+    scene, _ = scenes.mesh_heavy_scene(env_width=8, env_height=4)
+    assert len(scene) == 2 * 1023 * 1023 + 64 * 4096
+    cam = scenes.mesh_heavy_camera(1920, 1080, 1, 8)
+    pt = PathTracer(cam, context=gpu_context)
+    ids, t, stats = pt.trace_primary(scene, 16)
+    o = oracle.OracleScene.from_ray_scene(scene)
+    o_ids, o_t, o_stats = o.trace_primary(cam.desc(), 16)
+    np.testing.assert_array_equal(ids, o_ids)
+    np.testing.assert_array_equal(t, o_t)
+    assert stats == o_stats
+    assert (ids >= 0).mean() > 0.5  # the camera sees the height field
+    assert scene.bvh_node_count(gpu_context) == o.node_count()
+
+
 def test_randomized_scenes_match_oracle_and_bruteforce(gpu_context):
     # graphics/raytracing.rs:1340-1370 on the GPU: BVH hits equal brute force, stats equal.
     for seed in range(1, 17):
@@ -246,6 +264,58 @@ def test_moving_spheres_and_checker(gpu_context):
     ref, _ = _oracle_render(scene, cam)
     err = rel_err(img.pixels64, ref, floor=1e-12).max(axis=2)
     assert (err <= 1e-9).mean() >= 0.99
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_mesh_heavy_small(gpu_context, precision):
+    # The mesh-heavy generator at a small size: triangle meshes, GGX everywhere, an f32
+    # HDR sky with a 5e4 sun (next-event estimation forced by the environment).
+    scene, env = scenes.mesh_heavy_scene(size=40, tori=6, rings=8, tube=12, env_width=256, env_height=128)
+    cam = scenes.mesh_heavy_camera(48, 27, 2, 8)
+    pt = PathTracer(cam, precision=precision, context=gpu_context)
+    ref, acc = _oracle_render(scene, cam, env=env)
+    if precision == "f64":
+        img = pt.render_with_environment_hdr_image(scene, env, want64=True)
+        np.testing.assert_array_equal(img.accepted, acc)
+        err = rel_err(img.pixels64, ref, floor=1e-12).max(axis=2)
+        assert (err <= 1e-9).mean() >= 0.99, err.max()
+    else:
+        img = pt.render_with_environment_hdr_image(scene, env)
+        ref32, _ = _oracle_render(scene, cam, env=env, precision=0)
+        n = ref.shape[0] * ref.shape[1]
+        assert _divergent(img.pixels, ref) <= _divergent(ref32, ref) + 0.02 * n
+    assert np.isfinite(img.pixels).all()
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_noise_textures(gpu_context, precision):
+    # NoiseTexture plain, turbulence and marble (graphics/raytracing/texture.rs:278-352)
+    # on Lambertian spheres; the Perlin tables are made on the host in f64.
+    scene = RayScene()
+    ground = scene.add_material(RayMaterial.noise_lambertian(4.0, seed=7))
+    scene.add_sphere((0.0, -1000.0, 0.0), 1000.0, ground)
+    marble = scene.add_material(RayMaterial.marble_lambertian(4.0, seed=3))
+    scene.add_sphere((0.0, 2.0, 0.0), 2.0, marble)
+    turb = scene.add_material(RayMaterial.turbulence_lambertian(2.5, depth=5, seed=11))
+    scene.add_sphere((3.5, 1.0, 1.5), 1.0, turb)
+    scene.build_bvh()
+    cam = (RayCamera(48, 1.5).with_samples_per_pixel(4).with_max_depth(6).with_vertical_fov(20.0)
+           .with_look_at((13.0, 2.0, 3.0), (0.0, 2.0, 0.0)))
+    pt = PathTracer(cam, precision=precision, context=gpu_context)
+    ref, acc = _oracle_render(scene, cam)
+    if precision == "f64":
+        img = pt.render_hdr_image(scene, want64=True)
+        np.testing.assert_array_equal(img.accepted, acc)
+        err = rel_err(img.pixels64, ref, floor=1e-12).max(axis=2)
+        assert err.max() <= 1e-9, err.max()
+    else:
+        img = pt.render_hdr_image(scene)
+        ref32, _ = _oracle_render(scene, cam, precision=0)
+        n = ref.shape[0] * ref.shape[1]
+        assert _divergent(img.pixels, ref) <= _divergent(ref32, ref) + 0.02 * n
+        assert np.median(rel_err(img.pixels, ref, floor=1e-3)) <= 1e-5
+    # the textures vary over the image: not a constant grey
+    assert np.std(ref) > 1e-3
 
 
 def test_edge_cases(gpu_context):

@@ -327,3 +327,85 @@ def test_oracle_window_matches_full_image():
     full, _ = o.render(cam, threads=4)
     part, _ = o.render(cam, threads=2, window=(5, 3, 9, 7))
     np.testing.assert_array_equal(full[3:10, 5:14], part)
+
+
+# ---------------------------------------------------------------- Perlin noise
+def _perlin(seed, pts, depth=-1, precision=1):
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    out = np.zeros(len(pts))
+    oracle.lib().orc_perlin(seed, precision, depth, len(pts), pts.ctypes.data, out.ctypes.data)
+    return out
+
+
+def _perlin_python(seed, p):
+    """A second, independent restatement of Perlin::new + Perlin::noise (gmath/perlin.rs:19-58,
+    83-136) in plain Python floats, to pin the oracle's C++ version."""
+    state = seed
+
+    def unit():
+        nonlocal state
+        state = (state + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+        v = state
+        v = ((v ^ (v >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+        v = ((v ^ (v >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+        return ((v ^ (v >> 31)) >> 11) * (1.0 / 9007199254740992.0)
+
+    grads = []
+    for _ in range(256):
+        r1, r2 = unit(), unit()
+        z = 1.0 - 2.0 * r2
+        radius = math.sqrt(1.0 - z * z)
+        phi = 6.283185307179586 * r1
+        grads.append((math.cos(phi) * radius, math.sin(phi) * radius, z))
+    perms = []
+    for _ in range(3):
+        q = list(range(256))
+        for i in range(255, 0, -1):
+            t = int(unit() * (i + 1.0))
+            q[i], q[t] = q[t], q[i]
+        perms.append(q)
+    fx, fy, fz = (c - math.floor(c) for c in p)
+    bx, by, bz = (int(math.floor(c)) for c in p)
+    s = [v * v * (3.0 - 2.0 * v) for v in (fx, fy, fz)]
+    acc = 0.0
+    for ox in (0, 1):
+        for oy in (0, 1):
+            for oz in (0, 1):
+                g = grads[perms[0][(bx + ox) & 255] ^ perms[1][(by + oy) & 255] ^ perms[2][(bz + oz) & 255]]
+                dot = g[0] * (fx - ox) + g[1] * (fy - oy) + g[2] * (fz - oz)
+                bw = (s[0] if ox else 1.0 - s[0]) * (s[1] if oy else 1.0 - s[1]) * (s[2] if oz else 1.0 - s[2])
+                acc += bw * dot
+    return acc
+
+
+def test_perlin_repeatable_for_same_seed():  # gmath/perlin.rs:152-161
+    p = [[1.25, -0.5, 3.75]]
+    assert _perlin(7, p)[0] == _perlin(7, p)[0]
+    assert _perlin(7, p, depth=7)[0] == _perlin(7, p, depth=7)[0]
+
+
+def test_perlin_varies_with_seed_and_position():  # gmath/perlin.rs:163-173
+    a = _perlin(7, [[1.25, -0.5, 3.75], [1.5, -0.5, 3.75]])
+    b = _perlin(8, [[1.25, -0.5, 3.75]])
+    assert abs(a[0] - b[0]) > 2.220446049250313e-16
+    assert abs(a[0] - a[1]) > 2.220446049250313e-16
+
+
+def test_perlin_turbulence_non_negative():  # gmath/perlin.rs:175-180
+    assert _perlin(11, [[0.2, 0.4, 0.6]], depth=7)[0] >= 0.0
+
+
+def test_perlin_matches_independent_restatement():
+    rng = np.random.default_rng(5)
+    pts = rng.uniform(-40.0, 40.0, size=(24, 3))
+    pts[0] = (0.0, 0.0, 0.0)     # lattice point: noise 0
+    pts[1] = (-0.5, 255.5, 256.25)  # wraps the 256-entry tables
+    for seed in (1, 7, 1 << 40):
+        got = _perlin(seed, pts)
+        want = [_perlin_python(seed, p) for p in pts]
+        np.testing.assert_array_equal(got, want)
+    assert _perlin(3, [[0.0, 0.0, 0.0]])[0] == 0.0
+    # turbulence = |sum_k 0.5^k noise(2^k p)|
+    p = pts[2]
+    want = abs(sum(0.5 ** k * _perlin(9, [p * 2.0 ** k])[0] for k in range(5)))
+    assert abs(_perlin(9, [p], depth=5)[0] - want) <= 1e-15
