@@ -40,7 +40,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="cornell", choices=["cornell", "final", "mesh"])
+    ap.add_argument("--config", default="cornell", choices=["cornell", "final", "mesh", "batch"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--schedule", default="auto", choices=["auto", "wavefront", "persistent"])
@@ -74,6 +74,15 @@ def workload(name, width=0, grid=0):
                "sampling": f"stratified {grid}x{grid}", "lights": "HDR environment 2048x1024 f32 with sun (NEE)",
                "primitives": len(scene), "precision": "f32"}
         return scene, None, env, cam, cfg
+    if name == "batch":
+        scene, lights = scenes.batch_scene()
+        width = width or 512
+        cams = scenes.batch_cameras(64, width)
+        cfg = {"workload": "batch_64_frames_orbit_moving_spheres", "frames": len(cams), "width": width,
+               "height": width, "spp": "adaptive, minimum cycling 4/8/16/32/64, cap 256, threshold 0.02",
+               "max_depth": 50, "sampling": "random (adaptive)", "lights": "SamplingTargetList mixture (weight 0.5)",
+               "primitives": len(scene), "precision": "f32", "shutter": "[0, 1), two moving spheres"}
+        return scene, lights, None, cams, cfg
     scene = scenes.final_scene_ray_scene()
     width = width or 400
     cam = scenes.final_scene_camera(width, 32)
@@ -165,8 +174,11 @@ def traffic_from_profiles(kernel: str, workload_name: str):
 # ----------------------------------------------------------------------------------
 def cpu_baseline(scene, lights, env, cam, seconds: float):
     """The oracle (C++ restatement of the reference's rayon renderer) on a band of rows
-    of the same frame, with every host thread; returns (Msamples/s, threads, sample)."""
+    of the same frame (of the middle frame for a batch), with every host thread; returns
+    (Msamples/s, threads, sample)."""
     import oracle
+    if isinstance(cam, list):
+        cam = cam[len(cam) // 2]
     o = oracle.OracleScene.from_ray_scene(scene)
     la = lights.to_array() if lights is not None else None
     w, h, spp = cam.image_size()
@@ -241,10 +253,15 @@ def run_ours(args):
     torch.cuda.set_device(device)
     ctx = Context(device)
     scene, lights, env, cam, cfg = workload(args.config, args.width, args.grid)
+    cams = cam if isinstance(cam, list) else None
+    if cams is not None:
+        cam = cams[0]
     pt = PathTracer(cam, context=ctx, schedule=args.schedule, tail_slots=args.tail_slots)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
 
     def render():
+        if cams is not None:
+            return pt.render_batch_hdr_images(scene, cams, lights=lights, environment=env)[-1]
         if env is not None:
             return pt.render_with_environment_hdr_image(scene, env)
         if lights is not None:
@@ -312,19 +329,32 @@ def run_ours(args):
         eh = C.c_void_p()
         if env is not None:
             check(lib().gt_environment_create(ctx.handle, C.byref(env.desc()), C.byref(eh)))
-        w, h, _ = cam.image_size()
-        rgb = np.empty((h, w, 3), dtype=np.float32)
-        acc = np.empty((h, w), dtype=np.uint32)
-        f = abi.gt_frame()
-        f.struct_size = C.sizeof(abi.gt_frame)
-        f.width, f.height, f.device_buffers = w, h, 0
-        f.rgb, f.accepted = rgb.ctypes.data, acc.ctypes.data
+        outs, frames, descs = [], [], []
+        for c in (cams or [cam]):
+            w, h, _ = c.image_size()
+            rgb = np.empty((h, w, 3), dtype=np.float32)
+            acc = np.empty((h, w), dtype=np.uint32)
+            f = abi.gt_frame()
+            f.struct_size = C.sizeof(abi.gt_frame)
+            f.width, f.height, f.device_buffers = w, h, 0
+            f.rgb, f.accepted = rgb.ctypes.data, acc.ctypes.data
+            outs += [rgb, acc]
+            frames.append(f)
+            descs.append(c.desc())
         o = abi.gt_render_opts()
         o.struct_size = C.sizeof(abi.gt_render_opts)
         stt = abi.gt_render_stats()
         o.stats = C.pointer(stt)
-        check(lib().gt_render(sh, lh if la is not None else None, eh if env is not None else None,
-                              C.byref(cam.desc()), C.byref(o), C.byref(f)))
+        if cams is not None:
+            jobs = (abi.gt_frame_job * len(cams))()
+            for i in range(len(cams)):
+                jobs[i].camera = C.pointer(descs[i])
+                jobs[i].frame = C.pointer(frames[i])
+            check(lib().gt_render_batch(sh, lh if la is not None else None, eh if env is not None else None,
+                                        jobs, len(cams), C.byref(o)))
+        else:
+            check(lib().gt_render(sh, lh if la is not None else None, eh if env is not None else None,
+                                  C.byref(descs[0]), C.byref(o), C.byref(frames[0])))
         lib().gt_scene_destroy(sh)
         if la is not None:
             lib().gt_lights_destroy(lh)
@@ -335,12 +365,15 @@ def run_ours(args):
         nodes = max(len(prims) - 1, 1)
         h2d = len(prims) * 64 + len(prims) * 8 + nodes * 64 + len(mats) * 64 + (len(la) * 128 if la is not None else 0)
         h2d += env.texels.nbytes if env is not None else 0
-        d2h = rgb.nbytes + acc.nbytes
+        h2d += len(descs) * C.sizeof(abi.gt_camera_desc)
+        d2h = sum(x.nbytes for x in outs)
     e2e = statistics.median(e2e_vals) * world
 
     # Roofline of the dominant kernel from one profiled frame (events around every launch).
     prof = PathTracer(cam, context=ctx, profile=True, schedule=args.schedule, tail_slots=args.tail_slots)
-    if env is not None:
+    if cams is not None:
+        prof.render_batch_hdr_images(scene, cams, lights=lights, environment=env)
+    elif env is not None:
         prof.render_with_environment_hdr_image(scene, env)
     elif lights is not None:
         prof.render_with_lights_hdr_image(scene, lights)

@@ -50,6 +50,8 @@ def _declare(L: C.CDLL) -> None:
                                   P(abi.gt_bvh_stats)]),
         "gt_render_noalloc": (st, [C.c_void_p, C.c_void_p, C.c_void_p, P(abi.gt_camera_desc), C.c_void_p,
                                    C.c_void_p]),
+        "gt_render_batch": (st, [C.c_void_p, C.c_void_p, C.c_void_p, P(abi.gt_frame_job), C.c_uint32,
+                                 P(abi.gt_render_opts)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -85,4 +87,5 @@ EXPORTED_SYMBOLS = [
     "gt_context_destroy", "gt_scene_create", "gt_scene_destroy", "gt_scene_bvh_node_count",
     "gt_scene_emissive_targets", "gt_lights_create", "gt_lights_destroy", "gt_environment_create",
     "gt_environment_destroy", "gt_render", "gt_trace_rays", "gt_trace_primary", "gt_render_noalloc",
+    "gt_render_batch",
 ]

@@ -218,6 +218,10 @@ class gt_frame(C.Structure):
     ]
 
 
+class gt_frame_job(C.Structure):
+    _fields_ = [("camera", C.POINTER(gt_camera_desc)), ("frame", C.POINTER(gt_frame))]
+
+
 class gt_bvh_stats(C.Structure):
     _fields_ = [
         ("rays", C.c_uint64),
@@ -235,5 +239,5 @@ class gt_bvh_stats(C.Structure):
 
 STRUCTS = [
     gt_geometry, gt_primitive, gt_material, gt_scene_desc, gt_light_target, gt_environment_desc,
-    gt_camera_desc, gt_render_opts, gt_frame, gt_bvh_stats, gt_render_stats,
+    gt_camera_desc, gt_render_opts, gt_frame, gt_frame_job, gt_bvh_stats, gt_render_stats,
 ]

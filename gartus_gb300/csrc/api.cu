@@ -457,6 +457,44 @@ void gt_environment_destroy(gt_environment* e) {
     delete e;
 }
 
+gt_status gt_render_batch(gt_scene* s, const gt_lights* l, const gt_environment* e, const gt_frame_job* jobs,
+                          uint32_t count, const gt_render_opts* o) {
+    GT_GUARD_BEGIN
+    if (!s || (!jobs && count)) return fail(GT_ERR_INVALID_ARG, "null argument");
+    if (count == 0) return fail(GT_ERR_INVALID_ARG, "a batch needs at least one frame");
+    gt_render_opts opts;
+    std::memset(&opts, 0, sizeof(opts));
+    if (o) {
+        if (o->struct_size < sizeof(gt_render_opts)) return fail(GT_ERR_INVALID_ARG, "options struct_size too small");
+        opts = *o;
+    }
+    if (opts.precision > GT_PRECISION_F64) return fail(GT_ERR_INVALID_ARG, "unknown precision");
+    if (opts.aovs) return fail(GT_ERR_UNSUPPORTED, "denoising AOVs are not rendered in batches");
+    if ((l && l->ctx != s->ctx) || (e && e->ctx != s->ctx))
+        return fail(GT_ERR_INVALID_ARG, "lights, environment and scene must share a context");
+    std::vector<CamHost> cams(count);
+    std::vector<gt_frame*> frames(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const gt_frame_job& j = jobs[i];
+        if (!j.camera || !j.frame) return fail(GT_ERR_INVALID_ARG, "batch job without a camera or a frame");
+        if (j.frame->struct_size < sizeof(gt_frame)) return fail(GT_ERR_INVALID_ARG, "frame struct_size too small");
+        gt_status rc = validate_camera(*j.camera);
+        if (rc != GT_OK) return rc;
+        cams[i] = init_camera(*j.camera, e != nullptr);
+        if (j.frame->width != cams[i].width || j.frame->height != cams[i].height)
+            return fail(GT_ERR_INVALID_ARG, "frame size does not match the camera's image size");
+        if (!j.frame->rgb) return fail(GT_ERR_INVALID_ARG, "frame has no rgb buffer");
+        frames[i] = j.frame;
+    }
+    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    cudaError_t ce = cudaSetDevice(s->ctx->device);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
+    auto* env = const_cast<gt_environment*>(e);
+    if (opts.precision == GT_PRECISION_F64) return render_batch_f64(s, l, env, cams.data(), count, opts, frames.data());
+    return render_batch_f32(s, l, env, cams.data(), count, opts, frames.data());
+    GT_GUARD_END
+}
+
 gt_status gt_render(gt_scene* s, const gt_lights* l, const gt_environment* e, const gt_camera_desc* c,
                     const gt_render_opts* o, gt_frame* f) {
     GT_GUARD_BEGIN

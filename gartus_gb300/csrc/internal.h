@@ -106,6 +106,10 @@ gt_status render_f32(gt_scene* s, const gt_lights* l, gt_environment* e, const C
                      const gt_render_opts& opts, gt_frame* frame);
 gt_status render_f64(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost& cam,
                      const gt_render_opts& opts, gt_frame* frame);
+gt_status render_batch_f32(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost* cams, uint32_t count,
+                           const gt_render_opts& opts, gt_frame* const* frames);
+gt_status render_batch_f64(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost* cams, uint32_t count,
+                           const gt_render_opts& opts, gt_frame* const* frames);
 gt_status trace_rays_f64(gt_scene* s, const double* rays, uint32_t count, double tmin, double tmax,
                          int32_t* ids, double* t, gt_bvh_stats* stats);
 void free_gpu_f32(gt_scene* s);

@@ -10,6 +10,11 @@ gt_status render_f64(gt_scene* s, const gt_lights* l, gt_environment* e, const C
     return render_impl<double>(s, l, e, cam, opts, frame);
 }
 
+gt_status render_batch_f64(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost* cams, uint32_t count,
+                           const gt_render_opts& opts, gt_frame* const* frames) {
+    return render_batch_impl<double>(s, l, e, cams, count, opts, frames);
+}
+
 gt_status trace_rays_f64(gt_scene* s, const double* rays, uint32_t count, double tmin, double tmax,
                          int32_t* ids, double* t, gt_bvh_stats* stats) {
     return trace_impl<double>(s, rays, count, tmin, tmax, ids, t, stats);

@@ -891,6 +891,148 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
                             iters);
 }
 
+// Batched frames (many small frames of one scene, each with its own camera, sample count
+// and adaptive settings): every frame's pixels in one k_persistent launch in BATCH mode,
+// each pixel rendered with its frame's camera.  Pixels are taken in frame order; the
+// images equal one gt_render per frame.
+template <class R>
+gt_status render_batch_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost* cams, uint32_t count,
+                            const gt_render_opts& opts, gt_frame* const* frames) {
+    gt_context* ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    gt_status rc;
+    if ((rc = upload_scene<R>(s)) != GT_OK) return rc;
+    const bool use_lights = l != nullptr;
+    const bool use_env = e != nullptr;
+    Params<R> P;
+    std::memset(&P, 0, sizeof(P));
+    P.sc = gpu_of<R>(s).view;
+    if (use_lights) {
+        if ((rc = upload_lights<R>(const_cast<gt_lights*>(l))) != GT_OK) return rc;
+        P.lights = lights_of<R>(const_cast<gt_lights*>(l)).view;
+    }
+    if (use_env) {
+        if ((rc = upload_env<R>(e)) != GT_OK) return rc;
+        P.env = env_of<R>(e).view;
+    }
+    std::vector<CamDev<R>> cd(count);
+    std::vector<uint32_t> start(size_t(count) + 1);
+    uint64_t total = 0;
+    bool want64 = false;
+    for (uint32_t i = 0; i < count; ++i) {
+        cd[i] = cam_dev<R>(cams[i], use_lights, use_env);
+        start[i] = uint32_t(total);
+        total += uint64_t(cams[i].width) * cams[i].height;
+        if (total >= (1ull << 32)) return fail(GT_ERR_INVALID_ARG, "a batch holds fewer than 2^32 pixels");
+        want64 = want64 || frames[i]->rgb64 != nullptr;
+    }
+    start[count] = uint32_t(total);
+    const uint32_t n = uint32_t(total);
+    P.cam = cd[0];
+    P.num_frames = count;
+    P.ps.n = n;
+
+    auto lay = [&](Bump& bb, CamDev<R>** dcams, uint32_t** dstart, uint32_t** next, float** rgb, double** rgb64,
+                   uint32_t** acc) {
+        *dcams = bb.take<CamDev<R>>(count);
+        *dstart = bb.take<uint32_t>(size_t(count) + 1);
+        P.ps.counters = bb.take<uint32_t>(C_COUNT);
+        P.ps.totals = bb.take<unsigned long long>(8);
+        *next = bb.take<uint32_t>(1);
+        *rgb = bb.take<float>(size_t(n) * 3);
+        *rgb64 = want64 ? bb.take<double>(size_t(n) * 3) : nullptr;
+        *acc = bb.take<uint32_t>(size_t(n));
+    };
+    CamDev<R>* d_cams;
+    uint32_t *d_start, *d_next, *d_acc;
+    float* d_rgb;
+    double* d_rgb64;
+    Bump sizing{nullptr};
+    lay(sizing, &d_cams, &d_start, &d_next, &d_rgb, &d_rgb64, &d_acc);
+    if ((rc = ensure_workspace(ctx, sizing.off + 4096)) != GT_OK) return rc;
+    Bump b{static_cast<char*>(ctx->ws)};
+    lay(b, &d_cams, &d_start, &d_next, &d_rgb, &d_rgb64, &d_acc);
+    P.cams = d_cams;
+    P.frame_start = d_start;
+
+    EventPool ev;
+    if ((rc = ev.init()) != GT_OK) return rc;
+    double kms[GT_KERNEL_COUNT] = {0};
+    uint64_t klaunch[GT_KERNEL_COUNT] = {0};
+    GT_CUDA(cudaEventRecord(ev.begin, st));
+    GT_CUDA(cudaMemcpyAsync(d_cams, cd.data(), cd.size() * sizeof(CamDev<R>), cudaMemcpyHostToDevice, st));
+    GT_CUDA(cudaMemcpyAsync(d_start, start.data(), start.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    GT_CUDA(cudaMemsetAsync(P.ps.counters, 0, C_COUNT * sizeof(uint32_t), st));
+    GT_CUDA(cudaMemsetAsync(P.ps.totals, 0, 8 * sizeof(unsigned long long), st));
+    GT_CUDA(cudaMemsetAsync(d_next, 0, sizeof(uint32_t), st));
+    ctx->mapped[0] = 0;
+    ctx->mapped[1] = 0;
+    int per_sm = 0;
+    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<R, false, true>, 128, 0));
+    const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1);
+    const uint32_t blocks = std::max<uint32_t>(1u, std::min<uint32_t>(sms * uint32_t(std::max(per_sm, 1)), (n + 127) / 128));
+    cudaEvent_t a = nullptr, z = nullptr;
+    GT_CUDA(ev.pair(a, z));
+    GT_CUDA(cudaEventRecord(a, st));
+    k_persistent<R, false, true><<<blocks, 128, 0, st>>>(P, d_next, nullptr, nullptr, ctx->mapped_dev,
+                                                         ctx->mapped_dev + 1, d_rgb, d_rgb64, d_acc);
+    GT_CUDA(cudaGetLastError());
+    klaunch[GT_KERNEL_PERSISTENT] += 1;
+    GT_CUDA(cudaEventRecord(z, st));
+    bool cancelled = false;
+    if (opts.progress) { // the host polls the mapped pixel counter while the launch runs
+        for (;;) {
+            cudaError_t q = cudaEventQuery(z);
+            if (q == cudaSuccess) break;
+            if (q != cudaErrorNotReady) return cuda_fail(q, "batched render");
+            struct timespec ts{0, 2000000};
+            nanosleep(&ts, nullptr);
+            const uint32_t handed = std::min<uint32_t>(uint32_t(ctx->mapped[1]), n);
+            if (!cancelled && opts.progress(opts.progress_user, handed, n)) {
+                ctx->mapped[0] = 1;
+                cancelled = true;
+            }
+        }
+    }
+    ev.note(GT_KERNEL_PERSISTENT, a, z);
+    // Each frame's slice of the batch buffers into its own outputs.
+    for (uint32_t i = 0; i < count; ++i) {
+        gt_frame* f = frames[i];
+        const size_t o = start[i], np = size_t(start[i + 1]) - start[i];
+        const cudaMemcpyKind kind = f->device_buffers ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        GT_CUDA(cudaMemcpyAsync(f->rgb, d_rgb + o * 3, np * 3 * sizeof(float), kind, st));
+        if (f->rgb64) GT_CUDA(cudaMemcpyAsync(f->rgb64, d_rgb64 + o * 3, np * 3 * sizeof(double), kind, st));
+        if (f->accepted) GT_CUDA(cudaMemcpyAsync(f->accepted, d_acc + o, np * sizeof(uint32_t), kind, st));
+    }
+    GT_CUDA(cudaEventRecord(ev.end, st));
+    unsigned long long tot[8];
+    GT_CUDA(cudaMemcpyAsync(ctx->pinned + 2, P.ps.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    GT_CUDA(cudaMemcpyAsync(ctx->pinned + 10, P.ps.counters + C_ERROR, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GT_CUDA(cudaStreamSynchronize(st));
+    if (ctx->pinned[10]) return fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
+    if (cancelled) return fail(GT_ERR_CANCELLED, "render cancelled by the progress callback");
+    std::memcpy(tot, ctx->pinned + 2, 4 * sizeof(unsigned long long));
+    if (opts.stats) {
+        gt_render_stats& o = *opts.stats;
+        std::memset(&o, 0, sizeof(o));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev.begin, ev.end);
+        o.gpu_ms = ms;
+        o.iterations = 1;
+        o.rays = tot[0];
+        o.shadow_rays = tot[1];
+        o.samples = tot[2];
+        o.samples_started = tot[3];
+        o.persistent_rays = tot[0] + tot[1];
+        if (opts.profile) ev.harvest(kms);
+        for (int k = 0; k < GT_KERNEL_COUNT; ++k) {
+            o.kernel_ms[k] = opts.profile ? kms[k] : 0.0;
+            o.kernel_launches[k] = klaunch[k];
+        }
+    }
+    return GT_OK;
+}
+
 template <class R>
 gt_status trace_impl(gt_scene* s, const double* rays, uint32_t count, double tmin, double tmax, int32_t* ids,
                      double* t, gt_bvh_stats* stats) {

@@ -19,6 +19,11 @@ template <class R> struct Params {
     EnvDev<R> env;
     CamDev<R> cam;
     PathState<R> ps;
+    // Batched frames (k_persistent<R, false, true>): one camera per frame, frame f owns
+    // the global pixel range [frame_start[f], frame_start[f + 1]).
+    const CamDev<R>* cams;
+    const uint32_t* frame_start;
+    uint32_t num_frames;
 };
 
 GT_DEV uint32_t lane_id() { return threadIdx.x & 31u; }
@@ -224,11 +229,12 @@ template <class R> struct Shadow {
 // (camera.rs:165-195) and Russian roulette (camera.rs:2498-2523).  `prim` < 0 is a miss.
 // Returns true if the path continues to another bounce.
 template <class R>
-GT_DEV bool integrate_bounce(const Params<R>& P, Path<R>& p, int prim, R t, Rng& g, Shadow<R>& sh) {
+GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& p, int prim, R t, Rng& g,
+                             Shadow<R>& sh) {
     sh.valid[0] = sh.valid[1] = false;
     bool cont = false;
     if (prim < 0) {
-        V3<R> bg = P.cam.use_env ? env_radiance(P.env, p.d) : background(P.cam, p.d);
+        V3<R> bg = cam.use_env ? env_radiance(P.env, p.d) : background(cam, p.d);
         V3<R> miss = bg * p.miss_w;
         p.col = p.col + cmul(p.att, miss);
         return false;
@@ -243,13 +249,13 @@ GT_DEV bool integrate_bounce(const Params<R>& P, Path<R>& p, int prim, R t, Rng&
         p.d = s.dir;
         p.allow_emit = true;
         p.miss_w = R(1);
-        cont = rr_survives(P.cam, p.bounce, p.att, g);
+        cont = rr_survives(cam, p.bounce, p.att, g);
     } else if (s.kind == SC_PDF) {
-        if (P.cam.nee) {
+        if (cam.nee) {
             sh.o = h.p;
             sh.time = p.time;
             sh.att = p.att;
-            if (P.cam.use_lights) { // estimate_direct_lighting, camera.rs:2225-2262
+            if (cam.use_lights) { // estimate_direct_lighting, camera.rs:2225-2262
                 V3<R> ldir = lights_dir(P.lights, h.p, p.time, g);
                 R lp = lights_pdf(P.lights, h.p, p.time, ldir);
                 if (Num<R>::finite(lp) && lp > R(kEps)) {
@@ -262,7 +268,7 @@ GT_DEV bool integrate_bounce(const Params<R>& P, Path<R>& p, int prim, R t, Rng&
                     }
                 }
             }
-            if (P.cam.use_env) { // estimate_environment_lighting, camera.rs:2264-2297
+            if (cam.use_env) { // estimate_environment_lighting, camera.rs:2264-2297
                 V3<R> edir;
                 R ep;
                 env_sample(P.env, g, edir, ep);
@@ -281,16 +287,16 @@ GT_DEV bool integrate_bounce(const Params<R>& P, Path<R>& p, int prim, R t, Rng&
         V3<R> dir;
         R pdf;
         bool suppress = false, weight_env = false;
-        if (!P.cam.nee && P.cam.use_lights) {
-            const R w = P.cam.light_pdf_weight;
+        if (!cam.nee && cam.use_lights) {
+            const R w = cam.light_pdf_weight;
             if (rnd<R>(g) < w) dir = lights_dir(P.lights, h.p, p.time, g);
             else dir = matpdf_generate(s.pdf, g);
             pdf = w * lights_pdf(P.lights, h.p, p.time, dir) + (R(1) - w) * matpdf_value(s.pdf, dir);
         } else {
             dir = matpdf_generate(s.pdf, g);
             pdf = matpdf_value(s.pdf, dir);
-            suppress = P.cam.nee && P.cam.use_lights;
-            weight_env = P.cam.nee && P.cam.use_env;
+            suppress = cam.nee && cam.use_lights;
+            weight_env = cam.nee && cam.use_env;
         }
         if (Num<R>::finite(pdf) && pdf > R(kEps)) {
             R sp = mat_scattering_pdf(m, p.d, h, dir);
@@ -302,11 +308,11 @@ GT_DEV bool integrate_bounce(const Params<R>& P, Path<R>& p, int prim, R t, Rng&
                 p.d = dir;
                 p.allow_emit = !suppress;
                 p.miss_w = next_w;
-                cont = rr_survives(P.cam, p.bounce, p.att, g);
+                cont = rr_survives(cam, p.bounce, p.att, g);
             }
         }
     }
-    if (cont && p.bounce + 1 >= P.cam.max_depth) cont = false; // the bounce loop is exhausted
+    if (cont && p.bounce + 1 >= cam.max_depth) cont = false; // the bounce loop is exhausted
     if (cont) p.bounce += 1;
     return cont;
 }
@@ -344,7 +350,7 @@ template <class R> GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uin
     p.allow_emit = (flags & F_ALLOW_EMIT) != 0;
     Shadow<R> sh;
     const int prim = key == KEY_MISS ? -1 : P.ps.hit_prim[slot];
-    const bool cont = integrate_bounce(P, p, prim, key == KEY_MISS ? R(0) : P.ps.hit_t[slot], g, sh);
+    const bool cont = integrate_bounce(P, P.cam, p, prim, key == KEY_MISS ? R(0) : P.ps.hit_t[slot], g, sh);
     uint32_t sh_bits = 0;
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
@@ -543,13 +549,34 @@ template <class R> __global__ void __launch_bounds__(256) k_classify(Params<R> P
 // are still running (class_counts[0] entries), each thread picks up a slot's saved state
 // (its path mid-flight, or a finished sample waiting to be folded in) and, when the
 // slot's pixel is done, stores the pixel sums back for k_resolve.
-template <class R, bool RESUME>
+template <class R, bool RESUME, bool BATCH = false>
 __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next, const uint32_t* queues,
                                                     const uint32_t* class_counts, const volatile uint32_t* cancel,
                                                     volatile uint32_t* progress, float* rgb, double* rgb64,
                                                     uint32_t* accepted) {
-    const uint32_t n = RESUME ? class_counts[0] : P.cam.width * P.cam.height;
-    const uint32_t limit = P.cam.adaptive ? P.cam.adaptive_max : P.cam.spp;
+    const uint32_t n = RESUME ? class_counts[0] : (BATCH ? P.frame_start[P.num_frames] : P.cam.width * P.cam.height);
+    // The camera of the pixel being rendered: the frame's in a batch, else the launch's.
+    uint32_t frame = 0, local = 0;
+    auto cam = [&]() -> const CamDev<R>& {
+        if constexpr (BATCH) return P.cams[frame];
+        else return P.cam;
+    };
+    // Global pixel -> (frame, pixel within the frame) by binary search over frame_start.
+    auto locate = [&](uint32_t pix) {
+        if constexpr (BATCH) {
+            uint32_t lo = 0, hi = P.num_frames;
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (P.frame_start[mid] <= pix) lo = mid;
+                else hi = mid;
+            }
+            frame = lo;
+            local = pix - P.frame_start[lo];
+        } else {
+            local = pix;
+        }
+    };
+    auto sample_limit = [&]() -> uint32_t { return cam().adaptive ? cam().adaptive_max : cam().spp; };
     const R inf = Num<R>::inf();
     uint32_t prefix[NUM_COST_CLASSES + 1];
     prefix[0] = 0;
@@ -560,7 +587,7 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
         const uint32_t i = atomicAdd(next, 1u);
         if (i >= n) return n;
         if (progress && (i & 1023u) == 0) *progress = i;
-        if (RESUME) return i;
+        if (RESUME || BATCH) return i;
         uint32_t k = 0;
 #pragma unroll
         for (uint32_t c = 1; c < NUM_COST_CLASSES; ++c)
@@ -602,8 +629,9 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
         cont = !need_sample;
     };
     if (item < n) {
+        locate(pix);
         if (RESUME) resume(pix);
-        else g.s = pixel_seed(P.cam.seed, pix % P.cam.width, pix / P.cam.width);
+        else g.s = pixel_seed(cam().seed, local % cam().width, local / cam().width);
     }
     bool alive = item < n;
     // The loop is warp-uniform and reconverges at each phase boundary (__syncwarp), so
@@ -612,15 +640,16 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
     while (__any_sync(0xffffffffu, alive)) {
         if (alive && need_sample) {
             bool stop = false;
-            if (started > 0) stop = fold_sample(P.cam, a, c, acc_n, p.col);
+            if (started > 0) stop = fold_sample(cam(), a, c, acc_n, p.col);
             bool got = false;
             for (;;) {
-                const uint32_t x = pix % P.cam.width, y = pix / P.cam.width;
+                const uint32_t x = local % cam().width, y = local / cam().width;
+                const uint32_t limit = sample_limit();
                 while (!stop && started < limit) {
-                    camera_ray(P.cam, x, y, started, g, p.o, p.d, p.time);
+                    camera_ray(cam(), x, y, started, g, p.o, p.d, p.time);
                     ++started;
-                    if (P.cam.max_depth == 0) { // the bounce loop never runs: a black sample
-                        stop = fold_sample(P.cam, a, c, acc_n, V3<R>{0, 0, 0});
+                    if (cam().max_depth == 0) { // the bounce loop never runs: a black sample
+                        stop = fold_sample(cam(), a, c, acc_n, V3<R>{0, 0, 0});
                         continue;
                     }
                     p.att = V3<R>{1, 1, 1};
@@ -640,7 +669,7 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
                     P.ps.accepted[pix] = acc_n;
                     P.ps.st[pix] = make_uint4(uint32_t(g.s), uint32_t(g.s >> 32), F_DONE, started);
                 } else {
-                    const V3<R> v = pixel_estimate(P.cam, a, acc_n);
+                    const V3<R> v = pixel_estimate(cam(), a, acc_n);
                     if (rgb) {
                         rgb[size_t(pix) * 3 + 0] = float(v.x);
                         rgb[size_t(pix) * 3 + 1] = float(v.y);
@@ -662,16 +691,18 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
                 }
                 if (RESUME) {
                     pix = queues[item];
+                    locate(pix);
                     resume(pix);
                     if (!need_sample) break; // a path in flight: trace it
                     stop = false;
                     got = false;
                     // a finished sample: fold it in before starting the next one
-                    if (started > 0) stop = fold_sample(P.cam, a, c, acc_n, p.col);
+                    if (started > 0) stop = fold_sample(cam(), a, c, acc_n, p.col);
                     continue;
                 }
                 pix = item;
-                g.s = pixel_seed(P.cam.seed, pix % P.cam.width, pix / P.cam.width);
+                locate(pix);
+                g.s = pixel_seed(cam().seed, local % cam().width, local / cam().width);
                 a = R4<R>{0, 0, 0, 0};
                 c = R4<R>{0, 0, 0, 0};
                 acc_n = 0;
@@ -701,7 +732,7 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
                 ++n_shadow;
             } else {
                 ++n_rays;
-                cont = integrate_bounce(P, p, prim, t, g, sh);
+                cont = integrate_bounce(P, cam(), p, prim, t, g, sh);
                 pending = (sh.valid[0] ? 1u : 0u) | (sh.valid[1] ? 2u : 0u);
             }
             if (pending == 0 && !cont) need_sample = true;

@@ -766,6 +766,44 @@ class PathTracer:
         return PathTracer(self.camera, options, self.precision, self._ctx, self.profile, self.schedule,
                           self.tail_slots)
 
+    def render_batch_hdr_images(self, world: RayScene, cameras, lights: Optional[WeightedSamplingTargetList] = None,
+                                environment: Optional[EnvironmentLight] = None, want64: bool = False) -> list:
+        """One image per camera, all rendered in one launch (gt_render_batch): the per-frame
+        loop around render_with_*_hdr_image for an animation or a camera sweep.  This
+        tracer's camera is not used; each frame is rendered with its own."""
+        ctx = self.context
+        cams = list(cameras)
+        descs = [c.desc() for c in cams]
+        frames, images = [], []
+        for c in cams:
+            w, h, _ = c.image_size()
+            img = HdrImage(w, h, np.empty((h, w, 3), dtype=np.float32), np.empty((h, w), dtype=np.uint32),
+                           np.empty((h, w, 3), dtype=np.float64) if want64 else None)
+            f = abi.gt_frame()
+            f.struct_size = C.sizeof(abi.gt_frame)
+            f.width, f.height, f.device_buffers = w, h, 0
+            f.rgb = img.pixels.ctypes.data
+            f.accepted = img.accepted.ctypes.data
+            f.rgb64 = img.pixels64.ctypes.data if want64 else None
+            frames.append(f)
+            images.append(img)
+        jobs = (abi.gt_frame_job * len(cams))()
+        for i in range(len(cams)):
+            jobs[i].camera = C.pointer(descs[i])
+            jobs[i].frame = C.pointer(frames[i])
+        o = abi.gt_render_opts()
+        o.struct_size = C.sizeof(abi.gt_render_opts)
+        o.precision = abi.GT_PRECISION_F64 if self.precision == "f64" else abi.GT_PRECISION_F32
+        o.profile = 1 if self.profile else 0
+        stats = abi.gt_render_stats()
+        o.stats = C.pointer(stats)
+        sh = world._handle(ctx)
+        lh = lights._handle(ctx).h if lights is not None else None
+        eh = environment._handle(ctx).h if environment is not None else None
+        check(lib().gt_render_batch(sh.h, lh, eh, jobs, len(cams), C.byref(o)))
+        self.last_stats = stats.as_dict()
+        return images
+
     def _render(self, world: RayScene, lights: Optional[WeightedSamplingTargetList],
                 environment: Optional[EnvironmentLight], aovs: bool = False, want64: bool = False):
         ctx = self.context

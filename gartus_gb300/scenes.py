@@ -405,3 +405,38 @@ def mesh_heavy_camera(width: int = 1920, height: int = 1080, grid: int = 8, max_
             .with_vertical_fov(40.0)
             .with_look_at((0.0, 38.0, 75.0), (0.0, 8.0, 0.0))
             .with_view_up((0.0, 1.0, 0.0)))
+
+
+# ---------------------------------------------------- batched frames (cfg 3)
+def batch_scene() -> tuple[RayScene, SamplingTargetList]:
+    """The Cornell box with two MovingSpheres of radius 60 moving linearly over the
+    shutter interval [0, 1)."""
+    scene, lights = cornell_scene()
+    orange = scene.add_material(RayMaterial.lambertian((0.8, 0.45, 0.1)))
+    steel = scene.add_material(RayMaterial.metal((0.8, 0.85, 0.9), 0.05))
+    scene.add_moving_sphere((400.0, 90.0, 160.0), (400.0, 170.0, 160.0), 60.0, orange)
+    scene.add_moving_sphere((150.0, 330.0, 330.0), (230.0, 330.0, 300.0), 60.0, steel)
+    scene.build_bvh()
+    return scene, lights
+
+
+def batch_cameras(frames: int = 64, width: int = 512, spp_cycle=(4, 8, 16, 32, 64), max_samples: int = 256,
+                  threshold: float = 0.02, max_depth: int = 50) -> list:
+    """`frames` square cameras orbiting the box centre (278, 278, 278) over -60..60 degrees,
+    shutter [0, 1), adaptive random sampling whose minimum cycles through `spp_cycle` and
+    whose cap is `max_samples`; each frame has its own RNG seed."""
+    cams = []
+    for i in range(frames):
+        a = math.radians(-60.0 + 120.0 * i / max(frames - 1, 1))
+        look_from = (278.0 + 1078.0 * math.sin(a), 278.0, 278.0 - 1078.0 * math.cos(a))
+        spp = spp_cycle[i % len(spp_cycle)]
+        cams.append(RayCamera(width, 1.0)
+                    .with_adaptive_sampling(spp, max_samples, threshold)
+                    .with_max_depth(max_depth)
+                    .with_background((0.0, 0.0, 0.0))
+                    .with_vertical_fov(40.0)
+                    .with_look_at(look_from, (278.0, 278.0, 278.0))
+                    .with_view_up((0.0, 1.0, 0.0))
+                    .with_shutter_interval(0.0, 1.0)
+                    .with_rng_seed(1 + i))
+    return cams

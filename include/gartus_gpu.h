@@ -342,6 +342,22 @@ void gt_environment_destroy(gt_environment* environment);
 gt_status gt_render(gt_scene* scene, const gt_lights* lights, const gt_environment* environment,
                     const gt_camera_desc* camera, const gt_render_opts* opts, gt_frame* frame);
 
+/* One frame of a batched render: its camera and its caller-owned outputs. */
+typedef struct gt_frame_job {
+    const gt_camera_desc* camera;
+    gt_frame* frame;
+} gt_frame_job;
+
+/* Renders `count` frames of one scene — each with its own camera, pose, shutter, sample
+ * count and adaptive settings — in one persistent launch: the per-frame loop a caller
+ * would write around PathTracer::render_with_*_hdr_image (renderer.rs:101-117, 391-449)
+ * for an animation or a camera sweep.  Every frame's image, accepted counts and f64
+ * image equal what gt_render gives for that frame alone.  opts: precision, stats (summed
+ * over the batch), profile, progress (pixels handed out of the batch's total) and
+ * cancellation; `schedule` and `tail_slots` are ignored; `aovs` is GT_ERR_UNSUPPORTED. */
+gt_status gt_render_batch(gt_scene* scene, const gt_lights* lights, const gt_environment* environment,
+                          const gt_frame_job* jobs, uint32_t count, const gt_render_opts* opts);
+
 /* Closest-hit queries with traversal statistics on the reference-layout BVH in f64:
  * RayScene::hit (raytracing/scene.rs:1639-1657) and
  * RayScene::bvh_traversal_stats_for_rays (scene.rs:1478-1492).

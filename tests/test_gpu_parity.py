@@ -318,6 +318,57 @@ def test_noise_textures(gpu_context, precision):
     assert np.std(ref) > 1e-3
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_batch_matches_single_frames(gpu_context, precision):
+    # gt_render_batch: frames with different poses, seeds, adaptive minimums and sizes in
+    # one launch give each frame's gt_render image (bit-identical in f64).
+    scene, lights = scenes.batch_scene()
+    cams = scenes.batch_cameras(frames=5, width=20, spp_cycle=(2, 4, 8), max_samples=16, threshold=0.05)
+    cams.append(scenes.cornell_camera(12, 2, 20))  # a stratified frame of another size
+    pt = PathTracer(cams[0], precision=precision, context=gpu_context)
+    imgs = pt.render_batch_hdr_images(scene, cams, lights=lights, want64=precision == "f64")
+    assert pt.last_stats["samples"] == sum(int(i.accepted.sum()) for i in imgs)
+    for cam, img in zip(cams, imgs):
+        one = PathTracer(cam, precision=precision, context=gpu_context).render_with_lights_hdr_image(
+            scene, lights, want64=precision == "f64")
+        np.testing.assert_array_equal(img.accepted, one.accepted)
+        if precision == "f64":
+            np.testing.assert_array_equal(img.pixels64, one.pixels64)
+        else:
+            assert _divergent(img.pixels, one.pixels.astype(np.float64)) <= 0.05 * img.pixels.shape[0] * img.pixels.shape[1]
+    if precision == "f64":  # and the oracle agrees on one frame
+        ref, acc = _oracle_render(scene, cams[1], lights)
+        np.testing.assert_array_equal(imgs[1].accepted, acc)
+        assert rel_err(imgs[1].pixels64, ref, floor=1e-12).max() <= 1e-9
+
+
+def test_batch_rejects_bad_jobs(gpu_context):
+    scene, lights = scenes.batch_scene()
+    cam = scenes.batch_cameras(frames=1, width=8)[0]
+    with pytest.raises(GartusError) as e:
+        PathTracer(cam, context=gpu_context).render_batch_hdr_images(scene, [], lights=lights)
+    assert e.value.status == abi.GT_ERR_INVALID_ARG
+    f = abi.gt_frame()
+    f.struct_size = C.sizeof(abi.gt_frame)
+    buf = np.zeros((4, 4, 3), dtype=np.float32)
+    f.width, f.height, f.rgb = 4, 4, buf.ctypes.data  # 8x8 camera, 4x4 frame
+    jobs = (abi.gt_frame_job * 1)()
+    d = cam.desc()
+    jobs[0].camera = C.pointer(d)
+    jobs[0].frame = C.pointer(f)
+    o = abi.gt_render_opts()
+    o.struct_size = C.sizeof(abi.gt_render_opts)
+    assert lib().gt_render_batch(scene._handle(gpu_context).h, None, None, jobs, 1, C.byref(o)) == abi.GT_ERR_INVALID_ARG
+    f.width, f.height = 8, 8
+    buf8 = np.zeros((8, 8, 3), dtype=np.float32)
+    f.rgb = buf8.ctypes.data
+    o.aovs = 1
+    assert lib().gt_render_batch(scene._handle(gpu_context).h, None, None, jobs, 1, C.byref(o)) == abi.GT_ERR_UNSUPPORTED
+    o.aovs = 0
+    assert lib().gt_render_batch(scene._handle(gpu_context).h, None, None, jobs, 1, C.byref(o)) == abi.GT_OK
+    assert np.isfinite(buf8).all() and buf8.max() > 0
+
+
 def test_edge_cases(gpu_context):
     scene = scenes.final_scene_ray_scene()
     # max_depth 0: the bounce loop never runs, every sample is black (camera.rs:1742).
