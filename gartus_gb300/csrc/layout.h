@@ -9,6 +9,8 @@
 
 #include <stdint.h>
 
+#include "../../include/gartus_gpu.h"
+
 #if defined(__CUDACC__)
 #define GT_HD __host__ __device__
 #else
@@ -158,8 +160,10 @@ template <class R> struct PathState {
     uint32_t* q_mat; // 8 queues of capacity n (key = material kind, 7 = miss)
     uint32_t* q_shadow;
     uint32_t* q_migrate; // slots handed to the concurrent persistent kernel
+    uint32_t* q_handoff; // slots the side launch hands to its cooperative launch
     uint32_t* counters; // [0,1] trace, [2..10) mat keys, [10] shadow, [11] done, [12] error,
-                        // [13] migrated slots, [14] their pull counter, [15] tail slots
+                        // [13] migrated slots, [14] their pull counter, [15] tail slots,
+                        // [16..22) hand-over counters
     unsigned long long* totals; // [0] rays, [1] shadow rays, [2] accepted samples, [3] started samples,
                                 // [4] samples started by unfinished slots, [5] unfinished slots,
                                 // [6] queries traced by k_persistent
@@ -176,7 +180,14 @@ enum : uint32_t {
     C_MIGRATED = 13,
     C_MIGRATE_NEXT = 14,
     C_TAIL = 15, // slots finished by the tail launch
-    C_COUNT = 16
+    // hand-over of the tail and side launches to cooperative launches (one warp per slot)
+    C_TAIL_DONE = 16,
+    C_TAIL_COOP = 17,
+    C_TAIL_COOP_NEXT = 18,
+    C_SIDE_DONE = 19,
+    C_SIDE_COOP = 20,
+    C_SIDE_COOP_NEXT = 21,
+    C_COUNT = 24
 };
 
 enum : uint32_t { KEY_MISS = 7, NUM_KEYS = 8 };

@@ -85,8 +85,8 @@ extern "C" gt_status gt_render_noalloc(gt_scene* scene, const gt_lights* lights,
         P.cam = cam_dev<float>(cam, lights != nullptr, environment != nullptr);
         P.ps.n = n;
         P.ps.counters = reinterpret_cast<uint32_t*>(base);
-        P.ps.totals = reinterpret_cast<unsigned long long*>(base + 64);
-        uint32_t* next = reinterpret_cast<uint32_t*>(base + 128);
+        P.ps.totals = reinterpret_cast<unsigned long long*>(base + 128);
+        uint32_t* next = reinterpret_cast<uint32_t*>(base + 192);
         uint32_t* queues = reinterpret_cast<uint32_t*>(base + kHeaderBytes);
         cudaStream_t st = ctx->stream;
         // Every call shares g_scratch and it keeps the last call's contents: the header

@@ -427,6 +427,7 @@ template <class R> size_t layout_state(Bump& b, PathState<R>& ps, uint32_t n, bo
     ps.q_mat = b.take<uint32_t>(size_t(n) * NUM_KEYS);
     ps.q_shadow = b.take<uint32_t>(nee ? n : 1);
     ps.q_migrate = b.take<uint32_t>(n);
+    ps.q_handoff = b.take<uint32_t>(n);
     ps.counters = b.take<uint32_t>(C_COUNT);
     ps.totals = b.take<unsigned long long>(8);
     return b.off;
@@ -755,8 +756,13 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     // The last pixels of a frame are the longest sample chains; once no more than one
     // persistent launch's worth of slots is left, per-bounce launches would run nearly
     // empty, so the remaining slots finish in k_persistent's RESUME mode.
-    int tail_per_sm = 0;
+    int tail_per_sm = 0, coop_per_sm = 0;
     GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tail_per_sm, k_persistent<R, true>, 128, 0));
+    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&coop_per_sm, k_persistent<R, true, false, true>, 128, 0));
+    // Cooperative launches (one warp per slot): the tail's fills the GPU, the side
+    // stream's takes two blocks per SM next to the running wavefront.
+    const uint32_t coop_blocks = uint32_t(sms) * uint32_t(std::max(coop_per_sm, 1));
+    const uint32_t side_coop_blocks = uint32_t(sms) * uint32_t(std::min(std::max(coop_per_sm, 1), 2));
     uint32_t tail_slots = 0;
     if (opts.schedule == GT_SCHEDULE_AUTO)
         tail_slots = opts.tail_slots ? opts.tail_slots : uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1)) * 128u;
@@ -773,6 +779,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     auto migrate = [&]() -> gt_status {
         GT_CUDA(cudaMemsetAsync(P.ps.totals + 4, 0, 2 * sizeof(unsigned long long), st));
         GT_CUDA(cudaMemsetAsync(P.ps.counters + C_MIGRATED, 0, 2 * sizeof(uint32_t), st));
+        GT_CUDA(cudaMemsetAsync(P.ps.counters + C_SIDE_DONE, 0, 3 * sizeof(uint32_t), st));
         GT_CUDA(cudaMemsetAsync(P.ps.counters + C_TRACE1, 0, sizeof(uint32_t), st));
         k_progress_sum<R><<<slot_blocks, threads, 0, st>>>(P);
         k_migrate<R><<<slot_blocks, threads, 0, st>>>(P, kMigrateRatio);
@@ -784,11 +791,19 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         GT_CUDA(cudaEventRecord(fork, st));
         GT_CUDA(cudaStreamWaitEvent(ctx->side, fork, 0));
         const uint32_t side_blocks = uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1));
+        HandOff ho;
+        ho.done = P.ps.counters + C_SIDE_DONE;
+        ho.below = side_coop_blocks * 4u;
+        ho.list = P.ps.q_handoff;
+        ho.count = P.ps.counters + C_SIDE_COOP;
         k_persistent<R, true><<<side_blocks, 128, 0, ctx->side>>>(P, P.ps.counters + C_MIGRATE_NEXT, P.ps.q_migrate,
                                                                   P.ps.counters + C_MIGRATED, ctx->mapped_dev,
-                                                                  nullptr, nullptr, nullptr, nullptr);
+                                                                  nullptr, nullptr, nullptr, nullptr, ho);
+        k_persistent<R, true, false, true><<<side_coop_blocks, 128, 0, ctx->side>>>(
+            P, P.ps.counters + C_SIDE_COOP_NEXT, P.ps.q_handoff, P.ps.counters + C_SIDE_COOP, ctx->mapped_dev, nullptr,
+            nullptr, nullptr, nullptr);
         GT_CUDA(cudaGetLastError());
-        klaunch[GT_KERNEL_PERSISTENT] += 1;
+        klaunch[GT_KERNEL_PERSISTENT] += 2;
         GT_CUDA(cudaEventRecord(join, ctx->side));
         return GT_OK;
     };
@@ -852,14 +867,25 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         uint32_t* list = P.ps.q_trace[0];
         uint32_t* count = P.ps.counters + C_TAIL;
         GT_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t), st));
+        GT_CUDA(cudaMemsetAsync(P.ps.counters + C_TAIL_DONE, 0, 3 * sizeof(uint32_t), st));
         GT_CUDA(cudaMemsetAsync(d_next, 0, sizeof(uint32_t), st));
         k_collect<R><<<slot_blocks, threads, 0, st>>>(P, list, count);
         const uint32_t tblocks = uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1));
+        // The tail runs one slot per lane until no more slots are left than the
+        // cooperative launch has warps, then one slot per warp.
+        HandOff ho;
+        ho.done = P.ps.counters + C_TAIL_DONE;
+        ho.below = coop_blocks * 4u;
+        ho.list = P.ps.q_trace[1];
+        ho.count = P.ps.counters + C_TAIL_COOP;
         k_persistent<R, true><<<tblocks, 128, 0, st>>>(P, d_next, list, count, nullptr, nullptr, nullptr, nullptr,
-                                                       nullptr);
+                                                       nullptr, ho);
+        k_persistent<R, true, false, true><<<coop_blocks, 128, 0, st>>>(
+            P, P.ps.counters + C_TAIL_COOP_NEXT, P.ps.q_trace[1], P.ps.counters + C_TAIL_COOP, nullptr, nullptr, nullptr,
+            nullptr, nullptr);
         GT_CUDA(cudaGetLastError());
         klaunch[GT_KERNEL_OTHER] += 1;
-        klaunch[GT_KERNEL_PERSISTENT] += 1;
+        klaunch[GT_KERNEL_PERSISTENT] += 2;
         if (profile) {
             GT_CUDA(cudaEventRecord(z, st));
             ev.note(GT_KERNEL_PERSISTENT, a, z);

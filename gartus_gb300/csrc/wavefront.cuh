@@ -549,11 +549,20 @@ template <class R> __global__ void __launch_bounds__(256) k_classify(Params<R> P
 // are still running (class_counts[0] entries), each thread picks up a slot's saved state
 // (its path mid-flight, or a finished sample waiting to be folded in) and, when the
 // slot's pixel is done, stores the pixel sums back for k_resolve.
-template <class R, bool RESUME, bool BATCH = false>
+// Hand-over of a resume-mode k_persistent launch to a cooperative one (COOP: one warp per
+// slot) once few slots are left; all zero = never.
+struct HandOff {
+    uint32_t* done = nullptr;  // slots this launch has finished
+    uint32_t below = 0;        // hand over once (slots - done) <= below
+    uint32_t* list = nullptr;  // slots handed over
+    uint32_t* count = nullptr; // their number
+};
+
+template <class R, bool RESUME, bool BATCH = false, bool COOP = false>
 __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next, const uint32_t* queues,
                                                     const uint32_t* class_counts, const volatile uint32_t* cancel,
                                                     volatile uint32_t* progress, float* rgb, double* rgb64,
-                                                    uint32_t* accepted) {
+                                                    uint32_t* accepted, HandOff ho = HandOff()) {
     const uint32_t n = RESUME ? class_counts[0] : (BATCH ? P.frame_start[P.num_frames] : P.cam.width * P.cam.height);
     // The camera of the pixel being rendered: the frame's in a batch, else the launch's.
     uint32_t frame = 0, local = 0;
@@ -584,7 +593,14 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
     for (uint32_t k = 0; k < NUM_COST_CLASSES; ++k) prefix[k + 1] = prefix[k] + (RESUME ? 0u : class_counts[k]);
     auto fetch = [&]() -> uint32_t {
         if (cancel && *cancel) return n;
-        const uint32_t i = atomicAdd(next, 1u);
+        uint32_t i;
+        if constexpr (COOP) { // one slot per warp: every lane follows the same path
+            uint32_t v = 0;
+            if (lane_id() == 0) v = atomicAdd(next, 1u);
+            i = __shfl_sync(0xffffffffu, v, 0);
+        } else {
+            i = atomicAdd(next, 1u);
+        }
         if (i >= n) return n;
         if (progress && (i & 1023u) == 0) *progress = i;
         if (RESUME || BATCH) return i;
@@ -628,6 +644,22 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
         pending = 0;
         cont = !need_sample;
     };
+    // Saves the slot's state in the wavefront layout resume() reads (RESUME hand-over); a
+    // migrated slot stays marked so that the tail's k_collect leaves it to the side stream.
+    auto save = [&](uint32_t slot) {
+        uint32_t flags = P.ps.st[slot].z & F_MIGRATED;
+        if (!need_sample) {
+            flags = F_TRACE | (p.bounce & F_BOUNCE_MASK) | (p.allow_emit ? F_ALLOW_EMIT : 0u);
+            P.ps.ray_o[slot] = R4<R>{p.o.x, p.o.y, p.o.z, p.time};
+            P.ps.ray_d[slot] = R4<R>{p.d.x, p.d.y, p.d.z, p.miss_w};
+            P.ps.att[slot] = R4<R>{p.att.x, p.att.y, p.att.z, R(0)};
+        }
+        P.ps.col[slot] = R4<R>{p.col.x, p.col.y, p.col.z, R(0)};
+        P.ps.acc[slot] = a;
+        P.ps.comp[slot] = c;
+        P.ps.accepted[slot] = acc_n;
+        P.ps.st[slot] = make_uint4(uint32_t(g.s), uint32_t(g.s >> 32), flags, started);
+    };
     if (item < n) {
         locate(pix);
         if (RESUME) resume(pix);
@@ -637,7 +669,22 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
     // The loop is warp-uniform and reconverges at each phase boundary (__syncwarp), so
     // the warp executes setup, one traversal and one integration step together instead
     // of drifting apart into sub-warps at different instructions.
+    uint32_t iter = 0;
     while (__any_sync(0xffffffffu, alive)) {
+        if constexpr (RESUME && !COOP) {
+            // Hand-over: once no more slots are left than the cooperative launch has warps,
+            // lanes between samples or bounces save their slot, list it (with every slot not
+            // yet taken) and stop; a slot then runs on a warp of its own, where it is not
+            // slowed by other lanes' branches.
+            if (ho.below && (iter & 15u) == 0u && alive && pending == 0 &&
+                n - *reinterpret_cast<volatile uint32_t*>(ho.done) <= ho.below) {
+                save(pix);
+                ho.list[atomicAdd(ho.count, 1u)] = pix;
+                for (uint32_t it = fetch(); it < n; it = fetch()) ho.list[atomicAdd(ho.count, 1u)] = queues[it];
+                alive = false;
+            }
+        }
+        ++iter;
         if (alive && need_sample) {
             bool stop = false;
             if (started > 0) stop = fold_sample(cam(), a, c, acc_n, p.col);
@@ -664,10 +711,13 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
                 // The pixel is finished: write it (or hand its sums back to the
                 // wavefront's resolve) and take the next one.
                 if (RESUME) {
-                    P.ps.acc[pix] = a;
-                    P.ps.comp[pix] = c;
-                    P.ps.accepted[pix] = acc_n;
-                    P.ps.st[pix] = make_uint4(uint32_t(g.s), uint32_t(g.s >> 32), F_DONE, started);
+                    if (!COOP || lane_id() == 0) {
+                        P.ps.acc[pix] = a;
+                        P.ps.comp[pix] = c;
+                        P.ps.accepted[pix] = acc_n;
+                        P.ps.st[pix] = make_uint4(uint32_t(g.s), uint32_t(g.s >> 32), F_DONE, started);
+                        if (ho.done) atomicAdd(ho.done, 1u);
+                    }
                 } else {
                     const V3<R> v = pixel_estimate(cam(), a, acc_n);
                     if (rgb) {
@@ -740,9 +790,9 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
         __syncwarp();
     }
     // Throughput totals: warp-reduce, one atomic per warp (every lane of the launch's
-    // full warps arrives here).
+    // full warps arrives here); a cooperative warp counted its one path in every lane.
     __syncwarp();
-    for (int off = 16; off > 0; off >>= 1) {
+    for (int off = 16; off > 0 && !COOP; off >>= 1) {
         n_rays += __shfl_down_sync(0xffffffffu, n_rays, off);
         n_shadow += __shfl_down_sync(0xffffffffu, n_shadow, off);
         n_acc += __shfl_down_sync(0xffffffffu, n_acc, off);

@@ -466,17 +466,19 @@ def test_persistent_progress_and_cancel(gpu_context):
     assert np.isfinite(img.pixels).all()
 
 
-@pytest.mark.parametrize("schedule,tail,grid", [("wavefront", 0, 4), ("auto", 100, 4), ("auto", 1000000, 4),
-                                               ("auto", 1, 8)])
-def test_schedules_agree(gpu_context, schedule, tail, grid):
+@pytest.mark.parametrize("schedule,tail,grid,width", [("wavefront", 0, 4, 48), ("auto", 100, 4, 48),
+                                                     ("auto", 1000000, 4, 48), ("auto", 1, 8, 48),
+                                                     ("auto", 1000000, 4, 96)])
+def test_schedules_agree(gpu_context, schedule, tail, grid, width):
     # Every schedule evaluates the same per-pixel arithmetic in the same order: bit-identical
     # in f64 (no fused multiply-add anywhere), whether the wavefront runs to the end, hands
     # its last 100 slots to the persistent kernel, hands over at once, or (64 samples per
     # pixel, tail of one slot) first moves its slowest pixels to the concurrent persistent
-    # kernel; in f32 the compiler may fuse differently in the kernels, so images agree to
-    # f32 rounding.
+    # kernel.  At 96x96 the tail starts one slot per lane and hands its last slots to one
+    # warp each mid-path.  In f32 the compiler may fuse differently in the kernels, so
+    # images agree to f32 rounding.
     scene, lights = scenes.cornell_scene()
-    cam = scenes.cornell_camera(48, grid, 50)
+    cam = scenes.cornell_camera(width, grid, 50)
     a = PathTracer(cam, precision="f64", context=gpu_context, schedule=schedule, tail_slots=tail)
     b = PathTracer(cam, precision="f64", context=gpu_context, schedule="persistent")
     ia = a.render_with_lights_hdr_image(scene, lights, want64=True)
