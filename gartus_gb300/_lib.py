@@ -52,6 +52,13 @@ def _declare(L: C.CDLL) -> None:
                                    C.c_void_p]),
         "gt_render_batch": (st, [C.c_void_p, C.c_void_p, C.c_void_p, P(abi.gt_frame_job), C.c_uint32,
                                  P(abi.gt_render_opts)]),
+        "gt_accumulator_create": (st, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_void_p)]),
+        "gt_accumulator_destroy": (None, [C.c_void_p]),
+        "gt_accumulator_samples": (st, [C.c_void_p, P(C.c_uint32)]),
+        "gt_accumulator_save": (st, [C.c_void_p, C.c_void_p, C.c_uint64, P(C.c_uint64)]),
+        "gt_accumulator_load": (st, [C.c_void_p, C.c_void_p, C.c_uint64]),
+        "gt_render_accumulate": (st, [C.c_void_p, C.c_void_p, C.c_void_p, P(abi.gt_camera_desc), C.c_uint32,
+                                      C.c_void_p, P(abi.gt_render_opts), P(abi.gt_frame)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -87,5 +94,6 @@ EXPORTED_SYMBOLS = [
     "gt_context_destroy", "gt_scene_create", "gt_scene_destroy", "gt_scene_bvh_node_count",
     "gt_scene_emissive_targets", "gt_lights_create", "gt_lights_destroy", "gt_environment_create",
     "gt_environment_destroy", "gt_render", "gt_trace_rays", "gt_trace_primary", "gt_render_noalloc",
-    "gt_render_batch",
+    "gt_render_batch", "gt_accumulator_create", "gt_accumulator_destroy", "gt_accumulator_samples",
+    "gt_accumulator_save", "gt_accumulator_load", "gt_render_accumulate",
 ]

@@ -457,6 +457,169 @@ void gt_environment_destroy(gt_environment* e) {
     delete e;
 }
 
+// ------------------------------------------------------------ accumulators
+namespace {
+size_t accum_scalar(uint32_t precision) { return precision == GT_PRECISION_F64 ? sizeof(double) : sizeof(float); }
+// Checkpoint blob: header, then rng[n], sum[n], comp[n] (4 scalars each), accepted[n].
+struct AccumHeader {
+    uint32_t magic, version, width, height, precision, samples;
+    uint64_t seed;
+};
+constexpr uint32_t kAccumMagic = 0x47544143u; // "GTAC"
+uint64_t accum_payload(const gt_accumulator* a) {
+    const uint64_t n = uint64_t(a->width) * a->height;
+    return n * (sizeof(uint64_t) + 8 * accum_scalar(a->precision) + sizeof(uint32_t));
+}
+} // namespace
+
+gt_status gt_accumulator_create(gt_context* ctx, uint32_t width, uint32_t height, uint32_t precision,
+                                gt_accumulator** out) {
+    GT_GUARD_BEGIN
+    if (!ctx || !out) return fail(GT_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    if (width == 0 || height == 0 || uint64_t(width) * height > (1ull << 31))
+        return fail(GT_ERR_INVALID_ARG, "accumulator size must be positive and at most 2^31 pixels");
+    if (precision > GT_PRECISION_F64) return fail(GT_ERR_INVALID_ARG, "unknown precision");
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    auto* a = new gt_accumulator();
+    a->ctx = ctx;
+    a->width = width;
+    a->height = height;
+    a->precision = precision;
+    const size_t n = size_t(width) * height, r4 = 4 * accum_scalar(precision);
+    e = cudaMalloc(&a->rng, n * sizeof(uint64_t));
+    if (e == cudaSuccess) e = cudaMalloc(&a->sum, n * r4);
+    if (e == cudaSuccess) e = cudaMalloc(&a->comp, n * r4);
+    if (e == cudaSuccess) e = cudaMalloc(&a->accepted, n * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        cudaFree(a->rng);
+        cudaFree(a->sum);
+        cudaFree(a->comp);
+        cudaFree(a->accepted);
+        delete a;
+        return cuda_fail(e, "accumulator allocation");
+    }
+    *out = a;
+    return GT_OK;
+    GT_GUARD_END
+}
+
+void gt_accumulator_destroy(gt_accumulator* a) {
+    if (!a) return;
+    std::lock_guard<std::mutex> lock(a->ctx->mu);
+    cudaSetDevice(a->ctx->device);
+    cudaStreamSynchronize(a->ctx->stream);
+    cudaFree(a->rng);
+    cudaFree(a->sum);
+    cudaFree(a->comp);
+    cudaFree(a->accepted);
+    delete a;
+}
+
+gt_status gt_accumulator_samples(const gt_accumulator* a, uint32_t* samples) {
+    if (!a || !samples) return fail(GT_ERR_INVALID_ARG, "null argument");
+    *samples = a->samples;
+    return GT_OK;
+}
+
+gt_status gt_accumulator_save(const gt_accumulator* a, void* host, uint64_t capacity, uint64_t* size) {
+    GT_GUARD_BEGIN
+    if (!a || !size) return fail(GT_ERR_INVALID_ARG, "null argument");
+    const uint64_t need = sizeof(AccumHeader) + accum_payload(a);
+    *size = need;
+    if (!host) return GT_OK;
+    if (capacity < need) return fail(GT_ERR_INVALID_ARG, "checkpoint buffer too small");
+    std::lock_guard<std::mutex> lock(a->ctx->mu);
+    cudaError_t e = cudaSetDevice(a->ctx->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    AccumHeader h{kAccumMagic, 1u, a->width, a->height, a->precision, a->samples, a->seed};
+    auto* p = static_cast<char*>(host);
+    std::memcpy(p, &h, sizeof(h));
+    p += sizeof(h);
+    const size_t n = size_t(a->width) * a->height, r4 = 4 * accum_scalar(a->precision);
+    const void* src[4] = {a->rng, a->sum, a->comp, a->accepted};
+    const size_t bytes[4] = {n * sizeof(uint64_t), n * r4, n * r4, n * sizeof(uint32_t)};
+    for (int k = 0; k < 4; ++k) {
+        e = cudaMemcpy(p, src[k], bytes[k], cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "checkpoint copy");
+        p += bytes[k];
+    }
+    return GT_OK;
+    GT_GUARD_END
+}
+
+gt_status gt_accumulator_load(gt_accumulator* a, const void* host, uint64_t size) {
+    GT_GUARD_BEGIN
+    if (!a || !host) return fail(GT_ERR_INVALID_ARG, "null argument");
+    AccumHeader h;
+    if (size < sizeof(h)) return fail(GT_ERR_INVALID_ARG, "checkpoint too small");
+    std::memcpy(&h, host, sizeof(h));
+    if (h.magic != kAccumMagic || h.version != 1u) return fail(GT_ERR_INVALID_ARG, "not an accumulator checkpoint");
+    if (h.width != a->width || h.height != a->height || h.precision != a->precision)
+        return fail(GT_ERR_INVALID_ARG, "checkpoint size or precision differs from the accumulator's");
+    if (size < sizeof(h) + accum_payload(a)) return fail(GT_ERR_INVALID_ARG, "checkpoint truncated");
+    std::lock_guard<std::mutex> lock(a->ctx->mu);
+    cudaError_t e = cudaSetDevice(a->ctx->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    const char* p = static_cast<const char*>(host) + sizeof(h);
+    const size_t n = size_t(a->width) * a->height, r4 = 4 * accum_scalar(a->precision);
+    void* dst[4] = {a->rng, a->sum, a->comp, a->accepted};
+    const size_t bytes[4] = {n * sizeof(uint64_t), n * r4, n * r4, n * sizeof(uint32_t)};
+    for (int k = 0; k < 4; ++k) {
+        e = cudaMemcpy(dst[k], p, bytes[k], cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(e, "checkpoint copy");
+        p += bytes[k];
+    }
+    a->samples = h.samples;
+    a->seed = h.seed;
+    return GT_OK;
+    GT_GUARD_END
+}
+
+gt_status gt_render_accumulate(gt_scene* s, const gt_lights* l, const gt_environment* e, const gt_camera_desc* c,
+                               uint32_t samples, gt_accumulator* acc, const gt_render_opts* o, gt_frame* f) {
+    GT_GUARD_BEGIN
+    if (!s || !c || !acc || !f) return fail(GT_ERR_INVALID_ARG, "null argument");
+    if (acc->ctx != s->ctx) return fail(GT_ERR_INVALID_ARG, "accumulator and scene must share a context");
+    if (f->struct_size < sizeof(gt_frame)) return fail(GT_ERR_INVALID_ARG, "frame struct_size too small");
+    gt_render_opts opts;
+    std::memset(&opts, 0, sizeof(opts));
+    if (o) {
+        if (o->struct_size < sizeof(gt_render_opts)) return fail(GT_ERR_INVALID_ARG, "options struct_size too small");
+        opts = *o;
+    }
+    if (opts.schedule == GT_SCHEDULE_PERSISTENT || opts.schedule > GT_SCHEDULE_PERSISTENT)
+        return fail(GT_ERR_INVALID_ARG, "accumulation runs the auto or wavefront schedule");
+    opts.precision = acc->precision;
+    if ((l && l->ctx != s->ctx) || (e && e->ctx != s->ctx))
+        return fail(GT_ERR_INVALID_ARG, "lights, environment and scene must share a context");
+    if (c->pixel_sample_mode != GT_SAMPLE_RANDOM || c->adaptive)
+        return fail(GT_ERR_UNSUPPORTED, "accumulation needs random pixel sampling without adaptive stopping");
+    if (samples == 0 || uint64_t(acc->samples) + samples > 0xFFFFFFFFull)
+        return fail(GT_ERR_INVALID_ARG, "sample count must be positive and the total below 2^32");
+    if (acc->samples > 0 && c->rng_seed != acc->seed)
+        return fail(GT_ERR_INVALID_ARG, "the camera's rng_seed differs from the one the accumulation started with");
+    gt_camera_desc cd = *c;
+    cd.samples_per_pixel = 1; // validated as a plain random-sampling camera; the loop count is set below
+    gt_status rc = validate_camera(cd);
+    if (rc != GT_OK) return rc;
+    CamHost cam = init_camera(cd, e != nullptr);
+    if (cam.width != acc->width || cam.height != acc->height)
+        return fail(GT_ERR_INVALID_ARG, "the camera's image size differs from the accumulator's");
+    if (f->width != cam.width || f->height != cam.height)
+        return fail(GT_ERR_INVALID_ARG, "frame size does not match the camera's image size");
+    if (!f->rgb) return fail(GT_ERR_INVALID_ARG, "frame has no rgb buffer");
+    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    cudaError_t ce = cudaSetDevice(s->ctx->device);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
+    auto* env = const_cast<gt_environment*>(e);
+    if (acc->precision == GT_PRECISION_F64) return render_accumulate_f64(s, l, env, cam, opts, f, acc, samples);
+    return render_accumulate_f32(s, l, env, cam, opts, f, acc, samples);
+    GT_GUARD_END
+}
+
 gt_status gt_render_batch(gt_scene* s, const gt_lights* l, const gt_environment* e, const gt_frame_job* jobs,
                           uint32_t count, const gt_render_opts* o) {
     GT_GUARD_BEGIN

@@ -69,6 +69,19 @@ struct gt_context {
     uint32_t* mapped_dev = nullptr;
 };
 
+// Resumable accumulation state in device memory (one entry per pixel, in the
+// accumulator's precision): stream position, radiance sums, Kahan compensation, accepted.
+struct gt_accumulator {
+    gt_context* ctx = nullptr;
+    uint32_t width = 0, height = 0, precision = 0;
+    uint32_t samples = 0;  // samples per pixel accumulated
+    uint64_t seed = 0;     // the camera rng_seed the streams started from
+    uint64_t* rng = nullptr;
+    void* sum = nullptr;   // R4<R> per pixel
+    void* comp = nullptr;  // R4<R> per pixel
+    uint32_t* accepted = nullptr;
+};
+
 struct gt_scene {
     gt_context* ctx = nullptr;
     std::vector<gt_primitive> prims;
@@ -106,6 +119,10 @@ gt_status render_f32(gt_scene* s, const gt_lights* l, gt_environment* e, const C
                      const gt_render_opts& opts, gt_frame* frame);
 gt_status render_f64(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost& cam,
                      const gt_render_opts& opts, gt_frame* frame);
+gt_status render_accumulate_f32(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost& cam,
+                                const gt_render_opts& opts, gt_frame* frame, gt_accumulator* acc, uint32_t samples);
+gt_status render_accumulate_f64(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost& cam,
+                                const gt_render_opts& opts, gt_frame* frame, gt_accumulator* acc, uint32_t samples);
 gt_status render_batch_f32(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost* cams, uint32_t count,
                            const gt_render_opts& opts, gt_frame* const* frames);
 gt_status render_batch_f64(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost* cams, uint32_t count,

@@ -201,7 +201,8 @@ enum : uint32_t {
     F_DONE = 1u << 19,
     F_SHADOW0 = 1u << 20, // pending area-light shadow query
     F_SHADOW1 = 1u << 21, // pending environment shadow query
-    F_MIGRATED = 1u << 22 // finished by the concurrent persistent kernel, not the wavefront
+    F_MIGRATED = 1u << 22, // finished by the concurrent persistent kernel, not the wavefront
+    F_FRESH = 1u << 23     // resumed from an accumulator: no finished sample to fold in
 };
 
 // Error bits in counters[C_ERROR].

@@ -8,6 +8,11 @@ gt_status render_f32(gt_scene* s, const gt_lights* l, gt_environment* e, const C
     return render_impl<float>(s, l, e, cam, opts, frame);
 }
 
+gt_status render_accumulate_f32(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost& cam,
+                                const gt_render_opts& opts, gt_frame* frame, gt_accumulator* acc, uint32_t samples) {
+    return render_impl<float>(s, l, e, cam, opts, frame, acc, samples);
+}
+
 gt_status render_batch_f32(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost* cams, uint32_t count,
                            const gt_render_opts& opts, gt_frame* const* frames) {
     return render_batch_impl<float>(s, l, e, cams, count, opts, frames);

@@ -611,7 +611,8 @@ gt_status finish_render(gt_context* ctx, const Params<R>& P, gt_frame* frame, co
 
 template <class R>
 gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost& cam,
-                      const gt_render_opts& opts, gt_frame* frame) {
+                      const gt_render_opts& opts, gt_frame* frame, gt_accumulator* accum = nullptr,
+                      uint32_t add_samples = 0) {
     gt_context* ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     gt_status rc;
@@ -630,12 +631,13 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         P.env = env_of<R>(e).view;
     }
     P.cam = cam_dev<R>(cam, use_lights, use_env);
+    if (accum) P.cam.spp = accum->samples + add_samples; // the streams run on to the new total
     const uint32_t n = cam.width * cam.height;
     const bool nee = P.cam.nee && (use_lights || use_env);
 
     // Workspace: path state and queues (wavefront only), counters, and device staging
     // for host outputs.
-    const bool persistent = opts.schedule == GT_SCHEDULE_PERSISTENT;
+    const bool persistent = opts.schedule == GT_SCHEDULE_PERSISTENT && !accum;
     const bool host_out = frame->device_buffers == 0;
     auto lay = [&](Bump& bb) {
         if (persistent) {
@@ -704,6 +706,13 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         k_init<R><<<slot_blocks, threads, 0, st>>>(P);
         GT_CUDA(cudaGetLastError());
         klaunch[GT_KERNEL_OTHER] += 1;
+        if (accum && accum->samples > 0) {
+            k_accum_load<R><<<slot_blocks, threads, 0, st>>>(P, accum->rng, static_cast<const R4<R>*>(accum->sum),
+                                                             static_cast<const R4<R>*>(accum->comp), accum->accepted,
+                                                             accum->samples);
+            GT_CUDA(cudaGetLastError());
+            klaunch[GT_KERNEL_OTHER] += 1;
+        }
         if (profile) {
             GT_CUDA(cudaEventRecord(z, st));
             ev.note(GT_KERNEL_OTHER, a, z);
@@ -913,8 +922,19 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             ev.note(GT_KERNEL_OTHER, a, z);
         }
     }
-    return finish_render<R>(ctx, P, frame, opts, host_out, n, o_rgb, o_rgb64, o_acc, o_alb, o_nrm, ev, kms, klaunch,
-                            iters);
+    if (accum) {
+        k_accum_store<R><<<slot_blocks, threads, 0, st>>>(P, accum->rng, static_cast<R4<R>*>(accum->sum),
+                                                          static_cast<R4<R>*>(accum->comp), accum->accepted);
+        GT_CUDA(cudaGetLastError());
+        klaunch[GT_KERNEL_OTHER] += 1;
+    }
+    rc = finish_render<R>(ctx, P, frame, opts, host_out, n, o_rgb, o_rgb64, o_acc, o_alb, o_nrm, ev, kms, klaunch,
+                          iters);
+    if (rc == GT_OK && accum) {
+        accum->samples += add_samples;
+        accum->seed = cam.desc.rng_seed;
+    }
+    return rc;
 }
 
 // Batched frames (many small frames of one scene, each with its own camera, sample count

@@ -138,7 +138,7 @@ template <class R> __global__ void __launch_bounds__(256) k_generate(Params<R> P
                 Rng g{uint64_t(st.x) | (uint64_t(st.y) << 32)};
                 uint32_t started = st.w;
                 bool stop = false;
-                if (started > 0) stop = finish_sample(P, slot, xyz(P.ps.col[slot]));
+                if (started > 0 && !(st.z & F_FRESH)) stop = finish_sample(P, slot, xyz(P.ps.col[slot]));
                 const uint32_t x = slot % P.cam.width, y = slot / P.cam.width;
                 uint32_t flags = F_DONE;
                 while (!stop && started < limit) {
@@ -621,9 +621,11 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
     uint32_t pending = 0; // bit k: shadow query k still to trace
     bool cont = false;
     bool need_sample = true;
+    bool fresh = false; // resumed from an accumulator: no finished sample to fold in
     // Loads a wavefront slot's saved state (RESUME).
     auto resume = [&](uint32_t slot) {
         const uint4 st = P.ps.st[slot];
+        fresh = (st.z & F_FRESH) != 0;
         g.s = uint64_t(st.x) | (uint64_t(st.y) << 32);
         started = st.w;
         a = P.ps.acc[slot];
@@ -647,7 +649,7 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
     // Saves the slot's state in the wavefront layout resume() reads (RESUME hand-over); a
     // migrated slot stays marked so that the tail's k_collect leaves it to the side stream.
     auto save = [&](uint32_t slot) {
-        uint32_t flags = P.ps.st[slot].z & F_MIGRATED;
+        uint32_t flags = (P.ps.st[slot].z & F_MIGRATED) | (fresh ? F_FRESH : 0u);
         if (!need_sample) {
             flags = F_TRACE | (p.bounce & F_BOUNCE_MASK) | (p.allow_emit ? F_ALLOW_EMIT : 0u);
             P.ps.ray_o[slot] = R4<R>{p.o.x, p.o.y, p.o.z, p.time};
@@ -687,7 +689,8 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
         ++iter;
         if (alive && need_sample) {
             bool stop = false;
-            if (started > 0) stop = fold_sample(cam(), a, c, acc_n, p.col);
+            if (started > 0 && !fresh) stop = fold_sample(cam(), a, c, acc_n, p.col);
+            fresh = false;
             bool got = false;
             for (;;) {
                 const uint32_t x = local % cam().width, y = local / cam().width;
@@ -747,7 +750,8 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
                     stop = false;
                     got = false;
                     // a finished sample: fold it in before starting the next one
-                    if (started > 0) stop = fold_sample(cam(), a, c, acc_n, p.col);
+                    if (started > 0 && !fresh) stop = fold_sample(cam(), a, c, acc_n, p.col);
+                    fresh = false;
                     continue;
                 }
                 pix = item;
@@ -804,6 +808,31 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
         atomicAdd(&P.ps.totals[2], n_acc);
         atomicAdd(&P.ps.totals[3], n_started);
         atomicAdd(&P.ps.totals[6], n_rays + n_shadow);
+    }
+}
+
+// Resumable accumulation: slots start from an accumulator's streams and sums ...
+template <class R>
+__global__ void k_accum_load(Params<R> P, const uint64_t* rng, const R4<R>* sum, const R4<R>* comp,
+                             const uint32_t* accepted, uint32_t started) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.ps.n; i += gridDim.x * blockDim.x) {
+        const uint64_t s = rng[i];
+        P.ps.st[i] = make_uint4(uint32_t(s), uint32_t(s >> 32), F_NEWSAMPLE | F_FRESH, started);
+        P.ps.acc[i] = sum[i];
+        P.ps.comp[i] = comp[i];
+        P.ps.accepted[i] = accepted[i];
+    }
+}
+
+// ... and hand them back when the frame is done.
+template <class R>
+__global__ void k_accum_store(Params<R> P, uint64_t* rng, R4<R>* sum, R4<R>* comp, uint32_t* accepted) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.ps.n; i += gridDim.x * blockDim.x) {
+        const uint4 st = P.ps.st[i];
+        rng[i] = uint64_t(st.x) | (uint64_t(st.y) << 32);
+        sum[i] = P.ps.acc[i];
+        comp[i] = P.ps.comp[i];
+        accepted[i] = P.ps.accepted[i];
     }
 }
 

@@ -707,11 +707,54 @@ class HdrImage:
         g = np.sqrt(np.clip(c, 0.0, None))
         return (256.0 * np.clip(g, 0.0, 0.999)).astype(np.uint8)
 
+    def _linear(self) -> np.ndarray:
+        return self.pixels64 if self.pixels64 is not None else self.pixels.astype(np.float64)
+
+    def pfm_bytes(self) -> bytes:
+        """HdrImage::write_pfm (display.rs:365-387): little-endian f32, bottom row first,
+        non-finite components written as 0."""
+        c = self._linear()
+        c = np.where(np.isfinite(c), c, 0.0).astype("<f4")
+        return f"PF\n{self.width} {self.height}\n-1.0\n".encode() + np.ascontiguousarray(c[::-1]).tobytes()
+
+    def radiance_hdr_bytes(self) -> bytes:
+        """HdrImage::write_radiance_hdr with encode_rgbe (display.rs:394-407, 443-465): flat
+        RGBE pixels in storage order (top row first)."""
+        c = self._linear()
+        c = np.where(np.isfinite(c), np.maximum(c, 0.0), 0.0)
+        m = c.max(axis=2)
+        out = np.zeros(c.shape[:2] + (4,), dtype=np.uint8)
+        live = m > 1.0e-32
+        with np.errstate(divide="ignore"):
+            e = np.floor(np.log2(np.where(live, m, 1.0))).astype(np.int64) + 1
+        scale = 256.0 * np.ldexp(1.0, -e)
+        out[..., :3] = np.clip(c * scale[..., None], 0.0, 255.0).astype(np.uint8)
+        out[..., 3] = np.clip(e + 128, 0, 255).astype(np.uint8)
+        out[~live] = 0
+        head = f"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y {self.height} +X {self.width}\n".encode()
+        return head + out.tobytes()
+
     def save_pfm(self, path) -> None:
-        """Little-endian PFM, bottom row first (display.rs:359-388)."""
+        """HdrImage::save_pfm (display.rs:359-363)."""
         with open(path, "wb") as f:
-            f.write(f"PF\n{self.width} {self.height}\n-1.0\n".encode())
-            f.write(np.ascontiguousarray(self.pixels[::-1].astype("<f4")).tobytes())
+            f.write(self.pfm_bytes())
+
+    def save_radiance_hdr(self, path) -> None:
+        """HdrImage::save_radiance_hdr (display.rs:394-398)."""
+        with open(path, "wb") as f:
+            f.write(self.radiance_hdr_bytes())
+
+    def save_extension(self, path) -> None:
+        """HdrImage::save_extension (display.rs:419-431) for the HDR formats: .pfm, .hdr and
+        .rgbe keep the linear data; other extensions would go through a tone-mapped canvas
+        writer, which is outside this library."""
+        ext = str(path).rsplit(".", 1)[-1].lower() if "." in str(path) else ""
+        if ext == "pfm":
+            self.save_pfm(path)
+        elif ext in ("hdr", "rgbe"):
+            self.save_radiance_hdr(path)
+        else:
+            raise ValueError("only .pfm, .hdr and .rgbe are written here")
 
 
 @dataclass
@@ -721,6 +764,49 @@ class DenoisingAovs:
     beauty_linear: np.ndarray
     albedo_linear: np.ndarray
     normal_linear: np.ndarray
+
+
+class Accumulator:
+    """Accumulation state of one frame across renders (gt_accumulator): add samples with
+    PathTracer.render_accumulate, checkpoint with save() / load()."""
+
+    def __init__(self, width: int, height: int, precision: str = "f32", context: Optional[Context] = None):
+        if precision not in ("f32", "f64"):
+            raise ValueError("precision must be 'f32' or 'f64'")
+        self.ctx = context or Context.default()
+        self.width, self.height, self.precision = int(width), int(height), precision
+        h = C.c_void_p()
+        check(lib().gt_accumulator_create(self.ctx.handle, self.width, self.height,
+                                          abi.GT_PRECISION_F64 if precision == "f64" else abi.GT_PRECISION_F32,
+                                          C.byref(h)))
+        self.h = h
+
+    @property
+    def samples(self) -> int:
+        n = C.c_uint32()
+        check(lib().gt_accumulator_samples(self.h, C.byref(n)))
+        return int(n.value)
+
+    def save(self) -> bytes:
+        size = C.c_uint64()
+        check(lib().gt_accumulator_save(self.h, None, 0, C.byref(size)))
+        buf = C.create_string_buffer(size.value)
+        check(lib().gt_accumulator_save(self.h, buf, size.value, C.byref(size)))
+        return buf.raw
+
+    def load(self, blob: bytes) -> None:
+        check(lib().gt_accumulator_load(self.h, blob, len(blob)))
+
+    def close(self):
+        if self.h:
+            lib().gt_accumulator_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ------------------------------------------------------------------- renderer
@@ -765,6 +851,38 @@ class PathTracer:
     def with_options(self, options: RenderOptions) -> "PathTracer":
         return PathTracer(self.camera, options, self.precision, self._ctx, self.profile, self.schedule,
                           self.tail_slots)
+
+    def render_accumulate(self, world: RayScene, accumulator: Accumulator, samples: int,
+                          lights: Optional[WeightedSamplingTargetList] = None,
+                          environment: Optional[EnvironmentLight] = None) -> HdrImage:
+        """Adds `samples` samples per pixel to `accumulator` with this tracer's camera
+        (random sampling, no adaptive stopping) and returns the image of everything
+        accumulated so far (gt_render_accumulate)."""
+        ctx = accumulator.ctx
+        w, h, _ = self.camera.image_size()
+        want64 = accumulator.precision == "f64"
+        img = HdrImage(w, h, np.empty((h, w, 3), dtype=np.float32), np.empty((h, w), dtype=np.uint32),
+                       np.empty((h, w, 3), dtype=np.float64) if want64 else None)
+        f = abi.gt_frame()
+        f.struct_size = C.sizeof(abi.gt_frame)
+        f.width, f.height, f.device_buffers = w, h, 0
+        f.rgb = img.pixels.ctypes.data
+        f.accepted = img.accepted.ctypes.data
+        f.rgb64 = img.pixels64.ctypes.data if want64 else None
+        o = abi.gt_render_opts()
+        o.struct_size = C.sizeof(abi.gt_render_opts)
+        o.profile = 1 if self.profile else 0
+        o.schedule = abi.GT_SCHEDULE_WAVEFRONT if self.schedule == "wavefront" else abi.GT_SCHEDULE_AUTO
+        o.tail_slots = self.tail_slots
+        stats = abi.gt_render_stats()
+        o.stats = C.pointer(stats)
+        sh = world._handle(ctx)
+        lh = lights._handle(ctx).h if lights is not None else None
+        eh = environment._handle(ctx).h if environment is not None else None
+        check(lib().gt_render_accumulate(sh.h, lh, eh, C.byref(self.camera.desc()), int(samples), accumulator.h,
+                                         C.byref(o), C.byref(f)))
+        self.last_stats = stats.as_dict()
+        return img
 
     def render_batch_hdr_images(self, world: RayScene, cameras, lights: Optional[WeightedSamplingTargetList] = None,
                                 environment: Optional[EnvironmentLight] = None, want64: bool = False) -> list:

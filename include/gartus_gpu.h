@@ -342,6 +342,34 @@ void gt_environment_destroy(gt_environment* environment);
 gt_status gt_render(gt_scene* scene, const gt_lights* lights, const gt_environment* environment,
                     const gt_camera_desc* camera, const gt_render_opts* opts, gt_frame* frame);
 
+/* Accumulation state of one frame across calls (resumable rendering): per pixel the
+ * position in its sample stream, the running radiance sums and the accepted count —
+ * what the reference's pixel loop keeps in locals (camera.rs:2660-2723).  No reference
+ * counterpart: the reference's progressive rendering (PathTracer::render_progressive,
+ * renderer.rs:136-146) reports tiles as they finish; this is the GPU form of pausing
+ * and resuming a render, in memory or through a host checkpoint. */
+typedef struct gt_accumulator gt_accumulator;
+
+/* An empty accumulator for width x height pixels of the given precision (gt_precision). */
+gt_status gt_accumulator_create(gt_context* ctx, uint32_t width, uint32_t height, uint32_t precision,
+                                gt_accumulator** out);
+void gt_accumulator_destroy(gt_accumulator* acc);
+/* Samples per pixel accumulated so far. */
+gt_status gt_accumulator_samples(const gt_accumulator* acc, uint32_t* samples);
+/* Checkpoint: the state as an opaque host blob.  With host = NULL only *size is set. */
+gt_status gt_accumulator_save(const gt_accumulator* acc, void* host, uint64_t capacity, uint64_t* size);
+/* Restores a checkpoint made by gt_accumulator_save for the same size and precision. */
+gt_status gt_accumulator_load(gt_accumulator* acc, const void* host, uint64_t size);
+
+/* Renders `samples` more samples per pixel onto `acc` and writes the image of everything
+ * accumulated into `frame`.  The camera must use random pixel sampling without adaptive
+ * stopping (its samples_per_pixel is ignored) and keep the same rng_seed across calls;
+ * the image after k calls equals one gt_render with the summed sample count.  The
+ * precision is the accumulator's; opts.schedule PERSISTENT is not available here. */
+gt_status gt_render_accumulate(gt_scene* scene, const gt_lights* lights, const gt_environment* environment,
+                               const gt_camera_desc* camera, uint32_t samples, gt_accumulator* acc,
+                               const gt_render_opts* opts, gt_frame* frame);
+
 /* One frame of a batched render: its camera and its caller-owned outputs. */
 typedef struct gt_frame_job {
     const gt_camera_desc* camera;

@@ -369,6 +369,41 @@ def test_batch_rejects_bad_jobs(gpu_context):
     assert np.isfinite(buf8).all() and buf8.max() > 0
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_accumulate_equals_one_render(gpu_context, precision):
+    # gt_render_accumulate: 3 + 5 + 8 samples on one accumulator (with a host checkpoint
+    # and restore in between) give the image of one 16-sample render: each pixel's stream
+    # and Kahan sums simply continue.
+    from gartus_gb300.raytracing import Accumulator
+    scene, lights = scenes.cornell_scene()
+    base = scenes.cornell_camera(40, 1, 50).with_pixel_sample_mode(abi.GT_SAMPLE_RANDOM)
+    full = PathTracer(base.with_samples_per_pixel(16), precision=precision,
+                      context=gpu_context).render_with_lights_hdr_image(scene, lights, want64=precision == "f64")
+    pt = PathTracer(base, context=gpu_context)
+    acc = Accumulator(40, 40, precision, gpu_context)
+    pt.render_accumulate(scene, acc, 3, lights=lights)
+    blob = acc.save()
+    acc2 = Accumulator(40, 40, precision, gpu_context)
+    acc2.load(blob)
+    assert acc2.samples == 3
+    pt.render_accumulate(scene, acc2, 5, lights=lights)
+    img = pt.render_accumulate(scene, acc2, 8, lights=lights)
+    assert acc2.samples == 16
+    np.testing.assert_array_equal(img.accepted, full.accepted)
+    if precision == "f64":
+        np.testing.assert_array_equal(img.pixels64, full.pixels64)
+    else:  # the chunks may finish pixels in other kernels, which fuse f32 operations differently
+        assert _divergent(img.pixels, full.pixels.astype(np.float64)) <= 0.05 * 40 * 40
+    # Misuse is rejected: a stratified camera, another seed, a size mismatch.
+    with pytest.raises(GartusError) as e:
+        PathTracer(scenes.cornell_camera(40, 2, 50), context=gpu_context).render_accumulate(scene, acc2, 1, lights=lights)
+    assert e.value.status == abi.GT_ERR_UNSUPPORTED
+    with pytest.raises(GartusError):
+        PathTracer(base.with_rng_seed(99), context=gpu_context).render_accumulate(scene, acc2, 1, lights=lights)
+    with pytest.raises(GartusError):
+        Accumulator(8, 8, precision, gpu_context).load(blob)
+
+
 def test_edge_cases(gpu_context):
     scene = scenes.final_scene_ray_scene()
     # max_depth 0: the bounce loop never runs, every sample is black (camera.rs:1742).
