@@ -517,6 +517,8 @@ gt_status run_persistent(gt_context* ctx, Params<R>& P, uint32_t* d_next, float*
     klaunch[GT_KERNEL_OTHER] += 1;
     ctx->mapped[0] = 0;
     ctx->mapped[1] = 0;
+    if (opts.progress && opts.progress_rgb && o_rgb) // unfinished pixels read as 0 in progress images
+        GT_CUDA(cudaMemsetAsync(o_rgb, 0, size_t(n) * 3 * sizeof(float), st));
     int per_sm = 0;
     GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<R, false>, 128, 0));
     const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1);
@@ -540,6 +542,11 @@ gt_status run_persistent(gt_context* ctx, Params<R>& P, uint32_t* d_next, float*
             struct timespec ts{0, 2000000};
             nanosleep(&ts, nullptr);
             const uint32_t handed = std::min<uint32_t>(uint32_t(ctx->mapped[1]), n);
+            if (opts.progress_rgb && o_rgb) { // copied beside the running launch, on the side stream
+                GT_CUDA(cudaMemcpyAsync(opts.progress_rgb, o_rgb, size_t(n) * 3 * sizeof(float),
+                                        cudaMemcpyDeviceToHost, ctx->side));
+                GT_CUDA(cudaStreamSynchronize(ctx->side));
+            }
             if (!cancelled && opts.progress(opts.progress_user, uint64_t(handed) * limit, uint64_t(n) * limit)) {
                 ctx->mapped[0] = 1; // raise the cancel word: threads stop taking pixels
                 cancelled = true;
@@ -851,6 +858,17 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         if (may_migrate && !migrated && iters >= kMigrateAfter) {
             migrated = true;
             if ((rc = migrate()) != GT_OK) break;
+        }
+        if (opts.progress && opts.progress_rgb) { // the image as far as it is known
+            k_preview<R><<<slot_blocks, threads, 0, st>>>(P, o_rgb);
+            klaunch[GT_KERNEL_OTHER] += 1;
+            if ((ce = cudaMemcpyAsync(opts.progress_rgb, o_rgb, size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost,
+                                      st)) == cudaSuccess)
+                ce = cudaStreamSynchronize(st);
+            if (ce != cudaSuccess) {
+                rc = cuda_fail(ce, "progress image");
+                break;
+            }
         }
         if (opts.progress && opts.progress(opts.progress_user, uint64_t(done) * limit, uint64_t(n) * limit)) {
             rc = fail(GT_ERR_CANCELLED, "render cancelled by the progress callback");

@@ -436,6 +436,21 @@ template <class R> __global__ void __launch_bounds__(256) k_shadow(Params<R> P) 
     }
 }
 
+// Progressive preview: the estimate of every finished pixel, 0 elsewhere.
+template <class R> __global__ void k_preview(Params<R> P, float* rgb) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.ps.n; i += gridDim.x * blockDim.x) {
+        V3<R> c{0, 0, 0};
+        if (P.ps.st[i].z & F_DONE) {
+            const uint32_t a = P.ps.accepted[i];
+            const V3<R> s = xyz(P.ps.acc[i]);
+            c = P.cam.adaptive ? s : (a == 0 ? V3<R>{0, 0, 0} : cdiv(s, R(a)));
+        }
+        rgb[size_t(i) * 3 + 0] = float(c.x);
+        rgb[size_t(i) * 3 + 1] = float(c.y);
+        rgb[size_t(i) * 3 + 2] = float(c.z);
+    }
+}
+
 // Pixel estimate: sum / accepted (camera.rs:2993-2999) or the Welford mean.
 template <class R>
 __global__ void k_resolve(Params<R> P, float* rgb, double* rgb64, uint32_t* accepted) {

@@ -922,8 +922,40 @@ class PathTracer:
         self.last_stats = stats.as_dict()
         return images
 
+    def render_progressive(self, world: RayScene, progress, lights: Optional[WeightedSamplingTargetList] = None,
+                           environment: Optional[EnvironmentLight] = None) -> HdrImage:
+        """PathTracer::render_progressive (renderer.rs:136-146): `progress(update)` is called
+        while the frame renders with update.completed / update.total (samples) and
+        update.pixels, the image as far as it is known (finished pixels final, the rest 0).
+        An exception raised by `progress` stops the render and is re-raised, as the
+        reference returns the callback's first error."""
+        w, h, _ = self.camera.image_size()
+        preview = np.zeros((h, w, 3), dtype=np.float32)
+        raised: list = []
+
+        class Update:
+            def __init__(self, completed, total):
+                self.completed, self.total, self.pixels = int(completed), int(total), preview
+
+        @abi.GT_PROGRESS_FN
+        def cb(user, done, total):
+            try:
+                progress(Update(done, total))
+                return 0
+            except BaseException as exc:  # handed back to the caller after the cancel
+                raised.append(exc)
+                return 1
+
+        try:
+            return self._render(world, lights, environment, progress_fn=cb, progress_rgb=preview)
+        except GartusError:
+            if raised:
+                raise raised[0]
+            raise
+
     def _render(self, world: RayScene, lights: Optional[WeightedSamplingTargetList],
-                environment: Optional[EnvironmentLight], aovs: bool = False, want64: bool = False):
+                environment: Optional[EnvironmentLight], aovs: bool = False, want64: bool = False,
+                progress_fn=None, progress_rgb: Optional[np.ndarray] = None):
         ctx = self.context
         w, h, _ = self.camera.image_size()
         rgb = np.empty((h, w, 3), dtype=np.float32)
@@ -946,6 +978,9 @@ class PathTracer:
         o.profile = 1 if self.profile else 0
         o.schedule = self.SCHEDULES[self.schedule]
         o.tail_slots = self.tail_slots
+        if progress_fn is not None:
+            o.progress = progress_fn
+            o.progress_rgb = progress_rgb.ctypes.data if progress_rgb is not None else None
         stats = abi.gt_render_stats()
         o.stats = C.pointer(stats)
         sh = world._handle(ctx)

@@ -252,6 +252,13 @@ typedef struct gt_render_opts {
     uint32_t tail_slots;    /* GT_SCHEDULE_AUTO: hand over to the persistent kernel once at most
                                this many pixels are unfinished; 0 = as many as one persistent
                                launch keeps resident */
+    uint32_t reserved;
+    /* Optional host buffer of width*height*3 floats.  Before each progress call the library
+     * writes the image as far as it is known: finished pixels hold their final value, the
+     * others 0 (the partially filled `pixels` of ProgressiveRenderUpdate,
+     * camera.rs:3172-3270).  Pixels still being written by a running persistent launch
+     * may show a partial value. */
+    float* progress_rgb;
 } gt_render_opts;
 
 /* Caller-owned output images, row-major, 3 channels, y = 0 is the top row

@@ -470,6 +470,32 @@ def test_progress_callback_can_cancel(gpu_context):
     assert np.isfinite(img.pixels).all()
 
 
+@pytest.mark.parametrize("schedule", ["auto", "persistent"])
+def test_render_progressive(gpu_context, schedule):
+    # PathTracer::render_progressive (renderer.rs:136-146): updates carry the image as far
+    # as it is known; finished pixels already hold their final values.
+    scene, lights = scenes.cornell_scene()
+    cam = scenes.cornell_camera(320, 4, 50)
+    pt = PathTracer(cam, context=gpu_context, schedule=schedule)
+    seen = []
+    img = pt.render_progressive(scene, lambda u: seen.append((u.completed, u.total, u.pixels.copy())), lights=lights)
+    final = pt.render_with_lights_hdr_image(scene, lights)
+    np.testing.assert_array_equal(img.pixels, final.pixels)
+    assert seen and all(0 <= c <= t for c, t, _ in seen)
+    for _, _, px in seen:  # every channel is 0 (not yet known) or final
+        assert ((px == 0) | (px == final.pixels)).all()
+
+    class Stop(Exception):
+        pass
+
+    def stop(u):
+        raise Stop()
+
+    with pytest.raises(Stop):
+        pt.render_progressive(scene, stop, lights=lights)
+    assert np.isfinite(pt.render_with_lights_hdr_image(scene, lights).pixels).all()
+
+
 def test_persistent_progress_and_cancel(gpu_context):
     # The persistent kernel polls a host-mapped cancel word between pixels; the host
     # reports progress while it runs.  A cancelled render returns GT_ERR_CANCELLED and
