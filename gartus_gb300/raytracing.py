@@ -17,6 +17,7 @@ import copy
 import ctypes as C
 import math
 import threading
+import weakref
 from dataclasses import dataclass, field
 from typing import Optional, Sequence
 
@@ -236,7 +237,7 @@ class WeightedSamplingTargetList:
 
     def _handle(self, ctx: "Context"):
         h = self._handles.get(id(ctx))
-        if h is None:
+        if h is None or h.ctx is not ctx or not h.h:
             h = _LightsHandle(ctx, self.to_array())
             self._handles[id(ctx)] = h
         return h
@@ -270,6 +271,10 @@ class Context:
         check(lib().gt_context_create(int(device), C.byref(h)))
         self._h = h
         self.device = device
+        self._dependents = weakref.WeakSet()  # scene / lights / environment handles, accumulators
+
+    def _track(self, obj) -> None:
+        self._dependents.add(obj)
 
     @classmethod
     def default(cls) -> "Context":
@@ -283,7 +288,11 @@ class Context:
         return self._h
 
     def close(self):
+        """Destroys the context after every handle made on it (their C objects must not
+        outlive it)."""
         if self._h:
+            for d in list(self._dependents):
+                d.close()
             lib().gt_context_destroy(self._h)
             self._h = None
 
@@ -303,6 +312,7 @@ class _SceneHandle:
         h = C.c_void_p()
         check(lib().gt_scene_create(ctx.handle, C.byref(d), C.byref(h)))
         self.h = h
+        ctx._track(self)
 
     def close(self):
         if self.h:
@@ -321,7 +331,9 @@ class _LightsHandle:
         arr = np.ascontiguousarray(arr)
         h = C.c_void_p()
         check(lib().gt_lights_create(ctx.handle, arr.ctypes.data_as(C.c_void_p), len(arr), C.byref(h)))
+        self.ctx = ctx
         self.h = h
+        ctx._track(self)
 
     def close(self):
         if self.h:
@@ -472,7 +484,7 @@ class RayScene:
 
     def _handle(self, ctx: Context) -> _SceneHandle:
         h = self._handles.get(id(ctx))
-        if h is None:
+        if h is None or h.ctx is not ctx or not h.h:
             h = _SceneHandle(ctx, self.primitives_array(), self.materials_array(), self._leaf_size)
             self._handles[id(ctx)] = h
         return h
@@ -539,7 +551,7 @@ class EnvironmentLight:
 
     def _handle(self, ctx: Context):
         h = self._handles.get(id(ctx))
-        if h is None:
+        if h is None or h.ctx is not ctx or not h.h:
             h = _EnvHandle(ctx, self)
             self._handles[id(ctx)] = h
         return h
@@ -550,7 +562,9 @@ class _EnvHandle:
         d = env.desc()
         h = C.c_void_p()
         check(lib().gt_environment_create(ctx.handle, C.byref(d), C.byref(h)))
+        self.ctx = ctx
         self.h = h
+        ctx._track(self)
 
     def close(self):
         if self.h:
@@ -780,6 +794,7 @@ class Accumulator:
                                           abi.GT_PRECISION_F64 if precision == "f64" else abi.GT_PRECISION_F32,
                                           C.byref(h)))
         self.h = h
+        self.ctx._track(self)
 
     @property
     def samples(self) -> int:
