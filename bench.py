@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--schedule", default="auto", choices=["auto", "wavefront", "persistent"])
     ap.add_argument("--tail-slots", type=int, default=0,
                     help="auto schedule: unfinished pixels at which the persistent kernel takes over (0 = library)")
+    ap.add_argument("--stripes", type=int, default=0, help="wavefront stripes (0 = library default)")
     ap.add_argument("--width", type=int, default=0, help="smaller image for profiling runs (0 = the workload's)")
     ap.add_argument("--grid", type=int, default=0, help="stratified grid width for profiling runs (0 = 16)")
     ap.add_argument("--profile-run", action="store_true",
@@ -256,7 +257,7 @@ def run_ours(args):
     cams = cam if isinstance(cam, list) else None
     if cams is not None:
         cam = cams[0]
-    pt = PathTracer(cam, context=ctx, schedule=args.schedule, tail_slots=args.tail_slots)
+    pt = PathTracer(cam, context=ctx, schedule=args.schedule, tail_slots=args.tail_slots, stripes=args.stripes)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
 
     def render():
@@ -370,7 +371,8 @@ def run_ours(args):
     e2e = statistics.median(e2e_vals) * world
 
     # Roofline of the dominant kernel from one profiled frame (events around every launch).
-    prof = PathTracer(cam, context=ctx, profile=True, schedule=args.schedule, tail_slots=args.tail_slots)
+    prof = PathTracer(cam, context=ctx, profile=True, schedule=args.schedule, tail_slots=args.tail_slots,
+                      stripes=args.stripes)
     if cams is not None:
         prof.render_batch_hdr_images(scene, cams, lights=lights, environment=env)
     elif env is not None:

@@ -201,7 +201,7 @@ class gt_render_opts(C.Structure):
         ("stats", C.POINTER(gt_render_stats)),
         ("schedule", C.c_uint32),
         ("tail_slots", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("stripes", C.c_uint32),
         ("progress_rgb", C.c_void_p),
     ]
 

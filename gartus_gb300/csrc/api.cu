@@ -230,7 +230,11 @@ gt_status gt_context_create(int device, gt_context** out) {
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&ctx->pinned), 64);
+    for (int k = 0; k < gt_context::kMaxStripes && e == cudaSuccess; ++k) {
+        e = cudaStreamCreateWithFlags(&ctx->stripe_stream[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stripe_side[k], cudaStreamNonBlocking);
+    }
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&ctx->pinned), 1024);
     void* mapped = nullptr;
     if (e == cudaSuccess) e = cudaHostAlloc(&mapped, 64, cudaHostAllocMapped);
     if (e == cudaSuccess) {
@@ -241,6 +245,10 @@ gt_status gt_context_create(int device, gt_context** out) {
     if (e != cudaSuccess) {
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
         if (ctx->side) cudaStreamDestroy(ctx->side);
+        for (int k = 0; k < gt_context::kMaxStripes; ++k) {
+            if (ctx->stripe_stream[k]) cudaStreamDestroy(ctx->stripe_stream[k]);
+            if (ctx->stripe_side[k]) cudaStreamDestroy(ctx->stripe_side[k]);
+        }
         if (ctx->pinned) cudaFreeHost(ctx->pinned);
         if (ctx->mapped) cudaFreeHost(const_cast<uint32_t*>(ctx->mapped));
         delete ctx;
@@ -254,13 +262,16 @@ gt_status gt_context_create(int device, gt_context** out) {
 void gt_context_destroy(gt_context* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
-    cudaStreamSynchronize(ctx->side);
+    cudaDeviceSynchronize();
     cudaFree(ctx->ws);
     cudaFreeHost(ctx->pinned);
     cudaFreeHost(const_cast<uint32_t*>(ctx->mapped));
     cudaStreamDestroy(ctx->stream);
     cudaStreamDestroy(ctx->side);
+    for (int k = 0; k < gt_context::kMaxStripes; ++k) {
+        cudaStreamDestroy(ctx->stripe_stream[k]);
+        cudaStreamDestroy(ctx->stripe_side[k]);
+    }
     delete ctx;
 }
 

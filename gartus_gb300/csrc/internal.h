@@ -60,10 +60,15 @@ struct gt_context {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr; // concurrent persistent kernel for migrated wavefront slots
+    // Wavefront stripes: each runs its kernels on its own stream and its migrated slots on
+    // its own side stream.
+    static constexpr int kMaxStripes = 8;
+    cudaStream_t stripe_stream[kMaxStripes] = {};
+    cudaStream_t stripe_side[kMaxStripes] = {};
     std::mutex mu;
     void* ws = nullptr; // render workspace (path state, queues, staging)
     size_t ws_bytes = 0;
-    uint32_t* pinned = nullptr; // host-pinned copy of the loop counters
+    uint32_t* pinned = nullptr; // host-pinned copy of the loop counters (256 words)
     // Host memory mapped into the device: [0] cancel word, [1] pixels handed out.
     volatile uint32_t* mapped = nullptr;
     uint32_t* mapped_dev = nullptr;

@@ -165,10 +165,21 @@ template <class R> struct PathState {
                         // [13] migrated slots, [14] their pull counter, [15] tail slots,
                         // [16..22) hand-over counters
     unsigned long long* totals; // [0] rays, [1] shadow rays, [2] accepted samples, [3] started samples,
-                                // [4] samples started by unfinished slots, [5] unfinished slots,
                                 // [6] queries traced by k_persistent
+    unsigned long long* mstat;  // migration: samples started by unfinished slots, their number
     uint32_t n;
+    // Stripes: the frame's rows are dealt to `stripes` independent wavefronts (row r to
+    // stripe r % stripes), each with its own queues, counters and streams; this one owns
+    // `local_n` slots, and its queues hold up to `qcap` entries per key.
+    uint32_t stripe, stripes, row, local_n, qcap;
 };
+
+// Global slot of this stripe's j-th slot.
+template <class R> __host__ __device__ inline uint32_t stripe_slot(const PathState<R>& ps, uint32_t j) {
+    if (ps.stripes <= 1) return j;
+    const uint32_t r = j / ps.row, x = j - r * ps.row;
+    return (r * ps.stripes + ps.stripe) * ps.row + x;
+}
 
 enum : uint32_t {
     C_TRACE0 = 0,

@@ -405,7 +405,8 @@ struct Bump {
     }
 };
 
-template <class R> size_t layout_state(Bump& b, PathState<R>& ps, uint32_t n, bool nee) {
+// Per-slot path state, shared by every stripe (slot = pixel index).
+template <class R> void layout_slots(Bump& b, PathState<R>& ps, uint32_t n, bool nee) {
     ps.n = n;
     ps.ray_o = b.take<R4<R>>(n);
     ps.ray_d = b.take<R4<R>>(n);
@@ -422,15 +423,24 @@ template <class R> size_t layout_state(Bump& b, PathState<R>& ps, uint32_t n, bo
     ps.sh_d = b.take<R4<R>>(ns);
     ps.sh_a = b.take<R4<R>>(ns);
     ps.sh_s = b.take<R4<R>>(ns);
-    ps.q_trace[0] = b.take<uint32_t>(n);
-    ps.q_trace[1] = b.take<uint32_t>(n);
-    ps.q_mat = b.take<uint32_t>(size_t(n) * NUM_KEYS);
-    ps.q_shadow = b.take<uint32_t>(nee ? n : 1);
-    ps.q_migrate = b.take<uint32_t>(n);
-    ps.q_handoff = b.take<uint32_t>(n);
-    ps.counters = b.take<uint32_t>(C_COUNT);
     ps.totals = b.take<unsigned long long>(8);
-    return b.off;
+    ps.stripe = 0;
+    ps.stripes = 1;
+    ps.row = 0;
+    ps.local_n = n;
+}
+
+// One stripe's queues and counters, `cap` entries per queue.
+template <class R> void layout_queues(Bump& b, PathState<R>& ps, uint32_t cap, bool nee) {
+    ps.qcap = cap;
+    ps.q_trace[0] = b.take<uint32_t>(cap);
+    ps.q_trace[1] = b.take<uint32_t>(cap);
+    ps.q_mat = b.take<uint32_t>(size_t(cap) * NUM_KEYS);
+    ps.q_shadow = b.take<uint32_t>(nee ? cap : 1);
+    ps.q_migrate = b.take<uint32_t>(cap);
+    ps.q_handoff = b.take<uint32_t>(cap);
+    ps.counters = b.take<uint32_t>(C_COUNT);
+    ps.mstat = b.take<unsigned long long>(2);
 }
 
 inline gt_status ensure_workspace(gt_context* ctx, size_t bytes) {
@@ -438,6 +448,10 @@ inline gt_status ensure_workspace(gt_context* ctx, size_t bytes) {
     if (ctx->ws) {
         cudaStreamSynchronize(ctx->stream);
         cudaStreamSynchronize(ctx->side);
+        for (int k = 0; k < gt_context::kMaxStripes; ++k) {
+            cudaStreamSynchronize(ctx->stripe_stream[k]);
+            cudaStreamSynchronize(ctx->stripe_side[k]);
+        }
         cudaFree(ctx->ws);
         ctx->ws = nullptr;
         ctx->ws_bytes = 0;
@@ -642,10 +656,18 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     const uint32_t n = cam.width * cam.height;
     const bool nee = P.cam.nee && (use_lights || use_env);
 
-    // Workspace: path state and queues (wavefront only), counters, and device staging
-    // for host outputs.
+    // Workspace: path state (wavefront only), per-stripe queues and counters, and device
+    // staging for host outputs.
     const bool persistent = opts.schedule == GT_SCHEDULE_PERSISTENT && !accum;
     const bool host_out = frame->device_buffers == 0;
+    // Wavefront stripes: rows are dealt round-robin to K independent wavefronts on their
+    // own streams, whose kernels then overlap on the GPU (each kernel alone leaves SMs
+    // waiting on memory).
+    uint32_t K = opts.stripes ? opts.stripes : 4u;
+    K = std::max<uint32_t>(1u, std::min<uint32_t>({K, uint32_t(gt_context::kMaxStripes), cam.height}));
+    if (persistent) K = 1;
+    const uint32_t qcap = ((cam.height + K - 1) / K) * cam.width;
+    std::vector<Params<R>> SP(K);
     auto lay = [&](Bump& bb) {
         if (persistent) {
             P.ps.n = n;
@@ -653,9 +675,18 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             P.ps.totals = bb.take<unsigned long long>(8);
             P.ps.q_mat = bb.take<uint32_t>(size_t(n) * NUM_COST_CLASSES); // cost-ordered pixel queues
         } else {
-            layout_state<R>(bb, P.ps, n, nee);
+            layout_slots<R>(bb, P.ps, n, nee);
+            for (uint32_t k = 0; k < K; ++k) {
+                SP[k] = P;
+                layout_queues<R>(bb, SP[k].ps, qcap, nee);
+                SP[k].ps.stripe = k;
+                SP[k].ps.stripes = K;
+                SP[k].ps.row = cam.width;
+                SP[k].ps.local_n = ((cam.height - k + K - 1) / K) * cam.width;
+            }
+            P.ps.counters = SP[0].ps.counters; // the error word k_resolve-side checks read
         }
-        return bb.take<uint32_t>(1); // persistent pixel counter
+        return bb.take<uint32_t>(K); // persistent pixel counters (one per stripe's tail)
     };
     Bump sizing{nullptr};
     lay(sizing);
@@ -679,7 +710,6 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     const int sms = ctx->num_sms > 0 ? ctx->num_sms : 1;
     const uint32_t threads = 256;
     const uint32_t slot_blocks = std::max<uint32_t>(1u, std::min<uint32_t>((n + threads - 1) / threads, uint32_t(sms) * 8));
-    const uint32_t work_blocks = std::max<uint32_t>(1u, std::min<uint32_t>((n + threads - 1) / threads, uint32_t(sms) * 6));
 
     // Device time of the whole render, and in profile mode of every kernel launch.
     EventPool ev;
@@ -710,6 +740,8 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         cudaEvent_t a = nullptr, z = nullptr;
         if (profile) GT_CUDA(ev.pair(a, z));
         if (profile) GT_CUDA(cudaEventRecord(a, st));
+        for (uint32_t k = 0; k < K; ++k)
+            GT_CUDA(cudaMemsetAsync(SP[k].ps.counters, 0, C_COUNT * sizeof(uint32_t), st));
         k_init<R><<<slot_blocks, threads, 0, st>>>(P);
         GT_CUDA(cudaGetLastError());
         klaunch[GT_KERNEL_OTHER] += 1;
@@ -726,139 +758,223 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         }
     }
 
+    // Per-stripe launch sizes: a stripe owns about 1/K of the GPU.
+    int tail_per_sm = 0, coop_per_sm = 0;
+    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tail_per_sm, k_persistent<R, true>, 128, 0));
+    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&coop_per_sm, k_persistent<R, true, false, true>, 128, 0));
+    const uint32_t full_persist = uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1));
+    const uint32_t full_coop = uint32_t(sms) * uint32_t(std::max(coop_per_sm, 1));
+    const uint32_t lblocks = std::max<uint32_t>(1u, std::min<uint32_t>((qcap + threads - 1) / threads, uint32_t(sms) * 8));
+    const uint32_t wblocks = std::max<uint32_t>(1u, std::min<uint32_t>((qcap + threads - 1) / threads, uint32_t(sms) * 6));
+    const uint32_t tblocks = std::max<uint32_t>(uint32_t(sms), full_persist / K);
+    const uint32_t coop_blocks = std::max<uint32_t>(uint32_t(sms), full_coop / K);
+    const uint32_t side_blocks = std::max<uint32_t>(uint32_t(sms) / 2u, full_persist / K);
+    const uint32_t side_coop_blocks = std::max<uint32_t>(uint32_t(sms) / 2u, uint32_t(sms) * 2u / K);
+    uint32_t tail_slots = 0;
+    if (opts.schedule == GT_SCHEDULE_AUTO)
+        tail_slots = opts.tail_slots ? (opts.tail_slots + K - 1) / K : tblocks * 128u;
+    // Slow-slot migration: once per stripe, after kMigrateAfter iterations, the slots
+    // progressing at less than 1/kMigrateRatio of the stripe's mean sample rate move to
+    // k_persistent (resume mode) on the stripe's side stream.
+    constexpr uint64_t kMigrateAfter = 60;
+    constexpr float kMigrateRatio = 2.0f;
+    const bool may_migrate = opts.schedule == GT_SCHEDULE_AUTO;
+    ctx->mapped[0] = 0; // the side kernels' cancel word
+
     // One iteration = generate, trace, shade (+ shadow); two iterations (ping-pong trace
-    // queues) are captured once as a graph and replayed.
+    // queues) are captured once per stripe as a graph and replayed.
     const int kernels_per_iteration = nee ? 4 : 3;
-    auto launch_iteration = [&](uint32_t cur, bool timed) -> cudaError_t {
-        for (int k = 0; k < kernels_per_iteration; ++k) {
+    struct Stripe {
+        cudaStream_t st, side;
+        cudaGraphExec_t exec = nullptr;
+        uint64_t iters = 0;
+        uint32_t batch = 2;
+        bool running = true, migrated = false, tail = false;
+        cudaEvent_t fork = nullptr, join = nullptr;
+    };
+    std::vector<Stripe> S(K);
+    auto launch_iteration = [&](uint32_t k, uint32_t cur, bool timed) -> cudaError_t {
+        const cudaStream_t s = S[k].st;
+        for (int q = 0; q < kernels_per_iteration; ++q) {
             cudaEvent_t a = nullptr, z = nullptr;
             if (timed) {
                 cudaError_t e = ev.pair(a, z);
                 if (e != cudaSuccess) return e;
-                cudaEventRecord(a, st);
+                cudaEventRecord(a, s);
             }
-            if (k == 0) k_generate<R><<<slot_blocks, threads, 0, st>>>(P, cur);
-            else if (k == 1) k_trace<R><<<work_blocks, threads, 0, st>>>(P, cur);
-            else if (k == 2) k_shade<R><<<work_blocks, threads, 0, st>>>(P, cur);
-            else k_shadow<R><<<work_blocks, threads, 0, st>>>(P);
+            if (q == 0) k_generate<R><<<lblocks, threads, 0, s>>>(SP[k], cur);
+            else if (q == 1) k_trace<R><<<wblocks, threads, 0, s>>>(SP[k], cur);
+            else if (q == 2) k_shade<R><<<wblocks, threads, 0, s>>>(SP[k], cur);
+            else k_shadow<R><<<wblocks, threads, 0, s>>>(SP[k]);
             if (timed) {
-                cudaEventRecord(z, st);
-                ev.note(k == 0 ? GT_KERNEL_GENERATE : k == 1 ? GT_KERNEL_TRACE : k == 2 ? GT_KERNEL_SHADE : GT_KERNEL_SHADOW,
+                cudaEventRecord(z, s);
+                ev.note(q == 0 ? GT_KERNEL_GENERATE : q == 1 ? GT_KERNEL_TRACE : q == 2 ? GT_KERNEL_SHADE : GT_KERNEL_SHADOW,
                         a, z);
             }
         }
         return cudaGetLastError();
     };
-    cudaGraphExec_t exec = nullptr;
-    cudaError_t ce = cudaSuccess;
-    if (!profile) {
-        cudaGraph_t graph = nullptr;
-        GT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        cudaError_t le = launch_iteration(0, false);
-        if (le == cudaSuccess) le = launch_iteration(1, false);
-        ce = cudaStreamEndCapture(st, &graph);
-        if (le != cudaSuccess) return cuda_fail(le, "kernel launch during capture");
-        if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
-        ce = cudaGraphInstantiate(&exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (ce != cudaSuccess) return cuda_fail(ce, "cudaGraphInstantiate");
+    auto cleanup = [&]() {
+        for (auto& x : S)
+            if (x.exec) cudaGraphExecDestroy(x.exec);
+    };
+    cudaEvent_t init_done = nullptr;
+    GT_CUDA(ev.get(init_done));
+    GT_CUDA(cudaEventRecord(init_done, st));
+    for (uint32_t k = 0; k < K; ++k) {
+        S[k].st = ctx->stripe_stream[k];
+        S[k].side = ctx->stripe_side[k];
+        GT_CUDA(cudaStreamWaitEvent(S[k].st, init_done, 0));
+        if (!profile) {
+            cudaGraph_t graph = nullptr;
+            GT_CUDA(cudaStreamBeginCapture(S[k].st, cudaStreamCaptureModeThreadLocal));
+            cudaError_t le = launch_iteration(k, 0, false);
+            if (le == cudaSuccess) le = launch_iteration(k, 1, false);
+            cudaError_t ce = cudaStreamEndCapture(S[k].st, &graph);
+            if (le != cudaSuccess || ce != cudaSuccess) {
+                if (graph) cudaGraphDestroy(graph);
+                cleanup();
+                return cuda_fail(le != cudaSuccess ? le : ce, "wavefront graph capture");
+            }
+            ce = cudaGraphInstantiate(&S[k].exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ce != cudaSuccess) {
+                cleanup();
+                return cuda_fail(ce, "cudaGraphInstantiate");
+            }
+        }
     }
+
+    auto migrate = [&](uint32_t k) -> gt_status {
+        Params<R>& Q = SP[k];
+        const cudaStream_t s = S[k].st;
+        GT_CUDA(cudaMemsetAsync(Q.ps.mstat, 0, 2 * sizeof(unsigned long long), s));
+        GT_CUDA(cudaMemsetAsync(Q.ps.counters + C_MIGRATED, 0, 2 * sizeof(uint32_t), s));
+        GT_CUDA(cudaMemsetAsync(Q.ps.counters + C_SIDE_DONE, 0, 3 * sizeof(uint32_t), s));
+        GT_CUDA(cudaMemsetAsync(Q.ps.counters + C_TRACE1, 0, sizeof(uint32_t), s));
+        k_progress_sum<R><<<lblocks, threads, 0, s>>>(Q);
+        k_migrate<R><<<lblocks, threads, 0, s>>>(Q, kMigrateRatio);
+        k_drop_migrated<R><<<wblocks, threads, 0, s>>>(Q);
+        k_restore_queue<R><<<wblocks, threads, 0, s>>>(Q);
+        GT_CUDA(cudaGetLastError());
+        klaunch[GT_KERNEL_OTHER] += 4;
+        GT_CUDA(ev.pair(S[k].fork, S[k].join));
+        GT_CUDA(cudaEventRecord(S[k].fork, s));
+        GT_CUDA(cudaStreamWaitEvent(S[k].side, S[k].fork, 0));
+        HandOff ho;
+        ho.done = Q.ps.counters + C_SIDE_DONE;
+        ho.below = side_coop_blocks * 4u;
+        ho.list = Q.ps.q_handoff;
+        ho.count = Q.ps.counters + C_SIDE_COOP;
+        k_persistent<R, true><<<side_blocks, 128, 0, S[k].side>>>(Q, Q.ps.counters + C_MIGRATE_NEXT, Q.ps.q_migrate,
+                                                                   Q.ps.counters + C_MIGRATED, ctx->mapped_dev,
+                                                                   nullptr, nullptr, nullptr, nullptr, ho);
+        k_persistent<R, true, false, true><<<side_coop_blocks, 128, 0, S[k].side>>>(
+            Q, Q.ps.counters + C_SIDE_COOP_NEXT, Q.ps.q_handoff, Q.ps.counters + C_SIDE_COOP, ctx->mapped_dev, nullptr,
+            nullptr, nullptr, nullptr);
+        GT_CUDA(cudaGetLastError());
+        klaunch[GT_KERNEL_PERSISTENT] += 2;
+        GT_CUDA(cudaEventRecord(S[k].join, S[k].side));
+        S[k].migrated = true;
+        return GT_OK;
+    };
+    // The last pixels of a stripe are its longest sample chains; once no more than one
+    // persistent launch's worth of its slots is left, per-bounce launches would run
+    // nearly empty, so the remaining slots finish in k_persistent's RESUME mode: one slot
+    // per lane, then one slot per warp for the last ones.
+    auto run_tail = [&](uint32_t k) -> gt_status {
+        Params<R>& Q = SP[k];
+        const cudaStream_t s = S[k].st;
+        cudaEvent_t a = nullptr, z = nullptr;
+        if (profile) GT_CUDA(ev.pair(a, z));
+        if (profile) GT_CUDA(cudaEventRecord(a, s));
+        uint32_t* list = Q.ps.q_trace[0];
+        uint32_t* count = Q.ps.counters + C_TAIL;
+        GT_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t), s));
+        GT_CUDA(cudaMemsetAsync(Q.ps.counters + C_TAIL_DONE, 0, 3 * sizeof(uint32_t), s));
+        GT_CUDA(cudaMemsetAsync(d_next + k, 0, sizeof(uint32_t), s));
+        k_collect<R><<<lblocks, threads, 0, s>>>(Q, list, count);
+        HandOff ho;
+        ho.done = Q.ps.counters + C_TAIL_DONE;
+        ho.below = coop_blocks * 4u;
+        ho.list = Q.ps.q_trace[1];
+        ho.count = Q.ps.counters + C_TAIL_COOP;
+        k_persistent<R, true><<<tblocks, 128, 0, s>>>(Q, d_next + k, list, count, nullptr, nullptr, nullptr, nullptr,
+                                                      nullptr, ho);
+        k_persistent<R, true, false, true><<<coop_blocks, 128, 0, s>>>(
+            Q, Q.ps.counters + C_TAIL_COOP_NEXT, Q.ps.q_trace[1], Q.ps.counters + C_TAIL_COOP, nullptr, nullptr, nullptr,
+            nullptr, nullptr);
+        GT_CUDA(cudaGetLastError());
+        klaunch[GT_KERNEL_OTHER] += 1;
+        klaunch[GT_KERNEL_PERSISTENT] += 2;
+        if (profile) {
+            GT_CUDA(cudaEventRecord(z, s));
+            ev.note(GT_KERNEL_PERSISTENT, a, z);
+        }
+        S[k].tail = true;
+        return GT_OK;
+    };
 
     const uint32_t limit = P.cam.adaptive ? P.cam.adaptive_max : P.cam.spp;
     const uint64_t max_iters = uint64_t(limit) * uint64_t(std::max<uint32_t>(P.cam.max_depth, 1u)) + 8;
     uint64_t iters = 0;
-    uint32_t batch = 2;
     rc = GT_OK;
-    // The last pixels of a frame are the longest sample chains; once no more than one
-    // persistent launch's worth of slots is left, per-bounce launches would run nearly
-    // empty, so the remaining slots finish in k_persistent's RESUME mode.
-    int tail_per_sm = 0, coop_per_sm = 0;
-    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tail_per_sm, k_persistent<R, true>, 128, 0));
-    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&coop_per_sm, k_persistent<R, true, false, true>, 128, 0));
-    // Cooperative launches (one warp per slot): the tail's fills the GPU, the side
-    // stream's takes two blocks per SM next to the running wavefront.
-    const uint32_t coop_blocks = uint32_t(sms) * uint32_t(std::max(coop_per_sm, 1));
-    const uint32_t side_coop_blocks = uint32_t(sms) * uint32_t(std::min(std::max(coop_per_sm, 1), 2));
-    uint32_t tail_slots = 0;
-    if (opts.schedule == GT_SCHEDULE_AUTO)
-        tail_slots = opts.tail_slots ? opts.tail_slots : uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1)) * 128u;
-    bool run_tail = false;
-    // Slow-slot migration: once, after kMigrateAfter iterations, the slots progressing at
-    // less than 1/kMigrateRatio of the mean sample rate move to k_persistent (resume mode)
-    // on the context's side stream, concurrently with the rest of the wavefront.
-    constexpr uint64_t kMigrateAfter = 60;
-    constexpr float kMigrateRatio = 2.0f;
-    const bool may_migrate = opts.schedule == GT_SCHEDULE_AUTO;
-    bool migrated = false;
-    cudaEvent_t fork = nullptr, join = nullptr;
-    ctx->mapped[0] = 0; // the side kernel's cancel word
-    auto migrate = [&]() -> gt_status {
-        GT_CUDA(cudaMemsetAsync(P.ps.totals + 4, 0, 2 * sizeof(unsigned long long), st));
-        GT_CUDA(cudaMemsetAsync(P.ps.counters + C_MIGRATED, 0, 2 * sizeof(uint32_t), st));
-        GT_CUDA(cudaMemsetAsync(P.ps.counters + C_SIDE_DONE, 0, 3 * sizeof(uint32_t), st));
-        GT_CUDA(cudaMemsetAsync(P.ps.counters + C_TRACE1, 0, sizeof(uint32_t), st));
-        k_progress_sum<R><<<slot_blocks, threads, 0, st>>>(P);
-        k_migrate<R><<<slot_blocks, threads, 0, st>>>(P, kMigrateRatio);
-        k_drop_migrated<R><<<work_blocks, threads, 0, st>>>(P);
-        k_restore_queue<R><<<work_blocks, threads, 0, st>>>(P);
-        GT_CUDA(cudaGetLastError());
-        klaunch[GT_KERNEL_OTHER] += 4;
-        GT_CUDA(ev.pair(fork, join));
-        GT_CUDA(cudaEventRecord(fork, st));
-        GT_CUDA(cudaStreamWaitEvent(ctx->side, fork, 0));
-        const uint32_t side_blocks = uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1));
-        HandOff ho;
-        ho.done = P.ps.counters + C_SIDE_DONE;
-        ho.below = side_coop_blocks * 4u;
-        ho.list = P.ps.q_handoff;
-        ho.count = P.ps.counters + C_SIDE_COOP;
-        k_persistent<R, true><<<side_blocks, 128, 0, ctx->side>>>(P, P.ps.counters + C_MIGRATE_NEXT, P.ps.q_migrate,
-                                                                  P.ps.counters + C_MIGRATED, ctx->mapped_dev,
-                                                                  nullptr, nullptr, nullptr, nullptr, ho);
-        k_persistent<R, true, false, true><<<side_coop_blocks, 128, 0, ctx->side>>>(
-            P, P.ps.counters + C_SIDE_COOP_NEXT, P.ps.q_handoff, P.ps.counters + C_SIDE_COOP, ctx->mapped_dev, nullptr,
-            nullptr, nullptr, nullptr);
-        GT_CUDA(cudaGetLastError());
-        klaunch[GT_KERNEL_PERSISTENT] += 2;
-        GT_CUDA(cudaEventRecord(join, ctx->side));
-        return GT_OK;
-    };
-    for (;;) {
-        for (uint32_t k = 0; k < batch && ce == cudaSuccess; ++k) {
-            if (profile) {
-                ce = launch_iteration(0, true);
-                if (ce == cudaSuccess) ce = launch_iteration(1, true);
-            } else {
-                ce = cudaGraphLaunch(exec, st);
+    for (uint32_t active = K; active > 0 && rc == GT_OK;) {
+        cudaError_t ce = cudaSuccess;
+        for (uint32_t k = 0; k < K && ce == cudaSuccess; ++k) {
+            if (!S[k].running) continue;
+            for (uint32_t i = 0; i < S[k].batch && ce == cudaSuccess; ++i) {
+                if (profile) {
+                    ce = launch_iteration(k, 0, true);
+                    if (ce == cudaSuccess) ce = launch_iteration(k, 1, true);
+                } else {
+                    ce = cudaGraphLaunch(S[k].exec, S[k].st);
+                }
+                for (int q = 0; q < kernels_per_iteration; ++q) klaunch[GT_KERNEL_GENERATE + q] += 2;
             }
-            for (int kk = 0; kk < kernels_per_iteration; ++kk) klaunch[GT_KERNEL_GENERATE + kk] += 2;
+            S[k].iters += 2ull * S[k].batch;
+            iters = std::max(iters, S[k].iters);
+            if (ce == cudaSuccess)
+                ce = cudaMemcpyAsync(ctx->pinned + 64 + 2 * k, SP[k].ps.counters + C_DONE, 2 * sizeof(uint32_t),
+                                     cudaMemcpyDeviceToHost, S[k].st);
         }
+        for (uint32_t k = 0; k < K && ce == cudaSuccess; ++k)
+            if (S[k].running) ce = cudaStreamSynchronize(S[k].st);
         if (ce != cudaSuccess) {
             rc = cuda_fail(ce, "wavefront launch");
             break;
         }
-        iters += 2ull * batch;
-        ce = cudaMemcpyAsync(ctx->pinned, P.ps.counters + C_DONE, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
-        if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
-        if (ce != cudaSuccess) {
-            rc = cuda_fail(ce, "render loop");
-            break;
-        }
         if (profile) ev.harvest(kms);
-        const uint32_t done = ctx->pinned[0], err = ctx->pinned[1];
-        if (err) {
-            rc = fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
-            break;
+        uint64_t done_all = 0;
+        for (uint32_t k = 0; k < K; ++k) {
+            const uint32_t local = SP[k].ps.local_n;
+            if (!S[k].running) {
+                done_all += local;
+                continue;
+            }
+            const uint32_t done = ctx->pinned[64 + 2 * k], err = ctx->pinned[64 + 2 * k + 1];
+            done_all += std::min(done, local);
+            if (err) {
+                rc = fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
+                break;
+            }
+            if (done >= local) {
+                S[k].running = false;
+                --active;
+            } else if (local - done <= tail_slots) { // few pixels left: finish them in a persistent launch
+                if ((rc = run_tail(k)) != GT_OK) break;
+                S[k].running = false;
+                --active;
+            } else {
+                if (may_migrate && !S[k].migrated && S[k].iters >= kMigrateAfter && (rc = migrate(k)) != GT_OK) break;
+                if (S[k].iters > max_iters) {
+                    rc = fail(GT_ERR_INTERNAL, "wavefront did not terminate within its iteration bound");
+                    break;
+                }
+                S[k].batch = std::min<uint32_t>(S[k].batch * 2, profile ? 8u : 64u);
+            }
         }
-        if (done >= n) break;
-        if (n - done <= tail_slots) { // few pixels left: finish them in one persistent launch
-            run_tail = true;
-            break;
-        }
-        if (may_migrate && !migrated && iters >= kMigrateAfter) {
-            migrated = true;
-            if ((rc = migrate()) != GT_OK) break;
-        }
+        if (rc != GT_OK || active == 0) break;
         if (opts.progress && opts.progress_rgb) { // the image as far as it is known
             k_preview<R><<<slot_blocks, threads, 0, st>>>(P, o_rgb);
             klaunch[GT_KERNEL_OTHER] += 1;
@@ -870,58 +986,30 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
                 break;
             }
         }
-        if (opts.progress && opts.progress(opts.progress_user, uint64_t(done) * limit, uint64_t(n) * limit)) {
+        if (opts.progress && opts.progress(opts.progress_user, done_all * limit, uint64_t(n) * limit)) {
             rc = fail(GT_ERR_CANCELLED, "render cancelled by the progress callback");
             break;
         }
-        if (iters > max_iters) {
-            rc = fail(GT_ERR_INTERNAL, "wavefront did not terminate within its iteration bound");
-            break;
-        }
-        batch = std::min<uint32_t>(batch * 2, profile ? 8u : 64u);
     }
-    if (exec) cudaGraphExecDestroy(exec);
+    cleanup();
     if (rc != GT_OK) {
-        ctx->mapped[0] = 1; // the side kernel stops taking slots
-        cudaStreamSynchronize(st);
-        cudaStreamSynchronize(ctx->side);
+        ctx->mapped[0] = 1; // the side kernels stop taking slots
+        cudaDeviceSynchronize();
         return rc;
     }
-    if (run_tail) {
-        cudaEvent_t a = nullptr, z = nullptr;
-        if (profile) GT_CUDA(ev.pair(a, z));
-        if (profile) GT_CUDA(cudaEventRecord(a, st));
-        uint32_t* list = P.ps.q_trace[0];
-        uint32_t* count = P.ps.counters + C_TAIL;
-        GT_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t), st));
-        GT_CUDA(cudaMemsetAsync(P.ps.counters + C_TAIL_DONE, 0, 3 * sizeof(uint32_t), st));
-        GT_CUDA(cudaMemsetAsync(d_next, 0, sizeof(uint32_t), st));
-        k_collect<R><<<slot_blocks, threads, 0, st>>>(P, list, count);
-        const uint32_t tblocks = uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1));
-        // The tail runs one slot per lane until no more slots are left than the
-        // cooperative launch has warps, then one slot per warp.
-        HandOff ho;
-        ho.done = P.ps.counters + C_TAIL_DONE;
-        ho.below = coop_blocks * 4u;
-        ho.list = P.ps.q_trace[1];
-        ho.count = P.ps.counters + C_TAIL_COOP;
-        k_persistent<R, true><<<tblocks, 128, 0, st>>>(P, d_next, list, count, nullptr, nullptr, nullptr, nullptr,
-                                                       nullptr, ho);
-        k_persistent<R, true, false, true><<<coop_blocks, 128, 0, st>>>(
-            P, P.ps.counters + C_TAIL_COOP_NEXT, P.ps.q_trace[1], P.ps.counters + C_TAIL_COOP, nullptr, nullptr, nullptr,
-            nullptr, nullptr);
-        GT_CUDA(cudaGetLastError());
-        klaunch[GT_KERNEL_OTHER] += 1;
-        klaunch[GT_KERNEL_PERSISTENT] += 2;
-        if (profile) {
-            GT_CUDA(cudaEventRecord(z, st));
-            ev.note(GT_KERNEL_PERSISTENT, a, z);
+    // Join every stripe (and its side stream) before the resolve reads every slot.
+    for (uint32_t k = 0; k < K; ++k) {
+        cudaEvent_t end = nullptr;
+        GT_CUDA(ev.get(end));
+        GT_CUDA(cudaEventRecord(end, S[k].st));
+        GT_CUDA(cudaStreamWaitEvent(st, end, 0));
+        ev.free_events.push_back(end);
+        if (S[k].migrated) {
+            GT_CUDA(cudaStreamWaitEvent(st, S[k].join, 0));
+            ev.note(GT_KERNEL_PERSISTENT, S[k].fork, S[k].join);
         }
     }
-    if (migrated) { // join the side stream before the resolve reads every slot
-        GT_CUDA(cudaStreamWaitEvent(st, join, 0));
-        ev.note(GT_KERNEL_PERSISTENT, fork, join);
-    }
+    ev.free_events.push_back(init_done);
 
     {
         cudaEvent_t a = nullptr, z = nullptr;
@@ -946,8 +1034,28 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         GT_CUDA(cudaGetLastError());
         klaunch[GT_KERNEL_OTHER] += 1;
     }
-    rc = finish_render<R>(ctx, P, frame, opts, host_out, n, o_rgb, o_rgb64, o_acc, o_alb, o_nrm, ev, kms, klaunch,
+    // Per-stripe counters into the frame's: stack overflow flags, migrated and tail pixels.
+    Params<R> F = P;
+    F.ps.counters = SP[0].ps.counters;
+    std::vector<uint32_t> words(size_t(K) * C_COUNT);
+    for (uint32_t k = 0; k < K; ++k)
+        GT_CUDA(cudaMemcpyAsync(words.data() + size_t(k) * C_COUNT, SP[k].ps.counters, C_COUNT * sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, st));
+    rc = finish_render<R>(ctx, F, frame, opts, host_out, n, o_rgb, o_rgb64, o_acc, o_alb, o_nrm, ev, kms, klaunch,
                           iters);
+    if (rc == GT_OK) {
+        uint64_t migrated_px = 0, tail_px = 0;
+        for (uint32_t k = 0; k < K; ++k) {
+            const uint32_t* w = words.data() + size_t(k) * C_COUNT;
+            if (w[C_ERROR]) rc = fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
+            migrated_px += w[C_MIGRATED];
+            tail_px += w[C_TAIL];
+        }
+        if (rc == GT_OK && opts.stats) {
+            opts.stats->migrated_pixels = migrated_px;
+            opts.stats->tail_pixels = tail_px;
+        }
+    }
     if (rc == GT_OK && accum) {
         accum->samples += add_samples;
         accum->seed = cam.desc.rng_seed;

@@ -125,14 +125,15 @@ template <class R> __global__ void __launch_bounds__(256) k_generate(Params<R> P
         for (uint32_t k = 0; k < NUM_KEYS; ++k) P.ps.counters[C_MAT + k] = 0;
         P.ps.counters[C_SHADOW] = 0;
     }
-    const uint32_t n = P.ps.n;
+    const uint32_t n = P.ps.local_n;
     const uint32_t limit = P.cam.adaptive ? P.cam.adaptive_max : P.cam.spp;
     const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = warp0; base < n; base += stride) {
-        const uint32_t slot = base + lane_id();
+        const uint32_t j = base + lane_id();
+        const uint32_t slot = j < n ? stripe_slot(P.ps, j) : 0u;
         bool push = false;
-        if (slot < n) {
+        if (j < n) {
             uint4 st = P.ps.st[slot];
             if (st.z & F_NEWSAMPLE) {
                 Rng g{uint64_t(st.x) | (uint64_t(st.y) << 32)};
@@ -187,7 +188,7 @@ template <class R> __global__ void __launch_bounds__(256, 6) k_trace(Params<R> P
             P.ps.hit_prim[slot] = prim;
             key = prim < 0 ? KEY_MISS : uint32_t(P.sc.mats[__ldg(&P.sc.meta[prim].x) >> 3].kind);
         }
-        warp_push_keyed(valid, key, slot, P.ps.q_mat, P.ps.n, &P.ps.counters[C_MAT]);
+        warp_push_keyed(valid, key, slot, P.ps.q_mat, P.ps.qcap, &P.ps.counters[C_MAT]);
     }
 }
 
@@ -396,7 +397,7 @@ template <class R> __global__ void __launch_bounds__(256) k_shade(Params<R> P, u
 #pragma unroll
             for (uint32_t k = 1; k < NUM_KEYS; ++k)
                 if (i >= prefix[k]) key = k;
-            slot = P.ps.q_mat[size_t(key) * P.ps.n + (i - prefix[key])];
+            slot = P.ps.q_mat[size_t(key) * P.ps.qcap + (i - prefix[key])];
             cont = shade_slot(P, slot, key, shadow);
         }
         warp_push(cont, slot, P.ps.q_trace[cur ^ 1u], &P.ps.counters[C_TRACE0 + (cur ^ 1u)]);
@@ -853,12 +854,13 @@ __global__ void k_accum_store(Params<R> P, uint64_t* rng, R4<R>* sum, R4<R>* com
 
 // Lists the wavefront slots that have not finished their pixel (for the RESUME pass).
 template <class R> __global__ void __launch_bounds__(256) k_collect(Params<R> P, uint32_t* list, uint32_t* count) {
-    const uint32_t n = P.ps.n;
+    const uint32_t n = P.ps.local_n;
     const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = warp0; base < n; base += stride) {
-        const uint32_t slot = base + lane_id();
-        const bool live = slot < n && (P.ps.st[slot].z & (F_DONE | F_MIGRATED)) == 0;
+        const uint32_t j = base + lane_id();
+        const uint32_t slot = j < n ? stripe_slot(P.ps, j) : 0u;
+        const bool live = j < n && (P.ps.st[slot].z & (F_DONE | F_MIGRATED)) == 0;
         warp_push(live, slot, list, count);
     }
 }
@@ -869,12 +871,12 @@ template <class R> __global__ void __launch_bounds__(256) k_collect(Params<R> P,
 // is far below the mean move to a persistent kernel on a second stream, which runs them
 // concurrently with the wavefront at one bounce per loop instead of one per iteration.
 //
-// Pass 1: samples started by unfinished slots, and their number, into totals[4], [5].
+// Pass 1: samples started by unfinished slots, and their number, into mstat[0], [1].
 template <class R> __global__ void __launch_bounds__(256) k_progress_sum(Params<R> P) {
-    const uint32_t n = P.ps.n;
+    const uint32_t n = P.ps.local_n;
     unsigned long long s = 0, c = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint4 st = P.ps.st[i];
+        const uint4 st = P.ps.st[stripe_slot(P.ps, i)];
         if ((st.z & (F_DONE | F_MIGRATED)) == 0) {
             s += st.w;
             c += 1;
@@ -885,8 +887,8 @@ template <class R> __global__ void __launch_bounds__(256) k_progress_sum(Params<
         c += __shfl_down_sync(0xffffffffu, c, off);
     }
     if (lane_id() == 0 && c) {
-        atomicAdd(&P.ps.totals[4], s);
-        atomicAdd(&P.ps.totals[5], c);
+        atomicAdd(&P.ps.mstat[0], s);
+        atomicAdd(&P.ps.mstat[1], c);
     }
 }
 
@@ -894,14 +896,15 @@ template <class R> __global__ void __launch_bounds__(256) k_progress_sum(Params<
 // lists it in q_migrate and counts it as done for the wavefront's termination test.
 // A migrated slot keeps its path state; clearing F_NEWSAMPLE keeps k_generate away.
 template <class R> __global__ void __launch_bounds__(256) k_migrate(Params<R> P, float ratio) {
-    const uint32_t n = P.ps.n;
-    const double sum = double(P.ps.totals[4]), live = double(P.ps.totals[5]);
+    const uint32_t n = P.ps.local_n;
+    const double sum = double(P.ps.mstat[0]), live = double(P.ps.mstat[1]);
     const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = warp0; base < n; base += stride) {
-        const uint32_t slot = base + lane_id();
+        const uint32_t j = base + lane_id();
+        const uint32_t slot = j < n ? stripe_slot(P.ps, j) : 0u;
         bool mig = false;
-        if (slot < n && live > 0.0) {
+        if (j < n && live > 0.0) {
             uint4 st = P.ps.st[slot];
             mig = (st.z & (F_DONE | F_MIGRATED)) == 0 && double(st.w) * double(ratio) * live < sum;
             if (mig) {

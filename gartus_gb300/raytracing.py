@@ -845,7 +845,7 @@ class PathTracer:
 
     def __init__(self, camera: RayCamera, options: RenderOptions = RenderOptions(), precision: str = "f32",
                  context: Optional[Context] = None, profile: bool = False, schedule: str = "auto",
-                 tail_slots: int = 0):
+                 tail_slots: int = 0, stripes: int = 0):
         if precision not in ("f32", "f64"):
             raise ValueError("precision must be 'f32' or 'f64'")
         if schedule not in self.SCHEDULES:
@@ -856,6 +856,7 @@ class PathTracer:
         self.profile = profile
         self.schedule = schedule
         self.tail_slots = int(tail_slots)
+        self.stripes = int(stripes)
         self._ctx = context
         self.last_stats: Optional[dict] = None
 
@@ -865,7 +866,7 @@ class PathTracer:
 
     def with_options(self, options: RenderOptions) -> "PathTracer":
         return PathTracer(self.camera, options, self.precision, self._ctx, self.profile, self.schedule,
-                          self.tail_slots)
+                          self.tail_slots, self.stripes)
 
     def render_accumulate(self, world: RayScene, accumulator: Accumulator, samples: int,
                           lights: Optional[WeightedSamplingTargetList] = None,
@@ -889,6 +890,7 @@ class PathTracer:
         o.profile = 1 if self.profile else 0
         o.schedule = abi.GT_SCHEDULE_WAVEFRONT if self.schedule == "wavefront" else abi.GT_SCHEDULE_AUTO
         o.tail_slots = self.tail_slots
+        o.stripes = self.stripes
         stats = abi.gt_render_stats()
         o.stats = C.pointer(stats)
         sh = world._handle(ctx)
@@ -993,6 +995,7 @@ class PathTracer:
         o.profile = 1 if self.profile else 0
         o.schedule = self.SCHEDULES[self.schedule]
         o.tail_slots = self.tail_slots
+        o.stripes = self.stripes
         if progress_fn is not None:
             o.progress = progress_fn
             o.progress_rgb = progress_rgb.ctypes.data if progress_rgb is not None else None
@@ -1037,7 +1040,7 @@ class PathTracer:
     def render_with_light_connections_hdr_image(self, world, lights, want64: bool = False) -> HdrImage:
         cam = self.camera.with_direct_lighting_mode(abi.GT_DIRECT_NEXT_EVENT_ESTIMATION)
         return PathTracer(cam, self.options, self.precision, self._ctx, self.profile, self.schedule,
-                          self.tail_slots)._render(
+                          self.tail_slots, self.stripes)._render(
             world, lights, None, want64=want64)
 
     # render_with_environment_hdr_image (renderer.rs:431-449)

@@ -252,7 +252,9 @@ typedef struct gt_render_opts {
     uint32_t tail_slots;    /* GT_SCHEDULE_AUTO: hand over to the persistent kernel once at most
                                this many pixels are unfinished; 0 = as many as one persistent
                                launch keeps resident */
-    uint32_t reserved;
+    uint32_t stripes;       /* wavefront schedules: the frame's rows are dealt to this many
+                               independent wavefronts on their own streams, whose kernels
+                               overlap on the GPU; 0 = 4, at most 8; images do not depend on it */
     /* Optional host buffer of width*height*3 floats.  Before each progress call the library
      * writes the image as far as it is known: finished pixels hold their final value, the
      * others 0 (the partially filled `pixels` of ProgressiveRenderUpdate,
@@ -309,8 +311,10 @@ gt_status gt_camera_default(uint32_t image_width, double aspect_ratio, gt_camera
 gt_status gt_camera_image_size(const gt_camera_desc* camera, uint32_t* width, uint32_t* height,
                                uint32_t* samples_per_pixel);
 
-/* Creates a context on CUDA device `device` with its own stream. */
+/* Creates a context on CUDA device `device` with its own streams. */
 gt_status gt_context_create(int device, gt_context** out);
+/* Destroy every scene, light list, environment and accumulator made on a context before
+ * the context itself. */
 void gt_context_destroy(gt_context* context);
 
 /* Copies a RayScene to the device and builds its BVH on the host with the

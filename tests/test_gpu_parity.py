@@ -527,20 +527,21 @@ def test_persistent_progress_and_cancel(gpu_context):
     assert np.isfinite(img.pixels).all()
 
 
-@pytest.mark.parametrize("schedule,tail,grid,width", [("wavefront", 0, 4, 48), ("auto", 100, 4, 48),
-                                                     ("auto", 1000000, 4, 48), ("auto", 1, 8, 48),
-                                                     ("auto", 1000000, 4, 96)])
-def test_schedules_agree(gpu_context, schedule, tail, grid, width):
+@pytest.mark.parametrize("schedule,tail,grid,width,stripes", [("wavefront", 0, 4, 48, 0), ("auto", 100, 4, 48, 0),
+                                                             ("auto", 1000000, 4, 48, 0), ("auto", 1, 8, 48, 0),
+                                                             ("auto", 1000000, 4, 96, 0), ("wavefront", 0, 4, 50, 1),
+                                                             ("wavefront", 0, 4, 50, 3), ("auto", 1, 8, 50, 8)])
+def test_schedules_agree(gpu_context, schedule, tail, grid, width, stripes):
     # Every schedule evaluates the same per-pixel arithmetic in the same order: bit-identical
     # in f64 (no fused multiply-add anywhere), whether the wavefront runs to the end, hands
     # its last 100 slots to the persistent kernel, hands over at once, or (64 samples per
     # pixel, tail of one slot) first moves its slowest pixels to the concurrent persistent
     # kernel.  At 96x96 the tail starts one slot per lane and hands its last slots to one
-    # warp each mid-path.  In f32 the compiler may fuse differently in the kernels, so
+    # warp each mid-path; 1, 3 (rows not a multiple) and 8 wavefront stripes.  In f32 the compiler may fuse differently in the kernels, so
     # images agree to f32 rounding.
     scene, lights = scenes.cornell_scene()
     cam = scenes.cornell_camera(width, grid, 50)
-    a = PathTracer(cam, precision="f64", context=gpu_context, schedule=schedule, tail_slots=tail)
+    a = PathTracer(cam, precision="f64", context=gpu_context, schedule=schedule, tail_slots=tail, stripes=stripes)
     b = PathTracer(cam, precision="f64", context=gpu_context, schedule="persistent")
     ia = a.render_with_lights_hdr_image(scene, lights, want64=True)
     ib = b.render_with_lights_hdr_image(scene, lights, want64=True)
@@ -552,7 +553,7 @@ def test_schedules_agree(gpu_context, schedule, tail, grid, width):
         assert a.last_stats["migrated_pixels"] > 0
     if schedule == "wavefront":
         assert a.last_stats["migrated_pixels"] == 0 and a.last_stats["tail_pixels"] == 0
-    fa = PathTracer(cam, context=gpu_context, schedule=schedule,
-                    tail_slots=tail).render_with_lights_hdr_image(scene, lights)
+    fa = PathTracer(cam, context=gpu_context, schedule=schedule, tail_slots=tail,
+                    stripes=stripes).render_with_lights_hdr_image(scene, lights)
     fb = PathTracer(cam, context=gpu_context, schedule="persistent").render_with_lights_hdr_image(scene, lights)
     assert _divergent(fa.pixels, fb.pixels.astype(np.float64)) <= 0.05 * fa.pixels.shape[0] * fa.pixels.shape[1]
