@@ -761,7 +761,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     // Per-stripe launch sizes: a stripe owns about 1/K of the GPU.
     int tail_per_sm = 0, coop_per_sm = 0;
     GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tail_per_sm, k_persistent<R, true>, 128, 0));
-    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&coop_per_sm, k_persistent<R, true, false, true>, 128, 0));
+    coop_per_sm = tail_per_sm; // the cooperative mode is the same kernel
     const uint32_t full_persist = uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1));
     const uint32_t full_coop = uint32_t(sms) * uint32_t(std::max(coop_per_sm, 1));
     const uint32_t lblocks = std::max<uint32_t>(1u, std::min<uint32_t>((qcap + threads - 1) / threads, uint32_t(sms) * 8));
@@ -869,9 +869,11 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         k_persistent<R, true><<<side_blocks, 128, 0, S[k].side>>>(Q, Q.ps.counters + C_MIGRATE_NEXT, Q.ps.q_migrate,
                                                                    Q.ps.counters + C_MIGRATED, ctx->mapped_dev,
                                                                    nullptr, nullptr, nullptr, nullptr, ho);
-        k_persistent<R, true, false, true><<<side_coop_blocks, 128, 0, S[k].side>>>(
+        HandOff coop;
+        coop.coop = 1;
+        k_persistent<R, true><<<side_coop_blocks, 128, 0, S[k].side>>>(
             Q, Q.ps.counters + C_SIDE_COOP_NEXT, Q.ps.q_handoff, Q.ps.counters + C_SIDE_COOP, ctx->mapped_dev, nullptr,
-            nullptr, nullptr, nullptr);
+            nullptr, nullptr, nullptr, coop);
         GT_CUDA(cudaGetLastError());
         klaunch[GT_KERNEL_PERSISTENT] += 2;
         GT_CUDA(cudaEventRecord(S[k].join, S[k].side));
@@ -901,9 +903,11 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         ho.count = Q.ps.counters + C_TAIL_COOP;
         k_persistent<R, true><<<tblocks, 128, 0, s>>>(Q, d_next + k, list, count, nullptr, nullptr, nullptr, nullptr,
                                                       nullptr, ho);
-        k_persistent<R, true, false, true><<<coop_blocks, 128, 0, s>>>(
+        HandOff coop;
+        coop.coop = 1;
+        k_persistent<R, true><<<coop_blocks, 128, 0, s>>>(
             Q, Q.ps.counters + C_TAIL_COOP_NEXT, Q.ps.q_trace[1], Q.ps.counters + C_TAIL_COOP, nullptr, nullptr, nullptr,
-            nullptr, nullptr);
+            nullptr, nullptr, coop);
         GT_CUDA(cudaGetLastError());
         klaunch[GT_KERNEL_OTHER] += 1;
         klaunch[GT_KERNEL_PERSISTENT] += 2;

@@ -565,21 +565,25 @@ template <class R> __global__ void __launch_bounds__(256) k_classify(Params<R> P
 // are still running (class_counts[0] entries), each thread picks up a slot's saved state
 // (its path mid-flight, or a finished sample waiting to be folded in) and, when the
 // slot's pixel is done, stores the pixel sums back for k_resolve.
-// Hand-over of a resume-mode k_persistent launch to a cooperative one (COOP: one warp per
-// slot) once few slots are left; all zero = never.
+// Hand-over of a resume-mode k_persistent launch to a cooperative one (one warp per slot)
+// once few slots are left; all zero = never.  `coop` makes the launch itself cooperative.
+// Both modes run the same compiled code, so a slot's arithmetic does not depend on which
+// mode finishes it.
 struct HandOff {
     uint32_t* done = nullptr;  // slots this launch has finished
     uint32_t below = 0;        // hand over once (slots - done) <= below
     uint32_t* list = nullptr;  // slots handed over
     uint32_t* count = nullptr; // their number
+    uint32_t coop = 0;         // 1 = one slot per warp (RESUME launches only)
 };
 
-template <class R, bool RESUME, bool BATCH = false, bool COOP = false>
+template <class R, bool RESUME, bool BATCH = false>
 __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next, const uint32_t* queues,
                                                     const uint32_t* class_counts, const volatile uint32_t* cancel,
                                                     volatile uint32_t* progress, float* rgb, double* rgb64,
                                                     uint32_t* accepted, HandOff ho = HandOff()) {
     const uint32_t n = RESUME ? class_counts[0] : (BATCH ? P.frame_start[P.num_frames] : P.cam.width * P.cam.height);
+    const bool coop = RESUME && ho.coop != 0; // warp-uniform
     // The camera of the pixel being rendered: the frame's in a batch, else the launch's.
     uint32_t frame = 0, local = 0;
     auto cam = [&]() -> const CamDev<R>& {
@@ -610,7 +614,7 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
     auto fetch = [&]() -> uint32_t {
         if (cancel && *cancel) return n;
         uint32_t i;
-        if constexpr (COOP) { // one slot per warp: every lane follows the same path
+        if (coop) { // one slot per warp: every lane follows the same path
             uint32_t v = 0;
             if (lane_id() == 0) v = atomicAdd(next, 1u);
             i = __shfl_sync(0xffffffffu, v, 0);
@@ -689,7 +693,7 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
     // of drifting apart into sub-warps at different instructions.
     uint32_t iter = 0;
     while (__any_sync(0xffffffffu, alive)) {
-        if constexpr (RESUME && !COOP) {
+        if (RESUME && !coop) {
             // Hand-over: once no more slots are left than the cooperative launch has warps,
             // lanes between samples or bounces save their slot, list it (with every slot not
             // yet taken) and stop; a slot then runs on a warp of its own, where it is not
@@ -730,7 +734,7 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
                 // The pixel is finished: write it (or hand its sums back to the
                 // wavefront's resolve) and take the next one.
                 if (RESUME) {
-                    if (!COOP || lane_id() == 0) {
+                    if (!coop || lane_id() == 0) {
                         P.ps.acc[pix] = a;
                         P.ps.comp[pix] = c;
                         P.ps.accepted[pix] = acc_n;
@@ -812,7 +816,7 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
     // Throughput totals: warp-reduce, one atomic per warp (every lane of the launch's
     // full warps arrives here); a cooperative warp counted its one path in every lane.
     __syncwarp();
-    for (int off = 16; off > 0 && !COOP; off >>= 1) {
+    for (int off = 16; off > 0 && !coop; off >>= 1) {
         n_rays += __shfl_down_sync(0xffffffffu, n_rays, off);
         n_shadow += __shfl_down_sync(0xffffffffu, n_shadow, off);
         n_acc += __shfl_down_sync(0xffffffffu, n_acc, off);
