@@ -263,6 +263,8 @@ void gt_context_destroy(gt_context* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
+    for (auto& g : ctx->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     cudaFree(ctx->ws);
     cudaFreeHost(ctx->pinned);
     cudaFreeHost(const_cast<uint32_t*>(ctx->mapped));

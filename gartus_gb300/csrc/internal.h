@@ -65,6 +65,13 @@ struct gt_context {
     static constexpr int kMaxStripes = 8;
     cudaStream_t stripe_stream[kMaxStripes] = {};
     cudaStream_t stripe_side[kMaxStripes] = {};
+    // Each stripe's instantiated two-iteration graph, reused while its kernel parameters
+    // (scene, camera, workspace, launch sizes) stay the same from one render to the next.
+    struct CachedGraph {
+        std::vector<unsigned char> key;
+        cudaGraphExec_t exec = nullptr;
+    };
+    CachedGraph graphs[kMaxStripes];
     std::mutex mu;
     void* ws = nullptr; // render workspace (path state, queues, staging)
     size_t ws_bytes = 0;

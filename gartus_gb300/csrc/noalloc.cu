@@ -16,7 +16,9 @@ namespace gt {
 namespace {
 
 constexpr uint32_t kNoAllocMaxPixels = GT_NOALLOC_MAX_PIXELS;
-constexpr size_t kHeaderBytes = 512; // counters (64 B), totals (32 B), pixel counter (4 B)
+// Header: counters at 0 (C_COUNT words), totals at 128 (8 x 8 B), pixel counter at 192.
+constexpr size_t kHeaderBytes = 512;
+static_assert(C_COUNT * sizeof(uint32_t) <= 128, "counters overlap the totals in the scratch header");
 constexpr size_t kScratchBytes = kHeaderBytes + size_t(kNoAllocMaxPixels) * NUM_COST_CLASSES * sizeof(uint32_t);
 
 // The shared scratch.  Host code must not use this name as an address: on the host it

@@ -814,10 +814,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         }
         return cudaGetLastError();
     };
-    auto cleanup = [&]() {
-        for (auto& x : S)
-            if (x.exec) cudaGraphExecDestroy(x.exec);
-    };
+    auto cleanup = [&]() {}; // the graphs stay cached in the context
     cudaEvent_t init_done = nullptr;
     GT_CUDA(ev.get(init_done));
     GT_CUDA(cudaEventRecord(init_done, st));
@@ -826,6 +823,20 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         S[k].side = ctx->stripe_side[k];
         GT_CUDA(cudaStreamWaitEvent(S[k].st, init_done, 0));
         if (!profile) {
+            // Reuse the stripe's graph from the previous render when nothing it captured
+            // changed: its key is the stripe's kernel parameters and launch sizes.
+            std::vector<unsigned char> key(sizeof(Params<R>) + 4 * sizeof(uint32_t));
+            std::memcpy(key.data(), &SP[k], sizeof(Params<R>));
+            const uint32_t extra[4] = {lblocks, wblocks, uint32_t(kernels_per_iteration), uint32_t(sizeof(R))};
+            std::memcpy(key.data() + sizeof(Params<R>), extra, sizeof(extra));
+            gt_context::CachedGraph& cg = ctx->graphs[k];
+            if (cg.exec && cg.key == key) {
+                S[k].exec = cg.exec;
+                continue;
+            }
+            if (cg.exec) cudaGraphExecDestroy(cg.exec);
+            cg.exec = nullptr;
+            cg.key.clear();
             cudaGraph_t graph = nullptr;
             GT_CUDA(cudaStreamBeginCapture(S[k].st, cudaStreamCaptureModeThreadLocal));
             cudaError_t le = launch_iteration(k, 0, false);
@@ -839,9 +850,11 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             ce = cudaGraphInstantiate(&S[k].exec, graph, 0);
             cudaGraphDestroy(graph);
             if (ce != cudaSuccess) {
-                cleanup();
+                S[k].exec = nullptr;
                 return cuda_fail(ce, "cudaGraphInstantiate");
             }
+            cg.exec = S[k].exec;
+            cg.key = std::move(key);
         }
     }
 
