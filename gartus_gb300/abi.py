@@ -239,7 +239,20 @@ class gt_bvh_stats(C.Structure):
         return {name: int(getattr(self, name)) for name, _ in self._fields_}
 
 
+class gt_denoise_input(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32),
+        ("width", C.c_uint32),
+        ("height", C.c_uint32),
+        ("device_buffers", C.c_uint32),
+        ("beauty", C.c_void_p),
+        ("beauty_half", C.c_void_p),
+        ("albedo", C.c_void_p),
+        ("normal", C.c_void_p),
+    ]
+
+
 STRUCTS = [
     gt_geometry, gt_primitive, gt_material, gt_scene_desc, gt_light_target, gt_environment_desc,
-    gt_camera_desc, gt_render_opts, gt_frame, gt_frame_job, gt_bvh_stats, gt_render_stats,
+    gt_camera_desc, gt_render_opts, gt_frame, gt_frame_job, gt_bvh_stats, gt_render_stats, gt_denoise_input,
 ]

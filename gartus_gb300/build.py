@@ -31,6 +31,7 @@ UNITS = [
     ("render_f32.cu", ["-fmad=true"]),
     ("render_f64.cu", ["-fmad=false"]),
     ("noalloc.cu", ["-fmad=true"]),
+    ("denoise.cu", ["-fmad=true"]),
 ]
 CXX_UNITS = ["bvh_build.cpp", "scene_tables.cpp"]
 

@@ -156,16 +156,6 @@ gt_status cuda_fail(cudaError_t e, const char* what) {
 
 using namespace gt;
 
-#define GT_GUARD_BEGIN try {
-#define GT_GUARD_END                                                  \
-    }                                                                 \
-    catch (const std::bad_alloc&) {                                   \
-        return fail(GT_ERR_OOM, "host allocation failed");            \
-    }                                                                 \
-    catch (const std::exception& ex) {                                \
-        return fail(GT_ERR_INTERNAL, ex.what());                      \
-    }
-
 extern "C" {
 
 uint32_t gt_abi_version(void) { return GT_ABI_VERSION; }

@@ -1,0 +1,410 @@
+// denoise_kernels.cuh — kernels of the learned denoiser: a 5-level U-Net of 3x3 convs over
+// the beauty / albedo / normal AOVs (render_denoising_aovs, renderer.rs:121-129).
+//
+// Tensors are NHWC.  Activations and weights are BF16; every product is accumulated in FP32
+// by the tensor cores (mma.sync m16n8k16, BF16 inputs, FP32 accumulators).  A 3x3 conv is an
+// implicit GEMM: M = pixels, N = output channels, K = 9 taps x input channels.  Its input
+// gradient is the same GEMM with the taps flipped and the channel roles swapped; its weight
+// gradient is a GEMM over pixels (M = output channels, N = input channels, K = pixels).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gt {
+namespace dn {
+
+constexpr int kTile = 64;    // pixels per conv block (4 warps x 16)
+constexpr int kNChunk = 96;  // output channels per conv block (12 n8 tiles)
+
+__device__ __forceinline__ uint32_t lane() { return threadIdx.x & 31u; }
+
+__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+    return uint32_t(__bfloat16_as_ushort(lo)) | (uint32_t(__bfloat16_as_ushort(hi)) << 16);
+}
+
+// D += A (16x16, row) * B (16x8, col), BF16 in, FP32 accumulate.
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// Two consecutive BF16 channels (c even) of pixel (n, y, x), 0 outside the image.
+__device__ __forceinline__ uint32_t ld2(const __nv_bfloat16* t, int c_stride, int n, int y, int x, int h, int w,
+                                        int c) {
+    if (y < 0 || y >= h || x < 0 || x >= w) return 0u;
+    return __ldg(reinterpret_cast<const unsigned int*>(t + ((size_t(n) * h + y) * w + x) * c_stride + c));
+}
+
+struct ConvFwd {
+    const __nv_bfloat16* x;  // [n][h][w][cin]
+    int cin;                 // multiple of 16
+    const __nv_bfloat16* wt; // [cout_p][9][cin]
+    const float* bias;       // [cout] or null
+    int cout_p;              // multiple of 8 (rows of wt)
+    int cout;                // channels stored
+    __nv_bfloat16* y;        // [n][h][w][ldy] at channel offset yoff, or null
+    int ldy, yoff;
+    float* yf;               // [n][h][w][cout] FP32 output, or null
+    const float* res;        // FP32 residual added to yf ([n][h][w][cout]), or null
+    int relu;
+    int n, h, w;
+};
+
+// One block: 64 consecutive pixels of one image row x up to 96 output channels.
+__global__ void __launch_bounds__(128) k_conv_fwd(ConvFwd a) {
+    const int segs = (a.w + kTile - 1) / kTile;
+    const int seg = blockIdx.x % segs, row = blockIdx.x / segs;
+    const int y = row % a.h, n = row / a.h;
+    const int warp = threadIdx.x >> 5, g = lane() >> 2, t = lane() & 3;
+    const int x0 = seg * kTile + warp * 16;
+    const int co0 = blockIdx.y * kNChunk;
+    const int ntiles = min(kNChunk, a.cout_p - co0) / 8;
+    float acc[12][4];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    for (int tap = 0; tap < 9; ++tap) {
+        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+        for (int c0 = 0; c0 < a.cin; c0 += 16) {
+            uint32_t fa[4];
+            fa[0] = ld2(a.x, a.cin, n, y + dy, x0 + g + dx, a.h, a.w, c0 + 2 * t);
+            fa[1] = ld2(a.x, a.cin, n, y + dy, x0 + g + 8 + dx, a.h, a.w, c0 + 2 * t);
+            fa[2] = ld2(a.x, a.cin, n, y + dy, x0 + g + dx, a.h, a.w, c0 + 2 * t + 8);
+            fa[3] = ld2(a.x, a.cin, n, y + dy, x0 + g + 8 + dx, a.h, a.w, c0 + 2 * t + 8);
+#pragma unroll
+            for (int j = 0; j < 12; ++j) {
+                if (j >= ntiles) break;
+                const __nv_bfloat16* wr = a.wt + (size_t(co0 + j * 8 + g) * 9 + tap) * a.cin + c0 + 2 * t;
+                uint32_t fb[2];
+                fb[0] = __ldg(reinterpret_cast<const unsigned int*>(wr));
+                fb[1] = __ldg(reinterpret_cast<const unsigned int*>(wr + 8));
+                mma_bf16(acc[j], fa, fb);
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 12; ++j) {
+        if (j >= ntiles) break;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int x = x0 + g + 8 * half;
+            if (x >= a.w) continue;
+            const size_t p = (size_t(n) * a.h + y) * a.w + x;
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int co = co0 + j * 8 + 2 * t + e;
+                if (co >= a.cout) continue;
+                float v = acc[j][2 * half + e] + (a.bias ? a.bias[co] : 0.f);
+                if (a.relu) v = fmaxf(v, 0.f);
+                if (a.y) a.y[p * a.ldy + a.yoff + co] = __float2bfloat16(v);
+                if (a.yf) a.yf[p * a.cout + co] = v + (a.res ? a.res[p * a.cout + co] : 0.f);
+            }
+        }
+    }
+}
+
+// dW[co][tap][ci] += sum_p dY[p][co] * X[p + tap][ci]; one block per (tap, pixel range).
+// 8 warps share the (16-channel co tile, 8-channel ci tile) pairs; 16 pixels at a time are
+// staged in shared memory.
+struct ConvWgrad {
+    const __nv_bfloat16* dy; // [P][cout]
+    int cout;                // multiple of 16 (rows of dw)
+    const __nv_bfloat16* x;  // [P][cin]
+    int cin;                 // multiple of 16
+    float* dw;               // [cout][9][cin] (accumulated)
+    int n, h, w;
+};
+constexpr int kMaxCo = 96, kMaxCi = 176;
+__global__ void __launch_bounds__(256) k_conv_wgrad(ConvWgrad a) {
+    __shared__ __nv_bfloat16 sdy[16][kMaxCo + 8];
+    __shared__ __nv_bfloat16 sx[16][kMaxCi + 8];
+    const int tap = blockIdx.y, dy = tap / 3 - 1, dx = tap % 3 - 1;
+    const int warp = threadIdx.x >> 5, g = lane() >> 2, t = lane() & 3;
+    const int mt = a.cout / 16, nt = a.cin / 8, tiles = mt * nt;
+    // this warp's tiles: warp, warp + 8, ... (at most ceil(6 * 22 / 8) = 17)
+    constexpr int kMaxT = 17;
+    float acc[kMaxT][4];
+#pragma unroll
+    for (int j = 0; j < kMaxT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    const long long P = (long long)a.n * a.h * a.w;
+    for (long long p0 = (long long)blockIdx.x * 16; p0 < P; p0 += (long long)gridDim.x * 16) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < 16 * (a.cout / 2); i += blockDim.x) {
+            const int r = i / (a.cout / 2), c = (i % (a.cout / 2)) * 2;
+            const long long p = p0 + r;
+            uint32_t v = 0;
+            if (p < P) v = __ldg(reinterpret_cast<const unsigned int*>(a.dy + size_t(p) * a.cout + c));
+            *reinterpret_cast<uint32_t*>(&sdy[r][c]) = v;
+        }
+        for (int i = threadIdx.x; i < 16 * (a.cin / 2); i += blockDim.x) {
+            const int r = i / (a.cin / 2), c = (i % (a.cin / 2)) * 2;
+            const long long p = p0 + r;
+            uint32_t v = 0;
+            if (p < P) {
+                const int x = int(p % a.w), yy = int((p / a.w) % a.h), nn = int(p / ((long long)a.w * a.h));
+                v = ld2(a.x, a.cin, nn, yy + dy, x + dx, a.h, a.w, c);
+            }
+            *reinterpret_cast<uint32_t*>(&sx[r][c]) = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kMaxT; ++j) {
+            const int tile = warp + 8 * j;
+            if (tile >= tiles) break;
+            const int co0 = (tile / nt) * 16, ci0 = (tile % nt) * 8;
+            uint32_t fa[4], fb[2];
+            fa[0] = pack_bf16(sdy[2 * t][co0 + g], sdy[2 * t + 1][co0 + g]);
+            fa[1] = pack_bf16(sdy[2 * t][co0 + g + 8], sdy[2 * t + 1][co0 + g + 8]);
+            fa[2] = pack_bf16(sdy[2 * t + 8][co0 + g], sdy[2 * t + 9][co0 + g]);
+            fa[3] = pack_bf16(sdy[2 * t + 8][co0 + g + 8], sdy[2 * t + 9][co0 + g + 8]);
+            fb[0] = pack_bf16(sx[2 * t][ci0 + g], sx[2 * t + 1][ci0 + g]);
+            fb[1] = pack_bf16(sx[2 * t + 8][ci0 + g], sx[2 * t + 9][ci0 + g]);
+            mma_bf16(acc[j], fa, fb);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < kMaxT; ++j) {
+        const int tile = warp + 8 * j;
+        if (tile >= tiles) break;
+        const int co0 = (tile / nt) * 16, ci0 = (tile % nt) * 8;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int co = co0 + g + (e >= 2 ? 8 : 0), ci = ci0 + 2 * t + (e & 1);
+            atomicAdd(&a.dw[(size_t(co) * 9 + tap) * a.cin + ci], acc[j][e]);
+        }
+    }
+}
+
+// db[c] += sum_p dY[p][c] for the first `count` of `stride` channels (FP32 partial sums per
+// block, then atomics).
+__global__ void k_bias_grad(const __nv_bfloat16* dy, int stride, int count, long long P, float* db) {
+    for (int ch = threadIdx.x; ch < count; ch += blockDim.x) {
+        float s = 0.f;
+        for (long long p = blockIdx.x; p < P; p += gridDim.x) s += __bfloat162float(dy[size_t(p) * stride + ch]);
+        atomicAdd(&db[ch], s);
+    }
+}
+
+// g = g * (y > 0) elementwise (the output y was ReLU'd).
+__global__ void k_relu_bwd(__nv_bfloat16* g, const __nv_bfloat16* y, long long count) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+        if (!(__bfloat162float(y[i]) > 0.f)) g[i] = __float2bfloat16(0.f);
+}
+
+// 2x2 average pool: [n][h][w][c] -> [n][h/2][w/2][c].
+__global__ void k_pool(const __nv_bfloat16* x, __nv_bfloat16* y, int n, int h, int w, int c) {
+    const long long count = (long long)n * (h / 2) * (w / 2) * c;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+        const int ch = int(i % c);
+        const long long q = i / c;
+        const int xo = int(q % (w / 2)), yo = int((q / (w / 2)) % (h / 2)), nn = int(q / ((long long)(w / 2) * (h / 2)));
+        float s = 0.f;
+        for (int k = 0; k < 4; ++k)
+            s += __bfloat162float(x[((size_t(nn) * h + 2 * yo + (k >> 1)) * w + 2 * xo + (k & 1)) * c + ch]);
+        y[i] = __float2bfloat16(0.25f * s);
+    }
+}
+
+// Backward of the pool, added into dx: dx[2y+i][2x+j] += dy[y][x] / 4.
+__global__ void k_pool_bwd(const __nv_bfloat16* dy, __nv_bfloat16* dx, int n, int h, int w, int c) {
+    const long long count = (long long)n * h * w * c;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+        const int ch = int(i % c);
+        const long long q = i / c;
+        const int x = int(q % w), y = int((q / w) % h), nn = int(q / ((long long)w * h));
+        const float g = __bfloat162float(dy[((size_t(nn) * (h / 2) + y / 2) * (w / 2) + x / 2) * c + ch]);
+        dx[i] = __float2bfloat16(__bfloat162float(dx[i]) + 0.25f * g);
+    }
+}
+
+// Concatenate the 2x nearest upsampling of `lo` ([n][h/2][w/2][cl]) with `skip` ([n][h][w][cs])
+// into y ([n][h][w][cl + cs]).
+__global__ void k_upcat(const __nv_bfloat16* lo, int cl, const __nv_bfloat16* skip, int cs, __nv_bfloat16* y, int n,
+                        int h, int w) {
+    const int c = cl + cs;
+    const long long count = (long long)n * h * w * c;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+        const int ch = int(i % c);
+        const long long p = i / c;
+        const int x = int(p % w), yy = int((p / w) % h), nn = int(p / ((long long)w * h));
+        y[i] = ch < cl ? lo[((size_t(nn) * (h / 2) + yy / 2) * (w / 2) + x / 2) * cl + ch] : skip[size_t(p) * cs + ch - cl];
+    }
+}
+
+// Backward of k_upcat: dlo[y][x] = sum of the four upsampled gradients; dskip = its slice.
+__global__ void k_upcat_bwd(const __nv_bfloat16* dy, int cl, int cs, __nv_bfloat16* dlo, __nv_bfloat16* dskip, int n,
+                            int h, int w) {
+    const int c = cl + cs;
+    const long long lo_count = (long long)n * (h / 2) * (w / 2) * cl;
+    const long long sk_count = (long long)n * h * w * cs;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < lo_count + sk_count;
+         i += (long long)gridDim.x * blockDim.x) {
+        if (i < lo_count) {
+            const int ch = int(i % cl);
+            const long long q = i / cl;
+            const int x = int(q % (w / 2)), yy = int((q / (w / 2)) % (h / 2)), nn = int(q / ((long long)(w / 2) * (h / 2)));
+            float s = 0.f;
+            for (int k = 0; k < 4; ++k)
+                s += __bfloat162float(dy[((size_t(nn) * h + 2 * yy + (k >> 1)) * w + 2 * x + (k & 1)) * c + ch]);
+            dlo[i] = __float2bfloat16(s);
+        } else {
+            const long long j = i - lo_count;
+            const int ch = int(j % cs);
+            const long long p = j / cs;
+            dskip[j] = dy[size_t(p) * c + cl + ch];
+        }
+    }
+}
+
+// Network input: log(1 + beauty), albedo, normal (9 channels) into 16 BF16 channels, and
+// log(1 + beauty) in FP32 for the residual output.  Sources are [n][h][w][3]; the network's
+// images are [n][hp][wp] (hp >= h, wp >= w), the extra rows and columns repeating the last
+// ones.
+__global__ void k_pack_input(const float* beauty, const float* albedo, const float* normal, int n, int h, int w,
+                             int hp, int wp, __nv_bfloat16* x, float* lb) {
+    const long long P = (long long)n * hp * wp;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
+        const int xx = min(int(p % wp), w - 1), yy = min(int((p / wp) % hp), h - 1);
+        const long long nn = p / ((long long)wp * hp);
+        const size_t s = ((size_t(nn) * h + yy) * w + xx) * 3;
+        __nv_bfloat16* o = x + size_t(p) * 16;
+        for (int k = 0; k < 3; ++k) {
+            const float b = beauty[s + k];
+            const float l = log1pf(isfinite(b) ? fmaxf(b, 0.f) : 0.f);
+            lb[p * 3 + k] = l;
+            o[k] = __float2bfloat16(l);
+            o[3 + k] = __float2bfloat16(albedo ? albedo[s + k] : 0.f);
+            o[6 + k] = __float2bfloat16(normal ? normal[s + k] : 0.f);
+        }
+        for (int k = 9; k < 16; ++k) o[k] = __float2bfloat16(0.f);
+    }
+}
+
+// Loss: mean |out - log(1 + target)| over P x 3 values; its gradient into 16 BF16 channels.
+__global__ void k_l1_log1p(const float* out, const float* target, long long P, float* loss, __nv_bfloat16* g) {
+    const float inv = 1.f / float(P * 3);
+    float s = 0.f;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
+        for (int k = 0; k < 3; ++k) {
+            const float tv = target[p * 3 + k];
+            const float d = out[p * 3 + k] - log1pf(isfinite(tv) ? fmaxf(tv, 0.f) : 0.f);
+            s += fabsf(d);
+            g[size_t(p) * 16 + k] = __float2bfloat16(d > 0.f ? inv : (d < 0.f ? -inv : 0.f));
+        }
+        for (int k = 3; k < 16; ++k) g[size_t(p) * 16 + k] = __float2bfloat16(0.f);
+    }
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, s * inv);
+}
+
+// Adam on the FP32 master parameters (Kingma & Ba 2015).
+__global__ void k_adam(float* p, float* m, float* v, const float* g, long long count, float lr, float b1, float b2,
+                       float eps, float c1, float c2) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    }
+}
+
+// Master weights W[co][9][cin] (FP32) -> forward BF16 [cout_p][9][cin_p] and the flipped,
+// transposed input-gradient weights [cin_p][9][cout_pp]: Wf[ci][t][co] = W[co][8 - t][ci].
+__global__ void k_weights_bf16(const float* w, int cout, int cin, __nv_bfloat16* wb, int cout_p, int cin_p,
+                               __nv_bfloat16* wf, int cout_pp) {
+    const long long nb = (long long)cout_p * 9 * cin_p, nf = (long long)cin_p * 9 * cout_pp;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nb + nf; i += (long long)gridDim.x * blockDim.x) {
+        if (i < nb) {
+            const int ci = int(i % cin_p), tap = int((i / cin_p) % 9), co = int(i / (9LL * cin_p));
+            wb[i] = __float2bfloat16(co < cout && ci < cin ? w[(size_t(co) * 9 + tap) * cin + ci] : 0.f);
+        } else {
+            const long long j = i - nb;
+            const int co = int(j % cout_pp), tap = int((j / cout_pp) % 9), ci = int(j / (9LL * cout_pp));
+            wf[j] = __float2bfloat16(co < cout && ci < cin ? w[(size_t(co) * 9 + (8 - tap)) * cin + ci] : 0.f);
+        }
+    }
+}
+
+// Padded weight gradients -> flat gradient vector; the bias gradients are read in place.
+__global__ void k_gather_grad(const float* dwp, int cout, int cin, int cin_p, const float* dbp, float* g) {
+    const long long nw = (long long)cout * 9 * cin;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nw + cout; i += (long long)gridDim.x * blockDim.x) {
+        if (i < nw) {
+            const int ci = int(i % cin), tap = int((i / cin) % 9), co = int(i / (9LL * cin));
+            g[i] = dwp[(size_t(co) * 9 + tap) * cin_p + ci];
+        } else {
+            g[i] = dbp[i - nw];
+        }
+    }
+}
+
+// Output: exp(out) - 1, clamped at 0, cropped from [hp][wp][3] to [h][w][3].
+__global__ void k_unpack_output(const float* out, int h, int w, int wp, float* rgb) {
+    const long long count = (long long)h * w * 3;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+        const int k = int(i % 3);
+        const long long q = i / 3;
+        const int xx = int(q % w), yy = int(q / w);
+        rgb[i] = fmaxf(expm1f(out[(size_t(yy) * wp + xx) * 3 + k]), 0.f);
+    }
+}
+
+// Split-buffer residual test, one block per tile: keeps the denoised tile unless
+// mean((d - p)^2 / (p^2 + 0.01)) > threshold * mean((a - p)^2 / (p^2 + 0.01)), where p is the
+// render, a the mean of its first half of samples and d the denoised image; a tile that
+// fails keeps p.  flags[tile] = 1 and *count += 1 for each tile that falls back.
+__global__ void __launch_bounds__(256) k_tile_fallback(const float* d, const float* p, const float* a, int h, int w,
+                                                        int tile, float threshold, float* out, uint8_t* flags,
+                                                        uint32_t* count) {
+    __shared__ float sr[8], sn[8];
+    __shared__ int keep_plain;
+    const int tiles_x = (w + tile - 1) / tile;
+    const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+    const int x0 = tx * tile, y0 = ty * tile;
+    const int tw = min(tile, w - x0), th = min(tile, h - y0);
+    float r = 0.f, nz = 0.f;
+    for (int i = threadIdx.x; i < tw * th * 3; i += blockDim.x) {
+        const int k = i % 3, q = i / 3;
+        const size_t o = ((size_t(y0 + q / tw)) * w + x0 + q % tw) * 3 + k;
+        const float pv = isfinite(p[o]) ? p[o] : 0.f;
+        const float den = pv * pv + 0.01f;
+        const float dd = d[o] - pv, da = (isfinite(a[o]) ? a[o] : 0.f) - pv;
+        r += dd * dd / den;
+        nz += da * da / den;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        r += __shfl_down_sync(0xffffffffu, r, off);
+        nz += __shfl_down_sync(0xffffffffu, nz, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sr[threadIdx.x >> 5] = r;
+        sn[threadIdx.x >> 5] = nz;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float rs = 0.f, ns = 0.f;
+        for (int i = 0; i < int(blockDim.x >> 5); ++i) {
+            rs += sr[i];
+            ns += sn[i];
+        }
+        keep_plain = rs > threshold * ns ? 1 : 0;
+        flags[blockIdx.x] = uint8_t(keep_plain);
+        if (keep_plain) atomicAdd(count, 1u);
+    }
+    __syncthreads();
+    const float* src = keep_plain ? p : d;
+    for (int i = threadIdx.x; i < tw * th * 3; i += blockDim.x) {
+        const int k = i % 3, q = i / 3;
+        const size_t o = ((size_t(y0 + q / tw)) * w + x0 + q % tw) * 3 + k;
+        out[o] = src[o];
+    }
+}
+
+} // namespace dn
+} // namespace gt

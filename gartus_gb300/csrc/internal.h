@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -54,6 +56,18 @@ gt_status fail(gt_status status, const std::string& msg);
 gt_status cuda_fail(cudaError_t e, const char* what);
 
 } // namespace gt
+
+// Every extern "C" entry point runs its body inside these, so no C++ exception crosses the C ABI.
+#define GT_GUARD_BEGIN try {
+#define GT_GUARD_END                                                  \
+    }                                                                 \
+    catch (const std::bad_alloc&) {                                   \
+        return gt::fail(GT_ERR_OOM, "host allocation failed");        \
+    }                                                                 \
+    catch (const std::exception& ex) {                                \
+        return gt::fail(GT_ERR_INTERNAL, ex.what());                  \
+    }
+
 
 struct gt_context {
     int device = 0;

@@ -413,6 +413,69 @@ gt_status gt_trace_rays(gt_scene* scene, const double* rays, uint32_t count, dou
 gt_status gt_trace_primary(gt_scene* scene, const gt_camera_desc* camera, uint32_t stride,
                            int32_t* prim_ids, double* t, gt_bvh_stats* stats);
 
+/* ---------------------------------------------------------------- denoiser */
+
+/* A learned denoiser over the AOVs of PathTracer::render_denoising_aovs
+ * (renderer.rs:121-129; DenoisingAovs, camera.rs:491-526).  No reference counterpart: the
+ * reference produces the AOVs and stops there.  The network is a 5-level U-Net of 3x3
+ * convolutions (32/48/64/80/96 channels, ReLU, 2x2 average pooling, nearest upsampling
+ * concatenated with the skip) from log(1 + beauty), albedo and normal to log(1 + radiance),
+ * predicted as a residual over log(1 + beauty).  Weights and activations are BF16 with FP32
+ * accumulation on the tensor cores; training keeps FP32 master weights and uses Adam on an
+ * L1 loss in log(1 + x).
+ *
+ * Flat parameter layout (FP32), layer by layer: weights [cout][3][3][cin] then bias [cout].
+ * Layers: enc0a 9->32, enc0b 32->32, then per level l = 1..4 enc(l)a c(l-1)->c(l), enc(l)b
+ * c(l)->c(l); per level l = 3..0 dec(l)a c(l+1)+c(l)->c(l) (upsampled input first, then the
+ * skip), dec(l)b c(l)->c(l); out 32->3 (no ReLU). */
+typedef struct gt_denoiser gt_denoiser;
+
+/* A network with seeded He-normal weights (the output layer scaled by 0.1) and zero biases. */
+gt_status gt_denoiser_create(gt_context* ctx, uint64_t seed, gt_denoiser** out);
+void gt_denoiser_destroy(gt_denoiser* denoiser);
+gt_status gt_denoiser_param_count(const gt_denoiser* denoiser, uint64_t* count);
+/* Copies the FP32 parameters to / from host memory (`count` must equal the network's).
+ * Setting them resets the optimiser state. */
+gt_status gt_denoiser_get_params(const gt_denoiser* denoiser, float* host, uint64_t count);
+gt_status gt_denoiser_set_params(gt_denoiser* denoiser, const float* host, uint64_t count);
+
+/* One training step on a batch of n images of h x w pixels (h, w multiples of 16).  All
+ * image pointers are DEVICE memory, [n][h][w][3] floats: beauty (a low-sample render),
+ * albedo and normal (may be NULL: zeros), target (a high-sample render).  Runs the forward
+ * pass, the mean L1 loss on log(1 + max(x, 0)), the backward pass and, when lr > 0, one
+ * Adam step (beta 0.9 / 0.999, eps 1e-8).  *loss (optional) receives the loss before the
+ * step; grad (optional, host, param_count floats) the gradient in the flat layout. */
+gt_status gt_denoiser_train_step(gt_denoiser* denoiser, const float* beauty, const float* albedo,
+                                 const float* normal, const float* target, uint32_t n, uint32_t h,
+                                 uint32_t w, float lr, float* loss, float* grad);
+
+/* One frame to denoise.  Images are [height][width][3] floats, in host memory
+ * (device_buffers = 0) or device memory (1). */
+typedef struct gt_denoise_input {
+    uint32_t struct_size;
+    uint32_t width;
+    uint32_t height;
+    uint32_t device_buffers;
+    const float* beauty;      /* the render: mean of all its samples (required)                  */
+    const float* beauty_half; /* optional: mean of the first half of the same samples (the split
+                                 buffer); enables the per-tile fallback                          */
+    const float* albedo;      /* optional (zeros) */
+    const float* normal;      /* optional (zeros) */
+} gt_denoise_input;
+
+/* Denoises one frame into `out` (same memory kind and shape as the beauty image).
+ *
+ * Per-tile fallback (split-buffer residual test): with beauty_half given, the frame's
+ * samples split into two halves A = beauty_half and B = 2 * beauty - A.  For each tile of
+ * tile x tile pixels (0 = 16), with d = denoised and p = beauty,
+ *     residual = mean((d - p)^2 / (p^2 + 0.01)),  noise = mean((A - p)^2 / (p^2 + 0.01)),
+ * noise estimating p's own relative error.  When residual > threshold * noise (0 = 2.0:
+ * the denoiser's error exceeds p's noise) the tile keeps the plain render p.
+ * tile_fallback (optional, host, ceil(h/tile) * ceil(w/tile) bytes, row-major) receives 1
+ * for each tile that fell back; *fallback_count (optional) their number. */
+gt_status gt_denoise(gt_denoiser* denoiser, const gt_denoise_input* input, uint32_t tile, float threshold,
+                     float* out, uint8_t* tile_fallback, uint32_t* fallback_count);
+
 /* Largest image gt_render_noalloc accepts (1024 x 1024 pixels). */
 #define GT_NOALLOC_MAX_PIXELS 1048576u
 

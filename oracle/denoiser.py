@@ -1,0 +1,176 @@
+"""TEST INFRASTRUCTURE ONLY — the CPU oracle of the learned denoiser.
+
+The reference has no denoiser (it stops at the AOVs of PathTracer::render_denoising_aovs,
+raytracing/renderer.rs:121-129), so this oracle restates the library's own network
+definition in float64 with torch's CPU autograd, parameter for parameter in the flat
+layout gt_denoiser_get_params returns, and the split-buffer per-tile fallback test in
+numpy.  Only tests/ may use it, as the checker of the GPU kernels.
+
+Definitions restated here:
+  input     x = [log1p(max(beauty, 0)), albedo, normal]  (9 channels; non-finite beauty = 0;
+            images padded to multiples of 16 by repeating the last row and column)
+  network   5 levels of two 3x3 convs + ReLU (32/48/64/80/96 channels), 2x2 average
+            pooling between levels, nearest 2x upsampling concatenated (upsampled first,
+            then the skip) before the two decoder convs of each level, a final 3x3 conv
+            to 3 channels without ReLU
+  output    out = conv_out + log1p(max(beauty, 0));  image = max(expm1(out), 0)
+  loss      mean |out - log1p(max(target, 0))| over pixels and channels
+"""
+from __future__ import annotations
+
+import numpy as np
+
+CHANNELS = (32, 48, 64, 80, 96)
+
+
+def layer_shapes() -> list:
+    c = CHANNELS
+    shapes = [(9, c[0], True), (c[0], c[0], True)]
+    for lv in range(1, len(c)):
+        shapes += [(c[lv - 1], c[lv], True), (c[lv], c[lv], True)]
+    for lv in range(len(c) - 2, -1, -1):
+        shapes += [(c[lv + 1] + c[lv], c[lv], True), (c[lv], c[lv], True)]
+    shapes.append((c[0], 3, False))
+    return shapes
+
+
+def param_count() -> int:
+    return sum(cout * 9 * cin + cout for cin, cout, _ in layer_shapes())
+
+
+def _unflatten(params):
+    """Flat [cout][3][3][cin] + [cout] per layer -> torch conv weights [cout][cin][3][3]."""
+    out, off = [], 0
+    for cin, cout, relu in layer_shapes():
+        n = cout * 9 * cin
+        w = params[off:off + n].reshape(cout, 3, 3, cin).permute(0, 3, 1, 2)
+        off += n
+        b = params[off:off + cout]
+        off += cout
+        out.append((w, b, relu))
+    assert off == params.numel()
+    return out
+
+
+def _pad16(t):
+    """[n, c, h, w] -> padded to multiples of 16 by repeating the last row / column."""
+    import torch
+
+    h, w = t.shape[2], t.shape[3]
+    hp, wp = (h + 15) // 16 * 16, (w + 15) // 16 * 16
+    if hp != h:
+        t = torch.cat([t, t[:, :, -1:, :].expand(-1, -1, hp - h, -1)], dim=2)
+    if wp != w:
+        t = torch.cat([t, t[:, :, :, -1:].expand(-1, -1, -1, wp - w)], dim=3)
+    return t
+
+
+def _log1p_clean(x):
+    import torch
+
+    x = torch.where(torch.isfinite(x), x, torch.zeros_like(x))
+    return torch.log1p(torch.clamp(x, min=0.0))
+
+
+def forward_log(params, beauty, albedo=None, normal=None):
+    """Log-space output [n, hp, wp, 3] (float64 torch) for inputs [n, h, w, 3]."""
+    import torch
+    import torch.nn.functional as F
+
+    b = torch.as_tensor(beauty, dtype=torch.float64)
+    z = torch.zeros_like(b)
+    a = torch.as_tensor(albedo, dtype=torch.float64) if albedo is not None else z
+    nm = torch.as_tensor(normal, dtype=torch.float64) if normal is not None else z
+    lb = _log1p_clean(b)
+    x = torch.cat([lb, a, nm], dim=-1).permute(0, 3, 1, 2)
+    x = _pad16(x)
+    lbp = x[:, :3]
+    layers = _unflatten(params)
+
+    def conv(i, t):
+        w, bias, relu = layers[i]
+        y = F.conv2d(t, w, bias, padding=1)
+        return F.relu(y) if relu else y
+
+    L = len(CHANNELS)
+    skips = []
+    t = x
+    for lv in range(L):
+        if lv > 0:
+            t = F.avg_pool2d(t, 2)
+        t = conv(2 * lv + 1, conv(2 * lv, t))
+        skips.append(t)
+    for k, lv in enumerate(range(L - 2, -1, -1)):
+        up = F.interpolate(t, scale_factor=2, mode="nearest")
+        t = torch.cat([up, skips[lv]], dim=1)
+        base = 2 * L + 2 * k
+        t = conv(base + 1, conv(base, t))
+    out = conv(len(layers) - 1, t) + lbp
+    return out.permute(0, 2, 3, 1)
+
+
+def denoise(params, beauty, albedo=None, normal=None) -> np.ndarray:
+    """The denoised image [h, w, 3] of one frame (float64 numpy)."""
+    import torch
+
+    p = torch.as_tensor(np.asarray(params, dtype=np.float64))
+    add = lambda t: None if t is None else np.asarray(t, dtype=np.float64)[None]
+    h, w = beauty.shape[:2]
+    with torch.no_grad():
+        out = forward_log(p, add(beauty), add(albedo), add(normal))[0, :h, :w]
+    return np.maximum(np.expm1(out.numpy()), 0.0)
+
+
+def loss_and_grad(params, beauty, target, albedo=None, normal=None):
+    """(loss, flat gradient) in float64 for a batch [n, h, w, 3] (h, w multiples of 16)."""
+    import torch
+
+    p = torch.tensor(np.asarray(params, dtype=np.float64), requires_grad=True)
+    out = forward_log(p, beauty, albedo, normal)
+    tgt = _log1p_clean(torch.as_tensor(target, dtype=torch.float64))
+    loss = (out - tgt).abs().mean()
+    loss.backward()
+    return float(loss.detach()), p.grad.numpy().copy()
+
+
+def tile_fallback(denoised, plain, half, tile: int = 16, threshold: float = 2.0):
+    """The split-buffer residual test per tile: (image, flags).  A tile keeps the plain
+    render when mean((d - p)^2 / (p^2 + 0.01)) > threshold * mean((a - p)^2 / (p^2 + 0.01))."""
+    d = np.asarray(denoised, dtype=np.float64)
+    p = np.asarray(plain, dtype=np.float64)
+    a = np.asarray(half, dtype=np.float64)
+    p = np.where(np.isfinite(p), p, 0.0)
+    a = np.where(np.isfinite(a), a, 0.0)
+    h, w = p.shape[:2]
+    ty, tx = (h + tile - 1) // tile, (w + tile - 1) // tile
+    flags = np.zeros((ty, tx), dtype=np.uint8)
+    out = d.copy()
+    den = p * p + 0.01
+    for j in range(ty):
+        for i in range(tx):
+            sl = (slice(j * tile, (j + 1) * tile), slice(i * tile, (i + 1) * tile))
+            r = np.sum((d[sl] - p[sl]) ** 2 / den[sl])
+            nz = np.sum((a[sl] - p[sl]) ** 2 / den[sl])
+            if r > threshold * nz:
+                flags[j, i] = 1
+                out[sl] = p[sl]
+    return out, flags
+
+
+def tile_margin(denoised, plain, half, tile: int = 16, threshold: float = 2.0) -> np.ndarray:
+    """Per tile |r - threshold * noise| / (r + threshold * noise): how far each tile's
+    decision is from the boundary (small values may round either way in FP32)."""
+    d = np.asarray(denoised, dtype=np.float64)
+    p = np.asarray(plain, dtype=np.float64)
+    a = np.asarray(half, dtype=np.float64)
+    h, w = p.shape[:2]
+    ty, tx = (h + tile - 1) // tile, (w + tile - 1) // tile
+    m = np.zeros((ty, tx))
+    den = p * p + 0.01
+    for j in range(ty):
+        for i in range(tx):
+            sl = (slice(j * tile, (j + 1) * tile), slice(i * tile, (i + 1) * tile))
+            r = np.sum((d[sl] - p[sl]) ** 2 / den[sl])
+            nz = threshold * np.sum((a[sl] - p[sl]) ** 2 / den[sl])
+            m[j, i] = abs(r - nz) / max(r + nz, 1e-300)
+    return m

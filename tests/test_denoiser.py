@@ -1,0 +1,220 @@
+"""The learned denoiser: its BF16 tensor-core kernels against the float64 torch oracle
+(forward, loss and gradient), the split-buffer per-tile fallback against its numpy
+restatement, training, the host/device boundary, and what the trained network gains over
+the plain render.
+
+Tolerances.  Weights and activations are BF16 (8 significant bits) with FP32 accumulation,
+so the GPU network differs from the float64 oracle by BF16 rounding compounded over 19
+layers.  Stated bounds:
+  forward   |log1p(gpu) - log1p(oracle)|: mean <= 0.01, 99.9th percentile <= 0.08
+  loss      relative difference <= 1e-2
+  gradient  per layer: cosine similarity >= 0.99 and relative L2 error <= 0.15
+            (the whole vector: cosine >= 0.995)
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from gartus_gb300 import denoiser as dn
+from oracle import denoiser as odn
+
+
+def _random_params(seed: int, out_scale: float = 1.0) -> np.ndarray:
+    """He-normal weights for every layer (the output layer scaled by out_scale) and small
+    random biases: the network's correction is O(1), so the comparison exercises it."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    shapes = odn.layer_shapes()
+    for i, (cin, cout, relu) in enumerate(shapes):
+        sd = np.sqrt(2.0 / (9 * cin)) * (out_scale if i == len(shapes) - 1 else 1.0)
+        parts.append(rng.normal(0.0, sd, cout * 9 * cin))
+        parts.append(rng.normal(0.0, 0.05, cout))
+    return np.concatenate(parts).astype(np.float32)
+
+
+def _images(seed: int, n: int, h: int, w: int):
+    """Noisy-render-like inputs: beauty exponential with a smooth mean, albedo in [0, 1],
+    unit normals, and a smooth target."""
+    rng = np.random.default_rng(seed)
+    yy, xx = np.meshgrid(np.linspace(0, 1, h), np.linspace(0, 1, w), indexing="ij")
+    base = 0.5 + 2.0 * np.stack([np.sin(3 * xx + 1) ** 2, np.cos(2 * yy) ** 2, xx * yy], axis=-1)
+    target = np.broadcast_to(base, (n, h, w, 3)).astype(np.float32).copy()
+    beauty = (target * rng.exponential(1.0, (n, h, w, 3))).astype(np.float32)
+    albedo = rng.uniform(0.0, 1.0, (n, h, w, 3)).astype(np.float32)
+    nrm = rng.normal(size=(n, h, w, 3))
+    nrm = (nrm / np.linalg.norm(nrm, axis=-1, keepdims=True)).astype(np.float32)
+    return beauty, albedo, nrm, target
+
+
+# ----------------------------------------------------------------- CPU only
+def test_parameter_layout_matches_oracle():
+    assert dn.layer_shapes() == odn.layer_shapes()
+    assert dn.param_count() == odn.param_count() == 774083
+
+
+def test_oracle_tap_convention():
+    """Flat weights are [cout][ky][kx][cin]; tap (ky, kx) reads the input at (y + ky - 1,
+    x + kx - 1).  With only enc0a's (co 0, ky 0, kx 1, ci 0) weight set to 1 and a unit
+    first-layer path, out channel 0 of the first layer is log1p(beauty) one row up."""
+    torch = pytest.importorskip("torch")
+    import torch.nn.functional as F
+
+    p = np.zeros(odn.param_count())
+    cin, cout = 9, 32
+    w = np.zeros((cout, 3, 3, cin))
+    w[0, 0, 1, 0] = 1.0
+    p[:cout * 9 * cin] = w.ravel()
+    layers = odn._unflatten(torch.tensor(p))
+    x = torch.arange(16 * 16, dtype=torch.float64).reshape(1, 1, 16, 16)
+    x = torch.cat([x, torch.zeros(1, 8, 16, 16, dtype=torch.float64)], dim=1)
+    y = F.conv2d(x, layers[0][0], layers[0][1], padding=1)
+    assert torch.equal(y[0, 0, 1:, :], x[0, 0, :-1, :])
+    assert torch.all(y[0, 0, 0, :] == 0)
+
+
+def test_oracle_tile_fallback_known_answers():
+    rng = np.random.default_rng(3)
+    p = rng.uniform(0.5, 1.5, (40, 24, 3))
+    a = p + rng.normal(0.0, 0.1, p.shape)
+    # identical to the render: residual 0, every tile keeps the denoised image
+    out, flags = odn.tile_fallback(p.copy(), p, a, tile=16)
+    assert flags.shape == (3, 2) and not flags.any()
+    # far from the render in the lower-right tile only: that tile falls back, exactly
+    d = p.copy()
+    d[32:, 16:] += 5.0
+    out, flags = odn.tile_fallback(d, p, a, tile=16)
+    assert flags.tolist() == [[0, 0], [0, 0], [0, 1]]
+    assert np.array_equal(out[32:, 16:], p[32:, 16:]) and np.array_equal(out[:32], d[:32])
+    # a noiseless split (a == p) makes any residual fail
+    out, flags = odn.tile_fallback(p + 1e-3, p, p, tile=8)
+    assert flags.all()
+
+
+# ----------------------------------------------------------------------- GPU
+@pytest.fixture(scope="module")
+def den(gpu_context):
+    d = dn.Denoiser(seed=7, context=gpu_context)
+    yield d
+    d.close()
+
+
+def _log_err(g, o):
+    return np.abs(np.log1p(np.maximum(g, 0.0)) - np.log1p(np.maximum(o, 0.0)))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("h,w", [(64, 64), (40, 56), (17, 33)])
+def test_forward_matches_oracle(den, h, w):
+    params = _random_params(11)
+    den.set_params(params)
+    beauty, albedo, nrm, _ = _images(5, 1, h, w)
+    got, _ = den.denoise(beauty[0], albedo[0], nrm[0])
+    ref = odn.denoise(params, beauty[0], albedo[0], nrm[0])
+    err = _log_err(got, ref)
+    change = np.abs(np.log1p(ref) - np.log1p(np.maximum(beauty[0], 0)))
+    print(f"forward {h}x{w}: mean |dlog| {err.mean():.2e}, p99.9 {np.quantile(err, 0.999):.2e}, "
+          f"max {err.max():.2e}; the network's own change: mean {change.mean():.2e}")
+    assert change.mean() > 0.1  # the comparison covers a real correction, not the identity
+    assert err.mean() <= 0.01
+    assert np.quantile(err, 0.999) <= 0.08
+
+
+@pytest.mark.gpu
+def test_gradient_matches_oracle(den):
+    torch = pytest.importorskip("torch")
+    params = _random_params(12)
+    den.set_params(params)
+    beauty, albedo, nrm, target = _images(6, 2, 32, 48)
+    dev = [torch.from_numpy(a).cuda() for a in (beauty, albedo, nrm, target)]
+    loss, grad = den.train_step(dev[0], dev[3], dev[1], dev[2], lr=0.0, want_grad=True)
+    ref_loss, ref_grad = odn.loss_and_grad(params, beauty, target, albedo, nrm)
+    assert abs(loss - ref_loss) <= 1e-2 * abs(ref_loss)
+    cos_all = float(grad @ ref_grad / (np.linalg.norm(grad) * np.linalg.norm(ref_grad)))
+    print(f"loss gpu {loss:.6f} oracle {ref_loss:.6f}; gradient cosine {cos_all:.5f}")
+    assert cos_all >= 0.995
+    off = 0
+    for i, (cin, cout, _) in enumerate(odn.layer_shapes()):
+        n = cout * 9 * cin + cout
+        g, r = grad[off:off + n].astype(np.float64), ref_grad[off:off + n]
+        off += n
+        cos = float(g @ r / (np.linalg.norm(g) * np.linalg.norm(r) + 1e-300))
+        rel = float(np.linalg.norm(g - r) / (np.linalg.norm(r) + 1e-300))
+        print(f"  layer {i:2d} {cin:3d}->{cout:3d}: cosine {cos:.5f} rel L2 {rel:.3e}")
+        assert cos >= 0.99 and rel <= 0.15, i
+    # lr = 0 leaves the parameters unchanged
+    assert np.array_equal(den.get_params(), params)
+
+
+@pytest.mark.gpu
+def test_host_and_device_buffers_agree(den):
+    torch = pytest.importorskip("torch")
+    den.set_params(_random_params(13))
+    beauty, albedo, nrm, _ = _images(7, 1, 48, 80)
+    half = beauty[0] * np.float32(0.9)
+    host, hf = den.denoise(beauty[0], albedo[0], nrm[0], beauty_half=half)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    dev, df = den.denoise(t(beauty[0]), t(albedo[0]), t(nrm[0]), beauty_half=t(half))
+    assert np.array_equal(host, dev.cpu().numpy())
+    assert np.array_equal(hf, df)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tile", [16, 32, 7])
+def test_tile_fallback_matches_oracle(den, tile):
+    den.set_params(_random_params(14, out_scale=0.3))
+    beauty, albedo, nrm, target = _images(8, 1, 72, 104)
+    rng = np.random.default_rng(9)
+    half = (target[0] * rng.exponential(1.0, target[0].shape)).astype(np.float32)
+    # left columns: a split buffer without noise, so any residual sends the tile back
+    half[:, :40] = beauty[0][:, :40]
+    d, _ = den.denoise(beauty[0], albedo[0], nrm[0])
+    out, flags = den.denoise(beauty[0], albedo[0], nrm[0], beauty_half=half, tile=tile, threshold=1.5)
+    ref_out, ref_flags = odn.tile_fallback(d, beauty[0], half, tile=tile, threshold=1.5)
+    margin = odn.tile_margin(d, beauty[0], half, tile=tile, threshold=1.5)
+    decided = margin > 1e-4
+    print(f"tile {tile}: {int(ref_flags.sum())} of {ref_flags.size} tiles fall back")
+    assert 0 < ref_flags.sum() < ref_flags.size  # both outcomes are exercised
+    assert np.array_equal(flags[decided], ref_flags[decided])
+    # each tile holds exactly the denoised or the plain pixels, as its flag says
+    for j in range(flags.shape[0]):
+        for i in range(flags.shape[1]):
+            sl = (slice(j * tile, (j + 1) * tile), slice(i * tile, (i + 1) * tile))
+            src = beauty[0] if flags[j, i] else d
+            assert np.array_equal(out[sl], src[sl])
+
+
+@pytest.mark.gpu
+def test_training_reduces_loss(gpu_context):
+    torch = pytest.importorskip("torch")
+    d = dn.Denoiser(seed=3, context=gpu_context)
+    try:
+        beauty, albedo, nrm, target = _images(10, 4, 64, 64)
+        dev = [torch.from_numpy(a).cuda() for a in (beauty, albedo, nrm, target)]
+        losses = [d.train_step(dev[0], dev[3], dev[1], dev[2], lr=2e-3) for _ in range(60)]
+        print(f"loss {losses[0]:.4f} -> {losses[-1]:.4f}")
+        assert all(np.isfinite(losses))
+        assert losses[-1] < 0.6 * losses[0]
+    finally:
+        d.close()
+
+
+@pytest.mark.gpu
+def test_invalid_arguments_are_rejected(den):
+    torch = pytest.importorskip("torch")
+    from gartus_gb300._lib import GartusError
+
+    x = torch.zeros((1, 24, 32, 3), device="cuda")
+    with pytest.raises(GartusError, match="multiples of 16"):
+        den.train_step(x, x, lr=0.0)
+    with pytest.raises(GartusError, match="parameter count"):
+        den.set_params(np.zeros(10, dtype=np.float32))
+    bad = np.zeros(den.param_count, dtype=np.float32)
+    bad[5] = np.nan
+    with pytest.raises(GartusError, match="finite"):
+        den.set_params(bad)
+    img = np.ones((16, 16, 3), dtype=np.float32)
+    with pytest.raises(GartusError, match="tile"):
+        den.denoise(img, beauty_half=img, tile=2)
+    with pytest.raises(GartusError, match="threshold"):
+        den.denoise(img, beauty_half=img, threshold=-1.0)
