@@ -295,6 +295,23 @@ template <class R> GT_DEV HitRec<R> make_hit(const SceneDev<R>& sc, uint32_t i, 
     return h;
 }
 
+// Origin of a ray that leaves the surface at h.  In f32 the hit point and the primitives'
+// stored corners and edges carry rounding errors of a few ulps of the coordinates (about
+// 1e-4 at 500 units), more than t_min = 0.001 covers for a grazing ray near the edge
+// between two faces: such a ray can start just behind the neighbouring face's plane and
+// hit it from inside, after which the path is trapped in a closed object and its
+// throughput compounds without bound.  The f32 path therefore starts new rays
+// 2^-19 (max |p| + 1) off the surface, on the side the ray leaves towards (a scaled form
+// of the offset of Waechter and Binder, "A Fast and Robust Method for Avoiding
+// Self-Intersection", Ray Tracing Gems, 2019).  The f64 path keeps the reference's h.p.
+template <class R> GT_DEV V3<R> spawn_origin(const HitRec<R>& h, V3<R> dir);
+template <> GT_DEV V3<double> spawn_origin(const HitRec<double>& h, V3<double>) { return h.p; }
+template <> GT_DEV V3<float> spawn_origin(const HitRec<float>& h, V3<float> dir) {
+    const float m = fmaxf(fmaxf(fabsf(h.p.x), fabsf(h.p.y)), fabsf(h.p.z)) + 1.0f;
+    const float e = dot(dir, h.n) >= 0.0f ? m * 0x1p-19f : -m * 0x1p-19f;
+    return h.p + h.n * e;
+}
+
 // ------------------------------------------------------------------ materials
 // Perlin::noise (gmath/perlin.rs:36-58) and perlin_interp (106-124): the eight corner
 // gradients picked through the three permutations, weighted by smoothstep blends, summed

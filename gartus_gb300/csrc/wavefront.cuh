@@ -246,7 +246,7 @@ GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& 
     ScatterRec<R> s = mat_scatter(m, p.d, h, g);
     if (s.kind == SC_SPECULAR) {
         p.att = cmul(p.att, s.att);
-        p.o = h.p;
+        p.o = spawn_origin(h, s.dir);
         p.d = s.dir;
         p.allow_emit = true;
         p.miss_w = R(1);
@@ -284,6 +284,7 @@ GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& 
                     }
                 }
             }
+            if (sh.valid[0] || sh.valid[1]) sh.o = spawn_origin(h, sh.valid[0] ? sh.dir[0] : sh.dir[1]);
         }
         V3<R> dir;
         R pdf;
@@ -305,7 +306,7 @@ GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& 
                 R next_w = R(1);
                 if (weight_env) next_w = power_heuristic(pdf, env_pdf(P.env, dir));
                 p.att = cmul(p.att, s.att * (sp / pdf));
-                p.o = h.p;
+                p.o = spawn_origin(h, dir);
                 p.d = dir;
                 p.allow_emit = !suppress;
                 p.miss_w = next_w;
