@@ -40,7 +40,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="cornell", choices=["cornell", "final", "mesh", "batch"])
+    ap.add_argument("--config", default="cornell", choices=["cornell", "final", "mesh", "batch", "denoise"])
+    ap.add_argument("--target-spp", type=int, default=4096, help="denoise config: samples of the reference image")
+    ap.add_argument("--max-spp", type=int, default=1024, help="denoise config: largest plain sample count")
+    ap.add_argument("--scene", default="mesh", choices=["mesh", "cornell"],
+                    help="denoise config: the mesh-heavy workload or the Cornell box, both at 1920x1080")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--schedule", default="auto", choices=["auto", "wavefront", "persistent"])
@@ -197,8 +201,72 @@ def cpu_baseline(scene, lights, env, cam, seconds: float):
     return samples / dt / 1e6, threads, f"rows {y0}..{y0 + rows} of {h} ({w * rows} pixels x {spp} spp), f64", dt
 
 
+def run_denoise(args):
+    """Time to relMSE 1e-3 on the mesh-heavy workload at 1920x1080 (random sampling, depth
+    8): plain accumulation against the learned denoiser with its per-tile fallback."""
+    import numpy as np
+    import torch
+
+    from gartus_gb300 import abi, scenes
+    from gartus_gb300 import build as gbuild
+    from gartus_gb300.denoiser import Denoiser, convergence_sweep
+    from gartus_gb300.raytracing import Context
+
+    gbuild.build()
+    world, rank, local = dist_env()
+    if world > 1 and rank != 0:  # one GPU measures; replicas would repeat the same curve
+        return
+    ctx = Context(local if world > 1 else 0)
+    width = args.width or 1920
+    if args.scene == "mesh":
+        scene, env = scenes.mesh_heavy_scene()
+        lights = None
+        cam = scenes.mesh_heavy_camera(width, width * 1080 // 1920, 1, 8)
+        wl = {"workload": "mesh_heavy_perlin_tori_sun", "max_depth": 8}
+    else:
+        scene, lights = scenes.cornell_scene()
+        env = None
+        cam = scenes.cornell_camera(width, 1, 50)._with(aspect_ratio=1920.0 / 1080.0)
+        wl = {"workload": "cornell_box_ggx_glass_1080p", "max_depth": 50}
+    cam = cam.with_pixel_sample_mode(abi.GT_SAMPLE_RANDOM).with_samples_per_pixel(1)
+    w, h, _ = cam.image_size()
+    den = Denoiser.pretrained(context=ctx)
+    log = (lambda m: print(m, file=sys.stderr, flush=True))
+    with ClockSampler(ctx.device) as clocks:
+        r = convergence_sweep(den, scene, cam, lights, env, target_spp=args.target_spp, max_spp=args.max_spp,
+                              context=ctx, log=log)
+    value = r["denoised"]["time_s"] if r["denoised"] else None
+    line = {
+        "metric": "time-to-relMSE 1e-3", "value": value, "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 0,
+        "ms_per_step": value * 1e3 if value else None, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 render, bf16 network (fp32 accumulate)",
+        "data": "synthetic (seeded procedural scene)",
+        "config": {**wl, "width": w, "height": h, "sampling": "random", "reference_spp": args.target_spp,
+                   "reference": "two independent f32 renders of half the samples each (Kahan-compensated "
+                                "accumulation), their difference estimating the reference's own error",
+                   "plain_sweep_spp": f"1..{args.max_spp} doubling", "denoiser": "committed U-Net weights",
+                   "relmse": "mean over pixels of mean_c (x - T)^2 / (T^2 + 0.01), less the reference's own "
+                             "error, over all but the 0.1% of pixels with the largest error (raw values in curve)",
+                   "tile": 16, "threshold": 3.0},
+        "plain_time_s": r["plain"]["time_s"] if r["plain"] else None,
+        "plain_spp": r["plain"]["spp"] if r["plain"] else None,
+        "plain_extrapolated": r["plain"]["extrapolated"] if r["plain"] else None,
+        "goals": r["goals"], "plain_relmse_times_spp": r["plain_c"],
+        "denoised_spp": r["denoised"]["spp"] if r["denoised"] else None,
+        "speedup": r["speedup"], "best_denoised_relmse": r["best_denoised"],
+        "reference_error": r["reference_error"], "clocks": clocks.summary(),
+        "curve": r["curve"],
+    }
+    print(json.dumps(line))
+
+
 def run_reference_arm(args):
     world, rank, _ = dist_env()
+    if args.config == "denoise":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no denoiser, and its CPU path "
+                              "cannot render the 1080p reference image of this experiment within minutes"}))
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
@@ -438,6 +506,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference_arm(args)
+    elif args.config == "denoise":
+        run_denoise(args)
     else:
         run_ours(args)
 

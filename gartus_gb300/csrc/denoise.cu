@@ -528,7 +528,7 @@ gt_status gt_denoise(gt_denoiser* d, const gt_denoise_input* in, uint32_t tile, 
     if (h <= 0 || w <= 0 || h * w > (1LL << 26)) return fail(GT_ERR_INVALID_ARG, "image size out of range");
     if (tile == 0) tile = 16;
     if (tile < 4 || tile > 256) return fail(GT_ERR_INVALID_ARG, "tile must be 0 or in [4, 256]");
-    if (threshold == 0.f) threshold = 2.f;
+    if (threshold == 0.f) threshold = 3.f;
     if (!(threshold > 0.f) || !std::isfinite(threshold)) return fail(GT_ERR_INVALID_ARG, "threshold must be finite and > 0");
     const int hp = int((h + 15) / 16 * 16), wp = int((w + 15) / 16 * 16);
     const int tiles = int(((h + tile - 1) / tile) * ((w + tile - 1) / tile));

@@ -355,45 +355,65 @@ __global__ void k_unpack_output(const float* out, int h, int w, int wp, float* r
     }
 }
 
-// Split-buffer residual test, one block per tile: keeps the denoised tile unless
-// mean((d - p)^2 / (p^2 + 0.01)) > threshold * mean((a - p)^2 / (p^2 + 0.01)), where p is the
-// render, a the mean of its first half of samples and d the denoised image; a tile that
-// fails keeps p.  flags[tile] = 1 and *count += 1 for each tile that falls back.
+// Split-buffer residual test, one block per tile.  With p the render, a the mean of its
+// first half of samples, d the denoised image and N the tile's pixel count, per channel c:
+//     m_d = mean(d),  m_p = mean(p),  v = sum((a - p)^2) / N^2
+// (v estimates the variance of m_p: (a - p)^2 = (a - b)^2 / 4 estimates each pixel's
+// variance from its two halves).  The tile keeps p when the denoised tile's mean moved by
+// more than `threshold` standard errors, with 1% of the mean as a floor:
+//     sum_c (m_d - m_p)^2 > threshold^2 * sum_c (v + (0.01 m_p)^2)
+// flags[tile] = 1 and *count += 1 for each tile that falls back.
+constexpr float kFallbackRelFloor = 0.01f;
 __global__ void __launch_bounds__(256) k_tile_fallback(const float* d, const float* p, const float* a, int h, int w,
                                                         int tile, float threshold, float* out, uint8_t* flags,
                                                         uint32_t* count) {
-    __shared__ float sr[8], sn[8];
+    __shared__ float red[3][3][8]; // [sum d, sum p, sum (a-p)^2][channel][warp]
     __shared__ int keep_plain;
     const int tiles_x = (w + tile - 1) / tile;
     const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
     const int x0 = tx * tile, y0 = ty * tile;
     const int tw = min(tile, w - x0), th = min(tile, h - y0);
-    float r = 0.f, nz = 0.f;
-    for (int i = threadIdx.x; i < tw * th * 3; i += blockDim.x) {
-        const int k = i % 3, q = i / 3;
-        const size_t o = ((size_t(y0 + q / tw)) * w + x0 + q % tw) * 3 + k;
-        const float pv = isfinite(p[o]) ? p[o] : 0.f;
-        const float den = pv * pv + 0.01f;
-        const float dd = d[o] - pv, da = (isfinite(a[o]) ? a[o] : 0.f) - pv;
-        r += dd * dd / den;
-        nz += da * da / den;
+    float sd[3] = {0.f, 0.f, 0.f}, sp[3] = {0.f, 0.f, 0.f}, sv[3] = {0.f, 0.f, 0.f};
+    for (int q = threadIdx.x; q < tw * th; q += blockDim.x) {
+        const size_t o = (size_t(y0 + q / tw) * w + x0 + q % tw) * 3;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float pv = isfinite(p[o + k]) ? p[o + k] : 0.f;
+            const float av = isfinite(a[o + k]) ? a[o + k] : 0.f;
+            sd[k] += d[o + k];
+            sp[k] += pv;
+            sv[k] += (av - pv) * (av - pv);
+        }
     }
-    for (int off = 16; off > 0; off >>= 1) {
-        r += __shfl_down_sync(0xffffffffu, r, off);
-        nz += __shfl_down_sync(0xffffffffu, nz, off);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        sr[threadIdx.x >> 5] = r;
-        sn[threadIdx.x >> 5] = nz;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        for (int off = 16; off > 0; off >>= 1) {
+            sd[k] += __shfl_down_sync(0xffffffffu, sd[k], off);
+            sp[k] += __shfl_down_sync(0xffffffffu, sp[k], off);
+            sv[k] += __shfl_down_sync(0xffffffffu, sv[k], off);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            red[0][k][threadIdx.x >> 5] = sd[k];
+            red[1][k][threadIdx.x >> 5] = sp[k];
+            red[2][k][threadIdx.x >> 5] = sv[k];
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        float rs = 0.f, ns = 0.f;
-        for (int i = 0; i < int(blockDim.x >> 5); ++i) {
-            rs += sr[i];
-            ns += sn[i];
+        const float n = float(tw * th);
+        float shift = 0.f, var = 0.f;
+        for (int k = 0; k < 3; ++k) {
+            float td = 0.f, tp = 0.f, tv = 0.f;
+            for (int i = 0; i < int(blockDim.x >> 5); ++i) {
+                td += red[0][k][i];
+                tp += red[1][k][i];
+                tv += red[2][k][i];
+            }
+            const float md = td / n, mp = tp / n;
+            shift += (md - mp) * (md - mp);
+            var += tv / (n * n) + (kFallbackRelFloor * mp) * (kFallbackRelFloor * mp);
         }
-        keep_plain = rs > threshold * ns ? 1 : 0;
+        keep_plain = shift > threshold * threshold * var ? 1 : 0;
         flags[blockIdx.x] = uint8_t(keep_plain);
         if (keep_plain) atomicAdd(count, 1u);
     }
@@ -401,7 +421,7 @@ __global__ void __launch_bounds__(256) k_tile_fallback(const float* d, const flo
     const float* src = keep_plain ? p : d;
     for (int i = threadIdx.x; i < tw * th * 3; i += blockDim.x) {
         const int k = i % 3, q = i / 3;
-        const size_t o = ((size_t(y0 + q / tw)) * w + x0 + q % tw) * 3 + k;
+        const size_t o = (size_t(y0 + q / tw) * w + x0 + q % tw) * 3 + k;
         out[o] = src[o];
     }
 }

@@ -132,7 +132,7 @@ class Denoiser:
         return (float(loss.value), grad) if want_grad else float(loss.value)
 
     # -- inference
-    def denoise(self, beauty, albedo=None, normal=None, beauty_half=None, tile: int = 16, threshold: float = 2.0):
+    def denoise(self, beauty, albedo=None, normal=None, beauty_half=None, tile: int = 16, threshold: float = 3.0):
         """Denoises one [h, w, 3] frame.  Host numpy arrays give a numpy result, CUDA tensors
         a CUDA tensor.  With beauty_half (the mean of the first half of the same samples)
         each tile whose split-buffer residual test fails keeps the plain render; returns
@@ -318,7 +318,36 @@ def render_pair(ts: TrainingScene, low_spp: int, high_spp: int, seed: int, conte
     return img.pixels, albedo, normal, target
 
 
-def render_training_set(count: int, size: int = 256, low_spp=(1, 2, 4, 8), high_spp: int = 1024, first_seed: int = 0,
+def render_split(ts: TrainingScene, spp: int, seed: int, context: Optional[Context] = None):
+    """A render of `spp` samples per pixel with its split buffer and AOVs: (beauty,
+    beauty_half, albedo, normal), beauty_half being the mean of the first spp // 2 samples
+    of the same pixel streams (gt_render_accumulate twice on one accumulator)."""
+    w, h, _ = ts.camera.image_size()
+    cam = ts.camera.with_samples_per_pixel(spp).with_rng_seed(1 + 2 * seed)
+    tracer = PathTracer(cam, context=context)
+    acc = Accumulator(w, h, "f32", context=context)
+    try:
+        half = tracer.render_accumulate(ts.scene, acc, spp // 2, ts.lights, ts.environment).pixels.copy()
+        full = tracer.render_accumulate(ts.scene, acc, spp - spp // 2, ts.lights, ts.environment).pixels
+    finally:
+        acc.close()
+    _, albedo, normal = tracer._render(ts.scene, ts.lights, ts.environment, aovs=True)
+    return full, half, albedo, normal
+
+
+def evaluate(den: "Denoiser", ts: TrainingScene, spp: int, target: np.ndarray, seed: int, tile: int = 16,
+             threshold: float = 3.0, context: Optional[Context] = None) -> dict:
+    """relMSE against `target` of the plain render at `spp`, of its denoised image and of the
+    denoised image with the per-tile fallback."""
+    full, half, albedo, normal = render_split(ts, spp, seed, context)
+    d, _ = den.denoise(full, albedo, normal)
+    f, flags = den.denoise(full, albedo, normal, beauty_half=half, tile=tile, threshold=threshold)
+    return {"plain": relmse(full, target), "denoised": relmse(d, target), "fallback": relmse(f, target),
+            "fallback_tiles": int(flags.sum()), "tiles": int(flags.size)}
+
+
+def render_training_set(count: int, size: int = 256, low_spp=(1, 2, 4, 8, 16, 32, 64, 128), high_spp: int = 1024,
+                        first_seed: int = 0,
                         context: Optional[Context] = None, log=None):
     """`count` seeded scenes rendered by this path tracer; returns float32 arrays
     beauty, albedo, normal, target of shape [count, size, size, 3]."""
@@ -380,16 +409,126 @@ def relmse(x: np.ndarray, ref: np.ndarray) -> float:
     return float(np.mean((x - ref) ** 2 / (ref * ref + 1e-2)))
 
 
+def _accumulate(tracer, scene, acc, spp, lights, env, chunk):
+    """Adds spp samples in chunks; returns (image, device ms)."""
+    ms, img, done = 0.0, None, 0
+    while done < spp:
+        k = min(chunk, spp - done)
+        img = tracer.render_accumulate(scene, acc, k, lights, env)
+        ms += tracer.last_stats["gpu_ms"]
+        done += k
+    return img.pixels, ms
+
+
+def convergence_sweep(den: Denoiser, scene, camera: RayCamera, lights=None, environment=None,
+                      target_spp: int = 4096, max_spp: int = 1024, goal: float = 1e-3, tile: int = 16,
+                      threshold: float = 3.0, trim: float = 1e-3, context: Optional[Context] = None,
+                      log=None) -> dict:
+    """Time to reach relMSE `goal`, plain accumulation against denoised.
+
+    The reference image is two independent renders of target_spp / 2 samples, T1 and T2,
+    averaged; its own error is estimated from their difference,
+        e_T = mean((T1 - T2)^2 / 4 / (T^2 + 0.01)),
+    and subtracted from every measured relMSE (relMSE(x, T) = err(x) + e_T for x independent
+    of T).  The integrator's rare single-sample fireflies (caustics through glass onto the
+    light, grazing GGX) dominate a plain mean of per-pixel errors, so the decision uses the
+    mean over all but the `trim` fraction of pixels with the largest error; the untrimmed
+    values are reported beside it.  Plain accumulation doubles its sample count from 1 to max_spp on one
+    accumulator, so the image at N / 2 is the split buffer of the image at N.  The denoised
+    time at N is the render time to N, a 1-sample AOV render and the denoise call (host
+    buffers, copies included).  The camera must use random sampling."""
+    import torch
+
+    w, h, _ = camera.image_size()
+    chunk = 256
+    t_ref = []
+    for k, seed in enumerate((0x7A11, 0x7A12)):
+        acc = Accumulator(w, h, "f32", context=context)
+        tr = PathTracer(camera.with_rng_seed(seed), context=context)
+        img, ms = _accumulate(tr, scene, acc, target_spp // 2, lights, environment, chunk)
+        acc.close()
+        t_ref.append(img.astype(np.float64))
+        if log:
+            log(f"reference half {k + 1}: {target_spp // 2} spp in {ms / 1e3:.1f} s of device time")
+    T = 0.5 * (t_ref[0] + t_ref[1])
+    den_T = T * T + 1e-2
+    ref_px = np.mean((t_ref[0] - t_ref[1]) ** 2 / 4.0 / den_T, axis=-1)  # the reference's own error
+    e_T = float(np.mean(ref_px))
+
+    def errs(x):
+        """(trimmed, raw): relMSE against T less the reference's own error; trimmed drops the
+        0.1% of pixels with the largest error (single-sample fireflies of the integrator)."""
+        px = np.mean((np.asarray(x, dtype=np.float64) - T) ** 2 / den_T, axis=-1)
+        keep = px <= np.quantile(px, 1.0 - trim)
+        return float(np.mean(px[keep]) - np.mean(ref_px[keep])), float(np.mean(px)) - e_T
+
+    tr = PathTracer(camera.with_rng_seed(0x5EED), context=context)
+    t0 = time.perf_counter()
+    _, albedo, normal = PathTracer(camera.with_samples_per_pixel(1).with_rng_seed(0x5EED), context=context)._render(
+        scene, lights, environment, aovs=True)
+    aov_s = time.perf_counter() - t0
+    den.denoise(np.zeros((h, w, 3), np.float32))  # sizes the denoiser's buffers outside the timings
+    acc = Accumulator(w, h, "f32", context=context)
+    rows, prev, n, render_ms = [], None, 1, 0.0
+    try:
+        while n <= max_spp:
+            img, ms = _accumulate(tr, scene, acc, n - acc.samples, lights, environment, chunk)
+            render_ms += ms
+            pe, pr = errs(img)
+            row = {"spp": n, "render_s": render_ms / 1e3, "plain": pe, "plain_raw": pr}
+            if prev is not None:
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                d, flags = den.denoise(img, albedo, normal, beauty_half=prev, tile=tile, threshold=threshold)
+                dn_s = time.perf_counter() - t0
+                de, dr = errs(d)
+                row.update(denoised=de, denoised_raw=dr, denoise_s=dn_s, fallback_tiles=int(flags.sum()),
+                           denoised_time_s=render_ms / 1e3 + aov_s + dn_s)
+            rows.append(row)
+            if log:
+                log(" ".join(f"{k} {v:.4g}" if isinstance(v, float) else f"{k} {v}" for k, v in row.items()))
+            prev = img.copy()
+            n *= 2
+    finally:
+        acc.close()
+    # relMSE ~ C / N for plain accumulation: C from the last three points of the sweep
+    c_fit = float(np.median([r["plain"] * r["spp"] for r in rows[-3:]]))
+    s_per_spp = rows[-1]["render_s"] / rows[-1]["spp"]
+
+    def plain_time(g):
+        hit = next((r for r in rows if r["plain"] <= g), None)
+        if hit is not None:
+            return {"time_s": hit["render_s"], "spp": hit["spp"], "extrapolated": False}
+        if c_fit <= 0.0:
+            return None
+        n_star = c_fit / g
+        return {"time_s": s_per_spp * n_star, "spp": n_star, "extrapolated": True}
+
+    def denoised_time(g):
+        hit = next((r for r in rows if "denoised" in r and r["denoised"] <= g), None)
+        return {"time_s": hit["denoised_time_s"], "spp": hit["spp"]} if hit is not None else None
+
+    goals = {}
+    for g in sorted({goal, 1e-2, 5e-3, 2e-3, 1e-3}, reverse=True):
+        pt, dt = plain_time(g), denoised_time(g)
+        goals[f"{g:g}"] = {"plain": pt, "denoised": dt,
+                           "speedup": (pt["time_s"] / dt["time_s"]) if pt and dt else None}
+    return {"goal": goal, "trim": trim, "reference_error": e_T, "aov_s": aov_s, "curve": rows,
+            "plain_c": c_fit, "plain": plain_time(goal), "denoised": denoised_time(goal),
+            "speedup": goals[f"{goal:g}"]["speedup"], "goals": goals,
+            "best_denoised": min((r["denoised"] for r in rows if "denoised" in r), default=None)}
+
+
 def main(argv=None) -> int:
     import argparse
 
     import torch
 
     ap = argparse.ArgumentParser(description="Train the denoiser on scenes rendered by this path tracer.")
-    ap.add_argument("--scenes", type=int, default=192)
+    ap.add_argument("--scenes", type=int, default=384)
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--high-spp", type=int, default=1024)
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--steps", type=int, default=6000)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--crop", type=int, default=128)
     ap.add_argument("--lr", type=float, default=2e-3)

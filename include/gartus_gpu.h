@@ -465,12 +465,13 @@ typedef struct gt_denoise_input {
 
 /* Denoises one frame into `out` (same memory kind and shape as the beauty image).
  *
- * Per-tile fallback (split-buffer residual test): with beauty_half given, the frame's
- * samples split into two halves A = beauty_half and B = 2 * beauty - A.  For each tile of
- * tile x tile pixels (0 = 16), with d = denoised and p = beauty,
- *     residual = mean((d - p)^2 / (p^2 + 0.01)),  noise = mean((A - p)^2 / (p^2 + 0.01)),
- * noise estimating p's own relative error.  When residual > threshold * noise (0 = 2.0:
- * the denoiser's error exceeds p's noise) the tile keeps the plain render p.
+ * Per-tile fallback (split-buffer residual test): with beauty_half given, p = beauty and
+ * a = beauty_half, each tile of tile x tile pixels (0 = 16) of N pixels compares, per
+ * channel, the mean of the denoised tile m_d with the render's mean m_p.  The variance of
+ * m_p is estimated from the split as v = sum((a - p)^2) / N^2.  When
+ *     sum_c (m_d - m_p)^2 > threshold^2 * sum_c (v + (0.01 m_p)^2)
+ * (the denoiser moved the tile's mean by more than `threshold` standard errors, 0 = 3.0,
+ * with 1% of the mean as a floor) the tile keeps the plain render p.
  * tile_fallback (optional, host, ceil(h/tile) * ceil(w/tile) bytes, row-major) receives 1
  * for each tile that fell back; *fallback_count (optional) their number. */
 gt_status gt_denoise(gt_denoiser* denoiser, const gt_denoise_input* input, uint32_t tile, float threshold,

@@ -133,9 +133,7 @@ def loss_and_grad(params, beauty, target, albedo=None, normal=None):
     return float(loss.detach()), p.grad.numpy().copy()
 
 
-def tile_fallback(denoised, plain, half, tile: int = 16, threshold: float = 2.0):
-    """The split-buffer residual test per tile: (image, flags).  A tile keeps the plain
-    render when mean((d - p)^2 / (p^2 + 0.01)) > threshold * mean((a - p)^2 / (p^2 + 0.01))."""
+def _tile_stats(denoised, plain, half, tile, threshold):
     d = np.asarray(denoised, dtype=np.float64)
     p = np.asarray(plain, dtype=np.float64)
     a = np.asarray(half, dtype=np.float64)
@@ -143,34 +141,36 @@ def tile_fallback(denoised, plain, half, tile: int = 16, threshold: float = 2.0)
     a = np.where(np.isfinite(a), a, 0.0)
     h, w = p.shape[:2]
     ty, tx = (h + tile - 1) // tile, (w + tile - 1) // tile
-    flags = np.zeros((ty, tx), dtype=np.uint8)
-    out = d.copy()
-    den = p * p + 0.01
+    shift = np.zeros((ty, tx))
+    bound = np.zeros((ty, tx))
     for j in range(ty):
         for i in range(tx):
             sl = (slice(j * tile, (j + 1) * tile), slice(i * tile, (i + 1) * tile))
-            r = np.sum((d[sl] - p[sl]) ** 2 / den[sl])
-            nz = np.sum((a[sl] - p[sl]) ** 2 / den[sl])
-            if r > threshold * nz:
-                flags[j, i] = 1
-                out[sl] = p[sl]
+            n = p[sl].shape[0] * p[sl].shape[1]
+            md = d[sl].reshape(-1, 3).mean(axis=0)
+            mp = p[sl].reshape(-1, 3).mean(axis=0)
+            v = ((a[sl] - p[sl]) ** 2).reshape(-1, 3).sum(axis=0) / (n * n)
+            shift[j, i] = np.sum((md - mp) ** 2)
+            bound[j, i] = threshold * threshold * np.sum(v + (0.01 * mp) ** 2)
+    return d, p, shift, bound
+
+
+def tile_fallback(denoised, plain, half, tile: int = 16, threshold: float = 3.0):
+    """The split-buffer residual test per tile: (image, flags).  Per channel the tile means
+    m_d (denoised) and m_p (plain) and v = sum((a - p)^2) / N^2, the variance of m_p
+    estimated from the two halves; the tile keeps the plain render when
+    sum_c (m_d - m_p)^2 > threshold^2 * sum_c (v + (0.01 m_p)^2)."""
+    d, p, shift, bound = _tile_stats(denoised, plain, half, tile, threshold)
+    flags = (shift > bound).astype(np.uint8)
+    out = d.copy()
+    for j, i in zip(*np.nonzero(flags)):
+        sl = (slice(j * tile, (j + 1) * tile), slice(i * tile, (i + 1) * tile))
+        out[sl] = p[sl]
     return out, flags
 
 
-def tile_margin(denoised, plain, half, tile: int = 16, threshold: float = 2.0) -> np.ndarray:
-    """Per tile |r - threshold * noise| / (r + threshold * noise): how far each tile's
-    decision is from the boundary (small values may round either way in FP32)."""
-    d = np.asarray(denoised, dtype=np.float64)
-    p = np.asarray(plain, dtype=np.float64)
-    a = np.asarray(half, dtype=np.float64)
-    h, w = p.shape[:2]
-    ty, tx = (h + tile - 1) // tile, (w + tile - 1) // tile
-    m = np.zeros((ty, tx))
-    den = p * p + 0.01
-    for j in range(ty):
-        for i in range(tx):
-            sl = (slice(j * tile, (j + 1) * tile), slice(i * tile, (i + 1) * tile))
-            r = np.sum((d[sl] - p[sl]) ** 2 / den[sl])
-            nz = threshold * np.sum((a[sl] - p[sl]) ** 2 / den[sl])
-            m[j, i] = abs(r - nz) / max(r + nz, 1e-300)
-    return m
+def tile_margin(denoised, plain, half, tile: int = 16, threshold: float = 3.0) -> np.ndarray:
+    """Per tile |shift - bound| / (shift + bound): how far each tile's decision is from the
+    boundary (small values may round either way in FP32)."""
+    _, _, shift, bound = _tile_stats(denoised, plain, half, tile, threshold)
+    return np.abs(shift - bound) / np.maximum(shift + bound, 1e-300)

@@ -86,9 +86,16 @@ def test_oracle_tile_fallback_known_answers():
     out, flags = odn.tile_fallback(d, p, a, tile=16)
     assert flags.tolist() == [[0, 0], [0, 0], [0, 1]]
     assert np.array_equal(out[32:, 16:], p[32:, 16:]) and np.array_equal(out[:32], d[:32])
-    # a noiseless split (a == p) makes any residual fail
-    out, flags = odn.tile_fallback(p + 1e-3, p, p, tile=8)
+    # a noiseless split (a == p) leaves the 1% floor: a 5% shift of the mean falls back
+    # at threshold 3, a 2% shift does not
+    out, flags = odn.tile_fallback(p * 1.05, p, p, tile=8)
     assert flags.all()
+    out, flags = odn.tile_fallback(p * 1.02, p, p, tile=8)
+    assert not flags.any()
+    # noise in the split widens the bound: the same 5% shift stays denoised
+    noisy = p * (1.0 + rng.normal(0.0, 2.0, p.shape))
+    out, flags = odn.tile_fallback(p * 1.05, p, noisy, tile=8)
+    assert not flags.any()
 
 
 # ----------------------------------------------------------------------- GPU
@@ -165,13 +172,14 @@ def test_tile_fallback_matches_oracle(den, tile):
     den.set_params(_random_params(14, out_scale=0.3))
     beauty, albedo, nrm, target = _images(8, 1, 72, 104)
     rng = np.random.default_rng(9)
-    half = (target[0] * rng.exponential(1.0, target[0].shape)).astype(np.float32)
-    # left columns: a split buffer without noise, so any residual sends the tile back
+    # left columns: a split buffer without noise (only the 1% floor bounds the shift);
+    # right columns: a very noisy split whose bound no shift of the network reaches
+    half = (beauty[0] * (1.0 + 10.0 * rng.normal(size=beauty[0].shape))).astype(np.float32)
     half[:, :40] = beauty[0][:, :40]
     d, _ = den.denoise(beauty[0], albedo[0], nrm[0])
-    out, flags = den.denoise(beauty[0], albedo[0], nrm[0], beauty_half=half, tile=tile, threshold=1.5)
-    ref_out, ref_flags = odn.tile_fallback(d, beauty[0], half, tile=tile, threshold=1.5)
-    margin = odn.tile_margin(d, beauty[0], half, tile=tile, threshold=1.5)
+    out, flags = den.denoise(beauty[0], albedo[0], nrm[0], beauty_half=half, tile=tile, threshold=3.0)
+    ref_out, ref_flags = odn.tile_fallback(d, beauty[0], half, tile=tile, threshold=3.0)
+    margin = odn.tile_margin(d, beauty[0], half, tile=tile, threshold=3.0)
     decided = margin > 1e-4
     print(f"tile {tile}: {int(ref_flags.sum())} of {ref_flags.size} tiles fall back")
     assert 0 < ref_flags.sum() < ref_flags.size  # both outcomes are exercised
@@ -191,10 +199,12 @@ def test_training_reduces_loss(gpu_context):
     try:
         beauty, albedo, nrm, target = _images(10, 4, 64, 64)
         dev = [torch.from_numpy(a).cuda() for a in (beauty, albedo, nrm, target)]
-        losses = [d.train_step(dev[0], dev[3], dev[1], dev[2], lr=2e-3) for _ in range(60)]
-        print(f"loss {losses[0]:.4f} -> {losses[-1]:.4f}")
+        # the weight gradients are summed with atomics, so runs differ in the last bits and
+        # the trajectories drift apart: the bound leaves room for that
+        losses = [d.train_step(dev[0], dev[3], dev[1], dev[2], lr=2e-3) for _ in range(120)]
+        print(f"loss {losses[0]:.4f} -> {np.mean(losses[-10:]):.4f}")
         assert all(np.isfinite(losses))
-        assert losses[-1] < 0.6 * losses[0]
+        assert np.mean(losses[-10:]) < 0.7 * losses[0]
     finally:
         d.close()
 
@@ -218,3 +228,35 @@ def test_invalid_arguments_are_rejected(den):
         den.denoise(img, beauty_half=img, tile=2)
     with pytest.raises(GartusError, match="threshold"):
         den.denoise(img, beauty_half=img, threshold=-1.0)
+
+
+def test_committed_weights_file():
+    import struct
+    raw = dn.DEFAULT_WEIGHTS.read_bytes()
+    assert raw[:8] == dn.WEIGHTS_MAGIC
+    (n,) = struct.unpack("<Q", raw[8:16])
+    assert n == dn.param_count() and len(raw) == 16 + 4 * n
+    assert np.all(np.isfinite(np.frombuffer(raw[16:], dtype="<f4")))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [100000, 100001, 100002])
+def test_trained_denoiser_beats_plain(gpu_context, seed):
+    """The committed network (trained on scenes 0..383 of training_scene) on held-out
+    scenes of each family at 8 spp, against an independent 1024-spp render: the denoised
+    image's relMSE is at most a fifth of the plain render's, and the per-tile fallback
+    keeps nearly all of the gain."""
+    from gartus_gb300.raytracing import PathTracer
+
+    d = dn.Denoiser.pretrained(context=gpu_context)
+    try:
+        ts = dn.training_scene(seed, 256)
+        target = PathTracer(ts.camera.with_samples_per_pixel(1024).with_rng_seed(99),
+                            context=gpu_context)._render(ts.scene, ts.lights, ts.environment).pixels
+        r = dn.evaluate(d, ts, 8, target, seed, context=gpu_context)
+        print(f"scene {seed}: " + ", ".join(f"{k} {v:.4g}" for k, v in r.items()))
+        assert r["denoised"] <= 0.2 * r["plain"]
+        assert r["fallback"] <= 0.2 * r["plain"]
+        assert r["fallback_tiles"] <= r["tiles"] // 8
+    finally:
+        d.close()
