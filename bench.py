@@ -218,6 +218,35 @@ def run_denoise(args):
         return
     ctx = Context(local if world > 1 else 0)
     width = args.width or 1920
+    height = width * 1080 // 1920
+    den = Denoiser.pretrained(context=ctx)
+    gen = torch.Generator(device="cpu").manual_seed(5)
+    frame = [torch.rand((height, width, 3), generator=gen).cuda() for _ in range(3)]
+    half = (frame[0] * 0.9).contiguous()
+    if args.profile_run:  # denoise warmup+steps frames for an ncu capture; no timing, no output
+        for _ in range(args.warmup + args.steps):
+            den.denoise(frame[0], frame[1], frame[2], beauty_half=half)
+        torch.cuda.synchronize()
+        return
+    # Inference roofline: tensor-core FLOPs of one frame (2 * pixels * 9 * cin * cout per
+    # layer, padded channels included) over its time with device buffers.
+    for _ in range(3):
+        den.denoise(frame[0], frame[1], frame[2], beauty_half=half)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 10
+    for _ in range(reps):
+        den.denoise(frame[0], frame[1], frame[2], beauty_half=half)
+    torch.cuda.synchronize()
+    infer_s = (time.perf_counter() - t0) / reps
+    from gartus_gb300.denoiser import layer_shapes
+    hp, wp = (height + 15) // 16 * 16, (width + 15) // 16 * 16
+    lv = [0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 3, 3, 2, 2, 1, 1, 0, 0, 0]
+    flops = sum(2.0 * (hp >> l) * (wp >> l) * 9 * ((cin + 15) // 16 * 16) * ((cout + 7) // 8 * 8)
+                for l, (cin, cout, _) in zip(lv, layer_shapes()))
+    pk = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    bf16_peak = float(pk.get("bf16_tflops", 1900.0))
+    achieved = flops / infer_s / 1e12
     if args.scene == "mesh":
         scene, env = scenes.mesh_heavy_scene()
         lights = None
@@ -230,7 +259,6 @@ def run_denoise(args):
         wl = {"workload": "cornell_box_ggx_glass_1080p", "max_depth": 50}
     cam = cam.with_pixel_sample_mode(abi.GT_SAMPLE_RANDOM).with_samples_per_pixel(1)
     w, h, _ = cam.image_size()
-    den = Denoiser.pretrained(context=ctx)
     log = (lambda m: print(m, file=sys.stderr, flush=True))
     with ClockSampler(ctx.device) as clocks:
         r = convergence_sweep(den, scene, cam, lights, env, target_spp=args.target_spp, max_spp=args.max_spp,
@@ -255,6 +283,12 @@ def run_denoise(args):
         "denoised_spp": r["denoised"]["spp"] if r["denoised"] else None,
         "speedup": r["speedup"], "best_denoised_relmse": r["best_denoised"],
         "reference_error": r["reference_error"], "clocks": clocks.summary(),
+        "roofline": {"bound": "tensor", "kernel": "denoiser inference (19 k_conv_fwd + elementwise)",
+                     "achieved": achieved, "peak": bf16_peak,
+                     "peak_kind": "measured" if pk else "fallback", "unit": "TFLOP/s",
+                     "frac": achieved / bf16_peak, "traffic": None, "flops_per_frame": flops,
+                     "frame_ms": infer_s * 1e3, "frame": f"{width}x{height} (padded {wp}x{hp})"},
+        "gpu_launches": None,
         "curve": r["curve"],
     }
     print(json.dumps(line))
