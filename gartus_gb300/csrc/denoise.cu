@@ -107,6 +107,7 @@ struct gt_denoiser {
     float *dn = nullptr, *res = nullptr;
     uint8_t* flags = nullptr;
     uint32_t* flag_count = nullptr;
+    uint32_t* err = nullptr; // set by a tensor-core kernel whose mbarrier wait gave up
 };
 
 namespace {
@@ -206,10 +207,22 @@ gt_status refresh_weights(gt_denoiser* d, cudaStream_t st) {
     return GT_OK;
 }
 
+// Largest shared-memory request of a tensor-core convolution (N = 176: the input gradient
+// of the deepest decoder layer).
+constexpr int kTcSmemMax = tc_smem_bytes(176);
+
+void launch_conv_tc(gt_denoiser* d, ConvTc a, cudaStream_t st) {
+    a.n_mma = (a.cout_p + 15) / 16 * 16;
+    a.tmem_cols = uint32_t(tc_tmem_cols(a.n_mma));
+    a.err = d->err;
+    const int grid = (a.w + kTcM - 1) / kTcM * a.h * a.n;
+    k_conv_fwd_tc<<<grid, 128, tc_smem_bytes(a.n_mma), st>>>(a);
+}
+
 void conv(gt_denoiser* d, int li, const __nv_bfloat16* x, __nv_bfloat16* y, int ldy, float* yf, const float* res,
           int lv, cudaStream_t st) {
     const Layer& l = d->layers[li];
-    ConvFwd a;
+    ConvTc a;
     std::memset(&a, 0, sizeof(a));
     a.x = x;
     a.cin = l.cin_p;
@@ -225,14 +238,14 @@ void conv(gt_denoiser* d, int li, const __nv_bfloat16* x, __nv_bfloat16* y, int 
     a.n = d->n;
     a.h = d->h >> lv;
     a.w = d->w >> lv;
-    const dim3 grid((a.w + kTile - 1) / kTile * a.h * a.n, (l.cout_p + kNChunk - 1) / kNChunk);
-    k_conv_fwd<<<grid, 128, 0, st>>>(a);
+    launch_conv_tc(d, a, st);
 }
 
-// Input gradient: the forward kernel over dY with the flipped weights, no bias or ReLU.
+// Input gradient: the same convolution over dY with the flipped, transposed weights, no
+// bias or ReLU.
 void conv_dgrad(gt_denoiser* d, int li, const __nv_bfloat16* dy, __nv_bfloat16* dx, int lv, cudaStream_t st) {
     const Layer& l = d->layers[li];
-    ConvFwd a;
+    ConvTc a;
     std::memset(&a, 0, sizeof(a));
     a.x = dy;
     a.cin = l.cout_pp;
@@ -244,8 +257,15 @@ void conv_dgrad(gt_denoiser* d, int li, const __nv_bfloat16* dy, __nv_bfloat16* 
     a.n = d->n;
     a.h = d->h >> lv;
     a.w = d->w >> lv;
-    const dim3 grid((a.w + kTile - 1) / kTile * a.h * a.n, (l.cin_p + kNChunk - 1) / kNChunk);
-    k_conv_fwd<<<grid, 128, 0, st>>>(a);
+    launch_conv_tc(d, a, st);
+}
+
+gt_status check_err(gt_denoiser* d, cudaStream_t st) {
+    cudaError_t e = cudaMemcpyAsync(d->ctx->pinned, d->err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "denoiser");
+    if (d->ctx->pinned[0]) return fail(GT_ERR_TIMEOUT, "denoiser tensor-core pipeline wait timed out");
+    return GT_OK;
 }
 
 void conv_wgrad(gt_denoiser* d, int li, const __nv_bfloat16* dy, const __nv_bfloat16* x, int lv, cudaStream_t st) {
@@ -405,6 +425,9 @@ gt_status gt_denoiser_create(gt_context* ctx, uint64_t seed, gt_denoiser** out) 
     al(reinterpret_cast<void**>(&d->v), d->nparams * sizeof(float));
     al(reinterpret_cast<void**>(&d->g), d->nparams * sizeof(float));
     al(reinterpret_cast<void**>(&d->dbp), d->nparams * sizeof(float));
+    al(reinterpret_cast<void**>(&d->err), sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_conv_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemMax);
     d->wb.assign(d->layers.size(), nullptr);
     d->wf.assign(d->layers.size(), nullptr);
     d->dwp.assign(d->layers.size(), nullptr);
@@ -435,6 +458,7 @@ void gt_denoiser_destroy(gt_denoiser* d) {
     cudaFree(d->v);
     cudaFree(d->g);
     cudaFree(d->dbp);
+    cudaFree(d->err);
     for (auto* p : d->wb) cudaFree(p);
     for (auto* p : d->wf) cudaFree(p);
     for (auto* p : d->dwp) cudaFree(p);
@@ -492,6 +516,7 @@ gt_status gt_denoiser_train_step(gt_denoiser* d, const float* beauty, const floa
     if ((rc = refresh_weights(d, st)) != GT_OK) return rc;
     const int sms = d->ctx->num_sms > 0 ? d->ctx->num_sms : 1;
     const long long P = (long long)n * h * w;
+    cudaMemsetAsync(d->err, 0, sizeof(uint32_t), st);
     k_pack_input<<<grid_for(P, 256, sms), 256, 0, st>>>(beauty, albedo, normal, int(n), int(h), int(w), int(h),
                                                          int(w), d->x0, d->lb);
     forward(d, st);
@@ -512,6 +537,7 @@ gt_status gt_denoiser_train_step(gt_denoiser* d, const float* beauty, const floa
         e = cudaMemcpyAsync(grad, d->g, d->nparams * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "denoiser training step");
+    if ((rc = check_err(d, st)) != GT_OK) return rc;
     if (loss) *loss = l;
     return GT_OK;
     GT_GUARD_END
@@ -556,6 +582,7 @@ gt_status gt_denoise(gt_denoiser* d, const gt_denoise_input* in, uint32_t tile, 
     }
     float* result = in->device_buffers ? out : d->res;
     const int sms = d->ctx->num_sms > 0 ? d->ctx->num_sms : 1;
+    cudaMemsetAsync(d->err, 0, sizeof(uint32_t), st);
     k_pack_input<<<grid_for((long long)hp * wp, 256, sms), 256, 0, st>>>(beauty, albedo, normal, 1, int(h), int(w), hp,
                                                                           wp, d->x0, d->lb);
     forward(d, st);
@@ -574,6 +601,7 @@ gt_status gt_denoise(gt_denoiser* d, const gt_denoise_input* in, uint32_t tile, 
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "denoise");
     if (half) count = d->ctx->pinned[0];
+    if ((rc = check_err(d, st)) != GT_OK) return rc;
     if (!half && tile_fallback) std::memset(tile_fallback, 0, size_t(tiles));
     if (fallback_count) *fallback_count = count;
     return GT_OK;

@@ -2,10 +2,11 @@
 // the beauty / albedo / normal AOVs (render_denoising_aovs, renderer.rs:121-129).
 //
 // Tensors are NHWC.  Activations and weights are BF16; every product is accumulated in FP32
-// by the tensor cores (mma.sync m16n8k16, BF16 inputs, FP32 accumulators).  A 3x3 conv is an
-// implicit GEMM: M = pixels, N = output channels, K = 9 taps x input channels.  Its input
-// gradient is the same GEMM with the taps flipped and the channel roles swapped; its weight
-// gradient is a GEMM over pixels (M = output channels, N = input channels, K = pixels).
+// on the tensor cores.  A 3x3 conv is an implicit GEMM: M = pixels, N = output channels,
+// K = 9 taps x input channels (k_conv_fwd_tc: tcgen05.mma with the accumulator in tensor
+// memory).  Its input gradient is the same GEMM with the taps flipped and the channel roles
+// swapped; its weight gradient is a GEMM over pixels (M = output channels, N = input
+// channels, K = pixels; k_conv_wgrad, mma.sync m16n8k16).
 #pragma once
 
 #include <cuda_bf16.h>
@@ -14,9 +15,6 @@
 
 namespace gt {
 namespace dn {
-
-constexpr int kTile = 64;    // pixels per conv block (4 warps x 16)
-constexpr int kNChunk = 96;  // output channels per conv block (12 n8 tiles)
 
 __device__ __forceinline__ uint32_t lane() { return threadIdx.x & 31u; }
 
@@ -40,71 +38,216 @@ __device__ __forceinline__ uint32_t ld2(const __nv_bfloat16* t, int c_stride, in
     return __ldg(reinterpret_cast<const unsigned int*>(t + ((size_t(n) * h + y) * w + x) * c_stride + c));
 }
 
-struct ConvFwd {
-    const __nv_bfloat16* x;  // [n][h][w][cin]
-    int cin;                 // multiple of 16
+// ------------------------------------------------------------ tcgen05 convolution
+// The same 3x3 convolution on the 5th-generation tensor cores: one CTA computes 128
+// consecutive pixels of one image row (M = 128) for all N output channels, accumulating
+// D[pixel][co] in tensor memory (TMEM, FP32, one column per output channel).  K runs over
+// 16-channel chunks of the input; each chunk is staged once in shared memory as
+//   A: the 3 input rows y-1, y, y+1, pixels x0-1 .. x0+128 (130 staged rows per input row),
+//   B: the chunk's weights for all 9 taps,
+// in the K-major no-swizzle core-matrix layout (8 rows x 16 bytes per core matrix).  The
+// A rows of one input row are laid out contiguously at 16 bytes per pixel within each
+// 8-channel half, so the operand of horizontal tap dx is the same tile with its start
+// address moved by (dx + 1) x 16 bytes: 9 MMAs per chunk read 3 staged rows.  Two stages
+// overlap the next chunk's loads (cp.async, zero-filled outside the image) with the MMAs,
+// which one thread issues and commits to a per-stage mbarrier.
+constexpr int kTcM = 128;                     // pixels per CTA (MMA M)
+constexpr int kTcRows = 136;                  // staged pixels per input row (130 used)
+constexpr int kTcRowBytes = kTcRows * 16;     // one 8-channel half of one staged row
+constexpr int kTcATile = 2 * kTcRowBytes;     // one input row, 16 channels
+constexpr int kTcABytes = 3 * kTcATile;       // three input rows
+constexpr uint32_t kTcWaitLimit = 1u << 22;   // mbarrier polls before giving up
+
+__host__ __device__ constexpr int tc_stage_bytes(int n) { return (kTcABytes + 9 * n * 32 + 127) / 128 * 128; }
+__host__ __device__ constexpr int tc_smem_bytes(int n) { return 128 + 2 * tc_stage_bytes(n); }
+inline int tc_tmem_cols(int n) { return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : 256; }
+
+struct ConvTc {
+    const __nv_bfloat16* x; // [n][h][w][cin]
+    int cin;                // multiple of 16
     const __nv_bfloat16* wt; // [cout_p][9][cin]
-    const float* bias;       // [cout] or null
-    int cout_p;              // multiple of 8 (rows of wt)
-    int cout;                // channels stored
-    __nv_bfloat16* y;        // [n][h][w][ldy] at channel offset yoff, or null
+    const float* bias;      // [cout] or null
+    int cout_p;             // rows of wt
+    int n_mma;              // MMA N: cout_p rounded up to 16 (rows >= cout_p are zero)
+    int cout;               // channels stored
+    __nv_bfloat16* y;       // [n][h][w][ldy] at channel offset yoff, or null
     int ldy, yoff;
-    float* yf;               // [n][h][w][cout] FP32 output, or null
-    const float* res;        // FP32 residual added to yf ([n][h][w][cout]), or null
+    float* yf;              // [n][h][w][cout] FP32 output, or null
+    const float* res;       // FP32 residual added to yf, or null
     int relu;
     int n, h, w;
+    uint32_t tmem_cols;     // TMEM columns allocated (power of two >= n_mma, >= 32)
+    uint32_t* err;          // set to 1 if an mbarrier wait gave up
 };
 
-// One block: 64 consecutive pixels of one image row x up to 96 output channels.
-__global__ void __launch_bounds__(128) k_conv_fwd(ConvFwd a) {
-    const int segs = (a.w + kTile - 1) / kTile;
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+
+// Shared-memory matrix descriptor (K-major, no swizzle): start, leading-dimension byte
+// offset (between core matrices adjacent in K), stride byte offset (between 8-row groups),
+// descriptor version 1 at bits 46-47, layout type 0 (no swizzle) at bits 61-63.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return uint64_t((addr >> 4) & 0x3FFFu) | (uint64_t((lbo >> 4) & 0x3FFFu) << 16) |
+           (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (uint64_t(1) << 46);
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator (bits 4-5 = 1), A and B BF16 (bits
+// 7-9 and 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+__device__ __forceinline__ uint32_t tc_idesc(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(kTcM >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: false (and *err = 1) if the phase did not complete within the limit.
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity, uint32_t* err) {
+    for (uint32_t i = 0; i < kTcWaitLimit; ++i)
+        if (mbar_try_wait(addr, parity)) return true;
+    atomicOr(err, 1u);
+    return false;
+}
+
+__global__ void __launch_bounds__(128) k_conv_fwd_tc(ConvTc a) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 16);
+    const int N = a.n_mma;
+    const int stage_bytes = tc_stage_bytes(N);
+    uint8_t* stage_base = smem + 128;
+    const int segs = (a.w + kTcM - 1) / kTcM;
     const int seg = blockIdx.x % segs, row = blockIdx.x / segs;
-    const int y = row % a.h, n = row / a.h;
-    const int warp = threadIdx.x >> 5, g = lane() >> 2, t = lane() & 3;
-    const int x0 = seg * kTile + warp * 16;
-    const int co0 = blockIdx.y * kNChunk;
-    const int ntiles = min(kNChunk, a.cout_p - co0) / 8;
-    float acc[12][4];
+    const int y = row % a.h, img = row / a.h;
+    const int x0 = seg * kTcM;
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                     "r"(a.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    auto load_chunk = [&](int c, int s) {
+        uint8_t* A = stage_base + s * stage_bytes;
+        uint8_t* B = A + kTcABytes;
+        const uint32_t a_base = smem_u32(A), b_base = smem_u32(B);
+        // A: 3 input rows x 130 pixels x 2 halves of 8 channels
+        for (int i = tid; i < 3 * 130 * 2; i += blockDim.x) {
+            const int dyi = i / 260, rem = i % 260, r = rem >> 1, half = rem & 1;
+            const int px = x0 - 1 + r, py = y + dyi - 1;
+            const bool ok = px >= 0 && px < a.w && py >= 0 && py < a.h;
+            const __nv_bfloat16* src =
+                ok ? a.x + ((size_t(img) * a.h + py) * a.w + px) * a.cin + c * 16 + half * 8 : a.x;
+            cp_async16(a_base + dyi * kTcATile + half * kTcRowBytes + r * 16, src, ok ? 16u : 0u);
+        }
+        // B: 9 taps x N rows x 2 halves
+        for (int i = tid; i < 9 * N * 2; i += blockDim.x) {
+            const int tap = i / (2 * N), rem = i % (2 * N), nr = rem >> 1, half = rem & 1;
+            const bool ok = nr < a.cout_p;
+            const __nv_bfloat16* src = ok ? a.wt + (size_t(nr) * 9 + tap) * a.cin + c * 16 + half * 8 : a.wt;
+            cp_async16(b_base + tap * N * 32 + half * N * 16 + nr * 16, src, ok ? 16u : 0u);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+
+    const int nchunks = a.cin / 16;
+    const uint32_t idesc = tc_idesc(N);
+    bool ok = true;
+    load_chunk(0, 0);
+    for (int c = 0; c < nchunks && ok; ++c) {
+        const int s = c & 1;
+        if (c + 1 < nchunks) {
+            const int s1 = (c + 1) & 1;
+            if (c + 1 >= 2) ok = mbar_wait(smem_u32(&mbar[s1]), uint32_t(((c - 1) >> 1) & 1), a.err);
+            if (__syncthreads_or(!ok)) {
+                ok = false;
+                break;
+            }
+            load_chunk(c + 1, s1);
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t A = smem_u32(stage_base + s * stage_bytes), B = A + kTcABytes;
+            for (int tap = 0; tap < 9; ++tap) {
+                const int dyi = tap / 3, dxi = tap % 3;
+                const uint64_t ad = tc_desc(A + dyi * kTcATile + dxi * 16, kTcRowBytes, 128);
+                const uint64_t bd = tc_desc(B + tap * N * 32, N * 16, 128);
+                const uint32_t acc = (c > 0 || tap > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smem_u32(&mbar[s]))
+                         : "memory");
+        }
+    }
+    if (ok) {
+        const int last = nchunks - 1;
+        ok = mbar_wait(smem_u32(&mbar[last & 1]), uint32_t((last >> 1) & 1), a.err);
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    if (__syncthreads_or(!ok) == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        // Epilogue: thread t owns D row t (TMEM lane t): pixel x0 + t.
+        const int px = x0 + tid;
+        const size_t p = (size_t(img) * a.h + y) * a.w + px;
+        for (int cb = 0; cb < N; cb += 16) {
+            uint32_t r[16];
+            const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(cb);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];\n"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(taddr)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (px < a.w) {
 #pragma unroll
-    for (int j = 0; j < 12; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-    for (int tap = 0; tap < 9; ++tap) {
-        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-        for (int c0 = 0; c0 < a.cin; c0 += 16) {
-            uint32_t fa[4];
-            fa[0] = ld2(a.x, a.cin, n, y + dy, x0 + g + dx, a.h, a.w, c0 + 2 * t);
-            fa[1] = ld2(a.x, a.cin, n, y + dy, x0 + g + 8 + dx, a.h, a.w, c0 + 2 * t);
-            fa[2] = ld2(a.x, a.cin, n, y + dy, x0 + g + dx, a.h, a.w, c0 + 2 * t + 8);
-            fa[3] = ld2(a.x, a.cin, n, y + dy, x0 + g + 8 + dx, a.h, a.w, c0 + 2 * t + 8);
-#pragma unroll
-            for (int j = 0; j < 12; ++j) {
-                if (j >= ntiles) break;
-                const __nv_bfloat16* wr = a.wt + (size_t(co0 + j * 8 + g) * 9 + tap) * a.cin + c0 + 2 * t;
-                uint32_t fb[2];
-                fb[0] = __ldg(reinterpret_cast<const unsigned int*>(wr));
-                fb[1] = __ldg(reinterpret_cast<const unsigned int*>(wr + 8));
-                mma_bf16(acc[j], fa, fb);
+                for (int j = 0; j < 16; ++j) {
+                    const int co = cb + j;
+                    if (co >= a.cout) break;
+                    float v = __uint_as_float(r[j]) + (a.bias ? a.bias[co] : 0.f);
+                    if (a.relu) v = fmaxf(v, 0.f);
+                    if (a.y) a.y[p * a.ldy + a.yoff + co] = __float2bfloat16(v);
+                    if (a.yf) a.yf[p * a.cout + co] = v + (a.res ? a.res[p * a.cout + co] : 0.f);
+                }
             }
         }
     }
-#pragma unroll
-    for (int j = 0; j < 12; ++j) {
-        if (j >= ntiles) break;
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            const int x = x0 + g + 8 * half;
-            if (x >= a.w) continue;
-            const size_t p = (size_t(n) * a.h + y) * a.w + x;
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-                const int co = co0 + j * 8 + 2 * t + e;
-                if (co >= a.cout) continue;
-                float v = acc[j][2 * half + e] + (a.bias ? a.bias[co] : 0.f);
-                if (a.relu) v = fmaxf(v, 0.f);
-                if (a.y) a.y[p * a.ldy + a.yoff + co] = __float2bfloat16(v);
-                if (a.yf) a.yf[p * a.cout + co] = v + (a.res ? a.res[p * a.cout + co] : 0.f);
-            }
-        }
-    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
 }
 
 // dW[co][tap][ci] += sum_p dY[p][co] * X[p + tap][ci]; one block per (tap, pixel range).
