@@ -207,16 +207,34 @@ gt_status refresh_weights(gt_denoiser* d, cudaStream_t st) {
     return GT_OK;
 }
 
-// Largest shared-memory request of a tensor-core convolution (N = 176: the input gradient
-// of the deepest decoder layer).
-constexpr int kTcSmemMax = tc_smem_bytes(176);
+// Tile shape of a tensor-core convolution with N output channels: rows per CTA (each row's
+// accumulator takes a power-of-two range of TMEM columns, at most 512 in all) and pipeline
+// stages (2 while two CTAs fit in an SM's tensor memory, else 3).
+struct TcShape {
+    int rows, stride, stages;
+};
+constexpr TcShape tc_shape(int n) {
+    return TcShape{tc_pow2_cols(n) <= 128 ? 4 : 2, tc_pow2_cols(n),
+                   (tc_pow2_cols(n) <= 128 ? 4 : 2) * tc_pow2_cols(n) <= 256 ? 2 : 3};
+}
+// Largest shared-memory request (N = 176, the input gradient of the deepest decoder layer,
+// and N = 96).
+constexpr int kTcSmemMax =
+    tc_smem_bytes(176, tc_shape(176).rows, tc_shape(176).stages) > tc_smem_bytes(96, tc_shape(96).rows, tc_shape(96).stages)
+        ? tc_smem_bytes(176, tc_shape(176).rows, tc_shape(176).stages)
+        : tc_smem_bytes(96, tc_shape(96).rows, tc_shape(96).stages);
+static_assert(kTcSmemMax <= 227 * 1024, "tensor-core convolution needs more shared memory than a CTA has");
 
 void launch_conv_tc(gt_denoiser* d, ConvTc a, cudaStream_t st) {
     a.n_mma = (a.cout_p + 15) / 16 * 16;
-    a.tmem_cols = uint32_t(tc_tmem_cols(a.n_mma));
+    const TcShape sh = tc_shape(a.n_mma);
+    a.rows = sh.rows;
+    a.acc_stride = sh.stride;
+    a.stages = sh.stages;
+    a.tmem_cols = uint32_t(sh.rows * sh.stride);
     a.err = d->err;
-    const int grid = (a.w + kTcM - 1) / kTcM * a.h * a.n;
-    k_conv_fwd_tc<<<grid, 128, tc_smem_bytes(a.n_mma), st>>>(a);
+    const int grid = (a.w + kTcM - 1) / kTcM * ((a.h + a.rows - 1) / a.rows) * a.n;
+    k_conv_fwd_tc<<<grid, 128, tc_smem_bytes(a.n_mma, a.rows, a.stages), st>>>(a);
 }
 
 void conv(gt_denoiser* d, int li, const __nv_bfloat16* x, __nv_bfloat16* y, int ldy, float* yf, const float* res,

@@ -39,28 +39,35 @@ __device__ __forceinline__ uint32_t ld2(const __nv_bfloat16* t, int c_stride, in
 }
 
 // ------------------------------------------------------------ tcgen05 convolution
-// The same 3x3 convolution on the 5th-generation tensor cores: one CTA computes 128
-// consecutive pixels of one image row (M = 128) for all N output channels, accumulating
-// D[pixel][co] in tensor memory (TMEM, FP32, one column per output channel).  K runs over
-// 16-channel chunks of the input; each chunk is staged once in shared memory as
-//   A: the 3 input rows y-1, y, y+1, pixels x0-1 .. x0+128 (130 staged rows per input row),
+// The 3x3 convolution on the 5th-generation tensor cores.  One CTA computes R consecutive
+// output rows (R = 4, or 2 for wide layers) of 128 consecutive pixels (M = 128 per MMA)
+// for all N output channels, each row's D[pixel][co] accumulating in its own range of
+// tensor-memory columns (FP32).  K runs over 16-channel chunks of the input; each chunk is
+// staged once in shared memory as
+//   A: the R + 2 input rows y0-1 .. y0+R, pixels x0-1 .. x0+128 (130 staged rows per input
+//      row),
 //   B: the chunk's weights for all 9 taps,
 // in the K-major no-swizzle core-matrix layout (8 rows x 16 bytes per core matrix).  The
-// A rows of one input row are laid out contiguously at 16 bytes per pixel within each
+// staged pixels of one input row are contiguous at 16 bytes per pixel within each
 // 8-channel half, so the operand of horizontal tap dx is the same tile with its start
-// address moved by (dx + 1) x 16 bytes: 9 MMAs per chunk read 3 staged rows.  Two stages
-// overlap the next chunk's loads (cp.async, zero-filled outside the image) with the MMAs,
-// which one thread issues and commits to a per-stage mbarrier.
-constexpr int kTcM = 128;                     // pixels per CTA (MMA M)
+// address moved by (dx + 1) x 16 bytes, and vertical tap dy of output row r is staged row
+// r + dy + 1: 9R MMAs per chunk read R + 2 staged rows and one set of weights.  Two or three
+// stages overlap the next chunks' loads (cp.async, zero-filled outside the image) with the
+// MMAs, which one thread issues and commits to a per-stage mbarrier.
+constexpr int kTcM = 128;                     // pixels per MMA
 constexpr int kTcRows = 136;                  // staged pixels per input row (130 used)
 constexpr int kTcRowBytes = kTcRows * 16;     // one 8-channel half of one staged row
 constexpr int kTcATile = 2 * kTcRowBytes;     // one input row, 16 channels
-constexpr int kTcABytes = 3 * kTcATile;       // three input rows
+constexpr int kTcMaxStages = 3;
 constexpr uint32_t kTcWaitLimit = 1u << 22;   // mbarrier polls before giving up
 
-__host__ __device__ constexpr int tc_stage_bytes(int n) { return (kTcABytes + 9 * n * 32 + 127) / 128 * 128; }
-__host__ __device__ constexpr int tc_smem_bytes(int n) { return 128 + 2 * tc_stage_bytes(n); }
-inline int tc_tmem_cols(int n) { return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : 256; }
+__host__ __device__ constexpr int tc_stage_bytes(int n, int rows) {
+    return ((rows + 2) * kTcATile + 9 * n * 32 + 127) / 128 * 128;
+}
+__host__ __device__ constexpr int tc_smem_bytes(int n, int rows, int stages) {
+    return 128 + stages * tc_stage_bytes(n, rows);
+}
+__host__ __device__ constexpr int tc_pow2_cols(int n) { return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : 256; }
 
 struct ConvTc {
     const __nv_bfloat16* x; // [n][h][w][cin]
@@ -76,7 +83,10 @@ struct ConvTc {
     const float* res;       // FP32 residual added to yf, or null
     int relu;
     int n, h, w;
-    uint32_t tmem_cols;     // TMEM columns allocated (power of two >= n_mma, >= 32)
+    int rows;               // output rows per CTA (R)
+    int acc_stride;         // TMEM columns per row accumulator (power of two >= n_mma)
+    int stages;             // 2 or 3
+    uint32_t tmem_cols;     // TMEM columns allocated (rows * acc_stride)
     uint32_t* err;          // set to 1 if an mbarrier wait gave up
 };
 
@@ -84,6 +94,12 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__
 
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t bytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_pending(int pending) {
+    if (pending <= 0) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    else if (pending == 1) asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    else asm volatile("cp.async.wait_group 2;\n" ::: "memory");
 }
 
 // Shared-memory matrix descriptor (K-major, no swizzle): start, leading-dimension byte
@@ -120,15 +136,15 @@ __device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity, uint32
 
 __global__ void __launch_bounds__(128) k_conv_fwd_tc(ConvTc a) {
     extern __shared__ __align__(128) uint8_t smem[];
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 16);
-    const int N = a.n_mma;
-    const int stage_bytes = tc_stage_bytes(N);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem); // kTcMaxStages barriers
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 64);
+    const int N = a.n_mma, R = a.rows, S = a.stages;
+    const int stage_bytes = tc_stage_bytes(N, R);
+    const int a_bytes = (R + 2) * kTcATile;
     uint8_t* stage_base = smem + 128;
-    const int segs = (a.w + kTcM - 1) / kTcM;
-    const int seg = blockIdx.x % segs, row = blockIdx.x / segs;
-    const int y = row % a.h, img = row / a.h;
-    const int x0 = seg * kTcM;
+    const int segs = (a.w + kTcM - 1) / kTcM, groups = (a.h + R - 1) / R;
+    const int seg = blockIdx.x % segs, rg = (blockIdx.x / segs) % groups, img = blockIdx.x / (segs * groups);
+    const int y0 = rg * R, x0 = seg * kTcM;
     const int tid = threadIdx.x, warp = tid >> 5;
 
     if (warp == 0) {
@@ -138,8 +154,8 @@ __global__ void __launch_bounds__(128) k_conv_fwd_tc(ConvTc a) {
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[0])) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[1])) : "memory");
+        for (int s = 0; s < S; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[s])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -149,16 +165,15 @@ __global__ void __launch_bounds__(128) k_conv_fwd_tc(ConvTc a) {
 
     auto load_chunk = [&](int c, int s) {
         uint8_t* A = stage_base + s * stage_bytes;
-        uint8_t* B = A + kTcABytes;
-        const uint32_t a_base = smem_u32(A), b_base = smem_u32(B);
-        // A: 3 input rows x 130 pixels x 2 halves of 8 channels
-        for (int i = tid; i < 3 * 130 * 2; i += blockDim.x) {
-            const int dyi = i / 260, rem = i % 260, r = rem >> 1, half = rem & 1;
-            const int px = x0 - 1 + r, py = y + dyi - 1;
+        const uint32_t a_base = smem_u32(A), b_base = a_base + a_bytes;
+        // A: R + 2 input rows x 130 pixels x 2 halves of 8 channels
+        for (int i = tid; i < (R + 2) * 260; i += blockDim.x) {
+            const int ri = i / 260, rem = i % 260, r = rem >> 1, half = rem & 1;
+            const int px = x0 - 1 + r, py = y0 + ri - 1;
             const bool ok = px >= 0 && px < a.w && py >= 0 && py < a.h;
             const __nv_bfloat16* src =
                 ok ? a.x + ((size_t(img) * a.h + py) * a.w + px) * a.cin + c * 16 + half * 8 : a.x;
-            cp_async16(a_base + dyi * kTcATile + half * kTcRowBytes + r * 16, src, ok ? 16u : 0u);
+            cp_async16(a_base + ri * kTcATile + half * kTcRowBytes + r * 16, src, ok ? 16u : 0u);
         }
         // B: 9 taps x N rows x 2 halves
         for (int i = tid; i < 9 * N * 2; i += blockDim.x) {
@@ -173,36 +188,37 @@ __global__ void __launch_bounds__(128) k_conv_fwd_tc(ConvTc a) {
     const int nchunks = a.cin / 16;
     const uint32_t idesc = tc_idesc(N);
     bool ok = true;
-    load_chunk(0, 0);
-    for (int c = 0; c < nchunks && ok; ++c) {
-        const int s = c & 1;
-        if (c + 1 < nchunks) {
-            const int s1 = (c + 1) & 1;
-            if (c + 1 >= 2) ok = mbar_wait(smem_u32(&mbar[s1]), uint32_t(((c - 1) >> 1) & 1), a.err);
+    for (int c = 0; c < S - 1 && c < nchunks; ++c) load_chunk(c, c);
+    for (int c = 0; c < nchunks; ++c) {
+        const int s = c % S, cn = c + S - 1;
+        if (cn < nchunks) {
+            // stage cn % S was last read by chunk cn - S
+            if (cn >= S) ok = mbar_wait(smem_u32(&mbar[cn % S]), uint32_t(((cn - S) / S) & 1), a.err);
             if (__syncthreads_or(!ok)) {
                 ok = false;
                 break;
             }
-            load_chunk(c + 1, s1);
-            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            load_chunk(cn, cn % S);
         }
+        cp_async_wait_pending(min(S - 1, nchunks - 1 - c));
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const uint32_t A = smem_u32(stage_base + s * stage_bytes), B = A + kTcABytes;
+            const uint32_t A = smem_u32(stage_base + s * stage_bytes), B = A + a_bytes;
             for (int tap = 0; tap < 9; ++tap) {
                 const int dyi = tap / 3, dxi = tap % 3;
-                const uint64_t ad = tc_desc(A + dyi * kTcATile + dxi * 16, kTcRowBytes, 128);
                 const uint64_t bd = tc_desc(B + tap * N * 32, N * 16, 128);
                 const uint32_t acc = (c > 0 || tap > 0) ? 1u : 0u;
-                asm volatile(
-                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-                    : "memory");
+                for (int r = 0; r < R; ++r) {
+                    const uint64_t ad = tc_desc(A + (r + dyi) * kTcATile + dxi * 16, kTcRowBytes, 128);
+                    asm volatile(
+                        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                            tmem + uint32_t(r * a.acc_stride)),
+                        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                        : "memory");
+                }
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                              smem_u32(&mbar[s]))
@@ -211,35 +227,56 @@ __global__ void __launch_bounds__(128) k_conv_fwd_tc(ConvTc a) {
     }
     if (ok) {
         const int last = nchunks - 1;
-        ok = mbar_wait(smem_u32(&mbar[last & 1]), uint32_t((last >> 1) & 1), a.err);
+        ok = mbar_wait(smem_u32(&mbar[last % S]), uint32_t((last / S) & 1), a.err);
     }
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     if (__syncthreads_or(!ok) == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        // Epilogue: thread t owns D row t (TMEM lane t): pixel x0 + t.
+        // Epilogue: thread t owns D row t (TMEM lane t) of every row accumulator: pixel x0 + t.
         const int px = x0 + tid;
-        const size_t p = (size_t(img) * a.h + y) * a.w + px;
-        for (int cb = 0; cb < N; cb += 16) {
-            uint32_t r[16];
-            const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(cb);
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                "[%16];\n"
-                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                  "=r"(r[15])
-                : "r"(taddr)
-                : "memory");
-            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-            if (px < a.w) {
+        for (int r = 0; r < R; ++r) {
+            const int y = y0 + r;
+            const size_t p = (size_t(img) * a.h + y) * a.w + px;
+            const bool store = px < a.w && y < a.h;
+            for (int cb = 0; cb < N; cb += 16) {
+                uint32_t v[16];
+                const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(r * a.acc_stride + cb);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+                    "%15}, [%16];\n"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                      "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                      "=r"(v[14]), "=r"(v[15])
+                    : "r"(taddr)
+                    : "memory");
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (!store) continue;
+                if (a.y && !a.yf && cb + 16 <= a.cout && ((a.ldy | a.yoff) & 7) == 0) {
+                    // 16 channels = two 16-byte stores
+                    uint32_t packed[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        float f0 = __uint_as_float(v[2 * j]) + (a.bias ? a.bias[cb + 2 * j] : 0.f);
+                        float f1 = __uint_as_float(v[2 * j + 1]) + (a.bias ? a.bias[cb + 2 * j + 1] : 0.f);
+                        if (a.relu) {
+                            f0 = fmaxf(f0, 0.f);
+                            f1 = fmaxf(f1, 0.f);
+                        }
+                        packed[j] = pack_bf16(__float2bfloat16(f0), __float2bfloat16(f1));
+                    }
+                    uint4* dst = reinterpret_cast<uint4*>(a.y + p * a.ldy + a.yoff + cb);
+                    dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                    dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                    continue;
+                }
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     const int co = cb + j;
                     if (co >= a.cout) break;
-                    float v = __uint_as_float(r[j]) + (a.bias ? a.bias[co] : 0.f);
-                    if (a.relu) v = fmaxf(v, 0.f);
-                    if (a.y) a.y[p * a.ldy + a.yoff + co] = __float2bfloat16(v);
-                    if (a.yf) a.yf[p * a.cout + co] = v + (a.res ? a.res[p * a.cout + co] : 0.f);
+                    float f = __uint_as_float(v[j]) + (a.bias ? a.bias[co] : 0.f);
+                    if (a.relu) f = fmaxf(f, 0.f);
+                    if (a.y) a.y[p * a.ldy + a.yoff + co] = __float2bfloat16(f);
+                    if (a.yf) a.yf[p * a.cout + co] = f + (a.res ? a.res[p * a.cout + co] : 0.f);
                 }
             }
         }
