@@ -238,11 +238,13 @@ void launch_conv_tc(gt_denoiser* d, ConvTc a, cudaStream_t st) {
 }
 
 void conv(gt_denoiser* d, int li, const __nv_bfloat16* x, __nv_bfloat16* y, int ldy, float* yf, const float* res,
-          int lv, cudaStream_t st) {
+          int lv, cudaStream_t st, const __nv_bfloat16* lo = nullptr, int cl = 0) {
     const Layer& l = d->layers[li];
     ConvTc a;
     std::memset(&a, 0, sizeof(a));
     a.x = x;
+    a.lo = lo;
+    a.cl = cl;
     a.cin = l.cin_p;
     a.wt = d->wb[li];
     a.bias = d->p + l.b_off;
@@ -305,8 +307,10 @@ void conv_wgrad(gt_denoiser* d, int li, const __nv_bfloat16* dy, const __nv_bflo
                                                                                   d->dbp + l.b_off);
 }
 
-// Forward pass (inputs already packed); d->out = log-space prediction.
-void forward(gt_denoiser* d, cudaStream_t st) {
+// Forward pass (inputs already packed); d->out = log-space prediction.  Training keeps the
+// decoder's concatenated inputs for the weight gradients; inference reads the upsampled
+// half and the skip straight into the convolution's staging.
+void forward(gt_denoiser* d, cudaStream_t st, bool training) {
     const int sms = d->ctx->num_sms > 0 ? d->ctx->num_sms : 1;
     const __nv_bfloat16* in = d->x0;
     for (int lv = 0; lv < kLevels; ++lv) {
@@ -322,9 +326,13 @@ void forward(gt_denoiser* d, cudaStream_t st) {
     const __nv_bfloat16* lo = d->act[enc_a(kLevels - 1) + 1];
     for (int lv = kLevels - 2; lv >= 0; --lv) {
         const int cl = kCh[lv + 1], cs = kCh[lv], hh = d->h >> lv, ww = d->w >> lv;
-        k_upcat<<<grid_for((long long)d->n * hh * ww * (cl + cs), 256, sms), 256, 0, st>>>(
-            lo, cl, d->act[enc_a(lv) + 1], cs, d->cat[lv], d->n, hh, ww);
-        conv(d, dec_a(lv), d->cat[lv], d->act[dec_a(lv)], kCh[lv], nullptr, nullptr, lv, st);
+        if (training) {
+            k_upcat<<<grid_for((long long)d->n * hh * ww * (cl + cs), 256, sms), 256, 0, st>>>(
+                lo, cl, d->act[enc_a(lv) + 1], cs, d->cat[lv], d->n, hh, ww);
+            conv(d, dec_a(lv), d->cat[lv], d->act[dec_a(lv)], kCh[lv], nullptr, nullptr, lv, st);
+        } else {
+            conv(d, dec_a(lv), d->act[enc_a(lv) + 1], d->act[dec_a(lv)], kCh[lv], nullptr, nullptr, lv, st, lo, cl);
+        }
         conv(d, dec_a(lv) + 1, d->act[dec_a(lv)], d->act[dec_a(lv) + 1], kCh[lv], nullptr, nullptr, lv, st);
         lo = d->act[dec_a(lv) + 1];
     }
@@ -537,7 +545,7 @@ gt_status gt_denoiser_train_step(gt_denoiser* d, const float* beauty, const floa
     cudaMemsetAsync(d->err, 0, sizeof(uint32_t), st);
     k_pack_input<<<grid_for(P, 256, sms), 256, 0, st>>>(beauty, albedo, normal, int(n), int(h), int(w), int(h),
                                                          int(w), d->x0, d->lb);
-    forward(d, st);
+    forward(d, st, true);
     cudaMemsetAsync(d->loss, 0, sizeof(float), st);
     k_l1_log1p<<<grid_for(P, 256, sms), 256, 0, st>>>(d->out, target, P, d->loss, d->gout);
     if ((rc = backward(d, st)) != GT_OK) return rc;
@@ -603,7 +611,7 @@ gt_status gt_denoise(gt_denoiser* d, const gt_denoise_input* in, uint32_t tile, 
     cudaMemsetAsync(d->err, 0, sizeof(uint32_t), st);
     k_pack_input<<<grid_for((long long)hp * wp, 256, sms), 256, 0, st>>>(beauty, albedo, normal, 1, int(h), int(w), hp,
                                                                           wp, d->x0, d->lb);
-    forward(d, st);
+    forward(d, st, false);
     k_unpack_output<<<grid_for(h * w * 3, 256, sms), 256, 0, st>>>(d->out, int(h), int(w), wp, half ? d->dn : result);
     if (half) {
         cudaMemsetAsync(d->flag_count, 0, sizeof(uint32_t), st);

@@ -83,6 +83,8 @@ struct ConvTc {
     const float* res;       // FP32 residual added to yf, or null
     int relu;
     int n, h, w;
+    const __nv_bfloat16* lo; // optional: input channels [0, cl) are the 2x nearest upsampling of
+    int cl;                  // lo ([n][h/2][w/2][cl]) and the rest come from x ([n][h][w][cin - cl])
     int rows;               // output rows per CTA (R)
     int acc_stride;         // TMEM columns per row accumulator (power of two >= n_mma)
     int stages;             // 2 or 3
@@ -171,8 +173,16 @@ __global__ void __launch_bounds__(128) k_conv_fwd_tc(ConvTc a) {
             const int ri = i / 260, rem = i % 260, r = rem >> 1, half = rem & 1;
             const int px = x0 - 1 + r, py = y0 + ri - 1;
             const bool ok = px >= 0 && px < a.w && py >= 0 && py < a.h;
-            const __nv_bfloat16* src =
-                ok ? a.x + ((size_t(img) * a.h + py) * a.w + px) * a.cin + c * 16 + half * 8 : a.x;
+            const int ch = c * 16 + half * 8;
+            const __nv_bfloat16* src = a.x;
+            if (ok) {
+                if (!a.lo)
+                    src = a.x + ((size_t(img) * a.h + py) * a.w + px) * a.cin + ch;
+                else if (ch < a.cl)
+                    src = a.lo + ((size_t(img) * (a.h >> 1) + (py >> 1)) * (a.w >> 1) + (px >> 1)) * a.cl + ch;
+                else
+                    src = a.x + ((size_t(img) * a.h + py) * a.w + px) * (a.cin - a.cl) + (ch - a.cl);
+            }
             cp_async16(a_base + ri * kTcATile + half * kTcRowBytes + r * 16, src, ok ? 16u : 0u);
         }
         // B: 9 taps x N rows x 2 halves
