@@ -630,10 +630,14 @@ gt_status finish_render(gt_context* ctx, const Params<R>& P, gt_frame* frame, co
     return GT_OK;
 }
 
-template <class R>
+// One frame (BATCH = false) or, with BATCH = true, the frames bcams[0 .. bcount) of equal
+// width as one image of their rows stacked in order: every wavefront kernel then looks up
+// each slot's frame camera, and each frame's slice of the result goes to bframes[i].
+template <class R, bool BATCH = false>
 gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost& cam,
                       const gt_render_opts& opts, gt_frame* frame, gt_accumulator* accum = nullptr,
-                      uint32_t add_samples = 0) {
+                      uint32_t add_samples = 0, const CamHost* bcams = nullptr, uint32_t bcount = 0,
+                      gt_frame* const* bframes = nullptr) {
     gt_context* ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     gt_status rc;
@@ -653,22 +657,56 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     }
     P.cam = cam_dev<R>(cam, use_lights, use_env);
     if (accum) P.cam.spp = accum->samples + add_samples; // the streams run on to the new total
-    const uint32_t n = cam.width * cam.height;
-    const bool nee = P.cam.nee && (use_lights || use_env);
+    uint32_t n_pix = cam.width * cam.height;
+    uint32_t img_h = cam.height; // rows the stripes deal out
+    uint32_t limit_max = P.cam.adaptive ? P.cam.adaptive_max : P.cam.spp, depth_max = P.cam.max_depth;
+    bool any_nee = P.cam.nee && (use_lights || use_env), want64 = false;
+    std::vector<CamDev<R>> bcd;
+    std::vector<uint32_t> bstart;
+    if constexpr (BATCH) {
+        bcd.resize(bcount);
+        bstart.resize(size_t(bcount) + 1);
+        uint64_t total = 0;
+        img_h = 0;
+        for (uint32_t i = 0; i < bcount; ++i) {
+            bcd[i] = cam_dev<R>(bcams[i], use_lights, use_env);
+            bstart[i] = uint32_t(total);
+            total += uint64_t(bcams[i].width) * bcams[i].height;
+            if (total >= (1ull << 31)) return fail(GT_ERR_INVALID_ARG, "a batch holds fewer than 2^31 pixels");
+            img_h += bcams[i].height;
+            limit_max = std::max(limit_max, bcd[i].adaptive ? bcd[i].adaptive_max : bcd[i].spp);
+            depth_max = std::max(depth_max, bcd[i].max_depth);
+            any_nee = any_nee || (bcd[i].nee && (use_lights || use_env));
+            want64 = want64 || bframes[i]->rgb64 != nullptr;
+        }
+        bstart[bcount] = uint32_t(total);
+        n_pix = uint32_t(total);
+        P.num_frames = bcount;
+    }
+    const uint32_t n = n_pix;
+    const bool nee = any_nee;
 
     // Workspace: path state (wavefront only), per-stripe queues and counters, and device
     // staging for host outputs.
-    const bool persistent = opts.schedule == GT_SCHEDULE_PERSISTENT && !accum;
-    const bool host_out = frame->device_buffers == 0;
+    const bool persistent = !BATCH && opts.schedule == GT_SCHEDULE_PERSISTENT && !accum;
+    const bool host_out = BATCH || frame->device_buffers == 0;
     // Wavefront stripes: rows are dealt round-robin to K independent wavefronts on their
     // own streams, whose kernels then overlap on the GPU (each kernel alone leaves SMs
     // waiting on memory).
     uint32_t K = opts.stripes ? opts.stripes : 4u;
-    K = std::max<uint32_t>(1u, std::min<uint32_t>({K, uint32_t(gt_context::kMaxStripes), cam.height}));
+    K = std::max<uint32_t>(1u, std::min<uint32_t>({K, uint32_t(gt_context::kMaxStripes), img_h}));
     if (persistent) K = 1;
-    const uint32_t qcap = ((cam.height + K - 1) / K) * cam.width;
+    const uint32_t qcap = ((img_h + K - 1) / K) * cam.width;
     std::vector<Params<R>> SP(K);
+    CamDev<R>* d_cams = nullptr;
+    uint32_t* d_start = nullptr;
     auto lay = [&](Bump& bb) {
+        if constexpr (BATCH) {
+            d_cams = bb.take<CamDev<R>>(bcount);
+            d_start = bb.take<uint32_t>(size_t(bcount) + 1);
+            P.cams = d_cams;
+            P.frame_start = d_start;
+        }
         if (persistent) {
             P.ps.n = n;
             P.ps.counters = bb.take<uint32_t>(C_COUNT);
@@ -682,7 +720,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
                 SP[k].ps.stripe = k;
                 SP[k].ps.stripes = K;
                 SP[k].ps.row = cam.width;
-                SP[k].ps.local_n = ((cam.height - k + K - 1) / K) * cam.width;
+                SP[k].ps.local_n = ((img_h - k + K - 1) / K) * cam.width;
             }
             P.ps.counters = SP[0].ps.counters; // the error word k_resolve-side checks read
         }
@@ -701,11 +739,17 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     float* d_nrm = b.take<float>(size_t(n) * 3);
     double* d_rgb64 = b.take<double>(size_t(n) * 3);
     uint32_t* d_acc = b.take<uint32_t>(n);
-    float* o_rgb = host_out ? d_rgb : frame->rgb;
-    float* o_alb = host_out ? (frame->albedo ? d_alb : nullptr) : frame->albedo;
-    float* o_nrm = host_out ? (frame->normal ? d_nrm : nullptr) : frame->normal;
-    double* o_rgb64 = host_out ? (frame->rgb64 ? d_rgb64 : nullptr) : frame->rgb64;
-    uint32_t* o_acc = host_out ? (frame->accepted ? d_acc : nullptr) : frame->accepted;
+    float* o_rgb = d_rgb;
+    float *o_alb = nullptr, *o_nrm = nullptr;
+    double* o_rgb64 = want64 ? d_rgb64 : nullptr;
+    uint32_t* o_acc = d_acc;
+    if constexpr (!BATCH) {
+        o_rgb = host_out ? d_rgb : frame->rgb;
+        o_alb = host_out ? (frame->albedo ? d_alb : nullptr) : frame->albedo;
+        o_nrm = host_out ? (frame->normal ? d_nrm : nullptr) : frame->normal;
+        o_rgb64 = host_out ? (frame->rgb64 ? d_rgb64 : nullptr) : frame->rgb64;
+        o_acc = host_out ? (frame->accepted ? d_acc : nullptr) : frame->accepted;
+    }
 
     const int sms = ctx->num_sms > 0 ? ctx->num_sms : 1;
     const uint32_t threads = 256;
@@ -742,7 +786,12 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         if (profile) GT_CUDA(cudaEventRecord(a, st));
         for (uint32_t k = 0; k < K; ++k)
             GT_CUDA(cudaMemsetAsync(SP[k].ps.counters, 0, C_COUNT * sizeof(uint32_t), st));
-        k_init<R><<<slot_blocks, threads, 0, st>>>(P);
+        if constexpr (BATCH) {
+            GT_CUDA(cudaMemcpyAsync(d_cams, bcd.data(), bcd.size() * sizeof(CamDev<R>), cudaMemcpyHostToDevice, st));
+            GT_CUDA(cudaMemcpyAsync(d_start, bstart.data(), bstart.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                    st));
+        }
+        k_init<R, BATCH><<<slot_blocks, threads, 0, st>>>(P);
         GT_CUDA(cudaGetLastError());
         klaunch[GT_KERNEL_OTHER] += 1;
         if (accum && accum->samples > 0) {
@@ -760,7 +809,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
 
     // Per-stripe launch sizes: a stripe owns about 1/K of the GPU.
     int tail_per_sm = 0, coop_per_sm = 0;
-    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tail_per_sm, k_persistent<R, true>, 128, 0));
+    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tail_per_sm, k_persistent<R, true, BATCH>, 128, 0));
     coop_per_sm = tail_per_sm; // the cooperative mode is the same kernel
     const uint32_t full_persist = uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1));
     const uint32_t full_coop = uint32_t(sms) * uint32_t(std::max(coop_per_sm, 1));
@@ -802,9 +851,9 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
                 if (e != cudaSuccess) return e;
                 cudaEventRecord(a, s);
             }
-            if (q == 0) k_generate<R><<<lblocks, threads, 0, s>>>(SP[k], cur);
+            if (q == 0) k_generate<R, BATCH><<<lblocks, threads, 0, s>>>(SP[k], cur);
             else if (q == 1) k_trace<R><<<wblocks, threads, 0, s>>>(SP[k], cur);
-            else if (q == 2) k_shade<R><<<wblocks, threads, 0, s>>>(SP[k], cur);
+            else if (q == 2) k_shade<R, BATCH><<<wblocks, threads, 0, s>>>(SP[k], cur);
             else k_shadow<R><<<wblocks, threads, 0, s>>>(SP[k]);
             if (timed) {
                 cudaEventRecord(z, s);
@@ -879,12 +928,12 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         ho.below = side_coop_blocks * 4u;
         ho.list = Q.ps.q_handoff;
         ho.count = Q.ps.counters + C_SIDE_COOP;
-        k_persistent<R, true><<<side_blocks, 128, 0, S[k].side>>>(Q, Q.ps.counters + C_MIGRATE_NEXT, Q.ps.q_migrate,
+        k_persistent<R, true, BATCH><<<side_blocks, 128, 0, S[k].side>>>(Q, Q.ps.counters + C_MIGRATE_NEXT, Q.ps.q_migrate,
                                                                    Q.ps.counters + C_MIGRATED, ctx->mapped_dev,
                                                                    nullptr, nullptr, nullptr, nullptr, ho);
         HandOff coop;
         coop.coop = 1;
-        k_persistent<R, true><<<side_coop_blocks, 128, 0, S[k].side>>>(
+        k_persistent<R, true, BATCH><<<side_coop_blocks, 128, 0, S[k].side>>>(
             Q, Q.ps.counters + C_SIDE_COOP_NEXT, Q.ps.q_handoff, Q.ps.counters + C_SIDE_COOP, ctx->mapped_dev, nullptr,
             nullptr, nullptr, nullptr, coop);
         GT_CUDA(cudaGetLastError());
@@ -914,11 +963,11 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         ho.below = coop_blocks * 4u;
         ho.list = Q.ps.q_trace[1];
         ho.count = Q.ps.counters + C_TAIL_COOP;
-        k_persistent<R, true><<<tblocks, 128, 0, s>>>(Q, d_next + k, list, count, nullptr, nullptr, nullptr, nullptr,
+        k_persistent<R, true, BATCH><<<tblocks, 128, 0, s>>>(Q, d_next + k, list, count, nullptr, nullptr, nullptr, nullptr,
                                                       nullptr, ho);
         HandOff coop;
         coop.coop = 1;
-        k_persistent<R, true><<<coop_blocks, 128, 0, s>>>(
+        k_persistent<R, true, BATCH><<<coop_blocks, 128, 0, s>>>(
             Q, Q.ps.counters + C_TAIL_COOP_NEXT, Q.ps.q_trace[1], Q.ps.counters + C_TAIL_COOP, nullptr, nullptr, nullptr,
             nullptr, nullptr, coop);
         GT_CUDA(cudaGetLastError());
@@ -932,8 +981,8 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         return GT_OK;
     };
 
-    const uint32_t limit = P.cam.adaptive ? P.cam.adaptive_max : P.cam.spp;
-    const uint64_t max_iters = uint64_t(limit) * uint64_t(std::max<uint32_t>(P.cam.max_depth, 1u)) + 8;
+    const uint32_t limit = limit_max;
+    const uint64_t max_iters = uint64_t(limit) * uint64_t(std::max<uint32_t>(depth_max, 1u)) + 8;
     uint64_t iters = 0;
     rc = GT_OK;
     for (uint32_t active = K; active > 0 && rc == GT_OK;) {
@@ -992,7 +1041,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             }
         }
         if (rc != GT_OK || active == 0) break;
-        if (opts.progress && opts.progress_rgb) { // the image as far as it is known
+        if (!BATCH && opts.progress && opts.progress_rgb) { // the image as far as it is known
             k_preview<R><<<slot_blocks, threads, 0, st>>>(P, o_rgb);
             klaunch[GT_KERNEL_OTHER] += 1;
             if ((ce = cudaMemcpyAsync(opts.progress_rgb, o_rgb, size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost,
@@ -1032,10 +1081,10 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         cudaEvent_t a = nullptr, z = nullptr;
         if (profile) GT_CUDA(ev.pair(a, z));
         if (profile) GT_CUDA(cudaEventRecord(a, st));
-        k_resolve<R><<<slot_blocks, threads, 0, st>>>(P, o_rgb, o_rgb64, o_acc);
+        k_resolve<R, BATCH><<<slot_blocks, threads, 0, st>>>(P, o_rgb, o_rgb64, o_acc);
         GT_CUDA(cudaGetLastError());
         klaunch[GT_KERNEL_OTHER] += 1;
-        if (opts.aovs && (o_alb || o_nrm)) {
+        if (!BATCH && opts.aovs && (o_alb || o_nrm)) {
             k_aov<R><<<slot_blocks, threads, 0, st>>>(P, o_alb, o_nrm);
             GT_CUDA(cudaGetLastError());
             klaunch[GT_KERNEL_OTHER] += 1;
@@ -1058,8 +1107,21 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     for (uint32_t k = 0; k < K; ++k)
         GT_CUDA(cudaMemcpyAsync(words.data() + size_t(k) * C_COUNT, SP[k].ps.counters, C_COUNT * sizeof(uint32_t),
                                 cudaMemcpyDeviceToHost, st));
-    rc = finish_render<R>(ctx, F, frame, opts, host_out, n, o_rgb, o_rgb64, o_acc, o_alb, o_nrm, ev, kms, klaunch,
-                          iters);
+    if constexpr (BATCH) { // each frame's slice of the batch buffers into its own outputs
+        for (uint32_t i = 0; i < bcount; ++i) {
+            gt_frame* f = bframes[i];
+            const size_t o = bstart[i], np = size_t(bstart[i + 1]) - bstart[i];
+            const cudaMemcpyKind kind = f->device_buffers ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+            GT_CUDA(cudaMemcpyAsync(f->rgb, d_rgb + o * 3, np * 3 * sizeof(float), kind, st));
+            if (f->rgb64) GT_CUDA(cudaMemcpyAsync(f->rgb64, d_rgb64 + o * 3, np * 3 * sizeof(double), kind, st));
+            if (f->accepted) GT_CUDA(cudaMemcpyAsync(f->accepted, d_acc + o, np * sizeof(uint32_t), kind, st));
+        }
+        rc = finish_render<R>(ctx, F, nullptr, opts, false, n, o_rgb, o_rgb64, o_acc, o_alb, o_nrm, ev, kms, klaunch,
+                              iters);
+    } else {
+        rc = finish_render<R>(ctx, F, frame, opts, host_out, n, o_rgb, o_rgb64, o_acc, o_alb, o_nrm, ev, kms, klaunch,
+                              iters);
+    }
     if (rc == GT_OK) {
         uint64_t migrated_px = 0, tail_px = 0;
         for (uint32_t k = 0; k < K; ++k) {

@@ -19,12 +19,30 @@ template <class R> struct Params {
     EnvDev<R> env;
     CamDev<R> cam;
     PathState<R> ps;
-    // Batched frames (k_persistent<R, false, true>): one camera per frame, frame f owns
-    // the global pixel range [frame_start[f], frame_start[f + 1]).
+    // Batched frames (kernels instantiated with BATCH = true): one camera per frame,
+    // frame f owns the global pixel range [frame_start[f], frame_start[f + 1]).
     const CamDev<R>* cams;
     const uint32_t* frame_start;
     uint32_t num_frames;
 };
+
+// The camera of global pixel `pix` and the pixel's index within its frame: in a batch the
+// frame is found by binary search over frame_start; otherwise it is the render's camera.
+template <class R, bool BATCH> GT_DEV const CamDev<R>& cam_of(const Params<R>& P, uint32_t pix, uint32_t& local) {
+    if constexpr (BATCH) {
+        uint32_t lo = 0, hi = P.num_frames;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(&P.frame_start[mid]) <= pix) lo = mid;
+            else hi = mid;
+        }
+        local = pix - __ldg(&P.frame_start[lo]);
+        return P.cams[lo];
+    } else {
+        local = pix;
+        return P.cam;
+    }
+}
 
 GT_DEV uint32_t lane_id() { return threadIdx.x & 31u; }
 GT_DEV uint32_t lanemask_lt() { return (1u << lane_id()) - 1u; }
@@ -81,11 +99,13 @@ template <class R> GT_DEV R adaptive_error(V3<R> m2, uint32_t n) { // camera.rs:
     return Num<R>::sqrt(Num<R>::fmax(maxc(cdiv(var, R(n))), R(0)));
 }
 
-template <class R> __global__ void k_init(Params<R> P) {
+template <class R, bool BATCH = false> __global__ void k_init(Params<R> P) {
     const uint32_t n = P.ps.n;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t x = i % P.cam.width, y = i / P.cam.width;
-        const uint64_t s = pixel_seed(P.cam.seed, x, y);
+        uint32_t local;
+        const CamDev<R>& C = cam_of<R, BATCH>(P, i, local);
+        const uint32_t x = local % C.width, y = local / C.width;
+        const uint64_t s = pixel_seed(C.seed, x, y);
         P.ps.st[i] = make_uint4(uint32_t(s), uint32_t(s >> 32), F_NEWSAMPLE, 0u);
         P.ps.acc[i] = R4<R>{0, 0, 0, 0};
         P.ps.comp[i] = R4<R>{0, 0, 0, 0};
@@ -96,12 +116,12 @@ template <class R> __global__ void k_init(Params<R> P) {
 }
 
 // Folds a finished sample into the pixel; returns true when adaptive sampling stops.
-template <class R> GT_DEV bool finish_sample(const Params<R>& P, uint32_t slot, V3<R> s) {
+template <class R> GT_DEV bool finish_sample(const Params<R>& P, const CamDev<R>& C, uint32_t slot, V3<R> s) {
     if (!finite3(s)) return false; // non-finite samples are dropped (camera.rs:2984-2999, 2951-2953)
     R4<R> a = P.ps.acc[slot], c = P.ps.comp[slot];
     uint32_t acc_n = P.ps.accepted[slot] + 1;
     bool stop = false;
-    if (P.cam.adaptive) { // Welford update, camera.rs:2955-2960
+    if (C.adaptive) { // Welford update, camera.rs:2955-2960
         V3<R> mean = xyz(a), m2 = xyz(c);
         V3<R> delta = s - mean;
         mean = mean + cdiv(delta, R(acc_n));
@@ -109,7 +129,7 @@ template <class R> GT_DEV bool finish_sample(const Params<R>& P, uint32_t slot, 
         m2 = m2 + cmul(delta, delta2);
         a = R4<R>{mean.x, mean.y, mean.z, R(0)};
         c = R4<R>{m2.x, m2.y, m2.z, R(0)};
-        stop = acc_n >= P.cam.adaptive_min && adaptive_error(m2, acc_n) < P.cam.adaptive_threshold;
+        stop = acc_n >= C.adaptive_min && adaptive_error(m2, acc_n) < C.adaptive_threshold;
     } else {
         kahan_add(a, c, s);
     }
@@ -119,14 +139,13 @@ template <class R> GT_DEV bool finish_sample(const Params<R>& P, uint32_t slot, 
     return stop;
 }
 
-template <class R> __global__ void __launch_bounds__(256) k_generate(Params<R> P, uint32_t cur) {
+template <class R, bool BATCH = false> __global__ void __launch_bounds__(256) k_generate(Params<R> P, uint32_t cur) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         P.ps.counters[C_TRACE0 + (cur ^ 1u)] = 0;
         for (uint32_t k = 0; k < NUM_KEYS; ++k) P.ps.counters[C_MAT + k] = 0;
         P.ps.counters[C_SHADOW] = 0;
     }
     const uint32_t n = P.ps.local_n;
-    const uint32_t limit = P.cam.adaptive ? P.cam.adaptive_max : P.cam.spp;
     const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = warp0; base < n; base += stride) {
@@ -136,19 +155,22 @@ template <class R> __global__ void __launch_bounds__(256) k_generate(Params<R> P
         if (j < n) {
             uint4 st = P.ps.st[slot];
             if (st.z & F_NEWSAMPLE) {
+                uint32_t local;
+                const CamDev<R>& C = cam_of<R, BATCH>(P, slot, local);
+                const uint32_t limit = C.adaptive ? C.adaptive_max : C.spp;
                 Rng g{uint64_t(st.x) | (uint64_t(st.y) << 32)};
                 uint32_t started = st.w;
                 bool stop = false;
-                if (started > 0 && !(st.z & F_FRESH)) stop = finish_sample(P, slot, xyz(P.ps.col[slot]));
-                const uint32_t x = slot % P.cam.width, y = slot / P.cam.width;
+                if (started > 0 && !(st.z & F_FRESH)) stop = finish_sample(P, C, slot, xyz(P.ps.col[slot]));
+                const uint32_t x = local % C.width, y = local / C.width;
                 uint32_t flags = F_DONE;
                 while (!stop && started < limit) {
                     V3<R> o, d;
                     R time;
-                    camera_ray(P.cam, x, y, started, g, o, d, time);
+                    camera_ray(C, x, y, started, g, o, d, time);
                     ++started;
-                    if (P.cam.max_depth == 0) { // the bounce loop never runs: a black sample
-                        stop = finish_sample(P, slot, V3<R>{0, 0, 0});
+                    if (C.max_depth == 0) { // the bounce loop never runs: a black sample
+                        stop = finish_sample(P, C, slot, V3<R>{0, 0, 0});
                         continue;
                     }
                     P.ps.ray_o[slot] = R4<R>{o.x, o.y, o.z, time};
@@ -336,7 +358,8 @@ template <class R> GT_DEV void apply_shadow(const Params<R>& P, V3<R>& col, cons
 }
 
 // Wavefront shade step for `slot`: one bounce, pending shadow queries stored for k_shadow.
-template <class R> GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uint32_t key, bool& shadow) {
+template <class R, bool BATCH>
+GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uint32_t key, bool& shadow) {
     uint4 st = P.ps.st[slot];
     Rng g{uint64_t(st.x) | (uint64_t(st.y) << 32)};
     uint32_t flags = st.z;
@@ -352,7 +375,9 @@ template <class R> GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uin
     p.allow_emit = (flags & F_ALLOW_EMIT) != 0;
     Shadow<R> sh;
     const int prim = key == KEY_MISS ? -1 : P.ps.hit_prim[slot];
-    const bool cont = integrate_bounce(P, P.cam, p, prim, key == KEY_MISS ? R(0) : P.ps.hit_t[slot], g, sh);
+    uint32_t local;
+    const bool cont =
+        integrate_bounce(P, cam_of<R, BATCH>(P, slot, local), p, prim, key == KEY_MISS ? R(0) : P.ps.hit_t[slot], g, sh);
     uint32_t sh_bits = 0;
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
@@ -380,7 +405,7 @@ template <class R> GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uin
     return cont;
 }
 
-template <class R> __global__ void __launch_bounds__(256) k_shade(Params<R> P, uint32_t cur) {
+template <class R, bool BATCH = false> __global__ void __launch_bounds__(256) k_shade(Params<R> P, uint32_t cur) {
     uint32_t prefix[NUM_KEYS + 1];
     prefix[0] = 0;
 #pragma unroll
@@ -399,7 +424,7 @@ template <class R> __global__ void __launch_bounds__(256) k_shade(Params<R> P, u
             for (uint32_t k = 1; k < NUM_KEYS; ++k)
                 if (i >= prefix[k]) key = k;
             slot = P.ps.q_mat[size_t(key) * P.ps.qcap + (i - prefix[key])];
-            cont = shade_slot(P, slot, key, shadow);
+            cont = shade_slot<R, BATCH>(P, slot, key, shadow);
         }
         warp_push(cont, slot, P.ps.q_trace[cur ^ 1u], &P.ps.counters[C_TRACE0 + (cur ^ 1u)]);
         warp_push(shadow, slot, P.ps.q_shadow, &P.ps.counters[C_SHADOW]);
@@ -454,7 +479,7 @@ template <class R> __global__ void k_preview(Params<R> P, float* rgb) {
 }
 
 // Pixel estimate: sum / accepted (camera.rs:2993-2999) or the Welford mean.
-template <class R>
+template <class R, bool BATCH = false>
 __global__ void k_resolve(Params<R> P, float* rgb, double* rgb64, uint32_t* accepted) {
     const uint32_t n = P.ps.n;
     const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
@@ -466,7 +491,8 @@ __global__ void k_resolve(Params<R> P, float* rgb, double* rgb64, uint32_t* acce
             const uint32_t a = P.ps.accepted[i];
             V3<R> s = xyz(P.ps.acc[i]);
             V3<R> c;
-            if (P.cam.adaptive) c = s;
+            uint32_t local;
+            if (cam_of<R, BATCH>(P, i, local).adaptive) c = s;
             else c = a == 0 ? V3<R>{0, 0, 0} : cdiv(s, R(a));
             if (rgb) {
                 rgb[size_t(i) * 3 + 0] = float(c.x);

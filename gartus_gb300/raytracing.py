@@ -903,9 +903,11 @@ class PathTracer:
 
     def render_batch_hdr_images(self, world: RayScene, cameras, lights: Optional[WeightedSamplingTargetList] = None,
                                 environment: Optional[EnvironmentLight] = None, want64: bool = False) -> list:
-        """One image per camera, all rendered in one launch (gt_render_batch): the per-frame
-        loop around render_with_*_hdr_image for an animation or a camera sweep.  This
-        tracer's camera is not used; each frame is rendered with its own."""
+        """One image per camera, all rendered together (gt_render_batch): the per-frame loop
+        around render_with_*_hdr_image for an animation or a camera sweep.  This tracer's
+        camera is not used; each frame is rendered with its own.  In f32, frames of one
+        width run through the striped wavefront as one image of their rows (schedule
+        "auto" or "wavefront"); otherwise all pixels go through one persistent launch."""
         ctx = self.context
         cams = list(cameras)
         descs = [c.desc() for c in cams]
@@ -930,6 +932,9 @@ class PathTracer:
         o.struct_size = C.sizeof(abi.gt_render_opts)
         o.precision = abi.GT_PRECISION_F64 if self.precision == "f64" else abi.GT_PRECISION_F32
         o.profile = 1 if self.profile else 0
+        o.schedule = self.SCHEDULES[self.schedule]
+        o.tail_slots = self.tail_slots
+        o.stripes = self.stripes
         stats = abi.gt_render_stats()
         o.stats = C.pointer(stats)
         sh = world._handle(ctx)

@@ -388,12 +388,16 @@ typedef struct gt_frame_job {
 } gt_frame_job;
 
 /* Renders `count` frames of one scene — each with its own camera, pose, shutter, sample
- * count and adaptive settings — in one persistent launch: the per-frame loop a caller
- * would write around PathTracer::render_with_*_hdr_image (renderer.rs:101-117, 391-449)
- * for an animation or a camera sweep.  Every frame's image, accepted counts and f64
- * image equal what gt_render gives for that frame alone.  opts: precision, stats (summed
- * over the batch), profile, progress (pixels handed out of the batch's total) and
- * cancellation; `schedule` and `tail_slots` are ignored; `aovs` is GT_ERR_UNSUPPORTED. */
+ * count and adaptive settings — together: the per-frame loop a caller would write around
+ * PathTracer::render_with_*_hdr_image (renderer.rs:101-117, 391-449) for an animation or
+ * a camera sweep.  In f32 with schedule AUTO or WAVEFRONT, frames of one width run
+ * through the striped wavefront as one image of their stacked rows (every slot rendered
+ * with its frame's camera, graphs replayed, slow slots migrated, the tail finished in the
+ * persistent kernel); in f64, with schedule PERSISTENT, or with frames of different
+ * widths, all pixels go through one persistent launch.  Every frame's image and accepted
+ * counts equal what gt_render gives for that frame alone (bit for bit in f64).  opts:
+ * precision, schedule, tail_slots, stripes, stats (summed over the batch), profile,
+ * progress and cancellation; `progress_rgb` is not written; `aovs` is GT_ERR_UNSUPPORTED. */
 gt_status gt_render_batch(gt_scene* scene, const gt_lights* lights, const gt_environment* environment,
                           const gt_frame_job* jobs, uint32_t count, const gt_render_opts* opts);
 

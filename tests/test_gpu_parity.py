@@ -342,6 +342,26 @@ def test_batch_matches_single_frames(gpu_context, precision):
         assert rel_err(imgs[1].pixels64, ref, floor=1e-12).max() <= 1e-9
 
 
+@pytest.mark.parametrize("schedule", ["auto", "wavefront"])
+def test_batch_wavefront_matches_single_frames(gpu_context, schedule):
+    # Frames of one width in f32 run through the striped wavefront as one image of their
+    # rows: every frame equals its own gt_render (the same accepted counts; radiance within
+    # the f32 tolerance, as the batch kernels are separate instantiations).  Eight frames
+    # of 48x48 with adaptive sampling exercise the stripes, the migration and the tail.
+    scene, lights = scenes.batch_scene()
+    cams = scenes.batch_cameras(frames=8, width=48, spp_cycle=(4, 8, 16), max_samples=64, threshold=0.05)
+    cams.append(scenes.cornell_camera(48, 3, 20))  # a stratified frame of the same width
+    pt = PathTracer(cams[0], context=gpu_context, schedule=schedule)
+    imgs = pt.render_batch_hdr_images(scene, cams, lights=lights)
+    assert pt.last_stats["samples"] == sum(int(i.accepted.sum()) for i in imgs)
+    assert pt.last_stats["iterations"] > 1  # the wavefront ran (the persistent batch reports 1)
+    for cam, img in zip(cams, imgs):
+        one = PathTracer(cam, context=gpu_context).render_with_lights_hdr_image(scene, lights)
+        flipped = int((img.accepted != one.accepted).sum())
+        assert flipped <= 0.02 * img.accepted.size, flipped
+        assert _divergent(img.pixels, one.pixels.astype(np.float64)) <= 0.05 * img.pixels.shape[0] * img.pixels.shape[1]
+
+
 def test_batch_rejects_bad_jobs(gpu_context):
     scene, lights = scenes.batch_scene()
     cam = scenes.batch_cameras(frames=1, width=8)[0]
