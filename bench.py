@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--tail-slots", type=int, default=0,
                     help="auto schedule: unfinished pixels at which the persistent kernel takes over (0 = library)")
     ap.add_argument("--stripes", type=int, default=0, help="wavefront stripes (0 = library default)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="pick stripes, tail size and blocks per SM with gt_autotune before the warm-up")
     ap.add_argument("--width", type=int, default=0, help="smaller image for profiling runs (0 = the workload's)")
     ap.add_argument("--grid", type=int, default=0, help="stratified grid width for profiling runs (0 = 16)")
     ap.add_argument("--profile-run", action="store_true",
@@ -360,6 +362,10 @@ def run_ours(args):
     if cams is not None:
         cam = cams[0]
     pt = PathTracer(cam, context=ctx, schedule=args.schedule, tail_slots=args.tail_slots, stripes=args.stripes)
+    tuned = None
+    if args.autotune:  # a batch tunes on its first 16 frames
+        tuned = pt.autotune(scene, lights, env, cameras=cams[:16] if cams is not None else None)
+        print(f"autotune: {tuned}", file=sys.stderr, flush=True)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{device}")
 
     def render():
@@ -446,6 +452,7 @@ def run_ours(args):
             descs.append(c.desc())
         o = abi.gt_render_opts()
         o.struct_size = C.sizeof(abi.gt_render_opts)
+        pt._launch_opts(o)  # the same schedule and launch shapes as the timed leg
         stt = abi.gt_render_stats()
         o.stats = C.pointer(stt)
         if cams is not None:
@@ -473,8 +480,9 @@ def run_ours(args):
     e2e = statistics.median(e2e_vals) * world
 
     # Roofline of the dominant kernel from one profiled frame (events around every launch).
-    prof = PathTracer(cam, context=ctx, profile=True, schedule=args.schedule, tail_slots=args.tail_slots,
-                      stripes=args.stripes)
+    prof = PathTracer(cam, context=ctx, profile=True, schedule=args.schedule, tail_slots=pt.tail_slots,
+                      stripes=pt.stripes, generate_blocks_per_sm=pt.generate_blocks_per_sm,
+                      trace_blocks_per_sm=pt.trace_blocks_per_sm)
     if cams is not None:
         prof.render_batch_hdr_images(scene, cams, lights=lights, environment=env)
     elif env is not None:
@@ -516,7 +524,11 @@ def run_ours(args):
             "warmup": max(args.warmup, 3), "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
             "config": dict(cfg, l2="flushed between timed steps (512 MiB write)", schedule=args.schedule,
-                           parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+                           parallelism=f"replicas x{world}" if world > 1 else "single GPU",
+                           launch={"stripes": pt.stripes, "tail_slots": pt.tail_slots,
+                                   "generate_blocks_per_sm": pt.generate_blocks_per_sm,
+                                   "trace_blocks_per_sm": pt.trace_blocks_per_sm,
+                                   "from": "gt_autotune" if tuned else "library defaults"}),
             "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "clocks": clock,

@@ -59,6 +59,8 @@ def _declare(L: C.CDLL) -> None:
         "gt_accumulator_load": (st, [C.c_void_p, C.c_void_p, C.c_uint64]),
         "gt_render_accumulate": (st, [C.c_void_p, C.c_void_p, C.c_void_p, P(abi.gt_camera_desc), C.c_uint32,
                                       C.c_void_p, P(abi.gt_render_opts), P(abi.gt_frame)]),
+        "gt_autotune": (st, [C.c_void_p, C.c_void_p, C.c_void_p, P(abi.gt_frame_job), C.c_uint32,
+                             P(abi.gt_render_opts), P(abi.gt_autotune_report)]),
         "gt_denoiser_create": (st, [C.c_void_p, C.c_uint64, P(C.c_void_p)]),
         "gt_denoiser_destroy": (None, [C.c_void_p]),
         "gt_denoiser_param_count": (st, [C.c_void_p, P(C.c_uint64)]),
@@ -104,7 +106,7 @@ EXPORTED_SYMBOLS = [
     "gt_scene_emissive_targets", "gt_lights_create", "gt_lights_destroy", "gt_environment_create",
     "gt_environment_destroy", "gt_render", "gt_trace_rays", "gt_trace_primary", "gt_render_noalloc",
     "gt_render_batch", "gt_accumulator_create", "gt_accumulator_destroy", "gt_accumulator_samples",
-    "gt_accumulator_save", "gt_accumulator_load", "gt_render_accumulate", "gt_denoiser_create",
+    "gt_accumulator_save", "gt_accumulator_load", "gt_render_accumulate", "gt_autotune", "gt_denoiser_create",
     "gt_denoiser_destroy", "gt_denoiser_param_count", "gt_denoiser_get_params", "gt_denoiser_set_params",
     "gt_denoiser_train_step", "gt_denoise",
 ]

@@ -203,6 +203,8 @@ class gt_render_opts(C.Structure):
         ("tail_slots", C.c_uint32),
         ("stripes", C.c_uint32),
         ("progress_rgb", C.c_void_p),
+        ("generate_blocks_per_sm", C.c_uint32),
+        ("trace_blocks_per_sm", C.c_uint32),
     ]
 
 
@@ -239,6 +241,15 @@ class gt_bvh_stats(C.Structure):
         return {name: int(getattr(self, name)) for name, _ in self._fields_}
 
 
+class gt_autotune_report(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32),
+        ("trials", C.c_uint32),
+        ("given_ms", C.c_double),
+        ("best_ms", C.c_double),
+    ]
+
+
 class gt_denoise_input(C.Structure):
     _fields_ = [
         ("struct_size", C.c_uint32),
@@ -255,4 +266,5 @@ class gt_denoise_input(C.Structure):
 STRUCTS = [
     gt_geometry, gt_primitive, gt_material, gt_scene_desc, gt_light_target, gt_environment_desc,
     gt_camera_desc, gt_render_opts, gt_frame, gt_frame_job, gt_bvh_stats, gt_render_stats, gt_denoise_input,
+    gt_autotune_report,
 ]

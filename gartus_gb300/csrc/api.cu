@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstddef>
 #include <cstring>
+#include <initializer_list>
 #include <exception>
 #include <new>
 
@@ -691,6 +692,74 @@ gt_status gt_render(gt_scene* s, const gt_lights* l, const gt_environment* e, co
     auto* env = const_cast<gt_environment*>(e);
     if (opts.precision == GT_PRECISION_F64) return render_f64(s, l, env, cam, opts, f);
     return render_f32(s, l, env, cam, opts, f);
+    GT_GUARD_END
+}
+
+gt_status gt_autotune(gt_scene* s, const gt_lights* l, const gt_environment* e, const gt_frame_job* jobs,
+                      uint32_t count, gt_render_opts* opts, gt_autotune_report* report) {
+    GT_GUARD_BEGIN
+    if (!s || !jobs || !opts || count == 0) return fail(GT_ERR_INVALID_ARG, "null argument");
+    if (opts->struct_size < sizeof(gt_render_opts)) return fail(GT_ERR_INVALID_ARG, "options struct_size too small");
+    if (report && report->struct_size < sizeof(gt_autotune_report))
+        return fail(GT_ERR_INVALID_ARG, "report struct_size too small");
+    if (opts->schedule == GT_SCHEDULE_PERSISTENT)
+        return fail(GT_ERR_INVALID_ARG, "the persistent schedule has nothing to tune; use AUTO or WAVEFRONT");
+    uint32_t trials = 0;
+    // Device time of the second of two renders with `o` (the first captures its graphs).
+    auto timed = [&](const gt_render_opts& cand, double& ms) -> gt_status {
+        gt_render_opts o = cand;
+        gt_render_stats st;
+        o.stats = &st;
+        o.profile = 0;
+        o.progress = nullptr;
+        o.progress_rgb = nullptr;
+        for (int rep = 0; rep < 2; ++rep) {
+            const gt_status rc = count == 1 ? gt_render(s, l, e, jobs[0].camera, &o, jobs[0].frame)
+                                            : gt_render_batch(s, l, e, jobs, count, &o);
+            if (rc != GT_OK) return rc;
+        }
+        ++trials;
+        ms = st.gpu_ms;
+        return GT_OK;
+    };
+    gt_render_opts best = *opts;
+    double best_ms = 0.0;
+    gt_status rc = timed(best, best_ms);
+    if (rc != GT_OK) return rc;
+    const double given_ms = best_ms;
+    auto sweep = [&](uint32_t gt_render_opts::*field, std::initializer_list<uint32_t> values) -> gt_status {
+        const gt_render_opts start = best;
+        for (uint32_t v : values) {
+            if (start.*field == v) continue;
+            gt_render_opts cand = start;
+            cand.*field = v;
+            double ms = 0.0;
+            const gt_status r = timed(cand, ms);
+            if (r != GT_OK) return r;
+            if (ms < 0.99 * best_ms) {
+                best = cand;
+                best_ms = ms;
+            }
+        }
+        return GT_OK;
+    };
+    // Candidates around the library's defaults (0 = default).
+    if ((rc = sweep(&gt_render_opts::stripes, {1u, 2u, 3u, 4u, 6u, 8u})) != GT_OK) return rc;
+    if ((rc = sweep(&gt_render_opts::tail_slots, {0u, 4096u, 16384u, 65536u, 262144u})) != GT_OK) return rc;
+    if ((rc = sweep(&gt_render_opts::trace_blocks_per_sm, {4u, 6u, 8u, 12u})) != GT_OK) return rc;
+    if ((rc = sweep(&gt_render_opts::generate_blocks_per_sm, {4u, 8u, 16u})) != GT_OK) return rc;
+    best.stats = opts->stats;
+    best.profile = opts->profile;
+    best.progress = opts->progress;
+    best.progress_user = opts->progress_user;
+    best.progress_rgb = opts->progress_rgb;
+    *opts = best;
+    if (report) {
+        report->trials = trials;
+        report->given_ms = given_ms;
+        report->best_ms = best_ms;
+    }
+    return GT_OK;
     GT_GUARD_END
 }
 

@@ -813,8 +813,12 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     coop_per_sm = tail_per_sm; // the cooperative mode is the same kernel
     const uint32_t full_persist = uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1));
     const uint32_t full_coop = uint32_t(sms) * uint32_t(std::max(coop_per_sm, 1));
-    const uint32_t lblocks = std::max<uint32_t>(1u, std::min<uint32_t>((qcap + threads - 1) / threads, uint32_t(sms) * 8));
-    const uint32_t wblocks = std::max<uint32_t>(1u, std::min<uint32_t>((qcap + threads - 1) / threads, uint32_t(sms) * 6));
+    const uint32_t gen_per_sm = opts.generate_blocks_per_sm ? std::min<uint32_t>(opts.generate_blocks_per_sm, 32u) : 8u;
+    const uint32_t wave_per_sm = opts.trace_blocks_per_sm ? std::min<uint32_t>(opts.trace_blocks_per_sm, 32u) : 6u;
+    const uint32_t lblocks =
+        std::max<uint32_t>(1u, std::min<uint32_t>((qcap + threads - 1) / threads, uint32_t(sms) * gen_per_sm));
+    const uint32_t wblocks =
+        std::max<uint32_t>(1u, std::min<uint32_t>((qcap + threads - 1) / threads, uint32_t(sms) * wave_per_sm));
     const uint32_t tblocks = std::max<uint32_t>(uint32_t(sms), full_persist / K);
     const uint32_t coop_blocks = std::max<uint32_t>(uint32_t(sms), full_coop / K);
     const uint32_t side_blocks = std::max<uint32_t>(uint32_t(sms) / 2u, full_persist / K);

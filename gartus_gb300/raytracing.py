@@ -845,7 +845,8 @@ class PathTracer:
 
     def __init__(self, camera: RayCamera, options: RenderOptions = RenderOptions(), precision: str = "f32",
                  context: Optional[Context] = None, profile: bool = False, schedule: str = "auto",
-                 tail_slots: int = 0, stripes: int = 0):
+                 tail_slots: int = 0, stripes: int = 0, generate_blocks_per_sm: int = 0,
+                 trace_blocks_per_sm: int = 0):
         if precision not in ("f32", "f64"):
             raise ValueError("precision must be 'f32' or 'f64'")
         if schedule not in self.SCHEDULES:
@@ -857,6 +858,8 @@ class PathTracer:
         self.schedule = schedule
         self.tail_slots = int(tail_slots)
         self.stripes = int(stripes)
+        self.generate_blocks_per_sm = int(generate_blocks_per_sm)
+        self.trace_blocks_per_sm = int(trace_blocks_per_sm)
         self._ctx = context
         self.last_stats: Optional[dict] = None
 
@@ -866,7 +869,54 @@ class PathTracer:
 
     def with_options(self, options: RenderOptions) -> "PathTracer":
         return PathTracer(self.camera, options, self.precision, self._ctx, self.profile, self.schedule,
-                          self.tail_slots, self.stripes)
+                          self.tail_slots, self.stripes, self.generate_blocks_per_sm, self.trace_blocks_per_sm)
+
+    def _launch_opts(self, o) -> None:
+        """The tracer's schedule and launch shapes into a gt_render_opts."""
+        o.schedule = self.SCHEDULES[self.schedule]
+        o.tail_slots = self.tail_slots
+        o.stripes = self.stripes
+        o.generate_blocks_per_sm = self.generate_blocks_per_sm
+        o.trace_blocks_per_sm = self.trace_blocks_per_sm
+
+    def autotune(self, world: RayScene, lights: Optional[WeightedSamplingTargetList] = None,
+                 environment: Optional[EnvironmentLight] = None, cameras=None) -> dict:
+        """gt_autotune: times this tracer's frame (or the batch of `cameras`) under candidate
+        stripe counts, tail sizes and wavefront blocks per SM and keeps the fastest in this
+        tracer.  Returns {"trials", "given_ms", "best_ms", "stripes", "tail_slots",
+        "generate_blocks_per_sm", "trace_blocks_per_sm"}."""
+        ctx = self.context
+        cams = list(cameras) if cameras is not None else [self.camera]
+        descs = [c.desc() for c in cams]
+        frames, keep = [], []
+        for c in cams:
+            w, h, _ = c.image_size()
+            rgb = np.empty((h, w, 3), dtype=np.float32)
+            f = abi.gt_frame()
+            f.struct_size = C.sizeof(abi.gt_frame)
+            f.width, f.height, f.device_buffers = w, h, 0
+            f.rgb = rgb.ctypes.data
+            frames.append(f)
+            keep.append(rgb)
+        jobs = (abi.gt_frame_job * len(cams))()
+        for i in range(len(cams)):
+            jobs[i].camera = C.pointer(descs[i])
+            jobs[i].frame = C.pointer(frames[i])
+        o = abi.gt_render_opts()
+        o.struct_size = C.sizeof(abi.gt_render_opts)
+        o.precision = abi.GT_PRECISION_F64 if self.precision == "f64" else abi.GT_PRECISION_F32
+        self._launch_opts(o)
+        rep = abi.gt_autotune_report()
+        rep.struct_size = C.sizeof(abi.gt_autotune_report)
+        sh = world._handle(ctx)
+        lh = lights._handle(ctx).h if lights is not None else None
+        eh = environment._handle(ctx).h if environment is not None else None
+        check(lib().gt_autotune(sh.h, lh, eh, jobs, len(cams), C.byref(o), C.byref(rep)))
+        self.stripes, self.tail_slots = int(o.stripes), int(o.tail_slots)
+        self.generate_blocks_per_sm, self.trace_blocks_per_sm = int(o.generate_blocks_per_sm), int(o.trace_blocks_per_sm)
+        return {"trials": int(rep.trials), "given_ms": float(rep.given_ms), "best_ms": float(rep.best_ms),
+                "stripes": self.stripes, "tail_slots": self.tail_slots,
+                "generate_blocks_per_sm": self.generate_blocks_per_sm, "trace_blocks_per_sm": self.trace_blocks_per_sm}
 
     def render_accumulate(self, world: RayScene, accumulator: Accumulator, samples: int,
                           lights: Optional[WeightedSamplingTargetList] = None,
@@ -888,9 +938,9 @@ class PathTracer:
         o = abi.gt_render_opts()
         o.struct_size = C.sizeof(abi.gt_render_opts)
         o.profile = 1 if self.profile else 0
-        o.schedule = abi.GT_SCHEDULE_WAVEFRONT if self.schedule == "wavefront" else abi.GT_SCHEDULE_AUTO
-        o.tail_slots = self.tail_slots
-        o.stripes = self.stripes
+        self._launch_opts(o)
+        if self.schedule == "persistent":  # accumulation runs on the wavefront
+            o.schedule = abi.GT_SCHEDULE_AUTO
         stats = abi.gt_render_stats()
         o.stats = C.pointer(stats)
         sh = world._handle(ctx)
@@ -932,9 +982,7 @@ class PathTracer:
         o.struct_size = C.sizeof(abi.gt_render_opts)
         o.precision = abi.GT_PRECISION_F64 if self.precision == "f64" else abi.GT_PRECISION_F32
         o.profile = 1 if self.profile else 0
-        o.schedule = self.SCHEDULES[self.schedule]
-        o.tail_slots = self.tail_slots
-        o.stripes = self.stripes
+        self._launch_opts(o)
         stats = abi.gt_render_stats()
         o.stats = C.pointer(stats)
         sh = world._handle(ctx)
@@ -998,9 +1046,7 @@ class PathTracer:
         o.precision = abi.GT_PRECISION_F64 if self.precision == "f64" else abi.GT_PRECISION_F32
         o.aovs = 1 if aovs else 0
         o.profile = 1 if self.profile else 0
-        o.schedule = self.SCHEDULES[self.schedule]
-        o.tail_slots = self.tail_slots
-        o.stripes = self.stripes
+        self._launch_opts(o)
         if progress_fn is not None:
             o.progress = progress_fn
             o.progress_rgb = progress_rgb.ctypes.data if progress_rgb is not None else None
@@ -1045,7 +1091,8 @@ class PathTracer:
     def render_with_light_connections_hdr_image(self, world, lights, want64: bool = False) -> HdrImage:
         cam = self.camera.with_direct_lighting_mode(abi.GT_DIRECT_NEXT_EVENT_ESTIMATION)
         return PathTracer(cam, self.options, self.precision, self._ctx, self.profile, self.schedule,
-                          self.tail_slots, self.stripes)._render(
+                          self.tail_slots, self.stripes, self.generate_blocks_per_sm,
+                          self.trace_blocks_per_sm)._render(
             world, lights, None, want64=want64)
 
     # render_with_environment_hdr_image (renderer.rs:431-449)

@@ -261,6 +261,11 @@ typedef struct gt_render_opts {
      * camera.rs:3172-3270).  Pixels still being written by a running persistent launch
      * may show a partial value. */
     float* progress_rgb;
+    /* Wavefront launch shapes, in resident 256-thread blocks per SM (0 = the library's
+     * choice: 8 for the generate kernel, 6 for trace, shade and shadow); gt_autotune
+     * picks them per workload. */
+    uint32_t generate_blocks_per_sm;
+    uint32_t trace_blocks_per_sm;
 } gt_render_opts;
 
 /* Caller-owned output images, row-major, 3 channels, y = 0 is the top row
@@ -400,6 +405,25 @@ typedef struct gt_frame_job {
  * progress and cancellation; `progress_rgb` is not written; `aovs` is GT_ERR_UNSUPPORTED. */
 gt_status gt_render_batch(gt_scene* scene, const gt_lights* lights, const gt_environment* environment,
                           const gt_frame_job* jobs, uint32_t count, const gt_render_opts* opts);
+
+/* Autotuner (no reference counterpart: the reference has no launch parameters to tune).
+ * Renders the given jobs (count = 1: one gt_render of jobs[0]; count > 1: gt_render_batch)
+ * under candidate settings and writes the fastest into *opts: wavefront stripes, tail
+ * size and the wavefront kernels' blocks per SM, chosen one after another (coordinate
+ * descent), each candidate timed by the device time of its second render (the first
+ * captures its graphs).  A candidate replaces the current best only when at least 1%
+ * faster.  The jobs' frames receive the last render.  *opts supplies everything else
+ * (precision, schedule AUTO or WAVEFRONT); report (optional) receives the trial count and
+ * the device times with the given and the chosen options. */
+typedef struct gt_autotune_report {
+    uint32_t struct_size;
+    uint32_t trials;   /* renders timed */
+    double given_ms;   /* device time with the options as given */
+    double best_ms;    /* device time with the options written back */
+} gt_autotune_report;
+
+gt_status gt_autotune(gt_scene* scene, const gt_lights* lights, const gt_environment* environment,
+                      const gt_frame_job* jobs, uint32_t count, gt_render_opts* opts, gt_autotune_report* report);
 
 /* Closest-hit queries with traversal statistics on the reference-layout BVH in f64:
  * RayScene::hit (raytracing/scene.rs:1639-1657) and

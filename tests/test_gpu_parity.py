@@ -362,6 +362,29 @@ def test_batch_wavefront_matches_single_frames(gpu_context, schedule):
         assert _divergent(img.pixels, one.pixels.astype(np.float64)) <= 0.05 * img.pixels.shape[0] * img.pixels.shape[1]
 
 
+def test_autotune_keeps_the_image(gpu_context):
+    # gt_autotune times candidate stripe counts, tail sizes and blocks per SM on the frame
+    # and keeps the fastest; launch shapes never change the image.
+    scene, lights = scenes.cornell_scene()
+    cam = scenes.cornell_camera(64, 4, 20)
+    base = PathTracer(cam, context=gpu_context).render_with_lights_hdr_image(scene, lights)
+    pt = PathTracer(cam, context=gpu_context)
+    rep = pt.autotune(scene, lights)
+    print("autotune:", rep)
+    assert rep["trials"] >= 10
+    assert rep["best_ms"] <= rep["given_ms"]
+    assert 0 <= rep["stripes"] <= 8 and 0 <= rep["trace_blocks_per_sm"] <= 32
+    tuned = pt.render_with_lights_hdr_image(scene, lights)
+    np.testing.assert_array_equal(tuned.pixels, base.pixels)
+    np.testing.assert_array_equal(tuned.accepted, base.accepted)
+    # a batch tunes the same way
+    cams = scenes.batch_cameras(frames=3, width=32, spp_cycle=(4,), max_samples=8)
+    rep = PathTracer(cams[0], context=gpu_context).autotune(scene, lights, cameras=cams)
+    assert rep["trials"] >= 10
+    with pytest.raises(GartusError):
+        PathTracer(cam, context=gpu_context, schedule="persistent").autotune(scene, lights)
+
+
 def test_batch_rejects_bad_jobs(gpu_context):
     scene, lights = scenes.batch_scene()
     cam = scenes.batch_cameras(frames=1, width=8)[0]
