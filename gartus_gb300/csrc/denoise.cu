@@ -108,6 +108,7 @@ struct gt_denoiser {
     uint8_t* flags = nullptr;
     uint32_t* flag_count = nullptr;
     uint32_t* err = nullptr; // set by a tensor-core kernel whose mbarrier wait gave up
+    bool launch_failed = false; // a convolution could not be launched (tensor map encoding)
 };
 
 namespace {
@@ -225,7 +226,38 @@ constexpr int kTcSmemMax =
         : tc_smem_bytes(96, tc_shape(96).rows, tc_shape(96).stages);
 static_assert(kTcSmemMax <= 227 * 1024, "tensor-core convolution needs more shared memory than a CTA has");
 
-void launch_conv_tc(gt_denoiser* d, ConvTc a, cudaStream_t st) {
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime.
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// BF16 tensor map of `rank` dimensions (innermost first), unit element strides, no swizzle,
+// zero fill outside the tensor.
+bool encode_bf16(CUtensorMap* m, const void* base, int rank, const cuuint64_t* dims, const cuuint64_t* strides,
+                 const cuuint32_t* box) {
+    const EncodeTiledFn fn = encode_tiled();
+    if (!fn) return false;
+    const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, cuuint32_t(rank), const_cast<void*>(base), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Launches a tensor-core convolution: TMA staging when the input is one tensor, per-thread
+// staging when it is read as an upsampled half plus a skip tensor.
+gt_status launch_conv_tc(gt_denoiser* d, ConvTc a, cudaStream_t st) {
     a.n_mma = (a.cout_p + 15) / 16 * 16;
     const TcShape sh = tc_shape(a.n_mma);
     a.rows = sh.rows;
@@ -234,7 +266,43 @@ void launch_conv_tc(gt_denoiser* d, ConvTc a, cudaStream_t st) {
     a.tmem_cols = uint32_t(sh.rows * sh.stride);
     a.err = d->err;
     const int grid = (a.w + kTcM - 1) / kTcM * ((a.h + a.rows - 1) / a.rows) * a.n;
-    k_conv_fwd_tc<<<grid, 128, tc_smem_bytes(a.n_mma, a.rows, a.stages), st>>>(a);
+    const int smem = tc_smem_bytes(a.n_mma, a.rows, a.stages);
+    if (!a.lo) {
+        ConvTma t;
+        std::memset(&t, 0, sizeof(t));
+        const cuuint64_t xd[4] = {cuuint64_t(a.cin), cuuint64_t(a.w), cuuint64_t(a.h), cuuint64_t(a.n)};
+        const cuuint64_t xs[3] = {cuuint64_t(a.cin) * 2, cuuint64_t(a.w) * a.cin * 2,
+                                  cuuint64_t(a.h) * a.w * a.cin * 2};
+        const cuuint32_t xb[4] = {8, 130, 1, 1};
+        const cuuint64_t wd[3] = {cuuint64_t(a.cin), 9, cuuint64_t(a.cout_p)};
+        const cuuint64_t ws[2] = {cuuint64_t(a.cin) * 2, cuuint64_t(a.cin) * 2 * 9};
+        const cuuint32_t wb[3] = {8, 1, cuuint32_t(a.n_mma)};
+        if (!encode_bf16(&t.x, a.x, 4, xd, xs, xb) || !encode_bf16(&t.wt, a.wt, 3, wd, ws, wb))
+            return fail(GT_ERR_CUDA, "cannot encode the denoiser's tensor maps");
+        t.cin = a.cin;
+        t.cout_p = a.cout_p;
+        t.n_mma = a.n_mma;
+        t.cout = a.cout;
+        t.bias = a.bias;
+        t.y = a.y;
+        t.ldy = a.ldy;
+        t.yoff = a.yoff;
+        t.yf = a.yf;
+        t.res = a.res;
+        t.relu = a.relu;
+        t.n = a.n;
+        t.h = a.h;
+        t.w = a.w;
+        t.rows = a.rows;
+        t.acc_stride = a.acc_stride;
+        t.stages = a.stages;
+        t.tmem_cols = a.tmem_cols;
+        t.err = a.err;
+        k_conv_fwd_tma<<<grid, 128, smem, st>>>(t);
+    } else {
+        k_conv_fwd_tc<<<grid, 128, smem, st>>>(a);
+    }
+    return GT_OK;
 }
 
 void conv(gt_denoiser* d, int li, const __nv_bfloat16* x, __nv_bfloat16* y, int ldy, float* yf, const float* res,
@@ -258,7 +326,7 @@ void conv(gt_denoiser* d, int li, const __nv_bfloat16* x, __nv_bfloat16* y, int 
     a.n = d->n;
     a.h = d->h >> lv;
     a.w = d->w >> lv;
-    launch_conv_tc(d, a, st);
+    if (launch_conv_tc(d, a, st) != GT_OK) d->launch_failed = true;
 }
 
 // Input gradient: the same convolution over dY with the flipped, transposed weights, no
@@ -277,13 +345,18 @@ void conv_dgrad(gt_denoiser* d, int li, const __nv_bfloat16* dy, __nv_bfloat16* 
     a.n = d->n;
     a.h = d->h >> lv;
     a.w = d->w >> lv;
-    launch_conv_tc(d, a, st);
+    if (launch_conv_tc(d, a, st) != GT_OK) d->launch_failed = true;
 }
 
 gt_status check_err(gt_denoiser* d, cudaStream_t st) {
+    if (d->launch_failed) {
+        d->launch_failed = false;
+        return fail(GT_ERR_CUDA, "cannot encode the denoiser's tensor maps");
+    }
     cudaError_t e = cudaMemcpyAsync(d->ctx->pinned, d->err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "denoiser");
+    if (d->ctx->pinned[0] & 2u) return fail(GT_ERR_INTERNAL, "denoiser shared memory is not 128-byte aligned");
     if (d->ctx->pinned[0]) return fail(GT_ERR_TIMEOUT, "denoiser tensor-core pipeline wait timed out");
     return GT_OK;
 }
@@ -454,6 +527,8 @@ gt_status gt_denoiser_create(gt_context* ctx, uint64_t seed, gt_denoiser** out) 
     al(reinterpret_cast<void**>(&d->err), sizeof(uint32_t));
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_conv_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemMax);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_conv_fwd_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemMax);
     d->wb.assign(d->layers.size(), nullptr);
     d->wf.assign(d->layers.size(), nullptr);
     d->dwp.assign(d->layers.size(), nullptr);

@@ -9,6 +9,7 @@
 // channels, K = pixels; k_conv_wgrad, mma.sync m16n8k16).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -263,6 +264,193 @@ __global__ void __launch_bounds__(128) k_conv_fwd_tc(ConvTc a) {
                 if (!store) continue;
                 if (a.y && !a.yf && cb + 16 <= a.cout && ((a.ldy | a.yoff) & 7) == 0) {
                     // 16 channels = two 16-byte stores
+                    uint32_t packed[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        float f0 = __uint_as_float(v[2 * j]) + (a.bias ? a.bias[cb + 2 * j] : 0.f);
+                        float f1 = __uint_as_float(v[2 * j + 1]) + (a.bias ? a.bias[cb + 2 * j + 1] : 0.f);
+                        if (a.relu) {
+                            f0 = fmaxf(f0, 0.f);
+                            f1 = fmaxf(f1, 0.f);
+                        }
+                        packed[j] = pack_bf16(__float2bfloat16(f0), __float2bfloat16(f1));
+                    }
+                    uint4* dst = reinterpret_cast<uint4*>(a.y + p * a.ldy + a.yoff + cb);
+                    dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                    dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                    continue;
+                }
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int co = cb + j;
+                    if (co >= a.cout) break;
+                    float f = __uint_as_float(v[j]) + (a.bias ? a.bias[co] : 0.f);
+                    if (a.relu) f = fmaxf(f, 0.f);
+                    if (a.y) a.y[p * a.ldy + a.yoff + co] = __float2bfloat16(f);
+                    if (a.yf) a.yf[p * a.cout + co] = f + (a.res ? a.res[p * a.cout + co] : 0.f);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
+}
+
+// The same convolution with its operands staged by TMA (cp.async.bulk.tensor) instead of
+// per-thread copies.  A box of 8 channels x 130 pixels of one input row lands as 130
+// consecutive 16-byte rows, which is exactly one 8-channel half of a staged row above; a
+// box of 8 channels x 1 tap x N output channels of the weights lands as one half of one
+// tap's B operand.  One thread produces and issues: per chunk it posts the chunk's byte
+// count on the stage's `full` mbarrier, issues the 2(R + 2) + 18 boxes (zero-filled outside
+// the image), waits for them, issues the chunk's 9R MMAs and commits them to the stage's
+// `done` mbarrier; the stage is refilled once those MMAs have read it.  The other threads
+// wait at a barrier until the last commit, then all read TMEM in the epilogue.
+struct ConvTma {
+    CUtensorMap x;          // [n][h][w][cin] BF16: dims (cin, w, h, n), box (8, 130, 1, 1)
+    CUtensorMap wt;         // [cout_p][9][cin] BF16: dims (cin, 9, cout_p), box (8, 1, n_mma)
+    int cin, cout_p, n_mma, cout;
+    const float* bias;
+    __nv_bfloat16* y;
+    int ldy, yoff;
+    float* yf;
+    const float* res;
+    int relu;
+    int n, h, w;
+    int rows, acc_stride, stages;
+    uint32_t tmem_cols;
+    uint32_t* err;
+};
+
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];\n" ::"r"(dst),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(mbar)
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(dst),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(mbar)
+        : "memory");
+}
+
+__global__ void __launch_bounds__(128) k_conv_fwd_tma(const __grid_constant__ ConvTma a) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem);      // kTcMaxStages
+    uint64_t* done = reinterpret_cast<uint64_t*>(smem + 32); // kTcMaxStages
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 64);
+    __shared__ int failed;
+    const int N = a.n_mma, R = a.rows, S = a.stages;
+    const int stage_bytes = tc_stage_bytes(N, R);
+    const int a_bytes = (R + 2) * kTcATile;
+    uint8_t* stage_base = smem + 128;
+    const int segs = (a.w + kTcM - 1) / kTcM, groups = (a.h + R - 1) / R;
+    const int seg = blockIdx.x % segs, rg = (blockIdx.x / segs) % groups, img = blockIdx.x / (segs * groups);
+    const int y0 = rg * R, x0 = seg * kTcM;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t chunk_bytes = uint32_t((R + 2) * 2 * 130 * 16 + 9 * 2 * N * 16);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                     "r"(a.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        failed = (smem_u32(stage_base) & 127u) != 0u; // TMA destinations must be 128-byte aligned
+        for (int s = 0; s < S; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&full[s])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&done[s])) : "memory");
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        if (failed) atomicOr(a.err, 2u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    const int nchunks = a.cin / 16;
+
+    if (tid == 0 && !failed) {
+        auto load = [&](int c, int s) {
+            const uint32_t A = smem_u32(stage_base + s * stage_bytes), B = A + a_bytes;
+            const uint32_t fb = smem_u32(&full[s]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"(chunk_bytes)
+                         : "memory");
+            for (int ri = 0; ri < R + 2; ++ri)
+                for (int half = 0; half < 2; ++half)
+                    tma_load_4d(A + ri * kTcATile + half * kTcRowBytes, &a.x, c * 16 + half * 8, x0 - 1, y0 + ri - 1,
+                                img, fb);
+            for (int tap = 0; tap < 9; ++tap)
+                for (int half = 0; half < 2; ++half)
+                    tma_load_3d(B + tap * N * 32 + half * N * 16, &a.wt, c * 16 + half * 8, tap, 0, fb);
+        };
+        const uint32_t idesc = tc_idesc(N);
+        for (int c = 0; c < S && c < nchunks; ++c) load(c, c);
+        bool ok = true;
+        for (int c = 0; c < nchunks && ok; ++c) {
+            const int s = c % S;
+            ok = mbar_wait(smem_u32(&full[s]), uint32_t((c / S) & 1), a.err);
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t A = smem_u32(stage_base + s * stage_bytes), B = A + a_bytes;
+            for (int tap = 0; tap < 9; ++tap) {
+                const int dyi = tap / 3, dxi = tap % 3;
+                const uint64_t bd = tc_desc(B + tap * N * 32, N * 16, 128);
+                const uint32_t acc = (c > 0 || tap > 0) ? 1u : 0u;
+                for (int r = 0; r < R; ++r) {
+                    const uint64_t ad = tc_desc(A + (r + dyi) * kTcATile + dxi * 16, kTcRowBytes, 128);
+                    asm volatile(
+                        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                            tmem + uint32_t(r * a.acc_stride)),
+                        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                        : "memory");
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smem_u32(&done[s]))
+                         : "memory");
+            // refill the stage of the previous chunk once its MMAs have read it
+            const int cp = c - 1, cn = cp + S;
+            if (cp >= 0 && cn < nchunks) {
+                ok = mbar_wait(smem_u32(&done[cp % S]), uint32_t((cp / S) & 1), a.err);
+                if (ok) load(cn, cp % S);
+            }
+        }
+        if (ok) {
+            const int last = nchunks - 1;
+            ok = mbar_wait(smem_u32(&done[last % S]), uint32_t((last / S) & 1), a.err);
+        }
+        if (!ok) failed = 1;
+    }
+    __syncthreads();
+    if (!failed) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const int px = x0 + tid;
+        for (int r = 0; r < R; ++r) {
+            const int y = y0 + r;
+            const size_t p = (size_t(img) * a.h + y) * a.w + px;
+            const bool store = px < a.w && y < a.h;
+            for (int cb = 0; cb < N; cb += 16) {
+                uint32_t v[16];
+                const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(r * a.acc_stride + cb);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+                    "%15}, [%16];\n"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                      "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                      "=r"(v[14]), "=r"(v[15])
+                    : "r"(taddr)
+                    : "memory");
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (!store) continue;
+                if (a.y && !a.yf && cb + 16 <= a.cout && ((a.ldy | a.yoff) & 7) == 0) {
                     uint32_t packed[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
