@@ -37,6 +37,7 @@ GT_MAT_ISOTROPIC = 2
 GT_MAT_GGX = 3
 GT_MAT_METAL = 4
 GT_MAT_DIELECTRIC = 5
+GT_MAT_HENYEY_GREENSTEIN = 6
 
 # gt_texture_kind
 GT_TEX_SOLID = 0

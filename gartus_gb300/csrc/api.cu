@@ -278,7 +278,7 @@ gt_status gt_scene_create(gt_context* ctx, const gt_scene_desc* d, gt_scene** ou
     if (d->num_primitives > (1u << 28)) return fail(GT_ERR_INVALID_ARG, "too many primitives");
     for (uint32_t i = 0; i < d->num_materials; ++i) {
         const gt_material& m = d->materials[i];
-        if (m.kind > GT_MAT_DIELECTRIC) return fail(GT_ERR_INVALID_ARG, "unknown material kind");
+        if (m.kind > GT_MAT_HENYEY_GREENSTEIN) return fail(GT_ERR_INVALID_ARG, "unknown material kind");
         if (m.texture_kind > GT_TEX_NOISE) return fail(GT_ERR_INVALID_ARG, "unknown texture kind");
         if (m.texture_kind == GT_TEX_NOISE) {
             const double v = m.tex[1], depth = m.tex[2], lo = m.tex[3], hi = m.tex[4];
@@ -291,6 +291,8 @@ gt_status gt_scene_create(gt_context* ctx, const gt_scene_desc* d, gt_scene** ou
         if (!finite3(m.color) || !std::isfinite(m.param)) return fail(GT_ERR_INVALID_ARG, "material values must be finite");
         if (m.kind == GT_MAT_DIELECTRIC && !(m.param > 0.0))
             return fail(GT_ERR_INVALID_ARG, "refractive index must be positive and finite");
+        if (m.kind == GT_MAT_HENYEY_GREENSTEIN && !(std::fabs(m.param) < 1.0)) // material.rs:1334-1343
+            return fail(GT_ERR_INVALID_ARG, "Henyey-Greenstein anisotropy must be finite and in (-1, 1)");
     }
     for (uint32_t i = 0; i < d->num_primitives; ++i) {
         gt_status rc = validate_geometry(d->primitives[i].geometry);

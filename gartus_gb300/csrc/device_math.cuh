@@ -27,6 +27,7 @@ template <> struct Num<float> {
     static GT_DEV float inf() { return __int_as_float(0x7f800000); }
     static GT_DEV float sqrt(float x) { return sqrtf(x); }
     static GT_DEV float acos(float x) { return acosf(x); }
+    static GT_DEV float pow(float x, float y) { return powf(x, y); }
     static GT_DEV float atan2(float y, float x) { return atan2f(y, x); }
     static GT_DEV void sincos(float x, float* s, float* c) { sincosf(x, s, c); }
     static GT_DEV float fabs(float x) { return fabsf(x); }
@@ -43,6 +44,7 @@ template <> struct Num<double> {
     static GT_DEV double inf() { return __longlong_as_double(0x7ff0000000000000ULL); }
     static GT_DEV double sqrt(double x) { return ::sqrt(x); }
     static GT_DEV double acos(double x) { return ::acos(x); }
+    static GT_DEV double pow(double x, double y) { return ::pow(x, y); }
     static GT_DEV double atan2(double y, double x) { return ::atan2(y, x); }
     static GT_DEV void sincos(double x, double* s, double* c) { ::sincos(x, s, c); }
     static GT_DEV double fabs(double x) { return ::fabs(x); }
@@ -199,16 +201,29 @@ template <class R> GT_DEV R schlick_f(R cosine, R f0) { // sampling.rs:240-247
     return f0 + (R(1) - f0) * pow5(R(1) - clampr(cosine, R(0), R(1)));
 }
 
-// MaterialPdf on the path: Sphere, Cosine, GgxReflection (pdf.rs:46-104).
-enum : int { PDF_SPHERE = 0, PDF_COSINE = 1, PDF_GGX = 2 };
+// HenyeyGreensteinPdf::phase_value (gmath/sampling.rs:126-136), SPHERE_AREA = 4 pi.
+template <class R> GT_DEV R hg_phase(R cosine, R g) {
+    if (!Num<R>::finite(cosine) || !Num<R>::finite(g) || Num<R>::fabs(g) >= R(1)) return R(0);
+    R den = (R(1) + g * g) - (R(2) * g) * clampr(cosine, R(-1), R(1));
+    if (den <= R(kEps)) return R(0);
+    return (R(1) - g * g) / (R(4.0 * kPi) * Num<R>::pow(den, R(1.5)));
+}
+
+// MaterialPdf on the path: Sphere, Cosine, GgxReflection, HenyeyGreenstein (pdf.rs:46-104).
+enum : int { PDF_SPHERE = 0, PDF_COSINE = 1, PDF_GGX = 2, PDF_HG = 3 };
 template <class R> struct MatPdf {
     int kind;
     Onb<R> basis;
     V3<R> out; // GGX outgoing
-    R rough, alpha;
+    R rough, alpha; // GGX roughness and alpha; HenyeyGreenstein: rough = g
 };
 template <class R> GT_DEV R matpdf_value(const MatPdf<R>& p, V3<R> dir) {
     if (p.kind == PDF_SPHERE) return R(1) / R(4.0 * kPi); // sampling.rs:31-41
+    if (p.kind == PDF_HG) {                             // sampling.rs:139-147
+        R l = Num<R>::sqrt(len2(dir));
+        if (l <= R(kEps)) return R(0);
+        return hg_phase(dot(dir, p.basis.w) / l, p.rough);
+    }
     if (p.kind == PDF_COSINE) {                         // sampling.rs:66-78
         R l = Num<R>::sqrt(len2(dir));
         if (l <= R(kEps)) return R(0);
@@ -225,6 +240,23 @@ template <class R> GT_DEV R matpdf_value(const MatPdf<R>& p, V3<R> dir) {
 }
 template <class R> GT_DEV V3<R> matpdf_generate(const MatPdf<R>& p, Rng& g) {
     if (p.kind == PDF_SPHERE) return unit_vector_spherical<R>(g);
+    if (p.kind == PDF_HG) { // sampling.rs:149-164
+        const R an = p.rough;
+        R r1 = rnd<R>(g);
+        R r2 = rnd<R>(g);
+        R ct;
+        if (Num<R>::fabs(an) < R(1e-3)) {
+            ct = R(1) - R(2) * r1;
+        } else {
+            R term = (R(1) - an * an) / ((R(1) - an) + (R(2) * an) * r1);
+            ct = clampr(((R(1) + an * an) - term * term) / (R(2) * an), R(-1), R(1));
+        }
+        R st = Num<R>::sqrt(Num<R>::fmax(R(1) - ct * ct, R(0)));
+        R phi = R(2.0 * kPi) * r2;
+        R s, c;
+        Num<R>::sincos(phi, &s, &c);
+        return onb_local(p.basis, V3<R>{c * st, s * st, ct});
+    }
     if (p.kind == PDF_COSINE) return onb_local(p.basis, cosine_direction<R>(g));
     R r1 = rnd<R>(g); // sampling.rs:274-298
     R r2 = rnd<R>(g);

@@ -398,6 +398,13 @@ template <class R> GT_DEV ScatterRec<R> mat_scatter(const MatDev<R>& m, V3<R> di
         s.pdf.kind = PDF_SPHERE;
         s.att = mat_color(m, h.p);
         return s;
+    case 6: // HenyeyGreenstein, material.rs:1281-1295: the phase function around the incoming ray
+        if (!onb_from_w(din, s.pdf.basis)) return s;
+        s.kind = SC_PDF;
+        s.pdf.kind = PDF_HG;
+        s.pdf.rough = m.param;
+        s.att = mat_color(m, h.p);
+        return s;
     case 3: { // GgxMicrofacet, material.rs:1583-1597; GgxReflectionPdf::new sampling.rs:146-170
         V3<R> outgoing = -normalize(din);
         if (!onb_from_w(h.n, s.pdf.basis)) return s;
@@ -449,6 +456,13 @@ template <class R> GT_DEV R mat_scattering_pdf(const MatDev<R>& m, V3<R> din, co
     }
     case 2:
         return R(1) / (R(4) * R(kPi));
+    case 6: { // material.rs:1297-1302
+        MatPdf<R> p;
+        p.kind = PDF_HG;
+        p.rough = m.param;
+        if (!onb_from_w(din, p.basis)) return R(0);
+        return matpdf_value(p, dout);
+    }
     case 3: { // material.rs:1599-1617 and ggx_reflection_scattering_weight 1717-1758
         V3<R> outgoing = -normalize(din);
         V3<R> incoming = normalize(dout);

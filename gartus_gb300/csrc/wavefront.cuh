@@ -555,7 +555,8 @@ GT_DEV uint32_t cost_class(int prim_kind_or_miss) {
     case 4: return 1; // Metal
     case 3: return 2; // GGX
     case 0:           // Lambertian
-    case 2: return 3; // Isotropic
+    case 2:           // Isotropic
+    case 6: return 3; // HenyeyGreenstein
     default: return 4; // DiffuseLight or a miss
     }
 }

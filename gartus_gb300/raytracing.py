@@ -149,6 +149,18 @@ class RayMaterial:
         return RayMaterial(abi.GT_MAT_ISOTROPIC, albedo)
 
     @staticmethod
+    def henyey_greenstein(albedo, g) -> "RayMaterial":
+        """HenyeyGreenstein::new (material.rs:1175-1205): phase-function scattering around
+        the incoming direction with anisotropy g in (-1, 1) (the reference panics outside)."""
+        g = float(g)
+        albedo = _vec(albedo)
+        if not _finite(albedo):
+            raise ValueError("Henyey-Greenstein albedo must be finite")
+        if not (math.isfinite(g) and abs(g) < 1.0):
+            raise ValueError("Henyey-Greenstein anisotropy must be finite and in (-1, 1)")
+        return RayMaterial(abi.GT_MAT_HENYEY_GREENSTEIN, albedo, g)
+
+    @staticmethod
     def ggx_microfacet(specular_color, roughness) -> "RayMaterial":
         c = _vec(specular_color)
         if not _finite(c, float(roughness)):

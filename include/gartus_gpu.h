@@ -77,7 +77,10 @@ typedef enum gt_material_kind {
     GT_MAT_ISOTROPIC = 2,     /* color = albedo                         (material.rs:1124-1147) */
     GT_MAT_GGX = 3,           /* color = specular colour, param = roughness (material.rs:1583-1622) */
     GT_MAT_METAL = 4,         /* color = albedo, param = fuzz           (material.rs:2087-2112) */
-    GT_MAT_DIELECTRIC = 5     /* param = refraction index               (material.rs:2264-2351) */
+    GT_MAT_DIELECTRIC = 5,    /* param = refraction index               (material.rs:2264-2351) */
+    GT_MAT_HENYEY_GREENSTEIN = 6 /* color = albedo, param = anisotropy g in (-1, 1): phase function
+                                    around the incoming direction (material.rs:1175-1333,
+                                    HenyeyGreensteinPdf gmath/sampling.rs:86-165)          */
 } gt_material_kind;
 
 /* Colour source of a material (graphics/raytracing/texture.rs SolidColor, CheckerTexture,

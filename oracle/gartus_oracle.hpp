@@ -790,8 +790,17 @@ template <class R> inline R specular_luminance(V3<R> c) { // material.rs:1760-17
     return rclamp(R(0.2126) * c.x + R(0.7152) * c.y + R(0.0722) * c.z, R(0), R(1));
 }
 
-// MaterialPdf (pdf.rs:46-104) restricted to Sphere / Cosine / GgxReflection.
-enum PdfKind { PDF_SPHERE = 0, PDF_COSINE = 1, PDF_GGX = 2 };
+// HenyeyGreensteinPdf::phase_value (gmath/sampling.rs:126-136), SPHERE_AREA = 4 pi.
+template <class R> inline R hg_phase(R cosine, R g) {
+    if (!std::isfinite(cosine) || !std::isfinite(g) || std::fabs(g) >= R(1)) return R(0);
+    R den = (R(1) + g * g) - (R(2) * g) * rclamp(cosine, R(-1), R(1));
+    if (den <= R(kEps)) return R(0);
+    return (R(1) - g * g) / (R(4.0 * kPi) * std::pow(den, R(1.5)));
+}
+
+// MaterialPdf (pdf.rs:46-104) restricted to Sphere / Cosine / GgxReflection /
+// HenyeyGreenstein.
+enum PdfKind { PDF_SPHERE = 0, PDF_COSINE = 1, PDF_GGX = 2, PDF_HG = 3 };
 template <class R> struct MatPdf {
     int kind = PDF_SPHERE;
     Onb<R> basis;
@@ -800,6 +809,11 @@ template <class R> struct MatPdf {
 
     R value(V3<R> dir) const {
         if (kind == PDF_SPHERE) return R(1) / R(4.0 * kPi); // sampling.rs:31-41
+        if (kind == PDF_HG) {                               // sampling.rs:139-147; roughness holds g
+            R len = length(dir);
+            if (len <= R(kEps)) return R(0);
+            return hg_phase(dot(dir, basis.w) / len, roughness);
+        }
         if (kind == PDF_COSINE) {                         // sampling.rs:66-78
             R len = length(dir);
             if (len <= R(kEps)) return R(0);
@@ -818,6 +832,21 @@ template <class R> struct MatPdf {
     }
     V3<R> generate(SampleRng& rng) const {
         if (kind == PDF_SPHERE) return rng.random_unit_vector_spherical<R>();
+        if (kind == PDF_HG) { // sampling.rs:149-164
+            const R g = roughness;
+            R r1 = rng.random_double<R>();
+            R r2 = rng.random_double<R>();
+            R cos_t;
+            if (std::fabs(g) < R(1e-3)) {
+                cos_t = R(1) - R(2) * r1;
+            } else {
+                R term = (R(1) - g * g) / ((R(1) - g) + (R(2) * g) * r1);
+                cos_t = rclamp(((R(1) + g * g) - term * term) / (R(2) * g), R(-1), R(1));
+            }
+            R sin_t = std::sqrt(rmax(R(1) - cos_t * cos_t, R(0)));
+            R phi = R(2.0 * kPi) * r2;
+            return basis.local(V3<R>(std::cos(phi) * sin_t, std::sin(phi) * sin_t, cos_t));
+        }
         if (kind == PDF_COSINE) return basis.local(rng.random_cosine_direction<R>());
         // sampling.rs:274-298
         R r1 = rng.random_double<R>();
@@ -856,6 +885,13 @@ template <class R> inline Scatter<R> scatter(const Material<R>& m, const Ray<R>&
     case GT_MAT_ISOTROPIC: // material.rs:1124-1137
         s.kind = SCATTER_PDF;
         s.pdf.kind = PDF_SPHERE;
+        s.att = m.sample(h);
+        return s;
+    case GT_MAT_HENYEY_GREENSTEIN: // material.rs:1281-1295: around the incoming direction
+        if (!Onb<R>::from_w(in.d, s.pdf.basis)) return s;
+        s.kind = SCATTER_PDF;
+        s.pdf.kind = PDF_HG;
+        s.pdf.roughness = m.param;
         s.att = m.sample(h);
         return s;
     case GT_MAT_GGX: { // material.rs:1583-1597, GgxReflectionPdf::new sampling.rs:146-170
@@ -916,6 +952,13 @@ template <class R> inline R scattering_pdf(const Material<R>& m, const Ray<R>& i
     }
     case GT_MAT_ISOTROPIC:
         return R(1) / (R(4) * R(kPi)); // material.rs:1139-1141
+    case GT_MAT_HENYEY_GREENSTEIN: {  // material.rs:1297-1302
+        MatPdf<R> p;
+        p.kind = PDF_HG;
+        p.roughness = m.param;
+        if (!Onb<R>::from_w(in.d, p.basis)) return R(0);
+        return p.value(out_dir);
+    }
     case GT_MAT_GGX: {                  // material.rs:1599-1617, 1717-1758
         V3<R> outgoing = -normalized(in.d);
         V3<R> incoming = normalized(out_dir);

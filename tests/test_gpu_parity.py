@@ -602,3 +602,27 @@ def test_schedules_agree(gpu_context, schedule, tail, grid, width, stripes):
                     stripes=stripes).render_with_lights_hdr_image(scene, lights)
     fb = PathTracer(cam, context=gpu_context, schedule="persistent").render_with_lights_hdr_image(scene, lights)
     assert _divergent(fa.pixels, fb.pixels.astype(np.float64)) <= 0.05 * fa.pixels.shape[0] * fa.pixels.shape[1]
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_henyey_greenstein_spheres(gpu_context, precision):
+    # HenyeyGreenstein (material.rs:1175-1333): forward, backward and nearly isotropic
+    # (|g| < 1e-3 takes the isotropic branch) phase functions around the incoming ray.
+    scene = RayScene()
+    ground = scene.add_material(RayMaterial.lambertian((0.5, 0.5, 0.5)))
+    scene.add_sphere((0.0, -100.5, -1.0), 100.0, ground)
+    for x, g in ((-1.1, 0.6), (0.0, -0.4), (1.1, 0.0005)):
+        scene.add_sphere((x, 0.0, -1.2), 0.5, scene.add_material(RayMaterial.henyey_greenstein((0.8, 0.7, 0.6), g)))
+    scene.build_bvh()
+    cam = RayCamera(48, 1.5).with_samples_per_pixel(8).with_max_depth(10)
+    ref, acc = _oracle_render(scene, cam)
+    if precision == "f64":
+        img = PathTracer(cam, precision="f64", context=gpu_context).render_hdr_image(scene, want64=True)
+        np.testing.assert_array_equal(img.accepted, acc)
+        err = rel_err(img.pixels64, ref, floor=1e-12).max(axis=2)
+        assert (err <= 1e-9).mean() >= 0.99, err.max()
+    else:
+        img = PathTracer(cam, context=gpu_context).render_hdr_image(scene)
+        assert _divergent(img.pixels, ref) <= 0.05 * ref.shape[0] * ref.shape[1]
+    with pytest.raises(ValueError):
+        RayMaterial.henyey_greenstein((0.5, 0.5, 0.5), 1.0)

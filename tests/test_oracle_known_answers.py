@@ -409,3 +409,33 @@ def test_perlin_matches_independent_restatement():
     p = pts[2]
     want = abs(sum(0.5 ** k * _perlin(9, [p * 2.0 ** k])[0] for k in range(5)))
     assert abs(_perlin(9, [p], depth=5)[0] - want) <= 1e-15
+
+
+def _hg_pdf(g, forward, direction):
+    m = material(abi.GT_MAT_HENYEY_GREENSTEIN, (0.5, 0.5, 0.5), g)
+    return L.orc_scattering_pdf(C.byref(m), dptr([0, 0, 0] + list(forward) + [0]), dptr([0, 0, 0]),
+                                dptr([0, 0, 1]), 1, dptr(direction))
+
+
+def test_henyey_greenstein_pdf_biases_forward_or_backward():  # gmath/sampling.rs:485-497
+    close(_hg_pdf(0.0, (0, 0, 1), (0.25, 0.0, math.sqrt(1 - 0.0625))), 1.0 / (4.0 * math.pi))
+    assert _hg_pdf(0.6, (0, 0, 1), (0, 0, 1)) > _hg_pdf(0.6, (0, 0, 1), (0, 0, -1))
+    assert _hg_pdf(-0.6, (0, 0, 1), (0, 0, -1)) > _hg_pdf(-0.6, (0, 0, 1), (0, 0, 1))
+    # the phase function of g: (1 - g^2) / (4 pi (1 + g^2 - 2 g cos)^1.5), and 0 for a null direction
+    g, c = 0.3, 0.5
+    close(_hg_pdf(g, (0, 0, 2), (math.sqrt(1 - c * c), 0, c)),
+          (1 - g * g) / (4 * math.pi * (1 + g * g - 2 * g * c) ** 1.5))
+    assert _hg_pdf(g, (0, 0, 1), (0, 0, 0)) == 0.0
+
+
+def test_henyey_greenstein_samples_mean_cosine_near_anisotropy():  # gmath/sampling.rs:499-514
+    g = 0.55
+    m = material(abi.GT_MAT_HENYEY_GREENSTEIN, (0.2, 0.4, 0.6), g)
+    total = 0.0
+    n = 8192
+    for seed in range(n):
+        k, d, a = _scatter(m, [0, 0, 0, 0, 0, 3, 0], [0, 0, 0], [0, 0, 1], True, 107 + seed)
+        assert k == 2 and a == [0.2, 0.4, 0.6]  # a pdf scatter with the albedo
+        assert abs(math.sqrt(sum(x * x for x in d)) - 1.0) <= 1e-12
+        total += d[2]
+    assert abs(total / n - g) <= 0.035
