@@ -214,10 +214,10 @@ gt_status refresh_weights(gt_denoiser* d, cudaStream_t st) {
 struct TcShape {
     int rows, stride, stages;
 };
-constexpr TcShape tc_shape(int n) {
-    return TcShape{tc_pow2_cols(n) <= 128 ? 4 : 2, tc_pow2_cols(n),
-                   (tc_pow2_cols(n) <= 128 ? 4 : 2) * tc_pow2_cols(n) <= 256 ? 2 : 3};
+constexpr TcShape tc_shape_rows(int n, int rows) {
+    return TcShape{rows, tc_pow2_cols(n), rows * tc_pow2_cols(n) <= 256 ? 2 : 3};
 }
+constexpr TcShape tc_shape(int n) { return tc_shape_rows(n, tc_pow2_cols(n) <= 128 ? 4 : 2); }
 // Largest shared-memory request (N = 176, the input gradient of the deepest decoder layer,
 // and N = 96).
 constexpr int kTcSmemMax =
@@ -259,7 +259,13 @@ bool encode_bf16(CUtensorMap* m, const void* base, int rank, const cuuint64_t* d
 // staging when it is read as an upsampled half plus a skip tensor.
 gt_status launch_conv_tc(gt_denoiser* d, ConvTc a, cudaStream_t st) {
     a.n_mma = (a.cout_p + 15) / 16 * 16;
-    const TcShape sh = tc_shape(a.n_mma);
+    // Rows per CTA: the most that tensor memory allows, halved while the grid would give
+    // fewer than two CTAs per SM (the deep, small levels).
+    TcShape sh = tc_shape(a.n_mma);
+    const int sms = d->ctx->num_sms > 0 ? d->ctx->num_sms : 1;
+    const int segs = (a.w + kTcM - 1) / kTcM;
+    while (sh.rows > 1 && segs * ((a.h + sh.rows - 1) / sh.rows) * a.n < 2 * sms)
+        sh = tc_shape_rows(a.n_mma, sh.rows / 2);
     a.rows = sh.rows;
     a.acc_stride = sh.stride;
     a.stages = sh.stages;
