@@ -504,7 +504,10 @@ def run_ours(args):
     b_state = 2 * (32 + 12 + 8 + 4 + 4) + 8
     bytes_per_unit = {"trace": b_ray, "shade": float(b_state), "generate": float(b_state), "shadow": b_ray,
                       "persistent": b_ray}
-    units = {"trace": ps["rays"], "shade": ps["rays"], "generate": ps["samples_started"], "shadow": ps["shadow_rays"],
+    # closest-hit queries of the wavefront kernels: all of them less those traced inside
+    # k_persistent (exact without next-event shadow rays, which k_persistent also counts)
+    wave_rays = max(ps["rays"] - ps["persistent_rays"], 0)
+    units = {"trace": wave_rays, "shade": wave_rays, "generate": ps["samples_started"], "shadow": ps["shadow_rays"],
              "persistent": ps["persistent_rays"]}
     launches_dom = max(ps["kernel_launches"][dom], 1)
     avg_ms = kms[dom] / launches_dom
@@ -512,6 +515,15 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     achieved = algo_bytes / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else 0.0
     traffic = traffic_from_profiles(f"k_{dom}", cfg["workload"])
+    # every kernel's own roofline point from the same profiled frame
+    per_kernel = {}
+    for k in ("generate", "trace", "shade", "shadow", "persistent"):
+        nl = ps["kernel_launches"][k]
+        if nl == 0 or kms[k] <= 0:
+            continue
+        gbs = units[k] * bytes_per_unit[k] / nl / (kms[k] / nl / 1e3) / 1e9
+        per_kernel[f"k_{k}"] = {"achieved": gbs, "frac": gbs / peak, "avg_launch_ms": kms[k] / nl, "launches": nl,
+                                "bytes_per_unit": bytes_per_unit[k], "units_per_launch": units[k] / nl}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -536,7 +548,7 @@ def run_ours(args):
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "algorithmic_bytes_per_launch": algo_bytes,
                          "avg_launch_ms": avg_ms, "bytes_per_unit": bytes_per_unit[dom],
-                         "units_per_launch": units[dom] / launches_dom},
+                         "units_per_launch": units[dom] / launches_dom, "per_kernel": per_kernel},
             "cpu_baseline": cpu,
             "detail": {"wall_s_timed": wall_s, "rays_per_s": rays / (dev_ms / 1e3), "kernel_ms_profiled": kms,
                        "kernel_launches_profiled": ps["kernel_launches"], "iterations_per_frame": ps["iterations"],
