@@ -525,10 +525,10 @@ def main(argv=None) -> int:
     import torch
 
     ap = argparse.ArgumentParser(description="Train the denoiser on scenes rendered by this path tracer.")
-    ap.add_argument("--scenes", type=int, default=768)
+    ap.add_argument("--scenes", type=int, default=1536)
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--high-spp", type=int, default=1024)
-    ap.add_argument("--steps", type=int, default=12000)
+    ap.add_argument("--steps", type=int, default=24000)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--crop", type=int, default=128)
     ap.add_argument("--lr", type=float, default=2e-3)

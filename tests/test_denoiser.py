@@ -242,7 +242,7 @@ def test_committed_weights_file():
 @pytest.mark.gpu
 @pytest.mark.parametrize("seed", [100000, 100001, 100002])
 def test_trained_denoiser_beats_plain(gpu_context, seed):
-    """The committed network (trained on scenes 0..767 of training_scene) on held-out
+    """The committed network (trained on scenes 0..1535 of training_scene) on held-out
     scenes of each family at 8 spp, against an independent 1024-spp render: the denoised
     image's relMSE is at most a fifth of the plain render's, and the per-tile fallback
     keeps nearly all of the gain."""
