@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--tail-slots", type=int, default=0,
                     help="auto schedule: unfinished pixels at which the persistent kernel takes over (0 = library)")
     ap.add_argument("--stripes", type=int, default=0, help="wavefront stripes (0 = library default)")
+    ap.add_argument("--gpu-bvh", action="store_true",
+                    help="the f32 path traverses a linear BVH built on the GPU (GT_BVH_GPU_LBVH)")
     ap.add_argument("--autotune", action="store_true",
                     help="pick stripes, tail size and blocks per SM with gt_autotune before the warm-up")
     ap.add_argument("--width", type=int, default=0, help="smaller image for profiling runs (0 = the workload's)")
@@ -358,6 +360,9 @@ def run_ours(args):
     torch.cuda.set_device(device)
     ctx = Context(device)
     scene, lights, env, cam, cfg = workload(args.config, args.width, args.grid)
+    if args.gpu_bvh:
+        scene.use_gpu_bvh()
+        cfg = dict(cfg, bvh="linear BVH built on the GPU at upload (GT_BVH_GPU_LBVH)")
     cams = cam if isinstance(cam, list) else None
     if cams is not None:
         cam = cams[0]
@@ -428,6 +433,7 @@ def run_ours(args):
         d = abi.gt_scene_desc()
         d.struct_size = C.sizeof(abi.gt_scene_desc)
         d.num_primitives, d.num_materials, d.bvh_leaf_size = len(prims), len(mats), scene.leaf_size
+        d.bvh_builder = scene._bvh_builder
         d.primitives = prims.ctypes.data_as(C.POINTER(abi.gt_primitive))
         d.materials = mats.ctypes.data_as(C.POINTER(abi.gt_material))
         sh, lh = C.c_void_p(), C.c_void_p()

@@ -39,6 +39,9 @@ GT_MAT_METAL = 4
 GT_MAT_DIELECTRIC = 5
 GT_MAT_HENYEY_GREENSTEIN = 6
 
+GT_BVH_REFERENCE_SAH = 0
+GT_BVH_GPU_LBVH = 1
+
 # gt_texture_kind
 GT_TEX_SOLID = 0
 GT_TEX_CHECKER = 1
@@ -96,6 +99,8 @@ class gt_scene_desc(C.Structure):
         ("num_materials", C.c_uint32),
         ("bvh_leaf_size", C.c_uint32),
         ("materials", C.POINTER(gt_material)),
+        ("bvh_builder", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
 
 

@@ -32,6 +32,7 @@ UNITS = [
     ("render_f64.cu", ["-fmad=false"]),
     ("noalloc.cu", ["-fmad=true"]),
     ("denoise.cu", ["-fmad=true"]),
+    ("lbvh.cu", ["-fmad=true"]),
 ]
 CXX_UNITS = ["bvh_build.cpp", "scene_tables.cpp"]
 

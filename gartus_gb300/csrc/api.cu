@@ -148,6 +148,14 @@ gt_status fail(gt_status status, const std::string& msg) {
     g_last_error = msg;
     return status;
 }
+gt_status ensure_reference_bvh(gt_scene* s) {
+    if (s->bvh_ready) return GT_OK;
+    build_reference_bvh(s->prims.data(), uint32_t(s->prims.size()), s->leaf_size, s->bvh);
+    if (s->bvh.max_depth + 1 > 62) return fail(GT_ERR_UNSUPPORTED, "BVH deeper than the device traversal stack");
+    s->bvh_ready = true;
+    return GT_OK;
+}
+
 gt_status cuda_fail(cudaError_t e, const char* what) {
     g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? GT_ERR_OOM : GT_ERR_CUDA;
@@ -301,14 +309,20 @@ gt_status gt_scene_create(gt_context* ctx, const gt_scene_desc* d, gt_scene** ou
             return fail(GT_ERR_INVALID_ARG, "ray scene material id out of bounds"); // scene.rs:1158-1161
     }
     std::lock_guard<std::mutex> lock(ctx->mu);
+    const uint32_t builder = d->struct_size >= sizeof(gt_scene_desc) ? d->bvh_builder : 0u;
+    if (builder > GT_BVH_GPU_LBVH) return fail(GT_ERR_INVALID_ARG, "unknown BVH builder");
     auto* s = new gt_scene();
     s->ctx = ctx;
     s->prims.assign(d->primitives, d->primitives + d->num_primitives);
     s->mats.assign(d->materials, d->materials + d->num_materials);
-    build_reference_bvh(s->prims.data(), d->num_primitives, d->bvh_leaf_size ? d->bvh_leaf_size : 4u, s->bvh);
-    if (s->bvh.max_depth + 1 > 62) {
-        delete s;
-        return fail(GT_ERR_UNSUPPORTED, "BVH deeper than the device traversal stack");
+    s->bvh_builder = builder;
+    s->leaf_size = d->bvh_leaf_size ? d->bvh_leaf_size : 4u;
+    if (builder == GT_BVH_REFERENCE_SAH) {
+        const gt_status rc = ensure_reference_bvh(s);
+        if (rc != GT_OK) {
+            delete s;
+            return rc;
+        }
     }
     *out = s;
     return GT_OK;
@@ -326,9 +340,15 @@ void gt_scene_destroy(gt_scene* s) {
 }
 
 gt_status gt_scene_bvh_node_count(const gt_scene* s, uint32_t* count) {
+    GT_GUARD_BEGIN
     if (!s || !count) return fail(GT_ERR_INVALID_ARG, "null argument");
+    gt_scene* m = const_cast<gt_scene*>(s);
+    std::lock_guard<std::mutex> lock(m->ctx->mu);
+    const gt_status rc = ensure_reference_bvh(m);
+    if (rc != GT_OK) return rc;
     *count = uint32_t(s->bvh.nodes.size());
     return GT_OK;
+    GT_GUARD_END
 }
 
 gt_status gt_scene_emissive_targets(const gt_scene* s, gt_light_target* targets, uint32_t capacity, uint32_t* count) {

@@ -112,6 +112,9 @@ struct gt_scene {
     gt_context* ctx = nullptr;
     std::vector<gt_primitive> prims;
     std::vector<gt_material> mats;
+    uint32_t bvh_builder = GT_BVH_REFERENCE_SAH;
+    uint32_t leaf_size = 4;
+    bool bvh_ready = false; // `bvh` has been built (eagerly for the reference builder)
     gt::BuiltBvh bvh;
     gt::GpuScene<float> f32;
     gt::GpuScene<double> f64;
@@ -162,4 +165,13 @@ void free_lights_f64(gt_lights* l);
 void free_env_f32(gt_environment* e);
 void free_env_f64(gt_environment* e);
 
+} // namespace gt
+
+namespace gt {
+// The reference-layout SAH tree of `s`, built on first use (api.cu).
+gt_status ensure_reference_bvh(gt_scene* s);
+// A linear BVH for the f32 path built on the device from f32 primitive bounds; permutes
+// g.prims / g.meta into leaf order and sets the view's nodes and root (lbvh.cu).
+gt_status build_lbvh_f32(GpuScene<float>& g, uint32_t n, const float* boxes_host, const double* bounds_lo,
+                         const double* bounds_hi, cudaStream_t st, int sms);
 } // namespace gt

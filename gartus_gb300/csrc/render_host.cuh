@@ -76,12 +76,36 @@ template <class R> void free_gpu(gt_scene* s) {
 template <class R> gt_status upload_scene(gt_scene* s) {
     GpuScene<R>& g = gpu_of<R>(s);
     if (g.ready) return GT_OK;
+    // The f32 path of a GT_BVH_GPU_LBVH scene builds its tree on the device from the
+    // primitives in their given order; everything else uses the reference's SAH tree.
+    const bool gpu_bvh = sizeof(R) == 4 && s->bvh_builder == GT_BVH_GPU_LBVH;
+    if (!gpu_bvh) {
+        const gt_status rc = ensure_reference_bvh(s);
+        if (rc != GT_OK) return rc;
+    }
     const BuiltBvh& bvh = s->bvh;
     const size_t n = s->prims.size();
     std::vector<PrimRec<R>> recs(n);
     std::vector<uint2> meta(n);
+    std::vector<float> boxes(gpu_bvh ? n * 6 : 0); // f32 bounds, rounded outward
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};   // bounds of the box centres
+    if (gpu_bvh) {
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = 1e300;
+            hi[a] = -1e300;
+        }
+        for (size_t j = 0; j < n; ++j) {
+            const Aabb b = geometry_aabb(s->prims[j].geometry);
+            put_box<float>(boxes.data() + j * 6, b);
+            for (int a = 0; a < 3; ++a) {
+                const double c = 0.5 * (b.lo[a] + b.hi[a]);
+                lo[a] = std::fmin(lo[a], c);
+                hi[a] = std::fmax(hi[a], c);
+            }
+        }
+    }
     for (size_t j = 0; j < n; ++j) {
-        const uint32_t pi = bvh.order[j];
+        const uint32_t pi = gpu_bvh ? uint32_t(j) : bvh.order[j];
         const gt_primitive& p = s->prims[pi];
         const double* q = p.geometry.p;
         R* v = recs[j].v;
@@ -145,9 +169,10 @@ template <class R> gt_status upload_scene(gt_scene* s) {
         meta[j] = make_uint2(kind | (p.material << 3), pi);
     }
     // Internal nodes, renumbered densely in pre-order; leaf children become links.
-    std::vector<int32_t> internal_id(bvh.nodes.size(), -1);
+    const size_t ref_nodes = gpu_bvh ? 0 : bvh.nodes.size();
+    std::vector<int32_t> internal_id(ref_nodes, -1);
     int32_t ni = 0;
-    for (size_t i = 0; i < bvh.nodes.size(); ++i)
+    for (size_t i = 0; i < ref_nodes; ++i)
         if (!bvh.nodes[i].leaf) internal_id[i] = ni++;
     std::vector<Node<R>> nodes(static_cast<size_t>(ni));
     auto link_of = [&](uint32_t child, int32_t& link, int32_t& count) {
@@ -160,7 +185,7 @@ template <class R> gt_status upload_scene(gt_scene* s) {
             count = 0;
         }
     };
-    for (size_t i = 0; i < bvh.nodes.size(); ++i) {
+    for (size_t i = 0; i < ref_nodes; ++i) {
         const BuildNode& b = bvh.nodes[i];
         if (b.leaf) continue;
         Node<R>& nd = nodes[size_t(internal_id[i])];
@@ -234,7 +259,16 @@ template <class R> gt_status upload_scene(gt_scene* s) {
     v.mats = g.mats;
     v.num_prims = uint32_t(n);
     v.num_nodes = uint32_t(nodes.size());
-    if (!bvh.nodes.empty()) {
+    if (gpu_bvh && n > 0) {
+        cudaFree(g.nodes); // the device builder allocates its own node array
+        g.nodes = nullptr;
+        v.nodes = nullptr;
+        const int sms = s->ctx->num_sms > 0 ? s->ctx->num_sms : 1;
+        if constexpr (sizeof(R) == 4) {
+            const gt_status rc = build_lbvh_f32(g, uint32_t(n), boxes.data(), lo, hi, st, sms);
+            if (rc != GT_OK) return rc;
+        }
+    } else if (!gpu_bvh && !bvh.nodes.empty()) {
         put_box<R>(v.root_box, bvh.nodes[0].box);
         link_of(0, v.root_link, v.root_count);
     } else { // an empty scene: a root box that no ray can enter

@@ -310,7 +310,8 @@ class Context:
 
 
 class _SceneHandle:
-    def __init__(self, ctx: Context, prims: np.ndarray, mats: np.ndarray, leaf_size: int):
+    def __init__(self, ctx: Context, prims: np.ndarray, mats: np.ndarray, leaf_size: int,
+                 bvh_builder: int = abi.GT_BVH_REFERENCE_SAH):
         self.ctx = ctx
         prims = np.ascontiguousarray(prims)
         mats = np.ascontiguousarray(mats)
@@ -321,6 +322,7 @@ class _SceneHandle:
         d.num_materials = len(mats)
         d.materials = mats.ctypes.data_as(C.POINTER(abi.gt_material))
         d.bvh_leaf_size = leaf_size
+        d.bvh_builder = bvh_builder
         h = C.c_void_p()
         check(lib().gt_scene_create(ctx.handle, C.byref(d), C.byref(h)))
         self.h = h
@@ -369,6 +371,7 @@ class RayScene:
         self._chunks: list[np.ndarray] = []
         self._prims: Optional[np.ndarray] = np.zeros(0, dtype=PRIMITIVE_DTYPE)
         self._leaf_size = 4
+        self._bvh_builder = abi.GT_BVH_REFERENCE_SAH
         self._handles: dict = {}
 
     # -- tables
@@ -440,6 +443,16 @@ class RayScene:
     def build_bvh(self) -> None:
         self.build_bvh_with_options(4)
 
+    def use_gpu_bvh(self, enabled: bool = True) -> "RayScene":
+        """The f32 path traverses a linear BVH built on the GPU at upload (gt_bvh_builder
+        GT_BVH_GPU_LBVH) instead of the reference's SAH tree, which is then built on the
+        host only for f64 rendering and traversal statistics.  For large scenes."""
+        builder = abi.GT_BVH_GPU_LBVH if enabled else abi.GT_BVH_REFERENCE_SAH
+        if builder != self._bvh_builder:
+            self._bvh_builder = builder
+            self._invalidate()
+        return self
+
     def build_bvh_with_options(self, leaf_size: int = 4) -> None:
         """BvhBuildOptions::with_leaf_size clamps 0 to 1 (bvh.rs:73-77)."""
         self._leaf_size = max(int(leaf_size), 1)
@@ -497,7 +510,8 @@ class RayScene:
     def _handle(self, ctx: Context) -> _SceneHandle:
         h = self._handles.get(id(ctx))
         if h is None or h.ctx is not ctx or not h.h:
-            h = _SceneHandle(ctx, self.primitives_array(), self.materials_array(), self._leaf_size)
+            h = _SceneHandle(ctx, self.primitives_array(), self.materials_array(), self._leaf_size,
+                             self._bvh_builder)
             self._handles[id(ctx)] = h
         return h
 

@@ -111,6 +111,16 @@ typedef struct gt_material {
 
 /* A compiled RayScene (raytracing/scene.rs:1102-1106) with its BVH build options
  * (BvhBuildOptions, raytracing/bvh.rs:55-89). */
+/* Which tree the f32 throughput path traverses. */
+typedef enum gt_bvh_builder {
+    GT_BVH_REFERENCE_SAH = 0, /* the reference's binary SAH tree, built on the host at creation */
+    GT_BVH_GPU_LBVH = 1       /* a linear BVH built on the GPU when the scene is uploaded (Morton
+                                 order, Karras 2012): for large scenes whose host build would
+                                 dominate; f64 rendering and the traversal statistics still use
+                                 the reference tree, built on the host when first needed.  No
+                                 reference counterpart.                                        */
+} gt_bvh_builder;
+
 typedef struct gt_scene_desc {
     uint32_t struct_size; /* sizeof(gt_scene_desc) */
     uint32_t num_primitives;
@@ -118,6 +128,8 @@ typedef struct gt_scene_desc {
     uint32_t num_materials;
     uint32_t bvh_leaf_size; /* 0 selects the reference default of 4 */
     const gt_material* materials;
+    uint32_t bvh_builder;   /* gt_bvh_builder */
+    uint32_t reserved;
 } gt_scene_desc;
 
 /* One weighted sampling target (WeightedSamplingTargetList, raytracing/scene.rs:423-497).

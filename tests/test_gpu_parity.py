@@ -626,3 +626,52 @@ def test_henyey_greenstein_spheres(gpu_context, precision):
         assert _divergent(img.pixels, ref) <= 0.05 * ref.shape[0] * ref.shape[1]
     with pytest.raises(ValueError):
         RayMaterial.henyey_greenstein((0.5, 0.5, 0.5), 1.0)
+
+
+def test_gpu_bvh_matches_reference_tree(gpu_context):
+    # GT_BVH_GPU_LBVH: the f32 path traverses a tree built on the device (Morton order,
+    # Karras 2012).  The closest hits are the same primitives as with the reference SAH tree
+    # (only exact ties may resolve differently), so the f32 images agree with the SAH
+    # tree's and with the oracle within the f32 tolerance; f64 still uses the SAH tree.
+    scene, env = scenes.mesh_heavy_scene(size=40, tori=6, rings=8, tube=12, env_width=256, env_height=128)
+    cam = scenes.mesh_heavy_camera(48, 27, 2, 8)
+    sah = PathTracer(cam, context=gpu_context).render_with_environment_hdr_image(scene, env)
+    scene.use_gpu_bvh()
+    gpu = PathTracer(cam, context=gpu_context).render_with_environment_hdr_image(scene, env)
+    n = sah.pixels.shape[0] * sah.pixels.shape[1]
+    np.testing.assert_array_equal(gpu.accepted, sah.accepted)
+    assert _divergent(gpu.pixels, sah.pixels.astype(np.float64)) <= 0.02 * n
+    ref, _ = _oracle_render(scene, cam, env=env)
+    assert _divergent(gpu.pixels, ref) <= 0.1 * n
+    img64 = PathTracer(cam, precision="f64", context=gpu_context).render_with_environment_hdr_image(scene, env,
+                                                                                                  want64=True)
+    err = rel_err(img64.pixels64, ref, floor=1e-12).max(axis=2)
+    assert (err <= 1e-9).mean() >= 0.99
+    assert scene.bvh_node_count(gpu_context) > 0  # the reference tree, built on demand
+
+
+def test_gpu_bvh_edge_cases(gpu_context):
+    cam = RayCamera(16, 1.0).with_samples_per_pixel(2).with_max_depth(4).with_look_at((0, 0, 3), (0, 0, 0))
+    # one primitive (a leaf root) and an empty scene
+    for count in (1, 0):
+        s = RayScene()
+        m = s.add_material(RayMaterial.lambertian((0.5, 0.5, 0.5)))
+        for _ in range(count):
+            s.add_sphere((0.0, 0.0, 0.0), 0.5, m)
+        s.build_bvh()
+        a = PathTracer(cam, context=gpu_context).render_hdr_image(s)
+        s.use_gpu_bvh()
+        b = PathTracer(cam, context=gpu_context).render_hdr_image(s)
+        np.testing.assert_array_equal(a.pixels, b.pixels)
+    # many primitives with one box centre: equal Morton codes, split by index
+    s = RayScene()
+    m = s.add_material(RayMaterial.lambertian((0.5, 0.6, 0.7)))
+    for k in range(300):
+        r = 0.2 + 0.001 * k
+        s.add_sphere((0.0, 0.0, 0.0), r, m)
+    s.add_sphere((0.0, -100.5, 0.0), 100.0, m)
+    s.build_bvh()
+    a = PathTracer(cam, context=gpu_context).render_hdr_image(s)
+    s.use_gpu_bvh()
+    b = PathTracer(cam, context=gpu_context).render_hdr_image(s)
+    assert _divergent(b.pixels, a.pixels.astype(np.float64)) <= 0.02 * a.pixels.shape[0] * a.pixels.shape[1]
