@@ -46,6 +46,12 @@ GT_BVH_GPU_LBVH = 1
 GT_TEX_SOLID = 0
 GT_TEX_CHECKER = 1
 GT_TEX_NOISE = 2
+GT_TEX_IMAGE = 3
+# gt_texture_filter / gt_texture_wrap
+GT_FILTER_NEAREST = 0
+GT_FILTER_LINEAR = 1
+GT_WRAP_CLAMP = 0
+GT_WRAP_REPEAT = 1
 # gt_noise_variant
 GT_NOISE_PLAIN = 0
 GT_NOISE_TURBULENCE = 1
@@ -91,6 +97,18 @@ class gt_material(C.Structure):
     ]
 
 
+class gt_image(C.Structure):
+    _fields_ = [
+        ("width", C.c_uint32),
+        ("height", C.c_uint32),
+        ("rgb", C.c_void_p),
+        ("filter", C.c_uint32),
+        ("wrap_s", C.c_uint32),
+        ("wrap_t", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
 class gt_scene_desc(C.Structure):
     _fields_ = [
         ("struct_size", C.c_uint32),
@@ -100,7 +118,8 @@ class gt_scene_desc(C.Structure):
         ("bvh_leaf_size", C.c_uint32),
         ("materials", C.POINTER(gt_material)),
         ("bvh_builder", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("num_images", C.c_uint32),
+        ("images", C.POINTER(gt_image)),
     ]
 
 
@@ -270,7 +289,7 @@ class gt_denoise_input(C.Structure):
 
 
 STRUCTS = [
-    gt_geometry, gt_primitive, gt_material, gt_scene_desc, gt_light_target, gt_environment_desc,
+    gt_geometry, gt_primitive, gt_material, gt_image, gt_scene_desc, gt_light_target, gt_environment_desc,
     gt_camera_desc, gt_render_opts, gt_frame, gt_frame_job, gt_bvh_stats, gt_render_stats, gt_denoise_input,
     gt_autotune_report,
 ]

@@ -281,13 +281,18 @@ gt_status gt_scene_create(gt_context* ctx, const gt_scene_desc* d, gt_scene** ou
     if (!ctx || !d || !out) return fail(GT_ERR_INVALID_ARG, "null argument");
     *out = nullptr;
     if (d->struct_size < sizeof(gt_scene_desc)) return fail(GT_ERR_INVALID_ARG, "scene struct_size too small");
-    if ((d->num_primitives && !d->primitives) || (d->num_materials && !d->materials))
-        return fail(GT_ERR_INVALID_ARG, "null primitive or material array");
+    if ((d->num_primitives && !d->primitives) || (d->num_materials && !d->materials) || (d->num_images && !d->images))
+        return fail(GT_ERR_INVALID_ARG, "null primitive, material or image array");
     if (d->num_primitives > (1u << 28)) return fail(GT_ERR_INVALID_ARG, "too many primitives");
     for (uint32_t i = 0; i < d->num_materials; ++i) {
         const gt_material& m = d->materials[i];
         if (m.kind > GT_MAT_HENYEY_GREENSTEIN) return fail(GT_ERR_INVALID_ARG, "unknown material kind");
-        if (m.texture_kind > GT_TEX_NOISE) return fail(GT_ERR_INVALID_ARG, "unknown texture kind");
+        if (m.texture_kind > GT_TEX_IMAGE) return fail(GT_ERR_INVALID_ARG, "unknown texture kind");
+        if (m.texture_kind == GT_TEX_IMAGE) {
+            const double k = m.tex[0];
+            if (!(k >= 0.0 && k < double(d->num_images)) || k != std::floor(k))
+                return fail(GT_ERR_INVALID_ARG, "image texture index out of range");
+        }
         if (m.texture_kind == GT_TEX_NOISE) {
             const double v = m.tex[1], depth = m.tex[2], lo = m.tex[3], hi = m.tex[4];
             if (!std::isfinite(m.tex[0]) || !(v == 0.0 || v == 1.0 || v == 2.0) || !(depth >= 0.0 && depth <= 64.0) ||
@@ -316,6 +321,23 @@ gt_status gt_scene_create(gt_context* ctx, const gt_scene_desc* d, gt_scene** ou
     s->prims.assign(d->primitives, d->primitives + d->num_primitives);
     s->mats.assign(d->materials, d->materials + d->num_materials);
     s->bvh_builder = builder;
+    for (uint32_t i = 0; i < d->num_images; ++i) {
+        const gt_image& g = d->images[i];
+        const uint64_t texels = uint64_t(g.width) * g.height;
+        if (g.filter > GT_FILTER_LINEAR || g.wrap_s > GT_WRAP_REPEAT || g.wrap_t > GT_WRAP_REPEAT ||
+            texels > (1ull << 28) || (texels && !g.rgb)) {
+            delete s;
+            return fail(GT_ERR_INVALID_ARG, "image needs filter and wrap modes 0-1, at most 2^28 texels and its data");
+        }
+        ImageHost im;
+        im.w = texels ? g.width : 0u;
+        im.h = texels ? g.height : 0u;
+        im.filter = g.filter;
+        im.wrap_s = g.wrap_s;
+        im.wrap_t = g.wrap_t;
+        if (texels) im.rgb.assign(g.rgb, g.rgb + texels * 3);
+        s->images.push_back(std::move(im));
+    }
     s->leaf_size = d->bvh_leaf_size ? d->bvh_leaf_size : 4u;
     if (builder == GT_BVH_REFERENCE_SAH) {
         const gt_status rc = ensure_reference_bvh(s);

@@ -15,8 +15,16 @@
 
 namespace gt {
 
+// A scene's bitmap texture, copied from gt_image.
+struct ImageHost {
+    uint32_t w = 0, h = 0, filter = 0, wrap_s = 0, wrap_t = 0;
+    std::vector<uint8_t> rgb;
+};
+
 template <class R> struct GpuScene {
     bool ready = false;
+    uint8_t* texels = nullptr;     // every image's texels, back to back
+    ImageDev* images = nullptr;
     PrimRec<R>* prims = nullptr;
     uint2* meta = nullptr;
     Node<R>* nodes = nullptr;
@@ -112,6 +120,7 @@ struct gt_scene {
     gt_context* ctx = nullptr;
     std::vector<gt_primitive> prims;
     std::vector<gt_material> mats;
+    std::vector<gt::ImageHost> images;
     uint32_t bvh_builder = GT_BVH_REFERENCE_SAH;
     uint32_t leaf_size = 4;
     bool bvh_ready = false; // `bvh` has been built (eagerly for the reference builder)

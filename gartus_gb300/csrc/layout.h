@@ -49,6 +49,12 @@ template <class R> struct PerlinDev {
     uint16_t perm[3][256];
 };
 
+// One bitmap texture on the device (gt_image): 8-bit texels, row 0 at the top.
+struct ImageDev {
+    const uint8_t* rgb;
+    uint32_t w, h, filter, wrap_s, wrap_t, pad;
+};
+
 template <class R> struct MatDev {
     int32_t kind;
     int32_t tex;
@@ -60,6 +66,7 @@ template <class R> struct MatDev {
     int32_t noise_variant;
     int32_t noise_depth;
     const PerlinDev<R>* noise; // this material's tables (GT_TEX_NOISE)
+    const ImageDev* image;     // this material's bitmap (GT_TEX_IMAGE)
 };
 
 // Weighted sampling target (raytracing/scene.rs:423-497) with the geometry's derived

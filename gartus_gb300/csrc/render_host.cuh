@@ -68,6 +68,8 @@ template <class R> void free_gpu(gt_scene* s) {
     cudaFree(g.nodes);
     cudaFree(g.mats);
     cudaFree(g.perlin);
+    cudaFree(g.texels);
+    cudaFree(g.images);
     g = GpuScene<R>();
 }
 
@@ -235,6 +237,21 @@ template <class R> gt_status upload_scene(gt_scene* s) {
         GT_CUDA(cudaMalloc(&g.perlin, perlin.size() * sizeof(PerlinDev<R>)));
         for (size_t k = 0; k < perlin.size(); ++k) mats[perlin_of[k]].noise = g.perlin + k;
     }
+    std::vector<ImageDev> idev(s->images.size());
+    if (!s->images.empty()) { // the bitmaps back to back, one descriptor each
+        size_t total = 0;
+        for (const ImageHost& im : s->images) total += im.rgb.size();
+        GT_CUDA(cudaMalloc(&g.texels, std::max<size_t>(total, 16)));
+        GT_CUDA(cudaMalloc(&g.images, idev.size() * sizeof(ImageDev)));
+        size_t off = 0;
+        for (size_t k = 0; k < idev.size(); ++k) {
+            const ImageHost& im = s->images[k];
+            idev[k] = ImageDev{g.texels + off, im.w, im.h, im.filter, im.wrap_s, im.wrap_t, 0u};
+            off += im.rgb.size();
+        }
+        for (size_t i = 0; i < s->mats.size(); ++i)
+            if (s->mats[i].texture_kind == GT_TEX_IMAGE) mats[i].image = g.images + size_t(s->mats[i].tex[0]);
+    }
     GT_CUDA(cudaMalloc(&g.prims, std::max<size_t>(n, 1) * sizeof(PrimRec<R>)));
     GT_CUDA(cudaMalloc(&g.meta, std::max<size_t>(n, 1) * sizeof(uint2)));
     GT_CUDA(cudaMalloc(&g.nodes, std::max<size_t>(nodes.size(), 1) * sizeof(Node<R>)));
@@ -251,6 +268,12 @@ template <class R> gt_status upload_scene(gt_scene* s) {
     if (!perlin.empty())
         GT_CUDA(cudaMemcpyAsync(g.perlin, perlin.data(), perlin.size() * sizeof(PerlinDev<R>), cudaMemcpyHostToDevice,
                                 st));
+    for (size_t k = 0; k < idev.size(); ++k)
+        if (!s->images[k].rgb.empty())
+            GT_CUDA(cudaMemcpyAsync(const_cast<uint8_t*>(idev[k].rgb), s->images[k].rgb.data(), s->images[k].rgb.size(),
+                                    cudaMemcpyHostToDevice, st));
+    if (!idev.empty())
+        GT_CUDA(cudaMemcpyAsync(g.images, idev.data(), idev.size() * sizeof(ImageDev), cudaMemcpyHostToDevice, st));
     GT_CUDA(cudaStreamSynchronize(st));
     SceneDev<R>& v = g.view;
     v.prims = g.prims;

@@ -268,6 +268,7 @@ GT_DEV int traverse(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, R t
 // ------------------------------------------------------------------ hit record
 template <class R> struct HitRec {
     V3<R> p, n; // n oriented against the ray (SurfaceHit::with_uv, object.rs:127-149)
+    R u, v;     // texture coordinates, computed for image-textured materials only
     bool front;
     uint32_t mat;
 };
@@ -292,6 +293,28 @@ template <class R> GT_DEV HitRec<R> make_hit(const SceneDev<R>& sc, uint32_t i, 
     }
     h.front = dot(d, out) < R(0);
     h.n = h.front ? out : -out;
+    h.u = h.v = R(0);
+    if (sc.mats[h.mat].tex == GT_TEX_IMAGE) {
+        if (kind == K_SPHERE || kind == K_MOVING) { // sphere_uv, object.rs:1038-1042
+            const R theta = Num<R>::acos(-out.y);
+            const R phi = Num<R>::atan2(-out.z, out.x) + R(kPi);
+            h.u = phi / R(2.0 * kPi);
+            h.v = theta / R(kPi);
+        } else if (kind == K_TRIANGLE) { // the Moller-Trumbore barycentrics of tri_hit
+            const V3<R> p0 = xyz(ldg4(rec)), e1 = xyz(ldg4(rec + 4)), e2 = xyz(ldg4(rec + 8));
+            const V3<R> pvec = cross(d, e2);
+            const R inv_det = R(1) / dot(e1, pvec);
+            const V3<R> tvec = o - p0;
+            h.u = dot(tvec, pvec) * inv_det;
+            h.v = dot(d, cross(tvec, e1)) * inv_det;
+        } else { // QuadGeometry::plane_coordinates, geometry.rs:384-390
+            const V3<R> corner = xyz(ldg4(rec)), qu = xyz(ldg4(rec + 4)), qv = xyz(ldg4(rec + 8));
+            const V3<R> qw = xyz(ldg4(rec + 12));
+            const V3<R> planar = h.p - corner;
+            h.u = dot(qw, cross(planar, qv));
+            h.v = dot(qw, cross(qu, planar));
+        }
+    }
     return h;
 }
 
@@ -361,7 +384,70 @@ template <class R> GT_DEV R noise_intensity(const MatDev<R>& m, V3<R> p) {
     return R(0.5) * (R(1) + perlin_noise(m.noise, q));
 }
 
-template <class R> GT_DEV V3<R> mat_color(const MatDev<R>& m, V3<R> p) {
+// ImageTexture::sample_linear (raytracing/texture.rs:148-155) through Texture::sample
+// (graphics/texture.rs:202-208, 716-752): nearest or bilinear with Rgb::lerp's rounding to
+// bytes, clamp or repeat per axis, t = 1 at the top row, then (c / 255)^2.
+template <class R> GT_DEV R rem1(R x) { // f64::rem_euclid(x, 1.0)
+    const R r = Num<R>::fmod(x, R(1));
+    return r < R(0) ? r + R(1) : r;
+}
+template <class R> GT_DEV uint32_t to_u32(R x) { // `as u32` for the finite values here
+    return x <= R(0) ? 0u : (x >= R(4294967295.0) ? 4294967295u : uint32_t(x));
+}
+template <class R> GT_DEV void tex_axis(R value, uint32_t size, uint32_t mode, R& coord, uint32_t& lo, uint32_t& hi) {
+    if (mode == GT_WRAP_CLAMP) {
+        coord = clampr(value, R(0), R(1)) * R(size - 1);
+        lo = to_u32(Num<R>::floor(coord));
+        hi = min(lo + 1, size - 1);
+    } else {
+        coord = rem1(value) * R(size);
+        lo = min(to_u32(Num<R>::floor(coord)), size - 1);
+        hi = lo + 1 == size ? 0u : lo + 1;
+    }
+}
+template <class R> GT_DEV void texel_lerp(const uint8_t* a, const uint8_t* b, R t, uint8_t* out) {
+    t = clampr(t, R(0), R(1));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const R v = Num<R>::round(R(a[k]) + R(int(b[k]) - int(a[k])) * t);
+        out[k] = uint8_t(v <= R(0) ? 0 : (v >= R(255) ? 255 : int(v)));
+    }
+}
+template <class R> GT_DEV V3<R> image_color(const ImageDev* im, R u, R v) {
+    uint8_t c[3] = {0, 0, 0};
+    if (im == nullptr || im->w == 0 || im->h == 0) {
+        c[1] = c[2] = 255; // Rgb::CYAN
+    } else if (Num<R>::finite(u) && Num<R>::finite(v)) {
+        const uint8_t* px = im->rgb;
+        const uint32_t w = im->w, h = im->h;
+        if (im->filter == GT_FILTER_NEAREST) {
+            const R ws = im->wrap_s == GT_WRAP_REPEAT ? rem1(u) : clampr(u, R(0), R(1));
+            const R wt = im->wrap_t == GT_WRAP_REPEAT ? rem1(v) : clampr(v, R(0), R(1));
+            const uint32_t x = to_u32(Num<R>::round(ws * R(w - 1)));
+            const uint32_t y = to_u32(Num<R>::round((R(1) - wt) * R(h - 1)));
+            const uint8_t* t = px + (size_t(y) * w + x) * 3;
+            c[0] = t[0];
+            c[1] = t[1];
+            c[2] = t[2];
+        } else {
+            R x, y;
+            uint32_t x0, x1, y0, y1;
+            tex_axis(u, w, im->wrap_s, x, x0, x1);
+            tex_axis(R(1) - v, h, im->wrap_t, y, y0, y1);
+            const R tx = x - R(x0), ty = y - R(y0);
+            uint8_t top[3], bottom[3];
+            texel_lerp(px + (size_t(y0) * w + x0) * 3, px + (size_t(y0) * w + x1) * 3, tx, top);
+            texel_lerp(px + (size_t(y1) * w + x0) * 3, px + (size_t(y1) * w + x1) * 3, tx, bottom);
+            texel_lerp(top, bottom, ty, c);
+        }
+    }
+    const R r = R(c[0]) / R(255), g = R(c[1]) / R(255), b = R(c[2]) / R(255);
+    return V3<R>{r * r, g * g, b * b};
+}
+
+template <class R> GT_DEV V3<R> mat_color(const MatDev<R>& m, const HitRec<R>& h) {
+    if (m.tex == GT_TEX_IMAGE) return image_color(m.image, h.u, h.v);
+    const V3<R> p = h.p;
     if (m.tex == GT_TEX_NOISE) {
         const R i = noise_intensity(m, p);
         return V3<R>{i, i, i};
@@ -391,19 +477,19 @@ template <class R> GT_DEV ScatterRec<R> mat_scatter(const MatDev<R>& m, V3<R> di
         if (!onb_from_w(h.n, s.pdf.basis)) return s;
         s.kind = SC_PDF;
         s.pdf.kind = PDF_COSINE;
-        s.att = mat_color(m, h.p);
+        s.att = mat_color(m, h);
         return s;
     case 2: // Isotropic, material.rs:1124-1137
         s.kind = SC_PDF;
         s.pdf.kind = PDF_SPHERE;
-        s.att = mat_color(m, h.p);
+        s.att = mat_color(m, h);
         return s;
     case 6: // HenyeyGreenstein, material.rs:1281-1295: the phase function around the incoming ray
         if (!onb_from_w(din, s.pdf.basis)) return s;
         s.kind = SC_PDF;
         s.pdf.kind = PDF_HG;
         s.pdf.rough = m.param;
-        s.att = mat_color(m, h.p);
+        s.att = mat_color(m, h);
         return s;
     case 3: { // GgxMicrofacet, material.rs:1583-1597; GgxReflectionPdf::new sampling.rs:146-170
         V3<R> outgoing = -normalize(din);
@@ -414,7 +500,7 @@ template <class R> GT_DEV ScatterRec<R> mat_scatter(const MatDev<R>& m, V3<R> di
         s.pdf.alpha = ggx_alpha(s.pdf.rough);
         s.pdf.kind = PDF_GGX;
         s.kind = SC_PDF;
-        s.att = mat_color(m, h.p);
+        s.att = mat_color(m, h);
         return s;
     }
     case 4: { // Metal, material.rs:2087-2106
@@ -467,7 +553,7 @@ template <class R> GT_DEV R mat_scattering_pdf(const MatDev<R>& m, V3<R> din, co
         V3<R> outgoing = -normalize(din);
         V3<R> incoming = normalize(dout);
         if (dot(incoming, h.n) <= R(0) || dot(outgoing, h.n) <= R(0)) return R(0);
-        V3<R> sc = mat_color(m, h.p); // specular_luminance, material.rs:1760-1762
+        V3<R> sc = mat_color(m, h); // specular_luminance, material.rs:1760-1762
         R f0 = clampr(R(0.2126) * sc.x + R(0.7152) * sc.y + R(0.0722) * sc.z, R(0), R(1));
         V3<R> n = normalize(h.n), o = normalize(outgoing), i = normalize(incoming);
         R ndi = dot(n, i), ndo = dot(n, o);
@@ -489,14 +575,14 @@ template <class R> GT_DEV R mat_scattering_pdf(const MatDev<R>& m, V3<R> din, co
 }
 
 template <class R> GT_DEV V3<R> mat_emitted(const MatDev<R>& m, const HitRec<R>& h) {
-    if (m.kind == 1 && h.front) return mat_color(m, h.p); // material.rs:1008-1022
+    if (m.kind == 1 && h.front) return mat_color(m, h); // material.rs:1008-1022
     return V3<R>{0, 0, 0};
 }
 
 template <class R> GT_DEV V3<R> mat_albedo(const MatDev<R>& m, const HitRec<R>& h) { // denoise_albedo
     if (m.kind == 4) return load3(m.color);
     if (m.kind == 5) return V3<R>{1, 1, 1};
-    return mat_color(m, h.p);
+    return mat_color(m, h);
 }
 
 // ------------------------------------------------------------- light targets

@@ -84,6 +84,48 @@ class RayGeometry:
         return g
 
 
+# ------------------------------------------------------------------- textures
+class ImageTexture:
+    """ImageTexture (raytracing/texture.rs:110-156) over the bitmap Texture of
+    graphics/texture.rs: (H, W, 3) uint8 sRGB texels, row 0 at the top (t = 1), decoded to
+    linear light as (c / 255)^2.  Texture::new defaults to nearest filtering and clamped
+    coordinates (texture.rs:118-126); an empty image samples as cyan (texture.rs:150-152).
+    The texels are copied into the scene when a material using the texture is compiled."""
+
+    _FILTERS = {"nearest": abi.GT_FILTER_NEAREST, "linear": abi.GT_FILTER_LINEAR}
+    _WRAPS = {"clamp": abi.GT_WRAP_CLAMP, "repeat": abi.GT_WRAP_REPEAT}
+
+    def __init__(self, texels, filter: str = "nearest", wrap_s: str = "clamp", wrap_t: str = "clamp"):
+        texels = np.asarray(texels)
+        if texels.size == 0:
+            texels = np.zeros((0, 0, 3), dtype=np.uint8)
+        if texels.ndim != 3 or texels.shape[2] != 3 or texels.dtype != np.uint8:
+            raise ValueError("image texels must be a (H, W, 3) uint8 array")
+        if texels.shape[0] * texels.shape[1] > (1 << 28):
+            raise ValueError("image texture has more than 2^28 texels")
+        if filter not in self._FILTERS or wrap_s not in self._WRAPS or wrap_t not in self._WRAPS:
+            raise ValueError("image filter must be nearest|linear and wraps clamp|repeat")
+        self.texels = np.ascontiguousarray(texels)
+        self.filter, self.wrap_s, self.wrap_t = filter, wrap_s, wrap_t
+
+    def to_struct(self) -> abi.gt_image:
+        g = abi.gt_image()
+        g.height, g.width = self.texels.shape[0], self.texels.shape[1]
+        g.rgb = self.texels.ctypes.data if self.texels.size else None
+        g.filter = self._FILTERS[self.filter]
+        g.wrap_s = self._WRAPS[self.wrap_s]
+        g.wrap_t = self._WRAPS[self.wrap_t]
+        return g
+
+
+def _image_table(images: Sequence[ImageTexture]):
+    """A gt_image array for gt_scene_desc (it points into the textures' own texels)."""
+    arr = (abi.gt_image * max(len(images), 1))()
+    for i, im in enumerate(images):
+        arr[i] = im.to_struct()
+    return arr
+
+
 # ------------------------------------------------------------------ materials
 @dataclass(frozen=True)
 class RayMaterial:
@@ -94,6 +136,7 @@ class RayMaterial:
     param: float = 0.0
     texture_kind: int = abi.GT_TEX_SOLID
     tex: tuple = (0.0,) * 7
+    image: Optional[ImageTexture] = field(default=None, compare=False)
 
     @staticmethod
     def lambertian(albedo) -> "RayMaterial":
@@ -133,6 +176,42 @@ class RayMaterial:
         """Lambertian::marble (material.rs:442-446): NoiseTexture::marble(scale, 7, seed)."""
         return RayMaterial(abi.GT_MAT_LAMBERTIAN, (0.5, 0.5, 0.5), 0.0, abi.GT_TEX_NOISE,
                            RayMaterial._noise_tex(scale, abi.GT_NOISE_MARBLE, 7, seed))
+
+    @staticmethod
+    def _textured(kind: int, texture: ImageTexture, param: float = 0.0) -> "RayMaterial":
+        if not isinstance(texture, ImageTexture):
+            raise TypeError("textured materials take an ImageTexture")
+        return RayMaterial(kind, (0.0, 0.0, 0.0), param, abi.GT_TEX_IMAGE, (0.0,) * 7, texture)
+
+    @staticmethod
+    def textured_lambertian(texture: ImageTexture) -> "RayMaterial":
+        """RayMaterial::textured_lambertian (material.rs:2393-2397)."""
+        return RayMaterial._textured(abi.GT_MAT_LAMBERTIAN, texture)
+
+    @staticmethod
+    def textured_diffuse_light(texture: ImageTexture) -> "RayMaterial":
+        """RayMaterial::textured_diffuse_light (material.rs:2419-2423)."""
+        return RayMaterial._textured(abi.GT_MAT_DIFFUSE_LIGHT, texture)
+
+    @staticmethod
+    def textured_isotropic(texture: ImageTexture) -> "RayMaterial":
+        """RayMaterial::textured_isotropic (material.rs:2445-2449)."""
+        return RayMaterial._textured(abi.GT_MAT_ISOTROPIC, texture)
+
+    @staticmethod
+    def textured_henyey_greenstein(texture: ImageTexture, g) -> "RayMaterial":
+        """HenyeyGreenstein::from_texture (material.rs:1264-1270)."""
+        g = float(g)
+        if not (math.isfinite(g) and abs(g) < 1.0):
+            raise ValueError("Henyey-Greenstein anisotropy must be finite and in (-1, 1)")
+        return RayMaterial._textured(abi.GT_MAT_HENYEY_GREENSTEIN, texture, g)
+
+    @staticmethod
+    def textured_ggx_microfacet(texture: ImageTexture, roughness) -> "RayMaterial":
+        """GgxMicrofacet::from_texture (material.rs:1505-1511)."""
+        if not math.isfinite(float(roughness)):
+            raise ValueError("GGX microfacet material values must be finite")
+        return RayMaterial._textured(abi.GT_MAT_GGX, texture, min(max(float(roughness), 0.0), 1.0))
 
     @staticmethod
     def diffuse_light(emit) -> "RayMaterial":
@@ -311,10 +390,11 @@ class Context:
 
 class _SceneHandle:
     def __init__(self, ctx: Context, prims: np.ndarray, mats: np.ndarray, leaf_size: int,
-                 bvh_builder: int = abi.GT_BVH_REFERENCE_SAH):
+                 bvh_builder: int = abi.GT_BVH_REFERENCE_SAH, images: Sequence[ImageTexture] = ()):
         self.ctx = ctx
         prims = np.ascontiguousarray(prims)
         mats = np.ascontiguousarray(mats)
+        table = _image_table(images)
         d = abi.gt_scene_desc()
         d.struct_size = C.sizeof(abi.gt_scene_desc)
         d.num_primitives = len(prims)
@@ -323,6 +403,8 @@ class _SceneHandle:
         d.materials = mats.ctypes.data_as(C.POINTER(abi.gt_material))
         d.bvh_leaf_size = leaf_size
         d.bvh_builder = bvh_builder
+        d.num_images = len(images)
+        d.images = table
         h = C.c_void_p()
         check(lib().gt_scene_create(ctx.handle, C.byref(d), C.byref(h)))
         self.h = h
@@ -475,9 +557,22 @@ class RayScene:
 
     def materials_array(self) -> np.ndarray:
         arr = np.zeros(len(self._materials), dtype=MATERIAL_DTYPE)
+        index = {id(im): k for k, im in enumerate(self.images())}
         for i, m in enumerate(self._materials):
             arr[i] = m.to_record()
+            if m.image is not None:
+                arr[i]["tex"][0] = index[id(m.image)]
         return arr
+
+    def images(self) -> list:
+        """The distinct ImageTextures of the materials, in first-use order (the scene's
+        gt_image table; a GT_TEX_IMAGE material's tex[0] indexes it)."""
+        out, seen = [], set()
+        for m in self._materials:
+            if m.image is not None and id(m.image) not in seen:
+                seen.add(id(m.image))
+                out.append(m.image)
+        return out
 
     @property
     def leaf_size(self) -> int:
@@ -511,7 +606,7 @@ class RayScene:
         h = self._handles.get(id(ctx))
         if h is None or h.ctx is not ctx or not h.h:
             h = _SceneHandle(ctx, self.primitives_array(), self.materials_array(), self._leaf_size,
-                             self._bvh_builder)
+                             self._bvh_builder, self.images())
             self._handles[id(ctx)] = h
         return h
 

@@ -88,9 +88,31 @@ typedef enum gt_material_kind {
 typedef enum gt_texture_kind {
     GT_TEX_SOLID = 0,   /* the material's color                                           */
     GT_TEX_CHECKER = 1, /* tex[0] = scale, tex[1..4] = even colour, tex[4..7] = odd colour  */
-    GT_TEX_NOISE = 2    /* Perlin: tex[0] = scale, tex[1] = variant (gt_noise_variant),
+    GT_TEX_NOISE = 2,   /* Perlin: tex[0] = scale, tex[1] = variant (gt_noise_variant),
                            tex[2] = octave depth, tex[3] / tex[4] = seed bits 0-31 / 32-63  */
+    GT_TEX_IMAGE = 3    /* ImageTexture (raytracing/texture.rs:110-156): tex[0] = index into
+                           gt_scene_desc.images, sampled at the hit's (u, v)               */
 } gt_texture_kind;
+
+/* A bitmap texture (graphics/texture.rs Texture, sampled by Texture::sample 202-208):
+ * 8-bit sRGB texels, decoded to linear as (c / 255)^2 (LinearRgb::from_rgb_srgb). */
+typedef enum gt_texture_filter {
+    GT_FILTER_NEAREST = 0, /* sample_nearest, texture.rs:716-722 */
+    GT_FILTER_LINEAR = 1   /* sample_linear with u8 lerps, texture.rs:724-735 */
+} gt_texture_filter;
+typedef enum gt_texture_wrap {
+    GT_WRAP_CLAMP = 0,
+    GT_WRAP_REPEAT = 1
+} gt_texture_wrap;
+typedef struct gt_image {
+    uint32_t width;
+    uint32_t height;      /* an empty image (0 texels) samples as cyan (texture.rs:150-152) */
+    const uint8_t* rgb;   /* width * height * 3 bytes, row 0 at the top (t = 1) */
+    uint32_t filter;      /* gt_texture_filter */
+    uint32_t wrap_s;      /* gt_texture_wrap */
+    uint32_t wrap_t;
+    uint32_t reserved;
+} gt_image;
 
 /* NoiseTexture kinds (graphics/raytracing/texture.rs:287-291). */
 typedef enum gt_noise_variant {
@@ -129,7 +151,8 @@ typedef struct gt_scene_desc {
     uint32_t bvh_leaf_size; /* 0 selects the reference default of 4 */
     const gt_material* materials;
     uint32_t bvh_builder;   /* gt_bvh_builder */
-    uint32_t reserved;
+    uint32_t num_images;
+    const gt_image* images; /* textures referenced by GT_TEX_IMAGE materials (copied) */
 } gt_scene_desc;
 
 /* One weighted sampling target (WeightedSamplingTargetList, raytracing/scene.rs:423-497).

@@ -62,6 +62,7 @@ def lib() -> C.CDLL:
                 "orc_scatter": (i32, [vp, vp, vp, vp, i32, u64, vp, vp, vp]),
                 "orc_scattering_pdf": (f64, [vp, vp, vp, vp, i32, vp]),
                 "orc_cosine_pdf": (f64, [vp, vp]),
+                "orc_image_sample": (None, [vp, f64, f64, vp]),
             }
             for name, (res, args) in sig.items():
                 fn = getattr(L, name)
@@ -78,10 +79,13 @@ def _ptr(a: np.ndarray):
 class OracleScene:
     """A RayScene loaded into the oracle (f64 and f32 copies, reference BVH built)."""
 
-    def __init__(self, prims: np.ndarray, mats: np.ndarray, leaf_size: int = 4):
+    def __init__(self, prims: np.ndarray, mats: np.ndarray, leaf_size: int = 4, images=()):
         from gartus_gb300 import abi
+        from gartus_gb300.raytracing import _image_table
         self._prims = np.ascontiguousarray(prims)
         self._mats = np.ascontiguousarray(mats)
+        self._images = list(images)
+        self._table = _image_table(self._images)
         d = abi.gt_scene_desc()
         d.struct_size = C.sizeof(abi.gt_scene_desc)
         d.num_primitives = len(self._prims)
@@ -89,13 +93,15 @@ class OracleScene:
         d.num_materials = len(self._mats)
         d.materials = self._mats.ctypes.data_as(C.POINTER(abi.gt_material))
         d.bvh_leaf_size = leaf_size
+        d.num_images = len(self._images)
+        d.images = self._table
         self.h = lib().orc_scene_create(C.byref(d))
         if not self.h:
             raise ValueError("oracle rejected the scene")
 
     @classmethod
     def from_ray_scene(cls, scene) -> "OracleScene":
-        return cls(scene.primitives_array(), scene.materials_array(), scene.leaf_size)
+        return cls(scene.primitives_array(), scene.materials_array(), scene.leaf_size, scene.images())
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -175,3 +181,12 @@ def camera_vectors(camera_desc) -> np.ndarray:
     out = np.zeros(18)
     lib().orc_camera(C.byref(camera_desc), C.byref(w), C.byref(h), C.byref(spp), _ptr(out))
     return out.reshape(6, 3)
+
+
+def image_sample(texture, u: float, v: float) -> np.ndarray:
+    """ImageTexture::sample_linear (raytracing/texture.rs:148-155) of a
+    gartus_gb300.raytracing.ImageTexture at (u, v): linear RGB, float64."""
+    g = texture.to_struct()
+    out = np.zeros(3)
+    lib().orc_image_sample(C.byref(g), float(u), float(v), _ptr(out))
+    return out

@@ -692,6 +692,74 @@ struct Perlin {
 };
 
 // ------------------------------------------------------------------ materials
+// A bitmap texture (graphics/texture.rs Texture) and Texture::sample (texture.rs:202-208):
+// 8-bit texels, nearest or bilinear, clamp or repeat per axis, t = 1 at the top row.
+struct ImageData {
+    uint32_t w = 0, h = 0;
+    std::vector<uint8_t> rgb;
+    int filter = GT_FILTER_NEAREST, wrap_s = GT_WRAP_CLAMP, wrap_t = GT_WRAP_CLAMP;
+
+    // f64::rem_euclid(value, 1.0)
+    static double rem1(double x) {
+        double r = std::fmod(x, 1.0);
+        return r < 0.0 ? r + 1.0 : r;
+    }
+    static double wrap(double x, int mode) { return mode == GT_WRAP_REPEAT ? rem1(x) : rclamp(x, 0.0, 1.0); }
+    // Rust `f64 as u32` for the finite, non-negative values here (saturating).
+    static uint32_t to_u32(double x) { return x <= 0.0 ? 0u : (x >= 4294967295.0 ? 4294967295u : uint32_t(x)); }
+    const uint8_t* at(uint32_t x, uint32_t y) const { return rgb.data() + (size_t(y) * w + x) * 3; }
+    // linear_axis (texture.rs:737-752): (coordinate, low texel, high texel)
+    void axis(double value, uint32_t size, int mode, double& coord, uint32_t& lo, uint32_t& hi) const {
+        if (mode == GT_WRAP_CLAMP) {
+            coord = rclamp(value, 0.0, 1.0) * double(size - 1);
+            lo = to_u32(std::floor(coord));
+            hi = std::min(lo + 1, size - 1);
+        } else {
+            coord = rem1(value) * double(size);
+            lo = std::min(to_u32(std::floor(coord)), size - 1);
+            hi = lo + 1 == size ? 0 : lo + 1;
+        }
+    }
+    // Rgb::lerp (colors.rs:525-537): per channel round(a + (b - a) t) as u8, t clamped.
+    static void lerp(const uint8_t* a, const uint8_t* b, double t, uint8_t* out) {
+        t = rclamp(t, 0.0, 1.0);
+        for (int k = 0; k < 3; ++k) {
+            const double v = std::round(double(a[k]) + double(int(b[k]) - int(a[k])) * t);
+            out[k] = uint8_t(v <= 0.0 ? 0 : (v >= 255.0 ? 255 : v));
+        }
+    }
+    // ImageTexture::sample_linear (raytracing/texture.rs:148-155) then from_rgb_srgb.
+    template <class R> V3<R> sample(R u, R v) const {
+        uint8_t c[3] = {0, 0, 0};
+        if (w == 0 || h == 0) {
+            c[1] = c[2] = 255; // Rgb::CYAN
+        } else if (std::isfinite(double(u)) && std::isfinite(double(v))) {
+            const double s = double(u), t = double(v);
+            if (filter == GT_FILTER_NEAREST) { // sample_nearest, texture.rs:716-722
+                const double ws = wrap(s, wrap_s), wt = wrap(t, wrap_t);
+                const uint32_t x = to_u32(std::round(ws * double(w - 1)));
+                const uint32_t y = to_u32(std::round((1.0 - wt) * double(h - 1)));
+                std::memcpy(c, at(x, y), 3);
+            } else { // sample_linear, texture.rs:724-735
+                double x, y;
+                uint32_t x0, x1, y0, y1;
+                axis(s, w, wrap_s, x, x0, x1);
+                axis(1.0 - t, h, wrap_t, y, y0, y1);
+                const double tx = x - double(x0), ty = y - double(y0);
+                uint8_t top[3], bottom[3];
+                lerp(at(x0, y0), at(x1, y0), tx, top);
+                lerp(at(x0, y1), at(x1, y1), tx, bottom);
+                lerp(top, bottom, ty, c);
+            }
+        }
+        auto dec = [](uint8_t ch) { // LinearRgb::from_rgb_srgb, colors.rs:78-84
+            const double x = double(ch) / 255.0;
+            return R(x * x);
+        };
+        return V3<R>(dec(c[0]), dec(c[1]), dec(c[2]));
+    }
+};
+
 template <class R> struct Material {
     int kind = GT_MAT_LAMBERTIAN;
     int texture = GT_TEX_SOLID;
@@ -702,6 +770,7 @@ template <class R> struct Material {
     R noise_scale{1};
     int noise_variant = 0, noise_depth = 0;
     std::shared_ptr<Perlin> perlin;
+    std::shared_ptr<const ImageData> image;
     static Material from_desc(const gt_material& m) {
         Material r;
         r.kind = int(m.kind);
@@ -735,6 +804,7 @@ template <class R> struct Material {
             else i = R(0.5) * (R(1) + perlin->noise(q));
             return V3<R>{i, i, i};
         }
+        if (texture == GT_TEX_IMAGE) return image ? image->sample<R>(h.u, h.v) : V3<R>(0, 1, 1);
         if (texture == GT_TEX_CHECKER) {
             int64_t xi = as_i64(double(std::floor(tex_inv_scale * h.point.x)));
             int64_t yi = as_i64(double(std::floor(tex_inv_scale * h.point.y)));
@@ -1250,7 +1320,27 @@ template <class R> struct Scene {
         prims.clear();
         geoms.clear();
         materials.clear();
-        for (uint32_t i = 0; i < d.num_materials; ++i) materials.push_back(Material<R>::from_desc(d.materials[i]));
+        std::vector<std::shared_ptr<const ImageData>> images;
+        for (uint32_t i = 0; i < (d.images ? d.num_images : 0u); ++i) {
+            auto im = std::make_shared<ImageData>();
+            const gt_image& g = d.images[i];
+            im->w = g.width;
+            im->h = g.height;
+            im->filter = int(g.filter);
+            im->wrap_s = int(g.wrap_s);
+            im->wrap_t = int(g.wrap_t);
+            if (g.rgb) im->rgb.assign(g.rgb, g.rgb + size_t(g.width) * g.height * 3);
+            images.push_back(im);
+        }
+        for (uint32_t i = 0; i < d.num_materials; ++i) {
+            materials.push_back(Material<R>::from_desc(d.materials[i]));
+            if (d.materials[i].texture_kind == GT_TEX_IMAGE) {
+                const double k = d.materials[i].tex[0];
+                if (!(k >= 0 && k < double(images.size())) || k != std::floor(k))
+                    throw std::invalid_argument("image texture index out of range");
+                materials.back().image = images[size_t(k)];
+            }
+        }
         std::vector<Bounds> bounds;
         for (uint32_t i = 0; i < d.num_primitives; ++i) {
             const gt_primitive& p = d.primitives[i];

@@ -388,6 +388,20 @@ double orc_scattering_pdf(const gt_material* md, const double* ray7, const doubl
     h.front_face = front != 0;
     return scattering_pdf(m, r, h, V3<double>(dir[0], dir[1], dir[2]));
 }
+// ImageTexture sampling at (u, v) into linear RGB.
+void orc_image_sample(const gt_image* g, double u, double v, double* out) {
+    ImageData im;
+    im.w = g->width;
+    im.h = g->height;
+    im.filter = int(g->filter);
+    im.wrap_s = int(g->wrap_s);
+    im.wrap_t = int(g->wrap_t);
+    if (g->rgb) im.rgb.assign(g->rgb, g->rgb + size_t(g->width) * g->height * 3);
+    const V3<double> c = im.sample<double>(u, v);
+    out[0] = c.x;
+    out[1] = c.y;
+    out[2] = c.z;
+}
 double orc_cosine_pdf(const double* normal, const double* dir) {
     MatPdf<double> p;
     p.kind = PDF_COSINE;

@@ -16,7 +16,7 @@ import pytest
 import oracle
 from gartus_gb300 import abi, scenes
 from gartus_gb300._lib import GartusError, lib
-from gartus_gb300.raytracing import (EnvironmentLight, PathTracer, RayCamera, RayGeometry, RayMaterial,
+from gartus_gb300.raytracing import (EnvironmentLight, ImageTexture, PathTracer, RayCamera, RayGeometry, RayMaterial,
                                      RayScene, SamplingTargetList)
 from tests.helpers import rel_err
 
@@ -675,3 +675,65 @@ def test_gpu_bvh_edge_cases(gpu_context):
     s.use_gpu_bvh()
     b = PathTracer(cam, context=gpu_context).render_hdr_image(s)
     assert _divergent(b.pixels, a.pixels.astype(np.float64)) <= 0.02 * a.pixels.shape[0] * a.pixels.shape[1]
+
+
+def _textured_scene():
+    rng = np.random.default_rng(77)
+    checker = np.zeros((8, 8, 3), np.uint8)
+    checker[(np.arange(8)[:, None] + np.arange(8)[None, :]) % 2 == 0] = (230, 200, 40)
+    checker[(np.arange(8)[:, None] + np.arange(8)[None, :]) % 2 == 1] = (30, 60, 200)
+    noise = rng.integers(0, 256, size=(13, 17, 3), dtype=np.uint8)
+    floor_tex = ImageTexture(checker, filter="linear", wrap_s="repeat", wrap_t="repeat")
+    ball_tex = ImageTexture(noise)  # nearest, clamped
+    tri_tex = ImageTexture(noise[:5, :7], filter="linear")
+    lamp_tex = ImageTexture(np.full((2, 2, 3), 255, np.uint8))
+    scene = RayScene()
+    scene.add_quad((-3.0, -0.5, -4.0), (6.0, 0.0, 0.0), (0.0, 0.0, 5.0),
+                   scene.add_material(RayMaterial.textured_lambertian(floor_tex)))
+    scene.add_sphere((-0.6, 0.1, -1.4), 0.55, scene.add_material(RayMaterial.textured_lambertian(ball_tex)))
+    scene.add_sphere((0.7, 0.0, -1.1), 0.4, scene.add_material(RayMaterial.textured_ggx_microfacet(ball_tex, 0.4)))
+    scene.add_triangle((0.2, -0.5, -2.2), (1.6, -0.5, -2.0), (0.9, 0.9, -2.4),
+                       scene.add_material(RayMaterial.textured_lambertian(tri_tex)))
+    scene.add_quad((-1.0, 2.0, -2.0), (2.0, 0.0, 0.0), (0.0, 0.0, 1.0),
+                   scene.add_material(RayMaterial.textured_diffuse_light(lamp_tex)))
+    scene.build_bvh()
+    return scene
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_image_textures(gpu_context, precision):
+    # ImageTexture (raytracing/texture.rs:110-156) on a quad (linear, repeated), spheres
+    # (nearest, clamped; Lambertian and GGX) and a triangle, lit by a textured emitter;
+    # (u, v) come from sphere_uv, the quad's plane coordinates and the barycentrics.
+    scene = _textured_scene()
+    assert len(scene.images()) == 4
+    cam = (RayCamera(64, 1.5).with_samples_per_pixel(6).with_max_depth(8)
+           .with_background((0.05, 0.05, 0.08)))
+    ref, acc = _oracle_render(scene, cam)
+    if precision == "f64":
+        img = PathTracer(cam, precision="f64", context=gpu_context).render_hdr_image(scene, want64=True)
+        np.testing.assert_array_equal(img.accepted, acc)
+        err = rel_err(img.pixels64, ref, floor=1e-12).max(axis=2)
+        assert (err <= 1e-9).mean() >= 0.99, err.max()
+    else:
+        img = PathTracer(cam, context=gpu_context).render_hdr_image(scene)
+        ref32, _ = _oracle_render(scene, cam, precision=0)
+        n = ref.shape[0] * ref.shape[1]
+        assert _divergent(img.pixels, ref) <= _divergent(ref32, ref) + 0.02 * n
+    assert np.std(ref) > 1e-3
+
+
+def test_image_texture_edge_cases(gpu_context):
+    # an empty bitmap samples cyan; a texture index past the image table is rejected
+    scene = RayScene()
+    scene.add_quad((-2.0, -2.0, -1.0), (4.0, 0.0, 0.0), (0.0, 4.0, 0.0),
+                   scene.add_material(RayMaterial.textured_diffuse_light(ImageTexture(np.zeros((0, 0, 3), np.uint8)))))
+    scene.build_bvh()
+    cam = RayCamera(8, 1.0).with_samples_per_pixel(1).with_max_depth(2)
+    img = PathTracer(cam, precision="f64", context=gpu_context).render_hdr_image(scene, want64=True)
+    np.testing.assert_array_equal(img.pixels64[4, 4], [0.0, 1.0, 1.0])
+    bad = scene.materials_array()
+    bad[0]["tex"][0] = 1.0
+    with pytest.raises(GartusError):
+        from gartus_gb300.raytracing import _SceneHandle
+        _SceneHandle(gpu_context, scene.primitives_array(), bad, 4, abi.GT_BVH_REFERENCE_SAH, scene.images())
