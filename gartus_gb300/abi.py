@@ -52,6 +52,11 @@ GT_FILTER_NEAREST = 0
 GT_FILTER_LINEAR = 1
 GT_WRAP_CLAMP = 0
 GT_WRAP_REPEAT = 1
+# gt_medium_shape / gt_medium_transform
+GT_MEDIUM_SPHERE = 0
+GT_MEDIUM_BOX = 1
+GT_MEDIUM_ROTATE_Y = 1
+GT_MEDIUM_TRANSLATE = 2
 # gt_noise_variant
 GT_NOISE_PLAIN = 0
 GT_NOISE_TURBULENCE = 1
@@ -109,6 +114,19 @@ class gt_image(C.Structure):
     ]
 
 
+class gt_medium(C.Structure):
+    _fields_ = [
+        ("shape", C.c_uint32),
+        ("material", C.c_uint32),
+        ("p", C.c_double * 6),
+        ("rotate_y", C.c_double),
+        ("translate", C.c_double * 3),
+        ("density", C.c_double),
+        ("transform", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
 class gt_scene_desc(C.Structure):
     _fields_ = [
         ("struct_size", C.c_uint32),
@@ -120,6 +138,9 @@ class gt_scene_desc(C.Structure):
         ("bvh_builder", C.c_uint32),
         ("num_images", C.c_uint32),
         ("images", C.POINTER(gt_image)),
+        ("num_media", C.c_uint32),
+        ("reserved", C.c_uint32),
+        ("media", C.POINTER(gt_medium)),
     ]
 
 
@@ -289,7 +310,7 @@ class gt_denoise_input(C.Structure):
 
 
 STRUCTS = [
-    gt_geometry, gt_primitive, gt_material, gt_image, gt_scene_desc, gt_light_target, gt_environment_desc,
+    gt_geometry, gt_primitive, gt_material, gt_image, gt_medium, gt_scene_desc, gt_light_target, gt_environment_desc,
     gt_camera_desc, gt_render_opts, gt_frame, gt_frame_job, gt_bvh_stats, gt_render_stats, gt_denoise_input,
     gt_autotune_report,
 ]

@@ -307,6 +307,18 @@ gt_status gt_scene_create(gt_context* ctx, const gt_scene_desc* d, gt_scene** ou
         if (m.kind == GT_MAT_HENYEY_GREENSTEIN && !(std::fabs(m.param) < 1.0)) // material.rs:1334-1343
             return fail(GT_ERR_INVALID_ARG, "Henyey-Greenstein anisotropy must be finite and in (-1, 1)");
     }
+    if (d->num_media && !d->media) return fail(GT_ERR_INVALID_ARG, "null media array");
+    if (d->num_media > kMaxMedia) return fail(GT_ERR_INVALID_ARG, "at most 64 media per scene");
+    for (uint32_t i = 0; i < d->num_media; ++i) {
+        const gt_medium& m = d->media[i];
+        bool finite = std::isfinite(m.rotate_y) && finite3(m.translate);
+        for (int k = 0; k < 6; ++k) finite = finite && std::isfinite(m.p[k]);
+        if (m.shape > GT_MEDIUM_BOX || m.transform > (GT_MEDIUM_ROTATE_Y | GT_MEDIUM_TRANSLATE) || !finite)
+            return fail(GT_ERR_INVALID_ARG, "medium needs shape 0-1, transform bits 0-3 and finite values");
+        if (!(std::isfinite(m.density) && m.density > 0.0)) // medium.rs:93-96
+            return fail(GT_ERR_INVALID_ARG, "medium density must be positive and finite");
+        if (m.material >= d->num_materials) return fail(GT_ERR_INVALID_ARG, "medium material id out of bounds");
+    }
     for (uint32_t i = 0; i < d->num_primitives; ++i) {
         gt_status rc = validate_geometry(d->primitives[i].geometry);
         if (rc != GT_OK) return rc;
@@ -321,6 +333,7 @@ gt_status gt_scene_create(gt_context* ctx, const gt_scene_desc* d, gt_scene** ou
     s->prims.assign(d->primitives, d->primitives + d->num_primitives);
     s->mats.assign(d->materials, d->materials + d->num_materials);
     s->bvh_builder = builder;
+    s->media.assign(d->media, d->media + d->num_media);
     for (uint32_t i = 0; i < d->num_images; ++i) {
         const gt_image& g = d->images[i];
         const uint64_t texels = uint64_t(g.width) * g.height;

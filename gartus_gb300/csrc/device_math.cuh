@@ -37,6 +37,8 @@ template <> struct Num<float> {
     static GT_DEV float sin(float x) { return sinf(x); }
     static GT_DEV int32_t to_i32(float x) { return __float2int_rz(x); } // saturating, NaN -> 0 (Rust `as`)
     static GT_DEV float fmod(float a, float b) { return fmodf(a, b); }
+    static GT_DEV float log(float x) { return logf(x); }
+    static GT_DEV float min_positive() { return 0x1p-126f; } // f32::MIN_POSITIVE
     static GT_DEV float round(float x) { return roundf(x); }
     static GT_DEV bool finite(float x) { return isfinite(x); }
 };
@@ -54,6 +56,8 @@ template <> struct Num<double> {
     static GT_DEV double sin(double x) { return ::sin(x); }
     static GT_DEV int32_t to_i32(double x) { return __double2int_rz(x); } // saturating, NaN -> 0 (Rust `as`)
     static GT_DEV double fmod(double a, double b) { return ::fmod(a, b); }
+    static GT_DEV double log(double x) { return ::log(x); }
+    static GT_DEV double min_positive() { return 0x1p-1022; } // f64::MIN_POSITIVE
     static GT_DEV double round(double x) { return ::round(x); }
     static GT_DEV bool finite(double x) { return isfinite(x); }
 };

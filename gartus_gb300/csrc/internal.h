@@ -15,6 +15,9 @@
 
 namespace gt {
 
+// Media per scene: each ray tests all of them in order.
+constexpr uint32_t kMaxMedia = 64;
+
 // A scene's bitmap texture, copied from gt_image.
 struct ImageHost {
     uint32_t w = 0, h = 0, filter = 0, wrap_s = 0, wrap_t = 0;
@@ -25,6 +28,7 @@ template <class R> struct GpuScene {
     bool ready = false;
     uint8_t* texels = nullptr;     // every image's texels, back to back
     ImageDev* images = nullptr;
+    MediumDev<R>* media = nullptr;
     PrimRec<R>* prims = nullptr;
     uint2* meta = nullptr;
     Node<R>* nodes = nullptr;
@@ -121,6 +125,7 @@ struct gt_scene {
     std::vector<gt_primitive> prims;
     std::vector<gt_material> mats;
     std::vector<gt::ImageHost> images;
+    std::vector<gt_medium> media;
     uint32_t bvh_builder = GT_BVH_REFERENCE_SAH;
     uint32_t leaf_size = 4;
     bool bvh_ready = false; // `bvh` has been built (eagerly for the reference builder)

@@ -121,12 +121,29 @@ template <class R> struct CamDev {
     uint32_t use_lights, use_env;
 };
 
+// ConstantMedium (raytracing/volume/medium.rs:13-187): its boundary (one sphere, or the six
+// quads of box_object, object.rs:930-976, in PrimRec layout with derived quantities from
+// f64), the RotateY sine and cosine and the Translate offset (instance.rs), and -1/density.
+template <class R> struct MediumDev {
+    uint32_t parts;     // 1 (sphere) or 6 (box quads)
+    uint32_t mat;       // phase-function material
+    uint32_t transform; // gt_medium_transform bits
+    uint32_t pad;
+    R neg_inv_density;
+    R sin_t, cos_t;
+    R off[3];
+    PrimRec<R> part[6]; // K_SPHERE or K_QUAD records (a degenerate quad is never hit)
+    uint32_t kind[6];
+};
+
 // Scene view handed to kernels.
 template <class R> struct SceneDev {
     const PrimRec<R>* prims;
     const uint2* meta;
     const Node<R>* nodes;
     const MatDev<R>* mats;
+    const MediumDev<R>* media; // tested after the surfaces, in order
+    uint32_t num_media;
     R root_box[6];
     int32_t root_link; // >= 0 internal root node, < 0 ~first of a leaf root
     int32_t root_count;

@@ -70,7 +70,103 @@ template <class R> void free_gpu(gt_scene* s) {
     cudaFree(g.perlin);
     cudaFree(g.texels);
     cudaFree(g.images);
+    cudaFree(g.media);
     g = GpuScene<R>();
+}
+
+// One primitive's PrimRec (layout.h) from its gt_geometry, derived quantities in f64:
+// returns its kind (K_NEVER for the degenerate quads and triangles every query rejects,
+// geometry.rs:394-397, object.rs:192-203) or kBadKind for an unknown geometry kind.
+constexpr uint32_t kBadKind = 0xFFFFFFFFu;
+template <class R> uint32_t pack_prim(const gt_geometry& g, R* v) {
+    const double* q = g.p;
+    std::fill(v, v + 16, R(0));
+    uint32_t kind = g.kind;
+    switch (g.kind) {
+    case GT_GEOM_SPHERE:
+        put3(v, q);
+        v[3] = R(std::fmax(q[3], 0.0));
+        break;
+    case GT_GEOM_MOVING_SPHERE: {
+        put3(v, q);
+        v[3] = R(std::fmax(q[6], 0.0));
+        double dl[3] = {q[3] - q[0], q[4] - q[1], q[5] - q[2]};
+        put3(v + 4, dl);
+        break;
+    }
+    case GT_GEOM_TRIANGLE: {
+        double e1[3] = {q[3] - q[0], q[4] - q[1], q[5] - q[2]};
+        double e2[3] = {q[6] - q[0], q[7] - q[1], q[8] - q[2]};
+        double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        double len = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        double nrm[3] = {0, 0, 0};
+        if (!(len < 2.220446049250313e-16))
+            for (int k = 0; k < 3; ++k) nrm[k] = c[k] / len;
+        put3(v, q);
+        put3(v + 4, e1);
+        put3(v + 8, e2);
+        put3(v + 12, nrm);
+        if (nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2] <= 2.220446049250313e-16) kind = K_NEVER;
+        break;
+    }
+    case GT_GEOM_QUAD: {
+        const double* u = q + 3;
+        const double* w = q + 6;
+        double c[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+        double l2 = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+        double len = std::sqrt(l2);
+        double nrm[3] = {0, 0, 0};
+        if (!(len < 2.220446049250313e-16))
+            for (int k = 0; k < 3; ++k) nrm[k] = c[k] / len;
+        double pd = nrm[0] * q[0] + nrm[1] * q[1] + nrm[2] * q[2];
+        double ww[3] = {0, 0, 0};
+        if (!(l2 <= 2.220446049250313e-16))
+            for (int k = 0; k < 3; ++k) ww[k] = c[k] / l2;
+        put3(v, q);
+        v[3] = R(pd);
+        put3(v + 4, u);
+        v[7] = R(nrm[0]);
+        put3(v + 8, w);
+        v[11] = R(nrm[1]);
+        put3(v + 12, ww);
+        v[15] = R(nrm[2]);
+        if (l2 <= 2.220446049250313e-16) kind = K_NEVER; // area_squared() <= EPS
+        if (nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2] <= 2.220446049250313e-16) kind = K_NEVER;
+        break;
+    }
+    default:
+        return kBadKind;
+    }
+    return kind;
+}
+
+// A medium's boundary as primitives: its sphere, or box_object's six quads in their order
+// (object.rs:930-976: corners sorted per axis, sides spanned by dx, dy, dz and their
+// negations).  Returns the count.
+inline uint32_t medium_parts(const gt_medium& m, gt_geometry* out) {
+    std::memset(out, 0, 6 * sizeof(gt_geometry));
+    if (m.shape == GT_MEDIUM_SPHERE) {
+        out[0].kind = GT_GEOM_SPHERE;
+        for (int a = 0; a < 4; ++a) out[0].p[a] = m.p[a];
+        return 1;
+    }
+    const double mn[3] = {std::fmin(m.p[0], m.p[3]), std::fmin(m.p[1], m.p[4]), std::fmin(m.p[2], m.p[5])};
+    const double mx[3] = {std::fmax(m.p[0], m.p[3]), std::fmax(m.p[1], m.p[4]), std::fmax(m.p[2], m.p[5])};
+    const double dx[3] = {mx[0] - mn[0], 0.0, 0.0}, dy[3] = {0.0, mx[1] - mn[1], 0.0}, dz[3] = {0.0, 0.0, mx[2] - mn[2]};
+    const double ndx[3] = {-dx[0], -dx[1], -dx[2]}, ndz[3] = {-dz[0], -dz[1], -dz[2]};
+    const double q[6][3] = {{mn[0], mn[1], mx[2]}, {mx[0], mn[1], mx[2]}, {mx[0], mn[1], mn[2]},
+                            {mn[0], mn[1], mn[2]}, {mn[0], mx[1], mx[2]}, {mn[0], mn[1], mn[2]}};
+    const double* u[6] = {dx, ndz, ndx, dz, dx, dx};
+    const double* v[6] = {dy, dy, dy, dy, ndz, dz};
+    for (int i = 0; i < 6; ++i) {
+        out[i].kind = GT_GEOM_QUAD;
+        for (int a = 0; a < 3; ++a) {
+            out[i].p[a] = q[i][a];
+            out[i].p[3 + a] = u[i][a];
+            out[i].p[6 + a] = v[i][a];
+        }
+    }
+    return 6;
 }
 
 // Flattens the primitives into leaf order with derived quantities computed in f64
@@ -109,65 +205,8 @@ template <class R> gt_status upload_scene(gt_scene* s) {
     for (size_t j = 0; j < n; ++j) {
         const uint32_t pi = gpu_bvh ? uint32_t(j) : bvh.order[j];
         const gt_primitive& p = s->prims[pi];
-        const double* q = p.geometry.p;
-        R* v = recs[j].v;
-        std::fill(v, v + 16, R(0));
-        uint32_t kind = p.geometry.kind;
-        switch (p.geometry.kind) {
-        case GT_GEOM_SPHERE:
-            put3(v, q);
-            v[3] = R(std::fmax(q[3], 0.0));
-            break;
-        case GT_GEOM_MOVING_SPHERE: {
-            put3(v, q);
-            v[3] = R(std::fmax(q[6], 0.0));
-            double dl[3] = {q[3] - q[0], q[4] - q[1], q[5] - q[2]};
-            put3(v + 4, dl);
-            break;
-        }
-        case GT_GEOM_TRIANGLE: {
-            double e1[3] = {q[3] - q[0], q[4] - q[1], q[5] - q[2]};
-            double e2[3] = {q[6] - q[0], q[7] - q[1], q[8] - q[2]};
-            double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
-            double len = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
-            double nrm[3] = {0, 0, 0};
-            if (!(len < 2.220446049250313e-16))
-                for (int k = 0; k < 3; ++k) nrm[k] = c[k] / len;
-            put3(v, q);
-            put3(v + 4, e1);
-            put3(v + 8, e2);
-            put3(v + 12, nrm);
-            if (nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2] <= 2.220446049250313e-16) kind = K_NEVER;
-            break;
-        }
-        case GT_GEOM_QUAD: {
-            const double* u = q + 3;
-            const double* w = q + 6;
-            double c[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
-            double l2 = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
-            double len = std::sqrt(l2);
-            double nrm[3] = {0, 0, 0};
-            if (!(len < 2.220446049250313e-16))
-                for (int k = 0; k < 3; ++k) nrm[k] = c[k] / len;
-            double pd = nrm[0] * q[0] + nrm[1] * q[1] + nrm[2] * q[2];
-            double ww[3] = {0, 0, 0};
-            if (!(l2 <= 2.220446049250313e-16))
-                for (int k = 0; k < 3; ++k) ww[k] = c[k] / l2;
-            put3(v, q);
-            v[3] = R(pd);
-            put3(v + 4, u);
-            v[7] = R(nrm[0]);
-            put3(v + 8, w);
-            v[11] = R(nrm[1]);
-            put3(v + 12, ww);
-            v[15] = R(nrm[2]);
-            if (l2 <= 2.220446049250313e-16) kind = K_NEVER; // area_squared() <= EPS
-            if (nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2] <= 2.220446049250313e-16) kind = K_NEVER;
-            break;
-        }
-        default:
-            return fail(GT_ERR_INVALID_ARG, "unknown geometry kind");
-        }
+        const uint32_t kind = pack_prim<R>(p.geometry, recs[j].v);
+        if (kind == kBadKind) return fail(GT_ERR_INVALID_ARG, "unknown geometry kind");
         meta[j] = make_uint2(kind | (p.material << 3), pi);
     }
     // Internal nodes, renumbered densely in pre-order; leaf children become links.
@@ -252,6 +291,25 @@ template <class R> gt_status upload_scene(gt_scene* s) {
         for (size_t i = 0; i < s->mats.size(); ++i)
             if (s->mats[i].texture_kind == GT_TEX_IMAGE) mats[i].image = g.images + size_t(s->mats[i].tex[0]);
     }
+    // Media: boundary shapes in PrimRec layout, the RotateY sine and cosine of
+    // degrees_to_radians (raytracing.rs:150-152) and -1/density (medium.rs:97-101), in f64.
+    std::vector<MediumDev<R>> mdev(s->media.size());
+    for (size_t k = 0; k < mdev.size(); ++k) {
+        const gt_medium& gm = s->media[k];
+        MediumDev<R>& M = mdev[k];
+        std::memset(&M, 0, sizeof(M));
+        M.mat = gm.material;
+        M.transform = gm.transform;
+        M.neg_inv_density = R(-1.0 / gm.density);
+        const double rad = gm.rotate_y * 3.141592653589793 / 180.0;
+        M.sin_t = R(std::sin(rad));
+        M.cos_t = R(std::cos(rad));
+        for (int a = 0; a < 3; ++a) M.off[a] = R(gm.translate[a]);
+        gt_geometry parts[6];
+        M.parts = medium_parts(gm, parts);
+        for (uint32_t i = 0; i < M.parts; ++i) M.kind[i] = pack_prim<R>(parts[i], M.part[i].v);
+    }
+    if (!mdev.empty()) GT_CUDA(cudaMalloc(&g.media, mdev.size() * sizeof(MediumDev<R>)));
     GT_CUDA(cudaMalloc(&g.prims, std::max<size_t>(n, 1) * sizeof(PrimRec<R>)));
     GT_CUDA(cudaMalloc(&g.meta, std::max<size_t>(n, 1) * sizeof(uint2)));
     GT_CUDA(cudaMalloc(&g.nodes, std::max<size_t>(nodes.size(), 1) * sizeof(Node<R>)));
@@ -274,12 +332,16 @@ template <class R> gt_status upload_scene(gt_scene* s) {
                                     cudaMemcpyHostToDevice, st));
     if (!idev.empty())
         GT_CUDA(cudaMemcpyAsync(g.images, idev.data(), idev.size() * sizeof(ImageDev), cudaMemcpyHostToDevice, st));
+    if (!mdev.empty())
+        GT_CUDA(cudaMemcpyAsync(g.media, mdev.data(), mdev.size() * sizeof(MediumDev<R>), cudaMemcpyHostToDevice, st));
     GT_CUDA(cudaStreamSynchronize(st));
     SceneDev<R>& v = g.view;
     v.prims = g.prims;
     v.meta = g.meta;
     v.nodes = g.nodes;
     v.mats = g.mats;
+    v.media = g.media;
+    v.num_media = uint32_t(mdev.size());
     v.num_prims = uint32_t(n);
     v.num_nodes = uint32_t(nodes.size());
     if (gpu_bvh && n > 0) {
@@ -591,15 +653,22 @@ gt_status run_persistent(gt_context* ctx, Params<R>& P, uint32_t* d_next, float*
     if (opts.progress && opts.progress_rgb && o_rgb) // unfinished pixels read as 0 in progress images
         GT_CUDA(cudaMemsetAsync(o_rgb, 0, size_t(n) * 3 * sizeof(float), st));
     int per_sm = 0;
-    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<R, false>, 128, 0));
+    const bool media = P.sc.num_media != 0;
+    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, media ? k_persistent<R, false, false, true> : k_persistent<R, false>, 128, 0));
     const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1);
     const uint32_t blocks = std::max<uint32_t>(1u, std::min<uint32_t>(sms * uint32_t(std::max(per_sm, 1)), (n + 127) / 128));
     const bool profile = opts.profile != 0;
     cudaEvent_t a = nullptr, z = nullptr;
     GT_CUDA(ev.pair(a, z));
     GT_CUDA(cudaEventRecord(a, st));
-    k_persistent<R, false><<<blocks, 128, 0, st>>>(P, d_next, P.ps.q_mat, P.ps.counters + C_MAT, ctx->mapped_dev,
-                                            ctx->mapped_dev + 1, o_rgb, o_rgb64, o_acc);
+    if (media)
+        k_persistent<R, false, false, true><<<blocks, 128, 0, st>>>(P, d_next, P.ps.q_mat, P.ps.counters + C_MAT,
+                                                                   ctx->mapped_dev, ctx->mapped_dev + 1, o_rgb, o_rgb64,
+                                                                   o_acc);
+    else
+        k_persistent<R, false><<<blocks, 128, 0, st>>>(P, d_next, P.ps.q_mat, P.ps.counters + C_MAT, ctx->mapped_dev,
+                                                       ctx->mapped_dev + 1, o_rgb, o_rgb64, o_acc);
     GT_CUDA(cudaGetLastError());
     klaunch[GT_KERNEL_PERSISTENT] += 1;
     GT_CUDA(cudaEventRecord(z, st));
@@ -745,7 +814,12 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
 
     // Workspace: path state (wavefront only), per-stripe queues and counters, and device
     // staging for host outputs.
-    const bool persistent = !BATCH && opts.schedule == GT_SCHEDULE_PERSISTENT && !accum;
+    // A scene with media renders on the persistent schedule, whose MEDIA variant traces
+    // shadow queries in the reference's order of draws (accumulation resumes wavefront
+    // state, which that variant does not keep).
+    if (P.sc.num_media && (accum || BATCH))
+        return fail(GT_ERR_UNSUPPORTED, "a scene with media renders neither accumulated nor as a wavefront batch");
+    const bool persistent = (!BATCH && opts.schedule == GT_SCHEDULE_PERSISTENT && !accum) || P.sc.num_media != 0;
     const bool host_out = BATCH || frame->device_buffers == 0;
     // Wavefront stripes: rows are dealt round-robin to K independent wavefronts on their
     // own streams, whose kernels then overlap on the GPU (each kernel alone leaves SMs
@@ -1280,14 +1354,20 @@ gt_status render_batch_impl(gt_scene* s, const gt_lights* l, gt_environment* e, 
     ctx->mapped[0] = 0;
     ctx->mapped[1] = 0;
     int per_sm = 0;
-    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<R, false, true>, 128, 0));
+    const bool media = P.sc.num_media != 0;
+    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, media ? k_persistent<R, false, true, true> : k_persistent<R, false, true>, 128, 0));
     const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1);
     const uint32_t blocks = std::max<uint32_t>(1u, std::min<uint32_t>(sms * uint32_t(std::max(per_sm, 1)), (n + 127) / 128));
     cudaEvent_t a = nullptr, z = nullptr;
     GT_CUDA(ev.pair(a, z));
     GT_CUDA(cudaEventRecord(a, st));
-    k_persistent<R, false, true><<<blocks, 128, 0, st>>>(P, d_next, nullptr, nullptr, ctx->mapped_dev,
-                                                         ctx->mapped_dev + 1, d_rgb, d_rgb64, d_acc);
+    if (media)
+        k_persistent<R, false, true, true><<<blocks, 128, 0, st>>>(P, d_next, nullptr, nullptr, ctx->mapped_dev,
+                                                                   ctx->mapped_dev + 1, d_rgb, d_rgb64, d_acc);
+    else
+        k_persistent<R, false, true><<<blocks, 128, 0, st>>>(P, d_next, nullptr, nullptr, ctx->mapped_dev,
+                                                             ctx->mapped_dev + 1, d_rgb, d_rgb64, d_acc);
     GT_CUDA(cudaGetLastError());
     klaunch[GT_KERNEL_PERSISTENT] += 1;
     GT_CUDA(cudaEventRecord(z, st));

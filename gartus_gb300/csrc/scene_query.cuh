@@ -318,6 +318,87 @@ template <class R> GT_DEV HitRec<R> make_hit(const SceneDev<R>& sc, uint32_t i, 
     return h;
 }
 
+// ------------------------------------------------------------------------ media
+// rotate_y_point_inverse / rotate_y_vector_inverse (instance.rs): world into object space.
+template <class R> GT_DEV V3<R> rot_y_inv(V3<R> p, R s, R c) { return V3<R>{c * p.x - s * p.z, p.y, s * p.x + c * p.z}; }
+
+// The closest hit of a medium's boundary in (tmin, tmax), object space: a sphere, or
+// box_object's HittableList of six quads (scene.rs:177-197: a later quad must be strictly
+// closer to replace an earlier one).
+template <class R> GT_DEV bool boundary_hit(const MediumDev<R>& M, V3<R> o, V3<R> d, R tmin, R tmax, R& t) {
+    bool any = false;
+    for (uint32_t i = 0; i < M.parts; ++i) {
+        const R* rec = M.part[i].v;
+        R ti = R(0);
+        bool h = false;
+        if (M.kind[i] == K_SPHERE) {
+            h = sphere_root(V3<R>{rec[0], rec[1], rec[2]}, rec[3], o, d, tmin, tmax, ti);
+        } else if (M.kind[i] == K_QUAD) {
+            h = quad_hit(V3<R>{rec[0], rec[1], rec[2]}, V3<R>{rec[4], rec[5], rec[6]}, V3<R>{rec[8], rec[9], rec[10]},
+                         V3<R>{rec[7], rec[11], rec[15]}, V3<R>{rec[12], rec[13], rec[14]}, rec[3], o, d, tmin, tmax,
+                         ti);
+        }
+        if (h) {
+            tmax = ti;
+            t = ti;
+            any = true;
+        }
+    }
+    return any;
+}
+
+// The media of HittableList::hit_with_rng after the surfaces (scene.rs:177-197), each one
+// ConstantMedium::hit_with_rng (volume/medium.rs:119-187) through its Translate / RotateY:
+// the boundary's first hit anywhere on the line, clamped to tmin, and its next hit
+// 0.0001 further, clipped to the closest hit so far, bound the interval; a non-empty one
+// draws a sample and scatters at distance -ln(sample) / density when that falls inside.
+// `t` is the closest hit so far (infinity if none); returns -2 - index of the medium hit
+// last, or `prim` unchanged.
+template <class R> GT_DEV int media_hit(const SceneDev<R>& sc, V3<R> o, V3<R> d, R tmin, R& t, int prim, Rng& g) {
+    const R inf = Num<R>::inf();
+    for (uint32_t k = 0; k < sc.num_media; ++k) {
+        const MediumDev<R>& M = sc.media[k];
+        V3<R> oo = o, od = d;
+        if (M.transform & GT_MEDIUM_TRANSLATE) oo = oo - V3<R>{M.off[0], M.off[1], M.off[2]};
+        if (M.transform & GT_MEDIUM_ROTATE_Y) {
+            oo = rot_y_inv(oo, M.sin_t, M.cos_t);
+            od = rot_y_inv(od, M.sin_t, M.cos_t);
+        }
+        R entry = R(0), exit = R(0);
+        if (!boundary_hit(M, oo, od, -inf, inf, entry)) continue;
+        entry = Num<R>::fmax(entry, tmin);
+        if (!boundary_hit(M, oo, od, entry + R(0.0001), inf, exit)) continue;
+        exit = Num<R>::fmin(exit, t);
+        if (entry >= exit) continue;
+        entry = Num<R>::fmax(entry, R(0));
+        const R len = Num<R>::sqrt(len2(d));
+        if (len <= R(kEps)) continue;
+        const R inside = (exit - entry) * len;
+        const R sample = Num<R>::fmax(rnd<R>(g), Num<R>::min_positive());
+        const R dist = M.neg_inv_density * Num<R>::log(sample);
+        if (dist > inside) continue;
+        t = entry + dist / len;
+        prim = -2 - int(k);
+    }
+    return prim;
+}
+
+// medium_hit_record (volume/medium.rs:152-168): the world ray's point, normal +x, front face.
+template <class R> GT_DEV HitRec<R> make_medium_hit(const SceneDev<R>& sc, int prim, V3<R> o, V3<R> d, R t) {
+    HitRec<R> h;
+    h.p = o + d * t;
+    h.n = V3<R>{R(1), R(0), R(0)};
+    h.u = h.v = R(0);
+    h.front = true;
+    h.mat = sc.media[-2 - prim].mat;
+    return h;
+}
+
+// The hit record of a surface (prim >= 0) or a medium (prim <= -2).
+template <class R> GT_DEV HitRec<R> hit_of(const SceneDev<R>& sc, int prim, V3<R> o, V3<R> d, R time, R t) {
+    return prim >= 0 ? make_hit(sc, uint32_t(prim), o, d, time, t) : make_medium_hit(sc, prim, o, d, t);
+}
+
 // Origin of a ray that leaves the surface at h.  In f32 the hit point and the primitives'
 // stored corners and edges carry rounding errors of a few ulps of the coordinates (about
 // 1e-4 at 500 units), more than t_min = 0.001 covers for a grazing ray near the edge

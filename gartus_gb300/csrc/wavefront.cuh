@@ -245,24 +245,64 @@ template <class R> struct Shadow {
     V3<R> att;
     V3<R> s[2];
     R ratio[2];
+    uint32_t traced; // queries traced inline (scenes with media)
 };
+
+// Resolves shadow query k (after traversal) into the sample's radiance.
+template <class R, bool MEDIA = false>
+GT_DEV void apply_shadow(const Params<R>& P, V3<R>& col, const Shadow<R>& sh, int k, int prim, R t) {
+    const bool miss = MEDIA ? prim == -1 : prim < 0;
+    if (k == 0) { // closest hit; the emission of whatever is hit (camera.rs:2248-2261)
+        if (miss) return;
+        HitRec<R> h = MEDIA ? hit_of(P.sc, prim, sh.o, sh.dir[0], sh.time, t)
+                            : make_hit(P.sc, uint32_t(prim), sh.o, sh.dir[0], sh.time, t);
+        V3<R> e = mat_emitted(P.sc.mats[h.mat], h);
+        if (!finite3(e)) return;
+        V3<R> direct = cmul(sh.s[0], e) * sh.ratio[0];
+        col = col + cmul(sh.att, direct);
+    } else { // occlusion only (camera.rs:2284-2293)
+        if (!miss) return;
+        V3<R> direct = sh.s[1] * sh.ratio[1];
+        col = col + cmul(sh.att, direct);
+    }
+}
+
+// A next-event shadow query of a scene with media, traced where the reference traces it
+// (inside estimate_direct_lighting / estimate_environment_lighting, camera.rs:2248, 2284):
+// the world's closest hit, surfaces then media, whose draws come before the next sample
+// of the bounce.  The environment query needs the closest surface too, since it clips
+// the media's intervals.
+template <class R> GT_DEV void shadow_now(const Params<R>& P, V3<R>& col, Shadow<R>& sh, int k, Rng& g) {
+    const R inf = Num<R>::inf();
+    R t = inf;
+    int prim = traverse<R, false, false>(P.sc, sh.o, sh.dir[k], sh.time, R(kShadowAcne), inf, t, nullptr,
+                                         &P.ps.counters[C_ERROR], false);
+    if (prim < 0) t = inf;
+    prim = media_hit(P.sc, sh.o, sh.dir[k], R(kShadowAcne), t, prim, g);
+    apply_shadow<R, true>(P, col, sh, k, prim, t);
+    sh.traced += 1;
+}
 
 // One iteration of the bounce loop of ray_color (camera.rs:1742-1859): miss radiance,
 // emission, scatter, next-event sampling (camera.rs:2225-2297), continuation sample
 // (camera.rs:165-195) and Russian roulette (camera.rs:2498-2523).  `prim` < 0 is a miss.
 // Returns true if the path continues to another bounce.
-template <class R>
+// MEDIA: the scene has media; prim <= -2 is a medium hit and the shadow queries are traced
+// here, in the reference's order of draws, instead of being left in `sh`.
+template <class R, bool MEDIA = false>
 GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& p, int prim, R t, Rng& g,
                              Shadow<R>& sh) {
     sh.valid[0] = sh.valid[1] = false;
+    sh.traced = 0;
     bool cont = false;
-    if (prim < 0) {
+    if (MEDIA ? prim == -1 : prim < 0) {
         V3<R> bg = cam.use_env ? env_radiance(P.env, p.d) : background(cam, p.d);
         V3<R> miss = bg * p.miss_w;
         p.col = p.col + cmul(p.att, miss);
         return false;
     }
-    const HitRec<R> h = make_hit(P.sc, uint32_t(prim), p.o, p.d, p.time, t);
+    const HitRec<R> h =
+        MEDIA ? hit_of(P.sc, prim, p.o, p.d, p.time, t) : make_hit(P.sc, uint32_t(prim), p.o, p.d, p.time, t);
     const MatDev<R> m = P.sc.mats[h.mat];
     if (p.allow_emit) p.col = p.col + cmul(p.att, mat_emitted(m, h));
     ScatterRec<R> s = mat_scatter(m, p.d, h, g);
@@ -291,6 +331,12 @@ GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& 
                     }
                 }
             }
+            const bool area = sh.valid[0];
+            if (MEDIA && area) {
+                sh.o = spawn_origin(h, sh.dir[0]);
+                shadow_now(P, p.col, sh, 0, g);
+                sh.valid[0] = false;
+            }
             if (cam.use_env) { // estimate_environment_lighting, camera.rs:2264-2297
                 V3<R> edir;
                 R ep;
@@ -306,7 +352,15 @@ GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& 
                     }
                 }
             }
-            if (sh.valid[0] || sh.valid[1]) sh.o = spawn_origin(h, sh.valid[0] ? sh.dir[0] : sh.dir[1]);
+            if (MEDIA) {
+                if (sh.valid[1]) {
+                    if (!area) sh.o = spawn_origin(h, sh.dir[1]);
+                    shadow_now(P, p.col, sh, 1, g);
+                    sh.valid[1] = false;
+                }
+            } else if (sh.valid[0] || sh.valid[1]) {
+                sh.o = spawn_origin(h, sh.valid[0] ? sh.dir[0] : sh.dir[1]);
+            }
         }
         V3<R> dir;
         R pdf;
@@ -339,22 +393,6 @@ GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& 
     if (cont && p.bounce + 1 >= cam.max_depth) cont = false; // the bounce loop is exhausted
     if (cont) p.bounce += 1;
     return cont;
-}
-
-// Resolves shadow query k (after traversal) into the sample's radiance.
-template <class R> GT_DEV void apply_shadow(const Params<R>& P, V3<R>& col, const Shadow<R>& sh, int k, int prim, R t) {
-    if (k == 0) { // closest hit; the emission of whatever is hit (camera.rs:2248-2261)
-        if (prim < 0) return;
-        HitRec<R> h = make_hit(P.sc, uint32_t(prim), sh.o, sh.dir[0], sh.time, t);
-        V3<R> e = mat_emitted(P.sc.mats[h.mat], h);
-        if (!finite3(e)) return;
-        V3<R> direct = cmul(sh.s[0], e) * sh.ratio[0];
-        col = col + cmul(sh.att, direct);
-    } else { // occlusion only (camera.rs:2284-2293)
-        if (prim >= 0) return;
-        V3<R> direct = sh.s[1] * sh.ratio[1];
-        col = col + cmul(sh.att, direct);
-    }
 }
 
 // Wavefront shade step for `slot`: one bounce, pending shadow queries stored for k_shadow.
@@ -605,7 +643,9 @@ struct HandOff {
     uint32_t coop = 0;         // 1 = one slot per warp (RESUME launches only)
 };
 
-template <class R, bool RESUME, bool BATCH = false>
+// MEDIA: a scene with participating media; every ray's media draw from the pixel's stream
+// after its traversal, and shadow queries are traced inside integrate_bounce.
+template <class R, bool RESUME, bool BATCH = false, bool MEDIA = false>
 __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next, const uint32_t* queues,
                                                     const uint32_t* class_counts, const volatile uint32_t* cancel,
                                                     volatile uint32_t* progress, float* rgb, double* rgb64,
@@ -825,6 +865,10 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
             const R rt = which >= 0 ? sh.time : p.time;
             prim = traverse<R, false, false>(P.sc, ro, rd, rt, R(kShadowAcne), inf, t, nullptr,
                                              &P.ps.counters[C_ERROR], which == 1);
+            if constexpr (MEDIA) {
+                if (prim < 0) t = inf;
+                prim = media_hit(P.sc, ro, rd, R(kShadowAcne), t, prim, g);
+            }
         }
         __syncwarp();
         if (alive) {
@@ -834,8 +878,9 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
                 ++n_shadow;
             } else {
                 ++n_rays;
-                cont = integrate_bounce(P, cam(), p, prim, t, g, sh);
+                cont = integrate_bounce<R, MEDIA>(P, cam(), p, prim, t, g, sh);
                 pending = (sh.valid[0] ? 1u : 0u) | (sh.valid[1] ? 2u : 0u);
+                if constexpr (MEDIA) n_shadow += sh.traced;
             }
             if (pending == 0 && !cont) need_sample = true;
         }
@@ -991,8 +1036,14 @@ template <class R> __global__ void k_aov(Params<R> P, float* albedo, float* norm
             camera_ray(P.cam, x, y, k, g, o, d, time);
             int prim = traverse<R, false, false>(P.sc, o, d, time, R(kShadowAcne), inf, t, nullptr,
                                                  &P.ps.counters[C_ERROR]);
-            if (prim < 0) continue; // black on a miss
-            HitRec<R> h = make_hit(P.sc, uint32_t(prim), o, d, time, t);
+            if (P.sc.num_media) { // the media draw from the same stream (camera.rs:3104-3106)
+                if (prim < 0) t = inf;
+                prim = media_hit(P.sc, o, d, R(kShadowAcne), t, prim, g);
+                if (prim == -1) continue;
+            } else if (prim < 0) {
+                continue; // black on a miss
+            }
+            HitRec<R> h = hit_of(P.sc, prim, o, d, time, t);
             sa = sa + mat_albedo(P.sc.mats[h.mat], h);
             sn = sn + (h.n + V3<R>{1, 1, 1}) * R(0.5);
         }

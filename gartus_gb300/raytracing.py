@@ -118,12 +118,72 @@ class ImageTexture:
         return g
 
 
+def _media_table(media: Sequence) -> "C.Array":
+    """A gt_medium array for gt_scene_desc from (boundary, density, material id) entries."""
+    arr = (abi.gt_medium * max(len(media), 1))()
+    for i, (boundary, density, mat) in enumerate(media):
+        arr[i] = boundary.to_struct(density, mat)
+    return arr
+
+
 def _image_table(images: Sequence[ImageTexture]):
     """A gt_image array for gt_scene_desc (it points into the textures' own texels)."""
     arr = (abi.gt_image * max(len(images), 1))()
     for i, im in enumerate(images):
         arr[i] = im.to_struct()
     return arr
+
+
+# ---------------------------------------------------------------------- media
+class MediumBoundary:
+    """The boundary of a ConstantMedium: a Sphere or a box_object (object.rs:930-976),
+    optionally wrapped as Translate::new(RotateY::new(shape, degrees), offset)
+    (instance.rs), the composition the reference's smoke scenes use."""
+
+    def __init__(self, shape: int, p):
+        self.shape = shape
+        self.p = tuple(float(x) for x in p) + (0.0,) * (6 - len(p))
+        self.degrees: Optional[float] = None
+        self.offset: Optional[tuple] = None
+
+    @staticmethod
+    def sphere(center, radius) -> "MediumBoundary":
+        return MediumBoundary(abi.GT_MEDIUM_SPHERE, _vec(center) + (float(radius),))
+
+    @staticmethod
+    def box(a, b) -> "MediumBoundary":
+        return MediumBoundary(abi.GT_MEDIUM_BOX, _vec(a) + _vec(b))
+
+    def rotate_y(self, degrees) -> "MediumBoundary":
+        if self.degrees is not None or self.offset is not None:
+            raise ValueError("a medium boundary takes one RotateY, inside its Translate")
+        out = copy.copy(self)
+        out.degrees = float(degrees)
+        return out
+
+    def translate(self, offset) -> "MediumBoundary":
+        if self.offset is not None:
+            raise ValueError("a medium boundary takes one Translate")
+        out = copy.copy(self)
+        out.offset = _vec(offset)
+        return out
+
+    def to_struct(self, density: float, material: int) -> abi.gt_medium:
+        m = abi.gt_medium()
+        m.shape = self.shape
+        m.material = int(material)
+        for i, x in enumerate(self.p):
+            m.p[i] = x
+        m.transform = 0
+        if self.degrees is not None:
+            m.rotate_y = self.degrees
+            m.transform |= abi.GT_MEDIUM_ROTATE_Y
+        if self.offset is not None:
+            for i, x in enumerate(self.offset):
+                m.translate[i] = x
+            m.transform |= abi.GT_MEDIUM_TRANSLATE
+        m.density = float(density)
+        return m
 
 
 # ------------------------------------------------------------------ materials
@@ -390,11 +450,13 @@ class Context:
 
 class _SceneHandle:
     def __init__(self, ctx: Context, prims: np.ndarray, mats: np.ndarray, leaf_size: int,
-                 bvh_builder: int = abi.GT_BVH_REFERENCE_SAH, images: Sequence[ImageTexture] = ()):
+                 bvh_builder: int = abi.GT_BVH_REFERENCE_SAH, images: Sequence[ImageTexture] = (),
+                 media: Sequence = ()):
         self.ctx = ctx
         prims = np.ascontiguousarray(prims)
         mats = np.ascontiguousarray(mats)
         table = _image_table(images)
+        mtable = _media_table(media)
         d = abi.gt_scene_desc()
         d.struct_size = C.sizeof(abi.gt_scene_desc)
         d.num_primitives = len(prims)
@@ -405,6 +467,8 @@ class _SceneHandle:
         d.bvh_builder = bvh_builder
         d.num_images = len(images)
         d.images = table
+        d.num_media = len(media)
+        d.media = mtable
         h = C.c_void_p()
         check(lib().gt_scene_create(ctx.handle, C.byref(d), C.byref(h)))
         self.h = h
@@ -454,6 +518,7 @@ class RayScene:
         self._prims: Optional[np.ndarray] = np.zeros(0, dtype=PRIMITIVE_DTYPE)
         self._leaf_size = 4
         self._bvh_builder = abi.GT_BVH_REFERENCE_SAH
+        self._media: list = []
         self._handles: dict = {}
 
     # -- tables
@@ -520,6 +585,31 @@ class RayScene:
         mid = self.add_material(material)
         self.add_quad(corner, u, v, mid)
         return mid
+
+    # -- participating media
+    def add_constant_medium(self, boundary: MediumBoundary, density, albedo) -> int:
+        """ConstantMedium::new(boundary, density, albedo) (volume/medium.rs:30-39): an
+        Isotropic phase function.  Media follow the surfaces in the world's hit order, in
+        the order they are added (HittableList, scene.rs:177-197).  Returns the medium index."""
+        return self.add_medium_with_phase_function(boundary, density, RayMaterial.isotropic(albedo))
+
+    def add_medium_with_phase_function(self, boundary: MediumBoundary, density, material: RayMaterial) -> int:
+        """ConstantMedium::with_phase_function (volume/medium.rs:71-81)."""
+        density = float(density)
+        if not (math.isfinite(density) and density > 0.0):
+            raise ValueError("medium density must be positive and finite")  # medium.rs:93-96
+        if not isinstance(boundary, MediumBoundary):
+            raise TypeError("a medium boundary is a MediumBoundary")
+        if len(self._media) >= 64:
+            raise ValueError("at most 64 media per scene")
+        mid = self.add_material(material)
+        self._media.append((boundary, density, mid))
+        self._invalidate()
+        return len(self._media) - 1
+
+    def media(self) -> list:
+        """(boundary, density, material id) per medium, in hit order."""
+        return list(self._media)
 
     # -- BVH options
     def build_bvh(self) -> None:
@@ -606,7 +696,7 @@ class RayScene:
         h = self._handles.get(id(ctx))
         if h is None or h.ctx is not ctx or not h.h:
             h = _SceneHandle(ctx, self.primitives_array(), self.materials_array(), self._leaf_size,
-                             self._bvh_builder, self.images())
+                             self._bvh_builder, self.images(), self._media)
             self._handles[id(ctx)] = h
         return h
 

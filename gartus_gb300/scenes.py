@@ -11,7 +11,7 @@ import math
 import numpy as np
 
 from . import abi
-from .raytracing import GLASS, RayCamera, RayMaterial, RayScene, SamplingTargetList
+from .raytracing import GLASS, MediumBoundary, RayCamera, RayMaterial, RayScene, SamplingTargetList
 
 MASK = 0xFFFFFFFFFFFFFFFF
 
@@ -184,6 +184,33 @@ def cornell_camera(width: int = 600, grid: int = 16, max_depth: int = 50) -> Ray
             .with_vertical_fov(40.0)
             .with_look_at((278.0, 278.0, -800.0), (278.0, 278.0, 0.0))
             .with_view_up((0.0, 1.0, 0.0)))
+
+
+def cornell_smoke_scene() -> tuple[RayScene, SamplingTargetList]:
+    """cornell_smoke_world (raytracing/scenes.rs:296-378): the five walls and a 330x305
+    ceiling light of radiance 7, and the two boxes of the Cornell box as constant-density
+    media (density 0.01; black smoke in the tall box rotated 15 degrees, white smoke in the
+    short one rotated -18 degrees), tested after the walls in that order.  The light quad
+    is returned as a sampling target for next-event estimation."""
+    scene = RayScene()
+    red = scene.add_material(RayMaterial.lambertian((0.65, 0.05, 0.05)))
+    white = scene.add_material(RayMaterial.lambertian((0.73, 0.73, 0.73)))
+    green = scene.add_material(RayMaterial.lambertian((0.12, 0.45, 0.15)))
+    light = scene.add_material(RayMaterial.diffuse_light((7.0, 7.0, 7.0)))
+    scene.add_quad((555.0, 0.0, 0.0), (0.0, 555.0, 0.0), (0.0, 0.0, 555.0), green)
+    scene.add_quad((0.0, 0.0, 0.0), (0.0, 555.0, 0.0), (0.0, 0.0, 555.0), red)
+    scene.add_quad((113.0, 554.0, 127.0), (330.0, 0.0, 0.0), (0.0, 0.0, 305.0), light)
+    scene.add_quad((0.0, 555.0, 0.0), (555.0, 0.0, 0.0), (0.0, 0.0, 555.0), white)
+    scene.add_quad((0.0, 0.0, 0.0), (555.0, 0.0, 0.0), (0.0, 0.0, 555.0), white)
+    scene.add_quad((0.0, 0.0, 555.0), (555.0, 0.0, 0.0), (0.0, 555.0, 0.0), white)
+    tall = MediumBoundary.box((0.0, 0.0, 0.0), (165.0, 330.0, 165.0)).rotate_y(15.0).translate((265.0, 0.0, 295.0))
+    short = MediumBoundary.box((0.0, 0.0, 0.0), (165.0, 165.0, 165.0)).rotate_y(-18.0).translate((130.0, 0.0, 65.0))
+    scene.add_constant_medium(tall, 0.01, (0.0, 0.0, 0.0))
+    scene.add_constant_medium(short, 0.01, (1.0, 1.0, 1.0))
+    scene.build_bvh()
+    lights = SamplingTargetList()
+    lights.add_quad((113.0, 554.0, 127.0), (330.0, 0.0, 0.0), (0.0, 0.0, 305.0))
+    return scene, lights
 
 
 # -------------------------------------------------------- reference bench scene

@@ -143,6 +143,33 @@ typedef enum gt_bvh_builder {
                                  reference counterpart.                                        */
 } gt_bvh_builder;
 
+/* A constant-density participating medium (ConstantMedium, raytracing/volume/medium.rs:13-187)
+ * whose boundary is a sphere or a box_object (object.rs:930-976), optionally wrapped as
+ * Translate(RotateY(shape, rotate_y), translate) (instance.rs).  A scene with media renders as
+ * the reference's HittableList [the RayScene's surfaces, media[0], media[1], ...]
+ * (scene.rs:177-197): each ray's media are tested in order after the surfaces, and a medium
+ * whose boundary interval, clipped to the closest hit so far, is not empty draws one sample
+ * from the pixel's stream (path, shadow and AOV rays alike).  The ray queries
+ * gt_trace_rays / gt_trace_primary see the surfaces only, as RayScene::hit does. */
+typedef enum gt_medium_shape {
+    GT_MEDIUM_SPHERE = 0, /* p[0..3) centre, p[3] radius */
+    GT_MEDIUM_BOX = 1     /* p[0..3) / p[3..6) two opposite corners */
+} gt_medium_shape;
+typedef enum gt_medium_transform {
+    GT_MEDIUM_ROTATE_Y = 1, /* RotateY::new(shape, rotate_y degrees)              */
+    GT_MEDIUM_TRANSLATE = 2 /* Translate::new(.., translate), outside the rotation */
+} gt_medium_transform;
+typedef struct gt_medium {
+    uint32_t shape;       /* gt_medium_shape */
+    uint32_t material;    /* phase function (ConstantMedium::new uses Isotropic(albedo)) */
+    double p[6];
+    double rotate_y;      /* degrees */
+    double translate[3];
+    double density;       /* positive and finite (medium.rs:93-96) */
+    uint32_t transform;   /* gt_medium_transform bits */
+    uint32_t reserved;
+} gt_medium;
+
 typedef struct gt_scene_desc {
     uint32_t struct_size; /* sizeof(gt_scene_desc) */
     uint32_t num_primitives;
@@ -153,6 +180,9 @@ typedef struct gt_scene_desc {
     uint32_t bvh_builder;   /* gt_bvh_builder */
     uint32_t num_images;
     const gt_image* images; /* textures referenced by GT_TEX_IMAGE materials (copied) */
+    uint32_t num_media;
+    uint32_t reserved;
+    const gt_medium* media; /* participating media after the surfaces, in list order (copied) */
 } gt_scene_desc;
 
 /* One weighted sampling target (WeightedSamplingTargetList, raytracing/scene.rs:423-497).

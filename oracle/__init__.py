@@ -63,6 +63,7 @@ def lib() -> C.CDLL:
                 "orc_scattering_pdf": (f64, [vp, vp, vp, vp, i32, vp]),
                 "orc_cosine_pdf": (f64, [vp, vp]),
                 "orc_image_sample": (None, [vp, f64, f64, vp]),
+                "orc_medium_hit": (i32, [vp, vp, f64, f64, u64, vp, vp]),
             }
             for name, (res, args) in sig.items():
                 fn = getattr(L, name)
@@ -79,13 +80,15 @@ def _ptr(a: np.ndarray):
 class OracleScene:
     """A RayScene loaded into the oracle (f64 and f32 copies, reference BVH built)."""
 
-    def __init__(self, prims: np.ndarray, mats: np.ndarray, leaf_size: int = 4, images=()):
+    def __init__(self, prims: np.ndarray, mats: np.ndarray, leaf_size: int = 4, images=(), media=()):
         from gartus_gb300 import abi
-        from gartus_gb300.raytracing import _image_table
+        from gartus_gb300.raytracing import _image_table, _media_table
         self._prims = np.ascontiguousarray(prims)
         self._mats = np.ascontiguousarray(mats)
         self._images = list(images)
         self._table = _image_table(self._images)
+        self._media = list(media)
+        self._mtable = _media_table(self._media)
         d = abi.gt_scene_desc()
         d.struct_size = C.sizeof(abi.gt_scene_desc)
         d.num_primitives = len(self._prims)
@@ -95,13 +98,15 @@ class OracleScene:
         d.bvh_leaf_size = leaf_size
         d.num_images = len(self._images)
         d.images = self._table
+        d.num_media = len(self._media)
+        d.media = self._mtable
         self.h = lib().orc_scene_create(C.byref(d))
         if not self.h:
             raise ValueError("oracle rejected the scene")
 
     @classmethod
     def from_ray_scene(cls, scene) -> "OracleScene":
-        return cls(scene.primitives_array(), scene.materials_array(), scene.leaf_size, scene.images())
+        return cls(scene.primitives_array(), scene.materials_array(), scene.leaf_size, scene.images(), scene.media())
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -190,3 +195,16 @@ def image_sample(texture, u: float, v: float) -> np.ndarray:
     out = np.zeros(3)
     lib().orc_image_sample(C.byref(g), float(u), float(v), _ptr(out))
     return out
+
+
+def medium_hit(boundary, density: float, ray, tmin: float, tmax: float, seed: int):
+    """ConstantMedium::hit_with_rng of one medium (boundary a
+    gartus_gb300.raytracing.MediumBoundary) on ray = (origin, direction[, time]) with a
+    SampleRng seeded `seed`: (t or None, number of draws)."""
+    m = boundary.to_struct(density, 0)
+    r = np.zeros(7)
+    r[:len(np.ravel(ray))] = np.ravel(ray)
+    t = C.c_double()
+    n = C.c_uint32()
+    hit = lib().orc_medium_hit(C.byref(m), _ptr(r), float(tmin), float(tmax), int(seed), C.byref(t), C.byref(n))
+    return (t.value if hit else None), n.value

@@ -460,6 +460,98 @@ template <class R> inline bool intersect(const Prim<R>& p, const Ray<R>& ray, R 
     return false;
 }
 
+// ------------------------------------------------------------------- media
+// ConstantMedium (raytracing/volume/medium.rs) around a Sphere or a box_object
+// (object.rs:930-976), wrapped as Translate(RotateY(shape)) (instance.rs).
+template <class R> struct Medium {
+    std::vector<Prim<R>> parts; // the sphere, or the box's six sides in box_object's order
+    uint32_t material = 0;
+    bool rotate = false, translate = false;
+    R sin_theta{0}, cos_theta{1};
+    V3<R> offset;
+    R neg_inv_density{-1};
+
+    static Medium from_desc(const gt_medium& m) {
+        Medium md;
+        md.material = m.material;
+        md.rotate = (m.transform & GT_MEDIUM_ROTATE_Y) != 0;
+        md.translate = (m.transform & GT_MEDIUM_TRANSLATE) != 0;
+        const double radians = m.rotate_y * kPi / 180.0; // degrees_to_radians, raytracing.rs:150-152
+        md.sin_theta = R(std::sin(radians));
+        md.cos_theta = R(std::cos(radians));
+        md.offset = v3<R>(m.translate);
+        md.neg_inv_density = R(-1.0 / m.density);
+        auto quad = [&](double qx, double qy, double qz, const double* u, const double* v) {
+            gt_geometry g{};
+            g.kind = GT_GEOM_QUAD;
+            g.p[0] = qx, g.p[1] = qy, g.p[2] = qz;
+            for (int k = 0; k < 3; ++k) g.p[3 + k] = u[k], g.p[6 + k] = v[k];
+            md.parts.push_back(Prim<R>::from_geometry(g, m.material));
+        };
+        if (m.shape == GT_MEDIUM_SPHERE) {
+            gt_geometry g{};
+            g.kind = GT_GEOM_SPHERE;
+            for (int k = 0; k < 4; ++k) g.p[k] = m.p[k];
+            md.parts.push_back(Prim<R>::from_geometry(g, m.material));
+        } else {
+            double lo[3], hi[3];
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = std::fmin(m.p[k], m.p[3 + k]);
+                hi[k] = std::fmax(m.p[k], m.p[3 + k]);
+            }
+            const double dx[3] = {hi[0] - lo[0], 0, 0}, dy[3] = {0, hi[1] - lo[1], 0}, dz[3] = {0, 0, hi[2] - lo[2]};
+            const double mdx[3] = {-dx[0], -dx[1], -dx[2]}, mdz[3] = {-dz[0], -dz[1], -dz[2]};
+            quad(lo[0], lo[1], hi[2], dx, dy);  // front
+            quad(hi[0], lo[1], hi[2], mdz, dy); // right
+            quad(hi[0], lo[1], lo[2], mdx, dy); // back
+            quad(lo[0], lo[1], lo[2], dz, dy);  // left
+            quad(lo[0], hi[1], hi[2], dx, mdz); // top
+            quad(lo[0], lo[1], lo[2], dx, dz);  // bottom
+        }
+        return md;
+    }
+
+    // The boundary's closest hit in (tmin, tmax), through Translate then RotateY.
+    bool boundary(const Ray<R>& world, R tmin, R tmax, R& t) const {
+        Ray<R> r = world;
+        if (translate) r.o = r.o - offset;
+        if (rotate) { // rotate_y_point_inverse / rotate_y_vector_inverse
+            r.o = V3<R>(cos_theta * r.o.x - sin_theta * r.o.z, r.o.y, sin_theta * r.o.x + cos_theta * r.o.z);
+            r.d = V3<R>(cos_theta * r.d.x - sin_theta * r.d.z, r.d.y, sin_theta * r.d.x + cos_theta * r.d.z);
+        }
+        bool any = false;
+        for (const Prim<R>& p : parts) { // HittableList: each later side must be closer
+            Hit<R> h;
+            if (intersect(p, r, tmin, tmax, h)) {
+                tmax = h.t;
+                t = h.t;
+                any = true;
+            }
+        }
+        return any;
+    }
+
+    // ConstantMedium::hit_with_rng with boundary_interval (medium.rs:119-187).
+    bool hit(const Ray<R>& ray, R tmin, R tmax, SampleRng& rng, R& t) const {
+        const R inf = std::numeric_limits<R>::infinity();
+        R entry, exit;
+        if (!boundary(ray, -inf, inf, entry)) return false;
+        entry = std::fmax(entry, tmin);
+        if (!boundary(ray, entry + R(0.0001), inf, exit)) return false;
+        exit = std::fmin(exit, tmax);
+        if (entry >= exit) return false;
+        entry = std::fmax(entry, R(0));
+        const R len = std::sqrt(length_squared(ray.d));
+        if (len <= R(kEps)) return false;
+        const R inside = (exit - entry) * len;
+        const R sample = std::fmax(rng.random_double<R>(), std::numeric_limits<R>::min());
+        const R distance = neg_inv_density * std::log(sample);
+        if (distance > inside) return false;
+        t = entry + distance / len;
+        return true;
+    }
+};
+
 // ----------------------------------------------------------------------- BVH
 struct BvhStats { // BvhTraversalStats, bvh.rs:9-52
     uint64_t rays = 0, node_bounds_tests = 0, node_bounds_hits = 0, leaf_visits = 0, primitive_candidates = 0,
@@ -1314,12 +1406,21 @@ template <class R> struct Scene {
     std::vector<Prim<R>> prims;
     std::vector<gt_geometry> geoms;
     std::vector<Material<R>> materials;
+    std::vector<Medium<R>> media;
     FlatBvh bvh;
 
     void load(const gt_scene_desc& d) {
         prims.clear();
         geoms.clear();
         materials.clear();
+        media.clear();
+        for (uint32_t i = 0; i < (d.media ? d.num_media : 0u); ++i) {
+            const gt_medium& m = d.media[i];
+            if (m.material >= d.num_materials || !(std::isfinite(m.density) && m.density > 0.0) ||
+                m.shape > GT_MEDIUM_BOX)
+                throw std::invalid_argument("invalid medium");
+            media.push_back(Medium<R>::from_desc(m));
+        }
         std::vector<std::shared_ptr<const ImageData>> images;
         for (uint32_t i = 0; i < (d.images ? d.num_images : 0u); ++i) {
             auto im = std::make_shared<ImageData>();
@@ -1365,6 +1466,28 @@ template <class R> struct Scene {
                 best = h;
                 any = true;
             }
+        }
+        return any;
+    }
+
+    // HittableList::hit_with_rng over [this RayScene, media...] (scene.rs:177-197): the
+    // surfaces' closest hit, then each medium in order, clipped to the closest so far.  A
+    // medium hit is the medium_hit_record of medium.rs:152-168.
+    bool world_hit(const Ray<R>& ray, R tmin, R tmax, Hit<R>& out, SampleRng& rng) const {
+        bool any = hit(ray, tmin, tmax, out);
+        R closest = any ? out.t : tmax;
+        for (size_t k = 0; k < media.size(); ++k) {
+            R t;
+            if (!media[k].hit(ray, tmin, closest, rng, t)) continue;
+            closest = t;
+            out = Hit<R>();
+            out.point = ray.at(t);
+            out.normal = V3<R>(1, 0, 0);
+            out.t = t;
+            out.front_face = true;
+            out.prim = -2 - int(k);
+            out.material = media[k].material;
+            any = true;
         }
         return any;
     }
@@ -1601,7 +1724,7 @@ template <class R> struct Renderer {
         const R inf = std::numeric_limits<R>::infinity();
         for (uint32_t bounce = 0; bounce < cam.desc.max_depth; ++bounce) {
             Hit<R> rec;
-            if (!scene->hit(ray, R(kShadowAcne), inf, rec)) {
+            if (!scene->world_hit(ray, R(kShadowAcne), inf, rec, rng)) {
                 V3<R> miss = miss_radiance(ray.d) * miss_w;
                 return color + cmul(att, miss);
             }
@@ -1662,7 +1785,7 @@ template <class R> struct Renderer {
         R sp = scattering_pdf(m, in, rec, dir);
         if (!std::isfinite(sp) || sp <= R(0)) return V3<R>();
         Hit<R> lh;
-        if (!scene->hit(shadow, R(kShadowAcne), std::numeric_limits<R>::infinity(), lh)) return V3<R>();
+        if (!scene->world_hit(shadow, R(kShadowAcne), std::numeric_limits<R>::infinity(), lh, rng)) return V3<R>();
         V3<R> e = emitted(scene->materials[lh.material], lh);
         if (!finite3(e)) return V3<R>();
         return cmul(satt, e) * (sp / lp);
@@ -1680,7 +1803,7 @@ template <class R> struct Renderer {
         if (!std::isfinite(sp) || sp <= R(0)) return V3<R>();
         R mis = power_heuristic(ep, sp);
         Hit<R> sh;
-        if (scene->hit(shadow, R(kShadowAcne), std::numeric_limits<R>::infinity(), sh)) return V3<R>();
+        if (scene->world_hit(shadow, R(kShadowAcne), std::numeric_limits<R>::infinity(), sh, rng)) return V3<R>();
         return cmul(satt, env->radiance(dir)) * (mis * sp / ep);
     }
 
@@ -1742,7 +1865,7 @@ template <class R> struct Renderer {
         uint32_t n = cam.effective_spp();
         auto sample = [&](const Ray<R>& ray) {
             Hit<R> rec;
-            if (!scene->hit(ray, R(kShadowAcne), std::numeric_limits<R>::infinity(), rec)) return V3<R>();
+            if (!scene->world_hit(ray, R(kShadowAcne), std::numeric_limits<R>::infinity(), rec, rng)) return V3<R>();
             if (kind == 0) return denoise_albedo(scene->materials[rec.material], rec);
             return (rec.normal + V3<R>(1, 1, 1)) * R(0.5);
         };

@@ -388,6 +388,30 @@ double orc_scattering_pdf(const gt_material* md, const double* ray7, const doubl
     h.front_face = front != 0;
     return scattering_pdf(m, r, h, V3<double>(dir[0], dir[1], dir[2]));
 }
+// ConstantMedium::hit_with_rng of one medium alone on ray7 = {origin, direction, time} in
+// (tmin, tmax) with a SampleRng seeded `seed`: 1 and *t on a scatter, else 0; *draws = the
+// number of draws taken.
+int orc_medium_hit(const gt_medium* m, const double* ray7, double tmin, double tmax, uint64_t seed, double* t,
+                   uint32_t* draws) {
+    const Medium<double> md = Medium<double>::from_desc(*m);
+    Ray<double> r;
+    r.o = V3<double>(ray7[0], ray7[1], ray7[2]);
+    r.d = V3<double>(ray7[3], ray7[4], ray7[5]);
+    r.time = ray7[6];
+    SampleRng rng(seed);
+    SampleRng start = rng;
+    double th = 0.0;
+    const bool hit = md.hit(r, tmin, tmax, rng, th);
+    uint32_t n = 0;
+    while (start.state != rng.state && n < 8) {
+        start.next_u64();
+        ++n;
+    }
+    *draws = n;
+    *t = hit ? th : 0.0;
+    return hit ? 1 : 0;
+}
+
 // ImageTexture sampling at (u, v) into linear RGB.
 void orc_image_sample(const gt_image* g, double u, double v, double* out) {
     ImageData im;

@@ -737,3 +737,91 @@ def test_image_texture_edge_cases(gpu_context):
     with pytest.raises(GartusError):
         from gartus_gb300.raytracing import _SceneHandle
         _SceneHandle(gpu_context, scene.primitives_array(), bad, 4, abi.GT_BVH_REFERENCE_SAH, scene.images())
+
+
+def _smoke_camera(width, spp, depth=12):
+    return scenes.cornell_camera(width, 1, depth).with_pixel_sample_mode(abi.GT_SAMPLE_RANDOM).with_samples_per_pixel(spp)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("mode", ["plain", "mixture", "nee"])
+def test_media_smoke_scene(gpu_context, precision, mode):
+    # cornell_smoke_world (raytracing/scenes.rs:296-378): two ConstantMedium boxes under
+    # RotateY / Translate after the walls.  Each ray's media draw from the pixel's stream
+    # after its surfaces (scene.rs:177-197, medium.rs:170-187), next-event shadow rays
+    # included (camera.rs:2248), so the f64 image matches the oracle's only if every draw
+    # lands where the reference takes it.
+    scene, lights = scenes.cornell_smoke_scene()
+    cam = _smoke_camera(40, 6)
+    if mode == "nee":
+        cam = cam.with_direct_lighting_mode(abi.GT_DIRECT_NEXT_EVENT_ESTIMATION)
+    use = None if mode == "plain" else lights
+    pt = PathTracer(cam, precision=precision, context=gpu_context)
+    render = (lambda **k: pt.render_hdr_image(scene, **k)) if use is None else \
+        (lambda **k: pt.render_with_lights_hdr_image(scene, use, **k))
+    ref, acc = _oracle_render(scene, cam, use)
+    if precision == "f64":
+        img = render(want64=True)
+        np.testing.assert_array_equal(img.accepted, acc)
+        err = rel_err(img.pixels64, ref, floor=1e-12).max(axis=2)
+        assert (err <= 1e-9).mean() >= 0.99, err.max()
+    else:
+        img = render()
+        ref32, _ = _oracle_render(scene, cam, use, precision=0)
+        n = ref.shape[0] * ref.shape[1]
+        assert _divergent(img.pixels, ref) <= _divergent(ref32, ref) + 0.03 * n
+    st = pt.last_stats  # every ray ran in the persistent kernel's media variant
+    assert st["persistent_rays"] == st["rays"] + st["shadow_rays"]
+    assert (st["shadow_rays"] > 0) == (mode == "nee")
+    assert np.isfinite(img.pixels).all()
+
+
+def test_media_phase_function_environment_and_aovs(gpu_context):
+    # A sphere-bounded Henyey-Greenstein medium, a plain sphere medium and an environment
+    # light: the environment's shadow query (occlusion) draws for the media too
+    # (camera.rs:2284-2290); the denoising AOVs draw from the same stream (camera.rs:3104).
+    from gartus_gb300.raytracing import MediumBoundary
+    scene = RayScene()
+    ground = scene.add_material(RayMaterial.lambertian((0.5, 0.5, 0.5)))
+    scene.add_sphere((0.0, -100.5, -1.0), 100.0, ground)
+    scene.add_sphere((1.1, 0.0, -1.3), 0.45, scene.add_material(RayMaterial.metal((0.8, 0.8, 0.8), 0.1)))
+    scene.add_medium_with_phase_function(MediumBoundary.sphere((-0.6, 0.1, -1.2), 0.6), 1.5,
+                                         RayMaterial.henyey_greenstein((0.9, 0.8, 0.7), 0.5))
+    scene.add_constant_medium(MediumBoundary.box((-0.3, -0.5, -2.6), (0.5, 0.6, -1.8)).rotate_y(25.0),
+                              3.0, (0.4, 0.6, 0.9))
+    scene.build_bvh()
+    env = EnvironmentLight(_env_u8(7, 16, 8))
+    cam = RayCamera(40, 1.5).with_samples_per_pixel(6).with_max_depth(10)
+    img = PathTracer(cam, precision="f64", context=gpu_context).render_with_environment_hdr_image(
+        scene, env, want64=True)
+    ref, acc = _oracle_render(scene, cam, env=env)
+    np.testing.assert_array_equal(img.accepted, acc)
+    err = rel_err(img.pixels64, ref, floor=1e-12).max(axis=2)
+    assert (err <= 1e-9).mean() >= 0.99, err.max()
+    aovs = PathTracer(cam, precision="f64", context=gpu_context).render_denoising_aovs(scene)
+    _, _, alb, nrm = _oracle_render(scene, cam, aovs=True)
+    np.testing.assert_allclose(aovs.albedo_linear, alb, rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(aovs.normal_linear, nrm, rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_media_batch_and_unsupported(gpu_context, precision):
+    # A batch of a scene with media runs the persistent batch (MEDIA variant) and gives
+    # each frame's single render; accumulation of such a scene is refused.
+    from gartus_gb300.raytracing import Accumulator
+    scene, lights = scenes.cornell_smoke_scene()
+    cams = [_smoke_camera(24, 3).with_rng_seed(s) for s in (1, 2)] + [_smoke_camera(16, 2)]
+    pt = PathTracer(cams[0], precision=precision, context=gpu_context)
+    imgs = pt.render_batch_hdr_images(scene, cams, lights=lights, want64=precision == "f64")
+    for cam, img in zip(cams, imgs):
+        one = PathTracer(cam, precision=precision, context=gpu_context).render_with_lights_hdr_image(
+            scene, lights, want64=precision == "f64")
+        np.testing.assert_array_equal(img.accepted, one.accepted)
+        if precision == "f64":
+            np.testing.assert_array_equal(img.pixels64, one.pixels64)
+        else:
+            assert _divergent(img.pixels, one.pixels.astype(np.float64)) <= 0.05 * img.pixels.shape[0] * img.pixels.shape[1]
+    acc = Accumulator(24, 24, precision, gpu_context)
+    with pytest.raises(GartusError) as e:
+        PathTracer(cams[0], context=gpu_context).render_accumulate(scene, acc, 1, lights=lights)
+    assert e.value.status == abi.GT_ERR_UNSUPPORTED
