@@ -37,6 +37,7 @@ def _declare(L: C.CDLL) -> None:
         "gt_scene_create": (st, [C.c_void_p, P(abi.gt_scene_desc), P(C.c_void_p)]),
         "gt_scene_destroy": (None, [C.c_void_p]),
         "gt_scene_bvh_node_count": (st, [C.c_void_p, P(C.c_uint32)]),
+        "gt_scene_update_primitives": (st, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]),
         "gt_scene_emissive_targets": (st, [C.c_void_p, C.c_void_p, C.c_uint32, P(C.c_uint32)]),
         "gt_lights_create": (st, [C.c_void_p, C.c_void_p, C.c_uint32, P(C.c_void_p)]),
         "gt_lights_destroy": (None, [C.c_void_p]),
@@ -102,7 +103,7 @@ def check(status: int) -> None:
 
 EXPORTED_SYMBOLS = [
     "gt_abi_version", "gt_last_error", "gt_camera_default", "gt_camera_image_size", "gt_context_create",
-    "gt_context_destroy", "gt_scene_create", "gt_scene_destroy", "gt_scene_bvh_node_count",
+    "gt_context_destroy", "gt_scene_create", "gt_scene_destroy", "gt_scene_bvh_node_count", "gt_scene_update_primitives",
     "gt_scene_emissive_targets", "gt_lights_create", "gt_lights_destroy", "gt_environment_create",
     "gt_environment_destroy", "gt_render", "gt_trace_rays", "gt_trace_primary", "gt_render_noalloc",
     "gt_render_batch", "gt_accumulator_create", "gt_accumulator_destroy", "gt_accumulator_samples",

@@ -374,6 +374,36 @@ void gt_scene_destroy(gt_scene* s) {
     delete s;
 }
 
+gt_status gt_scene_update_primitives(gt_scene* s, uint32_t first, uint32_t count, const gt_primitive* prims) {
+    GT_GUARD_BEGIN
+    if (!s || (count && !prims)) return fail(GT_ERR_INVALID_ARG, "null argument");
+    if (uint64_t(first) + count > s->prims.size()) return fail(GT_ERR_INVALID_ARG, "primitive range out of bounds");
+    for (uint32_t i = 0; i < count; ++i) {
+        gt_status rc = validate_geometry(prims[i].geometry);
+        if (rc != GT_OK) return rc;
+        if (prims[i].material >= s->mats.size())
+            return fail(GT_ERR_INVALID_ARG, "ray scene material id out of bounds"); // scene.rs:1158-1161
+    }
+    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    cudaError_t ce = cudaSetDevice(s->ctx->device);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
+    ce = cudaStreamSynchronize(s->ctx->stream); // no render of this context still reads the old data
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamSynchronize");
+    std::copy(prims, prims + count, s->prims.begin() + first);
+    // The reference tree is rebuilt when next needed (the f64 path, statistics, the
+    // reference builder's f32 path); a GPU-built f32 tree is refitted now.
+    s->bvh_ready = false;
+    free_gpu_f64(s);
+    gt_status rc = update_f32(s, first, count);
+    if (rc != GT_OK) {
+        free_gpu_f32(s);
+        return rc;
+    }
+    if (s->bvh_builder == GT_BVH_REFERENCE_SAH) return ensure_reference_bvh(s);
+    return GT_OK;
+    GT_GUARD_END
+}
+
 gt_status gt_scene_bvh_node_count(const gt_scene* s, uint32_t* count) {
     GT_GUARD_BEGIN
     if (!s || !count) return fail(GT_ERR_INVALID_ARG, "null argument");

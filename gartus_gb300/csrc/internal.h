@@ -29,6 +29,14 @@ template <class R> struct GpuScene {
     uint8_t* texels = nullptr;     // every image's texels, back to back
     ImageDev* images = nullptr;
     MediumDev<R>* media = nullptr;
+    // GT_BVH_GPU_LBVH (f32 only): the tree's bottom-up links and leaf boxes, kept so that
+    // gt_scene_update_primitives can refit it in place.
+    int32_t* parent_leaf = nullptr;
+    int32_t* parent_int = nullptr;
+    uint32_t* arrivals = nullptr;
+    float* int_box = nullptr;
+    float* leaf_box = nullptr;
+    uint32_t* leaf_of = nullptr; // original primitive index -> leaf position
     PrimRec<R>* prims = nullptr;
     uint2* meta = nullptr;
     Node<R>* nodes = nullptr;
@@ -184,6 +192,9 @@ void free_env_f64(gt_environment* e);
 namespace gt {
 // The reference-layout SAH tree of `s`, built on first use (api.cu).
 gt_status ensure_reference_bvh(gt_scene* s);
+gt_status refit_lbvh_f32(GpuScene<float>& g, uint32_t n, uint32_t count, const uint32_t* index,
+                         const PrimRec<float>* recs, const uint2* meta, const float* boxes, cudaStream_t st, int sms);
+gt_status update_f32(gt_scene* s, uint32_t first, uint32_t count);
 // A linear BVH for the f32 path built on the device from f32 primitive bounds; permutes
 // g.prims / g.meta into leaf order and sets the view's nodes and root (lbvh.cu).
 gt_status build_lbvh_f32(GpuScene<float>& g, uint32_t n, const float* boxes_host, const double* bounds_lo,

@@ -132,6 +132,25 @@ __global__ void k_boxes(const float* leaf_box, int n, const int32_t* parent_leaf
     }
 }
 
+// leaf_of[original index] = leaf position.
+__global__ void k_invert(const uint32_t* order, uint32_t n, uint32_t* leaf_of) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) leaf_of[order[k]] = k;
+}
+
+// Refit input: updated primitives (original index, record, metadata, box) scattered into
+// their leaf positions.
+__global__ void k_update(const uint32_t* index, const PrimRec<float>* recs, const uint2* meta, const float* boxes,
+                         uint32_t count, const uint32_t* leaf_of, PrimRec<float>* prims, uint2* meta_out,
+                         float* leaf_box) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t k = leaf_of[index[i]];
+        prims[k] = recs[i];
+        meta_out[k] = meta[i];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) leaf_box[size_t(k) * 6 + a] = boxes[size_t(i) * 6 + a];
+    }
+}
+
 } // namespace
 
 gt_status build_lbvh_f32(GpuScene<float>& g, uint32_t n, const float* boxes_host, const double* bounds_lo,
@@ -156,15 +175,23 @@ gt_status build_lbvh_f32(GpuScene<float>& g, uint32_t n, const float* boxes_host
     cudaError_t e = cudaSuccess;
     const uint32_t ni = n > 1 ? n - 1 : 1;
     if (e == cudaSuccess) e = dmalloc(reinterpret_cast<void**>(&d_boxes), size_t(n) * 6 * sizeof(float));
-    if (e == cudaSuccess) e = dmalloc(reinterpret_cast<void**>(&d_sorted_boxes), size_t(n) * 6 * sizeof(float));
-    if (e == cudaSuccess) e = dmalloc(reinterpret_cast<void**>(&d_int_box), size_t(ni) * 6 * sizeof(float));
+    // The tree's links and boxes stay with the scene for refits (freed with it).
+    auto keep = [&](void** p, size_t bytes) -> cudaError_t { return cudaMalloc(p, std::max<size_t>(bytes, 1)); };
+    if (e == cudaSuccess) e = keep(reinterpret_cast<void**>(&g.leaf_box), size_t(n) * 6 * sizeof(float));
+    if (e == cudaSuccess) e = keep(reinterpret_cast<void**>(&g.int_box), size_t(ni) * 6 * sizeof(float));
+    if (e == cudaSuccess) e = keep(reinterpret_cast<void**>(&g.arrivals), size_t(ni) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = keep(reinterpret_cast<void**>(&g.parent_leaf), size_t(n) * sizeof(int32_t));
+    if (e == cudaSuccess) e = keep(reinterpret_cast<void**>(&g.parent_int), size_t(ni) * sizeof(int32_t));
+    if (e == cudaSuccess) e = keep(reinterpret_cast<void**>(&g.leaf_of), size_t(n) * sizeof(uint32_t));
+    d_sorted_boxes = g.leaf_box;
+    d_int_box = g.int_box;
+    d_arrivals = g.arrivals;
+    d_parent_leaf = g.parent_leaf;
+    d_parent_int = g.parent_int;
     if (e == cudaSuccess) e = dmalloc(reinterpret_cast<void**>(&d_codes), size_t(n) * sizeof(uint32_t));
     if (e == cudaSuccess) e = dmalloc(reinterpret_cast<void**>(&d_codes_sorted), size_t(n) * sizeof(uint32_t));
     if (e == cudaSuccess) e = dmalloc(reinterpret_cast<void**>(&d_index), size_t(n) * sizeof(uint32_t));
     if (e == cudaSuccess) e = dmalloc(reinterpret_cast<void**>(&d_order), size_t(n) * sizeof(uint32_t));
-    if (e == cudaSuccess) e = dmalloc(reinterpret_cast<void**>(&d_arrivals), size_t(ni) * sizeof(uint32_t));
-    if (e == cudaSuccess) e = dmalloc(reinterpret_cast<void**>(&d_parent_leaf), size_t(n) * sizeof(int32_t));
-    if (e == cudaSuccess) e = dmalloc(reinterpret_cast<void**>(&d_parent_int), size_t(ni) * sizeof(int32_t));
     if (e == cudaSuccess) e = dmalloc(reinterpret_cast<void**>(&d_prims), size_t(n) * sizeof(PrimRec<float>));
     if (e == cudaSuccess) e = dmalloc(reinterpret_cast<void**>(&d_meta), size_t(n) * sizeof(uint2));
     if (e == cudaSuccess)
@@ -191,6 +218,7 @@ gt_status build_lbvh_f32(GpuScene<float>& g, uint32_t n, const float* boxes_host
                                             30, st);
     if (e == cudaSuccess) {
         k_permute<<<blocks, threads, 0, st>>>(g.prims, g.meta, d_boxes, d_order, n, d_prims, d_meta, d_sorted_boxes);
+        k_invert<<<blocks, threads, 0, st>>>(d_order, n, g.leaf_of);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)
@@ -224,6 +252,62 @@ gt_status build_lbvh_f32(GpuScene<float>& g, uint32_t n, const float* boxes_host
     v.root_count = 0;
     v.nodes = g.nodes;
     v.num_nodes = ni;
+    return GT_OK;
+}
+
+} // namespace gt
+
+namespace gt {
+
+// Refit after gt_scene_update_primitives: the updated primitives go to their leaf positions
+// and every internal box is recomputed bottom-up along the kept links (the topology, and so
+// the leaf order, stays that of the build).
+gt_status refit_lbvh_f32(GpuScene<float>& g, uint32_t n, uint32_t count, const uint32_t* index,
+                         const PrimRec<float>* recs, const uint2* meta, const float* boxes, cudaStream_t st, int sms) {
+    if (count == 0 || n == 0) return GT_OK;
+    if (!g.leaf_of) return fail(GT_ERR_INTERNAL, "GPU BVH refit without its build links");
+    SceneDev<float>& v = g.view;
+    uint32_t* d_index = nullptr;
+    PrimRec<float>* d_recs = nullptr;
+    uint2* d_meta = nullptr;
+    float* d_boxes = nullptr;
+    cudaError_t e = cudaMalloc(&d_index, size_t(count) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&d_recs, size_t(count) * sizeof(PrimRec<float>));
+    if (e == cudaSuccess) e = cudaMalloc(&d_meta, size_t(count) * sizeof(uint2));
+    if (e == cudaSuccess) e = cudaMalloc(&d_boxes, size_t(count) * 6 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_index, index, size_t(count) * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_recs, recs, size_t(count) * sizeof(PrimRec<float>), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_meta, meta, size_t(count) * sizeof(uint2), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_boxes, boxes, size_t(count) * 6 * sizeof(float), cudaMemcpyHostToDevice, st);
+    const int threads = 256;
+    const int ublocks = int(std::max<uint64_t>(1, std::min<uint64_t>((count + threads - 1) / threads, uint64_t(sms) * 8)));
+    const int blocks = int(std::max<uint64_t>(1, std::min<uint64_t>((n + threads - 1) / threads, uint64_t(sms) * 8)));
+    if (e == cudaSuccess) {
+        k_update<<<ublocks, threads, 0, st>>>(d_index, d_recs, d_meta, d_boxes, count, g.leaf_of, g.prims, g.meta,
+                                              g.leaf_box);
+        e = cudaGetLastError();
+    }
+    float root[6] = {0, 0, 0, 0, 0, 0};
+    if (n == 1) {
+        if (e == cudaSuccess) e = cudaMemcpyAsync(root, g.leaf_box, sizeof(root), cudaMemcpyDeviceToHost, st);
+    } else {
+        if (e == cudaSuccess) e = cudaMemsetAsync(g.arrivals, 0, size_t(n - 1) * sizeof(uint32_t), st);
+        if (e == cudaSuccess) {
+            k_boxes<<<blocks, threads, 0, st>>>(g.leaf_box, int(n), g.parent_leaf, g.parent_int, g.arrivals, g.int_box,
+                                                g.nodes);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(root, g.int_box, sizeof(root), cudaMemcpyDeviceToHost, st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_index);
+    cudaFree(d_recs);
+    cudaFree(d_meta);
+    cudaFree(d_boxes);
+    if (e != cudaSuccess) return cuda_fail(e, "GPU BVH refit");
+    for (int a = 0; a < 6; ++a) v.root_box[a] = root[a];
     return GT_OK;
 }
 

@@ -71,6 +71,12 @@ template <class R> void free_gpu(gt_scene* s) {
     cudaFree(g.texels);
     cudaFree(g.images);
     cudaFree(g.media);
+    cudaFree(g.parent_leaf);
+    cudaFree(g.parent_int);
+    cudaFree(g.arrivals);
+    cudaFree(g.int_box);
+    cudaFree(g.leaf_box);
+    cudaFree(g.leaf_of);
     g = GpuScene<R>();
 }
 

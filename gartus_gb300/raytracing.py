@@ -586,6 +586,25 @@ class RayScene:
         self.add_quad(corner, u, v, mid)
         return mid
 
+    # -- animation
+    def update_primitives(self, first: int, primitives: np.ndarray) -> None:
+        """Replaces primitives [first, first + len) in place, keeping the scene's device
+        copies (gt_scene_update_primitives): the per-frame move of an animation's dynamic
+        geometry, which the reference rebuilds as the dynamic layer of a HittableLayers
+        split (scene.rs:227-351).  A scene using the GPU-built tree has it refitted on the
+        device; the reference tree is rebuilt on the host."""
+        arr = np.ascontiguousarray(primitives, dtype=PRIMITIVE_DTYPE)
+        prims = self.primitives_array()
+        first = int(first)
+        if first < 0 or first + len(arr) > len(prims):
+            raise ValueError("primitive range out of bounds")
+        if len(arr) and int(arr["material"].max()) >= len(self._materials):
+            raise ValueError("ray scene material id out of bounds")  # scene.rs:1158-1161
+        for h in list(self._handles.values()):
+            if h.h:
+                check(lib().gt_scene_update_primitives(h.h, first, len(arr), arr.ctypes.data_as(C.c_void_p)))
+        prims[first:first + len(arr)] = arr
+
     # -- participating media
     def add_constant_medium(self, boundary: MediumBoundary, density, albedo) -> int:
         """ConstantMedium::new(boundary, density, albedo) (volume/medium.rs:30-39): an

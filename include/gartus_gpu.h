@@ -396,6 +396,17 @@ void gt_context_destroy(gt_context* context);
 gt_status gt_scene_create(gt_context* context, const gt_scene_desc* desc, gt_scene** out);
 void gt_scene_destroy(gt_scene* scene);
 
+/* Replaces primitives [first, first + count) in place (same scene, same materials table):
+ * the per-frame update of an animation's moving geometry.  The reference rebuilds such a
+ * dynamic layer's BVH every frame (RayScene::build_bvh on the layer of a HittableLayers
+ * static + dynamic split, raytracing/scene.rs:227-351).  Here a scene created with
+ * GT_BVH_GPU_LBVH that is resident in f32 has its GPU-built tree refitted on the device
+ * (the updated records scattered to their leaves, every internal box recomputed bottom-up;
+ * the topology stays, so a refitted tree may be slower than a rebuilt one); the reference
+ * SAH tree, which the f64 path, the traversal statistics and GT_BVH_REFERENCE_SAH scenes
+ * use, is rebuilt on the host.  Waits for the context's stream first. */
+gt_status gt_scene_update_primitives(gt_scene* scene, uint32_t first, uint32_t count, const gt_primitive* primitives);
+
 /* RayScene::bvh_node_count (raytracing/scene.rs:1432-1437). */
 gt_status gt_scene_bvh_node_count(const gt_scene* scene, uint32_t* count);
 

@@ -15,7 +15,7 @@ import pytest
 
 import oracle
 from gartus_gb300 import abi, scenes
-from gartus_gb300._lib import GartusError, lib
+from gartus_gb300._lib import GartusError, check, lib
 from gartus_gb300.raytracing import (EnvironmentLight, ImageTexture, PathTracer, RayCamera, RayGeometry, RayMaterial,
                                      RayScene, SamplingTargetList)
 from tests.helpers import rel_err
@@ -825,3 +825,66 @@ def test_media_batch_and_unsupported(gpu_context, precision):
     with pytest.raises(GartusError) as e:
         PathTracer(cams[0], context=gpu_context).render_accumulate(scene, acc, 1, lights=lights)
     assert e.value.status == abi.GT_ERR_UNSUPPORTED
+
+
+def _bouncing_spheres(frame: int, n: int = 300):
+    """Frame `frame` of a small animation: n spheres on a floor, each moving on its own
+    seeded path (the dynamic layer), plus the floor (static)."""
+    rng = np.random.default_rng(17)
+    base = rng.uniform((-4, 0.2, -6), (4, 2.5, -1), size=(n, 3))
+    vel = rng.normal(size=(n, 3)) * 0.15
+    scene = RayScene()
+    floor = scene.add_material(RayMaterial.checker_lambertian(0.5, (0.2, 0.3, 0.1), (0.9, 0.9, 0.9)))
+    mats = [scene.add_material(RayMaterial.lambertian(tuple(rng.uniform(0.1, 0.9, 3)))) for _ in range(4)]
+    mats.append(scene.add_material(RayMaterial.metal((0.8, 0.8, 0.8), 0.05)))
+    light = scene.add_material(RayMaterial.diffuse_light((6.0, 6.0, 6.0)))
+    scene.add_quad((-10.0, 0.0, 2.0), (20.0, 0.0, 0.0), (0.0, 0.0, -14.0), floor)
+    scene.add_quad((-2.0, 6.0, -5.0), (4.0, 0.0, 0.0), (0.0, 0.0, 3.0), light)
+    for i in range(n):
+        c = base[i] + vel[i] * frame
+        c[1] = abs(c[1] - 0.2) + 0.2  # bounce off the floor
+        scene.add_sphere(tuple(c), 0.15 + 0.05 * (i % 3), mats[i % len(mats)])
+    scene.build_bvh()
+    return scene
+
+
+@pytest.mark.parametrize("builder", ["gpu", "reference"])
+def test_update_primitives_refit(gpu_context, builder):
+    # gt_scene_update_primitives moves the dynamic spheres in place between frames.  With
+    # the GPU-built tree the f32 path refits it on the device; the image then agrees with a
+    # scene built from scratch at that frame, and the f64 path (reference tree rebuilt on
+    # the host) with the oracle.
+    cam = RayCamera(48, 1.5).with_samples_per_pixel(4).with_max_depth(6).with_look_at((0.0, 2.0, 4.0), (0.0, 1.0, -3.0))
+    scene = _bouncing_spheres(0)
+    if builder == "gpu":
+        scene.use_gpu_bvh()
+    pt32 = PathTracer(cam, context=gpu_context)
+    pt64 = PathTracer(cam, precision="f64", context=gpu_context)
+    pt32.render_hdr_image(scene)  # both copies resident before the updates
+    pt64.render_hdr_image(scene, want64=True)
+    for frame in (1, 2, 5):
+        fresh = _bouncing_spheres(frame)
+        if builder == "gpu":
+            fresh.use_gpu_bvh()
+        moved = fresh.primitives_array()[2:]
+        scene.update_primitives(2, moved)
+        np.testing.assert_array_equal(scene.primitives_array(), fresh.primitives_array())
+        a = pt32.render_hdr_image(scene)
+        b = PathTracer(cam, context=gpu_context).render_hdr_image(fresh)
+        n = a.pixels.shape[0] * a.pixels.shape[1]
+        assert _divergent(a.pixels, b.pixels.astype(np.float64)) <= 0.01 * n
+        img64 = pt64.render_hdr_image(scene, want64=True)
+        ref, acc = _oracle_render(fresh, cam)
+        np.testing.assert_array_equal(img64.accepted, acc)
+        err = rel_err(img64.pixels64, ref, floor=1e-12).max(axis=2)
+        assert (err <= 1e-9).mean() >= 0.99
+        assert scene.bvh_node_count(gpu_context) == fresh.bvh_node_count(gpu_context)
+    with pytest.raises(ValueError):
+        scene.update_primitives(len(scene.primitives_array()), scene.primitives_array()[:1])
+    bad = scene.primitives_array()[:1].copy()
+    bad["material"] = 99
+    with pytest.raises(ValueError):
+        scene.update_primitives(0, bad)
+    with pytest.raises(GartusError):  # the library checks the range itself
+        check(lib().gt_scene_update_primitives(scene._handle(gpu_context).h, 10**6, 1,
+                                               scene.primitives_array()[:1].ctypes.data_as(C.c_void_p)))
