@@ -57,6 +57,7 @@ GT_MEDIUM_SPHERE = 0
 GT_MEDIUM_BOX = 1
 GT_MEDIUM_ROTATE_Y = 1
 GT_MEDIUM_TRANSLATE = 2
+GT_NORMAL_MAP_NEGATIVE_Y = 1
 # gt_noise_variant
 GT_NOISE_PLAIN = 0
 GT_NOISE_TURBULENCE = 1
@@ -99,6 +100,9 @@ class gt_material(C.Structure):
         ("color", C.c_double * 3),
         ("param", C.c_double),
         ("tex", C.c_double * 7),
+        ("normal_map", C.c_uint32),
+        ("normal_map_flags", C.c_uint32),
+        ("normal_map_strength", C.c_double),
     ]
 
 
@@ -127,6 +131,26 @@ class gt_medium(C.Structure):
     ]
 
 
+class gt_mesh(C.Structure):
+    _fields_ = [
+        ("num_primitives", C.c_uint32),
+        ("bvh_leaf_size", C.c_uint32),
+        ("primitives", C.c_void_p),
+        ("texcoords", C.c_void_p),
+        ("normals", C.c_void_p),
+        ("attribute_flags", C.c_void_p),
+    ]
+
+
+class gt_object(C.Structure):
+    _fields_ = [
+        ("mesh", C.c_uint32),
+        ("transformed", C.c_uint32),
+        ("transform", C.c_double * 16),
+        ("inverse", C.c_double * 16),
+    ]
+
+
 class gt_scene_desc(C.Structure):
     _fields_ = [
         ("struct_size", C.c_uint32),
@@ -139,8 +163,12 @@ class gt_scene_desc(C.Structure):
         ("num_images", C.c_uint32),
         ("images", C.POINTER(gt_image)),
         ("num_media", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("num_meshes", C.c_uint32),
         ("media", C.POINTER(gt_medium)),
+        ("meshes", C.POINTER(gt_mesh)),
+        ("num_objects", C.c_uint32),
+        ("reserved", C.c_uint32),
+        ("objects", C.POINTER(gt_object)),
     ]
 
 
@@ -310,7 +338,7 @@ class gt_denoise_input(C.Structure):
 
 
 STRUCTS = [
-    gt_geometry, gt_primitive, gt_material, gt_image, gt_medium, gt_scene_desc, gt_light_target, gt_environment_desc,
+    gt_geometry, gt_primitive, gt_material, gt_image, gt_medium, gt_mesh, gt_object, gt_scene_desc, gt_light_target, gt_environment_desc,
     gt_camera_desc, gt_render_opts, gt_frame, gt_frame_job, gt_bvh_stats, gt_render_stats, gt_denoise_input,
     gt_autotune_report,
 ]

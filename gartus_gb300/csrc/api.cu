@@ -306,6 +306,37 @@ gt_status gt_scene_create(gt_context* ctx, const gt_scene_desc* d, gt_scene** ou
             return fail(GT_ERR_INVALID_ARG, "refractive index must be positive and finite");
         if (m.kind == GT_MAT_HENYEY_GREENSTEIN && !(std::fabs(m.param) < 1.0)) // material.rs:1334-1343
             return fail(GT_ERR_INVALID_ARG, "Henyey-Greenstein anisotropy must be finite and in (-1, 1)");
+        if (m.normal_map) { // only Lambertian and GgxMicrofacet carry one (material.rs:456-460, 1505-1520)
+            if (m.normal_map > d->num_images || !(m.kind == GT_MAT_LAMBERTIAN || m.kind == GT_MAT_GGX) ||
+                !std::isfinite(m.normal_map_strength) || m.normal_map_flags > GT_NORMAL_MAP_NEGATIVE_Y)
+                return fail(GT_ERR_INVALID_ARG, "a normal map needs an image index, a Lambertian or GGX material, "
+                                                "a finite strength and flags 0-1");
+        }
+    }
+    if ((d->num_meshes && !d->meshes) || (d->num_objects && !d->objects))
+        return fail(GT_ERR_INVALID_ARG, "null mesh or object array");
+    for (uint32_t k = 0; k < d->num_meshes; ++k) {
+        const gt_mesh& mh = d->meshes[k];
+        if (mh.num_primitives && !mh.primitives) return fail(GT_ERR_INVALID_ARG, "null mesh primitives");
+        if (mh.num_primitives > (1u << 28)) return fail(GT_ERR_INVALID_ARG, "too many mesh primitives");
+        for (uint32_t i = 0; i < mh.num_primitives; ++i) {
+            gt_status rc = validate_geometry(mh.primitives[i].geometry);
+            if (rc != GT_OK) return rc;
+            if (mh.primitives[i].material >= d->num_materials)
+                return fail(GT_ERR_INVALID_ARG, "mesh material id out of bounds");
+        }
+        const size_t nuv = mh.texcoords ? size_t(mh.num_primitives) * 6 : 0, nvn = mh.normals ? size_t(mh.num_primitives) * 9 : 0;
+        for (size_t i = 0; i < nuv; ++i)
+            if (!std::isfinite(mh.texcoords[i])) return fail(GT_ERR_INVALID_ARG, "mesh texture coordinates must be finite");
+        for (size_t i = 0; i < nvn; ++i)
+            if (!std::isfinite(mh.normals[i])) return fail(GT_ERR_INVALID_ARG, "mesh vertex normals must be finite");
+    }
+    for (uint32_t k = 0; k < d->num_objects; ++k) {
+        const gt_object& o = d->objects[k];
+        if (o.mesh >= d->num_meshes || o.transformed > 1) return fail(GT_ERR_INVALID_ARG, "object needs a mesh index and transformed 0-1");
+        for (int a = 0; a < 16; ++a)
+            if (o.transformed && !(std::isfinite(o.transform[a]) && std::isfinite(o.inverse[a])))
+                return fail(GT_ERR_INVALID_ARG, "object matrices must be finite");
     }
     if (d->num_media && !d->media) return fail(GT_ERR_INVALID_ARG, "null media array");
     if (d->num_media > kMaxMedia) return fail(GT_ERR_INVALID_ARG, "at most 64 media per scene");
@@ -334,6 +365,27 @@ gt_status gt_scene_create(gt_context* ctx, const gt_scene_desc* d, gt_scene** ou
     s->mats.assign(d->materials, d->materials + d->num_materials);
     s->bvh_builder = builder;
     s->media.assign(d->media, d->media + d->num_media);
+    s->objects.assign(d->objects, d->objects + d->num_objects);
+    for (uint32_t k = 0; k < d->num_meshes; ++k) { // TriangleBvh::build (mesh.rs:645-652)
+        const gt_mesh& mh = d->meshes[k];
+        MeshHost m;
+        const size_t n = mh.num_primitives;
+        m.prims.assign(mh.primitives, mh.primitives + n);
+        if (mh.texcoords) m.uv.assign(mh.texcoords, mh.texcoords + n * 6);
+        if (mh.normals) m.vn.assign(mh.normals, mh.normals + n * 9);
+        m.attr.resize(n);
+        for (size_t i = 0; i < n; ++i) {
+            const uint8_t given = uint8_t((mh.texcoords ? 1 : 0) | (mh.normals ? 2 : 0));
+            m.attr[i] = mh.attribute_flags ? uint8_t(mh.attribute_flags[i] & given) : given;
+        }
+        m.leaf_size = mh.bvh_leaf_size ? mh.bvh_leaf_size : 4u;
+        build_reference_bvh(m.prims.data(), uint32_t(n), m.leaf_size, m.bvh);
+        if (m.bvh.max_depth + 1 > 62) {
+            delete s;
+            return fail(GT_ERR_UNSUPPORTED, "mesh BVH deeper than the device traversal stack");
+        }
+        s->meshes.push_back(std::move(m));
+    }
     for (uint32_t i = 0; i < d->num_images; ++i) {
         const gt_image& g = d->images[i];
         const uint64_t texels = uint64_t(g.width) * g.height;

@@ -189,19 +189,24 @@ Aabb geometry_aabb(const gt_geometry& g) {
 }
 
 void build_reference_bvh(const gt_primitive* prims, uint32_t count, uint32_t leaf_size, BuiltBvh& out) {
+    std::vector<Aabb> box(count);
+    for (uint32_t i = 0; i < count; ++i) box[i] = geometry_aabb(prims[i].geometry);
+    build_bvh_from_boxes(box.data(), count, leaf_size, out);
+}
+
+void build_bvh_from_boxes(const Aabb* boxes, uint32_t count, uint32_t leaf_size, BuiltBvh& out) {
     out.nodes.clear();
     out.order.resize(count);
     std::iota(out.order.begin(), out.order.end(), 0u);
     out.max_depth = 0;
     if (count == 0) return;
     if (leaf_size == 0) leaf_size = 1;
-    std::vector<Aabb> box(count);
+    std::vector<Aabb> box(boxes, boxes + count);
     Builder b{box, {}, {}, {}, out.order};
     b.cx.resize(count);
     b.cy.resize(count);
     b.cz.resize(count);
     for (uint32_t i = 0; i < count; ++i) {
-        box[i] = geometry_aabb(prims[i].geometry);
         b.cx[i] = 0.5 * (box[i].lo[0] + box[i].hi[0]); // Bounds3::centroid
         b.cy[i] = 0.5 * (box[i].lo[1] + box[i].hi[1]);
         b.cz[i] = 0.5 * (box[i].lo[2] + box[i].hi[2]);

@@ -36,4 +36,7 @@ Aabb geometry_aabb(const gt_geometry& g);
 // midpoint split whenever the buckets cannot separate the primitives.
 void build_reference_bvh(const gt_primitive* prims, uint32_t count, uint32_t leaf_size, BuiltBvh& out);
 
+// The same build over given boxes (a mesh's triangles, or world objects).
+void build_bvh_from_boxes(const Aabb* boxes, uint32_t count, uint32_t leaf_size, BuiltBvh& out);
+
 } // namespace gt

@@ -18,6 +18,15 @@ namespace gt {
 // Media per scene: each ray tests all of them in order.
 constexpr uint32_t kMaxMedia = 64;
 
+// A mesh copied from gt_mesh, with its tree (built at scene creation).
+struct MeshHost {
+    std::vector<gt_primitive> prims;
+    std::vector<double> uv, vn;  // 6 / 9 per primitive, or empty
+    std::vector<uint8_t> attr;   // presence bits per primitive
+    uint32_t leaf_size = 4;
+    BuiltBvh bvh;
+};
+
 // A scene's bitmap texture, copied from gt_image.
 struct ImageHost {
     uint32_t w = 0, h = 0, filter = 0, wrap_s = 0, wrap_t = 0;
@@ -29,6 +38,10 @@ template <class R> struct GpuScene {
     uint8_t* texels = nullptr;     // every image's texels, back to back
     ImageDev* images = nullptr;
     MediumDev<R>* media = nullptr;
+    MeshDev<R>* meshes = nullptr;
+    ObjectDev<R>* objects = nullptr;
+    Node<R>* tlas = nullptr;
+    std::vector<void*> mesh_allocs; // every mesh's device arrays
     // GT_BVH_GPU_LBVH (f32 only): the tree's bottom-up links and leaf boxes, kept so that
     // gt_scene_update_primitives can refit it in place.
     int32_t* parent_leaf = nullptr;
@@ -134,6 +147,8 @@ struct gt_scene {
     std::vector<gt_material> mats;
     std::vector<gt::ImageHost> images;
     std::vector<gt_medium> media;
+    std::vector<gt::MeshHost> meshes;
+    std::vector<gt_object> objects;
     uint32_t bvh_builder = GT_BVH_REFERENCE_SAH;
     uint32_t leaf_size = 4;
     bool bvh_ready = false; // `bvh` has been built (eagerly for the reference builder)

@@ -67,6 +67,9 @@ template <class R> struct MatDev {
     int32_t noise_depth;
     const PerlinDev<R>* noise; // this material's tables (GT_TEX_NOISE)
     const ImageDev* image;     // this material's bitmap (GT_TEX_IMAGE)
+    const ImageDev* normal_map; // tangent-space normal map, or null
+    R normal_strength;
+    int32_t normal_neg_y;       // 1 = -Y green channel
 };
 
 // Weighted sampling target (raytracing/scene.rs:423-497) with the geometry's derived
@@ -136,6 +139,23 @@ template <class R> struct MediumDev {
     uint32_t kind[6];
 };
 
+template <class R> struct SceneDev;
+
+// One mesh (TriangleMesh, raytracing/mesh.rs) in object space: a scene view of its own
+// primitives and BVH (sharing the scene's material table) and its per-primitive texture
+// coordinates (6) and vertex normals (9) in its leaf order, with presence bits
+// (bit 0 texture coordinates, bit 1 normals).
+template <class R> struct MeshDev;
+
+// A world object: a mesh, or MatrixInstance(mesh) with its object-to-world and
+// world-to-object matrices (row-major 4x4; the normal transform is the inverse transposed).
+template <class R> struct ObjectDev {
+    uint32_t mesh;
+    uint32_t transformed;
+    R xf[16];
+    R inv[16];
+};
+
 // Scene view handed to kernels.
 template <class R> struct SceneDev {
     const PrimRec<R>* prims;
@@ -144,11 +164,25 @@ template <class R> struct SceneDev {
     const MatDev<R>* mats;
     const MediumDev<R>* media; // tested after the surfaces, in order
     uint32_t num_media;
+    uint32_t num_objects;       // world objects, tested after the RayScene's surfaces
+    const MeshDev<R>* meshes;
+    const ObjectDev<R>* objects;
+    const Node<R>* tlas;        // BVH over the objects' world boxes (leaves index objects)
+    R tlas_box[6];
+    int32_t tlas_link;
+    int32_t tlas_count;
     R root_box[6];
     int32_t root_link; // >= 0 internal root node, < 0 ~first of a leaf root
     int32_t root_count;
     uint32_t num_prims;
     uint32_t num_nodes;
+};
+
+template <class R> struct MeshDev {
+    SceneDev<R> view;
+    const R* uv;
+    const R* vn;
+    const uint8_t* attr;
 };
 
 template <class R> struct LightsDev {

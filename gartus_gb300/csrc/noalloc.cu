@@ -100,12 +100,12 @@ extern "C" gt_status gt_render_noalloc(gt_scene* scene, const gt_lights* lights,
         const uint32_t cblocks = std::max<uint32_t>(1u, std::min<uint32_t>((n + 255) / 256, sms * 8));
         k_classify<float><<<cblocks, 256, 0, st>>>(P, queues, P.ps.counters + C_MAT);
         int per_sm = 0;
-        const bool media = P.sc.num_media != 0;
+        const bool world = P.sc.num_media != 0 || P.sc.num_objects != 0;
         ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, media ? k_persistent<float, false, false, true> : k_persistent<float, false>, 128, 0);
+            &per_sm, world ? k_persistent<float, false, false, true> : k_persistent<float, false>, 128, 0);
         if (ce != cudaSuccess) return cuda_fail(ce, "occupancy query");
         const uint32_t blocks = std::max<uint32_t>(1u, std::min<uint32_t>(sms * uint32_t(std::max(per_sm, 1)), (n + 127) / 128));
-        if (media)
+        if (world)
             k_persistent<float, false, false, true><<<blocks, 128, 0, st>>>(P, next, queues, P.ps.counters + C_MAT, nullptr,
                                                                            nullptr, rgb, nullptr, accepted);
         else

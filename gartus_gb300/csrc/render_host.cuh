@@ -71,6 +71,10 @@ template <class R> void free_gpu(gt_scene* s) {
     cudaFree(g.texels);
     cudaFree(g.images);
     cudaFree(g.media);
+    cudaFree(g.meshes);
+    cudaFree(g.objects);
+    cudaFree(g.tlas);
+    for (void* p : g.mesh_allocs) cudaFree(p);
     cudaFree(g.parent_leaf);
     cudaFree(g.parent_int);
     cudaFree(g.arrivals);
@@ -175,6 +179,170 @@ inline uint32_t medium_parts(const gt_medium& m, gt_geometry* out) {
     return 6;
 }
 
+// A reference-layout tree as device nodes: internal nodes renumbered densely in pre-order,
+// leaf children as links (~first, count); also the root's box and link (a root box no ray
+// enters for an empty tree).
+template <class R>
+void flatten_tree(const BuiltBvh& bvh, std::vector<Node<R>>& nodes, R* root_box, int32_t& root_link,
+                  int32_t& root_count) {
+    std::vector<int32_t> internal_id(bvh.nodes.size(), -1);
+    int32_t ni = 0;
+    for (size_t i = 0; i < bvh.nodes.size(); ++i)
+        if (!bvh.nodes[i].leaf) internal_id[i] = ni++;
+    nodes.assign(size_t(ni), Node<R>());
+    auto link_of = [&](uint32_t child, int32_t& link, int32_t& count) {
+        const BuildNode& c = bvh.nodes[child];
+        link = c.leaf ? ~int32_t(c.first) : internal_id[child];
+        count = c.leaf ? int32_t(c.count) : 0;
+    };
+    for (size_t i = 0; i < bvh.nodes.size(); ++i) {
+        const BuildNode& b = bvh.nodes[i];
+        if (b.leaf) continue;
+        Node<R>& nd = nodes[size_t(internal_id[i])];
+        put_box<R>(nd.box, bvh.nodes[b.left].box);
+        put_box<R>(nd.box + 6, bvh.nodes[b.right].box);
+        link_of(b.left, nd.link[0], nd.link[1]);
+        link_of(b.right, nd.link[2], nd.link[3]);
+    }
+    if (bvh.nodes.empty()) {
+        for (int k = 0; k < 3; ++k) {
+            root_box[k] = R(1);
+            root_box[3 + k] = R(-1);
+        }
+        root_link = ~0;
+        root_count = 0;
+    } else {
+        put_box<R>(root_box, bvh.nodes[0].box);
+        link_of(0, root_link, root_count);
+    }
+}
+
+// transform_point (raytracing/instance.rs:355-364): the homogeneous product, divided by w
+// when |w| > EPSILON.
+inline void xf_point_host(const double* m, const double* p, double* out) {
+    double r[4];
+    for (int i = 0; i < 4; ++i) r[i] = m[4 * i] * p[0] + m[4 * i + 1] * p[1] + m[4 * i + 2] * p[2] + m[4 * i + 3] * 1.0;
+    const bool div = std::fabs(r[3]) > 2.220446049250313e-16;
+    for (int i = 0; i < 3; ++i) out[i] = div ? r[i] / r[3] : r[i];
+}
+
+// Meshes (their primitives in their own tree's leaf order, attributes alongside) and world
+// objects (in the leaf order of a tree over their world boxes: the mesh's box, through
+// the instance transform's eight corners as transform_bounds does, instance.rs:319-335).
+template <class R> gt_status upload_meshes(gt_scene* s, GpuScene<R>& g, cudaStream_t st) {
+    SceneDev<R>& v = g.view;
+    v.num_objects = 0;
+    if (s->objects.empty()) return GT_OK;
+    auto dput = [&](const void* src, size_t bytes, void** dst) -> gt_status {
+        *dst = nullptr;
+        if (bytes == 0) return GT_OK;
+        GT_CUDA(cudaMalloc(dst, bytes));
+        g.mesh_allocs.push_back(*dst);
+        GT_CUDA(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, st));
+        return GT_OK;
+    };
+    std::vector<MeshDev<R>> md(s->meshes.size());
+    // Host staging stays alive until the copies finish (synchronised below).
+    std::vector<std::vector<PrimRec<R>>> keep_rec(md.size());
+    std::vector<std::vector<uint2>> keep_meta(md.size());
+    std::vector<std::vector<Node<R>>> keep_nodes(md.size());
+    std::vector<std::vector<R>> keep_uv(md.size()), keep_vn(md.size());
+    std::vector<std::vector<uint8_t>> keep_attr(md.size());
+    gt_status rc;
+    for (size_t k = 0; k < md.size(); ++k) {
+        const MeshHost& mh = s->meshes[k];
+        const size_t mn = mh.prims.size();
+        auto& rec = keep_rec[k];
+        auto& meta = keep_meta[k];
+        auto& uv = keep_uv[k];
+        auto& vn = keep_vn[k];
+        auto& attr = keep_attr[k];
+        rec.resize(mn);
+        meta.resize(mn);
+        attr.resize(mn);
+        if (!mh.uv.empty()) uv.resize(mn * 6);
+        if (!mh.vn.empty()) vn.resize(mn * 9);
+        for (size_t j = 0; j < mn; ++j) {
+            const uint32_t pi = mh.bvh.order[j];
+            const gt_primitive& p = mh.prims[pi];
+            const uint32_t kind = pack_prim<R>(p.geometry, rec[j].v);
+            if (kind == kBadKind) return fail(GT_ERR_INVALID_ARG, "unknown geometry kind");
+            meta[j] = make_uint2(kind | (p.material << 3), pi);
+            attr[j] = mh.attr[pi];
+            for (int a = 0; a < 6 && !uv.empty(); ++a) uv[j * 6 + a] = R(mh.uv[size_t(pi) * 6 + a]);
+            for (int a = 0; a < 9 && !vn.empty(); ++a) vn[j * 9 + a] = R(mh.vn[size_t(pi) * 9 + a]);
+        }
+        SceneDev<R> mv;
+        std::memset(&mv, 0, sizeof(mv));
+        flatten_tree<R>(mh.bvh, keep_nodes[k], mv.root_box, mv.root_link, mv.root_count);
+        void *dp, *dm, *dn, *du, *dv, *da;
+        if ((rc = dput(rec.data(), mn * sizeof(PrimRec<R>), &dp)) != GT_OK) return rc;
+        if ((rc = dput(meta.data(), mn * sizeof(uint2), &dm)) != GT_OK) return rc;
+        if ((rc = dput(keep_nodes[k].data(), keep_nodes[k].size() * sizeof(Node<R>), &dn)) != GT_OK) return rc;
+        if ((rc = dput(uv.data(), uv.size() * sizeof(R), &du)) != GT_OK) return rc;
+        if ((rc = dput(vn.data(), vn.size() * sizeof(R), &dv)) != GT_OK) return rc;
+        if ((rc = dput(attr.data(), attr.size(), &da)) != GT_OK) return rc;
+        mv.prims = static_cast<const PrimRec<R>*>(dp);
+        mv.meta = static_cast<const uint2*>(dm);
+        mv.nodes = static_cast<const Node<R>*>(dn);
+        mv.mats = g.mats;
+        mv.num_prims = uint32_t(mn);
+        mv.num_nodes = uint32_t(keep_nodes[k].size());
+        md[k] = MeshDev<R>{mv, static_cast<const R*>(du), static_cast<const R*>(dv), static_cast<const uint8_t*>(da)};
+    }
+    const size_t no = s->objects.size();
+    std::vector<Aabb> boxes(no);
+    for (size_t k = 0; k < no; ++k) {
+        const gt_object& o = s->objects[k];
+        const BuiltBvh& mb = s->meshes[o.mesh].bvh;
+        Aabb b = mb.nodes.empty() ? Aabb{{0, 0, 0}, {0, 0, 0}} : mb.nodes[0].box;
+        if (o.transformed && !mb.nodes.empty()) {
+            Aabb t{{1e300, 1e300, 1e300}, {-1e300, -1e300, -1e300}};
+            for (int c = 0; c < 8; ++c) {
+                const double p[3] = {(c & 1) ? b.hi[0] : b.lo[0], (c & 2) ? b.hi[1] : b.lo[1], (c & 4) ? b.hi[2] : b.lo[2]};
+                double q[3];
+                xf_point_host(o.transform, p, q);
+                for (int a = 0; a < 3; ++a) {
+                    t.lo[a] = std::fmin(t.lo[a], q[a]);
+                    t.hi[a] = std::fmax(t.hi[a], q[a]);
+                }
+            }
+            b = t;
+        }
+        boxes[k] = b;
+    }
+    BuiltBvh tl;
+    build_bvh_from_boxes(boxes.data(), uint32_t(no), 2, tl);
+    if (tl.max_depth + 1 > 30) return fail(GT_ERR_UNSUPPORTED, "object tree deeper than the device traversal stack");
+    std::vector<ObjectDev<R>> od(no);
+    for (size_t j = 0; j < no; ++j) {
+        const gt_object& o = s->objects[tl.order[j]];
+        std::memset(&od[j], 0, sizeof(od[j]));
+        od[j].mesh = o.mesh;
+        od[j].transformed = o.transformed;
+        for (int a = 0; a < 16; ++a) {
+            od[j].xf[a] = R(o.transform[a]);
+            od[j].inv[a] = R(o.inverse[a]);
+        }
+    }
+    std::vector<Node<R>> tnodes;
+    flatten_tree<R>(tl, tnodes, v.tlas_box, v.tlas_link, v.tlas_count);
+    GT_CUDA(cudaMalloc(&g.meshes, std::max<size_t>(md.size(), 1) * sizeof(MeshDev<R>)));
+    GT_CUDA(cudaMalloc(&g.objects, no * sizeof(ObjectDev<R>)));
+    GT_CUDA(cudaMalloc(&g.tlas, std::max<size_t>(tnodes.size(), 1) * sizeof(Node<R>)));
+    if (!md.empty())
+        GT_CUDA(cudaMemcpyAsync(g.meshes, md.data(), md.size() * sizeof(MeshDev<R>), cudaMemcpyHostToDevice, st));
+    GT_CUDA(cudaMemcpyAsync(g.objects, od.data(), no * sizeof(ObjectDev<R>), cudaMemcpyHostToDevice, st));
+    if (!tnodes.empty())
+        GT_CUDA(cudaMemcpyAsync(g.tlas, tnodes.data(), tnodes.size() * sizeof(Node<R>), cudaMemcpyHostToDevice, st));
+    GT_CUDA(cudaStreamSynchronize(st));
+    v.meshes = g.meshes;
+    v.objects = g.objects;
+    v.tlas = g.tlas;
+    v.num_objects = uint32_t(no);
+    return GT_OK;
+}
+
 // Flattens the primitives into leaf order with derived quantities computed in f64
 // (QuadGeometry::new, geometry.rs:271-301; TriangleGeometry::geometric_normal 171-179).
 template <class R> gt_status upload_scene(gt_scene* s) {
@@ -216,31 +384,10 @@ template <class R> gt_status upload_scene(gt_scene* s) {
         meta[j] = make_uint2(kind | (p.material << 3), pi);
     }
     // Internal nodes, renumbered densely in pre-order; leaf children become links.
-    const size_t ref_nodes = gpu_bvh ? 0 : bvh.nodes.size();
-    std::vector<int32_t> internal_id(ref_nodes, -1);
-    int32_t ni = 0;
-    for (size_t i = 0; i < ref_nodes; ++i)
-        if (!bvh.nodes[i].leaf) internal_id[i] = ni++;
-    std::vector<Node<R>> nodes(static_cast<size_t>(ni));
-    auto link_of = [&](uint32_t child, int32_t& link, int32_t& count) {
-        const BuildNode& c = bvh.nodes[child];
-        if (c.leaf) {
-            link = ~int32_t(c.first);
-            count = int32_t(c.count);
-        } else {
-            link = internal_id[child];
-            count = 0;
-        }
-    };
-    for (size_t i = 0; i < ref_nodes; ++i) {
-        const BuildNode& b = bvh.nodes[i];
-        if (b.leaf) continue;
-        Node<R>& nd = nodes[size_t(internal_id[i])];
-        put_box<R>(nd.box, bvh.nodes[b.left].box);
-        put_box<R>(nd.box + 6, bvh.nodes[b.right].box);
-        link_of(b.left, nd.link[0], nd.link[1]);
-        link_of(b.right, nd.link[2], nd.link[3]);
-    }
+    std::vector<Node<R>> nodes;
+    R root_box[6];
+    int32_t root_link = ~0, root_count = 0;
+    if (!gpu_bvh) flatten_tree<R>(bvh, nodes, root_box, root_link, root_count);
     std::vector<MatDev<R>> mats(s->mats.size());
     std::vector<PerlinDev<R>> perlin;
     std::vector<size_t> perlin_of; // material index of each table set
@@ -294,8 +441,15 @@ template <class R> gt_status upload_scene(gt_scene* s) {
             idev[k] = ImageDev{g.texels + off, im.w, im.h, im.filter, im.wrap_s, im.wrap_t, 0u};
             off += im.rgb.size();
         }
-        for (size_t i = 0; i < s->mats.size(); ++i)
-            if (s->mats[i].texture_kind == GT_TEX_IMAGE) mats[i].image = g.images + size_t(s->mats[i].tex[0]);
+        for (size_t i = 0; i < s->mats.size(); ++i) {
+            const gt_material& m = s->mats[i];
+            if (m.texture_kind == GT_TEX_IMAGE) mats[i].image = g.images + size_t(m.tex[0]);
+            if (m.normal_map) { // NormalMap::with_strength clamps at 0 (raytracing/texture.rs:198-202)
+                mats[i].normal_map = g.images + size_t(m.normal_map - 1);
+                mats[i].normal_strength = R(std::fmax(m.normal_map_strength, 0.0));
+                mats[i].normal_neg_y = (m.normal_map_flags & GT_NORMAL_MAP_NEGATIVE_Y) ? 1 : 0;
+            }
+        }
     }
     // Media: boundary shapes in PrimRec layout, the RotateY sine and cosine of
     // degrees_to_radians (raytracing.rs:150-152) and -1/density (medium.rs:97-101), in f64.
@@ -360,8 +514,9 @@ template <class R> gt_status upload_scene(gt_scene* s) {
             if (rc != GT_OK) return rc;
         }
     } else if (!gpu_bvh && !bvh.nodes.empty()) {
-        put_box<R>(v.root_box, bvh.nodes[0].box);
-        link_of(0, v.root_link, v.root_count);
+        for (int a = 0; a < 6; ++a) v.root_box[a] = root_box[a];
+        v.root_link = root_link;
+        v.root_count = root_count;
     } else { // an empty scene: a root box that no ray can enter
         for (int k = 0; k < 3; ++k) {
             v.root_box[k] = R(1);
@@ -370,6 +525,8 @@ template <class R> gt_status upload_scene(gt_scene* s) {
         v.root_link = ~0;
         v.root_count = 0;
     }
+    const gt_status mrc = upload_meshes<R>(s, g, st);
+    if (mrc != GT_OK) return mrc;
     g.ready = true;
     return GT_OK;
 }
@@ -659,16 +816,16 @@ gt_status run_persistent(gt_context* ctx, Params<R>& P, uint32_t* d_next, float*
     if (opts.progress && opts.progress_rgb && o_rgb) // unfinished pixels read as 0 in progress images
         GT_CUDA(cudaMemsetAsync(o_rgb, 0, size_t(n) * 3 * sizeof(float), st));
     int per_sm = 0;
-    const bool media = P.sc.num_media != 0;
+    const bool world = P.sc.num_media != 0 || P.sc.num_objects != 0;
     GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, media ? k_persistent<R, false, false, true> : k_persistent<R, false>, 128, 0));
+        &per_sm, world ? k_persistent<R, false, false, true> : k_persistent<R, false>, 128, 0));
     const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1);
     const uint32_t blocks = std::max<uint32_t>(1u, std::min<uint32_t>(sms * uint32_t(std::max(per_sm, 1)), (n + 127) / 128));
     const bool profile = opts.profile != 0;
     cudaEvent_t a = nullptr, z = nullptr;
     GT_CUDA(ev.pair(a, z));
     GT_CUDA(cudaEventRecord(a, st));
-    if (media)
+    if (world)
         k_persistent<R, false, false, true><<<blocks, 128, 0, st>>>(P, d_next, P.ps.q_mat, P.ps.counters + C_MAT,
                                                                    ctx->mapped_dev, ctx->mapped_dev + 1, o_rgb, o_rgb64,
                                                                    o_acc);
@@ -820,12 +977,13 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
 
     // Workspace: path state (wavefront only), per-stripe queues and counters, and device
     // staging for host outputs.
-    // A scene with media renders on the persistent schedule, whose MEDIA variant traces
-    // shadow queries in the reference's order of draws (accumulation resumes wavefront
-    // state, which that variant does not keep).
-    if (P.sc.num_media && (accum || BATCH))
-        return fail(GT_ERR_UNSUPPORTED, "a scene with media renders neither accumulated nor as a wavefront batch");
-    const bool persistent = (!BATCH && opts.schedule == GT_SCHEDULE_PERSISTENT && !accum) || P.sc.num_media != 0;
+    // A world with objects or media renders on the persistent schedule, whose WORLD variant
+    // traces shadow queries in the reference's order of draws (accumulation resumes
+    // wavefront state, which that variant does not keep).
+    const bool world = P.sc.num_media != 0 || P.sc.num_objects != 0;
+    if (world && (accum || BATCH))
+        return fail(GT_ERR_UNSUPPORTED, "a scene with objects or media renders neither accumulated nor as a wavefront batch");
+    const bool persistent = (!BATCH && opts.schedule == GT_SCHEDULE_PERSISTENT && !accum) || world;
     const bool host_out = BATCH || frame->device_buffers == 0;
     // Wavefront stripes: rows are dealt round-robin to K independent wavefronts on their
     // own streams, whose kernels then overlap on the GPU (each kernel alone leaves SMs
@@ -1360,15 +1518,15 @@ gt_status render_batch_impl(gt_scene* s, const gt_lights* l, gt_environment* e, 
     ctx->mapped[0] = 0;
     ctx->mapped[1] = 0;
     int per_sm = 0;
-    const bool media = P.sc.num_media != 0;
+    const bool world = P.sc.num_media != 0 || P.sc.num_objects != 0;
     GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, media ? k_persistent<R, false, true, true> : k_persistent<R, false, true>, 128, 0));
+        &per_sm, world ? k_persistent<R, false, true, true> : k_persistent<R, false, true>, 128, 0));
     const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1);
     const uint32_t blocks = std::max<uint32_t>(1u, std::min<uint32_t>(sms * uint32_t(std::max(per_sm, 1)), (n + 127) / 128));
     cudaEvent_t a = nullptr, z = nullptr;
     GT_CUDA(ev.pair(a, z));
     GT_CUDA(cudaEventRecord(a, st));
-    if (media)
+    if (world)
         k_persistent<R, false, true, true><<<blocks, 128, 0, st>>>(P, d_next, nullptr, nullptr, ctx->mapped_dev,
                                                                    ctx->mapped_dev + 1, d_rgb, d_rgb64, d_acc);
     else

@@ -268,6 +268,8 @@ GT_DEV int traverse(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, R t
 // ------------------------------------------------------------------ hit record
 template <class R> struct HitRec {
     V3<R> p, n; // n oriented against the ray (SurfaceHit::with_uv, object.rs:127-149)
+    V3<R> ns;   // shading normal (HitRecord::shading_normal): n except at mesh triangles with
+                // vertex normals or a normal map
     R u, v;     // texture coordinates, computed for image-textured materials only
     bool front;
     uint32_t mat;
@@ -293,6 +295,7 @@ template <class R> GT_DEV HitRec<R> make_hit(const SceneDev<R>& sc, uint32_t i, 
     }
     h.front = dot(d, out) < R(0);
     h.n = h.front ? out : -out;
+    h.ns = h.n;
     h.u = h.v = R(0);
     if (sc.mats[h.mat].tex == GT_TEX_IMAGE) {
         if (kind == K_SPHERE || kind == K_MOVING) { // sphere_uv, object.rs:1038-1042
@@ -388,15 +391,203 @@ template <class R> GT_DEV HitRec<R> make_medium_hit(const SceneDev<R>& sc, int p
     HitRec<R> h;
     h.p = o + d * t;
     h.n = V3<R>{R(1), R(0), R(0)};
+    h.ns = h.n;
     h.u = h.v = R(0);
     h.front = true;
     h.mat = sc.media[-2 - prim].mat;
     return h;
 }
 
-// The hit record of a surface (prim >= 0) or a medium (prim <= -2).
-template <class R> GT_DEV HitRec<R> hit_of(const SceneDev<R>& sc, int prim, V3<R> o, V3<R> d, R time, R t) {
-    return prim >= 0 ? make_hit(sc, uint32_t(prim), o, d, time, t) : make_medium_hit(sc, prim, o, d, t);
+// -------------------------------------------------------------- world objects
+// Matrix::transform_homogeneous_point with w = 1 (then transform_point's division by w when
+// |w| > EPSILON) and with w = 0 (transform_vector), instance.rs:355-369.
+template <class R> GT_DEV V3<R> xf_point(const R* m, V3<R> p) {
+    R r[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r[i] = m[4 * i] * p.x + m[4 * i + 1] * p.y + m[4 * i + 2] * p.z + m[4 * i + 3] * R(1);
+    if (Num<R>::fabs(r[3]) > R(kEps)) return V3<R>{r[0] / r[3], r[1] / r[3], r[2] / r[3]};
+    return V3<R>{r[0], r[1], r[2]};
+}
+template <class R> GT_DEV V3<R> xf_vector(const R* m, V3<R> v) {
+    R r[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) r[i] = m[4 * i] * v.x + m[4 * i + 1] * v.y + m[4 * i + 2] * v.z + m[4 * i + 3] * R(0);
+    return V3<R>{r[0], r[1], r[2]};
+}
+// transform_vector by the normal transform, the inverse's transpose: column i of `inv`.
+template <class R> GT_DEV V3<R> xf_normal(const R* inv, V3<R> v) {
+    R r[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) r[i] = inv[i] * v.x + inv[4 + i] * v.y + inv[8 + i] * v.z + inv[12 + i] * R(0);
+    return V3<R>{r[0], r[1], r[2]};
+}
+
+// The closest object hit in (tmin, t): the objects' tree, then each object's mesh tree in
+// object space (MatrixInstance::hit_with_rng transforms the ray by the inverse; the ray
+// parameter is unchanged, instance.rs:266-289).  On a closer hit sets t, obj (leaf-order
+// object index) and leaf (primitive in the mesh's leaf order).
+template <class R>
+GT_DEV bool objects_hit(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, R& t, int& obj, int& leaf,
+                        uint32_t* err) {
+    if (sc.num_objects == 0) return false;
+    bool any = false;
+    const RayT<R> rt = make_rayt(o, d);
+    struct Entry {
+        int32_t link, count;
+        R entry;
+    };
+    Entry stack[32];
+    int sp = 0;
+    R e0;
+    if (!hit_box(rt, sc.tlas_box, sc.tlas_box + 3, tmin, t, e0)) return false;
+    stack[sp++] = Entry{sc.tlas_link, sc.tlas_count, e0};
+    while (sp > 0) {
+        const Entry en = stack[--sp];
+        if (en.entry >= t) continue;
+        if (en.link < 0) { // a leaf: its objects
+            for (int32_t i = 0; i < en.count; ++i) {
+                const int k = ~en.link + i;
+                const ObjectDev<R>& ob = sc.objects[k];
+                const V3<R> oo = ob.transformed ? xf_point(ob.inv, o) : o;
+                const V3<R> od = ob.transformed ? xf_vector(ob.inv, d) : d;
+                R tt = t;
+                const int j = traverse<R, false, false>(sc.meshes[ob.mesh].view, oo, od, time, tmin, t, tt, nullptr, err);
+                if (j >= 0 && tt < t) {
+                    t = tt;
+                    obj = k;
+                    leaf = j;
+                    any = true;
+                }
+            }
+            continue;
+        }
+        const Node<R>& nd = sc.tlas[en.link];
+        R el, er;
+        const bool hl = hit_box(rt, nd.box, nd.box + 3, tmin, t, el);
+        const bool hr = hit_box(rt, nd.box + 6, nd.box + 9, tmin, t, er);
+        if (sp + 2 > 32) { // deeper than the host build allows; recorded, never expected
+            if (err) atomicOr(err, 1u);
+            break;
+        }
+        if (hl && hr) { // the nearer child on top
+            if (el <= er) {
+                stack[sp++] = Entry{nd.link[2], nd.link[3], er};
+                stack[sp++] = Entry{nd.link[0], nd.link[1], el};
+            } else {
+                stack[sp++] = Entry{nd.link[0], nd.link[1], el};
+                stack[sp++] = Entry{nd.link[2], nd.link[3], er};
+            }
+        } else if (hl) {
+            stack[sp++] = Entry{nd.link[0], nd.link[1], el};
+        } else if (hr) {
+            stack[sp++] = Entry{nd.link[2], nd.link[3], er};
+        }
+    }
+    return any;
+}
+
+// The hit record of mesh primitive `leaf` of leaf-order object `obj` at ray parameter t
+// (world ray o, d).  A mesh triangle (MeshTriangle::hit, mesh.rs:56-101): texture
+// coordinates interpolated from its vertices' (else the barycentrics), the shading normal
+// interpolated from its vertex normals (set_shading_normal, object.rs:469-479), and with
+// texture coordinates a tangent frame (mesh.rs:121-141, set_tangent_frame object.rs:495-517)
+// through which the material's normal map bends the shading normal (material.rs:1663-1684,
+// set_oriented_shading_normal object.rs:481-493).  Through a MatrixInstance the point and
+// the normal go back to world space and set_face_normal resets the shading normal to the
+// geometric one (instance.rs:277-288, object.rs:455-467); (u, v) are kept.
+template <class R>
+GT_DEV HitRec<R> make_mesh_hit(const SceneDev<R>& sc, int obj, int leaf, V3<R> o, V3<R> d, R time, R t) {
+    const ObjectDev<R>& ob = sc.objects[obj];
+    const MeshDev<R>& me = sc.meshes[ob.mesh];
+    const V3<R> oo = ob.transformed ? xf_point(ob.inv, o) : o;
+    const V3<R> od = ob.transformed ? xf_vector(ob.inv, d) : d;
+    HitRec<R> h = make_hit(me.view, uint32_t(leaf), oo, od, time, t);
+    const uint32_t kind = __ldg(&me.view.meta[leaf].x) & 7u;
+    const uint32_t attr = me.attr ? me.attr[leaf] : 0u;
+    if (kind == K_TRIANGLE && attr) {
+        const R* rec = me.view.prims[leaf].v;
+        const V3<R> p0 = xyz(ldg4(rec)), e1 = xyz(ldg4(rec + 4)), e2 = xyz(ldg4(rec + 8));
+        const V3<R> pvec = cross(od, e2);
+        const R inv_det = R(1) / dot(e1, pvec);
+        const V3<R> tvec = oo - p0;
+        const R bu = dot(tvec, pvec) * inv_det;
+        const R bv = dot(od, cross(tvec, e1)) * inv_det;
+        const R bw = R(1) - bu - bv;
+        const R* tc = me.uv + size_t(leaf) * 6;
+        if (attr & 1u) {
+            h.u = bw * tc[0] + bu * tc[2] + bv * tc[4];
+            h.v = bw * tc[1] + bu * tc[3] + bv * tc[5];
+        }
+        if (!ob.transformed) {
+            if (attr & 2u) {
+                const R* vn = me.vn + size_t(leaf) * 9;
+                const V3<R> sn = V3<R>{vn[0], vn[1], vn[2]} * bw + V3<R>{vn[3], vn[4], vn[5]} * bu +
+                                 V3<R>{vn[6], vn[7], vn[8]} * bv;
+                if (len2(sn) > R(kEps)) {
+                    const V3<R> u = normalize(sn);
+                    h.ns = h.front ? u : -u;
+                }
+            }
+            const MatDev<R>& m = me.view.mats[h.mat];
+            if ((attr & 1u) && m.normal_map) {
+                const R du1 = tc[2] - tc[0], dv1 = tc[3] - tc[1], du2 = tc[4] - tc[0], dv2 = tc[5] - tc[1];
+                const R det = du1 * dv2 - du2 * dv1;
+                if (Num<R>::fabs(det) > R(kEps)) {
+                    const R inv = R(1) / det;
+                    const V3<R> tg = (e1 * dv2 - e2 * dv1) * inv;
+                    const V3<R> bt = (e2 * du1 - e1 * du2) * inv;
+                    if (len2(tg) > R(kEps) && len2(bt) > R(kEps)) {
+                        const V3<R> n = h.ns; // set_tangent_frame around the shading normal
+                        V3<R> T = tg - n * dot(tg, n);
+                        if (len2(T) > R(kEps)) {
+                            T = normalize(T);
+                            const V3<R> ref = cross(n, T);
+                            V3<R> B = bt - n * dot(bt, n);
+                            B = B - T * dot(B, T);
+                            if (len2(B) <= R(kEps)) B = ref;
+                            const R hand = dot(B, ref) < R(0) ? R(-1) : R(1);
+                            B = normalize(ref * hand);
+                            const V3<R> tn = normal_map_sample(m.normal_map, m.normal_strength, m.normal_neg_y != 0, h.u, h.v);
+                            V3<R> nm = T * tn.x + B * tn.y + n * tn.z;
+                            if (len2(nm) > R(kEps)) {
+                                nm = normalize(nm);
+                                if (dot(nm, n) < R(0)) nm = -nm;
+                                if (len2(nm) > R(kEps)) h.ns = normalize(nm);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (ob.transformed) {
+        const V3<R> outward_obj = h.front ? h.n : -h.n;
+        h.p = xf_point(ob.xf, h.p);
+        const V3<R> outward = normalize(xf_normal(ob.inv, outward_obj));
+        h.front = dot(d, outward) < R(0);
+        h.n = h.front ? outward : -outward;
+        h.ns = h.n;
+    }
+    return h;
+}
+
+// HittableList::hit_with_rng over the whole world (scene.rs:177-197): the RayScene's
+// surfaces, then the objects, then the media in order (each clipped to the closest hit so
+// far; the media draw from g).  Fills h and returns true on a hit.
+template <class R>
+GT_DEV bool world_hit(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, Rng& g, HitRec<R>& h, uint32_t* err) {
+    const R inf = Num<R>::inf();
+    R t = inf;
+    int prim = traverse<R, false, false>(sc, o, d, time, tmin, inf, t, nullptr, err);
+    if (prim < 0) t = inf;
+    int obj = -1, leaf = -1;
+    objects_hit(sc, o, d, time, tmin, t, obj, leaf, err);
+    const int med = media_hit(sc, o, d, tmin, t, -1, g);
+    if (med <= -2) h = make_medium_hit(sc, med, o, d, t);
+    else if (obj >= 0) h = make_mesh_hit(sc, obj, leaf, o, d, time, t);
+    else if (prim >= 0) h = make_hit(sc, uint32_t(prim), o, d, time, t);
+    else return false;
+    return true;
 }
 
 // Origin of a ray that leaves the surface at h.  In f32 the hit point and the primitives'
@@ -494,36 +685,56 @@ template <class R> GT_DEV void texel_lerp(const uint8_t* a, const uint8_t* b, R 
         out[k] = uint8_t(v <= R(0) ? 0 : (v >= R(255) ? 255 : int(v)));
     }
 }
-template <class R> GT_DEV V3<R> image_color(const ImageDev* im, R u, R v) {
-    uint8_t c[3] = {0, 0, 0};
-    if (im == nullptr || im->w == 0 || im->h == 0) {
-        c[1] = c[2] = 255; // Rgb::CYAN
-    } else if (Num<R>::finite(u) && Num<R>::finite(v)) {
-        const uint8_t* px = im->rgb;
-        const uint32_t w = im->w, h = im->h;
-        if (im->filter == GT_FILTER_NEAREST) {
-            const R ws = im->wrap_s == GT_WRAP_REPEAT ? rem1(u) : clampr(u, R(0), R(1));
-            const R wt = im->wrap_t == GT_WRAP_REPEAT ? rem1(v) : clampr(v, R(0), R(1));
-            const uint32_t x = to_u32(Num<R>::round(ws * R(w - 1)));
-            const uint32_t y = to_u32(Num<R>::round((R(1) - wt) * R(h - 1)));
-            const uint8_t* t = px + (size_t(y) * w + x) * 3;
-            c[0] = t[0];
-            c[1] = t[1];
-            c[2] = t[2];
-        } else {
-            R x, y;
-            uint32_t x0, x1, y0, y1;
-            tex_axis(u, w, im->wrap_s, x, x0, x1);
-            tex_axis(R(1) - v, h, im->wrap_t, y, y0, y1);
-            const R tx = x - R(x0), ty = y - R(y0);
-            uint8_t top[3], bottom[3];
-            texel_lerp(px + (size_t(y0) * w + x0) * 3, px + (size_t(y0) * w + x1) * 3, tx, top);
-            texel_lerp(px + (size_t(y1) * w + x0) * 3, px + (size_t(y1) * w + x1) * 3, tx, bottom);
-            texel_lerp(top, bottom, ty, c);
-        }
+// Texture::sample (graphics/texture.rs:202-208, 696-752) of a non-empty bitmap: the 8-bit
+// texel (nearest) or the u8 lerps of four (linear); black at a non-finite (u, v).
+template <class R> GT_DEV void image_rgb8(const ImageDev* im, R u, R v, uint8_t* c) {
+    c[0] = c[1] = c[2] = 0;
+    if (!(Num<R>::finite(u) && Num<R>::finite(v))) return;
+    const uint8_t* px = im->rgb;
+    const uint32_t w = im->w, h = im->h;
+    if (im->filter == GT_FILTER_NEAREST) {
+        const R ws = im->wrap_s == GT_WRAP_REPEAT ? rem1(u) : clampr(u, R(0), R(1));
+        const R wt = im->wrap_t == GT_WRAP_REPEAT ? rem1(v) : clampr(v, R(0), R(1));
+        const uint32_t x = to_u32(Num<R>::round(ws * R(w - 1)));
+        const uint32_t y = to_u32(Num<R>::round((R(1) - wt) * R(h - 1)));
+        const uint8_t* t = px + (size_t(y) * w + x) * 3;
+        c[0] = t[0];
+        c[1] = t[1];
+        c[2] = t[2];
+    } else {
+        R x, y;
+        uint32_t x0, x1, y0, y1;
+        tex_axis(u, w, im->wrap_s, x, x0, x1);
+        tex_axis(R(1) - v, h, im->wrap_t, y, y0, y1);
+        const R tx = x - R(x0), ty = y - R(y0);
+        uint8_t top[3], bottom[3];
+        texel_lerp(px + (size_t(y0) * w + x0) * 3, px + (size_t(y0) * w + x1) * 3, tx, top);
+        texel_lerp(px + (size_t(y1) * w + x0) * 3, px + (size_t(y1) * w + x1) * 3, tx, bottom);
+        texel_lerp(top, bottom, ty, c);
     }
+}
+
+// ImageTexture::sample_linear (raytracing/texture.rs:148-155): cyan for an empty bitmap,
+// else the texel decoded as (c / 255)^2 (LinearRgb::from_rgb_srgb).
+template <class R> GT_DEV V3<R> image_color(const ImageDev* im, R u, R v) {
+    uint8_t c[3] = {0, 255, 255}; // Rgb::CYAN
+    if (im != nullptr && im->w != 0 && im->h != 0) image_rgb8(im, u, v, c);
     const R r = R(c[0]) / R(255), g = R(c[1]) / R(255), b = R(c[2]) / R(255);
     return V3<R>{r * r, g * g, b * b};
+}
+
+// NormalMap::sample_tangent_normal (raytracing/texture.rs:254-275): channels decoded as
+// 2 c / 255 - 1, x and y scaled by the strength, y negated for a -Y green channel, z
+// clamped at 0, normalised; +z for an empty bitmap or a near-zero result.
+template <class R> GT_DEV V3<R> normal_map_sample(const ImageDev* im, R strength, bool neg_y, R u, R v) {
+    const V3<R> up{R(0), R(0), R(1)};
+    if (im->w == 0 || im->h == 0) return up;
+    uint8_t c[3];
+    image_rgb8(im, u, v, c);
+    auto dec = [](uint8_t ch) { return R(2) * (R(ch) / R(255)) - R(1); };
+    const R green = neg_y ? -dec(c[1]) : dec(c[1]);
+    const V3<R> n{strength * dec(c[0]), strength * green, Num<R>::fmax(dec(c[2]), R(0))};
+    return len2(n) <= R(kEps) ? up : vdiv(n, Num<R>::sqrt(len2(n)));
 }
 
 template <class R> GT_DEV V3<R> mat_color(const MatDev<R>& m, const HitRec<R>& h) {
@@ -555,7 +766,7 @@ template <class R> GT_DEV ScatterRec<R> mat_scatter(const MatDev<R>& m, V3<R> di
     s.kind = SC_NONE;
     switch (m.kind) {
     case 0: // Lambertian, material.rs:508-521
-        if (!onb_from_w(h.n, s.pdf.basis)) return s;
+        if (!onb_from_w(h.ns, s.pdf.basis)) return s;
         s.kind = SC_PDF;
         s.pdf.kind = PDF_COSINE;
         s.att = mat_color(m, h);
@@ -574,7 +785,7 @@ template <class R> GT_DEV ScatterRec<R> mat_scatter(const MatDev<R>& m, V3<R> di
         return s;
     case 3: { // GgxMicrofacet, material.rs:1583-1597; GgxReflectionPdf::new sampling.rs:146-170
         V3<R> outgoing = -normalize(din);
-        if (!onb_from_w(h.n, s.pdf.basis)) return s;
+        if (!onb_from_w(h.ns, s.pdf.basis)) return s;
         s.pdf.out = normalize(outgoing);
         if (len2(s.pdf.out) <= R(kEps) || dot(s.pdf.out, s.pdf.basis.w) <= R(0)) return s;
         s.pdf.rough = clampr(m.param, R(0), R(1));
@@ -585,7 +796,7 @@ template <class R> GT_DEV ScatterRec<R> mat_scatter(const MatDev<R>& m, V3<R> di
         return s;
     }
     case 4: { // Metal, material.rs:2087-2106
-        V3<R> refl = reflect(normalize(din), h.n);
+        V3<R> refl = reflect(normalize(din), h.ns);
         V3<R> dir = refl + unit_vector_spherical<R>(g) * m.param;
         if (dot(dir, h.n) <= R(0)) return s;
         s.kind = SC_SPECULAR;
@@ -618,7 +829,7 @@ template <class R> GT_DEV ScatterRec<R> mat_scatter(const MatDev<R>& m, V3<R> di
 template <class R> GT_DEV R mat_scattering_pdf(const MatDev<R>& m, V3<R> din, const HitRec<R>& h, V3<R> dout) {
     switch (m.kind) {
     case 0: { // material.rs:523-530
-        R c = dot(h.n, normalize(dout));
+        R c = dot(h.ns, normalize(dout));
         return c <= R(0) ? R(0) : c / R(kPi);
     }
     case 2:
@@ -636,7 +847,7 @@ template <class R> GT_DEV R mat_scattering_pdf(const MatDev<R>& m, V3<R> din, co
         if (dot(incoming, h.n) <= R(0) || dot(outgoing, h.n) <= R(0)) return R(0);
         V3<R> sc = mat_color(m, h); // specular_luminance, material.rs:1760-1762
         R f0 = clampr(R(0.2126) * sc.x + R(0.7152) * sc.y + R(0.0722) * sc.z, R(0), R(1));
-        V3<R> n = normalize(h.n), o = normalize(outgoing), i = normalize(incoming);
+        V3<R> n = normalize(h.ns), o = normalize(outgoing), i = normalize(incoming);
         R ndi = dot(n, i), ndo = dot(n, o);
         if (ndi <= R(0) || ndo <= R(0)) return R(0);
         V3<R> half = normalize(i + o);

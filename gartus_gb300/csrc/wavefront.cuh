@@ -249,60 +249,60 @@ template <class R> struct Shadow {
 };
 
 // Resolves shadow query k (after traversal) into the sample's radiance.
-template <class R, bool MEDIA = false>
-GT_DEV void apply_shadow(const Params<R>& P, V3<R>& col, const Shadow<R>& sh, int k, int prim, R t) {
-    const bool miss = MEDIA ? prim == -1 : prim < 0;
+template <class R> GT_DEV void apply_shadow(const Params<R>& P, V3<R>& col, const Shadow<R>& sh, int k, int prim, R t) {
     if (k == 0) { // closest hit; the emission of whatever is hit (camera.rs:2248-2261)
-        if (miss) return;
-        HitRec<R> h = MEDIA ? hit_of(P.sc, prim, sh.o, sh.dir[0], sh.time, t)
-                            : make_hit(P.sc, uint32_t(prim), sh.o, sh.dir[0], sh.time, t);
+        if (prim < 0) return;
+        HitRec<R> h = make_hit(P.sc, uint32_t(prim), sh.o, sh.dir[0], sh.time, t);
         V3<R> e = mat_emitted(P.sc.mats[h.mat], h);
         if (!finite3(e)) return;
         V3<R> direct = cmul(sh.s[0], e) * sh.ratio[0];
         col = col + cmul(sh.att, direct);
     } else { // occlusion only (camera.rs:2284-2293)
-        if (!miss) return;
+        if (prim >= 0) return;
         V3<R> direct = sh.s[1] * sh.ratio[1];
         col = col + cmul(sh.att, direct);
     }
 }
 
-// A next-event shadow query of a scene with media, traced where the reference traces it
-// (inside estimate_direct_lighting / estimate_environment_lighting, camera.rs:2248, 2284):
-// the world's closest hit, surfaces then media, whose draws come before the next sample
-// of the bounce.  The environment query needs the closest surface too, since it clips
+// A next-event shadow query of a world with objects or media, traced where the reference
+// traces it (inside estimate_direct_lighting / estimate_environment_lighting,
+// camera.rs:2248, 2284): the world's closest hit, whose media draws come before the next
+// sample of the bounce.  The environment query needs the closest hit too, since it clips
 // the media's intervals.
 template <class R> GT_DEV void shadow_now(const Params<R>& P, V3<R>& col, Shadow<R>& sh, int k, Rng& g) {
-    const R inf = Num<R>::inf();
-    R t = inf;
-    int prim = traverse<R, false, false>(P.sc, sh.o, sh.dir[k], sh.time, R(kShadowAcne), inf, t, nullptr,
-                                         &P.ps.counters[C_ERROR], false);
-    if (prim < 0) t = inf;
-    prim = media_hit(P.sc, sh.o, sh.dir[k], R(kShadowAcne), t, prim, g);
-    apply_shadow<R, true>(P, col, sh, k, prim, t);
+    HitRec<R> h;
+    const bool hit = world_hit(P.sc, sh.o, sh.dir[k], sh.time, R(kShadowAcne), g, h, &P.ps.counters[C_ERROR]);
     sh.traced += 1;
+    if (k == 0) {
+        if (!hit) return;
+        const V3<R> e = mat_emitted(P.sc.mats[h.mat], h);
+        if (!finite3(e)) return;
+        col = col + cmul(sh.att, cmul(sh.s[0], e) * sh.ratio[0]);
+    } else if (!hit) {
+        col = col + cmul(sh.att, sh.s[1] * sh.ratio[1]);
+    }
 }
 
 // One iteration of the bounce loop of ray_color (camera.rs:1742-1859): miss radiance,
 // emission, scatter, next-event sampling (camera.rs:2225-2297), continuation sample
 // (camera.rs:165-195) and Russian roulette (camera.rs:2498-2523).  `prim` < 0 is a miss.
 // Returns true if the path continues to another bounce.
-// MEDIA: the scene has media; prim <= -2 is a medium hit and the shadow queries are traced
-// here, in the reference's order of draws, instead of being left in `sh`.
-template <class R, bool MEDIA = false>
+// WORLD: a world with objects or media; the hit record comes from world_hit (`wh`, prim 0
+// for a hit, -1 for a miss) and the shadow queries are traced here, in the reference's
+// order of draws, instead of being left in `sh`.
+template <class R, bool WORLD = false>
 GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& p, int prim, R t, Rng& g,
-                             Shadow<R>& sh) {
+                             Shadow<R>& sh, const HitRec<R>* wh = nullptr) {
     sh.valid[0] = sh.valid[1] = false;
     sh.traced = 0;
     bool cont = false;
-    if (MEDIA ? prim == -1 : prim < 0) {
+    if (prim < 0) {
         V3<R> bg = cam.use_env ? env_radiance(P.env, p.d) : background(cam, p.d);
         V3<R> miss = bg * p.miss_w;
         p.col = p.col + cmul(p.att, miss);
         return false;
     }
-    const HitRec<R> h =
-        MEDIA ? hit_of(P.sc, prim, p.o, p.d, p.time, t) : make_hit(P.sc, uint32_t(prim), p.o, p.d, p.time, t);
+    const HitRec<R> h = WORLD ? *wh : make_hit(P.sc, uint32_t(prim), p.o, p.d, p.time, t);
     const MatDev<R> m = P.sc.mats[h.mat];
     if (p.allow_emit) p.col = p.col + cmul(p.att, mat_emitted(m, h));
     ScatterRec<R> s = mat_scatter(m, p.d, h, g);
@@ -332,7 +332,7 @@ GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& 
                 }
             }
             const bool area = sh.valid[0];
-            if (MEDIA && area) {
+            if (WORLD && area) {
                 sh.o = spawn_origin(h, sh.dir[0]);
                 shadow_now(P, p.col, sh, 0, g);
                 sh.valid[0] = false;
@@ -352,7 +352,7 @@ GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& 
                     }
                 }
             }
-            if (MEDIA) {
+            if (WORLD) {
                 if (sh.valid[1]) {
                     if (!area) sh.o = spawn_origin(h, sh.dir[1]);
                     shadow_now(P, p.col, sh, 1, g);
@@ -643,9 +643,10 @@ struct HandOff {
     uint32_t coop = 0;         // 1 = one slot per warp (RESUME launches only)
 };
 
-// MEDIA: a scene with participating media; every ray's media draw from the pixel's stream
-// after its traversal, and shadow queries are traced inside integrate_bounce.
-template <class R, bool RESUME, bool BATCH = false, bool MEDIA = false>
+// WORLD: a world with objects or participating media: every ray goes through world_hit
+// (whose media draw from the pixel's stream), and shadow queries are traced inside
+// integrate_bounce.
+template <class R, bool RESUME, bool BATCH = false, bool WORLD = false>
 __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next, const uint32_t* queues,
                                                     const uint32_t* class_counts, const volatile uint32_t* cancel,
                                                     volatile uint32_t* progress, float* rgb, double* rgb64,
@@ -859,15 +860,16 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
         const int which = (pending & 1u) ? 0 : ((pending & 2u) ? 1 : -1);
         R t = R(0);
         int prim = -1;
+        HitRec<R> wrec;
         if (alive) {
             const V3<R> ro = which >= 0 ? sh.o : p.o;
             const V3<R> rd = which >= 0 ? sh.dir[which] : p.d;
             const R rt = which >= 0 ? sh.time : p.time;
-            prim = traverse<R, false, false>(P.sc, ro, rd, rt, R(kShadowAcne), inf, t, nullptr,
-                                             &P.ps.counters[C_ERROR], which == 1);
-            if constexpr (MEDIA) {
-                if (prim < 0) t = inf;
-                prim = media_hit(P.sc, ro, rd, R(kShadowAcne), t, prim, g);
+            if constexpr (WORLD) { // no query is ever pending here
+                prim = world_hit(P.sc, ro, rd, rt, R(kShadowAcne), g, wrec, &P.ps.counters[C_ERROR]) ? 0 : -1;
+            } else {
+                prim = traverse<R, false, false>(P.sc, ro, rd, rt, R(kShadowAcne), inf, t, nullptr,
+                                                 &P.ps.counters[C_ERROR], which == 1);
             }
         }
         __syncwarp();
@@ -878,9 +880,9 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
                 ++n_shadow;
             } else {
                 ++n_rays;
-                cont = integrate_bounce<R, MEDIA>(P, cam(), p, prim, t, g, sh);
+                cont = integrate_bounce<R, WORLD>(P, cam(), p, prim, t, g, sh, &wrec);
                 pending = (sh.valid[0] ? 1u : 0u) | (sh.valid[1] ? 2u : 0u);
-                if constexpr (MEDIA) n_shadow += sh.traced;
+                if constexpr (WORLD) n_shadow += sh.traced;
             }
             if (pending == 0 && !cont) need_sample = true;
         }
@@ -1034,18 +1036,17 @@ template <class R> __global__ void k_aov(Params<R> P, float* albedo, float* norm
             V3<R> o, d;
             R time, t;
             camera_ray(P.cam, x, y, k, g, o, d, time);
-            int prim = traverse<R, false, false>(P.sc, o, d, time, R(kShadowAcne), inf, t, nullptr,
-                                                 &P.ps.counters[C_ERROR]);
-            if (P.sc.num_media) { // the media draw from the same stream (camera.rs:3104-3106)
-                if (prim < 0) t = inf;
-                prim = media_hit(P.sc, o, d, R(kShadowAcne), t, prim, g);
-                if (prim == -1) continue;
-            } else if (prim < 0) {
-                continue; // black on a miss
+            HitRec<R> h;
+            if (P.sc.num_media || P.sc.num_objects) { // media draw from the same stream (camera.rs:3104-3106)
+                if (!world_hit(P.sc, o, d, time, R(kShadowAcne), g, h, &P.ps.counters[C_ERROR])) continue;
+            } else {
+                const int prim = traverse<R, false, false>(P.sc, o, d, time, R(kShadowAcne), inf, t, nullptr,
+                                                           &P.ps.counters[C_ERROR]);
+                if (prim < 0) continue; // black on a miss
+                h = make_hit(P.sc, uint32_t(prim), o, d, time, t);
             }
-            HitRec<R> h = hit_of(P.sc, prim, o, d, time, t);
             sa = sa + mat_albedo(P.sc.mats[h.mat], h);
-            sn = sn + (h.n + V3<R>{1, 1, 1}) * R(0.5);
+            sn = sn + (h.ns + V3<R>{1, 1, 1}) * R(0.5); // the shading normal (camera.rs:3112-3114)
         }
         sa = cdiv(sa, R(P.cam.spp));
         sn = cdiv(sn, R(P.cam.spp));

@@ -30,6 +30,7 @@ GEOMETRY_DTYPE = np.dtype([("kind", "<u4"), ("reserved", "<u4"), ("p", "<f8", (9
 PRIMITIVE_DTYPE = np.dtype([("geometry", GEOMETRY_DTYPE), ("material", "<u4"), ("reserved", "<u4")])
 MATERIAL_DTYPE = np.dtype([
     ("kind", "<u4"), ("texture_kind", "<u4"), ("color", "<f8", (3,)), ("param", "<f8"), ("tex", "<f8", (7,)),
+    ("normal_map", "<u4"), ("normal_map_flags", "<u4"), ("normal_map_strength", "<f8"),
 ])
 LIGHT_DTYPE = np.dtype([("geometry", GEOMETRY_DTYPE), ("weight", "<f8")])
 assert PRIMITIVE_DTYPE.itemsize == C.sizeof(abi.gt_primitive)
@@ -126,6 +127,156 @@ def _media_table(media: Sequence) -> "C.Array":
     return arr
 
 
+class NormalMap:
+    """NormalMap (raytracing/texture.rs:160-276): a tangent-space normal map over a bitmap
+    (sampled with its filter and wraps, channels decoded as 2 c / 255 - 1), strength 1 and
+    an OpenGL-style +Y green channel by default.  Attach with RayMaterial.with_normal_map."""
+
+    def __init__(self, texture: ImageTexture, strength: float = 1.0, flip_y: bool = False):
+        if not isinstance(texture, ImageTexture):
+            raise TypeError("a normal map samples an ImageTexture")
+        strength = float(strength)
+        if not math.isfinite(strength):
+            raise ValueError("normal-map strength must be finite")  # texture.rs:198-202
+        self.texture = texture
+        self.strength = max(strength, 0.0)
+        self.flip_y = bool(flip_y)
+
+
+def _lu_inverse(m) -> Optional[list]:
+    """Matrix::inverse (gmath/matrix.rs:171-178): Doolittle LU with partial pivoting
+    (lu_decomp, 285-338; a pivot below 1e-10 means singular) and forward / back substitution
+    of the identity's columns (solve_with_lu, 351-400).  Row-major 4x4 lists of floats."""
+    n = 4
+    L = [[1.0 if i == j else 0.0 for j in range(n)] for i in range(n)]
+    U = [list(map(float, row)) for row in m]
+    P = list(range(n))
+    for i in range(n):
+        max_row, max_val = i, abs(U[i][i])
+        for k in range(i + 1, n):
+            if abs(U[k][i]) > max_val:
+                max_val, max_row = abs(U[k][i]), k
+        if max_val < 1e-10:
+            return None
+        if max_row != i:
+            U[i], U[max_row] = U[max_row], U[i]
+            P[i], P[max_row] = P[max_row], P[i]
+            for k in range(i):
+                L[i][k], L[max_row][k] = L[max_row][k], L[i][k]
+        pivot = U[i][i]
+        for j in range(i + 1, n):
+            factor = U[j][i] / pivot
+            L[j][i] = factor
+            U[j][i] = 0.0
+            for k in range(i + 1, n):
+                U[j][k] = U[j][k] - factor * U[i][k]
+    inv = [[0.0] * n for _ in range(n)]
+    for col in range(n):
+        y = [0.0] * n
+        for i in range(n):
+            acc = 0.0
+            for j in range(i):
+                acc += L[i][j] * y[j]
+            y[i] = (1.0 if P[i] == col else 0.0) - acc
+        x = [0.0] * n
+        for i in reversed(range(n)):
+            acc = 0.0
+            for j in range(i + 1, n):
+                acc += U[i][j] * x[j]
+            x[i] = (y[i] - acc) / U[i][i]
+        for i in range(n):
+            inv[i][col] = x[i]
+    return inv
+
+
+class TriangleMesh:
+    """TriangleMesh (raytracing/mesh.rs:149-360): triangles (N, 3, 3) in object space with
+    one material, optional per-vertex texture coordinates (N, 3, 2) and vertex normals
+    (N, 3, 3) (MeshTriangle::with_texcoords / with_vertex_normals, mesh.rs:44-54), and its
+    own BVH (leaf size as BvhBuildOptions).  `present` (N,) optionally marks which triangles
+    carry those attributes (bit 0 texture coordinates, bit 1 normals)."""
+
+    def __init__(self, triangles, material: "RayMaterial", texcoords=None, normals=None, present=None,
+                 leaf_size: int = 4):
+        tri = np.asarray(triangles, dtype=np.float64)
+        if tri.ndim != 3 or tri.shape[1:] != (3, 3):
+            raise ValueError("triangles must be (N, 3, 3)")
+        geoms = np.zeros(len(tri), dtype=GEOMETRY_DTYPE)
+        geoms["kind"] = abi.GT_GEOM_TRIANGLE
+        geoms["p"] = tri.reshape(-1, 9)
+        self._init(geoms, material, texcoords, normals, present, leaf_size)
+
+    @classmethod
+    def from_geometry(cls, geometries: Sequence["RayGeometry"], material: "RayMaterial", leaf_size: int = 4):
+        """Any RayGeometry list as one object (spheres and quads too), for instancing."""
+        self = cls.__new__(cls)
+        geoms = np.zeros(len(geometries), dtype=GEOMETRY_DTYPE)
+        for i, g in enumerate(geometries):
+            geoms[i]["kind"] = g.kind
+            geoms[i]["p"] = g.p
+        self._init(geoms, material, None, None, None, leaf_size)
+        return self
+
+    def _init(self, geoms, material, texcoords, normals, present, leaf_size):
+        n = len(geoms)
+        self.geometry = geoms
+        self.material = material
+        self.texcoords = None if texcoords is None else np.ascontiguousarray(texcoords, dtype=np.float64).reshape(n, 6)
+        self.normals = None if normals is None else np.ascontiguousarray(normals, dtype=np.float64).reshape(n, 9)
+        self.present = None if present is None else np.ascontiguousarray(present, dtype=np.uint8).reshape(n)
+        for a in (self.texcoords, self.normals):
+            if a is not None and not np.isfinite(a).all():
+                raise ValueError("mesh attributes must be finite")
+        self.leaf_size = max(int(leaf_size), 1)
+
+    def __len__(self):
+        return len(self.geometry)
+
+
+class MatrixInstance:
+    """MatrixInstance::new(object, transform) (raytracing/instance.rs:225-254): a mesh placed
+    by a row-major 4x4 object-to-world matrix; its inverse is computed as Matrix::inverse
+    does.  Raises ValueError where the reference returns None (no 4x4 inverse)."""
+
+    def __init__(self, mesh: TriangleMesh, transform):
+        m = np.asarray(transform, dtype=np.float64)
+        if m.shape != (4, 4):
+            raise ValueError("an instance transform is a 4x4 matrix")
+        inv = _lu_inverse(m.tolist())
+        if inv is None:
+            raise ValueError("instance transform is not invertible")
+        self.mesh = mesh
+        self.transform = m.copy()
+        self.inverse = np.array(inv)
+
+
+def _mesh_tables(meshes: Sequence, objects: Sequence):
+    """gt_mesh / gt_object arrays from (primitives, texcoords, normals, present, leaf) entries
+    and (mesh index, transform or None, inverse) entries; the tuple ends with what must
+    stay alive while the description is used."""
+    marr = (abi.gt_mesh * max(len(meshes), 1))()
+    keep = []
+    for i, (prims, uv, vn, present, leaf) in enumerate(meshes):
+        prims = np.ascontiguousarray(prims)
+        keep += [prims, uv, vn, present]
+        marr[i].num_primitives = len(prims)
+        marr[i].bvh_leaf_size = leaf
+        marr[i].primitives = prims.ctypes.data if len(prims) else None
+        marr[i].texcoords = uv.ctypes.data if uv is not None else None
+        marr[i].normals = vn.ctypes.data if vn is not None else None
+        marr[i].attribute_flags = present.ctypes.data if present is not None else None
+    oarr = (abi.gt_object * max(len(objects), 1))()
+    for i, (mesh, xf, inv) in enumerate(objects):
+        oarr[i].mesh = mesh
+        oarr[i].transformed = 0 if xf is None else 1
+        if xf is not None:
+            for a, x in enumerate(np.ravel(xf)):
+                oarr[i].transform[a] = float(x)
+            for a, x in enumerate(np.ravel(inv)):
+                oarr[i].inverse[a] = float(x)
+    return len(meshes), marr, len(objects), oarr, keep
+
+
 def _image_table(images: Sequence[ImageTexture]):
     """A gt_image array for gt_scene_desc (it points into the textures' own texels)."""
     arr = (abi.gt_image * max(len(images), 1))()
@@ -197,6 +348,16 @@ class RayMaterial:
     texture_kind: int = abi.GT_TEX_SOLID
     tex: tuple = (0.0,) * 7
     image: Optional[ImageTexture] = field(default=None, compare=False)
+    normal_map: Optional[NormalMap] = field(default=None, compare=False)
+
+    def with_normal_map(self, normal_map: NormalMap) -> "RayMaterial":
+        """Lambertian / GgxMicrofacet::with_shared_normal_map (material.rs:456-460, 1505-1520):
+        bends the shading normal at mesh triangles with texture coordinates."""
+        if self.kind not in (abi.GT_MAT_LAMBERTIAN, abi.GT_MAT_GGX):
+            raise ValueError("only Lambertian and GGX microfacet materials take a normal map")
+        if not isinstance(normal_map, NormalMap):
+            raise TypeError("with_normal_map takes a NormalMap")
+        return RayMaterial(self.kind, self.color, self.param, self.texture_kind, self.tex, self.image, normal_map)
 
     @staticmethod
     def lambertian(albedo) -> "RayMaterial":
@@ -324,7 +485,9 @@ class RayMaterial:
         return self.kind == abi.GT_MAT_DIFFUSE_LIGHT
 
     def to_record(self) -> tuple:
-        return (self.kind, self.texture_kind, self.color, self.param, self.tex)
+        nm = self.normal_map
+        return (self.kind, self.texture_kind, self.color, self.param, self.tex, 0,
+                int(nm.flip_y) * abi.GT_NORMAL_MAP_NEGATIVE_Y if nm else 0, nm.strength if nm else 0.0)
 
 
 GLASS = 1.5  # RefractiveIndex::GLASS, graphics/lighting.rs:287
@@ -451,12 +614,13 @@ class Context:
 class _SceneHandle:
     def __init__(self, ctx: Context, prims: np.ndarray, mats: np.ndarray, leaf_size: int,
                  bvh_builder: int = abi.GT_BVH_REFERENCE_SAH, images: Sequence[ImageTexture] = (),
-                 media: Sequence = ()):
+                 media: Sequence = (), meshes: Sequence = (), objects: Sequence = ()):
         self.ctx = ctx
         prims = np.ascontiguousarray(prims)
         mats = np.ascontiguousarray(mats)
         table = _image_table(images)
         mtable = _media_table(media)
+        mesh_keep = _mesh_tables(meshes, objects)
         d = abi.gt_scene_desc()
         d.struct_size = C.sizeof(abi.gt_scene_desc)
         d.num_primitives = len(prims)
@@ -469,6 +633,7 @@ class _SceneHandle:
         d.images = table
         d.num_media = len(media)
         d.media = mtable
+        d.num_meshes, d.meshes, d.num_objects, d.objects = mesh_keep[:4]
         h = C.c_void_p()
         check(lib().gt_scene_create(ctx.handle, C.byref(d), C.byref(h)))
         self.h = h
@@ -519,6 +684,9 @@ class RayScene:
         self._leaf_size = 4
         self._bvh_builder = abi.GT_BVH_REFERENCE_SAH
         self._media: list = []
+        self._meshes: list = []
+        self._mesh_index: dict = {}
+        self._objects: list = []
         self._handles: dict = {}
 
     # -- tables
@@ -585,6 +753,36 @@ class RayScene:
         mid = self.add_material(material)
         self.add_quad(corner, u, v, mid)
         return mid
+
+    # -- world objects
+    def add_object(self, obj) -> int:
+        """A TriangleMesh, or a MatrixInstance of one, after the RayScene's surfaces in the
+        world's hit order (HittableList, scene.rs:177-197; the media come after them).  The
+        mesh's material joins the material table.  Returns the object index."""
+        mesh, xf, inv = (obj.mesh, obj.transform, obj.inverse) if isinstance(obj, MatrixInstance) else (obj, None, None)
+        if not isinstance(mesh, TriangleMesh):
+            raise TypeError("a world object is a TriangleMesh or a MatrixInstance of one")
+        key = id(mesh)
+        if key not in self._mesh_index:
+            mid = self.add_material(mesh.material)
+            self._mesh_index[key] = (len(self._meshes), mid)
+            self._meshes.append(mesh)
+        self._objects.append((self._mesh_index[key][0], xf, inv))
+        self._invalidate()
+        return len(self._objects) - 1
+
+    def mesh_list(self) -> list:
+        """(primitives, texcoords, normals, present, leaf size) per mesh, materials resolved."""
+        out = []
+        for mesh in self._meshes:
+            prims = np.zeros(len(mesh), dtype=PRIMITIVE_DTYPE)
+            prims["geometry"] = mesh.geometry
+            prims["material"] = self._mesh_index[id(mesh)][1]
+            out.append((prims, mesh.texcoords, mesh.normals, mesh.present, mesh.leaf_size))
+        return out
+
+    def object_list(self) -> list:
+        return list(self._objects)
 
     # -- animation
     def update_primitives(self, first: int, primitives: np.ndarray) -> None:
@@ -671,6 +869,8 @@ class RayScene:
             arr[i] = m.to_record()
             if m.image is not None:
                 arr[i]["tex"][0] = index[id(m.image)]
+            if m.normal_map is not None:
+                arr[i]["normal_map"] = 1 + index[id(m.normal_map.texture)]
         return arr
 
     def images(self) -> list:
@@ -678,9 +878,10 @@ class RayScene:
         gt_image table; a GT_TEX_IMAGE material's tex[0] indexes it)."""
         out, seen = [], set()
         for m in self._materials:
-            if m.image is not None and id(m.image) not in seen:
-                seen.add(id(m.image))
-                out.append(m.image)
+            for im in (m.image, m.normal_map.texture if m.normal_map is not None else None):
+                if im is not None and id(im) not in seen:
+                    seen.add(id(im))
+                    out.append(im)
         return out
 
     @property
@@ -715,7 +916,7 @@ class RayScene:
         h = self._handles.get(id(ctx))
         if h is None or h.ctx is not ctx or not h.h:
             h = _SceneHandle(ctx, self.primitives_array(), self.materials_array(), self._leaf_size,
-                             self._bvh_builder, self.images(), self._media)
+                             self._bvh_builder, self.images(), self._media, self.mesh_list(), self._objects)
             self._handles[id(ctx)] = h
         return h
 

@@ -127,7 +127,16 @@ typedef struct gt_material {
     double color[3];
     double param;
     double tex[7];
+    /* Tangent-space normal map (NormalMap, raytracing/texture.rs:160-276; Lambertian and
+     * GgxMicrofacet only, material.rs:456-460, 1663-1684): 1 + index into
+     * gt_scene_desc.images, 0 = none.  Applied at mesh triangles with texture coordinates
+     * (their tangent frame, mesh.rs:94-101). */
+    uint32_t normal_map;
+    uint32_t normal_map_flags; /* GT_NORMAL_MAP_NEGATIVE_Y: DirectX-style green channel */
+    double normal_map_strength;
 } gt_material;
+
+enum { GT_NORMAL_MAP_NEGATIVE_Y = 1 };
 
 /* ------------------------------------------------------------------- scene */
 
@@ -170,6 +179,30 @@ typedef struct gt_medium {
     uint32_t reserved;
 } gt_medium;
 
+/* A triangle mesh in object space (TriangleMesh, raytracing/mesh.rs:149-360, with its own
+ * BVH, mesh.rs:640-668): primitives (triangles; spheres and quads are accepted too, for
+ * instancing any RayScene-like object) with optional per-triangle texture coordinates and
+ * vertex normals (MeshTriangle, mesh.rs:22-141). */
+typedef struct gt_mesh {
+    uint32_t num_primitives;
+    uint32_t bvh_leaf_size;           /* 0 = 4 (BvhBuildOptions::default) */
+    const gt_primitive* primitives;   /* geometry and material per primitive */
+    const double* texcoords;          /* 6 per primitive (u0 v0 u1 v1 u2 v2) or NULL */
+    const double* normals;            /* 9 per primitive (n0 n1 n2) or NULL */
+    const uint8_t* attribute_flags;   /* per primitive: bit 0 texcoords, bit 1 normals present;
+                                         NULL = present wherever the array is given */
+} gt_mesh;
+
+/* One world object after the RayScene's surfaces: a mesh, or MatrixInstance(mesh,
+ * transform) (raytracing/instance.rs:205-317).  `inverse` is the instance's world-to-object
+ * matrix as MatrixInstance::inverse returns it; the normal transform is its transpose. */
+typedef struct gt_object {
+    uint32_t mesh;       /* index into gt_scene_desc.meshes */
+    uint32_t transformed; /* 0 = the mesh as it is, 1 = MatrixInstance */
+    double transform[16]; /* row-major object to world */
+    double inverse[16];   /* row-major world to object */
+} gt_object;
+
 typedef struct gt_scene_desc {
     uint32_t struct_size; /* sizeof(gt_scene_desc) */
     uint32_t num_primitives;
@@ -181,8 +214,13 @@ typedef struct gt_scene_desc {
     uint32_t num_images;
     const gt_image* images; /* textures referenced by GT_TEX_IMAGE materials (copied) */
     uint32_t num_media;
-    uint32_t reserved;
+    uint32_t num_meshes;
     const gt_medium* media; /* participating media after the surfaces, in list order (copied) */
+    const gt_mesh* meshes;  /* meshes that objects place (copied) */
+    uint32_t num_objects;
+    uint32_t reserved;
+    const gt_object* objects; /* world objects tested after the RayScene's surfaces and before
+                                 the media (copied) */
 } gt_scene_desc;
 
 /* One weighted sampling target (WeightedSamplingTargetList, raytracing/scene.rs:423-497).

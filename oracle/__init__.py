@@ -64,6 +64,7 @@ def lib() -> C.CDLL:
                 "orc_cosine_pdf": (f64, [vp, vp]),
                 "orc_image_sample": (None, [vp, f64, f64, vp]),
                 "orc_medium_hit": (i32, [vp, vp, f64, f64, u64, vp, vp]),
+                "orc_world_hit": (i32, [vp, vp, f64, f64, u64, vp]),
             }
             for name, (res, args) in sig.items():
                 fn = getattr(L, name)
@@ -80,15 +81,18 @@ def _ptr(a: np.ndarray):
 class OracleScene:
     """A RayScene loaded into the oracle (f64 and f32 copies, reference BVH built)."""
 
-    def __init__(self, prims: np.ndarray, mats: np.ndarray, leaf_size: int = 4, images=(), media=()):
+    def __init__(self, prims: np.ndarray, mats: np.ndarray, leaf_size: int = 4, images=(), media=(), meshes=(),
+                 objects=()):
         from gartus_gb300 import abi
-        from gartus_gb300.raytracing import _image_table, _media_table
+        from gartus_gb300.raytracing import _image_table, _media_table, _mesh_tables
         self._prims = np.ascontiguousarray(prims)
         self._mats = np.ascontiguousarray(mats)
         self._images = list(images)
         self._table = _image_table(self._images)
         self._media = list(media)
         self._mtable = _media_table(self._media)
+        self._meshes, self._objects = list(meshes), list(objects)
+        self._mesh_keep = _mesh_tables(self._meshes, self._objects)
         d = abi.gt_scene_desc()
         d.struct_size = C.sizeof(abi.gt_scene_desc)
         d.num_primitives = len(self._prims)
@@ -100,18 +104,31 @@ class OracleScene:
         d.images = self._table
         d.num_media = len(self._media)
         d.media = self._mtable
+        d.num_meshes, d.meshes, d.num_objects, d.objects = self._mesh_keep[:4]
         self.h = lib().orc_scene_create(C.byref(d))
         if not self.h:
             raise ValueError("oracle rejected the scene")
 
     @classmethod
     def from_ray_scene(cls, scene) -> "OracleScene":
-        return cls(scene.primitives_array(), scene.materials_array(), scene.leaf_size, scene.images(), scene.media())
+        return cls(scene.primitives_array(), scene.materials_array(), scene.leaf_size, scene.images(), scene.media(),
+                   scene.mesh_list(), scene.object_list())
 
     def __del__(self):
         if getattr(self, "h", None):
             lib().orc_scene_destroy(self.h)
             self.h = None
+
+    def world_hit(self, ray, tmin: float = 0.001, tmax: float = float("inf"), seed: int = 0):
+        """The world's closest hit (f64) of ray = (origin, direction[, time]), or None: a dict
+        of t, point, normal, shading_normal, u, v, front_face, material."""
+        r = np.zeros(7)
+        r[:len(np.ravel(ray))] = np.ravel(ray)
+        out = np.zeros(14)
+        if not lib().orc_world_hit(self.h, _ptr(r), float(tmin), float(tmax), int(seed), _ptr(out)):
+            return None
+        return {"t": out[0], "point": out[1:4], "normal": out[4:7], "shading_normal": out[7:10],
+                "u": out[10], "v": out[11], "front_face": bool(out[12]), "material": int(out[13])}
 
     def node_count(self) -> int:
         return lib().orc_scene_node_count(self.h)

@@ -331,6 +331,7 @@ inline Bounds geometry_bounds(const gt_geometry& g) {
 
 template <class R> struct Hit {
     V3<R> point, normal; // normal is oriented against the ray (SurfaceHit::with_uv)
+    V3<R> shading;       // HitRecord::shading_normal (the normal unless a mesh bends it)
     R t{0}, u{0}, v{0};
     bool front_face = false;
     int prim = -1;
@@ -374,6 +375,7 @@ template <class R> inline void sphere_uv(V3<R> p, R& u, R& v) {
 template <class R> inline void set_face(Hit<R>& h, const Ray<R>& ray, V3<R> outward) { // object.rs:127-149
     h.front_face = dot(ray.d, outward) < R(0);
     h.normal = h.front_face ? outward : -outward;
+    h.shading = h.normal;
 }
 
 // MovingSphereGeometry::outward_normal_at / SphereGeometry (geometry.rs:476-484, 530-538).
@@ -820,6 +822,37 @@ struct ImageData {
             out[k] = uint8_t(v <= 0.0 ? 0 : (v >= 255.0 ? 255 : v));
         }
     }
+    // NormalMap::sample_tangent_normal (raytracing/texture.rs:254-275).
+    template <class R> V3<R> tangent_normal(R u, R v, R strength, bool neg_y) const {
+        if (w == 0 || h == 0) return V3<R>(0, 0, 1);
+        uint8_t c[3];
+        rgb8(double(u), double(v), c);
+        auto dec = [](uint8_t ch) { return R(2.0 * (double(ch) / 255.0) - 1.0); };
+        const R green = neg_y ? -dec(c[1]) : dec(c[1]);
+        const V3<R> n(strength * dec(c[0]), strength * green, std::fmax(dec(c[2]), R(0)));
+        return length_squared(n) <= R(kEps) ? V3<R>(0, 0, 1) : normalized(n);
+    }
+    // Texture::sample (graphics/texture.rs:202-208) of a non-empty bitmap: the u8 texel.
+    void rgb8(double s, double t, uint8_t* c) const {
+        c[0] = c[1] = c[2] = 0;
+        if (!(std::isfinite(s) && std::isfinite(t))) return;
+        if (filter == GT_FILTER_NEAREST) { // sample_nearest, texture.rs:716-722
+            const double ws = wrap(s, wrap_s), wt = wrap(t, wrap_t);
+            const uint32_t x = to_u32(std::round(ws * double(w - 1)));
+            const uint32_t y = to_u32(std::round((1.0 - wt) * double(h - 1)));
+            std::memcpy(c, at(x, y), 3);
+        } else { // sample_linear, texture.rs:724-735
+            double x, y;
+            uint32_t x0, x1, y0, y1;
+            axis(s, w, wrap_s, x, x0, x1);
+            axis(1.0 - t, h, wrap_t, y, y0, y1);
+            const double tx = x - double(x0), ty = y - double(y0);
+            uint8_t top[3], bottom[3];
+            lerp(at(x0, y0), at(x1, y0), tx, top);
+            lerp(at(x0, y1), at(x1, y1), tx, bottom);
+            lerp(top, bottom, ty, c);
+        }
+    }
     // ImageTexture::sample_linear (raytracing/texture.rs:148-155) then from_rgb_srgb.
     template <class R> V3<R> sample(R u, R v) const {
         uint8_t c[3] = {0, 0, 0};
@@ -863,6 +896,9 @@ template <class R> struct Material {
     int noise_variant = 0, noise_depth = 0;
     std::shared_ptr<Perlin> perlin;
     std::shared_ptr<const ImageData> image;
+    std::shared_ptr<const ImageData> normal_map; // Lambertian / GgxMicrofacet::with_shared_normal_map
+    R normal_strength{1};
+    bool normal_neg_y = false;
     static Material from_desc(const gt_material& m) {
         Material r;
         r.kind = int(m.kind);
@@ -1038,7 +1074,7 @@ template <class R> inline Scatter<R> scatter(const Material<R>& m, const Ray<R>&
     Scatter<R> s;
     switch (m.kind) {
     case GT_MAT_LAMBERTIAN: { // material.rs:508-521
-        if (!Onb<R>::from_w(h.normal, s.pdf.basis)) return s;
+        if (!Onb<R>::from_w(h.shading, s.pdf.basis)) return s;
         s.kind = SCATTER_PDF;
         s.pdf.kind = PDF_COSINE;
         s.att = m.sample(h);
@@ -1060,7 +1096,7 @@ template <class R> inline Scatter<R> scatter(const Material<R>& m, const Ray<R>&
         V3<R> outgoing = -normalized(in.d);
         MatPdf<R> p;
         p.kind = PDF_GGX;
-        if (!Onb<R>::from_w(h.normal, p.basis)) return s;
+        if (!Onb<R>::from_w(h.shading, p.basis)) return s;
         p.outgoing = normalized(outgoing);
         if (length_squared(p.outgoing) <= R(kEps) || dot(p.outgoing, p.basis.w) <= R(0)) return s;
         p.roughness = rclamp(m.param, R(0), R(1));
@@ -1071,7 +1107,7 @@ template <class R> inline Scatter<R> scatter(const Material<R>& m, const Ray<R>&
         return s;
     }
     case GT_MAT_METAL: { // material.rs:2087-2106
-        V3<R> refl = reflected(normalized(in.d), h.normal);
+        V3<R> refl = reflected(normalized(in.d), h.shading);
         V3<R> dir = refl + rng.random_unit_vector_spherical<R>() * m.param;
         if (dot(dir, h.normal) <= R(0)) return s;
         s.kind = SCATTER_SPECULAR;
@@ -1109,7 +1145,7 @@ template <class R> inline Scatter<R> scatter(const Material<R>& m, const Ray<R>&
 template <class R> inline R scattering_pdf(const Material<R>& m, const Ray<R>& in, const Hit<R>& h, V3<R> out_dir) {
     switch (m.kind) {
     case GT_MAT_LAMBERTIAN: { // material.rs:523-530
-        R c = dot(h.normal, normalized(out_dir));
+        R c = dot(h.shading, normalized(out_dir));
         return c <= R(0) ? R(0) : c / R(kPi);
     }
     case GT_MAT_ISOTROPIC:
@@ -1126,7 +1162,7 @@ template <class R> inline R scattering_pdf(const Material<R>& m, const Ray<R>& i
         V3<R> incoming = normalized(out_dir);
         if (dot(incoming, h.normal) <= R(0) || dot(outgoing, h.normal) <= R(0)) return R(0);
         R f0 = specular_luminance(m.sample(h));
-        V3<R> n = normalized(h.normal);
+        V3<R> n = normalized(h.shading);
         V3<R> o = normalized(outgoing);
         V3<R> i = normalized(incoming);
         R ndi = dot(n, i), ndo = dot(n, o);
@@ -1402,11 +1438,89 @@ template <class R> struct Environment {
 };
 
 // --------------------------------------------------------------------- scene
+// ------------------------------------------------------------ meshes, instances
+// TriangleMesh (raytracing/mesh.rs): object-space primitives with optional per-triangle
+// texture coordinates and vertex normals.  Its hit is the closest over all primitives in
+// order (the mesh BVH of mesh.rs:640-668 returns the same hit up to exact ties).
+template <class R> struct MeshObj {
+    std::vector<Prim<R>> prims;
+    std::vector<double> uv, vn; // 6 / 9 per primitive or empty
+    std::vector<uint8_t> attr;  // bit 0 texcoords, bit 1 normals
+
+    // MeshTriangle::hit (mesh.rs:56-101) with the material's normal map
+    // (material.rs:1663-1684) for a closest hit `h` on primitive i.
+    void finish(const Material<R>& m, uint32_t i, const Ray<R>& ray, Hit<R>& h) const {
+        const Prim<R>& p = prims[i];
+        if (p.kind != GT_GEOM_TRIANGLE || attr.empty() || attr[i] == 0) return;
+        // the barycentrics of the hit: triangle_hit_ray's u, v (Hit u, v of a plain triangle)
+        const R bu = h.u, bv = h.v, bw = R(1) - bu - bv;
+        const double* tc = uv.empty() ? nullptr : uv.data() + size_t(i) * 6;
+        if (attr[i] & 1) {
+            h.u = bw * R(tc[0]) + bu * R(tc[2]) + bv * R(tc[4]);
+            h.v = bw * R(tc[1]) + bu * R(tc[3]) + bv * R(tc[5]);
+        }
+        if (attr[i] & 2) { // shading_normal + set_shading_normal (object.rs:469-479)
+            const double* n = vn.data() + size_t(i) * 9;
+            const V3<R> s = V3<R>(R(n[0]), R(n[1]), R(n[2])) * bw + V3<R>(R(n[3]), R(n[4]), R(n[5])) * bu +
+                            V3<R>(R(n[6]), R(n[7]), R(n[8])) * bv;
+            if (length_squared(s) > R(kEps)) h.shading = h.front_face ? normalized(s) : -normalized(s);
+        }
+        if (!(attr[i] & 1) || !m.normal_map) return;
+        // tangent_frame (mesh.rs:121-141)
+        const V3<R> e1 = p.b - p.a, e2 = p.c - p.a;
+        const R du1 = R(tc[2]) - R(tc[0]), dv1 = R(tc[3]) - R(tc[1]);
+        const R du2 = R(tc[4]) - R(tc[0]), dv2 = R(tc[5]) - R(tc[1]);
+        const R det = du1 * dv2 - du2 * dv1;
+        if (std::fabs(det) <= R(kEps)) return;
+        const R inv = R(1) / det;
+        const V3<R> tangent = (e1 * dv2 - e2 * dv1) * inv, bitangent = (e2 * du1 - e1 * du2) * inv;
+        if (!(length_squared(tangent) > R(kEps) && length_squared(bitangent) > R(kEps))) return;
+        // set_tangent_frame (object.rs:495-517)
+        const V3<R> n = h.shading;
+        V3<R> t = tangent - n * dot(tangent, n);
+        if (length_squared(t) <= R(kEps)) return;
+        t = normalized(t);
+        const V3<R> ref = cross(n, t);
+        V3<R> b = bitangent - n * dot(bitangent, n);
+        b = b - t * dot(b, t);
+        if (length_squared(b) <= R(kEps)) b = ref;
+        const R hand = dot(b, ref) < R(0) ? R(-1) : R(1);
+        b = normalized(ref * hand);
+        // normal_map_world_normal + set_oriented_shading_normal (object.rs:481-493)
+        const V3<R> tn = m.normal_map->template tangent_normal<R>(h.u, h.v, m.normal_strength, m.normal_neg_y);
+        V3<R> world = t * tn.x + b * tn.y + n * tn.z;
+        if (length_squared(world) <= R(kEps)) return;
+        world = normalized(world);
+        if (dot(world, n) < R(0)) world = -world;
+        if (length_squared(world) > R(kEps)) h.shading = normalized(world);
+    }
+};
+
+// A world object: a mesh, or MatrixInstance(mesh) (raytracing/instance.rs:205-317).
+template <class R> struct WorldObject {
+    uint32_t mesh = 0;
+    bool transformed = false;
+    R xf[16], inv[16];
+    static V3<R> point(const R* m, V3<R> p) { // transform_point, instance.rs:355-364
+        R r[4];
+        for (int i = 0; i < 4; ++i) r[i] = m[4 * i] * p.x + m[4 * i + 1] * p.y + m[4 * i + 2] * p.z + m[4 * i + 3] * R(1);
+        if (std::fabs(r[3]) > R(kEps)) return V3<R>(r[0] / r[3], r[1] / r[3], r[2] / r[3]);
+        return V3<R>(r[0], r[1], r[2]);
+    }
+    static V3<R> vector(const R* m, V3<R> v) { // transform_vector, instance.rs:366-369
+        R r[3];
+        for (int i = 0; i < 3; ++i) r[i] = m[4 * i] * v.x + m[4 * i + 1] * v.y + m[4 * i + 2] * v.z + m[4 * i + 3] * R(0);
+        return V3<R>(r[0], r[1], r[2]);
+    }
+};
+
 template <class R> struct Scene {
     std::vector<Prim<R>> prims;
     std::vector<gt_geometry> geoms;
     std::vector<Material<R>> materials;
     std::vector<Medium<R>> media;
+    std::vector<MeshObj<R>> meshes;
+    std::vector<WorldObject<R>> objects;
     FlatBvh bvh;
 
     void load(const gt_scene_desc& d) {
@@ -1414,6 +1528,37 @@ template <class R> struct Scene {
         geoms.clear();
         materials.clear();
         media.clear();
+        meshes.clear();
+        objects.clear();
+        for (uint32_t k = 0; k < (d.meshes ? d.num_meshes : 0u); ++k) {
+            const gt_mesh& gm = d.meshes[k];
+            MeshObj<R> m;
+            const size_t n = gm.num_primitives;
+            for (size_t i = 0; i < n; ++i) {
+                if (gm.primitives[i].material >= d.num_materials) throw std::invalid_argument("mesh material id");
+                m.prims.push_back(Prim<R>::from_geometry(gm.primitives[i].geometry, gm.primitives[i].material));
+            }
+            if (gm.texcoords) m.uv.assign(gm.texcoords, gm.texcoords + n * 6);
+            if (gm.normals) m.vn.assign(gm.normals, gm.normals + n * 9);
+            m.attr.resize(n);
+            for (size_t i = 0; i < n; ++i) {
+                const uint8_t given = uint8_t((gm.texcoords ? 1 : 0) | (gm.normals ? 2 : 0));
+                m.attr[i] = gm.attribute_flags ? uint8_t(gm.attribute_flags[i] & given) : given;
+            }
+            meshes.push_back(std::move(m));
+        }
+        for (uint32_t k = 0; k < (d.objects ? d.num_objects : 0u); ++k) {
+            const gt_object& go = d.objects[k];
+            if (go.mesh >= meshes.size()) throw std::invalid_argument("object mesh index");
+            WorldObject<R> o;
+            o.mesh = go.mesh;
+            o.transformed = go.transformed != 0;
+            for (int a = 0; a < 16; ++a) {
+                o.xf[a] = R(go.transform[a]);
+                o.inv[a] = R(go.inverse[a]);
+            }
+            objects.push_back(o);
+        }
         for (uint32_t i = 0; i < (d.media ? d.num_media : 0u); ++i) {
             const gt_medium& m = d.media[i];
             if (m.material >= d.num_materials || !(std::isfinite(m.density) && m.density > 0.0) ||
@@ -1435,6 +1580,13 @@ template <class R> struct Scene {
         }
         for (uint32_t i = 0; i < d.num_materials; ++i) {
             materials.push_back(Material<R>::from_desc(d.materials[i]));
+            if (d.materials[i].normal_map) {
+                const gt_material& gm = d.materials[i];
+                if (gm.normal_map > images.size()) throw std::invalid_argument("normal map index out of range");
+                materials.back().normal_map = images[gm.normal_map - 1];
+                materials.back().normal_strength = R(std::fmax(gm.normal_map_strength, 0.0)); // with_strength
+                materials.back().normal_neg_y = (gm.normal_map_flags & GT_NORMAL_MAP_NEGATIVE_Y) != 0;
+            }
             if (d.materials[i].texture_kind == GT_TEX_IMAGE) {
                 const double k = d.materials[i].tex[0];
                 if (!(k >= 0 && k < double(images.size())) || k != std::floor(k))
@@ -1473,9 +1625,52 @@ template <class R> struct Scene {
     // HittableList::hit_with_rng over [this RayScene, media...] (scene.rs:177-197): the
     // surfaces' closest hit, then each medium in order, clipped to the closest so far.  A
     // medium hit is the medium_hit_record of medium.rs:152-168.
+    // The world objects come between the surfaces and the media.
+    bool object_hit(const WorldObject<R>& o, const Ray<R>& ray, R tmin, R tmax, Hit<R>& out) const {
+        Ray<R> r = ray;
+        if (o.transformed) { // MatrixInstance::hit_with_rng (instance.rs:266-289)
+            r.o = WorldObject<R>::point(o.inv, ray.o);
+            r.d = WorldObject<R>::vector(o.inv, ray.d);
+        }
+        const MeshObj<R>& m = meshes[o.mesh];
+        R closest = tmax;
+        int best = -1;
+        Hit<R> h;
+        for (size_t i = 0; i < m.prims.size(); ++i) {
+            Hit<R> c;
+            if (intersect(m.prims[i], r, tmin, closest, c)) {
+                closest = c.t;
+                best = int(i);
+                h = c;
+            }
+        }
+        if (best < 0) return false;
+        h.prim = best;
+        h.material = m.prims[size_t(best)].material;
+        m.finish(materials[h.material], uint32_t(best), r, h);
+        if (o.transformed) { // (u, v) kept; set_face_normal resets the shading normal (object.rs:455-467)
+            const V3<R> outward_obj = h.front_face ? h.normal : -h.normal;
+            h.point = WorldObject<R>::point(o.xf, h.point);
+            R nt[16]; // normal_transform = inverse.transpose()
+            for (int i = 0; i < 4; ++i)
+                for (int j = 0; j < 4; ++j) nt[4 * i + j] = o.inv[4 * j + i];
+            set_face(h, ray, normalized(WorldObject<R>::vector(nt, outward_obj)));
+        }
+        out = h;
+        return true;
+    }
+
     bool world_hit(const Ray<R>& ray, R tmin, R tmax, Hit<R>& out, SampleRng& rng) const {
         bool any = hit(ray, tmin, tmax, out);
         R closest = any ? out.t : tmax;
+        for (const WorldObject<R>& o : objects) {
+            Hit<R> h;
+            if (object_hit(o, ray, tmin, closest, h)) {
+                closest = h.t;
+                out = h;
+                any = true;
+            }
+        }
         for (size_t k = 0; k < media.size(); ++k) {
             R t;
             if (!media[k].hit(ray, tmin, closest, rng, t)) continue;
@@ -1483,6 +1678,7 @@ template <class R> struct Scene {
             out = Hit<R>();
             out.point = ray.at(t);
             out.normal = V3<R>(1, 0, 0);
+            out.shading = out.normal;
             out.t = t;
             out.front_face = true;
             out.prim = -2 - int(k);
@@ -1867,7 +2063,7 @@ template <class R> struct Renderer {
             Hit<R> rec;
             if (!scene->world_hit(ray, R(kShadowAcne), std::numeric_limits<R>::infinity(), rec, rng)) return V3<R>();
             if (kind == 0) return denoise_albedo(scene->materials[rec.material], rec);
-            return (rec.normal + V3<R>(1, 1, 1)) * R(0.5);
+            return (rec.shading + V3<R>(1, 1, 1)) * R(0.5);
         };
         if (cam.desc.pixel_sample_mode == GT_SAMPLE_RANDOM) {
             for (uint32_t i = 0; i < n; ++i) sum = sum + sample(cam.ray_for_pixel_sample(x, y, rng));

@@ -363,6 +363,7 @@ int orc_scatter(const gt_material* md, const double* ray7, const double* point, 
     Hit<double> h;
     h.point = V3<double>(point[0], point[1], point[2]);
     h.normal = V3<double>(normal[0], normal[1], normal[2]);
+    h.shading = h.normal;
     h.front_face = front != 0;
     SampleRng rng(seed);
     Scatter<double> s = scatter(m, r, h, rng);
@@ -385,6 +386,7 @@ double orc_scattering_pdf(const gt_material* md, const double* ray7, const doubl
     Hit<double> h;
     h.point = V3<double>(point[0], point[1], point[2]);
     h.normal = V3<double>(normal[0], normal[1], normal[2]);
+    h.shading = h.normal;
     h.front_face = front != 0;
     return scattering_pdf(m, r, h, V3<double>(dir[0], dir[1], dir[2]));
 }
@@ -410,6 +412,25 @@ int orc_medium_hit(const gt_medium* m, const double* ray7, double tmin, double t
     *draws = n;
     *t = hit ? th : 0.0;
     return hit ? 1 : 0;
+}
+
+// The world's closest hit (surfaces, objects, media) of ray7 = {origin, direction, time} in
+// (tmin, tmax), f64, media drawing from a SampleRng seeded `seed`.  out[14] = t, point,
+// normal, shading normal, u, v, front face, material.  Returns 1 on a hit.
+int orc_world_hit(void* sp, const double* ray7, double tmin, double tmax, uint64_t seed, double* out) {
+    const Scene<double>& sc = static_cast<OrcScene*>(sp)->s64;
+    Ray<double> r;
+    r.o = V3<double>(ray7[0], ray7[1], ray7[2]);
+    r.d = V3<double>(ray7[3], ray7[4], ray7[5]);
+    r.time = ray7[6];
+    SampleRng rng(seed);
+    Hit<double> h;
+    if (!sc.world_hit(r, tmin, tmax, h, rng)) return 0;
+    const double v[14] = {h.t, h.point.x, h.point.y, h.point.z, h.normal.x, h.normal.y, h.normal.z,
+                          h.shading.x, h.shading.y, h.shading.z, h.u, h.v, h.front_face ? 1.0 : 0.0,
+                          double(h.material)};
+    std::memcpy(out, v, sizeof(v));
+    return 1;
 }
 
 // ImageTexture sampling at (u, v) into linear RGB.

@@ -888,3 +888,114 @@ def test_update_primitives_refit(gpu_context, builder):
     with pytest.raises(GartusError):  # the library checks the range itself
         check(lib().gt_scene_update_primitives(scene._handle(gpu_context).h, 10**6, 1,
                                                scene.primitives_array()[:1].ctypes.data_as(C.c_void_p)))
+
+
+def _uv_sphere(center, radius, rings=8, segs=12):
+    """A tessellated sphere: (N, 3, 3) triangles with per-vertex texture coordinates
+    (N, 3, 2) and smooth vertex normals (N, 3, 3)."""
+    tris, uvs, nrms = [], [], []
+
+    def vert(i, j):
+        th, ph = math.pi * i / rings, 2 * math.pi * j / segs
+        n = np.array([math.sin(th) * math.cos(ph), math.cos(th), math.sin(th) * math.sin(ph)])
+        return np.asarray(center) + radius * n, (j / segs, 1.0 - i / rings), n
+
+    for i in range(rings):
+        for j in range(segs):
+            a, b, c, d = vert(i, j), vert(i + 1, j), vert(i + 1, j + 1), vert(i, j + 1)
+            for t in ((a, b, c), (a, c, d)):
+                tris.append([v[0] for v in t])
+                uvs.append([v[1] for v in t])
+                nrms.append([v[2] for v in t])
+    return np.array(tris), np.array(uvs), np.array(nrms)
+
+
+def _mesh_world():
+    from gartus_gb300.raytracing import ImageTexture, MatrixInstance, NormalMap, TriangleMesh
+    rng = np.random.default_rng(23)
+    scene = RayScene()
+    floor = scene.add_material(RayMaterial.lambertian((0.6, 0.6, 0.6)))
+    light = scene.add_material(RayMaterial.diffuse_light((8.0, 8.0, 8.0)))
+    scene.add_quad((-6.0, -0.6, 2.0), (12.0, 0.0, 0.0), (0.0, 0.0, -12.0), floor)
+    scene.add_quad((-1.5, 3.5, -3.5), (3.0, 0.0, 0.0), (0.0, 0.0, 2.0), light)
+    bumps = rng.integers(60, 196, size=(8, 8, 3), dtype=np.uint8)
+    bumps[..., 2] = 230
+    tex = ImageTexture(rng.integers(0, 256, size=(6, 9, 3), dtype=np.uint8), filter="linear", wrap_s="repeat")
+    tris, uv, nrm = _uv_sphere((0.0, 0.0, 0.0), 0.6)
+    bumpy = TriangleMesh(tris, RayMaterial.textured_lambertian(tex).with_normal_map(
+        NormalMap(ImageTexture(bumps, filter="linear"), strength=1.5)), texcoords=uv, normals=nrm)
+    smooth = TriangleMesh(tris, RayMaterial.ggx_microfacet((0.9, 0.8, 0.6), 0.25).with_normal_map(
+        NormalMap(ImageTexture(bumps), flip_y=True)), texcoords=uv, normals=nrm,
+        present=np.where(np.arange(len(tris)) % 5 == 0, 1, 3))
+    ball = TriangleMesh.from_geometry([RayGeometry.sphere((0.0, 0.0, 0.0), 0.5)], RayMaterial.metal((0.9, 0.9, 0.9), 0.05))
+
+    def trs(t, deg, scale):
+        c, s = math.cos(math.radians(deg)), math.sin(math.radians(deg))
+        m = np.array([[c, 0, s, 0], [0, 1, 0, 0], [-s, 0, c, 0], [0, 0, 0, 1.0]]) @ np.diag(list(scale) + [1.0])
+        m[:3, 3] = t
+        return m
+
+    scene.add_object(TriangleMesh(tris + np.array([-1.4, 0.0, -3.0]), bumpy.material, texcoords=uv, normals=nrm))
+    scene.add_object(MatrixInstance(bumpy, trs((0.0, 0.0, -3.2), 30.0, (1.0, 1.0, 1.0))))
+    scene.add_object(MatrixInstance(smooth, trs((1.4, 0.1, -3.0), -20.0, (1.2, 0.8, 1.0))))
+    scene.add_object(TriangleMesh(tris + np.array([0.7, 0.9, -4.2]), smooth.material, texcoords=uv, normals=nrm))
+    scene.add_object(MatrixInstance(ball, trs((-0.6, -0.1, -2.0), 0.0, (1.0, 0.5, 1.0))))
+    scene.build_bvh()
+    lights = SamplingTargetList()
+    lights.add_quad((-1.5, 3.5, -3.5), (3.0, 0.0, 0.0), (0.0, 0.0, 2.0))
+    return scene, lights
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("mode", ["mixture", "nee"])
+def test_meshes_and_instances(gpu_context, precision, mode):
+    # TriangleMesh with texture coordinates, vertex normals and normal maps (mesh.rs:56-141,
+    # material.rs:1663-1684) and MatrixInstance (instance.rs:205-317) placing meshes and a
+    # sphere, after the RayScene's surfaces: the f64 image matches the oracle's.
+    scene, lights = _mesh_world()
+    cam = (RayCamera(48, 1.5).with_samples_per_pixel(4).with_max_depth(8)
+           .with_look_at((0.0, 1.0, 2.0), (0.0, 0.0, -3.0)).with_background((0.1, 0.1, 0.12)))
+    if mode == "nee":
+        cam = cam.with_direct_lighting_mode(abi.GT_DIRECT_NEXT_EVENT_ESTIMATION)
+    pt = PathTracer(cam, precision=precision, context=gpu_context)
+    ref, acc = _oracle_render(scene, cam, lights)
+    if precision == "f64":
+        img = pt.render_with_lights_hdr_image(scene, lights, want64=True)
+        np.testing.assert_array_equal(img.accepted, acc)
+        err = rel_err(img.pixels64, ref, floor=1e-12).max(axis=2)
+        assert (err <= 1e-9).mean() >= 0.99, err.max()
+    else:
+        img = pt.render_with_lights_hdr_image(scene, lights)
+        ref32, _ = _oracle_render(scene, cam, lights, precision=0)
+        n = ref.shape[0] * ref.shape[1]
+        assert _divergent(img.pixels, ref) <= _divergent(ref32, ref) + 0.03 * n
+    st = pt.last_stats
+    assert st["persistent_rays"] == st["rays"] + st["shadow_rays"]
+    assert np.std(ref) > 1e-3
+
+
+def test_meshes_aovs_batch_and_primary(gpu_context):
+    # The AOVs read the shading normal (camera.rs:3112-3114); a batch of an object world runs
+    # the persistent batch; gt_trace_rays sees the RayScene only, as RayScene::hit does.
+    scene, lights = _mesh_world()
+    cam = RayCamera(40, 1.5).with_samples_per_pixel(3).with_max_depth(6).with_look_at((0.0, 1.0, 2.0), (0.0, 0.0, -3.0))
+    aovs = PathTracer(cam, precision="f64", context=gpu_context).render_denoising_aovs(scene)
+    _, _, alb, nrm = _oracle_render(scene, cam, aovs=True)
+    np.testing.assert_allclose(aovs.albedo_linear, alb, rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(aovs.normal_linear, nrm, rtol=1e-6, atol=1e-6)
+    cams = [cam.with_rng_seed(5), cam.with_samples_per_pixel(2)]
+    for precision in ("f64", "f32"):
+        imgs = PathTracer(cam, precision=precision, context=gpu_context).render_batch_hdr_images(
+            scene, cams, lights=lights, want64=precision == "f64")
+        for c, img in zip(cams, imgs):
+            one = PathTracer(c, precision=precision, context=gpu_context).render_with_lights_hdr_image(
+                scene, lights, want64=precision == "f64")
+            if precision == "f64":
+                np.testing.assert_array_equal(img.pixels64, one.pixels64)
+            else:
+                assert _divergent(img.pixels, one.pixels.astype(np.float64)) <= 0.05 * img.pixels.shape[0] * img.pixels.shape[1]
+    rays = np.zeros((64, 7))
+    rays[:, :3] = (0.0, 1.0, 2.0)
+    rays[:, 3:6] = np.random.default_rng(4).normal(size=(64, 3)) * 0.3 + (0.0, -0.2, -1.0)
+    ids, _, _ = scene.hit_rays(rays, ctx=gpu_context)
+    assert set(np.unique(ids)) <= {-1, 0, 1} and (ids == 0).any()  # the floor and light quads only
