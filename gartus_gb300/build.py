@@ -28,9 +28,11 @@ NVCC_COMMON = [
 
 UNITS = [
     ("api.cu", []),
-    ("render_f32.cu", ["-fmad=true"]),
+    # The f32 throughput path: contracted multiply-adds and the hardware division and
+    # square root (within 2 ulp; its parity is held to the f32 tolerances, not bit-exact).
+    ("render_f32.cu", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
     ("render_f64.cu", ["-fmad=false"]),
-    ("noalloc.cu", ["-fmad=true"]),
+    ("noalloc.cu", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
     ("denoise.cu", ["-fmad=true"]),
     ("lbvh.cu", ["-fmad=true"]),
 ]
