@@ -40,7 +40,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="cornell", choices=["cornell", "final", "mesh", "batch", "denoise"])
+    ap.add_argument("--config", default="cornell", choices=["cornell", "final", "mesh", "batch", "smoke", "denoise"])
     ap.add_argument("--target-spp", type=int, default=4096, help="denoise config: samples of the reference image")
     ap.add_argument("--max-spp", type=int, default=1024, help="denoise config: largest plain sample count")
     ap.add_argument("--scene", default="mesh", choices=["mesh", "cornell"],
@@ -83,6 +83,14 @@ def workload(name, width=0, grid=0):
                "sampling": f"stratified {grid}x{grid}", "lights": "HDR environment 2048x1024 f32 with sun (NEE)",
                "primitives": len(scene), "precision": "f32"}
         return scene, None, env, cam, cfg
+    if name == "smoke":  # participating media: the persistent kernel's world variant
+        scene, _ = scenes.cornell_smoke_scene()
+        width, grid = width or 600, grid or 8
+        cam = scenes.cornell_camera(width, grid, 50)
+        cfg = {"workload": "cornell_smoke_media", "width": width, "height": width, "spp": grid * grid,
+               "max_depth": 50, "sampling": f"stratified {grid}x{grid}", "lights": "none (material sampling)",
+               "primitives": len(scene), "media": 2, "precision": "f32"}
+        return scene, None, None, cam, cfg
     if name == "batch":
         scene, lights = scenes.batch_scene()
         width = width or 512
