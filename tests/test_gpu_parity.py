@@ -999,3 +999,46 @@ def test_meshes_aovs_batch_and_primary(gpu_context):
     rays[:, 3:6] = np.random.default_rng(4).normal(size=(64, 3)) * 0.3 + (0.0, -0.2, -1.0)
     ids, _, _ = scene.hit_rays(rays, ctx=gpu_context)
     assert set(np.unique(ids)) <= {-1, 0, 1} and (ids == 0).any()  # the floor and light quads only
+
+
+def test_world_edge_cases(gpu_context):
+    # Objects and media together (objects before media in the hit order), an empty mesh
+    # placed twice, a texture-coordinate-only mesh with an image texture, and invalid
+    # world descriptions refused by the library.
+    from gartus_gb300.raytracing import ImageTexture, MatrixInstance, MediumBoundary, TriangleMesh, _SceneHandle
+    tris, uv, _ = _uv_sphere((0.0, 0.0, -2.5), 0.7, 6, 10)
+    scene = RayScene()
+    scene.add_quad((-4.0, -0.8, 1.0), (8.0, 0.0, 0.0), (0.0, 0.0, -8.0), scene.add_material(RayMaterial.lambertian((0.7,) * 3)))
+    tex = ImageTexture(np.random.default_rng(2).integers(0, 256, size=(4, 4, 3), dtype=np.uint8))
+    scene.add_object(TriangleMesh(tris, RayMaterial.textured_lambertian(tex), texcoords=uv))
+    empty = TriangleMesh(np.zeros((0, 3, 3)), RayMaterial.lambertian((0.5,) * 3))
+    scene.add_object(empty)
+    scene.add_object(MatrixInstance(empty, np.eye(4)))
+    scene.add_constant_medium(MediumBoundary.sphere((0.0, 0.0, -2.5), 1.2), 0.6, (0.8, 0.8, 0.9))
+    scene.build_bvh()
+    cam = RayCamera(32, 1.5).with_samples_per_pixel(4).with_max_depth(8).with_background((0.6, 0.7, 0.9))
+    img = PathTracer(cam, precision="f64", context=gpu_context).render_hdr_image(scene, want64=True)
+    ref, acc = _oracle_render(scene, cam)
+    np.testing.assert_array_equal(img.accepted, acc)
+    err = rel_err(img.pixels64, ref, floor=1e-12).max(axis=2)
+    assert (err <= 1e-9).mean() >= 0.99, err.max()
+    # invalid: an object naming a missing mesh, a normal map on a metal, an image index past the table
+    prims, mats = scene.primitives_array(), scene.materials_array()
+    meshes, objects = scene.mesh_list(), scene.object_list()
+    with pytest.raises(GartusError):
+        _SceneHandle(gpu_context, prims, mats, 4, abi.GT_BVH_REFERENCE_SAH, scene.images(), (), meshes, [(7, None, None)])
+    bad = mats.copy()
+    bad[0]["kind"] = abi.GT_MAT_METAL
+    bad[0]["normal_map"] = 1
+    with pytest.raises(GartusError):
+        _SceneHandle(gpu_context, prims, bad, 4, abi.GT_BVH_REFERENCE_SAH, scene.images(), (), meshes, objects)
+    bad = mats.copy()
+    bad[0]["normal_map"] = 9
+    with pytest.raises(GartusError):
+        _SceneHandle(gpu_context, prims, bad, 4, abi.GT_BVH_REFERENCE_SAH, scene.images(), (), meshes, objects)
+    # accumulating a world with objects or media is refused
+    from gartus_gb300.raytracing import Accumulator
+    acc_obj = Accumulator(32, 21, "f32", gpu_context)
+    with pytest.raises(GartusError) as e:
+        PathTracer(cam, context=gpu_context).render_accumulate(scene, acc_obj, 1)
+    assert e.value.status == abi.GT_ERR_UNSUPPORTED
