@@ -1105,7 +1105,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     // Per-stripe launch sizes: a stripe owns about 1/K of the GPU.
     int tail_per_sm = 0, coop_per_sm = 0;
     GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tail_per_sm, k_persistent<R, true, BATCH>, 128, 0));
-    coop_per_sm = tail_per_sm; // the cooperative mode is the same kernel
+    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&coop_per_sm, k_persistent<R, true, BATCH, false, true>, 128, 0));
     const uint32_t full_persist = uint32_t(sms) * uint32_t(std::max(tail_per_sm, 1));
     const uint32_t full_coop = uint32_t(sms) * uint32_t(std::max(coop_per_sm, 1));
     const uint32_t gen_per_sm = opts.generate_blocks_per_sm ? std::min<uint32_t>(opts.generate_blocks_per_sm, 32u) : 8u;
@@ -1232,7 +1232,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
                                                                    nullptr, nullptr, nullptr, nullptr, ho);
         HandOff coop;
         coop.coop = 1;
-        k_persistent<R, true, BATCH><<<side_coop_blocks, 128, 0, S[k].side>>>(
+        k_persistent<R, true, BATCH, false, true><<<side_coop_blocks, 128, 0, S[k].side>>>(
             Q, Q.ps.counters + C_SIDE_COOP_NEXT, Q.ps.q_handoff, Q.ps.counters + C_SIDE_COOP, ctx->mapped_dev, nullptr,
             nullptr, nullptr, nullptr, coop);
         GT_CUDA(cudaGetLastError());
@@ -1266,7 +1266,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
                                                       nullptr, ho);
         HandOff coop;
         coop.coop = 1;
-        k_persistent<R, true, BATCH><<<coop_blocks, 128, 0, s>>>(
+        k_persistent<R, true, BATCH, false, true><<<coop_blocks, 128, 0, s>>>(
             Q, Q.ps.counters + C_TAIL_COOP_NEXT, Q.ps.q_trace[1], Q.ps.counters + C_TAIL_COOP, nullptr, nullptr, nullptr,
             nullptr, nullptr, coop);
         GT_CUDA(cudaGetLastError());

@@ -154,6 +154,37 @@ template <class R> GT_DEV bool prim_hit(const SceneDev<R>& sc, uint32_t i, V3<R>
     }
 }
 
+// The closest hit of a scene of at most 32 primitives for one warp whose lanes all trace
+// the same ray (a path finished cooperatively): lane i tests leaf-order primitive i with
+// the traversal's own prim_hit, then a warp arg-min (ties to the lower index) replaces the
+// serial walk of the tree, whose dependent steps a lone warp cannot hide.  Only the
+// order of visits differs from the traversal: exactly equal distances may resolve to
+// another primitive.  Returns the primitive (all lanes) or -1; sets t_out on a hit.
+template <class R>
+GT_DEV int warp_closest(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, R tmax, R& t_out) {
+    const uint32_t lane = threadIdx.x & 31u;
+    R t = tmax;
+    int best = -1;
+    if (lane < sc.num_prims) {
+        R th;
+        if (prim_hit(sc, lane, o, d, time, tmin, tmax, th)) {
+            t = th;
+            best = int(lane);
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const R ot = __shfl_xor_sync(0xffffffffu, t, off);
+        const int ob = __shfl_xor_sync(0xffffffffu, best, off);
+        if (ob >= 0 && (best < 0 || ot < t || (ot == t && ob < best))) {
+            t = ot;
+            best = ob;
+        }
+    }
+    if (best >= 0) t_out = t;
+    return best;
+}
+
 struct TraceStats {
     unsigned long long node_tests, node_hits, leaf_visits, candidates, leaf_hits;
     uint32_t max_depth;

@@ -646,13 +646,16 @@ struct HandOff {
 // WORLD: a world with objects or participating media: every ray goes through world_hit
 // (whose media draw from the pixel's stream), and shadow queries are traced inside
 // integrate_bounce.
-template <class R, bool RESUME, bool BATCH = false, bool WORLD = false>
-__global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next, const uint32_t* queues,
+// COOP: the cooperative instantiation (one slot per warp, RESUME only), whose warps may
+// also intersect small scenes lane-parallel (warp_closest); kept apart so the one-slot-per-
+// lane launches keep their register budget.
+template <class R, bool RESUME, bool BATCH = false, bool WORLD = false, bool COOP = false>
+__global__ void __launch_bounds__(128, sizeof(R) == 8 ? 1 : (WORLD ? 3 : (BATCH ? 1 : 4))) k_persistent(Params<R> P, uint32_t* next, const uint32_t* queues,
                                                     const uint32_t* class_counts, const volatile uint32_t* cancel,
                                                     volatile uint32_t* progress, float* rgb, double* rgb64,
                                                     uint32_t* accepted, HandOff ho = HandOff()) {
     const uint32_t n = RESUME ? class_counts[0] : (BATCH ? P.frame_start[P.num_frames] : P.cam.width * P.cam.height);
-    const bool coop = RESUME && ho.coop != 0; // warp-uniform
+    const bool coop = RESUME && (COOP || ho.coop != 0); // warp-uniform
     // The camera of the pixel being rendered: the frame's in a batch, else the launch's.
     uint32_t frame = 0, local = 0;
     auto cam = [&]() -> const CamDev<R>& {
@@ -681,13 +684,13 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
 #pragma unroll
     for (uint32_t k = 0; k < NUM_COST_CLASSES; ++k) prefix[k + 1] = prefix[k] + (RESUME ? 0u : class_counts[k]);
     auto fetch = [&]() -> uint32_t {
-        if (cancel && *cancel) return n;
         uint32_t i;
-        if (coop) { // one slot per warp: every lane follows the same path
+        if (coop) { // one slot per warp: lane 0 decides for every lane, which then follow one path
             uint32_t v = 0;
-            if (lane_id() == 0) v = atomicAdd(next, 1u);
+            if (lane_id() == 0) v = (cancel && *cancel) ? n : atomicAdd(next, 1u);
             i = __shfl_sync(0xffffffffu, v, 0);
         } else {
+            if (cancel && *cancel) return n;
             i = atomicAdd(next, 1u);
         }
         if (i >= n) return n;
@@ -867,6 +870,8 @@ __global__ void __launch_bounds__(128) k_persistent(Params<R> P, uint32_t* next,
             const R rt = which >= 0 ? sh.time : p.time;
             if constexpr (WORLD) { // no query is ever pending here
                 prim = world_hit(P.sc, ro, rd, rt, R(kShadowAcne), g, wrec, &P.ps.counters[C_ERROR]) ? 0 : -1;
+            } else if (COOP && sizeof(R) == 4 && P.sc.num_prims <= 32u) { // warp-uniform
+                prim = warp_closest(P.sc, ro, rd, rt, R(kShadowAcne), inf, t);
             } else {
                 prim = traverse<R, false, false>(P.sc, ro, rd, rt, R(kShadowAcne), inf, t, nullptr,
                                                  &P.ps.counters[C_ERROR], which == 1);
