@@ -981,16 +981,15 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     // traces shadow queries in the reference's order of draws (accumulation resumes
     // wavefront state, which that variant does not keep).
     const bool world = P.sc.num_media != 0 || P.sc.num_objects != 0;
-    if (world && (accum || BATCH))
-        return fail(GT_ERR_UNSUPPORTED, "a scene with objects or media renders neither accumulated nor as a wavefront batch");
-    const bool persistent = (!BATCH && opts.schedule == GT_SCHEDULE_PERSISTENT && !accum) || world;
+    if (world && BATCH) return fail(GT_ERR_UNSUPPORTED, "a scene with objects or media does not render as a wavefront batch");
+    const bool persistent = (!BATCH && opts.schedule == GT_SCHEDULE_PERSISTENT && !accum) || (world && !accum);
     const bool host_out = BATCH || frame->device_buffers == 0;
     // Wavefront stripes: rows are dealt round-robin to K independent wavefronts on their
     // own streams, whose kernels then overlap on the GPU (each kernel alone leaves SMs
     // waiting on memory).
     uint32_t K = opts.stripes ? opts.stripes : 4u;
     K = std::max<uint32_t>(1u, std::min<uint32_t>({K, uint32_t(gt_context::kMaxStripes), img_h}));
-    if (persistent) K = 1;
+    if (persistent || world) K = 1;
     const uint32_t qcap = ((img_h + K - 1) / K) * cam.width;
     std::vector<Params<R>> SP(K);
     CamDev<R>* d_cams = nullptr;
@@ -1099,6 +1098,50 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         if (profile) {
             GT_CUDA(cudaEventRecord(z, st));
             ev.note(GT_KERNEL_OTHER, a, z);
+        }
+    }
+
+    if constexpr (!BATCH) {
+        if (world) { // accumulated world with objects or media: every pixel's chain continues from
+                     // the state just loaded in the RESUME mode of the persistent kernel's world variant
+            Params<R> Q = SP[0];
+            uint32_t* list = Q.ps.q_handoff; // n entries: one stripe
+            uint32_t* count = Q.ps.counters + C_TAIL;
+            GT_CUDA(cudaMemsetAsync(d_next, 0, sizeof(uint32_t), st));
+            k_list_all<<<slot_blocks, threads, 0, st>>>(list, n, count);
+            GT_CUDA(cudaGetLastError());
+            int per_sm = 0;
+            GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<R, true, false, true>, 128, 0));
+            const uint32_t blocks =
+                std::max<uint32_t>(1u, std::min<uint32_t>(uint32_t(sms) * uint32_t(std::max(per_sm, 1)), (n + 127) / 128));
+            cudaEvent_t a = nullptr, z = nullptr;
+            if (profile) GT_CUDA(ev.pair(a, z));
+            if (profile) GT_CUDA(cudaEventRecord(a, st));
+            k_persistent<R, true, false, true><<<blocks, 128, 0, st>>>(Q, d_next, list, count, nullptr, nullptr, nullptr,
+                                                                       nullptr, nullptr);
+            GT_CUDA(cudaGetLastError());
+            klaunch[GT_KERNEL_PERSISTENT] += 2;
+            if (profile) {
+                GT_CUDA(cudaEventRecord(z, st));
+                ev.note(GT_KERNEL_PERSISTENT, a, z);
+            }
+            k_resolve<R, false><<<slot_blocks, threads, 0, st>>>(P, o_rgb, o_rgb64, o_acc);
+            GT_CUDA(cudaGetLastError());
+            if (opts.aovs && (o_alb || o_nrm)) {
+                k_aov<R><<<slot_blocks, threads, 0, st>>>(P, o_alb, o_nrm);
+                GT_CUDA(cudaGetLastError());
+                klaunch[GT_KERNEL_OTHER] += 1;
+            }
+            k_accum_store<R><<<slot_blocks, threads, 0, st>>>(P, accum->rng, static_cast<R4<R>*>(accum->sum),
+                                                              static_cast<R4<R>*>(accum->comp), accum->accepted);
+            GT_CUDA(cudaGetLastError());
+            klaunch[GT_KERNEL_OTHER] += 2;
+            rc = finish_render<R>(ctx, P, frame, opts, host_out, n, o_rgb, o_rgb64, o_acc, o_alb, o_nrm, ev, kms, klaunch, 0);
+            if (rc == GT_OK) {
+                accum->samples += add_samples;
+                accum->seed = cam.desc.rng_seed;
+            }
+            return rc;
         }
     }
 

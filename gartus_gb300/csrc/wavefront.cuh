@@ -936,6 +936,12 @@ __global__ void k_accum_store(Params<R> P, uint64_t* rng, R4<R>* sum, R4<R>* com
     }
 }
 
+// Every slot in order, and their number (a RESUME pass over the whole image).
+static __global__ void k_list_all(uint32_t* list, uint32_t n, uint32_t* count) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) list[i] = i;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *count = n;
+}
+
 // Lists the wavefront slots that have not finished their pixel (for the RESUME pass).
 template <class R> __global__ void __launch_bounds__(256) k_collect(Params<R> P, uint32_t* list, uint32_t* count) {
     const uint32_t n = P.ps.local_n;

@@ -821,10 +821,21 @@ def test_media_batch_and_unsupported(gpu_context, precision):
             np.testing.assert_array_equal(img.pixels64, one.pixels64)
         else:
             assert _divergent(img.pixels, one.pixels.astype(np.float64)) <= 0.05 * img.pixels.shape[0] * img.pixels.shape[1]
+    # accumulation: 3 + 5 samples on one accumulator give the 8-sample render (the streams
+    # continue in the persistent kernel's world variant)
+    base = _smoke_camera(24, 1)
+    full = PathTracer(base.with_samples_per_pixel(8), precision=precision, context=gpu_context
+                      ).render_with_lights_hdr_image(scene, lights, want64=precision == "f64")
     acc = Accumulator(24, 24, precision, gpu_context)
-    with pytest.raises(GartusError) as e:
-        PathTracer(cams[0], context=gpu_context).render_accumulate(scene, acc, 1, lights=lights)
-    assert e.value.status == abi.GT_ERR_UNSUPPORTED
+    pt = PathTracer(base, context=gpu_context)
+    pt.render_accumulate(scene, acc, 3, lights=lights)
+    img = pt.render_accumulate(scene, acc, 5, lights=lights)
+    assert acc.samples == 8
+    np.testing.assert_array_equal(img.accepted, full.accepted)
+    if precision == "f64":
+        np.testing.assert_array_equal(img.pixels64, full.pixels64)
+    else:
+        assert _divergent(img.pixels, full.pixels.astype(np.float64)) <= 0.05 * 24 * 24
 
 
 def _bouncing_spheres(frame: int, n: int = 300):
@@ -1036,9 +1047,10 @@ def test_world_edge_cases(gpu_context):
     bad[0]["normal_map"] = 9
     with pytest.raises(GartusError):
         _SceneHandle(gpu_context, prims, bad, 4, abi.GT_BVH_REFERENCE_SAH, scene.images(), (), meshes, objects)
-    # accumulating a world with objects or media is refused
+    # a world with objects and media accumulates: 2 + 2 samples give the 4-sample render
     from gartus_gb300.raytracing import Accumulator
-    acc_obj = Accumulator(32, 21, "f32", gpu_context)
-    with pytest.raises(GartusError) as e:
-        PathTracer(cam, context=gpu_context).render_accumulate(scene, acc_obj, 1)
-    assert e.value.status == abi.GT_ERR_UNSUPPORTED
+    acc_obj = Accumulator(32, 21, "f64", gpu_context)
+    pt = PathTracer(cam.with_samples_per_pixel(1), context=gpu_context)
+    pt.render_accumulate(scene, acc_obj, 2)
+    two = pt.render_accumulate(scene, acc_obj, 2)
+    np.testing.assert_array_equal(two.pixels64, img.pixels64)
