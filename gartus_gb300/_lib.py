@@ -49,6 +49,10 @@ def _declare(L: C.CDLL) -> None:
                                C.c_void_p, P(abi.gt_bvh_stats)]),
         "gt_trace_primary": (st, [C.c_void_p, P(abi.gt_camera_desc), C.c_uint32, C.c_void_p, C.c_void_p,
                                   P(abi.gt_bvh_stats)]),
+        "gt_trace_rays_f32": (st, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_double, C.c_double, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, P(abi.gt_trace_report)]),
+        "gt_trace_primary_f32": (st, [C.c_void_p, P(abi.gt_camera_desc), C.c_uint32, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, P(abi.gt_trace_report)]),
         "gt_render_noalloc": (st, [C.c_void_p, C.c_void_p, C.c_void_p, P(abi.gt_camera_desc), C.c_void_p,
                                    C.c_void_p]),
         "gt_render_batch": (st, [C.c_void_p, C.c_void_p, C.c_void_p, P(abi.gt_frame_job), C.c_uint32,
@@ -105,7 +109,8 @@ EXPORTED_SYMBOLS = [
     "gt_abi_version", "gt_last_error", "gt_camera_default", "gt_camera_image_size", "gt_context_create",
     "gt_context_destroy", "gt_scene_create", "gt_scene_destroy", "gt_scene_bvh_node_count", "gt_scene_update_primitives",
     "gt_scene_emissive_targets", "gt_lights_create", "gt_lights_destroy", "gt_environment_create",
-    "gt_environment_destroy", "gt_render", "gt_trace_rays", "gt_trace_primary", "gt_render_noalloc",
+    "gt_environment_destroy", "gt_render", "gt_trace_rays", "gt_trace_primary", "gt_trace_rays_f32",
+    "gt_trace_primary_f32", "gt_render_noalloc",
     "gt_render_batch", "gt_accumulator_create", "gt_accumulator_destroy", "gt_accumulator_samples",
     "gt_accumulator_save", "gt_accumulator_load", "gt_render_accumulate", "gt_autotune", "gt_denoiser_create",
     "gt_denoiser_destroy", "gt_denoiser_param_count", "gt_denoiser_get_params", "gt_denoiser_set_params",

@@ -41,6 +41,8 @@ GT_MAT_HENYEY_GREENSTEIN = 6
 
 GT_BVH_REFERENCE_SAH = 0
 GT_BVH_GPU_LBVH = 1
+GT_F32_TREE_WIDE = 0
+GT_F32_TREE_BINARY = 1
 
 # gt_texture_kind
 GT_TEX_SOLID = 0
@@ -167,7 +169,7 @@ class gt_scene_desc(C.Structure):
         ("media", C.POINTER(gt_medium)),
         ("meshes", C.POINTER(gt_mesh)),
         ("num_objects", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("f32_tree", C.c_uint32),
         ("objects", C.POINTER(gt_object)),
     ]
 
@@ -315,6 +317,21 @@ class gt_bvh_stats(C.Structure):
         return {name: int(getattr(self, name)) for name, _ in self._fields_}
 
 
+class gt_trace_report(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32),
+        ("tree", C.c_uint32),
+        ("rays", C.c_uint64),
+        ("refined", C.c_uint64),
+        ("changed", C.c_uint64),
+        ("wide_nodes", C.c_uint32),
+        ("wide_depth", C.c_uint32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: int(getattr(self, name)) for name, _ in self._fields_ if name != "struct_size"}
+
+
 class gt_autotune_report(C.Structure):
     _fields_ = [
         ("struct_size", C.c_uint32),
@@ -340,5 +357,5 @@ class gt_denoise_input(C.Structure):
 STRUCTS = [
     gt_geometry, gt_primitive, gt_material, gt_image, gt_medium, gt_mesh, gt_object, gt_scene_desc, gt_light_target, gt_environment_desc,
     gt_camera_desc, gt_render_opts, gt_frame, gt_frame_job, gt_bvh_stats, gt_render_stats, gt_denoise_input,
-    gt_autotune_report,
+    gt_autotune_report, gt_trace_report,
 ]

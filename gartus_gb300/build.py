@@ -36,7 +36,7 @@ UNITS = [
     ("denoise.cu", ["-fmad=true"]),
     ("lbvh.cu", ["-fmad=true"]),
 ]
-CXX_UNITS = ["bvh_build.cpp", "scene_tables.cpp"]
+CXX_UNITS = ["bvh_build.cpp", "scene_tables.cpp", "wide_bvh.cpp"]
 
 
 def _nvcc() -> str:

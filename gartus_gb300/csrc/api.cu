@@ -359,8 +359,10 @@ gt_status gt_scene_create(gt_context* ctx, const gt_scene_desc* d, gt_scene** ou
     std::lock_guard<std::mutex> lock(ctx->mu);
     const uint32_t builder = d->struct_size >= sizeof(gt_scene_desc) ? d->bvh_builder : 0u;
     if (builder > GT_BVH_GPU_LBVH) return fail(GT_ERR_INVALID_ARG, "unknown BVH builder");
+    if (d->f32_tree > GT_F32_TREE_BINARY) return fail(GT_ERR_INVALID_ARG, "unknown f32 tree");
     auto* s = new gt_scene();
     s->ctx = ctx;
+    s->f32_tree = d->f32_tree;
     s->prims.assign(d->primitives, d->primitives + d->num_primitives);
     s->mats.assign(d->materials, d->materials + d->num_materials);
     s->bvh_builder = builder;
@@ -936,27 +938,68 @@ gt_status gt_trace_rays(gt_scene* s, const double* rays, uint32_t count, double 
     GT_GUARD_END
 }
 
-gt_status gt_trace_primary(gt_scene* s, const gt_camera_desc* c, uint32_t stride, int32_t* ids, double* t,
-                           gt_bvh_stats* stats) {
-    GT_GUARD_BEGIN
-    if (!s || !c || !ids) return fail(GT_ERR_INVALID_ARG, "null argument");
-    gt_status rc = validate_camera(*c);
-    if (rc != GT_OK) return rc;
-    if (stride == 0) stride = 1;
-    CamHost cam = init_camera(*c, false);
+// Probe rays RayCamera::ray_for_pixel (camera.rs:1641-1653) in f64 for every `stride`-th
+// pixel, row-major: {origin, direction, time} per ray.
+static std::vector<double> primary_rays(const gt_camera_desc& c, uint32_t stride) {
+    CamHost cam = init_camera(c, false);
     std::vector<double> rays;
     for (uint32_t y = 0; y < cam.height; y += stride)
         for (uint32_t x = 0; x < cam.width; x += stride) {
-            // RayCamera::ray_for_pixel (camera.rs:1641-1653), in f64.
             double pc[3];
             for (int k = 0; k < 3; ++k) pc[k] = (cam.pixel00[k] + cam.du[k] * double(x)) + cam.dv[k] * double(y);
             rays.push_back(cam.center[0]);
             rays.push_back(cam.center[1]);
             rays.push_back(cam.center[2]);
             for (int k = 0; k < 3; ++k) rays.push_back(pc[k] - cam.center[k]);
-            rays.push_back(c->shutter_start);
+            rays.push_back(c.shutter_start);
         }
+    return rays;
+}
+
+gt_status gt_trace_primary(gt_scene* s, const gt_camera_desc* c, uint32_t stride, int32_t* ids, double* t,
+                           gt_bvh_stats* stats) {
+    GT_GUARD_BEGIN
+    if (!s || !c || !ids) return fail(GT_ERR_INVALID_ARG, "null argument");
+    gt_status rc = validate_camera(*c);
+    if (rc != GT_OK) return rc;
+    const std::vector<double> rays = primary_rays(*c, stride ? stride : 1u);
     return gt_trace_rays(s, rays.data(), uint32_t(rays.size() / 7), 0.001, INFINITY, ids, t, stats);
+    GT_GUARD_END
+}
+
+gt_status gt_trace_rays_f32(gt_scene* s, const double* rays, uint32_t count, double tmin, double tmax, int32_t* ids,
+                            double* t, uint8_t* refined, gt_trace_report* report) {
+    GT_GUARD_BEGIN
+    if (!s || (count && (!rays || !ids))) return fail(GT_ERR_INVALID_ARG, "null argument");
+    if (report && report->struct_size < sizeof(gt_trace_report))
+        return fail(GT_ERR_INVALID_ARG, "report struct_size too small");
+    if (report) {
+        std::memset(reinterpret_cast<char*>(report) + sizeof(uint32_t), 0, sizeof(gt_trace_report) - sizeof(uint32_t));
+        report->rays = count;
+    }
+    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    cudaError_t ce = cudaSetDevice(s->ctx->device);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
+    if (s->prims.empty()) {
+        for (uint32_t i = 0; i < count; ++i) {
+            ids[i] = -1;
+            if (t) t[i] = 0.0;
+            if (refined) refined[i] = 0;
+        }
+        return GT_OK;
+    }
+    return trace_rays_f32(s, rays, count, tmin, tmax, ids, t, refined, report);
+    GT_GUARD_END
+}
+
+gt_status gt_trace_primary_f32(gt_scene* s, const gt_camera_desc* c, uint32_t stride, int32_t* ids, double* t,
+                               uint8_t* refined, gt_trace_report* report) {
+    GT_GUARD_BEGIN
+    if (!s || !c || !ids) return fail(GT_ERR_INVALID_ARG, "null argument");
+    gt_status rc = validate_camera(*c);
+    if (rc != GT_OK) return rc;
+    const std::vector<double> rays = primary_rays(*c, stride ? stride : 1u);
+    return gt_trace_rays_f32(s, rays.data(), uint32_t(rays.size() / 7), 0.001, INFINITY, ids, t, refined, report);
     GT_GUARD_END
 }
 

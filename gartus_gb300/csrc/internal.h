@@ -53,6 +53,8 @@ template <class R> struct GpuScene {
     PrimRec<R>* prims = nullptr;
     uint2* meta = nullptr;
     Node<R>* nodes = nullptr;
+    WideNode* wnodes = nullptr; // f32 only: the wide tree (null when the scene has none)
+    uint32_t wide_depth = 0, wide_nodes = 0;
     MatDev<R>* mats = nullptr;
     PerlinDev<R>* perlin = nullptr; // one table set per noise-textured material
     SceneDev<R> view{};
@@ -150,6 +152,7 @@ struct gt_scene {
     std::vector<gt::MeshHost> meshes;
     std::vector<gt_object> objects;
     uint32_t bvh_builder = GT_BVH_REFERENCE_SAH;
+    uint32_t f32_tree = GT_F32_TREE_WIDE;
     uint32_t leaf_size = 4;
     bool bvh_ready = false; // `bvh` has been built (eagerly for the reference builder)
     gt::BuiltBvh bvh;
@@ -193,6 +196,8 @@ gt_status render_batch_f32(gt_scene* s, const gt_lights* l, gt_environment* e, c
                            const gt_render_opts& opts, gt_frame* const* frames);
 gt_status render_batch_f64(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost* cams, uint32_t count,
                            const gt_render_opts& opts, gt_frame* const* frames);
+gt_status trace_rays_f32(gt_scene* s, const double* rays, uint32_t count, double tmin, double tmax, int32_t* ids,
+                         double* t, uint8_t* refined, gt_trace_report* rep);
 gt_status trace_rays_f64(gt_scene* s, const double* rays, uint32_t count, double tmin, double tmax,
                          int32_t* ids, double* t, gt_bvh_stats* stats);
 void free_gpu_f32(gt_scene* s);

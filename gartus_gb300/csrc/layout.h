@@ -10,6 +10,7 @@
 #include <stdint.h>
 
 #include "../../include/gartus_gpu.h"
+#include "wide_bvh.h"
 
 #if defined(__CUDACC__)
 #define GT_HD __host__ __device__
@@ -176,6 +177,9 @@ template <class R> struct SceneDev {
     int32_t root_count;
     uint32_t num_prims;
     uint32_t num_nodes;
+    // f32 only: the eight-wide compressed tree over the same leaves (leaf slots are the
+    // primitive order above), or null to traverse `nodes`.
+    const WideNode* wnodes;
 };
 
 template <class R> struct MeshDev {

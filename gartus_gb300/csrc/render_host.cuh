@@ -66,6 +66,7 @@ template <class R> void free_gpu(gt_scene* s) {
     cudaFree(g.prims);
     cudaFree(g.meta);
     cudaFree(g.nodes);
+    cudaFree(g.wnodes);
     cudaFree(g.mats);
     cudaFree(g.perlin);
     cudaFree(g.texels);
@@ -181,10 +182,11 @@ inline uint32_t medium_parts(const gt_medium& m, gt_geometry* out) {
 
 // A reference-layout tree as device nodes: internal nodes renumbered densely in pre-order,
 // leaf children as links (~first, count); also the root's box and link (a root box no ray
-// enters for an empty tree).
+// enters for an empty tree).  `slot_of` maps leaf slots to the device primitive order when
+// that order is the wide tree's (each leaf's primitives stay consecutive and in order).
 template <class R>
 void flatten_tree(const BuiltBvh& bvh, std::vector<Node<R>>& nodes, R* root_box, int32_t& root_link,
-                  int32_t& root_count) {
+                  int32_t& root_count, const std::vector<uint32_t>* slot_of = nullptr) {
     std::vector<int32_t> internal_id(bvh.nodes.size(), -1);
     int32_t ni = 0;
     for (size_t i = 0; i < bvh.nodes.size(); ++i)
@@ -192,7 +194,7 @@ void flatten_tree(const BuiltBvh& bvh, std::vector<Node<R>>& nodes, R* root_box,
     nodes.assign(size_t(ni), Node<R>());
     auto link_of = [&](uint32_t child, int32_t& link, int32_t& count) {
         const BuildNode& c = bvh.nodes[child];
-        link = c.leaf ? ~int32_t(c.first) : internal_id[child];
+        link = c.leaf ? ~int32_t(slot_of ? (*slot_of)[c.first] : c.first) : internal_id[child];
         count = c.leaf ? int32_t(c.count) : 0;
     };
     for (size_t i = 0; i < bvh.nodes.size(); ++i) {
@@ -357,6 +359,17 @@ template <class R> gt_status upload_scene(gt_scene* s) {
     }
     const BuiltBvh& bvh = s->bvh;
     const size_t n = s->prims.size();
+    // The f32 path of a reference-SAH scene traverses the eight-wide tree collapsed from it;
+    // its primitives then lie in the wide tree's leaf order (the binary tree's leaves keep
+    // their primitives consecutive in that order, so both trees index one array).
+    WideBvh wide;
+    const bool use_wide =
+        sizeof(R) == 4 && !gpu_bvh && s->f32_tree == GT_F32_TREE_WIDE && build_wide_bvh(bvh, wide);
+    std::vector<uint32_t> slot_of;
+    if (use_wide) {
+        slot_of.resize(n);
+        for (size_t j = 0; j < n; ++j) slot_of[wide.order[j]] = uint32_t(j);
+    }
     std::vector<PrimRec<R>> recs(n);
     std::vector<uint2> meta(n);
     std::vector<float> boxes(gpu_bvh ? n * 6 : 0); // f32 bounds, rounded outward
@@ -377,7 +390,7 @@ template <class R> gt_status upload_scene(gt_scene* s) {
         }
     }
     for (size_t j = 0; j < n; ++j) {
-        const uint32_t pi = gpu_bvh ? uint32_t(j) : bvh.order[j];
+        const uint32_t pi = gpu_bvh ? uint32_t(j) : bvh.order[use_wide ? wide.order[j] : j];
         const gt_primitive& p = s->prims[pi];
         const uint32_t kind = pack_prim<R>(p.geometry, recs[j].v);
         if (kind == kBadKind) return fail(GT_ERR_INVALID_ARG, "unknown geometry kind");
@@ -387,7 +400,7 @@ template <class R> gt_status upload_scene(gt_scene* s) {
     std::vector<Node<R>> nodes;
     R root_box[6];
     int32_t root_link = ~0, root_count = 0;
-    if (!gpu_bvh) flatten_tree<R>(bvh, nodes, root_box, root_link, root_count);
+    if (!gpu_bvh) flatten_tree<R>(bvh, nodes, root_box, root_link, root_count, use_wide ? &slot_of : nullptr);
     std::vector<MatDev<R>> mats(s->mats.size());
     std::vector<PerlinDev<R>> perlin;
     std::vector<size_t> perlin_of; // material index of each table set
@@ -474,6 +487,7 @@ template <class R> gt_status upload_scene(gt_scene* s) {
     GT_CUDA(cudaMalloc(&g.meta, std::max<size_t>(n, 1) * sizeof(uint2)));
     GT_CUDA(cudaMalloc(&g.nodes, std::max<size_t>(nodes.size(), 1) * sizeof(Node<R>)));
     GT_CUDA(cudaMalloc(&g.mats, std::max<size_t>(mats.size(), 1) * sizeof(MatDev<R>)));
+    if (use_wide) GT_CUDA(cudaMalloc(&g.wnodes, wide.nodes.size() * sizeof(WideNode)));
     cudaStream_t st = s->ctx->stream;
     if (n) {
         GT_CUDA(cudaMemcpyAsync(g.prims, recs.data(), n * sizeof(PrimRec<R>), cudaMemcpyHostToDevice, st));
@@ -481,6 +495,9 @@ template <class R> gt_status upload_scene(gt_scene* s) {
     }
     if (!nodes.empty())
         GT_CUDA(cudaMemcpyAsync(g.nodes, nodes.data(), nodes.size() * sizeof(Node<R>), cudaMemcpyHostToDevice, st));
+    if (use_wide)
+        GT_CUDA(cudaMemcpyAsync(g.wnodes, wide.nodes.data(), wide.nodes.size() * sizeof(WideNode),
+                                cudaMemcpyHostToDevice, st));
     if (!mats.empty())
         GT_CUDA(cudaMemcpyAsync(g.mats, mats.data(), mats.size() * sizeof(MatDev<R>), cudaMemcpyHostToDevice, st));
     if (!perlin.empty())
@@ -504,6 +521,9 @@ template <class R> gt_status upload_scene(gt_scene* s) {
     v.num_media = uint32_t(mdev.size());
     v.num_prims = uint32_t(n);
     v.num_nodes = uint32_t(nodes.size());
+    v.wnodes = use_wide ? g.wnodes : nullptr;
+    g.wide_depth = use_wide ? wide.depth : 0u;
+    g.wide_nodes = use_wide ? uint32_t(wide.nodes.size()) : 0u;
     if (gpu_bvh && n > 0) {
         cudaFree(g.nodes); // the device builder allocates its own node array
         g.nodes = nullptr;
@@ -1210,8 +1230,10 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     GT_CUDA(ev.get(init_done));
     GT_CUDA(cudaEventRecord(init_done, st));
     for (uint32_t k = 0; k < K; ++k) {
-        S[k].st = ctx->stripe_stream[k];
-        S[k].side = ctx->stripe_side[k];
+        // Profile mode issues every launch on the context stream, so launches run one at a
+        // time and each kernel's event pair measures that kernel alone.
+        S[k].st = profile ? st : ctx->stripe_stream[k];
+        S[k].side = profile ? st : ctx->stripe_side[k];
         GT_CUDA(cudaStreamWaitEvent(S[k].st, init_done, 0));
         if (!profile) {
             // Reuse the stripe's graph from the previous render when nothing it captured

@@ -192,13 +192,336 @@ struct TraceStats {
 
 constexpr int kStackSize = 64;
 
+// ----------------------------------------------------------- near-decision test
+// Check mode only: whether f32 rounding could change primitive i's hit decision for this
+// ray — its hit point within a few dozen f32 ulps (of the coordinates involved, scaled up
+// at grazing angles) of an edge, a determinant or plane angle near the reference's
+// rejection threshold, a sphere root near the tangent, or a distance near t_min.  Rays
+// with such a candidate (up to `tlim`) are re-traced in f64.
+template <class R> GT_DEV R amax3(V3<R> a) {
+    return Num<R>::fmax(Num<R>::fmax(Num<R>::fabs(a.x), Num<R>::fabs(a.y)), Num<R>::fabs(a.z));
+}
+template <class R>
+GT_DEV bool prim_near(const SceneDev<R>& sc, uint32_t i, V3<R> o, V3<R> d, R time, R tmin, R tlim) {
+    constexpr float kUlps = 64.0f * 5.9604645e-8f; // 64 units of 2^-24
+    const uint32_t kind = __ldg(&sc.meta[i].x) & 7u;
+    const R* rec = sc.prims[i].v;
+    const R dl = Num<R>::sqrt(len2(d));
+    if (!(dl > R(0))) return false;
+    if (kind == K_TRIANGLE) {
+        const V3<R> p0 = xyz(ldg4(rec)), e1 = xyz(ldg4(rec + 4)), e2 = xyz(ldg4(rec + 8));
+        const V3<R> pvec = cross(d, e2);
+        const R det = dot(e1, pvec);
+        const R nl = Num<R>::sqrt(len2(cross(e1, e2)));
+        if (Num<R>::fabs(det) < R(4e-10)) return true;
+        const R inv = R(1) / det;
+        const V3<R> tv = o - p0;
+        const R u = dot(tv, pvec) * inv;
+        const V3<R> qv = cross(tv, e1);
+        const R v = dot(d, qv) * inv;
+        const R t = dot(e2, qv) * inv;
+        const R w = R(1) - u - v;
+        const R graze = nl * dl / Num<R>::fabs(det); // 1 / |cos| of the ray against the plane
+        const R tol = R(kUlps) * (amax3(o) + Num<R>::fabs(t) * amax3(d) + amax3(p0)) * R(1.7320508) * graze;
+        const R hu = nl / Num<R>::sqrt(len2(e2)), hv = nl / Num<R>::sqrt(len2(e1)), hw = nl / Num<R>::sqrt(len2(e2 - e1));
+        const R du = u * hu, dv = v * hv, dw = w * hw;
+        if (!(du > -tol && dv > -tol && dw > -tol)) return false;
+        const R ttol = tol / dl;
+        if (!(t > tmin - ttol && t < tlim + ttol)) return false;
+        const R edge = Num<R>::fmin(Num<R>::fmin(Num<R>::fabs(du), Num<R>::fabs(dv)), Num<R>::fabs(dw));
+        return edge < tol || Num<R>::fabs(t - tmin) < ttol;
+    }
+    if (kind == K_SPHERE || kind == K_MOVING) {
+        R4<R> sp = ldg4(rec);
+        V3<R> c = xyz(sp);
+        if (kind == K_MOVING) c = c + xyz(ldg4(rec + 4)) * time;
+        const V3<R> oc = c - o;
+        const R a = len2(d);
+        const R h = dot(d, oc);
+        const R l2 = len2(oc);
+        const R cc = l2 - sp.w * sp.w;
+        const R disc = h * h - a * cc;
+        const R scale = h * h + a * (l2 + sp.w * sp.w);
+        const R ttol = R(kUlps) * (Num<R>::fabs(h) + Num<R>::sqrt(Num<R>::fabs(disc)) + Num<R>::sqrt(scale)) / a +
+                       R(kUlps) * (amax3(o) + amax3(c) + Num<R>::fabs(sp.w)) / dl;
+        if (Num<R>::fabs(disc) <= R(kUlps) * scale) { // tangent: both roots near h / a
+            const R tm = h / a;
+            return tm > tmin - ttol && tm < tlim + ttol;
+        }
+        if (disc < R(0)) return false;
+        const R sq = Num<R>::sqrt(disc);
+        const R r1 = (h - sq) / a, r2 = (h + sq) / a;
+        return Num<R>::fabs(r1 - tmin) < ttol || Num<R>::fabs(r2 - tmin) < ttol;
+    }
+    if (kind == K_QUAD) {
+        R4<R> A = ldg4(rec), B = ldg4(rec + 4), Cq = ldg4(rec + 8), E = ldg4(rec + 12);
+        const V3<R> corner = xyz(A), u = xyz(B), v = xyz(Cq), w = xyz(E), n = V3<R>{B.w, Cq.w, E.w};
+        const R denom = dot(n, d);
+        if (Num<R>::fabs(denom) < R(2e-8)) return true;
+        const R t = (A.w - dot(n, o)) / denom;
+        const V3<R> planar = (o + d * t) - corner;
+        const R al = dot(w, cross(planar, v));
+        const R be = dot(w, cross(u, planar));
+        const R uxv = R(1) / Num<R>::sqrt(len2(w));
+        const R ha = uxv / Num<R>::sqrt(len2(v)), hb = uxv / Num<R>::sqrt(len2(u));
+        const R graze = dl / Num<R>::fabs(denom);
+        const R tol = R(kUlps) * (amax3(o) + Num<R>::fabs(t) * amax3(d) + amax3(corner)) * R(1.7320508) * graze;
+        const R d0 = al * ha, d1 = (R(1) - al) * ha, d2 = be * hb, d3 = (R(1) - be) * hb;
+        if (!(d0 > -tol && d1 > -tol && d2 > -tol && d3 > -tol)) return false;
+        const R ttol = tol / dl;
+        if (!(t > tmin - ttol && t < tlim + ttol)) return false;
+        const R edge = Num<R>::fmin(Num<R>::fmin(Num<R>::fabs(d0), Num<R>::fabs(d1)),
+                                    Num<R>::fmin(Num<R>::fabs(d2), Num<R>::fabs(d3)));
+        return edge < tol || Num<R>::fabs(t - tmin) < ttol;
+    }
+    return false;
+}
+
+// Estimated absolute error of the f32 distance t at which ray (o, d) meets primitive i
+// (eight ulps of the quantities the distance is computed from: large for a big sphere
+// seen at a distance, whose root suffers cancellation, and at grazing angles).
+template <class R> GT_DEV R prim_t_err(const SceneDev<R>& sc, uint32_t i, V3<R> o, V3<R> d, R time, R t) {
+    constexpr float kUlps = 8.0f * 5.9604645e-8f;
+    const uint32_t kind = __ldg(&sc.meta[i].x) & 7u;
+    const R* rec = sc.prims[i].v;
+    const R dl = Num<R>::sqrt(len2(d));
+    const R pos = amax3(o) + Num<R>::fabs(t) * amax3(d);
+    if (kind == K_SPHERE || kind == K_MOVING) {
+        R4<R> sp = ldg4(rec);
+        V3<R> c = xyz(sp);
+        if (kind == K_MOVING) c = c + xyz(ldg4(rec + 4)) * time;
+        const V3<R> oc = c - o;
+        const R a = len2(d), h = dot(d, oc), l2 = len2(oc);
+        const R disc = Num<R>::fabs(h * h - a * (l2 - sp.w * sp.w));
+        const R ddisc = R(kUlps) * (h * h + a * (l2 + sp.w * sp.w));
+        const R dh = R(kUlps) * dl * (Num<R>::sqrt(l2) + amax3(c));
+        return (dh + ddisc / (R(2) * Num<R>::sqrt(Num<R>::fmax(disc, ddisc)))) / a + R(kUlps) * (pos + amax3(c)) / dl;
+    }
+    if (kind == K_TRIANGLE) {
+        const V3<R> p0 = xyz(ldg4(rec)), e1 = xyz(ldg4(rec + 4)), e2 = xyz(ldg4(rec + 8));
+        const R det = Num<R>::fabs(dot(e1, cross(d, e2)));
+        const R graze = Num<R>::sqrt(len2(cross(e1, e2))) * dl / Num<R>::fmax(det, R(1e-30));
+        return R(kUlps) * (pos + amax3(p0)) * R(1.7320508) * graze / dl;
+    }
+    if (kind == K_QUAD) {
+        R4<R> A = ldg4(rec), B = ldg4(rec + 4), Cq = ldg4(rec + 8), E = ldg4(rec + 12);
+        const V3<R> n = V3<R>{B.w, Cq.w, E.w};
+        const R denom = Num<R>::fmax(Num<R>::fabs(dot(n, d)), R(1e-30));
+        return R(kUlps) * (Num<R>::fabs(A.w) + amax3(o) + pos + amax3(xyz(A))) * R(1.7320508) / denom;
+    }
+    return R(0);
+}
+
+// Check mode state of one ray: whether a near decision was seen, and the estimated error
+// of the closest distance so far.
+template <class R> struct CheckState {
+    bool near;
+    R best_err;
+};
+
+// Check mode's culling distance: boxes are visited up to this far beyond the closest hit,
+// so that candidates whose distance may tie with it within f32 error are tested.
+template <class R> GT_DEV R check_limit(R closest, R best_err) {
+    return closest + Num<R>::fabs(closest) * R(0.00390625) + R(4) * best_err;
+}
+
+// One leaf primitive against the running closest hit.  Rendering: the reference's
+// interval (t_min, closest).  Check mode: the same decision (a primitive replaces the
+// closest only when nearer), plus the near flag when the two distances lie within their
+// estimated f32 errors (or 2^-16 relative) of each other, and for near-boundary candidates.
+template <class R, bool CHECK>
+GT_DEV bool leaf_test(const SceneDev<R>& sc, uint32_t i, V3<R> o, V3<R> d, R time, R tmin, R& closest,
+                      CheckState<R>* ck) {
+    R t;
+    if constexpr (!CHECK) {
+        if (prim_hit(sc, i, o, d, time, tmin, closest, t)) {
+            closest = t;
+            return true;
+        }
+        return false;
+    } else {
+        bool nearer = false;
+        const R inf = Num<R>::inf();
+        if (prim_hit(sc, i, o, d, time, tmin, inf, t)) {
+            const R e = prim_t_err(sc, i, o, d, time, t);
+            const R window = R(2) * (e + ck->best_err) + Num<R>::fabs(t) * R(1.52587890625e-5);
+            if (t < closest) {
+                if (closest < inf && closest - t <= window) ck->near = true;
+                closest = t;
+                ck->best_err = e;
+                nearer = true;
+            } else if (t - closest <= window) {
+                ck->near = true;
+            }
+        }
+        if (!ck->near && prim_near(sc, i, o, d, time, tmin, check_limit(closest, ck->best_err))) ck->near = true;
+        return nearer;
+    }
+}
+
+// ----------------------------------------------------- eight-wide traversal (f32)
+// Byte k (0-3) of w as an exact float: 0x4B0000kk is 2^23 + kk.
+template <int K> GT_DEV float byte_f(uint32_t w) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | uint32_t(K))) - 8388608.0f;
+}
+
+// Closest (or, with any_hit, first) hit over the compressed wide tree, with the same
+// semantics as the binary walk below: the same leaf test and interval, boxes that never
+// cull a primitive the f32 child box contains.  Per node one box test of up to eight
+// children: plane q of axis a lies at p_a + q s_a, so its distance is q (s_a / d_a) +
+// (p_a - o_a) / d_a, one fused multiply-add per plane.  The second term's rounding
+// (relative to itself, not to the distance) is covered by widening it per node by 4 ulps
+// of its own size; the far distance is then widened by 1 + 2^-21 as in the binary test.
+// Children are visited nearest-octant first: hit internal children form a group (node
+// index of the first child, 8 bits in visiting order, the internal-slot mask) of which
+// the first is descended into and the rest wait on a stack of at most kWideStack groups;
+// hit leaf children's primitives are tested at once.
+template <bool CHECK>
+GT_DEV int traverse_wide(const SceneDev<float>& sc, V3<float> o, V3<float> d, float time, float tmin, float tmax,
+                         float& t_out, uint32_t* err, bool any_hit, CheckState<float>* ck) {
+    const RayT<float> rt = make_rayt(o, d);
+    float root_entry;
+    if (!hit_box(rt, sc.root_box, sc.root_box + 3, tmin, tmax, root_entry)) return -1;
+    const uint32_t oct = (rt.inv[0] < 0.0f ? 1u : 0u) | (rt.inv[1] < 0.0f ? 2u : 0u) | (rt.inv[2] < 0.0f ? 4u : 0u);
+    const bool any_par = rt.par[0] || rt.par[1] || rt.par[2];
+    uint2 stack[kWideStack];
+    int sp = 0;
+    uint32_t node = 0;
+    float closest = tmax;
+    int best = -1;
+    for (;;) {
+        const uint4* np = reinterpret_cast<const uint4*>(sc.wnodes + node);
+        const uint4 c0 = __ldg(np), c1 = __ldg(np + 1), c2 = __ldg(np + 2), c3 = __ldg(np + 3), c4 = __ldg(np + 4);
+        const float cull = CHECK ? check_limit(closest, ck->best_err) : closest;
+        // Per axis: scale over direction, and the origin term widened for near and far planes.
+        float ax[3], bn[3], bf[3];
+        const uint32_t pw[3] = {c0.x, c0.y, c0.z};
+        const float ov[3] = {o.x, o.y, o.z};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float sa = __uint_as_float(((c0.w >> (8 * a)) & 0xffu) << 23);
+            if (rt.par[a]) { // no distance bound from this axis; containment is tested below
+                ax[a] = 0.0f;
+                bn[a] = -Num<float>::inf();
+                bf[a] = Num<float>::inf();
+            } else {
+                ax[a] = sa * rt.inv[a];
+                const float b = (__uint_as_float(pw[a]) - ov[a]) * rt.inv[a];
+                const float pad = fabsf(b) * 2.3841858e-7f; // 4 ulps of b
+                bn[a] = b - pad;
+                bf[a] = b + pad;
+            }
+        }
+        // Near and far plane words per axis (qlo for a positive direction component).
+        const bool nx = rt.inv[0] < 0.0f, ny = rt.inv[1] < 0.0f, nz = rt.inv[2] < 0.0f;
+        const uint32_t nx0 = nx ? c3.z : c2.x, nx1 = nx ? c3.w : c2.y, fx0 = nx ? c2.x : c3.z, fx1 = nx ? c2.y : c3.w;
+        const uint32_t ny0 = ny ? c4.x : c2.z, ny1 = ny ? c4.y : c2.w, fy0 = ny ? c2.z : c4.x, fy1 = ny ? c2.w : c4.y;
+        const uint32_t nz0 = nz ? c4.z : c3.x, nz1 = nz ? c4.w : c3.y, fz0 = nz ? c3.x : c4.z, fz1 = nz ? c3.y : c4.w;
+        const uint32_t imask = c0.w >> 24;
+        const uint32_t meta0 = c1.z, meta1 = c1.w;
+        uint32_t hits = 0;
+#define GT_WIDE_SLOT(S, WN_X, WF_X, WN_Y, WF_Y, WN_Z, WF_Z)                                                  \
+    {                                                                                                     \
+        const float tnx = fmaf(byte_f<(S)&3>(WN_X), ax[0], bn[0]), tfx = fmaf(byte_f<(S)&3>(WF_X), ax[0], bf[0]); \
+        const float tny = fmaf(byte_f<(S)&3>(WN_Y), ax[1], bn[1]), tfy = fmaf(byte_f<(S)&3>(WF_Y), ax[1], bf[1]); \
+        const float tnz = fmaf(byte_f<(S)&3>(WN_Z), ax[2], bn[2]), tfz = fmaf(byte_f<(S)&3>(WF_Z), ax[2], bf[2]); \
+        const float en = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));                                        \
+        const float ex = fminf(fminf(fminf(tfx, tfy), tfz) * 1.00000048f, cull);                           \
+        hits |= (ex > en ? 1u : 0u) << (S);                                                               \
+    }
+        GT_WIDE_SLOT(0, nx0, fx0, ny0, fy0, nz0, fz0)
+        GT_WIDE_SLOT(1, nx0, fx0, ny0, fy0, nz0, fz0)
+        GT_WIDE_SLOT(2, nx0, fx0, ny0, fy0, nz0, fz0)
+        GT_WIDE_SLOT(3, nx0, fx0, ny0, fy0, nz0, fz0)
+        GT_WIDE_SLOT(4, nx1, fx1, ny1, fy1, nz1, fz1)
+        GT_WIDE_SLOT(5, nx1, fx1, ny1, fy1, nz1, fz1)
+        GT_WIDE_SLOT(6, nx1, fx1, ny1, fy1, nz1, fz1)
+        GT_WIDE_SLOT(7, nx1, fx1, ny1, fy1, nz1, fz1)
+#undef GT_WIDE_SLOT
+        if (any_par) { // parallel axes: the origin must lie within the slab (one step of slack)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                if (!rt.par[a]) continue;
+                const float sa = __uint_as_float(((c0.w >> (8 * a)) & 0xffu) << 23);
+                const float q = (ov[a] - __uint_as_float(pw[a])) / sa;
+                const uint32_t lo0 = a == 0 ? c2.x : a == 1 ? c2.z : c3.x, lo1 = a == 0 ? c2.y : a == 1 ? c2.w : c3.y;
+                const uint32_t hi0 = a == 0 ? c3.z : a == 1 ? c4.x : c4.z, hi1 = a == 0 ? c3.w : a == 1 ? c4.y : c4.w;
+#pragma unroll
+                for (int s = 0; s < 8; ++s) {
+                    const uint32_t lw = s < 4 ? lo0 : lo1, hw = s < 4 ? hi0 : hi1;
+                    const float lo = float((lw >> (8 * (s & 3))) & 0xffu), hi = float((hw >> (8 * (s & 3))) & 0xffu);
+                    if (!(q >= lo - 1.0f && q <= hi + 1.0f)) hits &= ~(1u << s);
+                }
+            }
+        }
+        // Leaf children: their primitives, at once.
+        uint32_t pm = 0;
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            const uint32_t m = ((s < 4 ? meta0 : meta1) >> (8 * (s & 3))) & 0xffu;
+            if ((hits >> s) & 1u) pm |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+        }
+        const uint32_t pbase = c1.y;
+        while (pm) {
+            const uint32_t k = uint32_t(__ffs(pm)) - 1u;
+            pm &= pm - 1u;
+            if (leaf_test<float, CHECK>(sc, pbase + k, o, d, time, tmin, closest, ck)) {
+                best = int(pbase + k);
+                if (any_hit) {
+                    t_out = closest;
+                    return best;
+                }
+            }
+        }
+        // Internal children, in visiting order (bit i = slot i ^ oct).
+        const uint32_t ih = hits & imask;
+        uint32_t order = 0;
+#pragma unroll
+        for (int s = 0; s < 8; ++s) order |= ((ih >> s) & 1u) << (uint32_t(s) ^ oct);
+        uint32_t gbase, gbits;
+        if (order) {
+            gbase = c1.x;
+            gbits = order | (imask << 8);
+            const uint32_t rest = gbits & ~(1u << (__ffs(order) - 1));
+            if (rest & 0xffu) {
+                if (sp >= int(kWideStack)) {
+                    atomicOr(err, E_STACK_OVERFLOW);
+                    break;
+                }
+                stack[sp++] = make_uint2(gbase, rest);
+            }
+        } else {
+            if (sp == 0) break;
+            const uint2 top = stack[sp - 1];
+            gbase = top.x;
+            gbits = top.y;
+            const uint32_t rest = gbits & ~(1u << (__ffs(gbits & 0xffu) - 1));
+            if (rest & 0xffu)
+                stack[sp - 1].y = rest;
+            else
+                --sp;
+        }
+        const uint32_t slot = (uint32_t(__ffs(gbits & 0xffu)) - 1u) ^ oct;
+        node = gbase + uint32_t(__popc((gbits >> 8) & ((1u << slot) - 1u)));
+    }
+    t_out = closest;
+    return best;
+}
+
 // FlatBvh::hit_with_stats (bvh.rs:306-399): root test, LIFO stack of (node, entry t),
 // skip entries at or beyond the closest hit, test both children of an internal node and
 // push the farther first.  ANY = stop at the first hit (occlusion).  Returns the leaf-
-// order primitive index of the closest hit or -1; sets *err on stack overflow.
-template <class R, bool STATS, bool ANY>
+// order primitive index of the closest hit or -1; sets *err on stack overflow.  An f32
+// scene with a wide tree is traversed by traverse_wide instead (same result semantics),
+// except for the statistics, which are defined by this walk.  CHECK (f32 primary-hit
+// check): candidates slightly beyond the closest hit are tested too and *near reports
+// near ties and near-boundary candidates in ck; the result is the rendering walk's.
+template <class R, bool STATS, bool ANY, bool CHECK = false>
 GT_DEV int traverse(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, R tmax, R& t_out, TraceStats* st,
-                    uint32_t* err, bool any_hit = ANY) {
+                    uint32_t* err, bool any_hit = ANY, CheckState<R>* ck = nullptr) {
+    if constexpr (sizeof(R) == 4 && !STATS) {
+        if (sc.wnodes) return traverse_wide<CHECK>(sc, o, d, time, tmin, tmax, t_out, err, any_hit, ck);
+    }
     RayT<R> rt = make_rayt(o, d);
     if (STATS) st->node_tests += 1;
     R root_entry;
@@ -220,7 +543,8 @@ GT_DEV int traverse(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, R t
         const int32_t link = s_link[sp];
         const int32_t count = s_count[sp];
         const R et = s_t[sp];
-        if (et >= closest) continue;
+        const R cull = CHECK ? check_limit(closest, ck->best_err) : closest;
+        if (et >= cull) continue;
         if (link < 0) {
             // hit_ray_scene_indices (scene.rs:849-874) with Interval(t_min, closest).
             const uint32_t first = uint32_t(~link);
@@ -230,9 +554,7 @@ GT_DEV int traverse(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, R t
             }
             bool leaf_hit = false;
             for (int k = 0; k < count; ++k) {
-                R t;
-                if (prim_hit(sc, first + k, o, d, time, tmin, closest, t)) {
-                    closest = t;
+                if (leaf_test<R, CHECK>(sc, first + k, o, d, time, tmin, closest, ck)) {
                     best = int(first + k);
                     leaf_hit = true;
                     if (any_hit) {
@@ -246,29 +568,19 @@ GT_DEV int traverse(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, R t
         }
         const Node<R>& nd = sc.nodes[link];
         R b[12];
-        if (sizeof(R) == 4) {
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                R4<R> v = ldg4(nd.box + 4 * q);
-                b[4 * q] = v.x;
-                b[4 * q + 1] = v.y;
-                b[4 * q + 2] = v.z;
-                b[4 * q + 3] = v.w;
-            }
-        } else {
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                R4<R> v = ldg4(nd.box + 4 * q);
-                b[4 * q] = v.x;
-                b[4 * q + 1] = v.y;
-                b[4 * q + 2] = v.z;
-                b[4 * q + 3] = v.w;
-            }
+        for (int q = 0; q < 3; ++q) {
+            R4<R> v = ldg4(nd.box + 4 * q);
+            b[4 * q] = v.x;
+            b[4 * q + 1] = v.y;
+            b[4 * q + 2] = v.z;
+            b[4 * q + 3] = v.w;
         }
         const int4 ln = __ldg(reinterpret_cast<const int4*>(nd.link));
         R le, re;
-        const bool lh = hit_box(rt, b, b + 3, tmin, closest, le);
-        const bool rh = hit_box(rt, b + 6, b + 9, tmin, closest, re);
+        const R ccull = CHECK ? check_limit(closest, ck->best_err) : closest;
+        const bool lh = hit_box(rt, b, b + 3, tmin, ccull, le);
+        const bool rh = hit_box(rt, b + 6, b + 9, tmin, ccull, re);
         if (STATS) {
             st->node_tests += 2;
             st->node_hits += uint32_t(lh) + uint32_t(rh);

@@ -189,7 +189,7 @@ template <class R, bool BATCH = false> __global__ void __launch_bounds__(256) k_
     }
 }
 
-template <class R> __global__ void __launch_bounds__(256, 6) k_trace(Params<R> P, uint32_t cur) {
+template <class R> __global__ void __launch_bounds__(256, 4) k_trace(Params<R> P, uint32_t cur) {
     const uint32_t count = *reinterpret_cast<volatile uint32_t*>(&P.ps.counters[C_TRACE0 + cur]);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&P.ps.totals[0], (unsigned long long)count);
     const uint32_t* q = P.ps.q_trace[cur];
@@ -1093,6 +1093,26 @@ __global__ void k_trace_rays(SceneDev<R> sc, const double* rays, uint32_t count,
         atomicAdd(&stats[3], st.candidates);
         atomicAdd(&stats[4], st.leaf_hits);
         atomicMax(&stats[5], (unsigned long long)st.max_depth);
+    }
+}
+
+// The f32 primary-hit check: each ray through the f32 rendering walk (the wide tree where
+// the scene has one) in its check mode, which returns the rendering walk's closest hit
+// and flags rays whose decision f32 rounding may have changed (near ties, near edges,
+// near t_min) for an f64 re-trace.
+template <class R>
+__global__ void k_trace_rays_check(SceneDev<R> sc, const double* rays, uint32_t count, double tmin, double tmax,
+                                   int32_t* ids, double* tout, uint8_t* near_out, uint32_t* err) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const double* r = rays + size_t(i) * 7;
+        const V3<R> o{R(r[0]), R(r[1]), R(r[2])}, d{R(r[3]), R(r[4]), R(r[5])};
+        R t = R(0);
+        CheckState<R> ck{false, R(0)};
+        const int prim = traverse<R, false, false, true>(sc, o, d, R(r[6]), R(tmin), R(tmax), t, nullptr, err, false,
+                                                         &ck);
+        ids[i] = prim < 0 ? -1 : int32_t(__ldg(&sc.meta[prim].y));
+        tout[i] = prim < 0 ? 0.0 : double(t);
+        near_out[i] = ck.near ? 1 : 0;
     }
 }
 

@@ -614,7 +614,8 @@ class Context:
 class _SceneHandle:
     def __init__(self, ctx: Context, prims: np.ndarray, mats: np.ndarray, leaf_size: int,
                  bvh_builder: int = abi.GT_BVH_REFERENCE_SAH, images: Sequence[ImageTexture] = (),
-                 media: Sequence = (), meshes: Sequence = (), objects: Sequence = ()):
+                 media: Sequence = (), meshes: Sequence = (), objects: Sequence = (),
+                 f32_tree: int = abi.GT_F32_TREE_WIDE):
         self.ctx = ctx
         prims = np.ascontiguousarray(prims)
         mats = np.ascontiguousarray(mats)
@@ -629,6 +630,7 @@ class _SceneHandle:
         d.materials = mats.ctypes.data_as(C.POINTER(abi.gt_material))
         d.bvh_leaf_size = leaf_size
         d.bvh_builder = bvh_builder
+        d.f32_tree = f32_tree
         d.num_images = len(images)
         d.images = table
         d.num_media = len(media)
@@ -683,6 +685,7 @@ class RayScene:
         self._prims: Optional[np.ndarray] = np.zeros(0, dtype=PRIMITIVE_DTYPE)
         self._leaf_size = 4
         self._bvh_builder = abi.GT_BVH_REFERENCE_SAH
+        self._f32_tree = abi.GT_F32_TREE_WIDE
         self._media: list = []
         self._meshes: list = []
         self._mesh_index: dict = {}
@@ -842,6 +845,16 @@ class RayScene:
             self._invalidate()
         return self
 
+    def use_binary_f32_tree(self, enabled: bool = True) -> "RayScene":
+        """The f32 path walks the reference's binary tree (gt_f32_tree GT_F32_TREE_BINARY)
+        instead of the eight-wide compressed tree collapsed from it.  Same hits; for
+        comparisons."""
+        tree = abi.GT_F32_TREE_BINARY if enabled else abi.GT_F32_TREE_WIDE
+        if tree != self._f32_tree:
+            self._f32_tree = tree
+            self._invalidate()
+        return self
+
     def build_bvh_with_options(self, leaf_size: int = 4) -> None:
         """BvhBuildOptions::with_leaf_size clamps 0 to 1 (bvh.rs:73-77)."""
         self._leaf_size = max(int(leaf_size), 1)
@@ -916,7 +929,8 @@ class RayScene:
         h = self._handles.get(id(ctx))
         if h is None or h.ctx is not ctx or not h.h:
             h = _SceneHandle(ctx, self.primitives_array(), self.materials_array(), self._leaf_size,
-                             self._bvh_builder, self.images(), self._media, self.mesh_list(), self._objects)
+                             self._bvh_builder, self.images(), self._media, self.mesh_list(), self._objects,
+                             self._f32_tree)
             self._handles[id(ctx)] = h
         return h
 
@@ -937,6 +951,23 @@ class RayScene:
                                   len(rays), float(t_min), float(t_max), ids.ctypes.data_as(C.c_void_p),
                                   t.ctypes.data_as(C.c_void_p), C.byref(st)))
         return ids, t, st.as_dict()
+
+    def hit_rays_f32(self, rays: np.ndarray, t_min: float = SHADOW_ACNE_EPSILON, t_max: float = INFINITY,
+                     ctx: Optional[Context] = None):
+        """hit_rays through the renderer's f32 walk, with near-tie rays re-traced in f64
+        (gt_trace_rays_f32).  Returns (prim_ids, t, refined, report): refined is 0 for an
+        f32 result, 1 for an f64 re-trace that kept the primitive, 2 for one that changed it."""
+        rays = np.ascontiguousarray(rays, dtype=np.float64).reshape(-1, 7)
+        ids = np.empty(len(rays), dtype=np.int32)
+        t = np.empty(len(rays), dtype=np.float64)
+        refined = np.empty(len(rays), dtype=np.uint8)
+        rep = abi.gt_trace_report()
+        rep.struct_size = C.sizeof(abi.gt_trace_report)
+        check(lib().gt_trace_rays_f32(self._handle(ctx or Context.default()).h, rays.ctypes.data_as(C.c_void_p),
+                                      len(rays), float(t_min), float(t_max), ids.ctypes.data_as(C.c_void_p),
+                                      t.ctypes.data_as(C.c_void_p), refined.ctypes.data_as(C.c_void_p),
+                                      C.byref(rep)))
+        return ids, t, refined, rep.as_dict()
 
     def bvh_traversal_stats_for_rays(self, rays: np.ndarray, t_min: float = SHADOW_ACNE_EPSILON,
                                      t_max: float = INFINITY) -> dict:
@@ -1136,6 +1167,63 @@ class RayCamera:
 
 
 # --------------------------------------------------------------------- images
+def _gamma2_byte(c: np.ndarray) -> np.ndarray:
+    """Rgb::linear_to_gamma_component then (256 * clamp(., 0, 0.999)) as u8 (colors.rs:388-422):
+    the square root of the non-negative part, non-finite values as 0."""
+    c = np.nan_to_num(np.asarray(c, dtype=np.float64), nan=0.0, posinf=0.0, neginf=0.0)
+    g = np.sqrt(np.clip(c, 0.0, None))
+    return (256.0 * np.clip(g, 0.0, 0.999)).astype(np.uint8)
+
+
+def linear_color_to_rgb(color) -> tuple:
+    """linear_color_to_rgb (graphics/raytracing.rs:166-168): gamma-2 display bytes."""
+    return tuple(int(x) for x in _gamma2_byte(np.asarray(color, dtype=np.float64)))
+
+
+TONE_MAP_NONE, TONE_MAP_REINHARD, TONE_MAP_ACES = 0, 1, 2
+
+
+@dataclass(frozen=True)
+class ToneMap:
+    """ToneMap (graphics/display.rs:164-280): exposure, then the operator (none, Reinhard
+    x / (1 + x), or the ACES fit clamped to [0, 1]) on the finite non-negative part, then
+    gamma encoding (gamma 2 is the square root) and (256 * clamp(., 0, 0.999)) as u8."""
+
+    exposure: float = 1.0
+    operator: int = TONE_MAP_NONE
+    gamma: float = 2.0
+
+    def with_exposure(self, exposure: float) -> "ToneMap":
+        if not (math.isfinite(exposure) and exposure >= 0.0):
+            raise ValueError("tone-map exposure must be finite and non-negative")
+        return ToneMap(float(exposure), self.operator, self.gamma)
+
+    def with_operator(self, operator: int) -> "ToneMap":
+        if operator not in (TONE_MAP_NONE, TONE_MAP_REINHARD, TONE_MAP_ACES):
+            raise ValueError("unknown tone-mapping operator")
+        return ToneMap(self.exposure, int(operator), self.gamma)
+
+    def with_gamma(self, gamma: float) -> "ToneMap":
+        if not (math.isfinite(gamma) and gamma > 0.0):
+            raise ValueError("tone-map gamma must be positive and finite")
+        return ToneMap(self.exposure, self.operator, float(gamma))
+
+    def map_colors(self, c: np.ndarray) -> np.ndarray:
+        """ToneMap::map_color over an array of linear colours (display.rs:262-277)."""
+        v = np.asarray(c, dtype=np.float64) * self.exposure
+        v = np.where(np.isfinite(v), np.maximum(v, 0.0), 0.0)
+        if self.operator == TONE_MAP_REINHARD:
+            v = v / (1.0 + v)
+        elif self.operator == TONE_MAP_ACES:
+            v = np.clip(v * (2.51 * v + 0.03) / (v * (2.43 * v + 0.59) + 0.14), 0.0, 1.0)
+        if abs(self.gamma - 2.0) <= 2.220446049250313e-16:
+            g = np.sqrt(v)
+        else:
+            with np.errstate(divide="ignore", invalid="ignore"):
+                g = np.where(v <= 0.0, 0.0, np.power(np.maximum(v, 0.0), 1.0 / self.gamma))
+        return (256.0 * np.clip(g, 0.0, 0.999)).astype(np.uint8)
+
+
 @dataclass
 class HdrImage:
     """HdrImage (graphics/display.rs:282-440): row-major linear RGB, row 0 at the top."""
@@ -1151,6 +1239,10 @@ class HdrImage:
         c = np.nan_to_num(self.pixels.astype(np.float64), nan=0.0)
         g = np.sqrt(np.clip(c, 0.0, None))
         return (256.0 * np.clip(g, 0.0, 0.999)).astype(np.uint8)
+
+    def to_canvas_tone_mapped(self, tone_map: ToneMap) -> np.ndarray:
+        """HdrImage::to_canvas_tone_mapped (display.rs:338-350)."""
+        return tone_map.map_colors(self._linear())
 
     def _linear(self) -> np.ndarray:
         return self.pixels64 if self.pixels64 is not None else self.pixels.astype(np.float64)
@@ -1551,9 +1643,33 @@ class PathTracer:
         img, alb, nrm = self._render(scene, None if lights.is_empty() else lights, None, aovs=True)
         return DenoisingAovs(img.pixels, alb, nrm)
 
-    # render_scene_hdr_image (renderer.rs:321-324)
-    def render_scene_hdr_image(self, scene: "SurfaceScene") -> HdrImage:
-        return self.render_hdr_image(scene.to_ray_scene())
+    # render_ray_scene_with_light_connections (raytracing.rs:1748-1776): the scene's emissive
+    # targets as light connections
+    def render_ray_scene_with_light_connections_hdr_image(self, scene: RayScene, want64: bool = False) -> HdrImage:
+        return self.render_with_light_connections_hdr_image(scene, scene.emissive_targets(), want64=want64)
+
+    def render_tone_mapped(self, world: RayScene, tone_map: "ToneMap") -> np.ndarray:
+        """render_tone_mapped (renderer.rs:101-117 with ToneMap, display.rs:338-350)."""
+        return self.render_hdr_image(world).to_canvas_tone_mapped(tone_map)
+
+    # render_scene / render_scene_hdr_image / render_scene_denoising_aovs /
+    # render_scene_with_lights / render_scene_with_light_connections (renderer.rs:309-371):
+    # the surface scene compiled to a RayScene (Lambertian policy) on every call
+    def render_scene_hdr_image(self, scene: "SurfaceScene", want64: bool = False) -> HdrImage:
+        return self.render_hdr_image(scene.to_ray_scene(), want64=want64)
+
+    def render_scene(self, scene: "SurfaceScene") -> np.ndarray:
+        return self.render_scene_hdr_image(scene).to_canvas()
+
+    def render_scene_denoising_aovs(self, scene: "SurfaceScene") -> DenoisingAovs:
+        return self.render_denoising_aovs(scene.to_ray_scene())
+
+    def render_scene_with_lights(self, scene: "SurfaceScene", lights) -> np.ndarray:
+        return self.render_with_lights(scene.to_ray_scene(), lights)
+
+    def render_scene_with_light_connections_hdr_image(self, scene: "SurfaceScene", lights,
+                                                       want64: bool = False) -> HdrImage:
+        return self.render_with_light_connections_hdr_image(scene.to_ray_scene(), lights, want64=want64)
 
     def trace_primary(self, scene: RayScene, stride: int = 1):
         """Primary probe rays (ray_for_pixel) through the f64 reference-layout BVH:
@@ -1568,14 +1684,109 @@ class PathTracer:
                                      ids.ctypes.data_as(C.c_void_p), t.ctypes.data_as(C.c_void_p), C.byref(st)))
         return ids, t, st.as_dict()
 
+    def trace_primary_f32(self, scene: RayScene, stride: int = 1):
+        """The same probe rays through the renderer's f32 walk with near ties re-traced in
+        f64 (gt_trace_primary_f32): (prim_ids, t, refined, report)."""
+        w, h, _ = self.camera.image_size()
+        stride = max(int(stride), 1)
+        n = ((w + stride - 1) // stride) * ((h + stride - 1) // stride)
+        ids = np.empty(n, dtype=np.int32)
+        t = np.empty(n, dtype=np.float64)
+        refined = np.empty(n, dtype=np.uint8)
+        rep = abi.gt_trace_report()
+        rep.struct_size = C.sizeof(abi.gt_trace_report)
+        check(lib().gt_trace_primary_f32(scene._handle(self.context).h, C.byref(self.camera.desc()), stride,
+                                         ids.ctypes.data_as(C.c_void_p), t.ctypes.data_as(C.c_void_p),
+                                         refined.ctypes.data_as(C.c_void_p), C.byref(rep)))
+        return ids, t, refined, rep.as_dict()
+
 
 # ------------------------------------------------------------ surface scenes
+@dataclass(frozen=True)
+class SurfaceMaterial:
+    """SurfaceMaterial (graphics/material.rs:12-110): the renderer-neutral colours and the
+    optional refractive index that the ray materials are derived from."""
+
+    ambient_color: tuple = (0.1, 0.1, 0.1)
+    base_color: tuple = (0.5, 0.5, 0.5)
+    specular_color: tuple = (0.9, 0.9, 0.9)
+    shininess: float = 200.0
+    refractive_index: Optional[float] = None
+
+    def __post_init__(self):
+        vals = list(self.ambient_color) + list(self.base_color) + list(self.specular_color) + [self.shininess]
+        if not all(math.isfinite(float(x)) for x in vals):  # SurfaceMaterial::new asserts finite values
+            raise ValueError("surface material colours and shininess must be finite")
+        if self.refractive_index is not None and not (math.isfinite(self.refractive_index) and
+                                                      self.refractive_index > 0.0):
+            raise ValueError("refractive index must be positive and finite")  # lighting.rs:268-273
+
+    # SurfaceMaterial::as_* (raytracing/material.rs:2238-2262)
+    def as_lambertian(self) -> RayMaterial:
+        return RayMaterial.lambertian(self.base_color)
+
+    def as_metal(self, fuzz: float) -> RayMaterial:
+        return RayMaterial.metal(self.specular_color, fuzz)
+
+    def as_ggx_microfacet(self, roughness: float) -> RayMaterial:
+        return RayMaterial.ggx_microfacet(self.specular_color, roughness)
+
+    def as_dielectric(self) -> Optional[RayMaterial]:
+        return None if self.refractive_index is None else RayMaterial.dielectric(self.refractive_index)
+
+
+class SurfaceRayMaterialMode:
+    """SurfaceRayMaterialMode (raytracing/scene.rs:30-72): Lambertian (the default),
+    PreferDielectric, PreferMetal{fuzz} or Custom(mapper)."""
+
+    def __init__(self, kind: str, fuzz: float = 0.0, mapper=None):
+        if kind not in ("lambertian", "prefer_dielectric", "prefer_metal", "custom"):
+            raise ValueError("unknown surface material mode")
+        if kind == "custom" and mapper is None:
+            raise ValueError("a custom mode needs a mapper")
+        self.kind, self.fuzz, self.mapper = kind, float(fuzz), mapper
+
+    @classmethod
+    def lambertian(cls) -> "SurfaceRayMaterialMode":
+        return cls("lambertian")
+
+    @classmethod
+    def prefer_dielectric(cls) -> "SurfaceRayMaterialMode":
+        return cls("prefer_dielectric")
+
+    @classmethod
+    def prefer_metal(cls, fuzz: float) -> "SurfaceRayMaterialMode":
+        return cls("prefer_metal", fuzz=fuzz)
+
+    @classmethod
+    def custom(cls, mapper) -> "SurfaceRayMaterialMode":
+        return cls("custom", mapper=mapper)
+
+    def convert(self, material: SurfaceMaterial) -> RayMaterial:
+        """SurfaceRayMaterialMode::convert (scene.rs:56-67)."""
+        if self.kind == "lambertian":
+            return material.as_lambertian()
+        if self.kind == "prefer_dielectric":
+            d = material.as_dielectric()
+            return d if d is not None else material.as_lambertian()
+        if self.kind == "prefer_metal":
+            return material.as_metal(self.fuzz)
+        out = self.mapper(material)
+        if not isinstance(out, RayMaterial):
+            raise TypeError("a custom surface material mapper must return a RayMaterial")
+        return out
+
+
 @dataclass
 class SurfaceMesh:
-    """SurfaceMesh (graphics/scene.rs:17-60): triangles plus a base colour."""
+    """SurfaceMesh (graphics/scene.rs:17-60): triangles plus a surface material."""
 
     triangles: np.ndarray  # (N, 3, 3)
-    base_color: tuple = (0.5, 0.5, 0.5)
+    material: SurfaceMaterial = field(default_factory=SurfaceMaterial)
+
+    @property
+    def base_color(self) -> tuple:
+        return self.material.base_color
 
 
 @dataclass
@@ -1584,15 +1795,24 @@ class SurfaceScene:
 
     meshes: list = field(default_factory=list)
 
-    def add_mesh(self, triangles: np.ndarray, base_color=(0.5, 0.5, 0.5)) -> None:
-        self.meshes.append(SurfaceMesh(np.asarray(triangles, dtype=np.float64).reshape(-1, 3, 3), _vec(base_color)))
+    def add_mesh(self, triangles: np.ndarray, base_color=(0.5, 0.5, 0.5),
+                 material: Optional[SurfaceMaterial] = None) -> None:
+        mat = material if material is not None else SurfaceMaterial(base_color=_vec(base_color))
+        self.meshes.append(SurfaceMesh(np.asarray(triangles, dtype=np.float64).reshape(-1, 3, 3), mat))
+
+    def __len__(self) -> int:
+        return len(self.meshes)
 
     def to_ray_scene(self, leaf_size: int = 4) -> RayScene:
-        """SurfaceScene::to_ray_scene (scene.rs:1517-1547, 1606-1608): one Lambertian per
-        mesh from its base colour, triangles in mesh order, BVH built."""
+        """SurfaceScene::to_ray_scene (scene.rs:1606-1608): the Lambertian mode."""
+        return self.to_ray_scene_with_material_mode(SurfaceRayMaterialMode.lambertian(), leaf_size)
+
+    def to_ray_scene_with_material_mode(self, mode: SurfaceRayMaterialMode, leaf_size: int = 4) -> RayScene:
+        """RayScene::from_surface_scene_with_material_mode_and_bvh_options (scene.rs:1517-1547):
+        one material per mesh through `mode`, the meshes' triangles in order, BVH built."""
         scene = RayScene()
         for mesh in self.meshes:
-            mid = scene.add_material(RayMaterial.lambertian(mesh.base_color))
+            mid = scene.add_material(mode.convert(mesh.material))
             scene.add_triangles_array(mid, mesh.triangles)
         scene.build_bvh_with_options(leaf_size)
         return scene

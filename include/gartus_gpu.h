@@ -152,6 +152,17 @@ typedef enum gt_bvh_builder {
                                  reference counterpart.                                        */
 } gt_bvh_builder;
 
+/* The tree the f32 path traverses (no reference counterpart; the f64 path and the
+ * traversal statistics always walk the reference's binary tree).  GT_F32_TREE_WIDE: an
+ * eight-wide tree with byte-quantised child boxes, collapsed from the reference SAH tree
+ * (same leaves, same hits; the binary walk is kept where a scene has no wide form: a
+ * single leaf, leaves of more than four primitives, or a GT_BVH_GPU_LBVH scene).
+ * GT_F32_TREE_BINARY: the reference's binary tree. */
+typedef enum gt_f32_tree {
+    GT_F32_TREE_WIDE = 0,
+    GT_F32_TREE_BINARY = 1
+} gt_f32_tree;
+
 /* A constant-density participating medium (ConstantMedium, raytracing/volume/medium.rs:13-187)
  * whose boundary is a sphere or a box_object (object.rs:930-976), optionally wrapped as
  * Translate(RotateY(shape, rotate_y), translate) (instance.rs).  A scene with media renders as
@@ -218,7 +229,7 @@ typedef struct gt_scene_desc {
     const gt_medium* media; /* participating media after the surfaces, in list order (copied) */
     const gt_mesh* meshes;  /* meshes that objects place (copied) */
     uint32_t num_objects;
-    uint32_t reserved;
+    uint32_t f32_tree;        /* gt_f32_tree: the tree the f32 path traverses (0 = wide) */
     const gt_object* objects; /* world objects tested after the RayScene's surfaces and before
                                  the media (copied) */
 } gt_scene_desc;
@@ -399,6 +410,17 @@ typedef struct gt_bvh_stats {
     uint64_t max_stack_depth;
 } gt_bvh_stats;
 
+/* What gt_trace_rays_f32 / gt_trace_primary_f32 did. */
+typedef struct gt_trace_report {
+    uint32_t struct_size; /* sizeof(gt_trace_report) */
+    uint32_t tree;        /* gt_f32_tree the f32 walk traversed */
+    uint64_t rays;
+    uint64_t refined;     /* rays re-traced in f64: near ties, near edges, near t_min */
+    uint64_t changed;     /* of those, rays whose primitive the f64 re-trace changed */
+    uint32_t wide_nodes;  /* nodes of the scene's wide tree (0 without one) */
+    uint32_t wide_depth;  /* its levels */
+} gt_trace_report;
+
 /* Opaque handles. */
 typedef struct gt_context gt_context;
 typedef struct gt_scene gt_scene;
@@ -558,6 +580,24 @@ gt_status gt_trace_rays(gt_scene* scene, const double* rays, uint32_t count, dou
  * row-major probe order. */
 gt_status gt_trace_primary(gt_scene* scene, const gt_camera_desc* camera, uint32_t stride,
                            int32_t* prim_ids, double* t, gt_bvh_stats* stats);
+
+/* The same closest-hit queries as gt_trace_rays (RayScene::hit, raytracing/scene.rs:
+ * 1639-1657; the traversal of raytracing/bvh.rs:306-399) through the f32 walk the renderer
+ * uses: the wide tree (gt_f32_tree) or the binary one, f32 primitive tests.  Rays whose
+ * f32 decision may differ from f64 — a second candidate whose distance lies within the
+ * two distances' estimated f32 errors of the closest, a hit point within a few dozen f32
+ * ulps (scaled at grazing angles) of an edge, a distance near t_min — are re-traced by
+ * the f64 walk; their ids are then the
+ * reference's.  refined (may be NULL): per ray 0 = f32 result, 1 = re-traced (same
+ * primitive), 2 = re-traced (the f64 walk chose another primitive).  report may be NULL. */
+gt_status gt_trace_rays_f32(gt_scene* scene, const double* rays, uint32_t count, double t_min,
+                            double t_max, int32_t* prim_ids, double* t, uint8_t* refined,
+                            gt_trace_report* report);
+
+/* gt_trace_primary's probe rays (f64 camera, RayCamera::ray_for_pixel, camera.rs:
+ * 1641-1653) through gt_trace_rays_f32. */
+gt_status gt_trace_primary_f32(gt_scene* scene, const gt_camera_desc* camera, uint32_t stride,
+                               int32_t* prim_ids, double* t, uint8_t* refined, gt_trace_report* report);
 
 /* ---------------------------------------------------------------- denoiser */
 
