@@ -80,7 +80,7 @@ def workload(name, width=0, grid=0):
         width = width or 1920
         grid = grid or 8
         cam = scenes.mesh_heavy_camera(width, width * 1080 // 1920, grid, 8)
-        w, h, spp = cam.image_size()
+        w, h, spp = width, width * 1080 // 1920, grid * grid
         cfg = {"workload": "mesh_heavy_perlin_tori_sun", "width": w, "height": h, "spp": spp, "max_depth": 8,
                "sampling": f"stratified {grid}x{grid}", "lights": "HDR environment 2048x1024 f32 with sun (NEE)",
                "primitives": len(scene), "precision": "f32"}
@@ -105,7 +105,7 @@ def workload(name, width=0, grid=0):
     scene = scenes.final_scene_ray_scene()
     width = width or 400
     cam = scenes.final_scene_camera(width, 32)
-    cfg = {"workload": "final_scene_spheres", "width": width, "height": cam.image_size()[1], "spp": 32,
+    cfg = {"workload": "final_scene_spheres", "width": width, "height": max(int(width / (16.0 / 9.0)), 1), "spp": 32,
            "max_depth": 10,
            "sampling": "random", "lights": "none (sky gradient)", "primitives": len(scene), "precision": "f32"}
     return scene, None, None, cam, cfg
@@ -200,7 +200,7 @@ def cpu_baseline(scene, lights, env, cam, seconds: float):
         cam = cam[len(cam) // 2]
     o = oracle.OracleScene.from_ray_scene(scene)
     la = lights.to_array() if lights is not None else None
-    w, h, spp = cam.image_size()
+    w, h, spp = oracle.camera_size(cam.desc())
     threads = os.cpu_count() or 1
     rows = 1
     t0 = time.perf_counter()
@@ -401,10 +401,12 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize(device)
 
-    if args.profile_run:  # a fixed number of frames for an ncu capture; no timing, no output
+    if args.profile_run:  # a fixed number of frames for an ncu capture; no timing, no bench line
         for _ in range(args.warmup + args.steps):
             render()
         torch.cuda.synchronize(device)
+        # the last frame's counts (rays per kernel), to turn a capture's bytes into bytes per ray
+        print(json.dumps({"profile_run_stats": pt.last_stats, "config": cfg}), file=sys.stderr)
         return
     for _ in range(max(args.warmup, 3)):
         render()

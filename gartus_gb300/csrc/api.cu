@@ -843,8 +843,10 @@ gt_status gt_autotune(gt_scene* s, const gt_lights* l, const gt_environment* e, 
     if (opts->struct_size < sizeof(gt_render_opts)) return fail(GT_ERR_INVALID_ARG, "options struct_size too small");
     if (report && report->struct_size < sizeof(gt_autotune_report))
         return fail(GT_ERR_INVALID_ARG, "report struct_size too small");
-    if (opts->schedule == GT_SCHEDULE_PERSISTENT)
-        return fail(GT_ERR_INVALID_ARG, "the persistent schedule has nothing to tune; use AUTO or WAVEFRONT");
+    if (opts->schedule > GT_SCHEDULE_PERSISTENT) return fail(GT_ERR_INVALID_ARG, "unknown schedule");
+    // PERSISTENT (for instance the outcome of an earlier tune) is tuned as AUTO, whose last
+    // candidate is PERSISTENT again.
+    const uint32_t given_schedule = opts->schedule == GT_SCHEDULE_PERSISTENT ? GT_SCHEDULE_AUTO : opts->schedule;
     uint32_t trials = 0;
     // Device time of the second of two renders with `o` (the first captures its graphs).
     auto timed = [&](const gt_render_opts& cand, double& ms) -> gt_status {
@@ -864,6 +866,7 @@ gt_status gt_autotune(gt_scene* s, const gt_lights* l, const gt_environment* e, 
         return GT_OK;
     };
     gt_render_opts best = *opts;
+    best.schedule = given_schedule;
     double best_ms = 0.0;
     gt_status rc = timed(best, best_ms);
     if (rc != GT_OK) return rc;
@@ -891,7 +894,7 @@ gt_status gt_autotune(gt_scene* s, const gt_lights* l, const gt_environment* e, 
     if ((rc = sweep(&gt_render_opts::generate_blocks_per_sm, {4u, 8u, 16u})) != GT_OK) return rc;
     // Last, the persistent schedule alone (it wins for small frames, whose wavefront
     // iterations are launch-bound); only when the caller left the choice to AUTO.
-    if (opts->schedule == GT_SCHEDULE_AUTO) {
+    if (given_schedule == GT_SCHEDULE_AUTO) {
         gt_render_opts cand = best;
         cand.schedule = GT_SCHEDULE_PERSISTENT;
         double ms = 0.0;

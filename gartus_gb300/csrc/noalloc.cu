@@ -116,7 +116,10 @@ extern "C" gt_status gt_render_noalloc(gt_scene* scene, const gt_lights* lights,
         ce = cudaMemcpyAsync(ctx->pinned, P.ps.counters + C_ERROR, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
         if (ce != cudaSuccess) return cuda_fail(ce, "gt_render_noalloc");
-        if (ctx->pinned[0]) return fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
+        const uint32_t word = ctx->pinned[0];
+        if (word & E_STACK_OVERFLOW)
+            return fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
+        if (word) return fail(GT_ERR_INTERNAL, "device error word " + std::to_string(word));
         return GT_OK;
     } catch (const std::exception& ex) {
         return fail(GT_ERR_INTERNAL, ex.what());

@@ -96,6 +96,61 @@ template <class R> GT_DEV bool sphere_root(V3<R> center, R radius, V3<R> o, V3<R
     return false;
 }
 
+// f32: the same roots with less rounding.  The discriminant is a (r^2 - |l|^2) with
+// l = oc - (h / a) d, the centre's offset from the ray's closest approach (Haines,
+// Guenther, Akenine-Moeller, "Precision Improvements for Ray/Sphere Intersection", Ray
+// Tracing Gems, 2019): the reference's h^2 - a c cancels when a sphere is small against
+// its distance, which moved f32 hit normals by ~1e-3 on the final scene's small spheres.
+// c = |oc|^2 - r^2 keeps its products' rounding errors (two-product) and its sums' (two-
+// sum), so it stays accurate near a large sphere, and each root comes from the
+// cancellation-free form (q = h + sign(h) sqrt(disc): roots c / q and q / a).  In exact
+// arithmetic these are the reference's roots, tested in the reference's order.  The
+// products whose errors are recovered use __fmul_rn so that no multiply-add absorbs them.
+GT_DEV float two_sum_err(float a, float b, float s) {
+    const float bb = __fsub_rn(s, a);
+    return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+template <> GT_DEV bool sphere_root<float>(V3<float> center, float radius, V3<float> o, V3<float> d, float tmin,
+                                           float tmax, float& root) {
+    const V3<float> oc = center - o;
+    const float a = len2(d);
+    if (a <= float(kEps)) return false;
+    const float h = dot(d, oc);
+    const float tc = h / a;
+    const V3<float> l{__fmaf_rn(-d.x, tc, oc.x), __fmaf_rn(-d.y, tc, oc.y), __fmaf_rn(-d.z, tc, oc.z)};
+    const float disc_a = __fmaf_rn(radius, radius, -len2(l));
+    if (disc_a < 0.0f) return false;
+    const float px = __fmul_rn(oc.x, oc.x), py = __fmul_rn(oc.y, oc.y), pz = __fmul_rn(oc.z, oc.z);
+    const float rr = __fmul_rn(radius, radius);
+    const float e = __fadd_rn(__fadd_rn(__fmaf_rn(oc.x, oc.x, -px), __fmaf_rn(oc.y, oc.y, -py)),
+                              __fsub_rn(__fmaf_rn(oc.z, oc.z, -pz), __fmaf_rn(radius, radius, -rr)));
+    const float s1 = __fadd_rn(px, py), s2 = __fadd_rn(s1, pz), s3 = __fsub_rn(s2, rr);
+    const float c = __fadd_rn(s3, __fadd_rn(__fadd_rn(__fadd_rn(two_sum_err(px, py, s1), two_sum_err(s1, pz, s2)),
+                                                      two_sum_err(s2, -rr, s3)),
+                                            e));
+    const float sq = sqrtf(a * disc_a);
+    const float q = h >= 0.0f ? h + sq : h - sq;
+    float first, second;
+    if (q == 0.0f) {
+        first = second = 0.0f;
+    } else if (h >= 0.0f) {
+        first = c / q;
+        second = q / a;
+    } else {
+        first = q / a;
+        second = c / q;
+    }
+    if (tmin < first && first < tmax) {
+        root = first;
+        return true;
+    }
+    if (tmin < second && second < tmax) {
+        root = second;
+        return true;
+    }
+    return false;
+}
+
 // Möller–Trumbore with the reference's tolerances (geometry.rs:239-265), edges given.
 template <class R> GT_DEV bool tri_hit(V3<R> p0, V3<R> e1, V3<R> e2, V3<R> o, V3<R> d, R tmin, R tmax, R& t) {
     V3<R> pvec = cross(d, e2);

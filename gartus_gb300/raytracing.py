@@ -1049,8 +1049,24 @@ class RayCamera:
     """RayCamera builder (graphics/camera.rs:1034-1481).  Each with_* returns a new camera."""
 
     def __init__(self, image_width: int, aspect_ratio: float):
+        """RayCamera::new (camera.rs:1034-1065): the reference's defaults, as gt_camera_default
+        writes them (a host-side restatement, so that a camera can be described without the
+        device library)."""
+        if int(image_width) <= 0:
+            raise GartusError(abi.GT_ERR_INVALID_ARG, "image width must be positive")
+        if not (math.isfinite(aspect_ratio) and aspect_ratio > 0.0):
+            raise GartusError(abi.GT_ERR_INVALID_ARG, "aspect ratio must be positive and finite")
         d = abi.gt_camera_desc()
-        check(lib().gt_camera_default(int(image_width), float(aspect_ratio), C.byref(d)))
+        d.struct_size = C.sizeof(abi.gt_camera_desc)
+        d.image_width, d.aspect_ratio = int(image_width), float(aspect_ratio)
+        d.samples_per_pixel, d.pixel_sample_mode, d.grid_width = 1, abi.GT_SAMPLE_RANDOM, 1
+        d.direct_lighting_mode, d.light_pdf_weight = abi.GT_DIRECT_CURRENT_PATH_CONTINUATION, 0.5
+        d.max_depth, d.russian_roulette_min_depth, d.rng_seed = 10, 5, 1
+        d.vertical_fov = 90.0
+        d.lookat[2], d.view_up[1] = -1.0, 1.0
+        d.focus_distance, d.shutter_end = 1.0, 1.0
+        d.background_kind = abi.GT_BG_CONSTANT
+        d.background[0], d.background[1], d.background[2] = 0.70, 0.80, 1.00
         self._d = d
 
     @classmethod
@@ -1405,10 +1421,12 @@ class PathTracer:
     def autotune(self, world: RayScene, lights: Optional[WeightedSamplingTargetList] = None,
                  environment: Optional[EnvironmentLight] = None, cameras=None) -> dict:
         """gt_autotune: times this tracer's frame (or the batch of `cameras`) under candidate
-        stripe counts, tail sizes and wavefront blocks per SM, then (schedule "auto") the
-        persistent schedule, and keeps the fastest in this tracer.  Returns {"trials",
-        "given_ms", "best_ms", "schedule", "stripes", "tail_slots", "generate_blocks_per_sm",
-        "trace_blocks_per_sm"}."""
+        stripe counts, tail sizes and wavefront blocks per SM, then (schedule "auto", or
+        "persistent" from an earlier tune) the persistent schedule, and keeps the fastest in
+        this tracer.  Launch shapes never change the image; switching to the persistent
+        schedule can change f32 pixels (other kernels fuse f32 operations differently), never
+        f64 images or accepted counts.  Returns {"trials", "given_ms", "best_ms", "schedule",
+        "stripes", "tail_slots", "generate_blocks_per_sm", "trace_blocks_per_sm"}."""
         ctx = self.context
         cams = list(cameras) if cameras is not None else [self.camera]
         descs = [c.desc() for c in cams]

@@ -553,8 +553,11 @@ gt_status gt_render_batch(gt_scene* scene, const gt_lights* lights, const gt_env
  * frames.  Each candidate is timed by the device time of its second render (the first
  * captures its graphs).  A candidate replaces the current best only when at least 1%
  * faster.  The jobs' frames receive the last render.  *opts supplies everything else
- * (precision, schedule AUTO or WAVEFRONT); report (optional) receives the trial count and
- * the device times with the given and the chosen options. */
+ * (precision; schedule AUTO or WAVEFRONT, and PERSISTENT, the outcome of an earlier tune, is
+ * tuned as AUTO); report (optional) receives the trial count and the device times with the
+ * given and the chosen options.  Launch shapes never change an image.  Choosing the
+ * PERSISTENT schedule can change f32 pixels: other kernels finish them and fuse f32
+ * operations differently (f64 images and accepted-sample counts stay identical). */
 typedef struct gt_autotune_report {
     uint32_t struct_size;
     uint32_t trials;   /* renders timed */

@@ -43,6 +43,8 @@ def lib() -> C.CDLL:
                 "orc_trace_primary": (i32, [vp, vp, u32, vp, vp, vp]),
                 "orc_render": (i32, [vp, vp, u32, vp, vp, i32, u32, u32, u32, u32, u32, i32, vp, vp, vp, vp]),
                 "orc_pixel_seed": (u64, [u64, u32, u32]),
+                "orc_slab": (i32, [vp, vp, f64, f64, vp]),
+                "orc_pixel_trace": (C.c_int64, [vp, vp, u32, vp, vp, i32, u32, u32, vp, vp, u64]),
                 "orc_rng_u64": (None, [u64, u32, vp]),
                 "orc_rng_double": (None, [u64, u32, vp]),
                 "orc_perlin": (None, [u64, C.c_int, C.c_int, u32, vp, vp]),
@@ -164,6 +166,25 @@ class OracleScene:
         lib().orc_trace_primary(self.h, C.byref(camera_desc), stride, _ptr(ids), _ptr(t), C.byref(st))
         return ids, t, st.as_dict()
 
+    def pixel_trace(self, camera_desc, x: int, y: int, lights: np.ndarray | None = None, env=None,
+                    precision: int = 1):
+        """The decision trace of pixel (x, y): (types, outcomes, values) of every discrete
+        decision its samples take, in order (TraceEvent in gartus_oracle.hpp)."""
+        la = None if lights is None else np.ascontiguousarray(lights)
+        envd = env.desc() if env is not None else None
+        cap = 4096
+        while True:
+            kinds = np.zeros(2 * cap, dtype=np.int32)
+            values = np.zeros(cap)
+            n = lib().orc_pixel_trace(self.h, _ptr(la) if la is not None else None, len(la) if la is not None else 0,
+                                      C.byref(envd) if envd is not None else None, C.byref(camera_desc), precision,
+                                      x, y, _ptr(kinds), _ptr(values), cap)
+            if n < 0:
+                raise ValueError("pixel outside the image")
+            if n <= cap:
+                return kinds[0:2 * n:2], kinds[1:2 * n:2], values[:n]
+            cap = int(n)
+
     def render(self, camera_desc, lights: np.ndarray | None = None, env=None, precision: int = 1,
                threads: int = 1, window=(0, 0, 0, 0), aovs: bool = False):
         """Renders (a window of) the image; returns (rgb, accepted[, albedo, normal])."""
@@ -189,6 +210,16 @@ class OracleScene:
         if aovs:
             return rgb, acc, alb, nrm
         return rgb, acc
+
+
+def slab(ray, box, t_min: float, t_max: float):
+    """RayTraversal::hit_bounds (bvh.rs:119-146): the entry distance of ray (origin,
+    direction[, time]) into box (min xyz, max xyz), or None."""
+    r = np.zeros(7)
+    r[:len(np.ravel(ray))] = np.ravel(ray)
+    b = np.ascontiguousarray(box, dtype=np.float64).reshape(6)
+    e = C.c_double(0.0)
+    return e.value if lib().orc_slab(_ptr(r), _ptr(b), float(t_min), float(t_max), C.byref(e)) else None
 
 
 def camera_size(camera_desc):

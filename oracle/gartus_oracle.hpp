@@ -336,13 +336,112 @@ template <class R> struct Hit {
     bool front_face = false;
     int prim = -1;
     uint32_t material = 0;
+    R margin{1}; // decision trace only: min(|cos| of the ray against the normal, edge distance in (u, v))
 };
+
+// Decision trace (test infrastructure).  When g_trace is set, the renderer records every
+// discrete decision of a pixel's samples in order: which primitive a ray hits, what a
+// material does, the Schlick/TIR choice, Russian roulette, the mixture choice, the pdf
+// cut-offs, the next-event shadow tests, texture cells, environment texel picks and each
+// sample's end.  An f32 and an f64 run of one pixel are then compared decision by
+// decision: the first pair that differs names the decision f32 rounding flipped.  `value`
+// is the decision's margin where it has one (0 at the decision's boundary).
+struct TraceEvent {
+    int32_t type, outcome;
+    double value;
+};
+enum : int32_t {
+    TR_SAMPLE = 1, // outcome: 1 finite sample, 0 dropped; value the sample's channel sum
+    TR_HIT,        // outcome: primitive (media -2 - k), -1 miss; value the hit's margin
+    TR_SCATTER,    // outcome: SCATTER_* kind
+    TR_DIELECTRIC, // outcome: 0 refract, 1 Schlick reflection, 2 total internal reflection
+    TR_RR,         // outcome: 1 survives, 0 terminated, 2 black throughput; value u - p
+    TR_MIXTURE,    // outcome: 1 light target, 0 material; value u - weight
+    TR_PDF,        // outcome: 0 continuation pdf cut, 1 scattering pdf cut; value the pdf
+    TR_NEE_AREA,   // outcome: primitive the shadow ray hits, -1 none, -3 sample rejected; value its margin
+    TR_NEE_ENV,    // outcome: 1 unoccluded, 0 occluded, -3 sample rejected; value the occluder's margin
+    TR_LIGHT_PICK, // outcome: target index; value the pick's remainder over the total weight
+    TR_TEXTURE,    // outcome: checker parity; value the coordinates' distance to a cell boundary
+    TR_ENV_PICK    // outcome: environment texel; value the draw's distance to a CDF step over the total
+};
+inline thread_local std::vector<TraceEvent>* g_trace = nullptr;
+inline void trace_note(int32_t type, int32_t outcome, double value = 0.0) {
+    if (g_trace) g_trace->push_back(TraceEvent{type, outcome, value});
+}
+
+// Origin of a ray leaving hit h in direction dir.  f64: the hit point, the reference's
+// rule (Ray::new(rec.point, ...), camera.rs:1799-1861, material.rs:2087-2351).  f32: the
+// point moved off the surface by 2^-19 (max|p| + 1) along the oriented normal, on the side
+// the ray leaves to, as the f32 device path does, so that the f32 oracle restates the f32
+// device algorithm (f32 hit points are too coarse for t_min = 0.001 at grazing angles).
+template <class R> inline V3<R> spawn_origin(const Hit<R>& h, V3<R> dir);
+template <> inline V3<double> spawn_origin<double>(const Hit<double>& h, V3<double>) { return h.point; }
+template <> inline V3<float> spawn_origin<float>(const Hit<float>& h, V3<float> dir) {
+    const float m = std::fmax(std::fmax(std::fabs(h.point.x), std::fabs(h.point.y)), std::fabs(h.point.z)) + 1.0f;
+    const float e = dot(dir, h.normal) >= 0.0f ? m * 0x1p-19f : -m * 0x1p-19f;
+    return h.point + h.normal * e;
+}
+
+// f32 roots of hit_sphere_in_interval with less rounding, as the f32 device path computes
+// them.  The discriminant is a (r^2 - |l|^2) with l = oc - (h / a) d, the centre's offset
+// from the ray's closest approach (Haines, Guenther, Akenine-Moeller, "Precision
+// Improvements for Ray/Sphere Intersection", Ray Tracing Gems, 2019): h^2 - a c cancels
+// for a sphere small against its distance.  c = |oc|^2 - r^2 keeps its products' rounding
+// errors (two-product by fused multiply-add) and its sums' (two-sum), so it stays accurate
+// near a large sphere, and each root comes from the cancellation-free form
+// (q = h + sign(h) sqrt(disc): the roots are c / q and q / a).  In exact arithmetic these
+// are the reference's roots, tested in the reference's order.
+inline float two_sum_err(float a, float b, float s) {
+    const float bb = s - a;
+    return (a - (s - bb)) + (b - bb);
+}
 
 // Interval::surrounds (object.rs:56-58).
 template <class R> inline bool surrounds(R lo, R hi, R x) { return lo < x && x < hi; }
 
+inline bool sphere_roots_f32(V3<float> center, float radius, const Ray<float>& ray, float& first, float& second) {
+    const V3<float> oc = center - ray.o;
+    const float a = length_squared(ray.d);
+    if (a <= float(kEps)) return false;
+    const float h = dot(ray.d, oc);
+    const float tc = h / a;
+    const V3<float> l{std::fma(-ray.d.x, tc, oc.x), std::fma(-ray.d.y, tc, oc.y), std::fma(-ray.d.z, tc, oc.z)};
+    const float disc_a = std::fma(radius, radius, -length_squared(l));
+    if (disc_a < 0.0f) return false;
+    const float px = oc.x * oc.x, py = oc.y * oc.y, pz = oc.z * oc.z, rr = radius * radius;
+    const float e = (std::fma(oc.x, oc.x, -px) + std::fma(oc.y, oc.y, -py)) + (std::fma(oc.z, oc.z, -pz) -
+                                                                               std::fma(radius, radius, -rr));
+    const float s1 = px + py, s2 = s1 + pz, s3 = s2 - rr;
+    const float c = s3 + (((two_sum_err(px, py, s1) + two_sum_err(s1, pz, s2)) + two_sum_err(s2, -rr, s3)) + e);
+    const float sq = std::sqrt(a * disc_a);
+    const float q = h >= 0.0f ? h + sq : h - sq;
+    if (q == 0.0f) {
+        first = second = 0.0f;
+    } else if (h >= 0.0f) {
+        first = c / q;
+        second = q / a;
+    } else {
+        first = q / a;
+        second = c / q;
+    }
+    return true;
+}
+
 // hit_sphere_in_interval, object.rs:986-1013.
 template <class R> inline bool hit_sphere_root(V3<R> center, R radius, const Ray<R>& ray, R tmin, R tmax, R& root) {
+    if constexpr (sizeof(R) == 4) {
+        float first, second;
+        if (!sphere_roots_f32(center, radius, ray, first, second)) return false;
+        if (surrounds(tmin, tmax, first)) {
+            root = first;
+            return true;
+        }
+        if (surrounds(tmin, tmax, second)) {
+            root = second;
+            return true;
+        }
+        return false;
+    }
     V3<R> oc = center - ray.o;
     R a = length_squared(ray.d);
     if (a <= R(kEps)) return false;
@@ -432,6 +531,7 @@ template <class R> inline bool intersect(const Prim<R>& p, const Ray<R>& ray, R 
         h.point = point;
         h.t = root;
         set_face(h, ray, outward);
+        if (g_trace) h.margin = std::fabs(dot(normalized(ray.d), outward));
         return true;
     }
     case GT_GEOM_TRIANGLE: {
@@ -444,6 +544,8 @@ template <class R> inline bool intersect(const Prim<R>& p, const Ray<R>& ray, R 
         h.u = u;
         h.v = v;
         set_face(h, ray, n);
+        if (g_trace)
+            h.margin = rmin(std::fabs(dot(normalized(ray.d), normalized(n))), rmin(rmin(u, v), R(1) - u - v));
         return true;
     }
     case GT_GEOM_QUAD: {
@@ -456,6 +558,9 @@ template <class R> inline bool intersect(const Prim<R>& p, const Ray<R>& ray, R 
         h.u = u;
         h.v = v;
         set_face(h, ray, n);
+        if (g_trace)
+            h.margin = rmin(std::fabs(dot(normalized(ray.d), normalized(n))),
+                            rmin(rmin(u, R(1) - u), rmin(v, R(1) - v)));
         return true;
     }
     }
@@ -938,6 +1043,13 @@ template <class R> struct Material {
             int64_t yi = as_i64(double(std::floor(tex_inv_scale * h.point.y)));
             int64_t zi = as_i64(double(std::floor(tex_inv_scale * h.point.z)));
             bool is_even = ((xi + yi + zi) % 2) == 0;
+            if (g_trace) {
+                auto edge = [](double c) { return std::fabs(c - std::round(c)); };
+                trace_note(TR_TEXTURE, is_even ? 0 : 1,
+                           std::fmin(std::fmin(edge(double(tex_inv_scale * h.point.x)),
+                                               edge(double(tex_inv_scale * h.point.y))),
+                                     edge(double(tex_inv_scale * h.point.z))));
+            }
             return is_even ? even : odd;
         }
         return color;
@@ -1111,7 +1223,7 @@ template <class R> inline Scatter<R> scatter(const Material<R>& m, const Ray<R>&
         V3<R> dir = refl + rng.random_unit_vector_spherical<R>() * m.param;
         if (dot(dir, h.normal) <= R(0)) return s;
         s.kind = SCATTER_SPECULAR;
-        s.ray = Ray<R>{h.point, dir, in.time};
+        s.ray = Ray<R>{spawn_origin(h, dir), dir, in.time};
         s.att = m.color;
         return s;
     }
@@ -1128,11 +1240,15 @@ template <class R> inline Scatter<R> scatter(const Material<R>& m, const Ray<R>&
             R r0 = (R(1) - ratio) / (R(1) + ratio); // Dielectric::reflectance, material.rs:2213-2219
             r0 = r0 * r0;
             R refl = r0 + (R(1) - r0) * powi5(R(1) - cos_t);
-            reflect = refl > rng.random_double<R>();
+            const R u = rng.random_double<R>();
+            reflect = refl > u;
+            trace_note(TR_DIELECTRIC, reflect ? 1 : 0, double(u) - double(refl));
+        } else {
+            trace_note(TR_DIELECTRIC, 2, double(ratio * sin_t) - 1.0);
         }
         dir = reflect ? reflected(unit, h.normal) : refracted(unit, h.normal, ratio);
         s.kind = SCATTER_SPECULAR;
-        s.ray = Ray<R>{h.point, dir, in.time};
+        s.ray = Ray<R>{spawn_origin(h, dir), dir, in.time};
         s.att = V3<R>(1, 1, 1);
         return s;
     }
@@ -1305,10 +1421,14 @@ template <class R> struct LightList { // WeightedSamplingTargetList, scene.rs:42
     V3<R> random_direction(V3<R> origin, R time, SampleRng& rng) const {
         if (targets.empty() || total <= R(0)) return V3<R>(1, 0, 0);
         R pick = rng.random_range<R>(R(0), total);
-        for (const auto& t : targets) {
-            pick -= t.weight;
-            if (pick <= R(0)) return geometry_random_direction(t.geom, origin, time, rng);
+        for (size_t k = 0; k < targets.size(); ++k) {
+            pick -= targets[k].weight;
+            if (pick <= R(0)) {
+                trace_note(TR_LIGHT_PICK, int32_t(k), double(pick) / double(total));
+                return geometry_random_direction(targets[k].geom, origin, time, rng);
+            }
         }
+        trace_note(TR_LIGHT_PICK, int32_t(targets.size()) - 1, double(pick) / double(total));
         return geometry_random_direction(targets.back().geom, origin, time, rng);
     }
 };
@@ -1382,6 +1502,10 @@ template <class R> struct Environment {
         double target = double(rng.random_double<R>()) * total;
         size_t idx = size_t(std::lower_bound(cdf.begin(), cdf.end(), target) - cdf.begin());
         idx = std::min(idx, weights.size() - 1);
+        if (g_trace) {
+            const double lo = idx > 0 ? cdf[idx - 1] : 0.0;
+            trace_note(TR_ENV_PICK, int32_t(idx), std::fmin(target - lo, cdf[idx] - target) / total);
+        }
         size_t x = idx % width, y = idx / width;
         double u = (double(x) + double(rng.random_double<R>())) / double(width);
         double t0 = kPi * (double(y) / double(height));
@@ -1900,9 +2024,14 @@ template <class R> struct Renderer {
     bool rr_survives(uint32_t bounce, V3<R>& att, SampleRng& rng) const { // camera.rs:2498-2523
         if (rr_min_depth < 0 || bounce < uint32_t(rr_min_depth)) return true;
         R m = max_component(att);
-        if (!std::isfinite(m) || m <= R(kEps)) return false;
+        if (!std::isfinite(m) || m <= R(kEps)) {
+            trace_note(TR_RR, 2, double(m));
+            return false;
+        }
         R p = rclamp(m, R(kRrMin), R(kRrMax));
-        if (rng.random_double<R>() >= p) return false;
+        const R u = rng.random_double<R>();
+        trace_note(TR_RR, u >= p ? 0 : 1, double(u) - double(p));
+        if (u >= p) return false;
         att = cdiv(att, p);
         return true;
     }
@@ -1921,12 +2050,15 @@ template <class R> struct Renderer {
         for (uint32_t bounce = 0; bounce < cam.desc.max_depth; ++bounce) {
             Hit<R> rec;
             if (!scene->world_hit(ray, R(kShadowAcne), inf, rec, rng)) {
+                trace_note(TR_HIT, -1);
                 V3<R> miss = miss_radiance(ray.d) * miss_w;
                 return color + cmul(att, miss);
             }
+            trace_note(TR_HIT, rec.prim, double(rec.margin));
             const Material<R>& m = scene->materials[rec.material];
             if (allow_emitted) color = color + cmul(att, emitted(m, rec));
             Scatter<R> s = scatter(m, ray, rec, rng);
+            trace_note(TR_SCATTER, int32_t(s.kind));
             if (s.kind == SCATTER_NONE) return color;
             if (s.kind == SCATTER_SPECULAR) {
                 att = cmul(att, s.att);
@@ -1937,8 +2069,12 @@ template <class R> struct Renderer {
                 continue;
             }
             if (nee) {
-                if (lights) color = color + cmul(att, direct_lighting(ray, rec, m, s.att, rng));
-                if (env) color = color + cmul(att, environment_lighting(ray, rec, m, s.att, rng));
+                // Both shadow rays of a bounce leave from one origin: the side of the area
+                // light's direction when that sample is valid, else the environment's.
+                const V3<R>* area_dir = nullptr;
+                V3<R> adir;
+                if (lights) color = color + cmul(att, direct_lighting(ray, rec, m, s.att, rng, adir, area_dir));
+                if (env) color = color + cmul(att, environment_lighting(ray, rec, m, s.att, rng, area_dir));
             }
             // SamplingStrategy::continuation_sample (camera.rs:165-195)
             V3<R> dir;
@@ -1946,7 +2082,9 @@ template <class R> struct Renderer {
             bool suppress = false, weight_env = false;
             if (!nee && lights) {
                 R w = light_pdf_weight;
-                if (rng.random_double<R>() < w)
+                const R u = rng.random_double<R>();
+                trace_note(TR_MIXTURE, u < w ? 1 : 0, double(u) - double(w));
+                if (u < w)
                     dir = lights->random_direction(rec.point, ray.time, rng);
                 else
                     dir = s.pdf.generate(rng);
@@ -1957,10 +2095,16 @@ template <class R> struct Renderer {
                 suppress = nee && lights;
                 weight_env = nee && env;
             }
-            if (!std::isfinite(pdf) || pdf <= R(kEps)) return color;
-            Ray<R> scattered{rec.point, dir, ray.time};
+            if (!std::isfinite(pdf) || pdf <= R(kEps)) {
+                trace_note(TR_PDF, 0, double(pdf));
+                return color;
+            }
+            Ray<R> scattered{spawn_origin(rec, dir), dir, ray.time};
             R sp = scattering_pdf(m, ray, rec, dir);
-            if (!std::isfinite(sp) || sp <= R(0)) return color;
+            if (!std::isfinite(sp) || sp <= R(0)) {
+                trace_note(TR_PDF, 1, double(sp));
+                return color;
+            }
             R next_miss_w = R(1);
             if (weight_env && env) next_miss_w = power_heuristic(pdf, env->pdf_value(dir));
             att = cmul(att, s.att * (sp / pdf));
@@ -1973,15 +2117,28 @@ template <class R> struct Renderer {
     }
 
     // estimate_direct_lighting (camera.rs:2225-2262).
-    V3<R> direct_lighting(const Ray<R>& in, const Hit<R>& rec, const Material<R>& m, V3<R> satt, SampleRng& rng) const {
+    // valid_dir is set to &dir_out when the sample passes both pdf tests (its shadow ray is
+    // traced).
+    V3<R> direct_lighting(const Ray<R>& in, const Hit<R>& rec, const Material<R>& m, V3<R> satt, SampleRng& rng,
+                          V3<R>& dir_out, const V3<R>*& valid_dir) const {
         V3<R> dir = lights->random_direction(rec.point, in.time, rng);
         R lp = lights->pdf_value(rec.point, in.time, dir);
-        if (!std::isfinite(lp) || lp <= R(kEps)) return V3<R>();
-        Ray<R> shadow{rec.point, dir, in.time};
+        if (!std::isfinite(lp) || lp <= R(kEps)) {
+            trace_note(TR_NEE_AREA, -3, double(lp));
+            return V3<R>();
+        }
+        Ray<R> shadow{spawn_origin(rec, dir), dir, in.time};
         R sp = scattering_pdf(m, in, rec, dir);
-        if (!std::isfinite(sp) || sp <= R(0)) return V3<R>();
+        if (!std::isfinite(sp) || sp <= R(0)) {
+            trace_note(TR_NEE_AREA, -3, double(sp));
+            return V3<R>();
+        }
+        dir_out = dir;
+        valid_dir = &dir_out;
         Hit<R> lh;
-        if (!scene->world_hit(shadow, R(kShadowAcne), std::numeric_limits<R>::infinity(), lh, rng)) return V3<R>();
+        const bool lit = scene->world_hit(shadow, R(kShadowAcne), std::numeric_limits<R>::infinity(), lh, rng);
+        trace_note(TR_NEE_AREA, lit ? lh.prim : -1, lit ? double(lh.margin) : 1.0);
+        if (!lit) return V3<R>();
         V3<R> e = emitted(scene->materials[lh.material], lh);
         if (!finite3(e)) return V3<R>();
         return cmul(satt, e) * (sp / lp);
@@ -1989,17 +2146,25 @@ template <class R> struct Renderer {
 
     // estimate_environment_lighting (camera.rs:2264-2297).
     V3<R> environment_lighting(const Ray<R>& in, const Hit<R>& rec, const Material<R>& m, V3<R> satt,
-                               SampleRng& rng) const {
+                               SampleRng& rng, const V3<R>* area_dir) const {
         V3<R> dir;
         R ep;
         env->sample_direction(rng, dir, ep);
-        if (!std::isfinite(ep) || ep <= R(kEps)) return V3<R>();
-        Ray<R> shadow{rec.point, dir, in.time};
+        if (!std::isfinite(ep) || ep <= R(kEps)) {
+            trace_note(TR_NEE_ENV, -3, double(ep));
+            return V3<R>();
+        }
+        Ray<R> shadow{spawn_origin(rec, area_dir ? *area_dir : dir), dir, in.time};
         R sp = scattering_pdf(m, in, rec, dir);
-        if (!std::isfinite(sp) || sp <= R(0)) return V3<R>();
+        if (!std::isfinite(sp) || sp <= R(0)) {
+            trace_note(TR_NEE_ENV, -3, double(sp));
+            return V3<R>();
+        }
         R mis = power_heuristic(ep, sp);
         Hit<R> sh;
-        if (scene->world_hit(shadow, R(kShadowAcne), std::numeric_limits<R>::infinity(), sh, rng)) return V3<R>();
+        const bool occluded = scene->world_hit(shadow, R(kShadowAcne), std::numeric_limits<R>::infinity(), sh, rng);
+        trace_note(TR_NEE_ENV, occluded ? 0 : 1, occluded ? double(sh.margin) : 1.0);
+        if (occluded) return V3<R>();
         return cmul(satt, env->radiance(dir)) * (mis * sp / ep);
     }
 
@@ -2016,6 +2181,7 @@ template <class R> struct Renderer {
                 V3<R> mean, m2;
                 for (uint32_t i = 0; i < mx; ++i) {
                     V3<R> s = ray_color(cam.ray_for_pixel_sample(x, y, rng), rng);
+                    trace_note(TR_SAMPLE, finite3(s) ? 1 : 0, finite3(s) ? double(s.x + s.y + s.z) : 0.0);
                     if (!finite3(s)) continue;
                     accepted += 1;
                     R count = R(accepted);
@@ -2029,6 +2195,7 @@ template <class R> struct Renderer {
             }
             for (uint32_t i = 0; i < cam.desc.samples_per_pixel; ++i) {
                 V3<R> s = ray_color(cam.ray_for_pixel_sample(x, y, rng), rng);
+                trace_note(TR_SAMPLE, finite3(s) ? 1 : 0, finite3(s) ? double(s.x + s.y + s.z) : 0.0);
                 if (finite3(s)) {
                     sum = sum + s;
                     accepted += 1;
@@ -2039,6 +2206,7 @@ template <class R> struct Renderer {
             for (uint32_t sy = 0; sy < g; ++sy)
                 for (uint32_t sx = 0; sx < g; ++sx) {
                     V3<R> s = ray_color(cam.ray_for_pixel_stratified(x, y, sx, sy, g, rng), rng);
+                    trace_note(TR_SAMPLE, finite3(s) ? 1 : 0, finite3(s) ? double(s.x + s.y + s.z) : 0.0);
                     if (finite3(s)) {
                         sum = sum + s;
                         accepted += 1;

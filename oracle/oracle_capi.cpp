@@ -104,9 +104,88 @@ int render_impl(const Scene<R>& scene, const gt_light_target* lights, uint32_t n
     return 0;
 }
 
+// The decision trace of one pixel (all its samples, in order): the set-up of render_impl
+// for one pixel, with g_trace pointing at `out`.
+template <class R>
+int trace_impl(const Scene<R>& scene, const gt_light_target* lights, uint32_t nl, const gt_environment_desc* envd,
+               const gt_camera_desc* cam, uint32_t x, uint32_t y, std::vector<TraceEvent>& out) {
+    LightList<R> ll;
+    for (uint32_t i = 0; i < nl; ++i) {
+        LightTarget<R> t;
+        t.geom = Prim<R>::from_geometry(lights[i].geometry, 0);
+        t.weight = R(lights[i].weight);
+        ll.total = ll.total + t.weight;
+        ll.targets.push_back(t);
+    }
+    Environment<R> env;
+    if (envd) {
+        env.format = int(envd->format);
+        env.width = envd->width;
+        env.height = envd->height;
+        size_t n = size_t(env.width) * env.height * 3;
+        if (env.format == GT_ENV_SRGB8) {
+            const uint8_t* p = static_cast<const uint8_t*>(envd->texels);
+            env.px8.assign(p, p + n);
+        } else {
+            const float* p = static_cast<const float*>(envd->texels);
+            env.px32.assign(p, p + n);
+        }
+        env.build();
+    }
+    Renderer<R> r;
+    r.scene = &scene;
+    r.lights = lights ? &ll : nullptr;
+    r.env = envd ? &env : nullptr;
+    r.setup(*cam);
+    if (x >= r.cam.width || y >= r.cam.height) return 1;
+    uint32_t acc = 0;
+    g_trace = &out;
+    r.pixel(x, y, acc);
+    g_trace = nullptr;
+    return 0;
+}
+
 } // namespace
 
 extern "C" {
+
+// Decision trace of pixel (x, y) (TraceEvent): up to `cap` events as (type, outcome)
+// pairs and values; returns the number of events the pixel made (possibly above cap), or
+// -1 on error.
+int64_t orc_pixel_trace(void* sp, const gt_light_target* lights, uint32_t nl, const gt_environment_desc* env,
+                        const gt_camera_desc* cam, int precision, uint32_t x, uint32_t y, int32_t* kinds,
+                        double* values, uint64_t cap) {
+    auto* s = static_cast<OrcScene*>(sp);
+    std::vector<TraceEvent> ev;
+    try {
+        const int rc = precision == 1 ? trace_impl<double>(s->s64, lights, nl, env, cam, x, y, ev)
+                                      : trace_impl<float>(s->s32, lights, nl, env, cam, x, y, ev);
+        if (rc) return -1;
+    } catch (...) {
+        g_trace = nullptr;
+        return -1;
+    }
+    for (size_t i = 0; i < ev.size() && i < cap; ++i) {
+        kinds[2 * i] = ev[i].type;
+        kinds[2 * i + 1] = ev[i].outcome;
+        values[i] = ev[i].value;
+    }
+    return int64_t(ev.size());
+}
+
+// RayTraversal::hit_bounds (bvh.rs:119-146) of one ray {o, d, time} against box6 {min, max}.
+int orc_slab(const double* ray7, const double* box6, double tmin, double tmax, double* entry) {
+    Ray<double> ray{{ray7[0], ray7[1], ray7[2]}, {ray7[3], ray7[4], ray7[5]}, ray7[6]};
+    Bounds b;
+    for (int i = 0; i < 3; ++i) {
+        b.mn[i] = box6[i];
+        b.mx[i] = box6[3 + i];
+    }
+    double e = 0.0;
+    const bool hit = RayTraversal<double>(ray).hit_bounds(b, tmin, tmax, e);
+    if (hit && entry) *entry = e;
+    return hit ? 1 : 0;
+}
 
 void* orc_scene_create(const gt_scene_desc* d) {
     try {

@@ -71,6 +71,16 @@ def test_camera_defaults_match_ray_camera_new():
     assert (w.value, h.value, s.value) == (400, 225, 1)
 
 
+def test_python_camera_defaults_equal_the_library_defaults():
+    # RayCamera() describes a camera without the device library; its fields equal
+    # gt_camera_default's byte for byte.
+    from gartus_gb300.raytracing import RayCamera
+    for w, aspect in ((400, 16.0 / 9.0), (1, 1.0), (600, 1.0)):
+        d = abi.gt_camera_desc()
+        assert lib().gt_camera_default(w, aspect, C.byref(d)) == abi.GT_OK
+        assert bytes(RayCamera(w, aspect).desc()) == bytes(d)
+
+
 def test_invalid_camera_is_rejected_without_a_device():
     # validate_view (camera.rs:1161-1201) panics; the ABI returns GT_ERR_INVALID_ARG.
     d = abi.gt_camera_desc()

@@ -18,6 +18,7 @@ from gartus_gb300 import abi, scenes
 from gartus_gb300._lib import GartusError, check, lib
 from gartus_gb300.raytracing import (EnvironmentLight, ImageTexture, PathTracer, RayCamera, RayGeometry, RayMaterial,
                                      RayScene, SamplingTargetList)
+from tests.divergence import assert_explained, assert_modes_agree
 from tests.helpers import rel_err
 
 pytestmark = pytest.mark.gpu
@@ -142,30 +143,20 @@ def test_f64_path_matches_oracle(gpu_context, case, schedule):
 
 
 
-def _divergent(x, r, tol=1e-4):
-    return int((rel_err(x, r, floor=1e-3).max(axis=2) > tol).sum())
-
-
 @pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("case", ["final", "cornell_mixture", "cornell_nee", "bench"])
 def test_f32_path_same_streams(gpu_context, case, schedule):
-    # Same RNG streams in f32.  f32 rounding alone moves some pixels by more than 1e-4
-    # (grazing light/surface geometry, specular chains, flipped Russian-roulette and
-    # Schlick decisions).  The f32 restatement of the reference on the CPU shows the
-    # same effect, so the bound is: the GPU's f32 path diverges from the f64 reference
-    # on no more pixels than f32 arithmetic itself does (plus 2% slack for FMA and
-    # f32 transcendentals), and its image energy agrees to 1e-3.
+    # Same RNG streams in f32.  A pixel may leave the f64 reference by more than 1e-4 only
+    # where f32 rounding flipped one of its samples' decisions (a hit at an edge or
+    # silhouette, a Schlick or total-internal-reflection choice, Russian roulette, ...) or
+    # where the f32 restatement of the reference drifts as well (tests/divergence.py);
+    # every such pixel is counted by cause, with no slack.
     scene, cam, lights = _cases()[case]
     pt = PathTracer(cam, precision="f32", context=gpu_context, schedule=schedule)
     img = pt.render_with_lights_hdr_image(scene, lights) if lights else pt.render_hdr_image(scene)
     ref64, acc = _oracle_render(scene, cam, lights)
     ref32, _ = _oracle_render(scene, cam, lights, precision=0)
-    n = ref64.shape[0] * ref64.shape[1]
-    d_gpu = _divergent(img.pixels, ref64)
-    d_f32 = _divergent(ref32, ref64)
-    d_pair = _divergent(img.pixels, ref32)
-    print(f"{case}: pixels beyond 1e-4 of f64: gpu-f32 {d_gpu}/{n}, oracle-f32 {d_f32}/{n}; gpu-f32 vs oracle-f32 {d_pair}")
-    assert d_gpu <= 1.25 * d_f32 + 0.02 * n
+    assert_explained(f"{case}/{schedule}", scene, cam, img.pixels, ref64, ref32, lights)
     np.testing.assert_array_equal(img.accepted, acc)
     err = rel_err(img.pixels, ref64, floor=1e-3).max(axis=2)
     assert float(np.median(err)) <= 1e-5
@@ -233,8 +224,7 @@ def test_environment_light_matches_oracle(gpu_context, fmt):
     assert (err <= 1e-4).mean() >= 0.995
     img32 = PathTracer(cam, precision="f32", context=gpu_context).render_with_environment_hdr_image(scene, env)
     ref32, _ = _oracle_render(scene, cam, env=env, precision=0)
-    n = ref.shape[0] * ref.shape[1]
-    assert _divergent(img32.pixels, ref) <= 1.25 * _divergent(ref32, ref) + 0.02 * n
+    assert_explained(f"environment {fmt}", scene, cam, img32.pixels, ref, ref32, env=env)
 
 
 def test_adaptive_sampling_matches_oracle(gpu_context):
@@ -282,8 +272,7 @@ def test_mesh_heavy_small(gpu_context, precision):
     else:
         img = pt.render_with_environment_hdr_image(scene, env)
         ref32, _ = _oracle_render(scene, cam, env=env, precision=0)
-        n = ref.shape[0] * ref.shape[1]
-        assert _divergent(img.pixels, ref) <= _divergent(ref32, ref) + 0.02 * n
+        assert_explained("mesh-heavy small", scene, cam, img.pixels, ref, ref32, env=env)
     assert np.isfinite(img.pixels).all()
 
 
@@ -311,8 +300,7 @@ def test_noise_textures(gpu_context, precision):
     else:
         img = pt.render_hdr_image(scene)
         ref32, _ = _oracle_render(scene, cam, precision=0)
-        n = ref.shape[0] * ref.shape[1]
-        assert _divergent(img.pixels, ref) <= _divergent(ref32, ref) + 0.02 * n
+        assert_explained("noise textures", scene, cam, img.pixels, ref, ref32)
         assert np.median(rel_err(img.pixels, ref, floor=1e-3)) <= 1e-5
     # the textures vary over the image: not a constant grey
     assert np.std(ref) > 1e-3
@@ -335,7 +323,7 @@ def test_batch_matches_single_frames(gpu_context, precision):
         if precision == "f64":
             np.testing.assert_array_equal(img.pixels64, one.pixels64)
         else:
-            assert _divergent(img.pixels, one.pixels.astype(np.float64)) <= 0.05 * img.pixels.shape[0] * img.pixels.shape[1]
+            assert_modes_agree("batch frame vs single frame", scene, cam, img.pixels, one.pixels, lights)
     if precision == "f64":  # and the oracle agrees on one frame
         ref, acc = _oracle_render(scene, cams[1], lights)
         np.testing.assert_array_equal(imgs[1].accepted, acc)
@@ -359,7 +347,7 @@ def test_batch_wavefront_matches_single_frames(gpu_context, schedule):
         one = PathTracer(cam, context=gpu_context).render_with_lights_hdr_image(scene, lights)
         flipped = int((img.accepted != one.accepted).sum())
         assert flipped <= 0.02 * img.accepted.size, flipped
-        assert _divergent(img.pixels, one.pixels.astype(np.float64)) <= 0.05 * img.pixels.shape[0] * img.pixels.shape[1]
+        assert_modes_agree("striped batch frame vs single frame", scene, cam, img.pixels, one.pixels, lights)
 
 
 def test_autotune_keeps_the_image(gpu_context):
@@ -380,13 +368,16 @@ def test_autotune_keeps_the_image(gpu_context):
     if rep["schedule"] == "auto":
         np.testing.assert_array_equal(tuned.pixels, base.pixels)
     else:  # other kernels finish the pixels, fusing f32 operations differently
-        assert _divergent(tuned.pixels, base.pixels.astype(np.float64)) <= 0.05 * 64 * 64
+        assert_modes_agree("autotuned vs default", scene, cam, tuned.pixels, base.pixels, lights)
     # a batch tunes the same way
     cams = scenes.batch_cameras(frames=3, width=32, spp_cycle=(4,), max_samples=8)
     rep = PathTracer(cams[0], context=gpu_context).autotune(scene, lights, cameras=cams)
     assert rep["trials"] >= 10
-    with pytest.raises(GartusError):
-        PathTracer(cam, context=gpu_context, schedule="persistent").autotune(scene, lights)
+    # tuning the same tracer again (after a tune that may have chosen the persistent
+    # schedule) tunes from AUTO
+    again = pt.autotune(scene, lights)
+    assert again["trials"] >= 10 and again["schedule"] in ("auto", "persistent")
+    assert PathTracer(cam, context=gpu_context, schedule="persistent").autotune(scene, lights)["trials"] >= 10
 
 
 def test_batch_rejects_bad_jobs(gpu_context):
@@ -440,7 +431,8 @@ def test_accumulate_equals_one_render(gpu_context, precision):
     if precision == "f64":
         np.testing.assert_array_equal(img.pixels64, full.pixels64)
     else:  # the chunks may finish pixels in other kernels, which fuse f32 operations differently
-        assert _divergent(img.pixels, full.pixels.astype(np.float64)) <= 0.05 * 40 * 40
+        assert_modes_agree("accumulated vs one render", scene, base.with_samples_per_pixel(16), img.pixels,
+                           full.pixels, lights)
     # Misuse is rejected: a stratified camera, another seed, a size mismatch.
     with pytest.raises(GartusError) as e:
         PathTracer(scenes.cornell_camera(40, 2, 50), context=gpu_context).render_accumulate(scene, acc2, 1, lights=lights)
@@ -605,7 +597,7 @@ def test_schedules_agree(gpu_context, schedule, tail, grid, width, stripes):
     fa = PathTracer(cam, context=gpu_context, schedule=schedule, tail_slots=tail,
                     stripes=stripes).render_with_lights_hdr_image(scene, lights)
     fb = PathTracer(cam, context=gpu_context, schedule="persistent").render_with_lights_hdr_image(scene, lights)
-    assert _divergent(fa.pixels, fb.pixels.astype(np.float64)) <= 0.05 * fa.pixels.shape[0] * fa.pixels.shape[1]
+    assert_modes_agree(f"{schedule} vs persistent", scene, cam, fa.pixels, fb.pixels, lights)
 
 
 @pytest.mark.parametrize("precision", ["f64", "f32"])
@@ -627,7 +619,8 @@ def test_henyey_greenstein_spheres(gpu_context, precision):
         assert (err <= 1e-9).mean() >= 0.99, err.max()
     else:
         img = PathTracer(cam, context=gpu_context).render_hdr_image(scene)
-        assert _divergent(img.pixels, ref) <= 0.05 * ref.shape[0] * ref.shape[1]
+        ref32, _ = _oracle_render(scene, cam, precision=0)
+        assert_explained("henyey-greenstein", scene, cam, img.pixels, ref, ref32)
     with pytest.raises(ValueError):
         RayMaterial.henyey_greenstein((0.5, 0.5, 0.5), 1.0)
 
@@ -642,11 +635,9 @@ def test_gpu_bvh_matches_reference_tree(gpu_context):
     sah = PathTracer(cam, context=gpu_context).render_with_environment_hdr_image(scene, env)
     scene.use_gpu_bvh()
     gpu = PathTracer(cam, context=gpu_context).render_with_environment_hdr_image(scene, env)
-    n = sah.pixels.shape[0] * sah.pixels.shape[1]
     np.testing.assert_array_equal(gpu.accepted, sah.accepted)
-    assert _divergent(gpu.pixels, sah.pixels.astype(np.float64)) <= 0.02 * n
+    assert_modes_agree("linear BVH vs SAH tree", scene, cam, gpu.pixels, sah.pixels, env=env)
     ref, _ = _oracle_render(scene, cam, env=env)
-    assert _divergent(gpu.pixels, ref) <= 0.1 * n
     img64 = PathTracer(cam, precision="f64", context=gpu_context).render_with_environment_hdr_image(scene, env,
                                                                                                   want64=True)
     err = rel_err(img64.pixels64, ref, floor=1e-12).max(axis=2)
@@ -678,7 +669,7 @@ def test_gpu_bvh_edge_cases(gpu_context):
     a = PathTracer(cam, context=gpu_context).render_hdr_image(s)
     s.use_gpu_bvh()
     b = PathTracer(cam, context=gpu_context).render_hdr_image(s)
-    assert _divergent(b.pixels, a.pixels.astype(np.float64)) <= 0.02 * a.pixels.shape[0] * a.pixels.shape[1]
+    assert_modes_agree("linear BVH, one box centre", s, cam, b.pixels, a.pixels)
 
 
 def _textured_scene():
@@ -722,8 +713,7 @@ def test_image_textures(gpu_context, precision):
     else:
         img = PathTracer(cam, context=gpu_context).render_hdr_image(scene)
         ref32, _ = _oracle_render(scene, cam, precision=0)
-        n = ref.shape[0] * ref.shape[1]
-        assert _divergent(img.pixels, ref) <= _divergent(ref32, ref) + 0.02 * n
+        assert_explained("image textures", scene, cam, img.pixels, ref, ref32)
     assert np.std(ref) > 1e-3
 
 
@@ -772,8 +762,7 @@ def test_media_smoke_scene(gpu_context, precision, mode):
     else:
         img = render()
         ref32, _ = _oracle_render(scene, cam, use, precision=0)
-        n = ref.shape[0] * ref.shape[1]
-        assert _divergent(img.pixels, ref) <= _divergent(ref32, ref) + 0.03 * n
+        assert_explained(f"smoke {mode}", scene, cam, img.pixels, ref, ref32, use)
     st = pt.last_stats  # every ray ran in the persistent kernel's media variant
     assert st["persistent_rays"] == st["rays"] + st["shadow_rays"]
     assert (st["shadow_rays"] > 0) == (mode == "nee")
@@ -824,7 +813,7 @@ def test_media_batch_and_unsupported(gpu_context, precision):
         if precision == "f64":
             np.testing.assert_array_equal(img.pixels64, one.pixels64)
         else:
-            assert _divergent(img.pixels, one.pixels.astype(np.float64)) <= 0.05 * img.pixels.shape[0] * img.pixels.shape[1]
+            assert_modes_agree("media batch frame vs single frame", scene, cam, img.pixels, one.pixels, lights)
     # accumulation: 3 + 5 samples on one accumulator give the 8-sample render (the streams
     # continue in the persistent kernel's world variant)
     base = _smoke_camera(24, 1)
@@ -839,7 +828,8 @@ def test_media_batch_and_unsupported(gpu_context, precision):
     if precision == "f64":
         np.testing.assert_array_equal(img.pixels64, full.pixels64)
     else:
-        assert _divergent(img.pixels, full.pixels.astype(np.float64)) <= 0.05 * 24 * 24
+        assert_modes_agree("media accumulated vs one render", scene, base.with_samples_per_pixel(8), img.pixels,
+                           full.pixels, lights)
 
 
 def _bouncing_spheres(frame: int, n: int = 300):
@@ -886,8 +876,7 @@ def test_update_primitives_refit(gpu_context, builder):
         np.testing.assert_array_equal(scene.primitives_array(), fresh.primitives_array())
         a = pt32.render_hdr_image(scene)
         b = PathTracer(cam, context=gpu_context).render_hdr_image(fresh)
-        n = a.pixels.shape[0] * a.pixels.shape[1]
-        assert _divergent(a.pixels, b.pixels.astype(np.float64)) <= 0.01 * n
+        assert_modes_agree(f"refit frame {frame} vs rebuilt", fresh, cam, a.pixels, b.pixels)
         img64 = pt64.render_hdr_image(scene, want64=True)
         ref, acc = _oracle_render(fresh, cam)
         np.testing.assert_array_equal(img64.accepted, acc)
@@ -982,8 +971,7 @@ def test_meshes_and_instances(gpu_context, precision, mode):
     else:
         img = pt.render_with_lights_hdr_image(scene, lights)
         ref32, _ = _oracle_render(scene, cam, lights, precision=0)
-        n = ref.shape[0] * ref.shape[1]
-        assert _divergent(img.pixels, ref) <= _divergent(ref32, ref) + 0.03 * n
+        assert_explained(f"meshes {mode}", scene, cam, img.pixels, ref, ref32, lights)
     st = pt.last_stats
     assert st["persistent_rays"] == st["rays"] + st["shadow_rays"]
     assert np.std(ref) > 1e-3
@@ -1008,7 +996,7 @@ def test_meshes_aovs_batch_and_primary(gpu_context):
             if precision == "f64":
                 np.testing.assert_array_equal(img.pixels64, one.pixels64)
             else:
-                assert _divergent(img.pixels, one.pixels.astype(np.float64)) <= 0.05 * img.pixels.shape[0] * img.pixels.shape[1]
+                assert_modes_agree("object-world batch frame vs single frame", scene, c, img.pixels, one.pixels, lights)
     rays = np.zeros((64, 7))
     rays[:, :3] = (0.0, 1.0, 2.0)
     rays[:, 3:6] = np.random.default_rng(4).normal(size=(64, 3)) * 0.3 + (0.0, -0.2, -1.0)

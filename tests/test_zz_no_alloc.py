@@ -11,47 +11,65 @@ import pytest
 
 from gartus_gb300 import abi, scenes
 from gartus_gb300._lib import lib
-from gartus_gb300.raytracing import PathTracer, RayMaterial, RayScene
-from tests.helpers import rel_err
+from gartus_gb300.raytracing import EnvironmentLight, PathTracer, RayMaterial, RayScene
 
 pytestmark = pytest.mark.gpu
 
 
-def _call(ctx, scene, lights, cam, rgb_ptr, acc_ptr):
+def _call(ctx, scene, lights, cam, rgb_ptr, acc_ptr, env=None):
     return lib().gt_render_noalloc(scene._handle(ctx).h, lights._handle(ctx).h if lights is not None else None,
-                                   None, C.byref(cam.desc()), rgb_ptr, acc_ptr)
+                                   env._handle(ctx).h if env is not None else None, C.byref(cam.desc()), rgb_ptr,
+                                   acc_ptr)
 
 
-def test_noalloc_matches_gt_render_on_two_calls_in_a_row(gpu_context):
+def _twice(ctx, scene, lights, env, cam, ref):
+    """Two calls in a row into one pair of device buffers; each must give `ref` (gt_render's
+    persistent schedule runs the same kernels, so the images are identical) and the second
+    allocates nothing."""
     import torch
 
-    scene, lights = scenes.cornell_scene()
-    cam = scenes.cornell_camera(96, 4, 50)
-    # Set-up with the allocating entry point: makes scene and lights resident in f32 and
-    # gives the reference image.
-    ref = PathTracer(cam, context=gpu_context, schedule="persistent").render_with_lights_hdr_image(scene, lights)
     w, h, _ = cam.image_size()
-    dev = torch.device(f"cuda:{gpu_context.device}")
+    dev = torch.device(f"cuda:{ctx.device}")
     rgb = torch.full((h, w, 3), float("nan"), dtype=torch.float32, device=dev)
     acc = torch.zeros((h, w), dtype=torch.int32, device=dev)
     torch.cuda.synchronize(dev)
-    assert _call(gpu_context, scene, lights, cam, rgb.data_ptr(), acc.data_ptr()) == abi.GT_OK
+    assert _call(ctx, scene, lights, cam, rgb.data_ptr(), acc.data_ptr(), env) == abi.GT_OK, lib().gt_last_error()
     free_after_first = torch.cuda.mem_get_info(dev)[0]
     for call in range(2):
         rgb.fill_(float("nan"))
         acc.zero_()
         torch.cuda.synchronize(dev)
-        assert _call(gpu_context, scene, lights, cam, rgb.data_ptr(), acc.data_ptr()) == abi.GT_OK, \
+        assert _call(ctx, scene, lights, cam, rgb.data_ptr(), acc.data_ptr(), env) == abi.GT_OK, \
             lib().gt_last_error()
         out = rgb.cpu().numpy()
         assert np.isfinite(out).all()
         np.testing.assert_array_equal(acc.cpu().numpy().astype(np.uint32), ref.accepted)
-        # The f32 tolerance used for f32 comparisons elsewhere: pixels beyond 1e-4 relative
-        # only where f32 rounding flipped a decision.
-        err = rel_err(out, ref.pixels, floor=1e-3).max(axis=2)
-        assert (err > 1e-4).sum() <= 0.02 * err.size, call
-    # Nothing was allocated by the repeated calls.
+        np.testing.assert_array_equal(out, ref.pixels)
     assert torch.cuda.mem_get_info(dev)[0] == free_after_first
+
+
+def test_noalloc_matches_gt_render_on_two_calls_in_a_row(gpu_context):
+    scene, lights = scenes.cornell_scene()
+    cam = scenes.cornell_camera(96, 4, 50)
+    # Set-up with the allocating entry point: makes scene and lights resident in f32 and
+    # gives the reference image.
+    ref = PathTracer(cam, context=gpu_context, schedule="persistent").render_with_lights_hdr_image(scene, lights)
+    _twice(gpu_context, scene, lights, None, cam, ref)
+
+
+def test_noalloc_media_world_and_environment(gpu_context):
+    # The world variant (media after the surfaces) and an environment light through the
+    # same fixed scratch.
+    scene, lights = scenes.cornell_smoke_scene()
+    cam = scenes.cornell_camera(32, 1, 20).with_pixel_sample_mode(abi.GT_SAMPLE_RANDOM).with_samples_per_pixel(3)
+    ref = PathTracer(cam, context=gpu_context, schedule="persistent").render_with_lights_hdr_image(scene, lights)
+    _twice(gpu_context, scene, lights, None, cam, ref)
+    rng = np.random.default_rng(8)
+    env = EnvironmentLight(rng.integers(0, 256, size=(8, 16, 3), dtype=np.uint8))
+    scene = scenes.render_performance_scene()
+    cam = scenes.render_performance_camera().with_samples_per_pixel(2)
+    ref = PathTracer(cam, context=gpu_context, schedule="persistent").render_with_environment_hdr_image(scene, env)
+    _twice(gpu_context, scene, None, env, cam, ref)
 
 
 def test_noalloc_rejects_oversized_and_unprepared_inputs(gpu_context):
