@@ -362,7 +362,8 @@ enum : int32_t {
     TR_NEE_ENV,    // outcome: 1 unoccluded, 0 occluded, -3 sample rejected; value the occluder's margin
     TR_LIGHT_PICK, // outcome: target index; value the pick's remainder over the total weight
     TR_TEXTURE,    // outcome: checker parity; value the coordinates' distance to a cell boundary
-    TR_ENV_PICK    // outcome: environment texel; value the draw's distance to a CDF step over the total
+    TR_ENV_PICK,   // outcome: environment texel; value the draw's distance to a CDF step over the total
+    TR_THROUGHPUT  // not a decision (outcome 0): the path throughput's largest channel after a scatter
 };
 inline thread_local std::vector<TraceEvent>* g_trace = nullptr;
 inline void trace_note(int32_t type, int32_t outcome, double value = 0.0) {
@@ -2108,6 +2109,7 @@ template <class R> struct Renderer {
             R next_miss_w = R(1);
             if (weight_env && env) next_miss_w = power_heuristic(pdf, env->pdf_value(dir));
             att = cmul(att, s.att * (sp / pdf));
+            trace_note(TR_THROUGHPUT, 0, double(max_component(att)));
             ray = scattered;
             allow_emitted = !suppress;
             miss_w = next_miss_w;
