@@ -88,6 +88,10 @@ struct gt_denoiser {
     std::vector<__nv_bfloat16*> wb, wf; // forward / input-gradient BF16 weights
     std::vector<float*> dwp;             // padded FP32 weight gradients [cout_pp][9][cin_p]
     float* dbp = nullptr;                // bias gradients (each layer's at its b_off)
+    int wg_blocks = 1;                   // weight-gradient CTAs per tap
+    float* wpart = nullptr;              // their partial sums [9][wg_blocks][cout_pp][cin_p]
+    int bg_blocks = 1;                   // bias-gradient blocks
+    float* bpart = nullptr;              // their partial sums [bg_blocks][kBgMaxCh]
     // activations for the current (n, h, w)
     int n = 0, h = 0, w = 0;
     std::vector<void*> bufs;
@@ -367,23 +371,34 @@ gt_status check_err(gt_denoiser* d, cudaStream_t st) {
     return GT_OK;
 }
 
+// Weight and bias gradients of layer li: per-CTA partial sums reduced in a fixed order, so
+// the gradient does not depend on the order in which the CTAs run.
 void conv_wgrad(gt_denoiser* d, int li, const __nv_bfloat16* dy, const __nv_bfloat16* x, int lv, cudaStream_t st) {
     const Layer& l = d->layers[li];
-    ConvWgrad a;
+    ConvWgradTc a;
     a.dy = dy;
     a.cout = l.cout_pp;
     a.x = x;
     a.cin = l.cin_p;
-    a.dw = d->dwp[li];
     a.n = d->n;
     a.h = d->h >> lv;
     a.w = d->w >> lv;
     const long long P = (long long)a.n * a.h * a.w;
-    const int blocks = int(std::max<long long>(1, std::min<long long>((P + 15) / 16, 64)));
-    k_conv_wgrad<<<dim3(blocks, 9), 256, 0, st>>>(a);
+    const long long chunks = (P + kWgK - 1) / kWgK;
+    a.blocks = int(std::max<long long>(1, std::min<long long>(chunks, d->wg_blocks)));
+    a.part = d->wpart;
+    a.tmem_cols = uint32_t(tc_pow2_cols(a.cin));
+    a.err = d->err;
+    // At 256 tensor-memory columns a CTA asks for a third of the SM's shared memory, so
+    // that no more than two (512 columns) share an SM and none waits in tcgen05.alloc.
+    const int smem = a.tmem_cols == 256 ? std::max(wg_smem_bytes(a.cin), kWgSmemTwoPerSm) : wg_smem_bytes(a.cin);
+    k_conv_wgrad_tc<<<dim3(a.blocks, 9), 128, smem, st>>>(a);
     const int sms = d->ctx->num_sms > 0 ? d->ctx->num_sms : 1;
-    k_bias_grad<<<int(std::min<long long>(P, (long long)sms * 8)), 128, 0, st>>>(dy, l.cout_pp, l.cout, P,
-                                                                                  d->dbp + l.b_off);
+    k_wgrad_reduce<<<grid_for(9LL * a.cout * a.cin, 256, sms), 256, 0, st>>>(d->wpart, a.blocks, a.cout, a.cin,
+                                                                             d->dwp[li]);
+    const int bblocks = int(std::max<long long>(1, std::min<long long>(P, d->bg_blocks)));
+    k_bias_grad<<<bblocks, 128, 0, st>>>(dy, l.cout_pp, l.cout, P, d->bpart);
+    k_bias_reduce<<<1, 128, 0, st>>>(d->bpart, bblocks, l.cout, d->dbp + l.b_off);
 }
 
 // Forward pass (inputs already packed); d->out = log-space prediction.  Training keeps the
@@ -535,6 +550,17 @@ gt_status gt_denoiser_create(gt_context* ctx, uint64_t seed, gt_denoiser** out) 
         e = cudaFuncSetAttribute(k_conv_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemMax);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_conv_fwd_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemMax);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_conv_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 std::max(wg_smem_bytes(kWgMaxN), kWgSmemTwoPerSm));
+    // Two weight-gradient CTAs fit an SM (shared memory): about two per SM over the 9 taps.
+    const int sms = ctx->num_sms > 0 ? ctx->num_sms : 1;
+    d->wg_blocks = std::max(1, (2 * sms + 8) / 9);
+    d->bg_blocks = sms * 8;
+    size_t part_max = 0;
+    for (const Layer& l : d->layers) part_max = std::max(part_max, size_t(l.cout_pp) * l.cin_p);
+    al(reinterpret_cast<void**>(&d->wpart), 9 * size_t(d->wg_blocks) * part_max * sizeof(float));
+    al(reinterpret_cast<void**>(&d->bpart), size_t(d->bg_blocks) * kBgMaxCh * sizeof(float));
     d->wb.assign(d->layers.size(), nullptr);
     d->wf.assign(d->layers.size(), nullptr);
     d->dwp.assign(d->layers.size(), nullptr);
@@ -566,6 +592,8 @@ void gt_denoiser_destroy(gt_denoiser* d) {
     cudaFree(d->g);
     cudaFree(d->dbp);
     cudaFree(d->err);
+    cudaFree(d->wpart);
+    cudaFree(d->bpart);
     for (auto* p : d->wb) cudaFree(p);
     for (auto* p : d->wf) cudaFree(p);
     for (auto* p : d->dwp) cudaFree(p);

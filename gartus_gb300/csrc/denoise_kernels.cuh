@@ -6,7 +6,8 @@
 // K = 9 taps x input channels (k_conv_fwd_tc: tcgen05.mma with the accumulator in tensor
 // memory).  Its input gradient is the same GEMM with the taps flipped and the channel roles
 // swapped; its weight gradient is a GEMM over pixels (M = output channels, N = input
-// channels, K = pixels; k_conv_wgrad, mma.sync m16n8k16).
+// channels, K = pixels; k_conv_wgrad_tc, tcgen05.mma, reduced in a fixed order by
+// k_wgrad_reduce).
 #pragma once
 
 #include <cuda.h>
@@ -485,85 +486,199 @@ __global__ void __launch_bounds__(128) k_conv_fwd_tma(const __grid_constant__ Co
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
 }
 
-// dW[co][tap][ci] += sum_p dY[p][co] * X[p + tap][ci]; one block per (tap, pixel range).
-// 8 warps share the (16-channel co tile, 8-channel ci tile) pairs; 16 pixels at a time are
-// staged in shared memory.
-struct ConvWgrad {
-    const __nv_bfloat16* dy; // [P][cout]
-    int cout;                // multiple of 16 (rows of dw)
+// The weight gradient on the 5th-generation tensor cores: per tap, the GEMM
+// D[co][ci] = sum over pixels p of dY[p][co] * X[p + tap][ci] with M = output channels
+// (padded to 128 with zero rows), N = input channels (cin, a multiple of 16) and K = pixels.
+// CTA (b, tap) takes the 64-pixel chunks b, b + B, b + 2B, ... of the pixels; each chunk is
+// staged transposed into the K-major no-swizzle core-matrix layout (8 rows x 16 bytes:
+// 8 channels x 8 pixels) — A = dY^T [kc][co/8][co%8][8 pixels], B = X^T [kc][ci/8][ci%8][8
+// pixels] — and one thread issues its four K = 16 MMAs into the FP32 accumulator in tensor
+// memory and commits them to the stage's mbarrier; two stages overlap staging and MMAs.
+// The CTA writes its accumulator to its own slice of `part` ([tap][b][co][ci]); a second
+// kernel adds the slices in order of b, so the gradient is the same on every run.
+constexpr int kWgM = 128;            // MMA M (output channels, zero-padded)
+constexpr int kWgK = 64;             // pixels per staged chunk
+constexpr int kWgMaxN = 256;         // input channels (MMA N)
+constexpr int kWgABytes = (kWgK / 8) * (kWgM / 8) * 128;
+__host__ __device__ constexpr int wg_stage_bytes(int n) { return kWgABytes + (kWgK / 8) * (n / 8) * 128; }
+__host__ __device__ constexpr int wg_smem_bytes(int n) { return 128 + 2 * wg_stage_bytes(n); }
+constexpr int kWgSmemTwoPerSm = 78 * 1024; // three such CTAs exceed an SM's 228 KB
+
+struct ConvWgradTc {
+    const __nv_bfloat16* dy; // [P][cout] (pixels of n images of h x w)
+    int cout;                // multiple of 16, at most 128
     const __nv_bfloat16* x;  // [P][cin]
-    int cin;                 // multiple of 16
-    float* dw;               // [cout][9][cin] (accumulated)
+    int cin;                 // multiple of 16, at most 256 (MMA N)
+    float* part;             // [9][blocks][cout][cin]
+    int blocks;              // CTAs per tap (gridDim.x)
     int n, h, w;
+    uint32_t tmem_cols;      // power of two >= cin
+    uint32_t* err;
 };
-constexpr int kMaxCo = 96, kMaxCi = 176;
-__global__ void __launch_bounds__(256) k_conv_wgrad(ConvWgrad a) {
-    __shared__ __nv_bfloat16 sdy[16][kMaxCo + 8];
-    __shared__ __nv_bfloat16 sx[16][kMaxCi + 8];
+
+__global__ void __launch_bounds__(128) k_conv_wgrad_tc(ConvWgradTc a) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 64);
+    uint8_t* stage_base = smem + 128;
+    const int N = a.cin, stage_bytes = wg_stage_bytes(N);
     const int tap = blockIdx.y, dy = tap / 3 - 1, dx = tap % 3 - 1;
-    const int warp = threadIdx.x >> 5, g = lane() >> 2, t = lane() & 3;
-    const int mt = a.cout / 16, nt = a.cin / 8, tiles = mt * nt;
-    // this warp's tiles: warp, warp + 8, ... (at most ceil(6 * 22 / 8) = 17)
-    constexpr int kMaxT = 17;
-    float acc[kMaxT][4];
-#pragma unroll
-    for (int j = 0; j < kMaxT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    const int tid = threadIdx.x, warp = tid >> 5;
     const long long P = (long long)a.n * a.h * a.w;
-    for (long long p0 = (long long)blockIdx.x * 16; p0 < P; p0 += (long long)gridDim.x * 16) {
-        __syncthreads();
-        for (int i = threadIdx.x; i < 16 * (a.cout / 2); i += blockDim.x) {
-            const int r = i / (a.cout / 2), c = (i % (a.cout / 2)) * 2;
-            const long long p = p0 + r;
-            uint32_t v = 0;
-            if (p < P) v = __ldg(reinterpret_cast<const unsigned int*>(a.dy + size_t(p) * a.cout + c));
-            *reinterpret_cast<uint32_t*>(&sdy[r][c]) = v;
-        }
-        for (int i = threadIdx.x; i < 16 * (a.cin / 2); i += blockDim.x) {
-            const int r = i / (a.cin / 2), c = (i % (a.cin / 2)) * 2;
-            const long long p = p0 + r;
-            uint32_t v = 0;
-            if (p < P) {
-                const int x = int(p % a.w), yy = int((p / a.w) % a.h), nn = int(p / ((long long)a.w * a.h));
-                v = ld2(a.x, a.cin, nn, yy + dy, x + dx, a.h, a.w, c);
-            }
-            *reinterpret_cast<uint32_t*>(&sx[r][c]) = v;
-        }
-        __syncthreads();
+    const long long chunks = (P + kWgK - 1) / kWgK;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                     "r"(a.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < 2; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[s])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    // A rows co >= cout stay zero in both stages.
+    for (int i = tid; i < 2 * kWgABytes / 16; i += blockDim.x) {
+        const int s = i / (kWgABytes / 16), q = i % (kWgABytes / 16);
+        reinterpret_cast<uint4*>(stage_base + s * stage_bytes)[q] = make_uint4(0, 0, 0, 0);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    // Stages chunk `chunk` into stage s: dY^T into A, the tap-shifted X^T into B.
+    auto stage = [&](long long chunk, int s) {
+        uint8_t* A = stage_base + s * stage_bytes;
+        uint8_t* B = A + kWgABytes;
+        const long long p0 = chunk * kWgK;
+        const int cg = a.cout / 8, ng = N / 8;
+        for (int i = tid; i < kWgK * cg; i += blockDim.x) {
+            const int pl = i % kWgK, g = i / kWgK;
+            const long long p = p0 + pl;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (p < P) v = __ldg(reinterpret_cast<const uint4*>(a.dy + size_t(p) * a.cout + g * 8));
+            const uint16_t* e = reinterpret_cast<const uint16_t*>(&v);
+            uint8_t* dst = A + (pl >> 3) * ((kWgM / 8) * 128) + g * 128 + (pl & 7) * 2;
 #pragma unroll
-        for (int j = 0; j < kMaxT; ++j) {
-            const int tile = warp + 8 * j;
-            if (tile >= tiles) break;
-            const int co0 = (tile / nt) * 16, ci0 = (tile % nt) * 8;
-            uint32_t fa[4], fb[2];
-            fa[0] = pack_bf16(sdy[2 * t][co0 + g], sdy[2 * t + 1][co0 + g]);
-            fa[1] = pack_bf16(sdy[2 * t][co0 + g + 8], sdy[2 * t + 1][co0 + g + 8]);
-            fa[2] = pack_bf16(sdy[2 * t + 8][co0 + g], sdy[2 * t + 9][co0 + g]);
-            fa[3] = pack_bf16(sdy[2 * t + 8][co0 + g + 8], sdy[2 * t + 9][co0 + g + 8]);
-            fb[0] = pack_bf16(sx[2 * t][ci0 + g], sx[2 * t + 1][ci0 + g]);
-            fb[1] = pack_bf16(sx[2 * t + 8][ci0 + g], sx[2 * t + 9][ci0 + g]);
-            mma_bf16(acc[j], fa, fb);
+            for (int r = 0; r < 8; ++r) *reinterpret_cast<uint16_t*>(dst + r * 16) = e[r];
+        }
+        for (int i = tid; i < kWgK * ng; i += blockDim.x) {
+            const int pl = i % kWgK, g = i / kWgK;
+            const long long p = p0 + pl;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (p < P) {
+                const int x = int(p % a.w), y = int((p / a.w) % a.h), img = int(p / ((long long)a.w * a.h));
+                const int ys = y + dy, xs = x + dx;
+                if (ys >= 0 && ys < a.h && xs >= 0 && xs < a.w)
+                    v = __ldg(reinterpret_cast<const uint4*>(a.x + ((size_t(img) * a.h + ys) * a.w + xs) * N + g * 8));
+            }
+            const uint16_t* e = reinterpret_cast<const uint16_t*>(&v);
+            uint8_t* dst = B + (pl >> 3) * (ng * 128) + g * 128 + (pl & 7) * 2;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) *reinterpret_cast<uint16_t*>(dst + r * 16) = e[r];
+        }
+    };
+
+    const uint32_t idesc = tc_idesc(N);
+    bool ok = true;
+    int issued = 0; // chunks whose MMAs were committed
+    for (long long chunk = blockIdx.x; chunk < chunks; chunk += a.blocks, ++issued) {
+        const int s = issued & 1;
+        // stage s was last read by chunk issued - 2
+        if (issued >= 2) ok = mbar_wait(smem_u32(&mbar[s]), uint32_t(((issued - 2) >> 1) & 1), a.err);
+        if (__syncthreads_or(!ok)) {
+            ok = false;
+            break;
+        }
+        stage(chunk, s);
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t A = smem_u32(stage_base + s * stage_bytes), B = A + kWgABytes;
+#pragma unroll
+            for (int k = 0; k < kWgK / 16; ++k) {
+                const uint64_t ad = tc_desc(A + 2 * k * ((kWgM / 8) * 128), (kWgM / 8) * 128, 128);
+                const uint64_t bd = tc_desc(B + 2 * k * ((N / 8) * 128), (N / 8) * 128, 128);
+                const uint32_t acc = (issued > 0 || k > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smem_u32(&mbar[s]))
+                         : "memory");
         }
     }
+    // The MMAs read shared memory and write tensor memory until their last commit
+    // arrives: wait for it (bounded) also after a failed wait, before the memory is freed.
+    if (issued > 0) {
+        const int last = issued - 1;
+        if (!mbar_wait(smem_u32(&mbar[last & 1]), uint32_t((last >> 1) & 1), a.err)) ok = false;
+    }
+    if (__syncthreads_or(!ok) == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        // Thread t holds row t of D (TMEM lane t): output channel t.
+        const int co = tid;
+        float* dst = a.part + ((size_t(tap) * a.blocks + blockIdx.x) * a.cout + co) * N;
+        for (int cb = 0; cb < N; cb += 16) {
+            uint32_t v[16];
+            const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(cb);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+                "%15}, [%16];\n"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(taddr)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (co >= a.cout) continue;
 #pragma unroll
-    for (int j = 0; j < kMaxT; ++j) {
-        const int tile = warp + 8 * j;
-        if (tile >= tiles) break;
-        const int co0 = (tile / nt) * 16, ci0 = (tile % nt) * 8;
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const int co = co0 + g + (e >= 2 ? 8 : 0), ci = ci0 + 2 * t + (e & 1);
-            atomicAdd(&a.dw[(size_t(co) * 9 + tap) * a.cin + ci], acc[j][e]);
+            for (int j = 0; j < 16; j += 4)
+                *reinterpret_cast<float4*>(dst + cb + j) = make_float4(
+                    issued ? __uint_as_float(v[j]) : 0.f, issued ? __uint_as_float(v[j + 1]) : 0.f,
+                    issued ? __uint_as_float(v[j + 2]) : 0.f, issued ? __uint_as_float(v[j + 3]) : 0.f);
         }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
+}
+
+// dw[co][tap][ci] += sum over b = 0, 1, ... of part[tap][b][co][ci], in that order.
+__global__ void k_wgrad_reduce(const float* part, int blocks, int cout, int cin, float* dw) {
+    const long long count = 9LL * cout * cin;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+        const int ci = int(i % cin), co = int((i / cin) % cout), tap = int(i / ((long long)cin * cout));
+        float s = 0.f;
+        for (int b = 0; b < blocks; ++b) s += part[((size_t(tap) * blocks + b) * cout + co) * cin + ci];
+        dw[(size_t(co) * 9 + tap) * cin + ci] += s;
     }
 }
 
-// db[c] += sum_p dY[p][c] for the first `count` of `stride` channels (FP32 partial sums per
-// block, then atomics).
-__global__ void k_bias_grad(const __nv_bfloat16* dy, int stride, int count, long long P, float* db) {
+// Bias gradient, sum_p dY[p][c] for the first `count` of `stride` channels: FP32 partial
+// sums per block into part[block][c] (k_bias_reduce adds them in order of block).
+constexpr int kBgMaxCh = 128; // channels of a bias-gradient partial row
+__global__ void k_bias_grad(const __nv_bfloat16* dy, int stride, int count, long long P, float* part) {
     for (int ch = threadIdx.x; ch < count; ch += blockDim.x) {
         float s = 0.f;
         for (long long p = blockIdx.x; p < P; p += gridDim.x) s += __bfloat162float(dy[size_t(p) * stride + ch]);
-        atomicAdd(&db[ch], s);
+        part[size_t(blockIdx.x) * kBgMaxCh + ch] = s;
+    }
+}
+
+// db[ch] += the blocks' partial sums, in order of block.
+__global__ void k_bias_reduce(const float* part, int blocks, int count, float* db) {
+    for (int ch = threadIdx.x; ch < count; ch += blockDim.x) {
+        float s = 0.f;
+        for (int b = 0; b < blocks; ++b) s += part[size_t(b) * kBgMaxCh + ch];
+        db[ch] += s;
     }
 }
 

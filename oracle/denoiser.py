@@ -15,6 +15,14 @@ Definitions restated here:
             to 3 channels without ReLU
   output    out = conv_out + log1p(max(beauty, 0));  image = max(expm1(out), 0)
   loss      mean |out - log1p(max(target, 0))| over pixels and channels
+
+BF16-faithful mode (bf16=True): the same network with values and gradients rounded to
+BF16 where the library stores BF16 tensors — the network input, the weights (their
+gradient reaches the FP32 masters unrounded), every ReLU'd convolution output, the
+pooled tensors, and in the backward pass the gradient of each stored activation, of the
+concatenated decoder inputs, of the pooled tensors and of the prediction (the loss
+gradient).  Convolutions accumulate in float64 (the library in FP32), bias and residual
+stay unrounded.
 """
 from __future__ import annotations
 
@@ -72,10 +80,56 @@ def _log1p_clean(x):
     return torch.log1p(torch.clamp(x, min=0.0))
 
 
-def forward_log(params, beauty, albedo=None, normal=None):
-    """Log-space output [n, hp, wp, 3] (float64 torch) for inputs [n, h, w, 3]."""
+def _bf16(t):
+    import torch
+
+    return t.to(torch.bfloat16).to(torch.float64)
+
+
+def _rounders():
+    """(value and gradient, value only, gradient only) BF16 rounding as autograd functions."""
+    import torch
+
+    class Both(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, t):
+            return _bf16(t)
+
+        @staticmethod
+        def backward(ctx, g):
+            return _bf16(g)
+
+    class Value(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, t):
+            return _bf16(t)
+
+        @staticmethod
+        def backward(ctx, g):
+            return g
+
+    class Grad(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, t):
+            return t.clone()
+
+        @staticmethod
+        def backward(ctx, g):
+            return _bf16(g)
+
+    return Both.apply, Value.apply, Grad.apply
+
+
+def forward_log(params, beauty, albedo=None, normal=None, bf16=False):
+    """Log-space output [n, hp, wp, 3] (float64 torch) for inputs [n, h, w, 3]; bf16 rounds
+    where the library stores BF16 (the module docstring lists the points)."""
     import torch
     import torch.nn.functional as F
+
+    if bf16:
+        both, value, grad = _rounders()
+    else:
+        both = value = grad = lambda t: t
 
     b = torch.as_tensor(beauty, dtype=torch.float64)
     z = torch.zeros_like(b)
@@ -85,48 +139,50 @@ def forward_log(params, beauty, albedo=None, normal=None):
     x = torch.cat([lb, a, nm], dim=-1).permute(0, 3, 1, 2)
     x = _pad16(x)
     lbp = x[:, :3]
+    x = value(x)
     layers = _unflatten(params)
 
     def conv(i, t):
         w, bias, relu = layers[i]
-        y = F.conv2d(t, w, bias, padding=1)
-        return F.relu(y) if relu else y
+        y = F.conv2d(t, value(w), bias, padding=1)
+        return both(F.relu(y)) if relu else y
 
     L = len(CHANNELS)
     skips = []
     t = x
     for lv in range(L):
         if lv > 0:
-            t = F.avg_pool2d(t, 2)
+            t = both(F.avg_pool2d(t, 2))
         t = conv(2 * lv + 1, conv(2 * lv, t))
         skips.append(t)
     for k, lv in enumerate(range(L - 2, -1, -1)):
         up = F.interpolate(t, scale_factor=2, mode="nearest")
-        t = torch.cat([up, skips[lv]], dim=1)
+        t = grad(torch.cat([up, skips[lv]], dim=1))
         base = 2 * L + 2 * k
         t = conv(base + 1, conv(base, t))
-    out = conv(len(layers) - 1, t) + lbp
+    out = grad(conv(len(layers) - 1, t) + lbp)
     return out.permute(0, 2, 3, 1)
 
 
-def denoise(params, beauty, albedo=None, normal=None) -> np.ndarray:
-    """The denoised image [h, w, 3] of one frame (float64 numpy)."""
+def denoise(params, beauty, albedo=None, normal=None, bf16=False) -> np.ndarray:
+    """The denoised image [h, w, 3] of one frame (float64 numpy); bf16 as in forward_log."""
     import torch
 
     p = torch.as_tensor(np.asarray(params, dtype=np.float64))
     add = lambda t: None if t is None else np.asarray(t, dtype=np.float64)[None]
     h, w = beauty.shape[:2]
     with torch.no_grad():
-        out = forward_log(p, add(beauty), add(albedo), add(normal))[0, :h, :w]
+        out = forward_log(p, add(beauty), add(albedo), add(normal), bf16=bf16)[0, :h, :w]
     return np.maximum(np.expm1(out.numpy()), 0.0)
 
 
-def loss_and_grad(params, beauty, target, albedo=None, normal=None):
-    """(loss, flat gradient) in float64 for a batch [n, h, w, 3] (h, w multiples of 16)."""
+def loss_and_grad(params, beauty, target, albedo=None, normal=None, bf16=False):
+    """(loss, flat gradient) in float64 for a batch [n, h, w, 3] (h, w multiples of 16);
+    bf16 as in forward_log."""
     import torch
 
     p = torch.tensor(np.asarray(params, dtype=np.float64), requires_grad=True)
-    out = forward_log(p, beauty, albedo, normal)
+    out = forward_log(p, beauty, albedo, normal, bf16=bf16)
     tgt = _log1p_clean(torch.as_tensor(target, dtype=torch.float64))
     loss = (out - tgt).abs().mean()
     loss.backward()

@@ -363,7 +363,8 @@ enum : int32_t {
     TR_LIGHT_PICK, // outcome: target index; value the pick's remainder over the total weight
     TR_TEXTURE,    // outcome: checker parity; value the coordinates' distance to a cell boundary
     TR_ENV_PICK,   // outcome: environment texel; value the draw's distance to a CDF step over the total
-    TR_THROUGHPUT  // not a decision (outcome 0): the path throughput's largest channel after a scatter
+    TR_THROUGHPUT, // not a decision (outcome 0): the path throughput's largest channel after a scatter
+    TR_ADAPTIVE    // outcome: 1 the pixel stops, 0 it continues; value (error - threshold) / threshold
 };
 inline thread_local std::vector<TraceEvent>* g_trace = nullptr;
 inline void trace_note(int32_t type, int32_t outcome, double value = 0.0) {
@@ -2191,7 +2192,11 @@ template <class R> struct Renderer {
                     mean = mean + cdiv(delta, count);
                     V3<R> delta2 = s - mean;
                     m2 = m2 + cmul(delta, delta2);
-                    if (accepted >= mn && adaptive_error(m2, accepted) < R(cam.desc.adaptive_error_threshold)) break;
+                    if (accepted >= mn) {
+                        const R err = adaptive_error(m2, accepted), thr = R(cam.desc.adaptive_error_threshold);
+                        trace_note(TR_ADAPTIVE, err < thr ? 1 : 0, thr > R(0) ? double((err - thr) / thr) : double(err));
+                        if (err < thr) break;
+                    }
                 }
                 return mean;
             }
