@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--tail-slots", type=int, default=0,
                     help="auto schedule: unfinished pixels at which the persistent kernel takes over (0 = library)")
     ap.add_argument("--stripes", type=int, default=0, help="wavefront stripes (0 = library default)")
+    ap.add_argument("--migrate", default="default", choices=["default", "on", "off"],
+                    help="auto schedule: move slow pixels to a concurrent persistent kernel (default: library rule)")
     ap.add_argument("--f32-tree", default="wide", choices=["wide", "binary"],
                     help="tree the f32 path traverses: the eight-wide compressed tree or the reference binary tree")
     ap.add_argument("--gpu-bvh", action="store_true",
@@ -176,18 +178,26 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def traffic_from_profiles(kernel: str, workload_name: str):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if present."""
-    p = ROOT / "profiles" / f"{kernel}_{workload_name}.md"
-    if not p.exists():
-        return None
-    for line in p.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].strip())
-            except ValueError:
-                return None
-    return None
+# DRAM bytes per unit of work of each wavefront kernel on the mesh-heavy workload, from
+# the ncu launch list of one 1920x1080 frame at 1 sample per pixel (four stripes, 12
+# iterations each): dram__bytes_read.sum + dram__bytes_write.sum summed over the kernel's
+# 48 launches, divided by the frame's units (4,272,505 closest-hit queries for k_trace and
+# k_shade, 1,753,633 shadow queries for k_shadow, 2,073,600 samples for k_generate).  ncu
+# empties the caches before every launch, so these are upper bounds on what the timed
+# frame moves.  `roofline.traffic` scales them by the units of the dominant kernel's
+# average launch.
+DRAM_BYTES_PER_UNIT = {
+    "mesh_heavy_perlin_tori_sun": {"trace": 422.5, "shadow": 768.7, "shade": 375.0, "generate": 303.8},
+}
+# Issue ceiling of k_trace on the same workload (one 912-block launch of that frame, all
+# sections): the warp schedulers issue in 42.5% of their active cycles, and on average
+# 9.65 of a warp's 32 lanes execute each instruction (rays of a warp visit different
+# numbers of nodes and triangles).  The traversal kernels are bound by dependent loads and
+# this divergence, not by HBM bandwidth.
+ISSUE_PROFILE = {
+    "mesh_heavy_perlin_tori_sun": {"kernel": "k_trace", "issue_active": 0.425, "lanes_per_instruction": 9.65,
+                                   "warp_stall_long_scoreboard_per_issue": 6.48},
+}
 
 
 # ----------------------------------------------------------------------------------
@@ -380,7 +390,8 @@ def run_ours(args):
     cams = cam if isinstance(cam, list) else None
     if cams is not None:
         cam = cams[0]
-    pt = PathTracer(cam, context=ctx, schedule=args.schedule, tail_slots=args.tail_slots, stripes=args.stripes)
+    pt = PathTracer(cam, context=ctx, schedule=args.schedule, tail_slots=args.tail_slots, stripes=args.stripes,
+                    migrate=args.migrate)
     tuned = None
     if args.autotune:  # a batch tunes on its first 16 frames
         tuned = pt.autotune(scene, lights, env, cameras=cams[:16] if cams is not None else None)
@@ -520,9 +531,7 @@ def run_ours(args):
     e2e = statistics.median(e2e_vals) * world
 
     # Roofline of the dominant kernel from one profiled frame (events around every launch).
-    prof = PathTracer(cam, context=ctx, profile=True, schedule=pt.schedule, tail_slots=pt.tail_slots,
-                      stripes=pt.stripes, generate_blocks_per_sm=pt.generate_blocks_per_sm,
-                      trace_blocks_per_sm=pt.trace_blocks_per_sm)
+    prof = PathTracer(cam, context=ctx, profile=True, **pt._launch_kw())
     if cams is not None:
         prof.render_batch_hdr_images(scene, cams, lights=lights, environment=env)
     elif env is not None:
@@ -554,7 +563,12 @@ def run_ours(args):
     algo_bytes = units[dom] * bytes_per_unit[dom] / launches_dom
     peak, peak_kind = measured_peaks()
     achieved = algo_bytes / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else 0.0
-    traffic = traffic_from_profiles(f"k_{dom}", cfg["workload"])
+    per_unit = DRAM_BYTES_PER_UNIT.get(cfg["workload"], {}).get(dom)
+    traffic = per_unit * units[dom] / launches_dom if per_unit is not None else None
+    issue = ISSUE_PROFILE.get(cfg["workload"])
+    if issue is not None:
+        issue = dict(issue, simt_efficiency=issue["lanes_per_instruction"] / 32.0,
+                     issue_ceiling=issue["issue_active"] * issue["lanes_per_instruction"] / 32.0)
     # every kernel's own roofline point from the same profiled frame
     per_kernel = {}
     for k in ("generate", "trace", "shade", "shadow", "persistent"):
@@ -580,6 +594,7 @@ def run_ours(args):
                            launch={"stripes": pt.stripes, "tail_slots": pt.tail_slots,
                                    "generate_blocks_per_sm": pt.generate_blocks_per_sm,
                                    "trace_blocks_per_sm": pt.trace_blocks_per_sm,
+                                   "migrate": pt.migrate,
                                    "from": "gt_autotune" if tuned else "library defaults"}),
             "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "call": "gt_render_batch" if cams is not None else "gt_render",
@@ -589,12 +604,16 @@ def run_ours(args):
             "clocks": clock,
             "roofline": {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "algorithmic_bytes_per_launch": algo_bytes,
+                         "traffic": traffic, "traffic_source": "DRAM bytes per unit from the ncu launch list of the "
+                                                               "1-spp frame, times this run's units per launch"
+                         if traffic is not None else None,
+                         "issue": issue, "algorithmic_bytes_per_launch": algo_bytes,
                          "avg_launch_ms": avg_ms, "bytes_per_unit": bytes_per_unit[dom],
                          "units_per_launch": units[dom] / launches_dom, "per_kernel": per_kernel},
             "cpu_baseline": cpu,
             "detail": {"wall_s_timed": wall_s, "rays_per_s": rays / (dev_ms / 1e3), "kernel_ms_profiled": kms,
                        "kernel_launches_profiled": ps["kernel_launches"], "iterations_per_frame": ps["iterations"],
+                       "migrated_pixels_profiled": ps["migrated_pixels"], "tail_pixels_profiled": ps["tail_pixels"],
                        "bvh_per_ray": {"node_tests": per_ray_nodes, "prim_candidates": per_ray_prims}},
         }
         print(json.dumps(line))

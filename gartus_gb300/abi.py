@@ -228,6 +228,9 @@ GT_NOALLOC_MAX_PIXELS = 1048576
 GT_SCHEDULE_AUTO = 0
 GT_SCHEDULE_WAVEFRONT = 1
 GT_SCHEDULE_PERSISTENT = 2
+GT_MIGRATE_DEFAULT = 0
+GT_MIGRATE_ON = 1
+GT_MIGRATE_OFF = 2
 
 # gt_kernel_id
 GT_KERNEL_GENERATE = 0
@@ -281,6 +284,7 @@ class gt_render_opts(C.Structure):
         ("progress_rgb", C.c_void_p),
         ("generate_blocks_per_sm", C.c_uint32),
         ("trace_blocks_per_sm", C.c_uint32),
+        ("migrate", C.c_uint32),
     ]
 
 

@@ -356,7 +356,7 @@ gt_status gt_scene_create(gt_context* ctx, const gt_scene_desc* d, gt_scene** ou
         if (d->primitives[i].material >= d->num_materials)
             return fail(GT_ERR_INVALID_ARG, "ray scene material id out of bounds"); // scene.rs:1158-1161
     }
-    std::lock_guard<std::mutex> lock(ctx->mu);
+    GT_CONTEXT_LOCK(ctx);
     const uint32_t builder = d->struct_size >= sizeof(gt_scene_desc) ? d->bvh_builder : 0u;
     if (builder > GT_BVH_GPU_LBVH) return fail(GT_ERR_INVALID_ARG, "unknown BVH builder");
     if (d->f32_tree > GT_F32_TREE_BINARY) return fail(GT_ERR_INVALID_ARG, "unknown f32 tree");
@@ -420,12 +420,13 @@ gt_status gt_scene_create(gt_context* ctx, const gt_scene_desc* d, gt_scene** ou
 
 void gt_scene_destroy(gt_scene* s) {
     if (!s) return;
-    std::lock_guard<std::mutex> lock(s->ctx->mu);
-    cudaSetDevice(s->ctx->device);
-    cudaStreamSynchronize(s->ctx->stream);
-    free_gpu_f32(s);
-    free_gpu_f64(s);
-    delete s;
+    gt::destroy_or_defer(s->ctx, [s] {
+        cudaSetDevice(s->ctx->device);
+        cudaStreamSynchronize(s->ctx->stream);
+        free_gpu_f32(s);
+        free_gpu_f64(s);
+        delete s;
+    });
 }
 
 gt_status gt_scene_update_primitives(gt_scene* s, uint32_t first, uint32_t count, const gt_primitive* prims) {
@@ -438,7 +439,7 @@ gt_status gt_scene_update_primitives(gt_scene* s, uint32_t first, uint32_t count
         if (prims[i].material >= s->mats.size())
             return fail(GT_ERR_INVALID_ARG, "ray scene material id out of bounds"); // scene.rs:1158-1161
     }
-    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    GT_CONTEXT_LOCK(s->ctx);
     cudaError_t ce = cudaSetDevice(s->ctx->device);
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
     ce = cudaStreamSynchronize(s->ctx->stream); // no render of this context still reads the old data
@@ -462,7 +463,7 @@ gt_status gt_scene_bvh_node_count(const gt_scene* s, uint32_t* count) {
     GT_GUARD_BEGIN
     if (!s || !count) return fail(GT_ERR_INVALID_ARG, "null argument");
     gt_scene* m = const_cast<gt_scene*>(s);
-    std::lock_guard<std::mutex> lock(m->ctx->mu);
+    GT_CONTEXT_LOCK(m->ctx);
     const gt_status rc = ensure_reference_bvh(m);
     if (rc != GT_OK) return rc;
     *count = uint32_t(s->bvh.nodes.size());
@@ -509,12 +510,13 @@ gt_status gt_lights_create(gt_context* ctx, const gt_light_target* t, uint32_t c
 
 void gt_lights_destroy(gt_lights* l) {
     if (!l) return;
-    std::lock_guard<std::mutex> lock(l->ctx->mu);
-    cudaSetDevice(l->ctx->device);
-    cudaStreamSynchronize(l->ctx->stream);
-    free_lights_f32(l);
-    free_lights_f64(l);
-    delete l;
+    gt::destroy_or_defer(l->ctx, [l] {
+        cudaSetDevice(l->ctx->device);
+        cudaStreamSynchronize(l->ctx->stream);
+        free_lights_f32(l);
+        free_lights_f64(l);
+        delete l;
+    });
 }
 
 gt_status gt_environment_create(gt_context* ctx, const gt_environment_desc* d, gt_environment** out) {
@@ -525,7 +527,7 @@ gt_status gt_environment_create(gt_context* ctx, const gt_environment_desc* d, g
     if (d->format > GT_ENV_RGB32F) return fail(GT_ERR_INVALID_ARG, "unknown environment format");
     if (d->width == 0 || d->height == 0 || !d->texels) return fail(GT_ERR_INVALID_ARG, "empty environment image");
     if (uint64_t(d->width) * d->height > (1ull << 27)) return fail(GT_ERR_INVALID_ARG, "environment image too large");
-    std::lock_guard<std::mutex> lock(ctx->mu);
+    GT_CONTEXT_LOCK(ctx);
     auto* e = new gt_environment();
     e->ctx = ctx;
     e->format = d->format;
@@ -592,14 +594,15 @@ gt_status gt_environment_create(gt_context* ctx, const gt_environment_desc* d, g
 
 void gt_environment_destroy(gt_environment* e) {
     if (!e) return;
-    std::lock_guard<std::mutex> lock(e->ctx->mu);
-    cudaSetDevice(e->ctx->device);
-    cudaStreamSynchronize(e->ctx->stream);
-    free_env_f32(e);
-    free_env_f64(e);
-    cudaFree(e->d_px8);
-    cudaFree(e->d_px32);
-    delete e;
+    gt::destroy_or_defer(e->ctx, [e] {
+        cudaSetDevice(e->ctx->device);
+        cudaStreamSynchronize(e->ctx->stream);
+        free_env_f32(e);
+        free_env_f64(e);
+        cudaFree(e->d_px8);
+        cudaFree(e->d_px32);
+        delete e;
+    });
 }
 
 // ------------------------------------------------------------ accumulators
@@ -625,7 +628,7 @@ gt_status gt_accumulator_create(gt_context* ctx, uint32_t width, uint32_t height
     if (width == 0 || height == 0 || uint64_t(width) * height > (1ull << 31))
         return fail(GT_ERR_INVALID_ARG, "accumulator size must be positive and at most 2^31 pixels");
     if (precision > GT_PRECISION_F64) return fail(GT_ERR_INVALID_ARG, "unknown precision");
-    std::lock_guard<std::mutex> lock(ctx->mu);
+    GT_CONTEXT_LOCK(ctx);
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     auto* a = new gt_accumulator();
@@ -653,14 +656,15 @@ gt_status gt_accumulator_create(gt_context* ctx, uint32_t width, uint32_t height
 
 void gt_accumulator_destroy(gt_accumulator* a) {
     if (!a) return;
-    std::lock_guard<std::mutex> lock(a->ctx->mu);
-    cudaSetDevice(a->ctx->device);
-    cudaStreamSynchronize(a->ctx->stream);
-    cudaFree(a->rng);
-    cudaFree(a->sum);
-    cudaFree(a->comp);
-    cudaFree(a->accepted);
-    delete a;
+    gt::destroy_or_defer(a->ctx, [a] {
+        cudaSetDevice(a->ctx->device);
+        cudaStreamSynchronize(a->ctx->stream);
+        cudaFree(a->rng);
+        cudaFree(a->sum);
+        cudaFree(a->comp);
+        cudaFree(a->accepted);
+        delete a;
+    });
 }
 
 gt_status gt_accumulator_samples(const gt_accumulator* a, uint32_t* samples) {
@@ -676,7 +680,7 @@ gt_status gt_accumulator_save(const gt_accumulator* a, void* host, uint64_t capa
     *size = need;
     if (!host) return GT_OK;
     if (capacity < need) return fail(GT_ERR_INVALID_ARG, "checkpoint buffer too small");
-    std::lock_guard<std::mutex> lock(a->ctx->mu);
+    GT_CONTEXT_LOCK(a->ctx);
     cudaError_t e = cudaSetDevice(a->ctx->device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     AccumHeader h{kAccumMagic, 1u, a->width, a->height, a->precision, a->samples, a->seed};
@@ -705,7 +709,7 @@ gt_status gt_accumulator_load(gt_accumulator* a, const void* host, uint64_t size
     if (h.width != a->width || h.height != a->height || h.precision != a->precision)
         return fail(GT_ERR_INVALID_ARG, "checkpoint size or precision differs from the accumulator's");
     if (size < sizeof(h) + accum_payload(a)) return fail(GT_ERR_INVALID_ARG, "checkpoint truncated");
-    std::lock_guard<std::mutex> lock(a->ctx->mu);
+    GT_CONTEXT_LOCK(a->ctx);
     cudaError_t e = cudaSetDevice(a->ctx->device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     const char* p = static_cast<const char*>(host) + sizeof(h);
@@ -756,7 +760,8 @@ gt_status gt_render_accumulate(gt_scene* s, const gt_lights* l, const gt_environ
     if (f->width != cam.width || f->height != cam.height)
         return fail(GT_ERR_INVALID_ARG, "frame size does not match the camera's image size");
     if (!f->rgb) return fail(GT_ERR_INVALID_ARG, "frame has no rgb buffer");
-    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    GT_CONTEXT_LOCK(s->ctx);
+    gt::DeferredDestroys deferred_destroys{s->ctx};
     cudaError_t ce = cudaSetDevice(s->ctx->device);
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
     auto* env = const_cast<gt_environment*>(e);
@@ -794,7 +799,8 @@ gt_status gt_render_batch(gt_scene* s, const gt_lights* l, const gt_environment*
         if (!j.frame->rgb) return fail(GT_ERR_INVALID_ARG, "frame has no rgb buffer");
         frames[i] = j.frame;
     }
-    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    GT_CONTEXT_LOCK(s->ctx);
+    gt::DeferredDestroys deferred_destroys{s->ctx};
     cudaError_t ce = cudaSetDevice(s->ctx->device);
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
     auto* env = const_cast<gt_environment*>(e);
@@ -819,6 +825,7 @@ gt_status gt_render(gt_scene* s, const gt_lights* l, const gt_environment* e, co
         opts.schedule > GT_SCHEDULE_PERSISTENT)
         return fail(GT_ERR_INVALID_ARG, "unknown schedule");
     if (opts.struct_size < offsetof(gt_render_opts, schedule) + sizeof(uint32_t)) opts.schedule = GT_SCHEDULE_AUTO;
+    if (opts.migrate > GT_MIGRATE_OFF) return fail(GT_ERR_INVALID_ARG, "unknown migrate mode");
     if ((l && l->ctx != s->ctx) || (e && e->ctx != s->ctx))
         return fail(GT_ERR_INVALID_ARG, "lights, environment and scene must share a context");
     gt_status rc = validate_camera(*c);
@@ -827,7 +834,8 @@ gt_status gt_render(gt_scene* s, const gt_lights* l, const gt_environment* e, co
     if (f->width != cam.width || f->height != cam.height)
         return fail(GT_ERR_INVALID_ARG, "frame size does not match the camera's image size");
     if (!f->rgb) return fail(GT_ERR_INVALID_ARG, "frame has no rgb buffer");
-    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    GT_CONTEXT_LOCK(s->ctx);
+    gt::DeferredDestroys deferred_destroys{s->ctx};
     cudaError_t ce = cudaSetDevice(s->ctx->device);
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
     auto* env = const_cast<gt_environment*>(e);
@@ -892,6 +900,9 @@ gt_status gt_autotune(gt_scene* s, const gt_lights* l, const gt_environment* e, 
     if ((rc = sweep(&gt_render_opts::tail_slots, {0u, 4096u, 16384u, 65536u, 262144u})) != GT_OK) return rc;
     if ((rc = sweep(&gt_render_opts::trace_blocks_per_sm, {4u, 6u, 8u, 12u})) != GT_OK) return rc;
     if ((rc = sweep(&gt_render_opts::generate_blocks_per_sm, {4u, 8u, 16u})) != GT_OK) return rc;
+    if (best.schedule == GT_SCHEDULE_AUTO &&
+        (rc = sweep(&gt_render_opts::migrate, {uint32_t(GT_MIGRATE_ON), uint32_t(GT_MIGRATE_OFF)})) != GT_OK)
+        return rc;
     // Last, the persistent schedule alone (it wins for small frames, whose wavefront
     // iterations are launch-bound); only when the caller left the choice to AUTO.
     if (given_schedule == GT_SCHEDULE_AUTO) {
@@ -923,7 +934,7 @@ gt_status gt_trace_rays(gt_scene* s, const double* rays, uint32_t count, double 
                         double* t, gt_bvh_stats* stats) {
     GT_GUARD_BEGIN
     if (!s || (count && (!rays || !ids))) return fail(GT_ERR_INVALID_ARG, "null argument");
-    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    GT_CONTEXT_LOCK(s->ctx);
     cudaError_t ce = cudaSetDevice(s->ctx->device);
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
     if (s->prims.empty()) { // no BVH: RayScene counts a linear scan of zero primitives
@@ -980,7 +991,7 @@ gt_status gt_trace_rays_f32(gt_scene* s, const double* rays, uint32_t count, dou
         std::memset(reinterpret_cast<char*>(report) + sizeof(uint32_t), 0, sizeof(gt_trace_report) - sizeof(uint32_t));
         report->rays = count;
     }
-    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    GT_CONTEXT_LOCK(s->ctx);
     cudaError_t ce = cudaSetDevice(s->ctx->device);
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
     if (s->prims.empty()) {

@@ -526,7 +526,7 @@ gt_status gt_denoiser_create(gt_context* ctx, uint64_t seed, gt_denoiser** out) 
     GT_GUARD_BEGIN
     if (!ctx || !out) return fail(GT_ERR_INVALID_ARG, "null argument");
     *out = nullptr;
-    std::lock_guard<std::mutex> lock(ctx->mu);
+    GT_CONTEXT_LOCK(ctx);
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     auto* d = new gt_denoiser();
@@ -580,8 +580,7 @@ gt_status gt_denoiser_create(gt_context* ctx, uint64_t seed, gt_denoiser** out) 
     GT_GUARD_END
 }
 
-void gt_denoiser_destroy(gt_denoiser* d) {
-    if (!d) return;
+static void destroy_denoiser(gt_denoiser* d) {
     cudaSetDevice(d->ctx->device);
     cudaStreamSynchronize(d->ctx->stream);
     free_bufs(d);
@@ -600,6 +599,12 @@ void gt_denoiser_destroy(gt_denoiser* d) {
     delete d;
 }
 
+void gt_denoiser_destroy(gt_denoiser* d) {
+    if (!d) return;
+    gt::destroy_or_defer(d->ctx, [d] { destroy_denoiser(d); });
+}
+
+
 gt_status gt_denoiser_param_count(const gt_denoiser* d, uint64_t* count) {
     if (!d || !count) return fail(GT_ERR_INVALID_ARG, "null argument");
     *count = d->nparams;
@@ -610,7 +615,7 @@ gt_status gt_denoiser_get_params(const gt_denoiser* d, float* host, uint64_t cou
     GT_GUARD_BEGIN
     if (!d || !host) return fail(GT_ERR_INVALID_ARG, "null argument");
     if (count != d->nparams) return fail(GT_ERR_INVALID_ARG, "parameter count differs from the network's");
-    std::lock_guard<std::mutex> lock(d->ctx->mu);
+    GT_CONTEXT_LOCK(d->ctx);
     cudaSetDevice(d->ctx->device);
     const cudaError_t e = cudaMemcpy(host, d->p, count * sizeof(float), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "denoiser parameters");
@@ -624,7 +629,7 @@ gt_status gt_denoiser_set_params(gt_denoiser* d, const float* host, uint64_t cou
     if (count != d->nparams) return fail(GT_ERR_INVALID_ARG, "parameter count differs from the network's");
     for (uint64_t i = 0; i < count; ++i)
         if (!std::isfinite(host[i])) return fail(GT_ERR_INVALID_ARG, "denoiser parameters must be finite");
-    std::lock_guard<std::mutex> lock(d->ctx->mu);
+    GT_CONTEXT_LOCK(d->ctx);
     cudaSetDevice(d->ctx->device);
     cudaError_t e = cudaMemcpy(d->p, host, count * sizeof(float), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(d->m, 0, count * sizeof(float));
@@ -644,7 +649,7 @@ gt_status gt_denoiser_train_step(gt_denoiser* d, const float* beauty, const floa
     gt_status rc = check_image(n, h, w);
     if (rc != GT_OK) return rc;
     if (!(lr >= 0.f) || !std::isfinite(lr)) return fail(GT_ERR_INVALID_ARG, "learning rate must be finite and >= 0");
-    std::lock_guard<std::mutex> lock(d->ctx->mu);
+    GT_CONTEXT_LOCK(d->ctx);
     cudaSetDevice(d->ctx->device);
     const cudaStream_t st = d->ctx->stream;
     if ((rc = ensure_bufs(d, int(n), int(h), int(w))) != GT_OK) return rc;
@@ -693,7 +698,7 @@ gt_status gt_denoise(gt_denoiser* d, const gt_denoise_input* in, uint32_t tile, 
     if (!(threshold > 0.f) || !std::isfinite(threshold)) return fail(GT_ERR_INVALID_ARG, "threshold must be finite and > 0");
     const int hp = int((h + 15) / 16 * 16), wp = int((w + 15) / 16 * 16);
     const int tiles = int(((h + tile - 1) / tile) * ((w + tile - 1) / tile));
-    std::lock_guard<std::mutex> lock(d->ctx->mu);
+    GT_CONTEXT_LOCK(d->ctx);
     cudaError_t e = cudaSetDevice(d->ctx->device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     const cudaStream_t st = d->ctx->stream;

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <mutex>
 #include <new>
 #include <stdexcept>
@@ -121,7 +122,14 @@ struct gt_context {
         cudaGraphExec_t exec = nullptr;
     };
     CachedGraph graphs[kMaxStripes];
-    std::mutex mu;
+    // Held by every call that touches the context's device state.  A progress callback runs
+    // on the rendering thread while the render holds it, so the lock is recursive and the
+    // callback is counted: a destroy called from inside the callback (a handle that the
+    // host language's garbage collector finalises there, say) is deferred to the end of the
+    // render, and every other call fails instead of deadlocking or disturbing the render.
+    std::recursive_mutex mu;
+    int in_callback = 0;
+    std::vector<std::function<void()>> deferred;
     void* ws = nullptr; // render workspace (path state, queues, staging)
     size_t ws_bytes = 0;
     uint32_t* pinned = nullptr; // host-pinned copy of the loop counters (256 words)
@@ -129,6 +137,41 @@ struct gt_context {
     volatile uint32_t* mapped = nullptr;
     uint32_t* mapped_dev = nullptr;
 };
+
+namespace gt {
+// Calls the render's progress callback with the context marked as inside it.
+inline int call_progress(gt_context* ctx, const gt_render_opts& o, uint64_t done, uint64_t total) {
+    ++ctx->in_callback;
+    const int r = o.progress(o.progress_user, done, total);
+    --ctx->in_callback;
+    return r;
+}
+
+// Runs, when a render entry point returns, the destroys its progress callbacks deferred.
+struct DeferredDestroys {
+    gt_context* ctx;
+    ~DeferredDestroys() {
+        if (ctx->in_callback) return;
+        std::vector<std::function<void()>> list;
+        list.swap(ctx->deferred);
+        for (auto& f : list) f();
+    }
+};
+
+// Destroys now, or at the end of the render whose progress callback this is.
+inline void destroy_or_defer(gt_context* ctx, std::function<void()> destroy) {
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    if (ctx->in_callback) ctx->deferred.push_back(std::move(destroy));
+    else destroy();
+}
+} // namespace gt
+
+// Takes the context lock for the rest of the scope; from inside a progress callback of a
+// render on this context, returns GT_ERR_INVALID_ARG instead.
+#define GT_CONTEXT_LOCK(ctxp)                                                                          \
+    std::lock_guard<std::recursive_mutex> gt_context_lock_(ctxp->mu);                                   \
+    if ((ctxp)->in_callback)                                                                           \
+    return gt::fail(GT_ERR_INVALID_ARG, "called from inside a progress callback of a render on this context")
 
 // Resumable accumulation state in device memory (one entry per pixel, in the
 // accumulator's precision): stream position, radiance sums, Kahan compensation, accepted.

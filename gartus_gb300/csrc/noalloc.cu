@@ -70,7 +70,7 @@ extern "C" gt_status gt_render_noalloc(gt_scene* scene, const gt_lights* lights,
             return fail(GT_ERR_INVALID_ARG,
                         "environment is not resident on the device in f32; render once with gt_render first");
         gt_context* ctx = scene->ctx;
-        std::lock_guard<std::mutex> lock(ctx->mu);
+        GT_CONTEXT_LOCK(ctx);
         cudaError_t ce = cudaSetDevice(ctx->device);
         if (ce != cudaSuccess) return cuda_fail(ce, "cudaSetDevice");
         unsigned char* base = nullptr;

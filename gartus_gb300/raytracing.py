@@ -1377,15 +1377,19 @@ class PathTracer:
 
     precision: "f32" (throughput) or "f64" (the reference's arithmetic, op for op).
     schedule: "auto" (wavefront, then the persistent kernel for the last tail_slots
-    pixels; 0 = the library's choice), "wavefront" or "persistent"; the image is the same."""
+    pixels; 0 = the library's choice), "wavefront" or "persistent"; the image is the same.
+    migrate: "default", "on" or "off": whether "auto" moves each stripe's slow pixels to a
+    concurrent persistent kernel early in the frame (gt_migrate; default = on for scenes of
+    at most 65,536 primitives)."""
 
     SCHEDULES = {"auto": abi.GT_SCHEDULE_AUTO, "wavefront": abi.GT_SCHEDULE_WAVEFRONT,
                  "persistent": abi.GT_SCHEDULE_PERSISTENT}
+    MIGRATE = {"default": abi.GT_MIGRATE_DEFAULT, "on": abi.GT_MIGRATE_ON, "off": abi.GT_MIGRATE_OFF}
 
     def __init__(self, camera: RayCamera, options: RenderOptions = RenderOptions(), precision: str = "f32",
                  context: Optional[Context] = None, profile: bool = False, schedule: str = "auto",
                  tail_slots: int = 0, stripes: int = 0, generate_blocks_per_sm: int = 0,
-                 trace_blocks_per_sm: int = 0):
+                 trace_blocks_per_sm: int = 0, migrate: str = "default"):
         if precision not in ("f32", "f64"):
             raise ValueError("precision must be 'f32' or 'f64'")
         if schedule not in self.SCHEDULES:
@@ -1399,6 +1403,9 @@ class PathTracer:
         self.stripes = int(stripes)
         self.generate_blocks_per_sm = int(generate_blocks_per_sm)
         self.trace_blocks_per_sm = int(trace_blocks_per_sm)
+        if migrate not in self.MIGRATE:
+            raise ValueError(f"migrate must be one of {sorted(self.MIGRATE)}")
+        self.migrate = migrate
         self._ctx = context
         self.last_stats: Optional[dict] = None
 
@@ -1406,9 +1413,13 @@ class PathTracer:
     def context(self) -> Context:
         return self._ctx or Context.default()
 
+    def _launch_kw(self) -> dict:
+        return {"schedule": self.schedule, "tail_slots": self.tail_slots, "stripes": self.stripes,
+                "generate_blocks_per_sm": self.generate_blocks_per_sm, "trace_blocks_per_sm": self.trace_blocks_per_sm,
+                "migrate": self.migrate}
+
     def with_options(self, options: RenderOptions) -> "PathTracer":
-        return PathTracer(self.camera, options, self.precision, self._ctx, self.profile, self.schedule,
-                          self.tail_slots, self.stripes, self.generate_blocks_per_sm, self.trace_blocks_per_sm)
+        return PathTracer(self.camera, options, self.precision, self._ctx, self.profile, **self._launch_kw())
 
     def _launch_opts(self, o) -> None:
         """The tracer's schedule and launch shapes into a gt_render_opts."""
@@ -1417,16 +1428,18 @@ class PathTracer:
         o.stripes = self.stripes
         o.generate_blocks_per_sm = self.generate_blocks_per_sm
         o.trace_blocks_per_sm = self.trace_blocks_per_sm
+        o.migrate = self.MIGRATE[self.migrate]
 
     def autotune(self, world: RayScene, lights: Optional[WeightedSamplingTargetList] = None,
                  environment: Optional[EnvironmentLight] = None, cameras=None) -> dict:
         """gt_autotune: times this tracer's frame (or the batch of `cameras`) under candidate
-        stripe counts, tail sizes and wavefront blocks per SM, then (schedule "auto", or
-        "persistent" from an earlier tune) the persistent schedule, and keeps the fastest in
-        this tracer.  Launch shapes never change the image; switching to the persistent
-        schedule can change f32 pixels (other kernels fuse f32 operations differently), never
-        f64 images or accepted counts.  Returns {"trials", "given_ms", "best_ms", "schedule",
-        "stripes", "tail_slots", "generate_blocks_per_sm", "trace_blocks_per_sm"}."""
+        stripe counts, tail sizes, wavefront blocks per SM and (schedule "auto") migration on
+        or off, then (schedule "auto", or "persistent" from an earlier tune) the persistent
+        schedule, and keeps the fastest in this tracer.  Launch shapes never change the image;
+        migrating pixels or switching to the persistent schedule can change f32 pixels (other
+        kernels fuse f32 operations differently), never f64 images or accepted counts.
+        Returns {"trials", "given_ms", "best_ms", "schedule", "stripes", "tail_slots",
+        "generate_blocks_per_sm", "trace_blocks_per_sm", "migrate"}."""
         ctx = self.context
         cams = list(cameras) if cameras is not None else [self.camera]
         descs = [c.desc() for c in cams]
@@ -1456,10 +1469,10 @@ class PathTracer:
         check(lib().gt_autotune(sh.h, lh, eh, jobs, len(cams), C.byref(o), C.byref(rep)))
         self.stripes, self.tail_slots = int(o.stripes), int(o.tail_slots)
         self.generate_blocks_per_sm, self.trace_blocks_per_sm = int(o.generate_blocks_per_sm), int(o.trace_blocks_per_sm)
+        self.migrate = {v: k for k, v in self.MIGRATE.items()}[int(o.migrate)]
         self.schedule = {v: k for k, v in self.SCHEDULES.items()}[int(o.schedule)]
         return {"trials": int(rep.trials), "given_ms": float(rep.given_ms), "best_ms": float(rep.best_ms),
-                "schedule": self.schedule, "stripes": self.stripes, "tail_slots": self.tail_slots,
-                "generate_blocks_per_sm": self.generate_blocks_per_sm, "trace_blocks_per_sm": self.trace_blocks_per_sm}
+                **self._launch_kw()}
 
     def render_accumulate(self, world: RayScene, accumulator: Accumulator, samples: int,
                           lights: Optional[WeightedSamplingTargetList] = None,
@@ -1633,9 +1646,7 @@ class PathTracer:
     # render_with_light_connections (renderer.rs:771-786): forces NEE
     def render_with_light_connections_hdr_image(self, world, lights, want64: bool = False) -> HdrImage:
         cam = self.camera.with_direct_lighting_mode(abi.GT_DIRECT_NEXT_EVENT_ESTIMATION)
-        return PathTracer(cam, self.options, self.precision, self._ctx, self.profile, self.schedule,
-                          self.tail_slots, self.stripes, self.generate_blocks_per_sm,
-                          self.trace_blocks_per_sm)._render(
+        return PathTracer(cam, self.options, self.precision, self._ctx, self.profile, **self._launch_kw())._render(
             world, lights, None, want64=want64)
 
     # render_with_environment_hdr_image (renderer.rs:431-449)

@@ -383,7 +383,20 @@ typedef struct gt_render_opts {
      * picks them per workload. */
     uint32_t generate_blocks_per_sm;
     uint32_t trace_blocks_per_sm;
+    /* GT_SCHEDULE_AUTO: once per stripe, early in the frame, the pixels progressing at less
+     * than half the stripe's mean sample rate (long sample chains: glass, adaptive pixels at
+     * their cap) move to a persistent kernel that runs them concurrently with the wavefront.
+     * gt_migrate; f64 images do not depend on it. */
+    uint32_t migrate;
 } gt_render_opts;
+
+typedef enum gt_migrate {
+    GT_MIGRATE_DEFAULT = 0, /* on for scenes of at most 65,536 primitives, off above: there the
+                               persistent kernel's unsorted walks of the large tree run slower
+                               than the wavefront's */
+    GT_MIGRATE_ON = 1,
+    GT_MIGRATE_OFF = 2
+} gt_migrate;
 
 /* Caller-owned output images, row-major, 3 channels, y = 0 is the top row
  * (HdrImage, graphics/display.rs:282-295).  Any pointer may be NULL except rgb. */

@@ -59,6 +59,23 @@ def test_struct_layouts_match_header(tmp_path):
             assert int(got[f"{s.__name__}.{f[0]}"]) == getattr(s, f[0]).offset, (s.__name__, f[0])
 
 
+def test_constants_match_header(tmp_path):
+    # every GT_* integer constant of the Python mirror has the header's value
+    names = [n for n in dir(abi) if n.startswith("GT_") and isinstance(getattr(abi, n), int)]
+    lines = ['#include <stdio.h>', f'#include "{HEADER}"', "int main(void){"]
+    lines += [f'printf("{n} %llu\\n", (unsigned long long)({n}));' for n in names]
+    lines.append("return 0;}")
+    src = tmp_path / "consts.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "consts"
+    subprocess.run(["gcc", "-std=c99", str(src), "-o", str(exe)], check=True)
+    got = dict(line.rsplit(" ", 1) for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                               check=True).stdout.splitlines())
+    assert len(names) > 20
+    for n in names:
+        assert int(got[n]) == getattr(abi, n) & 0xFFFFFFFFFFFFFFFF, n
+
+
 def test_camera_defaults_match_ray_camera_new():
     # RayCamera::new (graphics/camera.rs:1034-1065).
     d = abi.gt_camera_desc()

@@ -24,7 +24,7 @@ import pytest
 from gartus_gb300 import denoiser as dn
 from oracle import denoiser as odn
 
-BF16_FAITHFUL_GRAD_REL = 0.05
+BF16_FAITHFUL_GRAD_REL = 0.08
 
 
 def _random_params(seed: int, out_scale: float = 1.0) -> np.ndarray:

@@ -365,9 +365,9 @@ def test_autotune_keeps_the_image(gpu_context):
     assert rep["schedule"] in ("auto", "persistent") and pt.schedule == rep["schedule"]
     tuned = pt.render_with_lights_hdr_image(scene, lights)
     np.testing.assert_array_equal(tuned.accepted, base.accepted)
-    if rep["schedule"] == "auto":
+    if rep["schedule"] == "auto" and rep["migrate"] == "default":
         np.testing.assert_array_equal(tuned.pixels, base.pixels)
-    else:  # other kernels finish the pixels, fusing f32 operations differently
+    else:  # other kernels finish (some) pixels, fusing f32 operations differently
         assert_modes_agree("autotuned vs default", scene, cam, tuned.pixels, base.pixels, lights)
     # a batch tunes the same way
     cams = scenes.batch_cameras(frames=3, width=32, spp_cycle=(4,), max_samples=8)
@@ -535,6 +535,34 @@ def test_render_progressive(gpu_context, schedule):
     with pytest.raises(Stop):
         pt.render_progressive(scene, stop, lights=lights)
     assert np.isfinite(pt.render_with_lights_hdr_image(scene, lights).pixels).all()
+
+
+@pytest.mark.parametrize("schedule", ["wavefront", "persistent"])
+def test_calls_from_inside_a_progress_callback(gpu_context, schedule):
+    # The progress callback runs on the rendering thread while the render holds the
+    # context.  A handle released there (the last reference dropped, as when the garbage
+    # collector finalises it) is destroyed once the render returns; any other call on the
+    # context fails with GT_ERR_INVALID_ARG instead of deadlocking.
+    scene, lights = scenes.cornell_scene()
+    doomed = [scenes.cornell_scene()[0]]
+    doomed[0]._handle(gpu_context)  # resident on the device
+    pt = PathTracer(scenes.cornell_camera(256, 4, 50), context=gpu_context, schedule=schedule)
+    errors = []
+
+    def progress(update):
+        if doomed:
+            doomed.pop()  # gt_scene_destroy from inside the callback
+            try:
+                PathTracer(scenes.cornell_camera(16, 1, 5), context=gpu_context).render_with_lights_hdr_image(
+                    scene, lights)
+            except GartusError as e:
+                errors.append(str(e))
+
+    img = pt.render_progressive(scene, progress, lights=lights)
+    assert not doomed and np.isfinite(img.pixels).all()
+    assert len(errors) == 1 and "progress callback" in errors[0], errors
+    again = pt.render_with_lights_hdr_image(scene, lights)
+    np.testing.assert_array_equal(again.pixels, img.pixels)
 
 
 def test_persistent_progress_and_cancel(gpu_context):
