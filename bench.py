@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--tail-slots", type=int, default=0,
                     help="auto schedule: unfinished pixels at which the persistent kernel takes over (0 = library)")
     ap.add_argument("--stripes", type=int, default=0, help="wavefront stripes (0 = library default)")
+    ap.add_argument("--rng", default="pixel", choices=["pixel", "substreams"],
+                    help="per-sample random streams: the reference's (one per pixel) or the throughput mode's "
+                         "(one per pixel and sample)")
     ap.add_argument("--migrate", default="default", choices=["default", "on", "off"],
                     help="auto schedule: move slow pixels to a concurrent persistent kernel (default: library rule)")
     ap.add_argument("--f32-tree", default="wide", choices=["wide", "binary"],
@@ -391,7 +394,7 @@ def run_ours(args):
     if cams is not None:
         cam = cams[0]
     pt = PathTracer(cam, context=ctx, schedule=args.schedule, tail_slots=args.tail_slots, stripes=args.stripes,
-                    migrate=args.migrate)
+                    migrate=args.migrate, rng=args.rng)
     tuned = None
     if args.autotune:  # a batch tunes on its first 16 frames
         tuned = pt.autotune(scene, lights, env, cameras=cams[:16] if cams is not None else None)
@@ -589,7 +592,8 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": dict(cfg, l2="flushed between timed steps (512 MiB write)", schedule=pt.schedule,
+            "rng": pt.rng,
+            "config": dict(cfg, l2="flushed between timed steps (512 MiB write)", schedule=pt.schedule, rng=pt.rng,
                            parallelism=f"replicas x{world}" if world > 1 else "single GPU",
                            launch={"stripes": pt.stripes, "tail_slots": pt.tail_slots,
                                    "generate_blocks_per_sm": pt.generate_blocks_per_sm,

@@ -231,6 +231,8 @@ GT_SCHEDULE_PERSISTENT = 2
 GT_MIGRATE_DEFAULT = 0
 GT_MIGRATE_ON = 1
 GT_MIGRATE_OFF = 2
+GT_RNG_PIXEL = 0
+GT_RNG_SUBSTREAMS = 1
 
 # gt_kernel_id
 GT_KERNEL_GENERATE = 0
@@ -285,6 +287,7 @@ class gt_render_opts(C.Structure):
         ("generate_blocks_per_sm", C.c_uint32),
         ("trace_blocks_per_sm", C.c_uint32),
         ("migrate", C.c_uint32),
+        ("rng", C.c_uint32),
     ]
 
 

@@ -741,6 +741,7 @@ gt_status gt_render_accumulate(gt_scene* s, const gt_lights* l, const gt_environ
     }
     if (opts.schedule == GT_SCHEDULE_PERSISTENT || opts.schedule > GT_SCHEDULE_PERSISTENT)
         return fail(GT_ERR_INVALID_ARG, "accumulation runs the auto or wavefront schedule");
+    if (opts.rng != GT_RNG_PIXEL) return fail(GT_ERR_UNSUPPORTED, "accumulation continues the pixels' own streams");
     opts.precision = acc->precision;
     if ((l && l->ctx != s->ctx) || (e && e->ctx != s->ctx))
         return fail(GT_ERR_INVALID_ARG, "lights, environment and scene must share a context");
@@ -783,6 +784,9 @@ gt_status gt_render_batch(gt_scene* s, const gt_lights* l, const gt_environment*
     }
     if (opts.precision > GT_PRECISION_F64) return fail(GT_ERR_INVALID_ARG, "unknown precision");
     if (opts.aovs) return fail(GT_ERR_UNSUPPORTED, "denoising AOVs are not rendered in batches");
+    if (opts.rng > GT_RNG_SUBSTREAMS) return fail(GT_ERR_INVALID_ARG, "unknown rng mode");
+    if (opts.rng == GT_RNG_SUBSTREAMS && opts.precision == GT_PRECISION_F64)
+        return fail(GT_ERR_UNSUPPORTED, "substream batches render in f32");
     if ((l && l->ctx != s->ctx) || (e && e->ctx != s->ctx))
         return fail(GT_ERR_INVALID_ARG, "lights, environment and scene must share a context");
     std::vector<CamHost> cams(count);
@@ -826,6 +830,7 @@ gt_status gt_render(gt_scene* s, const gt_lights* l, const gt_environment* e, co
         return fail(GT_ERR_INVALID_ARG, "unknown schedule");
     if (opts.struct_size < offsetof(gt_render_opts, schedule) + sizeof(uint32_t)) opts.schedule = GT_SCHEDULE_AUTO;
     if (opts.migrate > GT_MIGRATE_OFF) return fail(GT_ERR_INVALID_ARG, "unknown migrate mode");
+    if (opts.rng > GT_RNG_SUBSTREAMS) return fail(GT_ERR_INVALID_ARG, "unknown rng mode");
     if ((l && l->ctx != s->ctx) || (e && e->ctx != s->ctx))
         return fail(GT_ERR_INVALID_ARG, "lights, environment and scene must share a context");
     gt_status rc = validate_camera(*c);

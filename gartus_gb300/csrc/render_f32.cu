@@ -19,7 +19,9 @@ gt_status render_batch_f32(gt_scene* s, const gt_lights* l, gt_environment* e, c
                            const gt_render_opts& opts, gt_frame* const* frames) {
     bool same_width = true;
     for (uint32_t i = 1; i < count; ++i) same_width = same_width && cams[i].width == cams[0].width;
-    if (opts.schedule != GT_SCHEDULE_PERSISTENT && same_width && s->media.empty() && s->objects.empty())
+    // substreams: the frames' pixels are work items of one list, whatever their widths
+    if (opts.rng == GT_RNG_SUBSTREAMS ||
+        (opts.schedule != GT_SCHEDULE_PERSISTENT && same_width && s->media.empty() && s->objects.empty()))
         return render_impl<float, true>(s, l, e, cams[0], opts, nullptr, nullptr, 0, cams, count, frames);
     return render_batch_impl<float>(s, l, e, cams, count, opts, frames);
 }

@@ -939,6 +939,69 @@ gt_status finish_render(gt_context* ctx, const Params<R>& P, gt_frame* frame, co
     return GT_OK;
 }
 
+// Throughput mode: rounds of samples for every pixel still sampling, as many samples per
+// round as keep the round near kSubItems items (so rounds grow as adaptive pixels stop).
+// Each round traces its (pixel, sample) items in one k_substream launch and folds them into
+// the pixels' sums in sample order (k_sub_fold), which also lists the pixels that go on.
+constexpr uint64_t kSubItems = uint64_t(1) << 24; // work items per round, at most (or one per pixel)
+
+inline uint32_t sub_round_size(uint32_t count, uint32_t remaining) {
+    return std::max<uint32_t>(1u, std::min<uint64_t>(remaining, kSubItems / std::max<uint32_t>(count, 1u)));
+}
+
+template <class R, bool BATCH>
+gt_status run_substreams(gt_context* ctx, Params<R>& P, uint32_t* const list[2], R4<R>* out, unsigned long long* next,
+                         uint32_t n, uint32_t limit_max, const gt_render_opts& opts, EventPool& ev, double* kms,
+                         uint64_t* klaunch, uint64_t& rounds) {
+    cudaStream_t st = ctx->stream;
+    const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1);
+    int per_sm = 0;
+    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_substream<R, BATCH>, 128, 0));
+    const uint32_t blocks = sms * uint32_t(std::max(per_sm, 1));
+    const uint32_t fblocks = std::max<uint32_t>(1u, std::min<uint32_t>((n + 255) / 256, sms * 8));
+    const bool profile = opts.profile != 0;
+    k_list_all<<<fblocks, 256, 0, st>>>(list[0], n, P.ps.counters + C_TRACE0);
+    GT_CUDA(cudaGetLastError());
+    klaunch[GT_KERNEL_OTHER] += 1;
+    uint32_t count = n, cur = 0;
+    for (uint32_t first = 0, round = 0; count > 0 && first < limit_max; first += round, cur ^= 1u) {
+        round = sub_round_size(count, limit_max - first);
+        cudaEvent_t a = nullptr, z = nullptr;
+        GT_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned long long), st));
+        GT_CUDA(cudaMemsetAsync(P.ps.counters + C_TRACE0 + (cur ^ 1u), 0, sizeof(uint32_t), st));
+        if (profile) {
+            GT_CUDA(ev.pair(a, z));
+            GT_CUDA(cudaEventRecord(a, st));
+        }
+        k_substream<R, BATCH><<<blocks, 128, 0, st>>>(P, list[cur], count, first, round, out, next);
+        GT_CUDA(cudaGetLastError());
+        klaunch[GT_KERNEL_PERSISTENT] += 1;
+        if (profile) {
+            GT_CUDA(cudaEventRecord(z, st));
+            ev.note(GT_KERNEL_PERSISTENT, a, z);
+            GT_CUDA(ev.pair(a, z));
+            GT_CUDA(cudaEventRecord(a, st));
+        }
+        k_sub_fold<R, BATCH><<<fblocks, 256, 0, st>>>(P, list[cur], count, first, round, out, list[cur ^ 1u],
+                                                      P.ps.counters + C_TRACE0 + (cur ^ 1u));
+        GT_CUDA(cudaGetLastError());
+        klaunch[GT_KERNEL_OTHER] += 1;
+        if (profile) {
+            GT_CUDA(cudaEventRecord(z, st));
+            ev.note(GT_KERNEL_OTHER, a, z);
+        }
+        GT_CUDA(cudaMemcpyAsync(ctx->pinned, P.ps.counters + C_TRACE0 + (cur ^ 1u), sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, st));
+        GT_CUDA(cudaStreamSynchronize(st));
+        count = ctx->pinned[0];
+        ++rounds;
+        const uint64_t done = std::min<uint64_t>(uint64_t(first) + round, limit_max);
+        if (opts.progress && call_progress(ctx, opts, done * n, uint64_t(limit_max) * n))
+            return fail(GT_ERR_CANCELLED, "render cancelled by the progress callback");
+    }
+    return GT_OK;
+}
+
 // One frame (BATCH = false) or, with BATCH = true, the frames bcams[0 .. bcount) of equal
 // width as one image of their rows stacked in order: every wavefront kernel then looks up
 // each slot's frame camera, and each frame's slice of the result goes to bframes[i].
@@ -1002,18 +1065,26 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     // wavefront state, which that variant does not keep).
     const bool world = P.sc.num_media != 0 || P.sc.num_objects != 0;
     if (world && BATCH) return fail(GT_ERR_UNSUPPORTED, "a scene with objects or media does not render as a wavefront batch");
-    const bool persistent = (!BATCH && opts.schedule == GT_SCHEDULE_PERSISTENT && !accum) || (world && !accum);
+    // Throughput mode: every (pixel, sample) pair of a round is a work item.
+    const bool subs = opts.rng == GT_RNG_SUBSTREAMS;
+    if (subs && (world || accum))
+        return fail(GT_ERR_UNSUPPORTED, "substreams render neither worlds with objects or media nor accumulations");
+    const uint64_t sub_items = std::max<uint64_t>(kSubItems, n_pix); // one round's sample radiance
+    const bool persistent = !subs && ((!BATCH && opts.schedule == GT_SCHEDULE_PERSISTENT && !accum) || (world && !accum));
     const bool host_out = BATCH || frame->device_buffers == 0;
     // Wavefront stripes: rows are dealt round-robin to K independent wavefronts on their
     // own streams, whose kernels then overlap on the GPU (each kernel alone leaves SMs
     // waiting on memory).
     uint32_t K = opts.stripes ? opts.stripes : 4u;
     K = std::max<uint32_t>(1u, std::min<uint32_t>({K, uint32_t(gt_context::kMaxStripes), img_h}));
-    if (persistent || world) K = 1;
+    if (persistent || world || subs) K = 1;
     const uint32_t qcap = ((img_h + K - 1) / K) * cam.width;
     std::vector<Params<R>> SP(K);
     CamDev<R>* d_cams = nullptr;
     uint32_t* d_start = nullptr;
+    uint32_t* sub_list[2] = {nullptr, nullptr};
+    R4<R>* sub_out = nullptr;
+    unsigned long long* sub_next = nullptr;
     auto lay = [&](Bump& bb) {
         if constexpr (BATCH) {
             d_cams = bb.take<CamDev<R>>(bcount);
@@ -1021,7 +1092,15 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             P.cams = d_cams;
             P.frame_start = d_start;
         }
-        if (persistent) {
+        if (subs) { // per-pixel sums, two pixel lists, one round's sample radiance
+            layout_slots<R>(bb, P.ps, n, false);
+            P.ps.counters = bb.take<uint32_t>(C_COUNT);
+            sub_list[0] = bb.take<uint32_t>(n);
+            sub_list[1] = bb.take<uint32_t>(n);
+            sub_out = bb.take<R4<R>>(sub_items);
+            sub_next = bb.take<unsigned long long>(1);
+            SP[0] = P;
+        } else if (persistent) {
             P.ps.n = n;
             P.ps.counters = bb.take<uint32_t>(C_COUNT);
             P.ps.totals = bb.take<unsigned long long>(8);
@@ -1118,6 +1197,36 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         if (profile) {
             GT_CUDA(cudaEventRecord(z, st));
             ev.note(GT_KERNEL_OTHER, a, z);
+        }
+    }
+
+    if (subs) {
+        uint64_t rounds = 0;
+        if ((rc = run_substreams<R, BATCH>(ctx, P, sub_list, sub_out, sub_next, n, limit_max, opts, ev, kms, klaunch,
+                                           rounds)) != GT_OK)
+            return rc;
+        k_resolve<R, BATCH><<<slot_blocks, threads, 0, st>>>(P, o_rgb, o_rgb64, o_acc);
+        GT_CUDA(cudaGetLastError());
+        klaunch[GT_KERNEL_OTHER] += 1;
+        if (!BATCH && opts.aovs && (o_alb || o_nrm)) { // the AOV pass keeps the reference's pixel streams
+            k_aov<R><<<slot_blocks, threads, 0, st>>>(P, o_alb, o_nrm);
+            GT_CUDA(cudaGetLastError());
+            klaunch[GT_KERNEL_OTHER] += 1;
+        }
+        if constexpr (BATCH) {
+            for (uint32_t i = 0; i < bcount; ++i) {
+                gt_frame* f = bframes[i];
+                const size_t o = bstart[i], np = size_t(bstart[i + 1]) - bstart[i];
+                const cudaMemcpyKind kind = f->device_buffers ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+                GT_CUDA(cudaMemcpyAsync(f->rgb, d_rgb + o * 3, np * 3 * sizeof(float), kind, st));
+                if (f->rgb64) GT_CUDA(cudaMemcpyAsync(f->rgb64, d_rgb64 + o * 3, np * 3 * sizeof(double), kind, st));
+                if (f->accepted) GT_CUDA(cudaMemcpyAsync(f->accepted, d_acc + o, np * sizeof(uint32_t), kind, st));
+            }
+            return finish_render<R>(ctx, P, nullptr, opts, false, n, o_rgb, o_rgb64, o_acc, o_alb, o_nrm, ev, kms,
+                                    klaunch, rounds);
+        } else {
+            return finish_render<R>(ctx, P, frame, opts, host_out, n, o_rgb, o_rgb64, o_acc, o_alb, o_nrm, ev, kms,
+                                    klaunch, rounds);
         }
     }
 

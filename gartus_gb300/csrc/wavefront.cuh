@@ -955,6 +955,171 @@ template <class R> __global__ void __launch_bounds__(256) k_collect(Params<R> P,
     }
 }
 
+// Throughput mode (gt_render_opts.rng = GT_RNG_SUBSTREAMS; no reference counterpart).
+// Sample s of pixel (x, y) draws from its own SplitMix64 stream, started at
+// pixel_seed(seed, x, y) ^ sample_key(s), instead of continuing the pixel's one stream:
+// statistically the reference's estimator, not its stream.  Samples are then independent,
+// so every (pixel, sample) pair of a round is a work item and no pixel's samples form a
+// chain.  k_substream traces a round's items; k_sub_fold adds each pixel's samples in
+// sample order (Kahan sums, or Welford with the adaptive stop exactly where the reference
+// would stop), so the image does not depend on the order in which items ran.
+GT_DEV uint64_t sample_key(uint64_t s) {
+    uint64_t z = (s + 1) * 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+// Items a lane claims at a time (one atomicAdd per claim).
+constexpr uint32_t kSubClaim = 16;
+
+// Round `first` .. first + S - 1 of the `count` pixels in `list`: item i is sample
+// first + i / count of pixel list[i % count] (sample-major, so neighbouring lanes trace
+// neighbouring pixels).  Its radiance goes to out[i] with w = 1, or w = 0 where the sample
+// lies beyond the pixel's sample limit.  Each loop turn traces one ray per lane: a pending
+// shadow query first, as k_persistent does, then the path's next ray.
+template <class R, bool BATCH>
+__global__ void __launch_bounds__(128, sizeof(R) == 8 ? 1 : 4)
+    k_substream(Params<R> P, const uint32_t* list, uint32_t count, uint32_t first, uint32_t S, R4<R>* out,
+                unsigned long long* next) {
+    const unsigned long long items = (unsigned long long)count * S;
+    const R inf = Num<R>::inf();
+    unsigned long long item = 0, end = 0;
+    unsigned long long n_rays = 0, n_shadow = 0;
+    Path<R> p;
+    Shadow<R> sh;
+    Rng g{0};
+    uint32_t pending = 0, pix = 0, frame = 0;
+    bool cont = false; // the path has a next ray (once its pending shadow queries are traced)
+    size_t slot_out = 0;
+    // The camera of the item's pixel: its frame's in a batch, else the render's.
+    auto cam = [&]() -> const CamDev<R>& {
+        if constexpr (BATCH) return P.cams[frame];
+        else return P.cam;
+    };
+    // Sets up the lane's next item that is a sample; false once the items are used up.
+    auto start = [&]() -> bool {
+        for (;;) {
+            if (item == end) {
+                item = atomicAdd(next, (unsigned long long)kSubClaim);
+                if (item >= items) return false;
+                end = item + kSubClaim < items ? item + kSubClaim : items;
+            }
+            const uint32_t j = uint32_t(item / count), k = uint32_t(item % count);
+            slot_out = size_t(item);
+            ++item;
+            pix = list[k];
+            uint32_t local = pix;
+            if constexpr (BATCH) { // frame by binary search over the frame offsets
+                uint32_t lo = 0, hi = P.num_frames;
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (__ldg(&P.frame_start[mid]) <= pix) lo = mid;
+                    else hi = mid;
+                }
+                frame = lo;
+                local = pix - __ldg(&P.frame_start[lo]);
+            }
+            const CamDev<R>& C = cam();
+            const uint32_t s = first + j;
+            if (s >= (C.adaptive ? C.adaptive_max : C.spp)) {
+                out[slot_out] = R4<R>{0, 0, 0, 0};
+                continue;
+            }
+            const uint32_t x = local % C.width, y = local / C.width;
+            g.s = pixel_seed(C.seed, x, y) ^ sample_key(s);
+            camera_ray(C, x, y, s, g, p.o, p.d, p.time);
+            if (C.max_depth == 0) { // the bounce loop never runs: a black sample
+                out[slot_out] = R4<R>{0, 0, 0, 1};
+                continue;
+            }
+            p.att = V3<R>{1, 1, 1};
+            p.col = V3<R>{0, 0, 0};
+            p.miss_w = R(1);
+            p.bounce = 0;
+            p.allow_emit = true;
+            pending = 0;
+            cont = true;
+            return true;
+        }
+    };
+    bool alive = start();
+    while (__any_sync(0xffffffffu, alive)) {
+        const int which = (pending & 1u) ? 0 : ((pending & 2u) ? 1 : -1);
+        R t = R(0);
+        int prim = -1;
+        if (alive) {
+            const V3<R> ro = which >= 0 ? sh.o : p.o;
+            const V3<R> rd = which >= 0 ? sh.dir[which] : p.d;
+            const R rt = which >= 0 ? sh.time : p.time;
+            prim = traverse<R, false, false>(P.sc, ro, rd, rt, R(kShadowAcne), inf, t, nullptr,
+                                             &P.ps.counters[C_ERROR], which == 1);
+        }
+        __syncwarp();
+        if (alive) {
+            if (which >= 0) {
+                apply_shadow(P, p.col, sh, which, prim, t);
+                pending &= ~(1u << which);
+                ++n_shadow;
+            } else {
+                HitRec<R> wrec;
+                ++n_rays;
+                cont = integrate_bounce<R, false>(P, cam(), p, prim, t, g, sh, &wrec);
+                pending = (sh.valid[0] ? 1u : 0u) | (sh.valid[1] ? 2u : 0u);
+            }
+            if (pending == 0 && !cont) {
+                out[slot_out] = R4<R>{p.col.x, p.col.y, p.col.z, R(1)};
+                alive = start();
+            }
+        }
+        __syncwarp();
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        n_rays += __shfl_down_sync(0xffffffffu, n_rays, off);
+        n_shadow += __shfl_down_sync(0xffffffffu, n_shadow, off);
+    }
+    if (lane_id() == 0) {
+        atomicAdd(&P.ps.totals[0], n_rays);
+        atomicAdd(&P.ps.totals[1], n_shadow);
+        atomicAdd(&P.ps.totals[6], n_rays + n_shadow);
+    }
+}
+
+// Folds round first .. first + S - 1 into each listed pixel's sums in sample order; pixels
+// that neither stopped (adaptive) nor reached their sample limit go to next_list.
+template <class R, bool BATCH>
+__global__ void __launch_bounds__(256) k_sub_fold(Params<R> P, const uint32_t* list, uint32_t count, uint32_t first,
+                                                  uint32_t S, const R4<R>* out, uint32_t* next_list,
+                                                  uint32_t* next_count) {
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = warp0; base < count; base += stride) {
+        const uint32_t k = base + lane_id();
+        bool more = false;
+        uint32_t pix = 0;
+        if (k < count) {
+            pix = list[k];
+            uint32_t local;
+            const CamDev<R>& C = cam_of<R, BATCH>(P, pix, local);
+            const uint32_t limit = C.adaptive ? C.adaptive_max : C.spp;
+            R4<R> a = P.ps.acc[pix], c = P.ps.comp[pix];
+            uint32_t acc_n = P.ps.accepted[pix], started = P.ps.st[pix].w;
+            bool stop = false;
+            for (uint32_t j = 0; j < S && first + j < limit && !stop; ++j) {
+                const R4<R> v = out[size_t(j) * count + k];
+                started = first + j + 1;
+                stop = fold_sample(C, a, c, acc_n, xyz(v));
+            }
+            P.ps.acc[pix] = a;
+            P.ps.comp[pix] = c;
+            P.ps.accepted[pix] = acc_n;
+            P.ps.st[pix].w = started;
+            more = !stop && started < limit;
+        }
+        warp_push(more, pix, next_list, next_count);
+    }
+}
+
 // Slow-slot migration.  A wavefront slot advances one bounce per iteration, so a frame
 // lasts as long as its longest per-pixel sample chain (pixels behind glass run several
 // times the median number of bounces).  Early in the frame the slots whose sample rate

@@ -1380,16 +1380,20 @@ class PathTracer:
     pixels; 0 = the library's choice), "wavefront" or "persistent"; the image is the same.
     migrate: "default", "on" or "off": whether "auto" moves each stripe's slow pixels to a
     concurrent persistent kernel early in the frame (gt_migrate; default = on for scenes of
-    at most 65,536 primitives)."""
+    at most 65,536 primitives).
+    rng: "pixel" (the reference: each pixel's samples continue one random stream) or
+    "substreams" (throughput mode: each sample draws from its own stream, so all of a
+    pixel's samples run in parallel; the same estimator, not the same numbers)."""
 
     SCHEDULES = {"auto": abi.GT_SCHEDULE_AUTO, "wavefront": abi.GT_SCHEDULE_WAVEFRONT,
                  "persistent": abi.GT_SCHEDULE_PERSISTENT}
     MIGRATE = {"default": abi.GT_MIGRATE_DEFAULT, "on": abi.GT_MIGRATE_ON, "off": abi.GT_MIGRATE_OFF}
+    RNG = {"pixel": abi.GT_RNG_PIXEL, "substreams": abi.GT_RNG_SUBSTREAMS}
 
     def __init__(self, camera: RayCamera, options: RenderOptions = RenderOptions(), precision: str = "f32",
                  context: Optional[Context] = None, profile: bool = False, schedule: str = "auto",
                  tail_slots: int = 0, stripes: int = 0, generate_blocks_per_sm: int = 0,
-                 trace_blocks_per_sm: int = 0, migrate: str = "default"):
+                 trace_blocks_per_sm: int = 0, migrate: str = "default", rng: str = "pixel"):
         if precision not in ("f32", "f64"):
             raise ValueError("precision must be 'f32' or 'f64'")
         if schedule not in self.SCHEDULES:
@@ -1405,7 +1409,10 @@ class PathTracer:
         self.trace_blocks_per_sm = int(trace_blocks_per_sm)
         if migrate not in self.MIGRATE:
             raise ValueError(f"migrate must be one of {sorted(self.MIGRATE)}")
+        if rng not in self.RNG:
+            raise ValueError(f"rng must be one of {sorted(self.RNG)}")
         self.migrate = migrate
+        self.rng = rng
         self._ctx = context
         self.last_stats: Optional[dict] = None
 
@@ -1416,7 +1423,7 @@ class PathTracer:
     def _launch_kw(self) -> dict:
         return {"schedule": self.schedule, "tail_slots": self.tail_slots, "stripes": self.stripes,
                 "generate_blocks_per_sm": self.generate_blocks_per_sm, "trace_blocks_per_sm": self.trace_blocks_per_sm,
-                "migrate": self.migrate}
+                "migrate": self.migrate, "rng": self.rng}
 
     def with_options(self, options: RenderOptions) -> "PathTracer":
         return PathTracer(self.camera, options, self.precision, self._ctx, self.profile, **self._launch_kw())
@@ -1429,6 +1436,7 @@ class PathTracer:
         o.generate_blocks_per_sm = self.generate_blocks_per_sm
         o.trace_blocks_per_sm = self.trace_blocks_per_sm
         o.migrate = self.MIGRATE[self.migrate]
+        o.rng = self.RNG[self.rng]
 
     def autotune(self, world: RayScene, lights: Optional[WeightedSamplingTargetList] = None,
                  environment: Optional[EnvironmentLight] = None, cameras=None) -> dict:

@@ -388,7 +388,19 @@ typedef struct gt_render_opts {
      * their cap) move to a persistent kernel that runs them concurrently with the wavefront.
      * gt_migrate; f64 images do not depend on it. */
     uint32_t migrate;
+    /* Per-sample random streams, gt_rng.  GT_RNG_PIXEL (the reference, camera.rs:2669):
+     * each pixel's samples continue one stream.  GT_RNG_SUBSTREAMS (throughput mode, no
+     * reference counterpart): sample s of pixel (x, y) draws from its own SplitMix64 stream
+     * started at pixel_seed(seed, x, y) ^ sample_key(s), where sample_key(s) is SplitMix64's
+     * output for state (s + 1) * 0x9E3779B97F4A7C15; the samples of a pixel are then
+     * independent and run in parallel.  The estimator is the reference's (adaptive
+     * sampling stops at the same sample for the same sample values), the streams are not.
+     * The schedule is ignored; accumulation, worlds with objects or media, and f64 batches
+     * return GT_ERR_UNSUPPORTED. */
+    uint32_t rng;
 } gt_render_opts;
+
+typedef enum gt_rng { GT_RNG_PIXEL = 0, GT_RNG_SUBSTREAMS = 1 } gt_rng;
 
 typedef enum gt_migrate {
     GT_MIGRATE_DEFAULT = 0, /* on for scenes of at most 65,536 primitives, off above: there the

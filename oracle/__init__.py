@@ -41,10 +41,10 @@ def lib() -> C.CDLL:
                 "orc_trace_rays": (i32, [vp, vp, u32, f64, f64, i32, i32, vp, vp, vp, vp]),
                 "orc_camera": (i32, [vp, vp, vp, vp, vp]),
                 "orc_trace_primary": (i32, [vp, vp, u32, vp, vp, vp]),
-                "orc_render": (i32, [vp, vp, u32, vp, vp, i32, u32, u32, u32, u32, u32, i32, vp, vp, vp, vp]),
+                "orc_render": (i32, [vp, vp, u32, vp, vp, i32, u32, u32, u32, u32, u32, u32, i32, vp, vp, vp, vp]),
                 "orc_pixel_seed": (u64, [u64, u32, u32]),
                 "orc_slab": (i32, [vp, vp, f64, f64, vp]),
-                "orc_pixel_trace": (C.c_int64, [vp, vp, u32, vp, vp, i32, u32, u32, vp, vp, u64]),
+                "orc_pixel_trace": (C.c_int64, [vp, vp, u32, vp, vp, i32, u32, u32, u32, vp, vp, u64]),
                 "orc_rng_u64": (None, [u64, u32, vp]),
                 "orc_rng_double": (None, [u64, u32, vp]),
                 "orc_perlin": (None, [u64, C.c_int, C.c_int, u32, vp, vp]),
@@ -78,6 +78,11 @@ def lib() -> C.CDLL:
 
 def _ptr(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+# Per-sample random streams of a render: the reference's (one per pixel) or the GPU
+# throughput mode's (one per pixel and sample).
+RNG_MODES = {"pixel": 0, "substreams": 1}
 
 
 class OracleScene:
@@ -167,9 +172,10 @@ class OracleScene:
         return ids, t, st.as_dict()
 
     def pixel_trace(self, camera_desc, x: int, y: int, lights: np.ndarray | None = None, env=None,
-                    precision: int = 1):
+                    precision: int = 1, rng: str = "pixel"):
         """The decision trace of pixel (x, y): (types, outcomes, values) of every discrete
-        decision its samples take, in order (TraceEvent in gartus_oracle.hpp)."""
+        decision its samples take, in order (TraceEvent in gartus_oracle.hpp); rng as in
+        render."""
         la = None if lights is None else np.ascontiguousarray(lights)
         envd = env.desc() if env is not None else None
         cap = 4096
@@ -178,7 +184,7 @@ class OracleScene:
             values = np.zeros(cap)
             n = lib().orc_pixel_trace(self.h, _ptr(la) if la is not None else None, len(la) if la is not None else 0,
                                       C.byref(envd) if envd is not None else None, C.byref(camera_desc), precision,
-                                      x, y, _ptr(kinds), _ptr(values), cap)
+                                      RNG_MODES[rng], x, y, _ptr(kinds), _ptr(values), cap)
             if n < 0:
                 raise ValueError("pixel outside the image")
             if n <= cap:
@@ -186,8 +192,10 @@ class OracleScene:
             cap = int(n)
 
     def render(self, camera_desc, lights: np.ndarray | None = None, env=None, precision: int = 1,
-               threads: int = 1, window=(0, 0, 0, 0), aovs: bool = False):
-        """Renders (a window of) the image; returns (rgb, accepted[, albedo, normal])."""
+               threads: int = 1, window=(0, 0, 0, 0), aovs: bool = False, rng: str = "pixel"):
+        """Renders (a window of) the image; returns (rgb, accepted[, albedo, normal]).  rng:
+        "pixel" (each pixel's samples continue one stream, the reference) or "substreams"
+        (sample s of pixel (x, y) draws from pixel_seed ^ sample_key(s))."""
         w, h, spp = camera_size(camera_desc)
         x0, y0, ww, hh = window
         ww = ww or w
@@ -203,8 +211,8 @@ class OracleScene:
             lp = _ptr(lights)
             nl = len(lights)
         envd = C.byref(env.desc()) if env is not None else None
-        rc = lib().orc_render(self.h, lp, nl, envd, C.byref(camera_desc), precision, threads, x0, y0, ww, hh,
-                              int(aovs), _ptr(rgb), _ptr(alb), _ptr(nrm), _ptr(acc))
+        rc = lib().orc_render(self.h, lp, nl, envd, C.byref(camera_desc), precision, RNG_MODES[rng], threads, x0,
+                              y0, ww, hh, int(aovs), _ptr(rgb), _ptr(alb), _ptr(nrm), _ptr(acc))
         if rc != 0:
             raise RuntimeError(f"oracle render failed ({rc})")
         if aovs:

@@ -201,6 +201,16 @@ inline uint64_t pixel_seed(uint64_t seed, uint32_t x, uint32_t y) {
     return z ^ (z >> 31);
 }
 
+// The throughput mode's per-sample substream key (no reference counterpart): SplitMix64's
+// output for state (s + 1) * golden gamma; sample s of pixel (x, y) starts its own stream
+// at pixel_seed(seed, x, y) ^ sample_key(s).
+inline uint64_t sample_key(uint64_t s) {
+    uint64_t z = (s + 1) * 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
 // -------------------------------------------------------------------- bounds
 // Bounds3, gmath/polygon_matrix.rs:19-140 (always f64: the BVH is built in f64).
 struct Bounds {
@@ -2013,6 +2023,9 @@ template <class R> struct Renderer {
     bool nee = false;
     R light_pdf_weight{0.5};
     int rr_min_depth = 5;
+    // Throughput mode: every sample draws from its own (pixel, sample) substream instead
+    // of continuing the pixel's one stream (statistically equivalent, not stream-identical).
+    bool substreams = false;
 
     void setup(const gt_camera_desc& d) {
         cam.init(d);
@@ -2174,7 +2187,12 @@ template <class R> struct Renderer {
     // render_world_linear_pixel_with_context (camera.rs:2660-2723) plus adaptive
     // sampling (2937-2982).  Returns the pixel colour and the accepted-sample count.
     V3<R> pixel(uint32_t x, uint32_t y, uint32_t& accepted) const {
-        SampleRng rng(pixel_seed(cam.desc.rng_seed, x, y));
+        const uint64_t seed = pixel_seed(cam.desc.rng_seed, x, y);
+        SampleRng rng(seed);
+        // Sample i's stream: the pixel's, continued; or its own substream.
+        auto start_sample = [&](uint32_t i) {
+            if (substreams) rng = SampleRng(seed ^ sample_key(i));
+        };
         V3<R> sum;
         accepted = 0;
         if (cam.desc.pixel_sample_mode == GT_SAMPLE_RANDOM) {
@@ -2183,6 +2201,7 @@ template <class R> struct Renderer {
                 uint32_t mx = std::max<uint32_t>(cam.desc.adaptive_max_samples, mn);
                 V3<R> mean, m2;
                 for (uint32_t i = 0; i < mx; ++i) {
+                    start_sample(i);
                     V3<R> s = ray_color(cam.ray_for_pixel_sample(x, y, rng), rng);
                     trace_note(TR_SAMPLE, finite3(s) ? 1 : 0, finite3(s) ? double(s.x + s.y + s.z) : 0.0);
                     if (!finite3(s)) continue;
@@ -2201,6 +2220,7 @@ template <class R> struct Renderer {
                 return mean;
             }
             for (uint32_t i = 0; i < cam.desc.samples_per_pixel; ++i) {
+                start_sample(i);
                 V3<R> s = ray_color(cam.ray_for_pixel_sample(x, y, rng), rng);
                 trace_note(TR_SAMPLE, finite3(s) ? 1 : 0, finite3(s) ? double(s.x + s.y + s.z) : 0.0);
                 if (finite3(s)) {
@@ -2212,6 +2232,7 @@ template <class R> struct Renderer {
             uint32_t g = cam.grid_width();
             for (uint32_t sy = 0; sy < g; ++sy)
                 for (uint32_t sx = 0; sx < g; ++sx) {
+                    start_sample(sy * g + sx);
                     V3<R> s = ray_color(cam.ray_for_pixel_stratified(x, y, sx, sy, g, rng), rng);
                     trace_note(TR_SAMPLE, finite3(s) ? 1 : 0, finite3(s) ? double(s.x + s.y + s.z) : 0.0);
                     if (finite3(s)) {

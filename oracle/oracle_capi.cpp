@@ -28,8 +28,8 @@ template <class R> void fill_stats(const BvhStats& st, gt_bvh_stats* out) {
 
 template <class R>
 int render_impl(const Scene<R>& scene, const gt_light_target* lights, uint32_t nl, const gt_environment_desc* envd,
-                const gt_camera_desc* cam, uint32_t threads, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h,
-                int aovs, double* rgb, double* albedo, double* normal, uint32_t* accepted) {
+                const gt_camera_desc* cam, uint32_t rng_mode, uint32_t threads, uint32_t x0, uint32_t y0, uint32_t w,
+                uint32_t h, int aovs, double* rgb, double* albedo, double* normal, uint32_t* accepted) {
     LightList<R> ll;
     for (uint32_t i = 0; i < nl; ++i) {
         LightTarget<R> t;
@@ -58,6 +58,7 @@ int render_impl(const Scene<R>& scene, const gt_light_target* lights, uint32_t n
     r.lights = lights ? &ll : nullptr;
     r.env = envd ? &env : nullptr;
     r.setup(*cam);
+    r.substreams = rng_mode == 1;
     if (w == 0) w = r.cam.width;
     if (h == 0) h = r.cam.height;
     if (x0 + w > r.cam.width || y0 + h > r.cam.height) return 1;
@@ -108,7 +109,7 @@ int render_impl(const Scene<R>& scene, const gt_light_target* lights, uint32_t n
 // for one pixel, with g_trace pointing at `out`.
 template <class R>
 int trace_impl(const Scene<R>& scene, const gt_light_target* lights, uint32_t nl, const gt_environment_desc* envd,
-               const gt_camera_desc* cam, uint32_t x, uint32_t y, std::vector<TraceEvent>& out) {
+               const gt_camera_desc* cam, uint32_t rng_mode, uint32_t x, uint32_t y, std::vector<TraceEvent>& out) {
     LightList<R> ll;
     for (uint32_t i = 0; i < nl; ++i) {
         LightTarget<R> t;
@@ -137,6 +138,7 @@ int trace_impl(const Scene<R>& scene, const gt_light_target* lights, uint32_t nl
     r.lights = lights ? &ll : nullptr;
     r.env = envd ? &env : nullptr;
     r.setup(*cam);
+    r.substreams = rng_mode == 1;
     if (x >= r.cam.width || y >= r.cam.height) return 1;
     uint32_t acc = 0;
     g_trace = &out;
@@ -153,13 +155,13 @@ extern "C" {
 // pairs and values; returns the number of events the pixel made (possibly above cap), or
 // -1 on error.
 int64_t orc_pixel_trace(void* sp, const gt_light_target* lights, uint32_t nl, const gt_environment_desc* env,
-                        const gt_camera_desc* cam, int precision, uint32_t x, uint32_t y, int32_t* kinds,
-                        double* values, uint64_t cap) {
+                        const gt_camera_desc* cam, int precision, uint32_t rng_mode, uint32_t x, uint32_t y,
+                        int32_t* kinds, double* values, uint64_t cap) {
     auto* s = static_cast<OrcScene*>(sp);
     std::vector<TraceEvent> ev;
     try {
-        const int rc = precision == 1 ? trace_impl<double>(s->s64, lights, nl, env, cam, x, y, ev)
-                                      : trace_impl<float>(s->s32, lights, nl, env, cam, x, y, ev);
+        const int rc = precision == 1 ? trace_impl<double>(s->s64, lights, nl, env, cam, rng_mode, x, y, ev)
+                                      : trace_impl<float>(s->s32, lights, nl, env, cam, rng_mode, x, y, ev);
         if (rc) return -1;
     } catch (...) {
         g_trace = nullptr;
@@ -299,17 +301,18 @@ int orc_trace_primary(void* sp, const gt_camera_desc* d, uint32_t stride, int32_
 }
 
 // Renders the window [x0, x0+w) x [y0, y0+h) (w = h = 0: the whole image).
-// precision: 1 = Oracle<double>, 0 = Oracle<float>.  Returns 0 on success.
+// precision: 1 = Oracle<double>, 0 = Oracle<float>; rng_mode: 0 = the pixel's one stream
+// (the reference), 1 = a substream per sample.  Returns 0 on success.
 int orc_render(void* sp, const gt_light_target* lights, uint32_t nl, const gt_environment_desc* env,
-               const gt_camera_desc* cam, int precision, uint32_t threads, uint32_t x0, uint32_t y0, uint32_t w,
-               uint32_t h, int aovs, double* rgb, double* albedo, double* normal, uint32_t* accepted) {
+               const gt_camera_desc* cam, int precision, uint32_t rng_mode, uint32_t threads, uint32_t x0, uint32_t y0,
+               uint32_t w, uint32_t h, int aovs, double* rgb, double* albedo, double* normal, uint32_t* accepted) {
     auto* s = static_cast<OrcScene*>(sp);
     try {
         if (precision == 1)
-            return render_impl<double>(s->s64, lights, nl, env, cam, threads, x0, y0, w, h, aovs, rgb, albedo, normal,
-                                       accepted);
-        return render_impl<float>(s->s32, lights, nl, env, cam, threads, x0, y0, w, h, aovs, rgb, albedo, normal,
-                                  accepted);
+            return render_impl<double>(s->s64, lights, nl, env, cam, rng_mode, threads, x0, y0, w, h, aovs, rgb, albedo,
+                                       normal, accepted);
+        return render_impl<float>(s->s32, lights, nl, env, cam, rng_mode, threads, x0, y0, w, h, aovs, rgb, albedo,
+                                  normal, accepted);
     } catch (...) {
         return 2;
     }

@@ -76,7 +76,7 @@ def first_flip(t64, t32):
     return None if len(a_t) == len(b_t) else n
 
 
-def classify(scene, cam, x32, ref64, ref32, lights=None, env=None, tol=1e-4, limit=None):
+def classify(scene, cam, x32, ref64, ref32, lights=None, env=None, tol=1e-4, limit=None, rng="pixel"):
     """Causes of the pixels where the f32 image x32 leaves the f64 reference ref64 by more
     than tol: a Counter of cause names and a list of (y, x, cause, margin) entries, where
     margin is the f64 run's margin of the attributed decision where it has one (for an
@@ -86,8 +86,8 @@ def classify(scene, cam, x32, ref64, ref32, lights=None, env=None, tol=1e-4, lim
     div = divergent_pixels(x32, ref64, tol)
     counts, rows = Counter(), []
     for y, x in np.argwhere(div)[:limit]:
-        t64 = o.pixel_trace(cam.desc(), int(x), int(y), la, env, precision=1)
-        t32 = o.pixel_trace(cam.desc(), int(x), int(y), la, env, precision=0)
+        t64 = o.pixel_trace(cam.desc(), int(x), int(y), la, env, precision=1, rng=rng)
+        t32 = o.pixel_trace(cam.desc(), int(x), int(y), la, env, precision=0, rng=rng)
         k = first_flip(t64, t32)
         margin = None
         if k is not None:
@@ -123,10 +123,11 @@ def report(name, counts, total):
     print(f"{name}: {n}/{total} pixels beyond 1e-4 of f64 — {parts if parts else 'none'}")
 
 
-def assert_explained(name, scene, cam, x32, ref64, ref32, lights=None, env=None, tol=1e-4):
+def assert_explained(name, scene, cam, x32, ref64, ref32, lights=None, env=None, tol=1e-4, rng="pixel"):
     """Classifies the f32 image's divergent pixels, prints the counts by cause, and fails
-    on any unexplained pixel (zero slack).  Returns the Counter."""
-    counts, rows = classify(scene, cam, x32, ref64, ref32, lights, env, tol)
+    on any unexplained pixel (zero slack).  Returns the Counter.  rng: the per-sample
+    streams the images were rendered with ("pixel" or "substreams")."""
+    counts, rows = classify(scene, cam, x32, ref64, ref32, lights, env, tol, rng=rng)
     report(name, counts, ref64.shape[0] * ref64.shape[1])
     bad = [r for r in rows if r[2] == UNEXPLAINED]
     assert not bad, f"{name}: {len(bad)} unexplained divergent pixels, first {bad[:5]}"
@@ -136,16 +137,16 @@ def assert_explained(name, scene, cam, x32, ref64, ref32, lights=None, env=None,
     return counts
 
 
-def assert_modes_agree(name, scene, cam, a, b, lights=None, env=None, tol=1e-4):
+def assert_modes_agree(name, scene, cam, a, b, lights=None, env=None, tol=1e-4, rng="pixel"):
     """Two f32 renders of one frame by different kernels (a batch and a single frame,
     accumulated chunks and one render, another schedule): every pixel where they differ
     must be a pixel where one of them leaves the f64 reference for an explained cause."""
     o = oracle.OracleScene.from_ray_scene(scene)
     la = lights.to_array() if lights is not None else None
-    ref64, _ = o.render(cam.desc(), la, env, precision=1, threads=8)
-    ref32, _ = o.render(cam.desc(), la, env, precision=0, threads=8)
-    assert_explained(f"{name} (a)", scene, cam, a, ref64, ref32, lights, env, tol)
-    assert_explained(f"{name} (b)", scene, cam, b, ref64, ref32, lights, env, tol)
+    ref64, _ = o.render(cam.desc(), la, env, precision=1, threads=8, rng=rng)
+    ref32, _ = o.render(cam.desc(), la, env, precision=0, threads=8, rng=rng)
+    assert_explained(f"{name} (a)", scene, cam, a, ref64, ref32, lights, env, tol, rng=rng)
+    assert_explained(f"{name} (b)", scene, cam, b, ref64, ref32, lights, env, tol, rng=rng)
     differ = divergent_pixels(a, np.asarray(b, dtype=np.float64), tol)
     covered = divergent_pixels(a, ref64, tol) | divergent_pixels(b, ref64, tol)
     assert not (differ & ~covered).any(), f"{name}: {int((differ & ~covered).sum())} pixels differ between the " \
