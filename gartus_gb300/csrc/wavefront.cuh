@@ -189,7 +189,7 @@ template <class R, bool BATCH = false> __global__ void __launch_bounds__(256) k_
     }
 }
 
-template <class R> __global__ void __launch_bounds__(256, 4) k_trace(Params<R> P, uint32_t cur) {
+template <class R> __global__ void __launch_bounds__(256, 6) k_trace(Params<R> P, uint32_t cur) {
     const uint32_t count = *reinterpret_cast<volatile uint32_t*>(&P.ps.counters[C_TRACE0 + cur]);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&P.ps.totals[0], (unsigned long long)count);
     const uint32_t* q = P.ps.q_trace[cur];
@@ -469,7 +469,7 @@ template <class R, bool BATCH = false> __global__ void __launch_bounds__(256) k_
     }
 }
 
-template <class R> __global__ void __launch_bounds__(256, 3) k_shadow(Params<R> P) {
+template <class R> __global__ void __launch_bounds__(256, 5) k_shadow(Params<R> P) {
     const uint32_t count = *reinterpret_cast<volatile uint32_t*>(&P.ps.counters[C_SHADOW]);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&P.ps.totals[1], (unsigned long long)count);
     const R inf = Num<R>::inf();
