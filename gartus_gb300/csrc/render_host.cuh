@@ -1002,6 +1002,102 @@ gt_status run_substreams(gt_context* ctx, Params<R>& P, uint32_t* const list[2],
     return GT_OK;
 }
 
+// Throughput mode on the wavefront (one frame): each round's (pixel, sample) items are the
+// wavefront's slots.  k_sub_init seeds every slot's own stream, k_generate starts each
+// slot's one sample and, when its path has ended, writes its radiance out; the bounces run
+// through k_trace, k_shade and k_shadow as in the reference mode, sorted by material, and
+// a round ends when every slot is done (at most max_depth + 1 iterations, as no slot
+// starts a second sample).  k_sub_fold then adds the round to the pixels' sums.
+constexpr uint64_t kSubWaveItems = uint64_t(1) << 24; // slots of one round (or one per pixel)
+
+template <class R>
+gt_status run_sub_wavefront(gt_context* ctx, Params<R>& P, Params<R>& W, SubRound<R>* d_sub, uint32_t* const list[2],
+                            R4<R>* out, uint32_t cap, uint32_t n, uint32_t limit_max, bool nee,
+                            const gt_render_opts& opts, EventPool& ev, double* kms, uint64_t* klaunch,
+                            uint64_t& rounds) {
+    cudaStream_t st = ctx->stream;
+    const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1), threads = 256;
+    const uint32_t gen_per_sm = opts.generate_blocks_per_sm ? std::min<uint32_t>(opts.generate_blocks_per_sm, 32u) : 8u;
+    const uint32_t wave_per_sm = opts.trace_blocks_per_sm ? std::min<uint32_t>(opts.trace_blocks_per_sm, 32u) : 6u;
+    const bool profile = opts.profile != 0;
+    const uint32_t fblocks = std::max<uint32_t>(1u, std::min<uint32_t>((n + 255) / 256, sms * 8));
+    // the fold's pixel lists count into words the wavefront does not use in this mode
+    uint32_t* list_count[2] = {P.ps.counters + C_SIDE_DONE, P.ps.counters + C_SIDE_COOP};
+    GT_CUDA(cudaMemsetAsync(W.ps.counters, 0, C_COUNT * sizeof(uint32_t), st));
+    k_list_all<<<fblocks, 256, 0, st>>>(list[0], n, list_count[0]);
+    GT_CUDA(cudaGetLastError());
+    klaunch[GT_KERNEL_OTHER] += 1;
+    uint32_t count = n, cur = 0;
+    for (uint32_t first = 0, round = 0; count > 0 && first < limit_max; first += round, cur ^= 1u) {
+        round = std::max<uint32_t>(1u, std::min<uint32_t>(limit_max - first, cap / count));
+        const uint32_t items = count * round;
+        W.ps.n = items;
+        W.ps.local_n = items;
+        W.ps.stripe = 0;
+        W.ps.stripes = 1;
+        W.ps.row = items;
+        const SubRound<R> h{list[cur], out, count, first};
+        GT_CUDA(cudaMemcpyAsync(d_sub, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+        GT_CUDA(cudaMemsetAsync(W.ps.counters, 0, (C_DONE + 1) * sizeof(uint32_t), st));
+        const uint32_t lblocks = std::max<uint32_t>(1u, std::min<uint32_t>((items + threads - 1) / threads, sms * gen_per_sm));
+        const uint32_t wblocks = std::max<uint32_t>(1u, std::min<uint32_t>((items + threads - 1) / threads, sms * wave_per_sm));
+        k_sub_init<R><<<lblocks, threads, 0, st>>>(W);
+        GT_CUDA(cudaGetLastError());
+        klaunch[GT_KERNEL_OTHER] += 1;
+        // Iterations in batches between checks of the done count: a path lasts at most
+        // max_depth + 1 iterations (camera ray, bounces, and its radiance written out).
+        const uint32_t max_iters = 2u * (W.cam.max_depth + 2u) + 8u;
+        uint32_t iters = 0, q = 0;
+        for (;;) {
+            const uint32_t batch = iters == 0 ? std::min<uint32_t>(W.cam.max_depth + 2u, 16u) : 2u;
+            for (uint32_t b = 0; b < batch; ++b, ++iters, q ^= 1u) {
+                for (int kk = 0; kk < (nee ? 4 : 3); ++kk) {
+                    cudaEvent_t a = nullptr, z = nullptr;
+                    if (profile) {
+                        GT_CUDA(ev.pair(a, z));
+                        GT_CUDA(cudaEventRecord(a, st));
+                    }
+                    if (kk == 0) k_generate<R><<<lblocks, threads, 0, st>>>(W, q);
+                    else if (kk == 1) k_trace<R><<<wblocks, threads, 0, st>>>(W, q);
+                    else if (kk == 2) k_shade<R><<<wblocks, threads, 0, st>>>(W, q);
+                    else k_shadow<R><<<wblocks, threads, 0, st>>>(W);
+                    GT_CUDA(cudaGetLastError());
+                    if (profile) {
+                        GT_CUDA(cudaEventRecord(z, st));
+                        ev.note(kk == 0 ? GT_KERNEL_GENERATE : kk == 1 ? GT_KERNEL_TRACE : kk == 2 ? GT_KERNEL_SHADE
+                                                                                                 : GT_KERNEL_SHADOW,
+                                a, z);
+                    }
+                }
+                klaunch[GT_KERNEL_GENERATE] += 1;
+                klaunch[GT_KERNEL_TRACE] += 1;
+                klaunch[GT_KERNEL_SHADE] += 1;
+                if (nee) klaunch[GT_KERNEL_SHADOW] += 1;
+            }
+            GT_CUDA(cudaMemcpyAsync(ctx->pinned, W.ps.counters + C_DONE, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+            GT_CUDA(cudaStreamSynchronize(st));
+            if (ctx->pinned[0] >= items) break;
+            if (iters > max_iters) return fail(GT_ERR_INTERNAL, "substream round did not finish within its iteration bound");
+        }
+        rounds += iters;
+        GT_CUDA(cudaMemsetAsync(list_count[cur ^ 1u], 0, sizeof(uint32_t), st));
+        k_sub_fold<R, false><<<fblocks, 256, 0, st>>>(P, list[cur], count, first, round, out, list[cur ^ 1u],
+                                                      list_count[cur ^ 1u]);
+        GT_CUDA(cudaGetLastError());
+        klaunch[GT_KERNEL_OTHER] += 1;
+        GT_CUDA(cudaMemcpyAsync(ctx->pinned, list_count[cur ^ 1u], sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        GT_CUDA(cudaStreamSynchronize(st));
+        count = ctx->pinned[0];
+        const uint64_t done = std::min<uint64_t>(uint64_t(first) + round, limit_max);
+        if (opts.progress && call_progress(ctx, opts, done * n, uint64_t(limit_max) * n))
+            return fail(GT_ERR_CANCELLED, "render cancelled by the progress callback");
+    }
+    // the wavefront's stack-overflow flag into the pixel state's counters
+    GT_CUDA(cudaMemcpyAsync(P.ps.counters + C_ERROR, W.ps.counters + C_ERROR, sizeof(uint32_t),
+                            cudaMemcpyDeviceToDevice, st));
+    return GT_OK;
+}
+
 // One frame (BATCH = false) or, with BATCH = true, the frames bcams[0 .. bcount) of equal
 // width as one image of their rows stacked in order: every wavefront kernel then looks up
 // each slot's frame camera, and each frame's slice of the result goes to bframes[i].
@@ -1069,7 +1165,15 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     const bool subs = opts.rng == GT_RNG_SUBSTREAMS;
     if (subs && (world || accum))
         return fail(GT_ERR_UNSUPPORTED, "substreams render neither worlds with objects or media nor accumulations");
-    const uint64_t sub_items = std::max<uint64_t>(kSubItems, n_pix); // one round's sample radiance
+    // A single frame of a scene with more than kSubWaveMinPrims primitives runs its rounds
+    // through the wavefront kernels (k_generate starts each slot's one sample); a batch, or
+    // a small scene, through k_substream.  Measured (Msamples/s, wavefront / k_substream):
+    // final scene (485 spheres) 933 / 669, mesh-heavy 332 / 185, Cornell box (13) 1,376 /
+    // 1,804: with a tiny tree the one-kernel path loop is cheaper than the wavefront's
+    // path-state traffic.
+    constexpr uint32_t kSubWaveMinPrims = 64;
+    const bool sub_wave = subs && !BATCH && P.sc.num_prims > kSubWaveMinPrims;
+    const uint64_t sub_items = std::max<uint64_t>(sub_wave ? kSubWaveItems : kSubItems, n_pix);
     const bool persistent = !subs && ((!BATCH && opts.schedule == GT_SCHEDULE_PERSISTENT && !accum) || (world && !accum));
     const bool host_out = BATCH || frame->device_buffers == 0;
     // Wavefront stripes: rows are dealt round-robin to K independent wavefronts on their
@@ -1085,6 +1189,8 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     uint32_t* sub_list[2] = {nullptr, nullptr};
     R4<R>* sub_out = nullptr;
     unsigned long long* sub_next = nullptr;
+    Params<R> W = P;               // substream wavefront: one round's item slots
+    SubRound<R>* d_sub = nullptr;
     auto lay = [&](Bump& bb) {
         if constexpr (BATCH) {
             d_cams = bb.take<CamDev<R>>(bcount);
@@ -1099,6 +1205,14 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             sub_list[1] = bb.take<uint32_t>(n);
             sub_out = bb.take<R4<R>>(sub_items);
             sub_next = bb.take<unsigned long long>(1);
+            if (sub_wave) { // the wavefront's slots are a round's items
+                W = P;
+                layout_slots<R>(bb, W.ps, uint32_t(sub_items), nee);
+                layout_queues<R>(bb, W.ps, uint32_t(sub_items), nee);
+                W.ps.totals = P.ps.totals;
+                d_sub = bb.take<SubRound<R>>(1);
+                W.sub = d_sub;
+            }
             SP[0] = P;
         } else if (persistent) {
             P.ps.n = n;
@@ -1202,9 +1316,13 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
 
     if (subs) {
         uint64_t rounds = 0;
-        if ((rc = run_substreams<R, BATCH>(ctx, P, sub_list, sub_out, sub_next, n, limit_max, opts, ev, kms, klaunch,
-                                           rounds)) != GT_OK)
-            return rc;
+        if (sub_wave)
+            rc = run_sub_wavefront<R>(ctx, P, W, d_sub, sub_list, sub_out, uint32_t(sub_items), n, limit_max, nee, opts,
+                                      ev, kms, klaunch, rounds);
+        else
+            rc = run_substreams<R, BATCH>(ctx, P, sub_list, sub_out, sub_next, n, limit_max, opts, ev, kms, klaunch,
+                                          rounds);
+        if (rc != GT_OK) return rc;
         k_resolve<R, BATCH><<<slot_blocks, threads, 0, st>>>(P, o_rgb, o_rgb64, o_acc);
         GT_CUDA(cudaGetLastError());
         klaunch[GT_KERNEL_OTHER] += 1;

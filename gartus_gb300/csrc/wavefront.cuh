@@ -13,6 +13,14 @@
 
 namespace gt {
 
+// One round of the throughput mode on the wavefront: slot i holds sample
+// first + i / count of pixel list[i % count]; its radiance goes to out[i].
+template <class R> struct SubRound {
+    const uint32_t* list;
+    R4<R>* out;
+    uint32_t count, first;
+};
+
 template <class R> struct Params {
     SceneDev<R> sc;
     LightsDev<R> lights;
@@ -24,6 +32,9 @@ template <class R> struct Params {
     const CamDev<R>* cams;
     const uint32_t* frame_start;
     uint32_t num_frames;
+    // Throughput mode (substreams) on the wavefront: the current round, in device memory
+    // so that a stripe's cached graph serves every round; null in the reference mode.
+    const SubRound<R>* sub;
 };
 
 // The camera of global pixel `pix` and the pixel's index within its frame: in a batch the
@@ -148,11 +159,43 @@ template <class R, bool BATCH = false> __global__ void __launch_bounds__(256) k_
     const uint32_t n = P.ps.local_n;
     const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
     const uint32_t stride = gridDim.x * blockDim.x;
+    SubRound<R> sr{nullptr, nullptr, 0u, 0u};
+    if constexpr (!BATCH) {
+        if (P.sub) sr = *P.sub;
+    }
     for (uint32_t base = warp0; base < n; base += stride) {
         const uint32_t j = base + lane_id();
         const uint32_t slot = j < n ? stripe_slot(P.ps, j) : 0u;
         bool push = false;
-        if (j < n) {
+        if (j < n && sr.list) { // substreams: the slot's one sample, then its radiance out
+            uint4 st = P.ps.st[slot];
+            if (st.z & F_NEWSAMPLE) {
+                uint32_t flags = F_DONE;
+                Rng g{uint64_t(st.x) | (uint64_t(st.y) << 32)};
+                if (st.w > 0) {
+                    const R4<R> c = P.ps.col[slot];
+                    sr.out[slot] = R4<R>{c.x, c.y, c.z, R(1)};
+                } else {
+                    const CamDev<R>& C = P.cam;
+                    const uint32_t pix = sr.list[slot % sr.count], s = sr.first + slot / sr.count;
+                    V3<R> o, d;
+                    R time;
+                    camera_ray(C, pix % C.width, pix / C.width, s, g, o, d, time);
+                    if (C.max_depth == 0) { // the bounce loop never runs: a black sample
+                        sr.out[slot] = R4<R>{0, 0, 0, R(1)};
+                    } else {
+                        P.ps.ray_o[slot] = R4<R>{o.x, o.y, o.z, time};
+                        P.ps.ray_d[slot] = R4<R>{d.x, d.y, d.z, R(1)};
+                        P.ps.att[slot] = R4<R>{1, 1, 1, 0};
+                        P.ps.col[slot] = R4<R>{0, 0, 0, 0};
+                        flags = F_TRACE | F_ALLOW_EMIT;
+                        push = true;
+                    }
+                }
+                if (!push) atomicAdd(&P.ps.counters[C_DONE], 1u);
+                P.ps.st[slot] = make_uint4(uint32_t(g.s), uint32_t(g.s >> 32), flags, 1u);
+            }
+        } else if (j < n) {
             uint4 st = P.ps.st[slot];
             if (st.z & F_NEWSAMPLE) {
                 uint32_t local;
@@ -1117,6 +1160,33 @@ __global__ void __launch_bounds__(256) k_sub_fold(Params<R> P, const uint32_t* l
             more = !stop && started < limit;
         }
         warp_push(more, pix, next_list, next_count);
+    }
+}
+
+// Round set-up of the throughput mode on the wavefront: slot i gets its sample's own
+// stream, or is done at once (w = 0 in out) when the sample lies beyond the pixel's limit.
+template <class R> __global__ void __launch_bounds__(256) k_sub_init(Params<R> P) {
+    const SubRound<R> sr = *P.sub;
+    const uint32_t n = P.ps.local_n;
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = warp0; base < n; base += stride) {
+        const uint32_t slot = base + lane_id();
+        bool done = false;
+        if (slot < n) {
+            const uint32_t pix = sr.list[slot % sr.count], s = sr.first + slot / sr.count;
+            const CamDev<R>& C = P.cam;
+            if (s >= (C.adaptive ? C.adaptive_max : C.spp)) {
+                sr.out[slot] = R4<R>{0, 0, 0, 0};
+                P.ps.st[slot] = make_uint4(0u, 0u, F_DONE, 0u);
+                done = true;
+            } else {
+                const uint64_t seed = pixel_seed(C.seed, pix % C.width, pix / C.width) ^ sample_key(s);
+                P.ps.st[slot] = make_uint4(uint32_t(seed), uint32_t(seed >> 32), F_NEWSAMPLE, 0u);
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, done);
+        if (m && lane_id() == 0) atomicAdd(&P.ps.counters[C_DONE], uint32_t(__popc(m)));
     }
 }
 
