@@ -1011,8 +1011,8 @@ gt_status run_substreams(gt_context* ctx, Params<R>& P, uint32_t* const list[2],
 constexpr uint64_t kSubWaveItems = uint64_t(1) << 24; // slots of one round (or one per pixel)
 
 template <class R>
-gt_status run_sub_wavefront(gt_context* ctx, Params<R>& P, Params<R>& W, SubRound<R>* d_sub, uint32_t* const list[2],
-                            R4<R>* out, uint32_t cap, uint32_t n, uint32_t limit_max, bool nee,
+gt_status run_sub_wavefront(gt_context* ctx, Params<R>& P, std::vector<Params<R>>& SW, SubRound<R>* d_sub,
+                            uint32_t* const list[2], R4<R>* out, uint32_t cap, uint32_t n, uint32_t limit_max, bool nee,
                             const gt_render_opts& opts, EventPool& ev, double* kms, uint64_t* klaunch,
                             uint64_t& rounds) {
     cudaStream_t st = ctx->stream;
@@ -1020,10 +1020,11 @@ gt_status run_sub_wavefront(gt_context* ctx, Params<R>& P, Params<R>& W, SubRoun
     const uint32_t gen_per_sm = opts.generate_blocks_per_sm ? std::min<uint32_t>(opts.generate_blocks_per_sm, 32u) : 8u;
     const uint32_t wave_per_sm = opts.trace_blocks_per_sm ? std::min<uint32_t>(opts.trace_blocks_per_sm, 32u) : 6u;
     const bool profile = opts.profile != 0;
+    const uint32_t K = uint32_t(SW.size());
     const uint32_t fblocks = std::max<uint32_t>(1u, std::min<uint32_t>((n + 255) / 256, sms * 8));
     // the fold's pixel lists count into words the wavefront does not use in this mode
     uint32_t* list_count[2] = {P.ps.counters + C_SIDE_DONE, P.ps.counters + C_SIDE_COOP};
-    GT_CUDA(cudaMemsetAsync(W.ps.counters, 0, C_COUNT * sizeof(uint32_t), st));
+    for (uint32_t k = 0; k < K; ++k) GT_CUDA(cudaMemsetAsync(SW[k].ps.counters, 0, C_COUNT * sizeof(uint32_t), st));
     k_list_all<<<fblocks, 256, 0, st>>>(list[0], n, list_count[0]);
     GT_CUDA(cudaGetLastError());
     klaunch[GT_KERNEL_OTHER] += 1;
@@ -1031,53 +1032,139 @@ gt_status run_sub_wavefront(gt_context* ctx, Params<R>& P, Params<R>& W, SubRoun
     for (uint32_t first = 0, round = 0; count > 0 && first < limit_max; first += round, cur ^= 1u) {
         round = std::max<uint32_t>(1u, std::min<uint32_t>(limit_max - first, cap / count));
         const uint32_t items = count * round;
-        W.ps.n = items;
-        W.ps.local_n = items;
-        W.ps.stripe = 0;
-        W.ps.stripes = 1;
-        W.ps.row = items;
+        const uint32_t kk = std::min(K, round); // stripes with rows this round
         const SubRound<R> h{list[cur], out, count, first};
         GT_CUDA(cudaMemcpyAsync(d_sub, &h, sizeof(h), cudaMemcpyHostToDevice, st));
-        GT_CUDA(cudaMemsetAsync(W.ps.counters, 0, (C_DONE + 1) * sizeof(uint32_t), st));
-        const uint32_t lblocks = std::max<uint32_t>(1u, std::min<uint32_t>((items + threads - 1) / threads, sms * gen_per_sm));
-        const uint32_t wblocks = std::max<uint32_t>(1u, std::min<uint32_t>((items + threads - 1) / threads, sms * wave_per_sm));
-        k_sub_init<R><<<lblocks, threads, 0, st>>>(W);
-        GT_CUDA(cudaGetLastError());
-        klaunch[GT_KERNEL_OTHER] += 1;
-        // Iterations in batches between checks of the done count: a path lasts at most
+        for (uint32_t k = 0; k < kk; ++k)
+            GT_CUDA(cudaMemsetAsync(SW[k].ps.counters, 0, (C_DONE + 1) * sizeof(uint32_t), st));
+        cudaEvent_t ready = nullptr;
+        GT_CUDA(ev.get(ready));
+        GT_CUDA(cudaEventRecord(ready, st));
+        ev.free_events.push_back(ready);
+        std::vector<cudaStream_t> ss(kk);
+        std::vector<uint32_t> local(kk), lblocks(kk), wblocks(kk);
+        for (uint32_t k = 0; k < kk; ++k) {
+            Params<R>& Q = SW[k];
+            Q.ps.n = items;
+            Q.ps.stripe = k;
+            Q.ps.stripes = kk;
+            Q.ps.row = count;
+            Q.ps.local_n = local[k] = ((round - k + kk - 1) / kk) * count;
+            lblocks[k] = std::max<uint32_t>(1u, std::min<uint32_t>((local[k] + threads - 1) / threads, sms * gen_per_sm));
+            wblocks[k] = std::max<uint32_t>(1u, std::min<uint32_t>((local[k] + threads - 1) / threads, sms * wave_per_sm));
+            ss[k] = profile ? st : ctx->stripe_stream[k];
+            GT_CUDA(cudaStreamWaitEvent(ss[k], ready, 0));
+            k_sub_init<R><<<lblocks[k], threads, 0, ss[k]>>>(Q);
+            GT_CUDA(cudaGetLastError());
+            klaunch[GT_KERNEL_OTHER] += 1;
+        }
+        // Iterations in batches between checks of the done counts: a path lasts at most
         // max_depth + 1 iterations (camera ray, bounces, and its radiance written out).
-        const uint32_t max_iters = 2u * (W.cam.max_depth + 2u) + 8u;
-        uint32_t iters = 0, q = 0;
-        for (;;) {
-            const uint32_t batch = iters == 0 ? std::min<uint32_t>(W.cam.max_depth + 2u, 16u) : 2u;
-            for (uint32_t b = 0; b < batch; ++b, ++iters, q ^= 1u) {
-                for (int kk = 0; kk < (nee ? 4 : 3); ++kk) {
-                    cudaEvent_t a = nullptr, z = nullptr;
-                    if (profile) {
-                        GT_CUDA(ev.pair(a, z));
-                        GT_CUDA(cudaEventRecord(a, st));
-                    }
-                    if (kk == 0) k_generate<R><<<lblocks, threads, 0, st>>>(W, q);
-                    else if (kk == 1) k_trace<R><<<wblocks, threads, 0, st>>>(W, q);
-                    else if (kk == 2) k_shade<R><<<wblocks, threads, 0, st>>>(W, q);
-                    else k_shadow<R><<<wblocks, threads, 0, st>>>(W);
-                    GT_CUDA(cudaGetLastError());
-                    if (profile) {
-                        GT_CUDA(cudaEventRecord(z, st));
-                        ev.note(kk == 0 ? GT_KERNEL_GENERATE : kk == 1 ? GT_KERNEL_TRACE : kk == 2 ? GT_KERNEL_SHADE
-                                                                                                 : GT_KERNEL_SHADOW,
-                                a, z);
-                    }
-                }
-                klaunch[GT_KERNEL_GENERATE] += 1;
-                klaunch[GT_KERNEL_TRACE] += 1;
-                klaunch[GT_KERNEL_SHADE] += 1;
-                if (nee) klaunch[GT_KERNEL_SHADOW] += 1;
+        const uint32_t max_iters = 2u * (P.cam.max_depth + 2u) + 8u;
+        std::vector<bool> running(kk, true);
+        std::vector<uint32_t> q(kk, 0u);
+        uint32_t iters = 0, active = kk;
+        // The first batch of iterations of stripe k, launched directly or (outside profile
+        // mode) captured once as a graph that is relaunched while the stripe's kernel
+        // parameters and launch sizes stay the same (rounds of one size, renders of one frame).
+        // Without next-event queries k_shade writes each finished sample out, so after the
+        // first iteration only k_generate's counter resets are needed.
+        auto launch_iterations = [&](uint32_t k, uint32_t batch) -> cudaError_t {
+            for (uint32_t b = 0; b < batch; ++b) {
+                const uint32_t qq = (q[k] + b) & 1u;
+                if (b == 0 || nee) k_generate<R><<<lblocks[k], threads, 0, ss[k]>>>(SW[k], qq);
+                else k_iteration_reset<R><<<1, 32, 0, ss[k]>>>(SW[k], qq);
+                k_trace<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k], qq);
+                k_shade<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k], qq);
+                if (nee) k_shadow<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k]);
             }
-            GT_CUDA(cudaMemcpyAsync(ctx->pinned, W.ps.counters + C_DONE, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-            GT_CUDA(cudaStreamSynchronize(st));
-            if (ctx->pinned[0] >= items) break;
-            if (iters > max_iters) return fail(GT_ERR_INTERNAL, "substream round did not finish within its iteration bound");
+            return cudaGetLastError();
+        };
+        auto graph_batch = [&](uint32_t k, uint32_t batch) -> gt_status {
+            std::vector<unsigned char> key(sizeof(Params<R>) + 5 * sizeof(uint32_t));
+            std::memcpy(key.data(), &SW[k], sizeof(Params<R>));
+            const uint32_t extra[5] = {batch, lblocks[k], wblocks[k], nee ? 1u : 0u, 0x5B5u};
+            std::memcpy(key.data() + sizeof(Params<R>), extra, sizeof(extra));
+            gt_context::CachedGraph& cg = ctx->graphs[k];
+            if (!(cg.exec && cg.key == key)) {
+                if (cg.exec) cudaGraphExecDestroy(cg.exec);
+                cg.exec = nullptr;
+                cg.key.clear();
+                cudaGraph_t graph = nullptr;
+                GT_CUDA(cudaStreamBeginCapture(ss[k], cudaStreamCaptureModeThreadLocal));
+                const cudaError_t le = launch_iterations(k, batch);
+                const cudaError_t ce = cudaStreamEndCapture(ss[k], &graph);
+                if (le != cudaSuccess || ce != cudaSuccess) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return cuda_fail(le != cudaSuccess ? le : ce, "substream graph capture");
+                }
+                const cudaError_t ie = cudaGraphInstantiate(&cg.exec, graph, 0);
+                cudaGraphDestroy(graph);
+                if (ie != cudaSuccess) {
+                    cg.exec = nullptr;
+                    return cuda_fail(ie, "cudaGraphInstantiate");
+                }
+                cg.key = std::move(key);
+            }
+            GT_CUDA(cudaGraphLaunch(cg.exec, ss[k]));
+            return GT_OK;
+        };
+        while (active > 0) {
+            const uint32_t batch = iters == 0 ? std::min<uint32_t>(P.cam.max_depth + 2u, 16u) : 2u;
+            for (uint32_t k = 0; k < kk; ++k) {
+                if (!running[k]) continue;
+                if (iters == 0 && !profile) {
+                    gt_status grc;
+                    if ((grc = graph_batch(k, batch)) != GT_OK) return grc;
+                    q[k] ^= batch & 1u;
+                    klaunch[GT_KERNEL_GENERATE] += nee ? batch : 1u;
+                    klaunch[GT_KERNEL_OTHER] += nee ? 0u : batch - 1u;
+                    klaunch[GT_KERNEL_TRACE] += batch;
+                    klaunch[GT_KERNEL_SHADE] += batch;
+                    if (nee) klaunch[GT_KERNEL_SHADOW] += batch;
+                    GT_CUDA(cudaMemcpyAsync(ctx->pinned + 64 + k, SW[k].ps.counters + C_DONE, sizeof(uint32_t),
+                                            cudaMemcpyDeviceToHost, ss[k]));
+                    continue;
+                }
+                for (uint32_t b = 0; b < batch; ++b, q[k] ^= 1u) {
+                    for (int kind = 0; kind < (nee ? 4 : 3); ++kind) {
+                        cudaEvent_t a = nullptr, z = nullptr;
+                        if (profile) {
+                            GT_CUDA(ev.pair(a, z));
+                            GT_CUDA(cudaEventRecord(a, ss[k]));
+                        }
+                        const bool gen = iters + b == 0 || nee;
+                        if (kind == 0 && gen) k_generate<R><<<lblocks[k], threads, 0, ss[k]>>>(SW[k], q[k]);
+                        else if (kind == 0) k_iteration_reset<R><<<1, 32, 0, ss[k]>>>(SW[k], q[k]);
+                        else if (kind == 1) k_trace<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k], q[k]);
+                        else if (kind == 2) k_shade<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k], q[k]);
+                        else k_shadow<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k]);
+                        GT_CUDA(cudaGetLastError());
+                        if (profile) {
+                            GT_CUDA(cudaEventRecord(z, ss[k]));
+                            ev.note(kind == 0 ? GT_KERNEL_GENERATE
+                                              : kind == 1 ? GT_KERNEL_TRACE : kind == 2 ? GT_KERNEL_SHADE : GT_KERNEL_SHADOW,
+                                    a, z);
+                        }
+                    }
+                    klaunch[iters + b == 0 || nee ? GT_KERNEL_GENERATE : GT_KERNEL_OTHER] += 1;
+                    klaunch[GT_KERNEL_TRACE] += 1;
+                    klaunch[GT_KERNEL_SHADE] += 1;
+                    if (nee) klaunch[GT_KERNEL_SHADOW] += 1;
+                }
+                GT_CUDA(cudaMemcpyAsync(ctx->pinned + 64 + k, SW[k].ps.counters + C_DONE, sizeof(uint32_t),
+                                        cudaMemcpyDeviceToHost, ss[k]));
+            }
+            iters += batch;
+            for (uint32_t k = 0; k < kk; ++k)
+                if (running[k]) GT_CUDA(cudaStreamSynchronize(ss[k]));
+            for (uint32_t k = 0; k < kk; ++k)
+                if (running[k] && ctx->pinned[64 + k] >= local[k]) {
+                    running[k] = false;
+                    --active;
+                }
+            if (active > 0 && iters > max_iters)
+                return fail(GT_ERR_INTERNAL, "substream round did not finish within its iteration bound");
         }
         rounds += iters;
         GT_CUDA(cudaMemsetAsync(list_count[cur ^ 1u], 0, sizeof(uint32_t), st));
@@ -1092,9 +1179,13 @@ gt_status run_sub_wavefront(gt_context* ctx, Params<R>& P, Params<R>& W, SubRoun
         if (opts.progress && call_progress(ctx, opts, done * n, uint64_t(limit_max) * n))
             return fail(GT_ERR_CANCELLED, "render cancelled by the progress callback");
     }
-    // the wavefront's stack-overflow flag into the pixel state's counters
-    GT_CUDA(cudaMemcpyAsync(P.ps.counters + C_ERROR, W.ps.counters + C_ERROR, sizeof(uint32_t),
-                            cudaMemcpyDeviceToDevice, st));
+    // the stripes' stack-overflow flags
+    for (uint32_t k = 0; k < K; ++k)
+        GT_CUDA(cudaMemcpyAsync(ctx->pinned + 64 + k, SW[k].ps.counters + C_ERROR, sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, st));
+    GT_CUDA(cudaStreamSynchronize(st));
+    for (uint32_t k = 0; k < K; ++k)
+        if (ctx->pinned[64 + k]) return fail(GT_ERR_INTERNAL, "traversal stack overflow (BVH deeper than the device stack)");
     return GT_OK;
 }
 
@@ -1191,6 +1282,12 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     unsigned long long* sub_next = nullptr;
     Params<R> W = P;               // substream wavefront: one round's item slots
     SubRound<R>* d_sub = nullptr;
+    // its stripes (sample rows dealt round-robin, as pixel rows are in the reference mode)
+    // (default 2: final scene 928 / 995 / 876 / 704 Msamples/s with 1 / 2 / 4 / 8 stripes,
+    // mesh-heavy 332 / 399 / 405 / 399)
+    const uint32_t sub_k = std::max<uint32_t>(1u, std::min<uint32_t>(opts.stripes ? opts.stripes : 2u,
+                                                                      uint32_t(gt_context::kMaxStripes)));
+    std::vector<Params<R>> SW(sub_wave ? sub_k : 0u);
     auto lay = [&](Bump& bb) {
         if constexpr (BATCH) {
             d_cams = bb.take<CamDev<R>>(bcount);
@@ -1205,13 +1302,16 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             sub_list[1] = bb.take<uint32_t>(n);
             sub_out = bb.take<R4<R>>(sub_items);
             sub_next = bb.take<unsigned long long>(1);
-            if (sub_wave) { // the wavefront's slots are a round's items
+            if (sub_wave) { // the wavefront's slots are a round's items, rows dealt to stripes
                 W = P;
                 layout_slots<R>(bb, W.ps, uint32_t(sub_items), nee);
-                layout_queues<R>(bb, W.ps, uint32_t(sub_items), nee);
                 W.ps.totals = P.ps.totals;
                 d_sub = bb.take<SubRound<R>>(1);
                 W.sub = d_sub;
+                for (uint32_t k = 0; k < sub_k; ++k) {
+                    SW[k] = W;
+                    layout_queues<R>(bb, SW[k].ps, uint32_t(sub_items / sub_k + n), nee);
+                }
             }
             SP[0] = P;
         } else if (persistent) {
@@ -1317,8 +1417,8 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     if (subs) {
         uint64_t rounds = 0;
         if (sub_wave)
-            rc = run_sub_wavefront<R>(ctx, P, W, d_sub, sub_list, sub_out, uint32_t(sub_items), n, limit_max, nee, opts,
-                                      ev, kms, klaunch, rounds);
+            rc = run_sub_wavefront<R>(ctx, P, SW, d_sub, sub_list, sub_out, uint32_t(sub_items), n, limit_max, nee,
+                                      opts, ev, kms, klaunch, rounds);
         else
             rc = run_substreams<R, BATCH>(ctx, P, sub_list, sub_out, sub_next, n, limit_max, opts, ev, kms, klaunch,
                                           rounds);

@@ -232,6 +232,15 @@ template <class R, bool BATCH = false> __global__ void __launch_bounds__(256) k_
     }
 }
 
+// The per-iteration counter resets of k_generate, for substream iterations after the first
+// in scenes without next-event queries (there k_shade writes each finished sample out, so
+// no slot needs k_generate again).
+template <class R> __global__ void k_iteration_reset(Params<R> P, uint32_t cur) {
+    if (threadIdx.x == 0) P.ps.counters[C_TRACE0 + (cur ^ 1u)] = 0;
+    if (threadIdx.x < NUM_KEYS) P.ps.counters[C_MAT + threadIdx.x] = 0;
+    if (threadIdx.x == 0) P.ps.counters[C_SHADOW] = 0;
+}
+
 template <class R> __global__ void __launch_bounds__(256, 6) k_trace(Params<R> P, uint32_t cur) {
     const uint32_t count = *reinterpret_cast<volatile uint32_t*>(&P.ps.counters[C_TRACE0 + cur]);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&P.ps.totals[0], (unsigned long long)count);
@@ -440,7 +449,7 @@ GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& 
 
 // Wavefront shade step for `slot`: one bounce, pending shadow queries stored for k_shadow.
 template <class R, bool BATCH>
-GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uint32_t key, bool& shadow) {
+GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uint32_t key, bool& shadow, bool& done) {
     uint4 st = P.ps.st[slot];
     Rng g{uint64_t(st.x) | (uint64_t(st.y) << 32)};
     uint32_t flags = st.z;
@@ -477,6 +486,11 @@ GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uint32_t key, bool& sh
         P.ps.ray_o[slot] = R4<R>{p.o.x, p.o.y, p.o.z, p.time};
         P.ps.ray_d[slot] = R4<R>{p.d.x, p.d.y, p.d.z, p.miss_w};
         P.ps.att[slot] = R4<R>{p.att.x, p.att.y, p.att.z, R(0)};
+    } else if (P.sub && sh_bits == 0) { // substreams: the slot's one sample is complete
+        const R4<R> o = R4<R>{p.col.x, p.col.y, p.col.z, R(1)};
+        P.sub->out[slot] = o;
+        flags = F_DONE;
+        done = true;
     } else {
         flags |= F_NEWSAMPLE;
     }
@@ -497,7 +511,7 @@ template <class R, bool BATCH = false> __global__ void __launch_bounds__(256) k_
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = warp0; base < total; base += stride) {
         const uint32_t i = base + lane_id();
-        bool cont = false, shadow = false;
+        bool cont = false, shadow = false, done = false;
         uint32_t slot = 0;
         if (i < total) {
             uint32_t key = 0;
@@ -505,10 +519,12 @@ template <class R, bool BATCH = false> __global__ void __launch_bounds__(256) k_
             for (uint32_t k = 1; k < NUM_KEYS; ++k)
                 if (i >= prefix[k]) key = k;
             slot = P.ps.q_mat[size_t(key) * P.ps.qcap + (i - prefix[key])];
-            cont = shade_slot<R, BATCH>(P, slot, key, shadow);
+            cont = shade_slot<R, BATCH>(P, slot, key, shadow, done);
         }
         warp_push(cont, slot, P.ps.q_trace[cur ^ 1u], &P.ps.counters[C_TRACE0 + (cur ^ 1u)]);
         warp_push(shadow, slot, P.ps.q_shadow, &P.ps.counters[C_SHADOW]);
+        const unsigned fin = __ballot_sync(0xffffffffu, done);
+        if (fin && lane_id() == 0) atomicAdd(&P.ps.counters[C_DONE], uint32_t(__popc(fin)));
     }
 }
 
@@ -1171,9 +1187,10 @@ template <class R> __global__ void __launch_bounds__(256) k_sub_init(Params<R> P
     const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = warp0; base < n; base += stride) {
-        const uint32_t slot = base + lane_id();
+        const uint32_t j = base + lane_id();
+        const uint32_t slot = j < n ? stripe_slot(P.ps, j) : 0u;
         bool done = false;
-        if (slot < n) {
+        if (j < n) {
             const uint32_t pix = sr.list[slot % sr.count], s = sr.first + slot / sr.count;
             const CamDev<R>& C = P.cam;
             if (s >= (C.adaptive ? C.adaptive_max : C.spp)) {
