@@ -943,7 +943,7 @@ gt_status finish_render(gt_context* ctx, const Params<R>& P, gt_frame* frame, co
 // round as keep the round near kSubItems items (so rounds grow as adaptive pixels stop).
 // Each round traces its (pixel, sample) items in one k_substream launch and folds them into
 // the pixels' sums in sample order (k_sub_fold), which also lists the pixels that go on.
-constexpr uint64_t kSubItems = uint64_t(1) << 24; // work items per round, at most (or one per pixel)
+constexpr uint64_t kSubItems = uint64_t(1) << 26; // work items per round, at most (or one per pixel)
 
 inline uint32_t sub_round_size(uint32_t count, uint32_t remaining) {
     return std::max<uint32_t>(1u, std::min<uint64_t>(remaining, kSubItems / std::max<uint32_t>(count, 1u)));

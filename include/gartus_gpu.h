@@ -371,7 +371,8 @@ typedef struct gt_render_opts {
                                launch keeps resident */
     uint32_t stripes;       /* wavefront schedules: the frame's rows are dealt to this many
                                independent wavefronts on their own streams, whose kernels
-                               overlap on the GPU; 0 = 4, at most 8; images do not depend on it */
+                               overlap on the GPU; 0 = 4 (2 for the sample rows of the
+                               substream mode), at most 8; images do not depend on it */
     /* Optional host buffer of width*height*3 floats.  Before each progress call the library
      * writes the image as far as it is known: finished pixels hold their final value, the
      * others 0 (the partially filled `pixels` of ProgressiveRenderUpdate,
@@ -573,16 +574,17 @@ gt_status gt_render_batch(gt_scene* scene, const gt_lights* lights, const gt_env
 /* Autotuner (no reference counterpart: the reference has no launch parameters to tune).
  * Renders the given jobs (count = 1: one gt_render of jobs[0]; count > 1: gt_render_batch)
  * under candidate settings and writes the fastest into *opts: wavefront stripes, tail
- * size and the wavefront kernels' blocks per SM, chosen one after another (coordinate
- * descent), and last (schedule AUTO only) the persistent schedule, which wins for small
- * frames.  Each candidate is timed by the device time of its second render (the first
+ * size, the wavefront kernels' blocks per SM and (schedule AUTO) slow-pixel migration on
+ * or off, chosen one after another (coordinate descent), and last (schedule AUTO only) the
+ * persistent schedule, which wins for small frames.  Each candidate is timed by the device time of its second render (the first
  * captures its graphs).  A candidate replaces the current best only when at least 1%
  * faster.  The jobs' frames receive the last render.  *opts supplies everything else
  * (precision; schedule AUTO or WAVEFRONT, and PERSISTENT, the outcome of an earlier tune, is
  * tuned as AUTO); report (optional) receives the trial count and the device times with the
  * given and the chosen options.  Launch shapes never change an image.  Choosing the
- * PERSISTENT schedule can change f32 pixels: other kernels finish them and fuse f32
- * operations differently (f64 images and accepted-sample counts stay identical). */
+ * PERSISTENT schedule or another migration setting can change f32 pixels: other kernels
+ * finish them and fuse f32 operations differently (f64 images and accepted-sample counts
+ * stay identical).  The rng mode of *opts is kept. */
 typedef struct gt_autotune_report {
     uint32_t struct_size;
     uint32_t trials;   /* renders timed */
