@@ -86,6 +86,20 @@ def test_f32_substreams_explained(gpu_context, case):
     np.testing.assert_array_equal(again.pixels, img.pixels)
 
 
+def test_substream_stripes_and_engines_agree(gpu_context):
+    # The wavefront engine deals a round's sample rows to stripes; every slot runs the same
+    # arithmetic whichever stripe holds it and the fold adds samples in sample order, so
+    # the image does not depend on the stripe count (1, 2 and 3 stripes over the 128
+    # sample rows of an 80 x 45 frame; 3 leaves the stripes uneven).
+    final = scenes.final_scene_ray_scene()
+    cam = scenes.final_scene_camera(80, 128)
+    imgs = [PathTracer(cam, context=gpu_context, rng="substreams", stripes=k).render_hdr_image(final)
+            for k in (1, 2, 3)]
+    for img in imgs[1:]:
+        np.testing.assert_array_equal(img.pixels, imgs[0].pixels)
+        np.testing.assert_array_equal(img.accepted, imgs[0].accepted)
+
+
 def test_substreams_converge_to_the_reference(gpu_context):
     # Check 3 at 576 spp: the f32 substream image's relMSE against an f64 image of the
     # reference's own streams is no larger than the noise floor between two such images.
