@@ -945,14 +945,20 @@ gt_status finish_render(gt_context* ctx, const Params<R>& P, gt_frame* frame, co
 // the pixels' sums in sample order (k_sub_fold), which also lists the pixels that go on.
 constexpr uint64_t kSubItems = uint64_t(1) << 26; // work items per round, at most (or one per pixel)
 
-inline uint32_t sub_round_size(uint32_t count, uint32_t remaining) {
-    return std::max<uint32_t>(1u, std::min<uint64_t>(remaining, kSubItems / std::max<uint32_t>(count, 1u)));
+// With adaptive sampling a pixel may stop at any sample of a round, and the round's later
+// samples of that pixel are traced for nothing: rounds then take at most
+// kSubAdaptiveRound samples per pixel.
+constexpr uint32_t kSubAdaptiveRound = 8;
+
+inline uint32_t sub_round_size(uint32_t count, uint32_t remaining, bool adaptive) {
+    const uint64_t r = std::min<uint64_t>(remaining, kSubItems / std::max<uint32_t>(count, 1u));
+    return std::max<uint32_t>(1u, uint32_t(adaptive ? std::min<uint64_t>(r, kSubAdaptiveRound) : r));
 }
 
 template <class R, bool BATCH>
 gt_status run_substreams(gt_context* ctx, Params<R>& P, uint32_t* const list[2], R4<R>* out, unsigned long long* next,
-                         uint32_t n, uint32_t limit_max, const gt_render_opts& opts, EventPool& ev, double* kms,
-                         uint64_t* klaunch, uint64_t& rounds) {
+                         uint32_t n, uint32_t limit_max, bool adaptive, const gt_render_opts& opts, EventPool& ev,
+                         double* kms, uint64_t* klaunch, uint64_t& rounds) {
     cudaStream_t st = ctx->stream;
     const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1);
     int per_sm = 0;
@@ -965,7 +971,7 @@ gt_status run_substreams(gt_context* ctx, Params<R>& P, uint32_t* const list[2],
     klaunch[GT_KERNEL_OTHER] += 1;
     uint32_t count = n, cur = 0;
     for (uint32_t first = 0, round = 0; count > 0 && first < limit_max; first += round, cur ^= 1u) {
-        round = sub_round_size(count, limit_max - first);
+        round = sub_round_size(count, limit_max - first, adaptive);
         cudaEvent_t a = nullptr, z = nullptr;
         GT_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned long long), st));
         GT_CUDA(cudaMemsetAsync(P.ps.counters + C_TRACE0 + (cur ^ 1u), 0, sizeof(uint32_t), st));
@@ -1031,6 +1037,7 @@ gt_status run_sub_wavefront(gt_context* ctx, Params<R>& P, std::vector<Params<R>
     uint32_t count = n, cur = 0;
     for (uint32_t first = 0, round = 0; count > 0 && first < limit_max; first += round, cur ^= 1u) {
         round = std::max<uint32_t>(1u, std::min<uint32_t>(limit_max - first, cap / count));
+        if (P.cam.adaptive) round = std::min(round, kSubAdaptiveRound);
         const uint32_t items = count * round;
         const uint32_t kk = std::min(K, round); // stripes with rows this round
         const SubRound<R> h{list[cur], out, count, first};
@@ -1219,7 +1226,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     uint32_t n_pix = cam.width * cam.height;
     uint32_t img_h = cam.height; // rows the stripes deal out
     uint32_t limit_max = P.cam.adaptive ? P.cam.adaptive_max : P.cam.spp, depth_max = P.cam.max_depth;
-    bool any_nee = P.cam.nee && (use_lights || use_env), want64 = false;
+    bool any_nee = P.cam.nee && (use_lights || use_env), want64 = false, any_adaptive = P.cam.adaptive != 0;
     std::vector<CamDev<R>> bcd;
     std::vector<uint32_t> bstart;
     if constexpr (BATCH) {
@@ -1236,6 +1243,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             limit_max = std::max(limit_max, bcd[i].adaptive ? bcd[i].adaptive_max : bcd[i].spp);
             depth_max = std::max(depth_max, bcd[i].max_depth);
             any_nee = any_nee || (bcd[i].nee && (use_lights || use_env));
+            any_adaptive = any_adaptive || bcd[i].adaptive != 0;
             want64 = want64 || bframes[i]->rgb64 != nullptr;
         }
         bstart[bcount] = uint32_t(total);
@@ -1420,8 +1428,8 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             rc = run_sub_wavefront<R>(ctx, P, SW, d_sub, sub_list, sub_out, uint32_t(sub_items), n, limit_max, nee,
                                       opts, ev, kms, klaunch, rounds);
         else
-            rc = run_substreams<R, BATCH>(ctx, P, sub_list, sub_out, sub_next, n, limit_max, opts, ev, kms, klaunch,
-                                          rounds);
+            rc = run_substreams<R, BATCH>(ctx, P, sub_list, sub_out, sub_next, n, limit_max, any_adaptive, opts, ev,
+                                          kms, klaunch, rounds);
         if (rc != GT_OK) return rc;
         k_resolve<R, BATCH><<<slot_blocks, threads, 0, st>>>(P, o_rgb, o_rgb64, o_acc);
         GT_CUDA(cudaGetLastError());
