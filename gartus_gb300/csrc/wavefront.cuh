@@ -500,7 +500,7 @@ GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uint32_t key, bool& sh
     return cont;
 }
 
-template <class R, bool BATCH = false> __global__ void __launch_bounds__(256, 4) k_shade(Params<R> P, uint32_t cur) {
+template <class R, bool BATCH = false> __global__ void __launch_bounds__(256, BATCH ? 2 : 4) k_shade(Params<R> P, uint32_t cur) {
     uint32_t prefix[NUM_KEYS + 1];
     prefix[0] = 0;
 #pragma unroll
