@@ -133,6 +133,51 @@ def test_substream_batch_equals_single_frames(gpu_context):
                            rng="substreams")
 
 
+def test_substream_aovs_progress_and_cancel(gpu_context):
+    # The AOV pass keeps the reference's per-pixel streams (render_denoising_aovs is its own
+    # render in the reference), so the substream render's albedo and normal planes equal
+    # the reference mode's; the beauty plane is the substream image.  Progress is reported
+    # after every round, and a callback that cancels ends the render with GT_ERR_CANCELLED.
+    scene = scenes.final_scene_ray_scene()
+    cam = scenes.final_scene_camera(64, 8)
+    sub = PathTracer(cam, context=gpu_context, rng="substreams").render_denoising_aovs(scene)
+    ref = PathTracer(cam, context=gpu_context).render_denoising_aovs(scene)
+    np.testing.assert_array_equal(sub.albedo_linear, ref.albedo_linear)
+    np.testing.assert_array_equal(sub.normal_linear, ref.normal_linear)
+    img = PathTracer(cam, context=gpu_context, rng="substreams").render_hdr_image(scene)
+    np.testing.assert_array_equal(sub.beauty_linear, img.pixels)
+    for engine_scene, engine_cam in ((scene, scenes.final_scene_camera(256, 256)),       # wavefront
+                                     (scenes.cornell_scene()[0], scenes.cornell_camera(256, 16, 50))):  # k_substream
+        seen = []
+        pt = PathTracer(engine_cam, context=gpu_context, rng="substreams")
+        img = pt.render_progressive(engine_scene, lambda u: seen.append((u.completed, u.total)))
+        assert seen and all(0 < c <= t for c, t in seen) and seen[-1][0] == seen[-1][1], seen
+        assert np.isfinite(img.pixels).all()
+
+        class Stop(Exception):
+            pass
+
+        def stop(u):
+            raise Stop()
+
+        with pytest.raises(Stop):
+            pt.render_progressive(engine_scene, stop)
+
+
+def test_migrate_modes_keep_f64_images(gpu_context):
+    # Migration is a scheduling choice: on, off and the default give the same f64 image
+    # and accepted counts (Cornell at 64 spp per pixel, so that pixels migrate).
+    scene, lights = scenes.cornell_scene()
+    cam = scenes.cornell_camera(48, 8, 50)
+    imgs = {m: PathTracer(cam, precision="f64", context=gpu_context, migrate=m).render_with_lights_hdr_image(
+        scene, lights, want64=True) for m in ("default", "on", "off")}
+    for m in ("on", "off"):
+        np.testing.assert_array_equal(imgs[m].pixels64, imgs["default"].pixels64)
+        np.testing.assert_array_equal(imgs[m].accepted, imgs["default"].accepted)
+    with pytest.raises(ValueError):
+        PathTracer(cam, migrate="sometimes")
+
+
 def test_substream_unsupported_uses(gpu_context):
     scene, lights = scenes.cornell_scene()
     cam = scenes.cornell_camera(16, 1, 5)
