@@ -190,16 +190,16 @@ def measured_peaks():
 # frame moves.  `roofline.traffic` scales them by the units of the dominant kernel's
 # average launch.
 DRAM_BYTES_PER_UNIT = {
-    "mesh_heavy_perlin_tori_sun": {"trace": 422.5, "shadow": 768.7, "shade": 375.0, "generate": 303.8},
+    "mesh_heavy_perlin_tori_sun": {"trace": 473.0, "shadow": 825.1, "shade": 537.6, "generate": 304.3},
 }
 # Issue ceiling of k_trace on the same workload (one 912-block launch of that frame, all
-# sections): the warp schedulers issue in 42.5% of their active cycles, and on average
-# 9.65 of a warp's 32 lanes execute each instruction (rays of a warp visit different
+# sections): the warp schedulers issue in 41.3% of their active cycles, and on average
+# 9.80 of a warp's 32 lanes execute each instruction (rays of a warp visit different
 # numbers of nodes and triangles).  The traversal kernels are bound by dependent loads and
 # this divergence, not by HBM bandwidth.
 ISSUE_PROFILE = {
-    "mesh_heavy_perlin_tori_sun": {"kernel": "k_trace", "issue_active": 0.425, "lanes_per_instruction": 9.65,
-                                   "warp_stall_long_scoreboard_per_issue": 6.48},
+    "mesh_heavy_perlin_tori_sun": {"kernel": "k_trace", "issue_active": 0.413, "lanes_per_instruction": 9.80,
+                                   "warp_stall_long_scoreboard_per_issue": 6.91},
 }
 
 

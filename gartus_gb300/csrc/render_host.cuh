@@ -1272,7 +1272,9 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     // path-state traffic.
     constexpr uint32_t kSubWaveMinPrims = 64;
     const bool sub_wave = subs && !BATCH && P.sc.num_prims > kSubWaveMinPrims;
-    const uint64_t sub_items = std::max<uint64_t>(sub_wave ? kSubWaveItems : kSubItems, n_pix);
+    // one round's items at most: the cap, or the frame's samples when it has fewer
+    const uint64_t sub_items = std::max<uint64_t>(
+        std::min<uint64_t>(sub_wave ? kSubWaveItems : kSubItems, uint64_t(n_pix) * std::max(limit_max, 1u)), n_pix);
     const bool persistent = !subs && ((!BATCH && opts.schedule == GT_SCHEDULE_PERSISTENT && !accum) || (world && !accum));
     const bool host_out = BATCH || frame->device_buffers == 0;
     // Wavefront stripes: rows are dealt round-robin to K independent wavefronts on their
