@@ -709,7 +709,7 @@ struct HandOff {
 // also intersect small scenes lane-parallel (warp_closest); kept apart so the one-slot-per-
 // lane launches keep their register budget.
 template <class R, bool RESUME, bool BATCH = false, bool WORLD = false, bool COOP = false>
-__global__ void __launch_bounds__(128, sizeof(R) == 8 ? 1 : (WORLD ? 3 : 4)) k_persistent(Params<R> P, uint32_t* next, const uint32_t* queues,
+__global__ void __launch_bounds__(128, sizeof(R) == 8 ? 1 : 4) k_persistent(Params<R> P, uint32_t* next, const uint32_t* queues,
                                                     const uint32_t* class_counts, const volatile uint32_t* cancel,
                                                     volatile uint32_t* progress, float* rgb, double* rgb64,
                                                     uint32_t* accepted, HandOff ho = HandOff()) {
