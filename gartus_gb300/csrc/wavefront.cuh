@@ -1038,7 +1038,7 @@ constexpr uint32_t kSubClaim = 16;
 // lies beyond the pixel's sample limit.  Each loop turn traces one ray per lane: a pending
 // shadow query first, as k_persistent does, then the path's next ray.
 template <class R, bool BATCH>
-__global__ void __launch_bounds__(128, sizeof(R) == 8 ? 1 : 4)
+__global__ void __launch_bounds__(128, sizeof(R) == 8 ? 1 : 5)
     k_substream(Params<R> P, const uint32_t* list, uint32_t count, uint32_t first, uint32_t S, R4<R>* out,
                 unsigned long long* next) {
     const unsigned long long items = (unsigned long long)count * S;
