@@ -1,9 +1,13 @@
 """Throughput benchmark of the GB300 wavefront path tracer (Msamples/s).
 
-Workload (default): the Cornell box of cornell_box_world (raytracing/scenes.rs:226-294)
-with a GGX box and a glass sphere, 600x600, 16x16 stratified samples (256 spp), max depth
-50, the ceiling light sampled through a SamplingTargetList mixture — one step is one full
-frame.  `--config final` runs the reference's final scene (400x225, 32 spp) instead.
+Workload (default): the mesh-heavy frame, 1920x1080 with 8x8 stratified samples (64 spp),
+max depth 8, 2,355,202 triangles (a 1024x1024 Perlin height field and 64 tori) under a
+2048x1024 f32 sky with a sun, sampled by next-event estimation — one step is one full
+frame.  `--config cornell` runs the Cornell box of cornell_box_world
+(raytracing/scenes.rs:226-294) with a GGX box and a glass sphere (600x600, 256 spp, depth
+50), `--config final` the reference's final scene (400x225, 32 spp), `--config batch` 64
+adaptive animation frames, `--config smoke` a world with two media, `--config denoise` the
+denoiser's time to a relMSE; `--rng substreams` the throughput mode.
 
 Arms:
   default          : this library (f32 wavefront) through the C ABI.
