@@ -955,10 +955,25 @@ inline uint32_t sub_round_size(uint32_t count, uint32_t remaining, bool adaptive
     return std::max<uint32_t>(1u, uint32_t(adaptive ? std::min<uint64_t>(r, kSubAdaptiveRound) : r));
 }
 
+// Before a progress call of the throughput mode: the frame as far as its folded samples
+// know it, copied into opts.progress_rgb (single frames).
+template <class R>
+gt_status sub_progress_image(gt_context* ctx, Params<R>& P, float* o_rgb, uint32_t n, const gt_render_opts& opts) {
+    if (!opts.progress_rgb || !o_rgb) return GT_OK;
+    const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1);
+    k_sub_preview<R><<<std::max<uint32_t>(1u, std::min<uint32_t>((n + 255) / 256, sms * 8)), 256, 0, ctx->stream>>>(
+        P, o_rgb);
+    GT_CUDA(cudaGetLastError());
+    GT_CUDA(cudaMemcpyAsync(opts.progress_rgb, o_rgb, size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    GT_CUDA(cudaStreamSynchronize(ctx->stream));
+    return GT_OK;
+}
+
 template <class R, bool BATCH>
 gt_status run_substreams(gt_context* ctx, Params<R>& P, uint32_t* const list[2], R4<R>* out, unsigned long long* next,
-                         uint32_t n, uint32_t limit_max, bool adaptive, const gt_render_opts& opts, EventPool& ev,
-                         double* kms, uint64_t* klaunch, uint64_t& rounds) {
+                         uint32_t n, uint32_t limit_max, bool adaptive, float* o_rgb, const gt_render_opts& opts,
+                         EventPool& ev, double* kms, uint64_t* klaunch, uint64_t& rounds) {
     cudaStream_t st = ctx->stream;
     const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1);
     int per_sm = 0;
@@ -1002,8 +1017,14 @@ gt_status run_substreams(gt_context* ctx, Params<R>& P, uint32_t* const list[2],
         count = ctx->pinned[0];
         ++rounds;
         const uint64_t done = std::min<uint64_t>(uint64_t(first) + round, limit_max);
-        if (opts.progress && call_progress(ctx, opts, done * n, uint64_t(limit_max) * n))
-            return fail(GT_ERR_CANCELLED, "render cancelled by the progress callback");
+        if (opts.progress) {
+            if constexpr (!BATCH) {
+                gt_status prc;
+                if ((prc = sub_progress_image<R>(ctx, P, o_rgb, n, opts)) != GT_OK) return prc;
+            }
+            if (call_progress(ctx, opts, done * n, uint64_t(limit_max) * n))
+                return fail(GT_ERR_CANCELLED, "render cancelled by the progress callback");
+        }
     }
     return GT_OK;
 }
@@ -1019,7 +1040,7 @@ constexpr uint64_t kSubWaveItems = uint64_t(1) << 24; // slots of one round (or 
 template <class R>
 gt_status run_sub_wavefront(gt_context* ctx, Params<R>& P, std::vector<Params<R>>& SW, SubRound<R>* d_sub,
                             uint32_t* const list[2], R4<R>* out, uint32_t cap, uint32_t n, uint32_t limit_max, bool nee,
-                            const gt_render_opts& opts, EventPool& ev, double* kms, uint64_t* klaunch,
+                            float* o_rgb, const gt_render_opts& opts, EventPool& ev, double* kms, uint64_t* klaunch,
                             uint64_t& rounds) {
     cudaStream_t st = ctx->stream;
     const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1), threads = 256;
@@ -1183,8 +1204,12 @@ gt_status run_sub_wavefront(gt_context* ctx, Params<R>& P, std::vector<Params<R>
         GT_CUDA(cudaStreamSynchronize(st));
         count = ctx->pinned[0];
         const uint64_t done = std::min<uint64_t>(uint64_t(first) + round, limit_max);
-        if (opts.progress && call_progress(ctx, opts, done * n, uint64_t(limit_max) * n))
-            return fail(GT_ERR_CANCELLED, "render cancelled by the progress callback");
+        if (opts.progress) {
+            gt_status prc;
+            if ((prc = sub_progress_image<R>(ctx, P, o_rgb, n, opts)) != GT_OK) return prc;
+            if (call_progress(ctx, opts, done * n, uint64_t(limit_max) * n))
+                return fail(GT_ERR_CANCELLED, "render cancelled by the progress callback");
+        }
     }
     // the stripes' stack-overflow flags
     for (uint32_t k = 0; k < K; ++k)
@@ -1428,10 +1453,10 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         uint64_t rounds = 0;
         if (sub_wave)
             rc = run_sub_wavefront<R>(ctx, P, SW, d_sub, sub_list, sub_out, uint32_t(sub_items), n, limit_max, nee,
-                                      opts, ev, kms, klaunch, rounds);
+                                      o_rgb, opts, ev, kms, klaunch, rounds);
         else
-            rc = run_substreams<R, BATCH>(ctx, P, sub_list, sub_out, sub_next, n, limit_max, any_adaptive, opts, ev,
-                                          kms, klaunch, rounds);
+            rc = run_substreams<R, BATCH>(ctx, P, sub_list, sub_out, sub_next, n, limit_max, any_adaptive, o_rgb,
+                                          opts, ev, kms, klaunch, rounds);
         if (rc != GT_OK) return rc;
         k_resolve<R, BATCH><<<slot_blocks, threads, 0, st>>>(P, o_rgb, o_rgb64, o_acc);
         GT_CUDA(cudaGetLastError());

@@ -1179,6 +1179,17 @@ __global__ void __launch_bounds__(256) k_sub_fold(Params<R> P, const uint32_t* l
     }
 }
 
+// Progress image of the throughput mode (one frame): every pixel's estimate from the
+// samples folded so far.
+template <class R> __global__ void __launch_bounds__(256) k_sub_preview(Params<R> P, float* rgb) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.ps.n; i += gridDim.x * blockDim.x) {
+        const V3<R> c = pixel_estimate(P.cam, P.ps.acc[i], P.ps.accepted[i]);
+        rgb[size_t(i) * 3 + 0] = float(c.x);
+        rgb[size_t(i) * 3 + 1] = float(c.y);
+        rgb[size_t(i) * 3 + 2] = float(c.z);
+    }
+}
+
 // Round set-up of the throughput mode on the wavefront: slot i gets its sample's own
 // stream, or is done at once (w = 0 in out) when the sample lies beyond the pixel's limit.
 template <class R> __global__ void __launch_bounds__(256) k_sub_init(Params<R> P) {

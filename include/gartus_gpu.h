@@ -377,7 +377,8 @@ typedef struct gt_render_opts {
      * writes the image as far as it is known: finished pixels hold their final value, the
      * others 0 (the partially filled `pixels` of ProgressiveRenderUpdate,
      * camera.rs:3172-3270).  Pixels still being written by a running persistent launch
-     * may show a partial value. */
+     * may show a partial value; in the substream mode (rng) every pixel holds the estimate of
+     * the samples folded so far. */
     float* progress_rgb;
     /* Wavefront launch shapes, in resident 256-thread blocks per SM (0 = the library's
      * choice: 8 for the generate kernel, 6 for trace, shade and shadow); gt_autotune

@@ -137,7 +137,8 @@ def test_substream_aovs_progress_and_cancel(gpu_context):
     # The AOV pass keeps the reference's per-pixel streams (render_denoising_aovs is its own
     # render in the reference), so the substream render's albedo and normal planes equal
     # the reference mode's; the beauty plane is the substream image.  Progress is reported
-    # after every round, and a callback that cancels ends the render with GT_ERR_CANCELLED.
+    # after every round with the image of the samples folded so far, and a callback that
+    # cancels ends the render with GT_ERR_CANCELLED.
     scene = scenes.final_scene_ray_scene()
     cam = scenes.final_scene_camera(64, 8)
     sub = PathTracer(cam, context=gpu_context, rng="substreams").render_denoising_aovs(scene)
@@ -148,11 +149,14 @@ def test_substream_aovs_progress_and_cancel(gpu_context):
     np.testing.assert_array_equal(sub.beauty_linear, img.pixels)
     for engine_scene, engine_cam in ((scene, scenes.final_scene_camera(256, 256)),       # wavefront
                                      (scenes.cornell_scene()[0], scenes.cornell_camera(256, 16, 50))):  # k_substream
-        seen = []
+        seen, last = [], []
         pt = PathTracer(engine_cam, context=gpu_context, rng="substreams")
-        img = pt.render_progressive(engine_scene, lambda u: seen.append((u.completed, u.total)))
+        img = pt.render_progressive(engine_scene,
+                                    lambda u: (seen.append((u.completed, u.total)), last.append(u.pixels.copy())))
         assert seen and all(0 < c <= t for c, t in seen) and seen[-1][0] == seen[-1][1], seen
         assert np.isfinite(img.pixels).all()
+        # the last progress image is the frame from every folded sample: the result
+        np.testing.assert_array_equal(last[-1], img.pixels)
 
         class Stop(Exception):
             pass
