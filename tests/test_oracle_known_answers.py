@@ -439,3 +439,29 @@ def test_henyey_greenstein_samples_mean_cosine_near_anisotropy():  # gmath/sampl
         assert abs(math.sqrt(sum(x * x for x in d)) - 1.0) <= 1e-12
         total += d[2]
     assert abs(total / n - g) <= 0.035
+
+
+def test_decision_trace_adaptive_stop_and_substreams():
+    # The decision trace records each adaptive stop test (type 14: outcome 1 = stop, value
+    # (error - threshold) / threshold); the pixel's accepted samples end at the first stop.
+    # With per-sample substreams the same pixel takes other decisions (its own streams).
+    scene, lights = scenes.batch_scene()
+    cam = scenes.batch_cameras(frames=3, width=24, spp_cycle=(4,), max_samples=64, threshold=0.05)[1]
+    o = oracle.OracleScene.from_ray_scene(scene)
+    la = lights.to_array()
+    rgb, acc = o.render(cam.desc(), la, None, precision=1, threads=4)
+    y, x = 12, 12
+    types, outcomes, values = o.pixel_trace(cam.desc(), x, y, la, None, precision=1)
+    adaptive = np.flatnonzero(types == 14)
+    assert adaptive.size > 0
+    stops = np.flatnonzero((types == 14) & (outcomes == 1))
+    # every test before the stop continued, with the error above the threshold
+    assert np.all(values[adaptive[outcomes[adaptive] == 0]] >= 0)
+    if stops.size:
+        assert stops[0] == adaptive[-1] and values[stops[0]] < 0
+    samples = np.count_nonzero((types == 1) & (outcomes == 1))
+    assert samples == acc[y, x]
+    t_sub = o.pixel_trace(cam.desc(), x, y, la, None, precision=1, rng="substreams")
+    assert not (len(t_sub[0]) == len(types) and np.array_equal(t_sub[1], outcomes) and np.array_equal(t_sub[2], values))
+    sub, _ = o.render(cam.desc(), la, None, precision=1, threads=4, rng="substreams")
+    assert sub.shape == rgb.shape and not np.array_equal(sub, rgb)
