@@ -1583,8 +1583,12 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             }
             if (q == 0) k_generate<R, BATCH><<<lblocks, threads, 0, s>>>(SP[k], cur);
             else if (q == 1) k_trace<R><<<wblocks, threads, 0, s>>>(SP[k], cur);
-            else if (q == 2) k_shade<R, BATCH><<<wblocks, threads, 0, s>>>(SP[k], cur);
-            else k_shadow<R><<<wblocks, threads, 0, s>>>(SP[k]);
+            // shade and shadow grids at most their resident blocks (one wave)
+            else if (q == 2)
+                k_shade<R, BATCH><<<std::min<uint32_t>(wblocks, uint32_t(sms) * kShadeBlocksPerSm), threads, 0, s>>>(
+                    SP[k], cur);
+            else
+                k_shadow<R><<<std::min<uint32_t>(wblocks, uint32_t(sms) * kShadowBlocksPerSm), threads, 0, s>>>(SP[k]);
             if (timed) {
                 cudaEventRecord(z, s);
                 ev.note(q == 0 ? GT_KERNEL_GENERATE : q == 1 ? GT_KERNEL_TRACE : q == 2 ? GT_KERNEL_SHADE : GT_KERNEL_SHADOW,

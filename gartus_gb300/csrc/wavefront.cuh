@@ -241,7 +241,12 @@ template <class R> __global__ void k_iteration_reset(Params<R> P, uint32_t cur) 
     if (threadIdx.x == 0) P.ps.counters[C_SHADOW] = 0;
 }
 
-template <class R> __global__ void __launch_bounds__(256, 6) k_trace(Params<R> P, uint32_t cur) {
+// Resident 256-thread blocks per SM of the f32 traversal and shade kernels (their launch
+// bounds): more than the registers alone would allow, spilling into L1, because the
+// stripes' launches then share the SMs better (mesh-heavy frame 297 -> 332 Msamples/s).
+constexpr uint32_t kTraceBlocksPerSm = 6, kShadowBlocksPerSm = 5, kShadeBlocksPerSm = 4;
+
+template <class R> __global__ void __launch_bounds__(256, kTraceBlocksPerSm) k_trace(Params<R> P, uint32_t cur) {
     const uint32_t count = *reinterpret_cast<volatile uint32_t*>(&P.ps.counters[C_TRACE0 + cur]);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&P.ps.totals[0], (unsigned long long)count);
     const uint32_t* q = P.ps.q_trace[cur];
@@ -500,7 +505,8 @@ GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uint32_t key, bool& sh
     return cont;
 }
 
-template <class R, bool BATCH = false> __global__ void __launch_bounds__(256, BATCH ? 2 : 4) k_shade(Params<R> P, uint32_t cur) {
+template <class R, bool BATCH = false>
+__global__ void __launch_bounds__(256, BATCH ? 2u : kShadeBlocksPerSm) k_shade(Params<R> P, uint32_t cur) {
     uint32_t prefix[NUM_KEYS + 1];
     prefix[0] = 0;
 #pragma unroll
@@ -528,7 +534,7 @@ template <class R, bool BATCH = false> __global__ void __launch_bounds__(256, BA
     }
 }
 
-template <class R> __global__ void __launch_bounds__(256, 5) k_shadow(Params<R> P) {
+template <class R> __global__ void __launch_bounds__(256, kShadowBlocksPerSm) k_shadow(Params<R> P) {
     const uint32_t count = *reinterpret_cast<volatile uint32_t*>(&P.ps.counters[C_SHADOW]);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&P.ps.totals[1], (unsigned long long)count);
     const R inf = Num<R>::inf();
