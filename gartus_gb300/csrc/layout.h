@@ -209,7 +209,8 @@ template <class R> struct PathState {
     R4<R>* col;     // sample radiance xyz
     uint4* st;      // rng lo, rng hi, flags, samples started
     R* hit_t;       // closest-hit distance
-    int32_t* hit_prim; // leaf-order primitive slot or -1
+    int32_t* hit_prim; // leaf-order primitive slot or -1 (an object hit: the mesh's leaf)
+    int32_t* hit_obj;  // leaf-order object hit or -1 (worlds with objects; else null)
     R4<R>* acc;     // running sum (or Welford mean)
     R4<R>* comp;    // Kahan compensation (or Welford M2)
     uint32_t* accepted;

@@ -708,7 +708,7 @@ struct Bump {
 };
 
 // Per-slot path state, shared by every stripe (slot = pixel index).
-template <class R> void layout_slots(Bump& b, PathState<R>& ps, uint32_t n, bool nee) {
+template <class R> void layout_slots(Bump& b, PathState<R>& ps, uint32_t n, bool nee, bool objects = false) {
     ps.n = n;
     ps.ray_o = b.take<R4<R>>(n);
     ps.ray_d = b.take<R4<R>>(n);
@@ -717,6 +717,7 @@ template <class R> void layout_slots(Bump& b, PathState<R>& ps, uint32_t n, bool
     ps.st = b.take<uint4>(n);
     ps.hit_t = b.take<R>(n);
     ps.hit_prim = b.take<int32_t>(n);
+    ps.hit_obj = objects ? b.take<int32_t>(n) : nullptr;
     ps.acc = b.take<R4<R>>(n);
     ps.comp = b.take<R4<R>>(n);
     ps.accepted = b.take<uint32_t>(n);
@@ -1280,10 +1281,15 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
 
     // Workspace: path state (wavefront only), per-stripe queues and counters, and device
     // staging for host outputs.
-    // A world with objects or media renders on the persistent schedule, whose WORLD variant
-    // traces shadow queries in the reference's order of draws (accumulation resumes
-    // wavefront state, which that variant does not keep).
+    // A world with media renders on the persistent schedule, whose WORLD variant traces
+    // shadow queries in the reference's order of draws (a medium's hit draws from the
+    // pixel's stream); accumulation resumes wavefront state in that variant's RESUME mode.
+    // A world with objects and no media draws nothing in its hits, so it renders on the
+    // wavefront (OBJ kernels: the rays also test the objects), and its tail in the world
+    // variant.
     const bool world = P.sc.num_media != 0 || P.sc.num_objects != 0;
+    const bool media = P.sc.num_media != 0;
+    const bool obj_wave = world && !media && !BATCH;
     if (world && BATCH) return fail(GT_ERR_UNSUPPORTED, "a scene with objects or media does not render as a wavefront batch");
     // Throughput mode: every (pixel, sample) pair of a round is a work item.
     const bool subs = opts.rng == GT_RNG_SUBSTREAMS;
@@ -1300,14 +1306,14 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     // one round's items at most: the cap, or the frame's samples when it has fewer
     const uint64_t sub_items = std::max<uint64_t>(
         std::min<uint64_t>(sub_wave ? kSubWaveItems : kSubItems, uint64_t(n_pix) * std::max(limit_max, 1u)), n_pix);
-    const bool persistent = !subs && ((!BATCH && opts.schedule == GT_SCHEDULE_PERSISTENT && !accum) || (world && !accum));
+    const bool persistent = !subs && ((!BATCH && opts.schedule == GT_SCHEDULE_PERSISTENT && !accum) || (media && !accum));
     const bool host_out = BATCH || frame->device_buffers == 0;
     // Wavefront stripes: rows are dealt round-robin to K independent wavefronts on their
     // own streams, whose kernels then overlap on the GPU (each kernel alone leaves SMs
     // waiting on memory).
     uint32_t K = opts.stripes ? opts.stripes : 4u;
     K = std::max<uint32_t>(1u, std::min<uint32_t>({K, uint32_t(gt_context::kMaxStripes), img_h}));
-    if (persistent || world || subs) K = 1;
+    if (persistent || media || subs) K = 1;
     const uint32_t qcap = ((img_h + K - 1) / K) * cam.width;
     std::vector<Params<R>> SP(K);
     CamDev<R>* d_cams = nullptr;
@@ -1355,7 +1361,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             P.ps.totals = bb.take<unsigned long long>(8);
             P.ps.q_mat = bb.take<uint32_t>(size_t(n) * NUM_COST_CLASSES); // cost-ordered pixel queues
         } else {
-            layout_slots<R>(bb, P.ps, n, nee);
+            layout_slots<R>(bb, P.ps, n, nee, obj_wave);
             for (uint32_t k = 0; k < K; ++k) {
                 SP[k] = P;
                 layout_queues<R>(bb, SP[k].ps, qcap, nee);
@@ -1484,8 +1490,8 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     }
 
     if constexpr (!BATCH) {
-        if (world) { // accumulated world with objects or media: every pixel's chain continues from
-                     // the state just loaded in the RESUME mode of the persistent kernel's world variant
+        if (media) { // accumulated world with media: every pixel's chain continues from the
+                     // state just loaded in the RESUME mode of the persistent kernel's world variant
             Params<R> Q = SP[0];
             uint32_t* list = Q.ps.q_handoff; // n entries: one stripe
             uint32_t* count = Q.ps.counters + C_TAIL;
@@ -1555,8 +1561,9 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     constexpr uint64_t kMigrateAfter = 60;
     constexpr float kMigrateRatio = 2.0f;
     constexpr uint32_t kMigrateMaxPrims = 65536;
+    // (not in a world with objects: the side kernel is the plain persistent variant)
     const bool may_migrate =
-        opts.schedule == GT_SCHEDULE_AUTO &&
+        opts.schedule == GT_SCHEDULE_AUTO && !obj_wave &&
         (opts.migrate == GT_MIGRATE_ON || (opts.migrate == GT_MIGRATE_DEFAULT && P.sc.num_prims <= kMigrateMaxPrims));
     ctx->mapped[0] = 0; // the side kernels' cancel word
 
@@ -1581,14 +1588,19 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
                 if (e != cudaSuccess) return e;
                 cudaEventRecord(a, s);
             }
-            if (q == 0) k_generate<R, BATCH><<<lblocks, threads, 0, s>>>(SP[k], cur);
-            else if (q == 1) k_trace<R><<<wblocks, threads, 0, s>>>(SP[k], cur);
             // shade and shadow grids at most their resident blocks (one wave)
-            else if (q == 2)
-                k_shade<R, BATCH><<<std::min<uint32_t>(wblocks, uint32_t(sms) * kShadeBlocksPerSm), threads, 0, s>>>(
-                    SP[k], cur);
-            else
-                k_shadow<R><<<std::min<uint32_t>(wblocks, uint32_t(sms) * kShadowBlocksPerSm), threads, 0, s>>>(SP[k]);
+            const uint32_t shade_blocks = std::min<uint32_t>(wblocks, uint32_t(sms) * kShadeBlocksPerSm);
+            const uint32_t shadow_blocks = std::min<uint32_t>(wblocks, uint32_t(sms) * kShadowBlocksPerSm);
+            if (q == 0) k_generate<R, BATCH><<<lblocks, threads, 0, s>>>(SP[k], cur);
+            else if (obj_wave) {
+                if constexpr (!BATCH) {
+                    if (q == 1) k_trace<R, true><<<wblocks, threads, 0, s>>>(SP[k], cur);
+                    else if (q == 2) k_shade<R, false, true><<<shade_blocks, threads, 0, s>>>(SP[k], cur);
+                    else k_shadow<R, true><<<shadow_blocks, threads, 0, s>>>(SP[k]);
+                }
+            } else if (q == 1) k_trace<R><<<wblocks, threads, 0, s>>>(SP[k], cur);
+            else if (q == 2) k_shade<R, BATCH><<<shade_blocks, threads, 0, s>>>(SP[k], cur);
+            else k_shadow<R><<<shadow_blocks, threads, 0, s>>>(SP[k]);
             if (timed) {
                 cudaEventRecord(z, s);
                 ev.note(q == 0 ? GT_KERNEL_GENERATE : q == 1 ? GT_KERNEL_TRACE : q == 2 ? GT_KERNEL_SHADE : GT_KERNEL_SHADOW,
@@ -1694,6 +1706,21 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         GT_CUDA(cudaMemsetAsync(Q.ps.counters + C_TAIL_DONE, 0, 3 * sizeof(uint32_t), s));
         GT_CUDA(cudaMemsetAsync(d_next + k, 0, sizeof(uint32_t), s));
         k_collect<R><<<lblocks, threads, 0, s>>>(Q, list, count);
+        if constexpr (!BATCH) {
+            if (obj_wave) { // the world variant, one slot per lane to the end
+                k_persistent<R, true, false, true><<<tblocks, 128, 0, s>>>(Q, d_next + k, list, count, nullptr, nullptr,
+                                                                           nullptr, nullptr, nullptr);
+                GT_CUDA(cudaGetLastError());
+                klaunch[GT_KERNEL_OTHER] += 1;
+                klaunch[GT_KERNEL_PERSISTENT] += 1;
+                if (profile) {
+                    GT_CUDA(cudaEventRecord(z, s));
+                    ev.note(GT_KERNEL_PERSISTENT, a, z);
+                }
+                S[k].tail = true;
+                return GT_OK;
+            }
+        }
         HandOff ho;
         ho.done = Q.ps.counters + C_TAIL_DONE;
         ho.below = coop_blocks * 4u;

@@ -246,7 +246,12 @@ template <class R> __global__ void k_iteration_reset(Params<R> P, uint32_t cur) 
 // stripes' launches then share the SMs better (mesh-heavy frame 297 -> 332 Msamples/s).
 constexpr uint32_t kTraceBlocksPerSm = 6, kShadowBlocksPerSm = 5, kShadeBlocksPerSm = 4;
 
-template <class R> __global__ void __launch_bounds__(256, kTraceBlocksPerSm) k_trace(Params<R> P, uint32_t cur) {
+// OBJ: a world with objects and no media (whose hits draw no random numbers, so the
+// deferred shadow queries keep the reference's order of draws): after the RayScene's tree
+// the ray tests the objects (objects_hit, as world_hit does), and an object hit stores the
+// object in hit_obj and the mesh's leaf in hit_prim.
+template <class R, bool OBJ = false>
+__global__ void __launch_bounds__(256, kTraceBlocksPerSm) k_trace(Params<R> P, uint32_t cur) {
     const uint32_t count = *reinterpret_cast<volatile uint32_t*>(&P.ps.counters[C_TRACE0 + cur]);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&P.ps.totals[0], (unsigned long long)count);
     const uint32_t* q = P.ps.q_trace[cur];
@@ -263,9 +268,20 @@ template <class R> __global__ void __launch_bounds__(256, kTraceBlocksPerSm) k_t
             R t = R(0);
             int prim = traverse<R, false, false>(P.sc, xyz(o), xyz(d), o.w, R(kShadowAcne), inf, t, nullptr,
                                                  &P.ps.counters[C_ERROR]);
+            uint32_t mat = prim < 0 ? 0u : __ldg(&P.sc.meta[prim].x) >> 3;
+            if constexpr (OBJ) {
+                if (prim < 0) t = inf;
+                int obj = -1, leaf = -1;
+                objects_hit(P.sc, xyz(o), xyz(d), o.w, R(kShadowAcne), t, obj, leaf, &P.ps.counters[C_ERROR]);
+                if (obj >= 0) {
+                    prim = leaf;
+                    mat = __ldg(&P.sc.meshes[P.sc.objects[obj].mesh].view.meta[leaf].x) >> 3;
+                }
+                P.ps.hit_obj[slot] = obj;
+            }
             P.ps.hit_t[slot] = t;
             P.ps.hit_prim[slot] = prim;
-            key = prim < 0 ? KEY_MISS : uint32_t(P.sc.mats[__ldg(&P.sc.meta[prim].x) >> 3].kind);
+            key = prim < 0 ? KEY_MISS : uint32_t(P.sc.mats[mat].kind);
         }
         warp_push_keyed(valid, key, slot, P.ps.q_mat, P.ps.qcap, &P.ps.counters[C_MAT]);
     }
@@ -306,10 +322,13 @@ template <class R> struct Shadow {
 };
 
 // Resolves shadow query k (after traversal) into the sample's radiance.
-template <class R> GT_DEV void apply_shadow(const Params<R>& P, V3<R>& col, const Shadow<R>& sh, int k, int prim, R t) {
+// `wh`: the hit record of an object hit (closest-hit query of a world with objects).
+template <class R>
+GT_DEV void apply_shadow(const Params<R>& P, V3<R>& col, const Shadow<R>& sh, int k, int prim, R t,
+                         const HitRec<R>* wh = nullptr) {
     if (k == 0) { // closest hit; the emission of whatever is hit (camera.rs:2248-2261)
         if (prim < 0) return;
-        HitRec<R> h = make_hit(P.sc, uint32_t(prim), sh.o, sh.dir[0], sh.time, t);
+        HitRec<R> h = wh ? *wh : make_hit(P.sc, uint32_t(prim), sh.o, sh.dir[0], sh.time, t);
         V3<R> e = mat_emitted(P.sc.mats[h.mat], h);
         if (!finite3(e)) return;
         V3<R> direct = cmul(sh.s[0], e) * sh.ratio[0];
@@ -347,7 +366,9 @@ template <class R> GT_DEV void shadow_now(const Params<R>& P, V3<R>& col, Shadow
 // WORLD: a world with objects or media; the hit record comes from world_hit (`wh`, prim 0
 // for a hit, -1 for a miss) and the shadow queries are traced here, in the reference's
 // order of draws, instead of being left in `sh`.
-template <class R, bool WORLD = false>
+// OBJ: the wavefront's world with objects; a non-null `wh` is an object hit's record,
+// and the shadow queries are left in `sh` as usual.
+template <class R, bool WORLD = false, bool OBJ = false>
 GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& p, int prim, R t, Rng& g,
                              Shadow<R>& sh, const HitRec<R>* wh = nullptr) {
     sh.valid[0] = sh.valid[1] = false;
@@ -359,7 +380,7 @@ GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& 
         p.col = p.col + cmul(p.att, miss);
         return false;
     }
-    const HitRec<R> h = WORLD ? *wh : make_hit(P.sc, uint32_t(prim), p.o, p.d, p.time, t);
+    const HitRec<R> h = WORLD || (OBJ && wh) ? *wh : make_hit(P.sc, uint32_t(prim), p.o, p.d, p.time, t);
     const MatDev<R> m = P.sc.mats[h.mat];
     if (p.allow_emit) p.col = p.col + cmul(p.att, mat_emitted(m, h));
     ScatterRec<R> s = mat_scatter(m, p.d, h, g);
@@ -453,7 +474,7 @@ GT_DEV bool integrate_bounce(const Params<R>& P, const CamDev<R>& cam, Path<R>& 
 }
 
 // Wavefront shade step for `slot`: one bounce, pending shadow queries stored for k_shadow.
-template <class R, bool BATCH>
+template <class R, bool BATCH, bool OBJ = false>
 GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uint32_t key, bool& shadow, bool& done) {
     uint4 st = P.ps.st[slot];
     Rng g{uint64_t(st.x) | (uint64_t(st.y) << 32)};
@@ -470,9 +491,18 @@ GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uint32_t key, bool& sh
     p.allow_emit = (flags & F_ALLOW_EMIT) != 0;
     Shadow<R> sh;
     const int prim = key == KEY_MISS ? -1 : P.ps.hit_prim[slot];
+    const R t = key == KEY_MISS ? R(0) : P.ps.hit_t[slot];
     uint32_t local;
-    const bool cont =
-        integrate_bounce(P, cam_of<R, BATCH>(P, slot, local), p, prim, key == KEY_MISS ? R(0) : P.ps.hit_t[slot], g, sh);
+    HitRec<R> oh;
+    const HitRec<R>* ohp = nullptr;
+    if constexpr (OBJ) {
+        const int obj = key == KEY_MISS ? -1 : P.ps.hit_obj[slot];
+        if (obj >= 0) {
+            oh = make_mesh_hit(P.sc, obj, prim, p.o, p.d, p.time, t);
+            ohp = &oh;
+        }
+    }
+    const bool cont = integrate_bounce<R, false, OBJ>(P, cam_of<R, BATCH>(P, slot, local), p, prim, t, g, sh, ohp);
     uint32_t sh_bits = 0;
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
@@ -505,7 +535,7 @@ GT_DEV bool shade_slot(const Params<R>& P, uint32_t slot, uint32_t key, bool& sh
     return cont;
 }
 
-template <class R, bool BATCH = false>
+template <class R, bool BATCH = false, bool OBJ = false>
 __global__ void __launch_bounds__(256, BATCH ? 2u : kShadeBlocksPerSm) k_shade(Params<R> P, uint32_t cur) {
     uint32_t prefix[NUM_KEYS + 1];
     prefix[0] = 0;
@@ -525,7 +555,7 @@ __global__ void __launch_bounds__(256, BATCH ? 2u : kShadeBlocksPerSm) k_shade(P
             for (uint32_t k = 1; k < NUM_KEYS; ++k)
                 if (i >= prefix[k]) key = k;
             slot = P.ps.q_mat[size_t(key) * P.ps.qcap + (i - prefix[key])];
-            cont = shade_slot<R, BATCH>(P, slot, key, shadow, done);
+            cont = shade_slot<R, BATCH, OBJ>(P, slot, key, shadow, done);
         }
         warp_push(cont, slot, P.ps.q_trace[cur ^ 1u], &P.ps.counters[C_TRACE0 + (cur ^ 1u)]);
         warp_push(shadow, slot, P.ps.q_shadow, &P.ps.counters[C_SHADOW]);
@@ -534,7 +564,10 @@ __global__ void __launch_bounds__(256, BATCH ? 2u : kShadeBlocksPerSm) k_shade(P
     }
 }
 
-template <class R> __global__ void __launch_bounds__(256, kShadowBlocksPerSm) k_shadow(Params<R> P) {
+// OBJ: a world with objects: the closest-hit query (k = 0) also tests the objects below
+// the RayScene's hit, the occlusion query (k = 1) the objects when the RayScene is clear.
+template <class R, bool OBJ = false>
+__global__ void __launch_bounds__(256, kShadowBlocksPerSm) k_shadow(Params<R> P) {
     const uint32_t count = *reinterpret_cast<volatile uint32_t*>(&P.ps.counters[C_SHADOW]);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&P.ps.totals[1], (unsigned long long)count);
     const R inf = Num<R>::inf();
@@ -559,6 +592,23 @@ template <class R> __global__ void __launch_bounds__(256, kShadowBlocksPerSm) k_
                                                           nullptr, &P.ps.counters[C_ERROR])
                               : traverse<R, false, true>(P.sc, sh.o, sh.dir[k], sh.time, R(kShadowAcne), inf, t,
                                                          nullptr, &P.ps.counters[C_ERROR]);
+            if constexpr (OBJ) {
+                int obj = -1, leaf = -1;
+                if (k == 0) {
+                    if (prim < 0) t = inf;
+                    objects_hit(P.sc, sh.o, sh.dir[k], sh.time, R(kShadowAcne), t, obj, leaf, &P.ps.counters[C_ERROR]);
+                    if (obj >= 0) {
+                        const HitRec<R> oh = make_mesh_hit(P.sc, obj, leaf, sh.o, sh.dir[k], sh.time, t);
+                        apply_shadow(P, col, sh, k, leaf, t, &oh);
+                        continue;
+                    }
+                } else if (prim < 0) {
+                    R to = inf;
+                    if (objects_hit(P.sc, sh.o, sh.dir[k], sh.time, R(kShadowAcne), to, obj, leaf,
+                                    &P.ps.counters[C_ERROR]))
+                        prim = leaf;
+                }
+            }
             apply_shadow(P, col, sh, k, prim, t);
         }
         P.ps.col[slot] = R4<R>{col.x, col.y, col.z, R(0)};

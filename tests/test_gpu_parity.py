@@ -978,18 +978,21 @@ def _mesh_world():
     return scene, lights
 
 
+@pytest.mark.parametrize("schedule", ["wavefront", "persistent"])
 @pytest.mark.parametrize("precision", ["f64", "f32"])
 @pytest.mark.parametrize("mode", ["mixture", "nee"])
-def test_meshes_and_instances(gpu_context, precision, mode):
+def test_meshes_and_instances(gpu_context, precision, mode, schedule):
     # TriangleMesh with texture coordinates, vertex normals and normal maps (mesh.rs:56-141,
     # material.rs:1663-1684) and MatrixInstance (instance.rs:205-317) placing meshes and a
-    # sphere, after the RayScene's surfaces: the f64 image matches the oracle's.
+    # sphere, after the RayScene's surfaces: the f64 image matches the oracle's, on the
+    # wavefront (whose kernels test the objects after the RayScene) and in the persistent
+    # kernel's world variant.
     scene, lights = _mesh_world()
     cam = (RayCamera(48, 1.5).with_samples_per_pixel(4).with_max_depth(8)
            .with_look_at((0.0, 1.0, 2.0), (0.0, 0.0, -3.0)).with_background((0.1, 0.1, 0.12)))
     if mode == "nee":
         cam = cam.with_direct_lighting_mode(abi.GT_DIRECT_NEXT_EVENT_ESTIMATION)
-    pt = PathTracer(cam, precision=precision, context=gpu_context)
+    pt = PathTracer(cam, precision=precision, context=gpu_context, schedule=schedule)
     ref, acc = _oracle_render(scene, cam, lights)
     if precision == "f64":
         img = pt.render_with_lights_hdr_image(scene, lights, want64=True)
@@ -999,10 +1002,46 @@ def test_meshes_and_instances(gpu_context, precision, mode):
     else:
         img = pt.render_with_lights_hdr_image(scene, lights)
         ref32, _ = _oracle_render(scene, cam, lights, precision=0)
-        assert_explained(f"meshes {mode}", scene, cam, img.pixels, ref, ref32, lights)
+        assert_explained(f"meshes {mode} {schedule}", scene, cam, img.pixels, ref, ref32, lights)
     st = pt.last_stats
-    assert st["persistent_rays"] == st["rays"] + st["shadow_rays"]
+    assert st["persistent_rays"] == (st["rays"] + st["shadow_rays"] if schedule == "persistent" else 0)
+    assert (st["shadow_rays"] > 0) == (mode == "nee")
     assert np.std(ref) > 1e-3
+
+
+@pytest.mark.parametrize("mode", ["mixture", "nee"])
+def test_object_world_schedules_agree(gpu_context, mode):
+    # A world with objects and no media: the wavefront (one or three stripes), the automatic
+    # schedule (the wavefront, then its last slots in the world variant of the persistent
+    # kernel) and the persistent kernel evaluate the same arithmetic in the same order, so
+    # the f64 images and the ray counts are identical; 2 + 2 accumulated samples (which run
+    # on the wavefront too) give the 4-sample render.
+    from gartus_gb300.raytracing import Accumulator
+    scene, lights = _mesh_world()
+    cam = (RayCamera(64, 1.5).with_samples_per_pixel(4).with_max_depth(8)
+           .with_look_at((0.0, 1.0, 2.0), (0.0, 0.0, -3.0)).with_background((0.1, 0.1, 0.12)))
+    if mode == "nee":
+        cam = cam.with_direct_lighting_mode(abi.GT_DIRECT_NEXT_EVENT_ESTIMATION)
+    runs = {}
+    for name, kw in (("persistent", dict(schedule="persistent")), ("wavefront", dict(schedule="wavefront")),
+                     ("stripes", dict(schedule="wavefront", stripes=3)), ("auto", dict(tail_slots=1000))):
+        pt = PathTracer(cam, precision="f64", context=gpu_context, **kw)
+        runs[name] = (pt.render_with_lights_hdr_image(scene, lights, want64=True), dict(pt.last_stats))
+    img0, st0 = runs["persistent"]
+    for name in ("wavefront", "stripes", "auto"):
+        img, st = runs[name]
+        np.testing.assert_array_equal(img.pixels64, img0.pixels64)
+        np.testing.assert_array_equal(img.accepted, img0.accepted)
+        for key in ("samples", "rays", "shadow_rays"):
+            assert st[key] == st0[key], (name, key, st[key], st0[key])
+    assert runs["wavefront"][1]["persistent_rays"] == 0
+    assert 0 < runs["auto"][1]["persistent_rays"] < runs["auto"][1]["rays"] + runs["auto"][1]["shadow_rays"]
+    acc = Accumulator(64, 42, "f64", gpu_context)
+    pt = PathTracer(cam.with_samples_per_pixel(2), precision="f64", context=gpu_context)
+    pt.render_accumulate(scene, acc, 2, lights=lights)
+    two = pt.render_accumulate(scene, acc, 2, lights=lights)
+    np.testing.assert_array_equal(two.pixels64, img0.pixels64)
+    np.testing.assert_array_equal(two.accepted, img0.accepted)
 
 
 def test_meshes_aovs_batch_and_primary(gpu_context):
