@@ -349,7 +349,10 @@ typedef struct gt_render_stats {
     uint64_t persistent_rays; /* closest-hit + shadow queries traced inside k_persistent launches           */
 } gt_render_stats;
 
-/* How the frame is scheduled on the GPU.  All give identical images. */
+/* How the frame is scheduled on the GPU.  All give identical images.  A scene with media
+ * (gt_scene_desc.media) always runs the persistent kernel, whose hits draw the media's
+ * random numbers in the reference's order; a scene with objects and no media runs every
+ * schedule. */
 typedef enum gt_schedule {
     GT_SCHEDULE_AUTO = 0,       /* wavefront until few pixels are left, then the persistent kernel
                                    finishes them (gt_render_opts.tail_slots)                      */
