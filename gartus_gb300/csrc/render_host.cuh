@@ -1041,8 +1041,8 @@ constexpr uint64_t kSubWaveItems = uint64_t(1) << 24; // slots of one round (or 
 template <class R>
 gt_status run_sub_wavefront(gt_context* ctx, Params<R>& P, std::vector<Params<R>>& SW, SubRound<R>* d_sub,
                             uint32_t* const list[2], R4<R>* out, uint32_t cap, uint32_t n, uint32_t limit_max, bool nee,
-                            float* o_rgb, const gt_render_opts& opts, EventPool& ev, double* kms, uint64_t* klaunch,
-                            uint64_t& rounds) {
+                            bool objects, float* o_rgb, const gt_render_opts& opts, EventPool& ev, double* kms,
+                            uint64_t* klaunch, uint64_t& rounds) {
     cudaStream_t st = ctx->stream;
     const uint32_t sms = uint32_t(ctx->num_sms > 0 ? ctx->num_sms : 1), threads = 256;
     const uint32_t gen_per_sm = opts.generate_blocks_per_sm ? std::min<uint32_t>(opts.generate_blocks_per_sm, 32u) : 8u;
@@ -1098,14 +1098,27 @@ gt_status run_sub_wavefront(gt_context* ctx, Params<R>& P, std::vector<Params<R>
         // parameters and launch sizes stay the same (rounds of one size, renders of one frame).
         // Without next-event queries k_shade writes each finished sample out, so after the
         // first iteration only k_generate's counter resets are needed.
+        // trace (1), shade (2) or shadow (3) of stripe k; a world with objects runs the
+        // kernels' OBJ instantiations
+        auto launch_kind = [&](int kind, uint32_t k, uint32_t qq) {
+            if (objects) {
+                if (kind == 1) k_trace<R, true><<<wblocks[k], threads, 0, ss[k]>>>(SW[k], qq);
+                else if (kind == 2) k_shade<R, false, true><<<wblocks[k], threads, 0, ss[k]>>>(SW[k], qq);
+                else k_shadow<R, true><<<wblocks[k], threads, 0, ss[k]>>>(SW[k]);
+            } else {
+                if (kind == 1) k_trace<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k], qq);
+                else if (kind == 2) k_shade<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k], qq);
+                else k_shadow<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k]);
+            }
+        };
         auto launch_iterations = [&](uint32_t k, uint32_t batch) -> cudaError_t {
             for (uint32_t b = 0; b < batch; ++b) {
                 const uint32_t qq = (q[k] + b) & 1u;
                 if (b == 0 || nee) k_generate<R><<<lblocks[k], threads, 0, ss[k]>>>(SW[k], qq);
                 else k_iteration_reset<R><<<1, 32, 0, ss[k]>>>(SW[k], qq);
-                k_trace<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k], qq);
-                k_shade<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k], qq);
-                if (nee) k_shadow<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k]);
+                launch_kind(1, k, qq);
+                launch_kind(2, k, qq);
+                if (nee) launch_kind(3, k, qq);
             }
             return cudaGetLastError();
         };
@@ -1165,9 +1178,7 @@ gt_status run_sub_wavefront(gt_context* ctx, Params<R>& P, std::vector<Params<R>
                         const bool gen = iters + b == 0 || nee;
                         if (kind == 0 && gen) k_generate<R><<<lblocks[k], threads, 0, ss[k]>>>(SW[k], q[k]);
                         else if (kind == 0) k_iteration_reset<R><<<1, 32, 0, ss[k]>>>(SW[k], q[k]);
-                        else if (kind == 1) k_trace<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k], q[k]);
-                        else if (kind == 2) k_shade<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k], q[k]);
-                        else k_shadow<R><<<wblocks[k], threads, 0, ss[k]>>>(SW[k]);
+                        else launch_kind(kind, k, q[k]);
                         GT_CUDA(cudaGetLastError());
                         if (profile) {
                             GT_CUDA(cudaEventRecord(z, ss[k]));
@@ -1293,16 +1304,16 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     if (world && BATCH) return fail(GT_ERR_UNSUPPORTED, "a scene with objects or media does not render as a wavefront batch");
     // Throughput mode: every (pixel, sample) pair of a round is a work item.
     const bool subs = opts.rng == GT_RNG_SUBSTREAMS;
-    if (subs && (world || accum))
-        return fail(GT_ERR_UNSUPPORTED, "substreams render neither worlds with objects or media nor accumulations");
-    // A single frame of a scene with more than kSubWaveMinPrims primitives runs its rounds
-    // through the wavefront kernels (k_generate starts each slot's one sample); a batch, or
-    // a small scene, through k_substream.  Measured (Msamples/s, wavefront / k_substream):
+    if (subs && (media || accum))
+        return fail(GT_ERR_UNSUPPORTED, "substreams render neither worlds with media nor accumulations");
+    // A single frame of a scene with objects or with more than kSubWaveMinPrims primitives
+    // runs its rounds through the wavefront kernels (k_generate starts each slot's one
+    // sample); a batch, or a small scene, through k_substream.  Measured (Msamples/s, wavefront / k_substream):
     // final scene (485 spheres) 933 / 669, mesh-heavy 332 / 185, Cornell box (13) 1,376 /
     // 1,804: with a tiny tree the one-kernel path loop is cheaper than the wavefront's
     // path-state traffic.
     constexpr uint32_t kSubWaveMinPrims = 64;
-    const bool sub_wave = subs && !BATCH && P.sc.num_prims > kSubWaveMinPrims;
+    const bool sub_wave = subs && !BATCH && (P.sc.num_prims > kSubWaveMinPrims || obj_wave);
     // one round's items at most: the cap, or the frame's samples when it has fewer
     const uint64_t sub_items = std::max<uint64_t>(
         std::min<uint64_t>(sub_wave ? kSubWaveItems : kSubItems, uint64_t(n_pix) * std::max(limit_max, 1u)), n_pix);
@@ -1345,7 +1356,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             sub_next = bb.take<unsigned long long>(1);
             if (sub_wave) { // the wavefront's slots are a round's items, rows dealt to stripes
                 W = P;
-                layout_slots<R>(bb, W.ps, uint32_t(sub_items), nee);
+                layout_slots<R>(bb, W.ps, uint32_t(sub_items), nee, obj_wave);
                 W.ps.totals = P.ps.totals;
                 d_sub = bb.take<SubRound<R>>(1);
                 W.sub = d_sub;
@@ -1459,7 +1470,7 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         uint64_t rounds = 0;
         if (sub_wave)
             rc = run_sub_wavefront<R>(ctx, P, SW, d_sub, sub_list, sub_out, uint32_t(sub_items), n, limit_max, nee,
-                                      o_rgb, opts, ev, kms, klaunch, rounds);
+                                      obj_wave, o_rgb, opts, ev, kms, klaunch, rounds);
         else
             rc = run_substreams<R, BATCH>(ctx, P, sub_list, sub_out, sub_next, n, limit_max, any_adaptive, o_rgb,
                                           opts, ev, kms, klaunch, rounds);

@@ -400,8 +400,8 @@ typedef struct gt_render_opts {
      * output for state (s + 1) * 0x9E3779B97F4A7C15; the samples of a pixel are then
      * independent and run in parallel.  The estimator is the reference's (adaptive
      * sampling stops at the same sample for the same sample values), the streams are not.
-     * The schedule is ignored; accumulation, worlds with objects or media, and f64 batches
-     * return GT_ERR_UNSUPPORTED. */
+     * The schedule is ignored; accumulation, worlds with media, batches of worlds with
+     * objects, and f64 batches return GT_ERR_UNSUPPORTED. */
     uint32_t rng;
 } gt_render_opts;
 

@@ -16,7 +16,7 @@ import pytest
 import oracle
 from gartus_gb300 import abi, scenes
 from gartus_gb300._lib import GartusError
-from gartus_gb300.raytracing import Accumulator, PathTracer
+from gartus_gb300.raytracing import Accumulator, PathTracer, RayCamera
 from tests.divergence import assert_explained, assert_modes_agree
 from tests.helpers import rel_err
 
@@ -42,6 +42,8 @@ def _cases():
     cornell, lights = scenes.cornell_scene()
     batch, blights = scenes.batch_scene()
     mesh, env = scenes.mesh_heavy_scene(size=40, tori=6, rings=8, tube=12, env_width=256, env_height=128)
+    from tests.test_gpu_parity import _mesh_world
+    objects, olights = _mesh_world()
     return {
         # random sampling with defocus; 512 x 288 x 128 spp (18.9 M samples) spans several
         # rounds of (pixel, sample) items
@@ -53,10 +55,15 @@ def _cases():
         "adaptive": (batch, scenes.batch_cameras(frames=3, width=40, spp_cycle=(8,), max_samples=64,
                                                  threshold=0.05)[1], blights, None),
         "environment": (mesh, scenes.mesh_heavy_camera(48, 27, 3, 8), None, env),
+        # meshes and instances (a world with objects: the wavefront's OBJ kernels), NEE
+        "objects": (objects, RayCamera(48, 1.5).with_samples_per_pixel(6).with_max_depth(8)
+                    .with_look_at((0.0, 1.0, 2.0), (0.0, 0.0, -3.0)).with_background((0.1, 0.1, 0.12))
+                    .with_direct_lighting_mode(abi.GT_DIRECT_NEXT_EVENT_ESTIMATION), olights, None),
     }
 
 
-@pytest.mark.parametrize("case", ["final_rounds", "cornell_mixture", "cornell_nee", "adaptive", "environment"])
+@pytest.mark.parametrize("case", ["final_rounds", "cornell_mixture", "cornell_nee", "adaptive", "environment",
+                                  "objects"])
 def test_f64_substreams_match_oracle(gpu_context, case):
     scene, cam, lights, env = _cases()[case]
     pt = PathTracer(cam, precision="f64", context=gpu_context, rng="substreams")
@@ -71,7 +78,8 @@ def test_f64_substreams_match_oracle(gpu_context, case):
     assert not np.array_equal(ref, ref_pixel)
 
 
-@pytest.mark.parametrize("case", ["final_rounds", "cornell_mixture", "cornell_nee", "adaptive", "environment"])
+@pytest.mark.parametrize("case", ["final_rounds", "cornell_mixture", "cornell_nee", "adaptive", "environment",
+                                  "objects"])
 def test_f32_substreams_explained(gpu_context, case):
     scene, cam, lights, env = _cases()[case]
     pt = PathTracer(cam, context=gpu_context, rng="substreams")
@@ -194,7 +202,12 @@ def test_substream_unsupported_uses(gpu_context):
     with pytest.raises(GartusError, match="f32"):
         PathTracer(cam, precision="f64", context=gpu_context, rng="substreams").render_batch_hdr_images(
             scene, [cam, cam], lights=lights)
-    # worlds with media
+    # worlds with media, and batches of worlds with objects
+    from tests.test_gpu_parity import _mesh_world
+    objects, olights = _mesh_world()
+    with pytest.raises(GartusError, match="objects or media"):
+        PathTracer(cam, context=gpu_context, rng="substreams").render_batch_hdr_images(objects, [cam, cam],
+                                                                                       lights=olights)
     smoke, _ = scenes.cornell_smoke_scene()
     with pytest.raises(GartusError, match="substreams"):
         PathTracer(cam, context=gpu_context, rng="substreams").render_hdr_image(smoke)
