@@ -231,6 +231,8 @@ inline void xf_point_host(const double* m, const double* p, double* out) {
 // Meshes (their primitives in their own tree's leaf order, attributes alongside) and world
 // objects (in the leaf order of a tree over their world boxes: the mesh's box, through
 // the instance transform's eight corners as transform_bounds does, instance.rs:319-335).
+// In f32 a mesh's tree is collapsed to the eight-wide form as the RayScene's is (its
+// primitives then in the wide tree's leaf order), unless the scene asks for binary trees.
 template <class R> gt_status upload_meshes(gt_scene* s, GpuScene<R>& g, cudaStream_t st) {
     SceneDev<R>& v = g.view;
     v.num_objects = 0;
@@ -250,6 +252,7 @@ template <class R> gt_status upload_meshes(gt_scene* s, GpuScene<R>& g, cudaStre
     std::vector<std::vector<Node<R>>> keep_nodes(md.size());
     std::vector<std::vector<R>> keep_uv(md.size()), keep_vn(md.size());
     std::vector<std::vector<uint8_t>> keep_attr(md.size());
+    std::vector<WideBvh> keep_wide(md.size());
     gt_status rc;
     for (size_t k = 0; k < md.size(); ++k) {
         const MeshHost& mh = s->meshes[k];
@@ -264,8 +267,15 @@ template <class R> gt_status upload_meshes(gt_scene* s, GpuScene<R>& g, cudaStre
         attr.resize(mn);
         if (!mh.uv.empty()) uv.resize(mn * 6);
         if (!mh.vn.empty()) vn.resize(mn * 9);
+        WideBvh& wide = keep_wide[k];
+        const bool use_wide = sizeof(R) == 4 && s->f32_tree == GT_F32_TREE_WIDE && build_wide_bvh(mh.bvh, wide);
+        std::vector<uint32_t> slot_of;
+        if (use_wide) {
+            slot_of.resize(mn);
+            for (size_t j = 0; j < mn; ++j) slot_of[wide.order[j]] = uint32_t(j);
+        }
         for (size_t j = 0; j < mn; ++j) {
-            const uint32_t pi = mh.bvh.order[j];
+            const uint32_t pi = mh.bvh.order[use_wide ? wide.order[j] : j];
             const gt_primitive& p = mh.prims[pi];
             const uint32_t kind = pack_prim<R>(p.geometry, rec[j].v);
             if (kind == kBadKind) return fail(GT_ERR_INVALID_ARG, "unknown geometry kind");
@@ -276,14 +286,16 @@ template <class R> gt_status upload_meshes(gt_scene* s, GpuScene<R>& g, cudaStre
         }
         SceneDev<R> mv;
         std::memset(&mv, 0, sizeof(mv));
-        flatten_tree<R>(mh.bvh, keep_nodes[k], mv.root_box, mv.root_link, mv.root_count);
-        void *dp, *dm, *dn, *du, *dv, *da;
+        flatten_tree<R>(mh.bvh, keep_nodes[k], mv.root_box, mv.root_link, mv.root_count, use_wide ? &slot_of : nullptr);
+        void *dp, *dm, *dn, *du, *dv, *da, *dw = nullptr;
         if ((rc = dput(rec.data(), mn * sizeof(PrimRec<R>), &dp)) != GT_OK) return rc;
         if ((rc = dput(meta.data(), mn * sizeof(uint2), &dm)) != GT_OK) return rc;
         if ((rc = dput(keep_nodes[k].data(), keep_nodes[k].size() * sizeof(Node<R>), &dn)) != GT_OK) return rc;
         if ((rc = dput(uv.data(), uv.size() * sizeof(R), &du)) != GT_OK) return rc;
         if ((rc = dput(vn.data(), vn.size() * sizeof(R), &dv)) != GT_OK) return rc;
         if ((rc = dput(attr.data(), attr.size(), &da)) != GT_OK) return rc;
+        if (use_wide && (rc = dput(wide.nodes.data(), wide.nodes.size() * sizeof(WideNode), &dw)) != GT_OK) return rc;
+        mv.wnodes = static_cast<const WideNode*>(dw);
         mv.prims = static_cast<const PrimRec<R>*>(dp);
         mv.meta = static_cast<const uint2*>(dm);
         mv.nodes = static_cast<const Node<R>*>(dn);

@@ -571,10 +571,11 @@ GT_DEV int traverse_wide(const SceneDev<float>& sc, V3<float> o, V3<float> d, fl
 // except for the statistics, which are defined by this walk.  CHECK (f32 primary-hit
 // check): candidates slightly beyond the closest hit are tested too and *near reports
 // near ties and near-boundary candidates in ck; the result is the rendering walk's.
-template <class R, bool STATS, bool ANY, bool CHECK = false>
+// BINARY: this walk even where the scene has a wide tree.
+template <class R, bool STATS, bool ANY, bool CHECK = false, bool BINARY = false>
 GT_DEV int traverse(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, R tmax, R& t_out, TraceStats* st,
                     uint32_t* err, bool any_hit = ANY, CheckState<R>* ck = nullptr) {
-    if constexpr (sizeof(R) == 4 && !STATS) {
+    if constexpr (sizeof(R) == 4 && !STATS && !BINARY) {
         if (sc.wnodes) return traverse_wide<CHECK>(sc, o, d, time, tmin, tmax, t_out, err, any_hit, ck);
     }
     RayT<R> rt = make_rayt(o, d);
@@ -823,8 +824,10 @@ template <class R> GT_DEV V3<R> xf_normal(const R* inv, V3<R> v) {
 // The closest object hit in (tmin, t): the objects' tree, then each object's mesh tree in
 // object space (MatrixInstance::hit_with_rng transforms the ray by the inverse; the ray
 // parameter is unchanged, instance.rs:266-289).  On a closer hit sets t, obj (leaf-order
-// object index) and leaf (primitive in the mesh's leaf order).
-template <class R>
+// object index) and leaf (primitive in the mesh's leaf order).  BINARY: the meshes' binary
+// trees even where they have wide ones (the persistent world variant, whose registers are
+// already spent: its frames ran 23% slower with the wide walk inside).
+template <class R, bool BINARY = false>
 GT_DEV bool objects_hit(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, R& t, int& obj, int& leaf,
                         uint32_t* err) {
     if (sc.num_objects == 0) return false;
@@ -849,7 +852,8 @@ GT_DEV bool objects_hit(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin,
                 const V3<R> oo = ob.transformed ? xf_point(ob.inv, o) : o;
                 const V3<R> od = ob.transformed ? xf_vector(ob.inv, d) : d;
                 R tt = t;
-                const int j = traverse<R, false, false>(sc.meshes[ob.mesh].view, oo, od, time, tmin, t, tt, nullptr, err);
+                const int j =
+                    traverse<R, false, false, false, BINARY>(sc.meshes[ob.mesh].view, oo, od, time, tmin, t, tt, nullptr, err);
                 if (j >= 0 && tt < t) {
                     t = tt;
                     obj = k;
@@ -979,7 +983,7 @@ GT_DEV bool world_hit(const SceneDev<R>& sc, V3<R> o, V3<R> d, R time, R tmin, R
     int prim = traverse<R, false, false>(sc, o, d, time, tmin, inf, t, nullptr, err);
     if (prim < 0) t = inf;
     int obj = -1, leaf = -1;
-    objects_hit(sc, o, d, time, tmin, t, obj, leaf, err);
+    objects_hit<R, true>(sc, o, d, time, tmin, t, obj, leaf, err);
     const int med = media_hit(sc, o, d, tmin, t, -1, g);
     if (med <= -2) h = make_medium_hit(sc, med, o, d, t);
     else if (obj >= 0) h = make_mesh_hit(sc, obj, leaf, o, d, time, t);

@@ -1044,6 +1044,22 @@ def test_object_world_schedules_agree(gpu_context, mode):
     np.testing.assert_array_equal(two.accepted, img0.accepted)
 
 
+def test_object_meshes_wide_and_binary_trees(gpu_context):
+    # In f32 each object's mesh is walked through its eight-wide tree (the RayScene's walk,
+    # traverse_wide); with binary f32 trees requested it keeps the reference tree.  The two
+    # f32 images agree within the f32 tolerance, and the wide one is explained against the
+    # oracle by test_meshes_and_instances.
+    wide, lights = _mesh_world()
+    binary, _ = _mesh_world()
+    binary.use_binary_f32_tree(True)
+    cam = (RayCamera(64, 1.5).with_samples_per_pixel(4).with_max_depth(8)
+           .with_look_at((0.0, 1.0, 2.0), (0.0, 0.0, -3.0)).with_background((0.1, 0.1, 0.12))
+           .with_direct_lighting_mode(abi.GT_DIRECT_NEXT_EVENT_ESTIMATION))
+    a = PathTracer(cam, context=gpu_context).render_with_lights_hdr_image(wide, lights)
+    b = PathTracer(cam, context=gpu_context).render_with_lights_hdr_image(binary, lights)
+    assert_modes_agree("object meshes: wide vs binary f32 trees", wide, cam, a.pixels, b.pixels, lights)
+
+
 def test_meshes_aovs_batch_and_primary(gpu_context):
     # The AOVs read the shading normal (camera.rs:3112-3114); a batch of an object world runs
     # the persistent batch; gt_trace_rays sees the RayScene only, as RayScene::hit does.
