@@ -13,15 +13,16 @@ gt_status render_accumulate_f32(gt_scene* s, const gt_lights* l, gt_environment*
     return render_impl<float>(s, l, e, cam, opts, frame, acc, samples);
 }
 
-// Frames of one width run through the striped wavefront as one image of their rows; the
-// persistent schedule, or frames of different widths, use the one-launch persistent batch.
+// Frames of one width run through the striped wavefront as one image of their rows (worlds
+// with objects too); the persistent schedule, frames of different widths, or a world with
+// media use the one-launch persistent batch.
 gt_status render_batch_f32(gt_scene* s, const gt_lights* l, gt_environment* e, const CamHost* cams, uint32_t count,
                            const gt_render_opts& opts, gt_frame* const* frames) {
     bool same_width = true;
     for (uint32_t i = 1; i < count; ++i) same_width = same_width && cams[i].width == cams[0].width;
     // substreams: the frames' pixels are work items of one list, whatever their widths
     if (opts.rng == GT_RNG_SUBSTREAMS ||
-        (opts.schedule != GT_SCHEDULE_PERSISTENT && same_width && s->media.empty() && s->objects.empty()))
+        (opts.schedule != GT_SCHEDULE_PERSISTENT && same_width && s->media.empty()))
         return render_impl<float, true>(s, l, e, cams[0], opts, nullptr, nullptr, 0, cams, count, frames);
     return render_batch_impl<float>(s, l, e, cams, count, opts, frames);
 }

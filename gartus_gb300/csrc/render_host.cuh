@@ -1308,14 +1308,15 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
     // shadow queries in the reference's order of draws (a medium's hit draws from the
     // pixel's stream); accumulation resumes wavefront state in that variant's RESUME mode.
     // A world with objects and no media draws nothing in its hits, so it renders on the
-    // wavefront (OBJ kernels: the rays also test the objects), and its tail in the world
-    // variant.
+    // wavefront (OBJ kernels: the rays also test the objects), single frames and batches,
+    // and its tail in the world variant.
     const bool world = P.sc.num_media != 0 || P.sc.num_objects != 0;
     const bool media = P.sc.num_media != 0;
-    const bool obj_wave = world && !media && !BATCH;
-    if (world && BATCH) return fail(GT_ERR_UNSUPPORTED, "a scene with objects or media does not render as a wavefront batch");
+    const bool obj_wave = world && !media;
+    if (BATCH && media) return fail(GT_ERR_UNSUPPORTED, "a scene with media does not render as a wavefront batch");
     // Throughput mode: every (pixel, sample) pair of a round is a work item.
     const bool subs = opts.rng == GT_RNG_SUBSTREAMS;
+    if (BATCH && subs && world) return fail(GT_ERR_UNSUPPORTED, "a substream batch does not render a scene with objects");
     if (subs && (media || accum))
         return fail(GT_ERR_UNSUPPORTED, "substreams render neither worlds with media nor accumulations");
     // A single frame of a scene with objects or with more than kSubWaveMinPrims primitives
@@ -1616,11 +1617,9 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
             const uint32_t shadow_blocks = std::min<uint32_t>(wblocks, uint32_t(sms) * kShadowBlocksPerSm);
             if (q == 0) k_generate<R, BATCH><<<lblocks, threads, 0, s>>>(SP[k], cur);
             else if (obj_wave) {
-                if constexpr (!BATCH) {
-                    if (q == 1) k_trace<R, true><<<wblocks, threads, 0, s>>>(SP[k], cur);
-                    else if (q == 2) k_shade<R, false, true><<<shade_blocks, threads, 0, s>>>(SP[k], cur);
-                    else k_shadow<R, true><<<shadow_blocks, threads, 0, s>>>(SP[k]);
-                }
+                if (q == 1) k_trace<R, true><<<wblocks, threads, 0, s>>>(SP[k], cur);
+                else if (q == 2) k_shade<R, BATCH, true><<<shade_blocks, threads, 0, s>>>(SP[k], cur);
+                else k_shadow<R, true><<<shadow_blocks, threads, 0, s>>>(SP[k]);
             } else if (q == 1) k_trace<R><<<wblocks, threads, 0, s>>>(SP[k], cur);
             else if (q == 2) k_shade<R, BATCH><<<shade_blocks, threads, 0, s>>>(SP[k], cur);
             else k_shadow<R><<<shadow_blocks, threads, 0, s>>>(SP[k]);
@@ -1729,20 +1728,18 @@ gt_status render_impl(gt_scene* s, const gt_lights* l, gt_environment* e, const 
         GT_CUDA(cudaMemsetAsync(Q.ps.counters + C_TAIL_DONE, 0, 3 * sizeof(uint32_t), s));
         GT_CUDA(cudaMemsetAsync(d_next + k, 0, sizeof(uint32_t), s));
         k_collect<R><<<lblocks, threads, 0, s>>>(Q, list, count);
-        if constexpr (!BATCH) {
-            if (obj_wave) { // the world variant, one slot per lane to the end
-                k_persistent<R, true, false, true><<<tblocks, 128, 0, s>>>(Q, d_next + k, list, count, nullptr, nullptr,
-                                                                           nullptr, nullptr, nullptr);
-                GT_CUDA(cudaGetLastError());
-                klaunch[GT_KERNEL_OTHER] += 1;
-                klaunch[GT_KERNEL_PERSISTENT] += 1;
-                if (profile) {
-                    GT_CUDA(cudaEventRecord(z, s));
-                    ev.note(GT_KERNEL_PERSISTENT, a, z);
-                }
-                S[k].tail = true;
-                return GT_OK;
+        if (obj_wave) { // the world variant, one slot per lane to the end
+            k_persistent<R, true, BATCH, true><<<tblocks, 128, 0, s>>>(Q, d_next + k, list, count, nullptr, nullptr,
+                                                                       nullptr, nullptr, nullptr);
+            GT_CUDA(cudaGetLastError());
+            klaunch[GT_KERNEL_OTHER] += 1;
+            klaunch[GT_KERNEL_PERSISTENT] += 1;
+            if (profile) {
+                GT_CUDA(cudaEventRecord(z, s));
+                ev.note(GT_KERNEL_PERSISTENT, a, z);
             }
+            S[k].tail = true;
+            return GT_OK;
         }
         HandOff ho;
         ho.done = Q.ps.counters + C_TAIL_DONE;

@@ -1062,7 +1062,9 @@ def test_object_meshes_wide_and_binary_trees(gpu_context):
 
 def test_meshes_aovs_batch_and_primary(gpu_context):
     # The AOVs read the shading normal (camera.rs:3112-3114); a batch of an object world runs
-    # the persistent batch; gt_trace_rays sees the RayScene only, as RayScene::hit does.
+    # on the wavefront (f32 frames of one width; its OBJ kernels in BATCH mode) or the
+    # persistent batch (f64), and each frame equals its single render; gt_trace_rays sees
+    # the RayScene only, as RayScene::hit does.
     scene, lights = _mesh_world()
     cam = RayCamera(40, 1.5).with_samples_per_pixel(3).with_max_depth(6).with_look_at((0.0, 1.0, 2.0), (0.0, 0.0, -3.0))
     aovs = PathTracer(cam, precision="f64", context=gpu_context).render_denoising_aovs(scene)

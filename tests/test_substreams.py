@@ -205,7 +205,7 @@ def test_substream_unsupported_uses(gpu_context):
     # worlds with media, and batches of worlds with objects
     from tests.test_gpu_parity import _mesh_world
     objects, olights = _mesh_world()
-    with pytest.raises(GartusError, match="objects or media"):
+    with pytest.raises(GartusError, match="substream batch"):
         PathTracer(cam, context=gpu_context, rng="substreams").render_batch_hdr_images(objects, [cam, cam],
                                                                                        lights=olights)
     smoke, _ = scenes.cornell_smoke_scene()
