@@ -567,8 +567,9 @@ typedef struct gt_frame_job {
  * a camera sweep.  In f32 with schedule AUTO or WAVEFRONT, frames of one width run
  * through the striped wavefront as one image of their stacked rows (every slot rendered
  * with its frame's camera, graphs replayed, slow slots migrated, the tail finished in the
- * persistent kernel); in f64, with schedule PERSISTENT, or with frames of different
- * widths, all pixels go through one persistent launch.  Every frame's image and accepted
+ * persistent kernel; no migration in a world with objects); in f64, with schedule
+ * PERSISTENT, with frames of different widths, or for a scene with media, all pixels go
+ * through one persistent launch.  Every frame's image and accepted
  * counts equal what gt_render gives for that frame alone (bit for bit in f64).  opts:
  * precision, schedule, tail_slots, stripes, stats (summed over the batch), profile,
  * progress and cancellation; `progress_rgb` is not written; `aovs` is GT_ERR_UNSUPPORTED. */
