@@ -391,7 +391,7 @@ typedef struct gt_render_opts {
     /* GT_SCHEDULE_AUTO: once per stripe, early in the frame, the pixels progressing at less
      * than half the stripe's mean sample rate (long sample chains: glass, adaptive pixels at
      * their cap) move to a persistent kernel that runs them concurrently with the wavefront.
-     * gt_migrate; f64 images do not depend on it. */
+     * gt_migrate; f64 images do not depend on it.  Never in a world with objects. */
     uint32_t migrate;
     /* Per-sample random streams, gt_rng.  GT_RNG_PIXEL (the reference, camera.rs:2669):
      * each pixel's samples continue one stream.  GT_RNG_SUBSTREAMS (throughput mode, no
