@@ -61,6 +61,12 @@ def cases():
     for i in range(37):
         stack.add_sphere((0.0, 0.0, 0.0), 1.0 + (i % 5) * 0.1, m)
     out["coincident_37"] = stack
+    # a mesh's own tree (TriangleMesh, leaf size 4): the f32 wavefront walks object meshes
+    # through the same wide form, their primitives in its leaf order
+    torus = RayScene()
+    m = torus.add_material(RayMaterial.lambertian((0.5, 0.5, 0.5)))
+    torus.add_triangles_array(m, scenes.torus_triangles((0.0, 0.0, 0.0), 0.35, 1.0, 32, 64))
+    out["torus_mesh_4096"] = torus
     for leaf in (1, 2, 3):
         s = scenes.final_scene_ray_scene()
         s.build_bvh_with_options(leaf)
