@@ -34,9 +34,14 @@ Aabb geometry_aabb(const gt_geometry& g);
 // 12 centroid buckets along the largest centroid axis, first minimum of
 // SA_L*n_L + SA_R*n_R, in-place swap partition, and a stable centroid-then-index
 // midpoint split whenever the buckets cannot separate the primitives.
-void build_reference_bvh(const gt_primitive* prims, uint32_t count, uint32_t leaf_size, BuiltBvh& out);
+// `threads` host threads build the subtrees of ranges of at most `cut` primitives once
+// the top of the tree is built (0: the machine's threads, at most 16, and a cut chosen
+// from the count; serial below 65,536 primitives); the tree does not depend on either.
+void build_reference_bvh(const gt_primitive* prims, uint32_t count, uint32_t leaf_size, BuiltBvh& out,
+                         uint32_t threads = 0, uint32_t cut = 0);
 
 // The same build over given boxes (a mesh's triangles, or world objects).
-void build_bvh_from_boxes(const Aabb* boxes, uint32_t count, uint32_t leaf_size, BuiltBvh& out);
+void build_bvh_from_boxes(const Aabb* boxes, uint32_t count, uint32_t leaf_size, BuiltBvh& out, uint32_t threads = 0,
+                          uint32_t cut = 0);
 
 } // namespace gt

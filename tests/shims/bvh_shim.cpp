@@ -4,10 +4,12 @@
 
 #include "../../gartus_gb300/csrc/bvh_build.h"
 
+// threads, cut: the parallel build's settings (0, 0: the library's defaults).
 extern "C" int shim_build(const gt_primitive* prims, uint32_t count, uint32_t leaf, uint32_t* node_count,
-                          double* bounds, uint32_t* info, uint32_t* order, uint32_t capacity, uint32_t* depth) {
+                          double* bounds, uint32_t* info, uint32_t* order, uint32_t capacity, uint32_t* depth,
+                          uint32_t threads, uint32_t cut) {
     gt::BuiltBvh b;
-    gt::build_reference_bvh(prims, count, leaf, b);
+    gt::build_reference_bvh(prims, count, leaf, b, threads, cut);
     *node_count = uint32_t(b.nodes.size());
     *depth = b.max_depth;
     if (b.nodes.size() > capacity) return 1;

@@ -24,11 +24,11 @@ def shim(tmp_path_factory):
     lib = C.CDLL(str(out))
     lib.shim_build.restype = C.c_int
     lib.shim_build.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                               C.c_uint32, C.c_void_p]
+                               C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32]
     return lib
 
 
-def product_bvh(shim, scene):
+def product_bvh(shim, scene, threads=0, cut=0):
     prims = np.ascontiguousarray(scene.primitives_array())
     cap = max(2 * len(prims), 1)
     n, depth = C.c_uint32(), C.c_uint32()
@@ -37,7 +37,7 @@ def product_bvh(shim, scene):
     order = np.zeros(len(prims), dtype=np.uint32)
     assert shim.shim_build(prims.ctypes.data_as(C.c_void_p), len(prims), scene.leaf_size, C.byref(n),
                            bounds.ctypes.data_as(C.c_void_p), info.ctypes.data_as(C.c_void_p),
-                           order.ctypes.data_as(C.c_void_p), cap, C.byref(depth)) == 0
+                           order.ctypes.data_as(C.c_void_p), cap, C.byref(depth), threads, cut) == 0
     return bounds[: n.value], info[: n.value], order, depth.value
 
 
@@ -79,10 +79,13 @@ def cases():
     return out
 
 
+# (threads, cut): the library's defaults (serial at these sizes), and the parallel build
+# with subtrees of at most 16 primitives on four threads.
+@pytest.mark.parametrize("threads,cut", [(0, 0), (4, 16)])
 @pytest.mark.parametrize("name", list(cases().keys()))
-def test_product_builder_matches_oracle(shim, name):
+def test_product_builder_matches_oracle(shim, name, threads, cut):
     scene = cases()[name]
-    bounds, info, order, depth = product_bvh(shim, scene)
+    bounds, info, order, depth = product_bvh(shim, scene, threads, cut)
     o = oracle.OracleScene.from_ray_scene(scene)
     ob, oi, oo = o.bvh()
     assert len(bounds) == len(ob)
@@ -90,6 +93,22 @@ def test_product_builder_matches_oracle(shim, name):
     np.testing.assert_array_equal(bounds, ob)
     np.testing.assert_array_equal(order, oo)
     assert 1 <= depth <= 61
+
+
+def test_parallel_build_of_a_large_scene(shim):
+    # 80,000 triangles: above the size where the library builds in parallel by default;
+    # the parallel tree equals the oracle's and the serial build's node for node.
+    scene = RayScene()
+    m = scene.add_material(RayMaterial.lambertian((0.5, 0.5, 0.5)))
+    scene.add_triangles_array(m, grid_triangles(200, 11))
+    par = product_bvh(shim, scene)
+    ser = product_bvh(shim, scene, threads=1)
+    for a, b in zip(par, ser):
+        np.testing.assert_array_equal(a, b)
+    ob, oi, oo = oracle.OracleScene.from_ray_scene(scene).bvh()
+    np.testing.assert_array_equal(par[1], oi)
+    np.testing.assert_array_equal(par[0], ob)
+    np.testing.assert_array_equal(par[2], oo)
 
 
 def test_empty_scene_has_no_nodes(shim):
