@@ -156,8 +156,10 @@ typedef enum gt_bvh_builder {
  * traversal statistics always walk the reference's binary tree).  GT_F32_TREE_WIDE: an
  * eight-wide tree with byte-quantised child boxes, collapsed from the reference SAH tree
  * (same leaves, same hits; the binary walk is kept where a scene has no wide form: a
- * single leaf, leaves of more than four primitives, or a GT_BVH_GPU_LBVH scene).
- * GT_F32_TREE_BINARY: the reference's binary tree. */
+ * single leaf, leaves of more than four primitives, or a GT_BVH_GPU_LBVH scene).  The
+ * meshes of world objects get their own wide trees the same way, walked by the wavefront
+ * schedules (the persistent kernel walks their binary trees).
+ * GT_F32_TREE_BINARY: the reference's binary tree, for the RayScene and the meshes. */
 typedef enum gt_f32_tree {
     GT_F32_TREE_WIDE = 0,
     GT_F32_TREE_BINARY = 1
